@@ -1,0 +1,577 @@
+// C ABI: context life cycle, mesh/BC upload and the step entry points (include/afvm.h).
+//
+// afvm_ctx_create mirrors the reference's Function.initialize -> external_init
+// (adFVM/solver.py:61-71, adFVM/cpp/external.cpp:21-42): the mesh moves to the device once;
+// every later call passes only the state. The derived per-cell tables are computed here in
+// double with the reference's expressions (op.py:45-63 gradient weights, op.py:12-29 div
+// weights, density.py:390-402 accumulation order).
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+#include "ctx.cuh"
+
+namespace afvm {
+
+int fail(Ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+int cuda_fail(Ctx* c, cudaError_t e, const char* what) {
+    return fail(c, AFVM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+const char* const kKernelNames[KID_COUNT] = {"k_prim", "k_grad", "k_flux", "k_update", "k_objective",
+                                             "k_finish", "k_adj_flux", "k_adj_gather", "k_adj_grad",
+                                             "k_adj_prim", "k_adj_misc", "k_sensitivity"};
+
+static cudaEvent_t take_event(Ctx* c) {
+    if (!c->eventPool.empty()) {
+        cudaEvent_t ev = c->eventPool.back();
+        c->eventPool.pop_back();
+        return ev;
+    }
+    cudaEvent_t ev = nullptr;
+    cudaEventCreate(&ev);
+    return ev;
+}
+
+ProfScope::ProfScope(Ctx* c_, int id, cudaStream_t s_) : c(c_), s(s_), on(c_->prof) {
+    if (!on) return;
+    e.id = id;
+    e.a = take_event(c);
+    e.b = take_event(c);
+    cudaEventRecord(e.a, s);
+}
+
+ProfScope::~ProfScope() {
+    if (!on) return;
+    cudaEventRecord(e.b, s);
+    c->profEntries.push_back(e);
+}
+
+namespace {
+
+// bounded allocation bookkeeping
+int dalloc(Ctx* c, void** p, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c, AFVM_ERR_OOM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed");
+    }
+    c->allocs.push_back(*p);
+    c->bytes += (int64_t)bytes;
+    return AFVM_OK;
+}
+
+template <typename T>
+int upload(Ctx* c, const T** dst, const std::vector<T>& v) {
+    void* p = nullptr;
+    int st = dalloc(c, &p, v.size() * sizeof(T));
+    if (st) return st;
+    cudaError_t e = cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(c, e, "mesh upload");
+    *dst = (const T*)p;
+    return AFVM_OK;
+}
+
+struct HostTables {
+    // faces
+    std::vector<int32_t> own, nbr;
+    std::vector<double> nrm, area, dlt, du, lw, qw;
+    std::vector<uint8_t> fkind;
+    std::vector<int32_t> gsrc, gkind;
+    std::vector<double> gval;
+    // cells
+    std::vector<int32_t> gnb, accf;
+    std::vector<double> gw, gsn, rvol, accw, vol;
+};
+
+template <typename R>
+std::vector<R> cast(const std::vector<double>& v) {
+    return std::vector<R>(v.begin(), v.end());
+}
+
+template <typename R>
+int upload_mesh(Ctx* c, const HostTables& h, MeshDev<R>& m) {
+    int st;
+    m.nIC = c->nIC; m.nIF = c->nIF; m.nF = c->nF; m.nC = c->nC; m.nG = c->nG;
+    if ((st = upload(c, &m.own, h.own))) return st;
+    if ((st = upload(c, &m.nbr, h.nbr))) return st;
+    if ((st = upload(c, &m.nrm, cast<R>(h.nrm)))) return st;
+    if ((st = upload(c, &m.area, cast<R>(h.area)))) return st;
+    if ((st = upload(c, &m.dlt, cast<R>(h.dlt)))) return st;
+    if ((st = upload(c, &m.du, cast<R>(h.du)))) return st;
+    if ((st = upload(c, &m.lw, cast<R>(h.lw)))) return st;
+    if ((st = upload(c, &m.qw, cast<R>(h.qw)))) return st;
+    if ((st = upload(c, &m.fkind, h.fkind))) return st;
+    if ((st = upload(c, &m.gsrc, h.gsrc))) return st;
+    if ((st = upload(c, &m.gkind, h.gkind))) return st;
+    if ((st = upload(c, &m.gval, cast<R>(h.gval)))) return st;
+    if ((st = upload(c, &m.gnb, h.gnb))) return st;
+    if ((st = upload(c, &m.gw, cast<R>(h.gw)))) return st;
+    if ((st = upload(c, &m.gsn, cast<R>(h.gsn)))) return st;
+    if ((st = upload(c, &m.rvol, cast<R>(h.rvol)))) return st;
+    if ((st = upload(c, &m.accf, h.accf))) return st;
+    if ((st = upload(c, &m.accw, cast<R>(h.accw)))) return st;
+    if ((st = upload(c, &m.vol, cast<R>(h.vol)))) return st;
+    return AFVM_OK;
+}
+
+int bc_code(int kind, bool isU) {
+    switch (kind) {
+        case AFVM_BC_ZERO_GRADIENT: return GK_COPY;
+        case AFVM_BC_CYCLIC: return GK_COPY;
+        case AFVM_BC_SYMMETRY_PLANE: return isU ? GK_SYM : GK_COPY;
+        case AFVM_BC_FIXED_VALUE: return GK_FIXED;
+        case AFVM_BC_CBC_UPT: return GK_FIXED;
+        default: return -1;
+    }
+}
+
+int build_tables(Ctx* c, const afvm_mesh_tensors* M, const afvm_patch_bc* bcs, HostTables& h) {
+    const int nIC = M->nInternalCells, nIF = M->nInternalFaces, nF = M->nFaces, nC = M->nCells;
+    const int nG = nC - nIC;
+    if (nIC <= 0 || nIF < 0 || nF < nIF || nG != nF - nIF)
+        return fail(c, AFVM_ERR_BAD_ARG, "inconsistent mesh sizes");
+    if (M->nRemoteCells != 0) return fail(c, AFVM_ERR_UNSUPPORTED, "processor patches need a multi-partition run");
+    c->nIC = nIC; c->nIF = nIF; c->nF = nF; c->nC = nC; c->nG = nG;
+    c->nPatches = M->nPatches;
+    // faces
+    h.own.assign(M->owner, M->owner + nF);
+    h.nbr.assign(M->neighbour, M->neighbour + nF);
+    for (int f = 0; f < nF; f++) {
+        if (h.own[f] < 0 || h.own[f] >= nIC) return fail(c, AFVM_ERR_BAD_ARG, "owner out of range");
+        if (h.nbr[f] < 0 || h.nbr[f] >= nC) return fail(c, AFVM_ERR_BAD_ARG, "neighbour out of range");
+        if (f < nIF && h.nbr[f] >= nIC) return fail(c, AFVM_ERR_BAD_ARG, "internal face with a ghost neighbour");
+        if (f >= nIF && h.nbr[f] != nIC + (f - nIF)) return fail(c, AFVM_ERR_BAD_ARG, "ghost id of a boundary face");
+    }
+    h.nrm.resize(3 * (size_t)nF); h.du.resize(3 * (size_t)nF);
+    h.lw.resize(2 * (size_t)nF); h.qw.resize(6 * (size_t)nF);
+    h.area.assign(M->areas, M->areas + nF);
+    h.dlt.assign(M->deltas, M->deltas + nF);
+    for (int f = 0; f < nF; f++) {
+        for (int k = 0; k < 3; k++) {
+            h.nrm[(size_t)k * nF + f] = M->normals[3 * (size_t)f + k];
+            h.du[(size_t)k * nF + f] = M->deltasUnit[3 * (size_t)f + k];
+        }
+        for (int k = 0; k < 2; k++) h.lw[(size_t)k * nF + f] = M->linearWeights[2 * (size_t)f + k];
+        for (int k = 0; k < 6; k++) h.qw[(size_t)k * nF + f] = M->quadraticWeights[6 * (size_t)f + k];
+    }
+    // patches (sorted order) -> boundary-face kinds, ghost sources and BC codes
+    h.fkind.assign(nG, (uint8_t)FACE_BOUNDARY);
+    h.gsrc.assign(nG, -1);
+    h.gkind.assign(nG, 0);
+    h.gval.assign(5 * (size_t)nG, 0.0);
+    std::vector<int> rank(nF);
+    std::iota(rank.begin(), rank.end(), 0);
+    int pos = nIF;
+    c->objStart = 0; c->objN = 0;
+    for (int pi = 0; pi < M->nPatches; pi++) {
+        const afvm_patch& p = M->patches[pi];
+        const afvm_patch_bc& b = bcs[pi];
+        if (p.nFaces < 0 || p.startFace < nIF || p.startFace + p.nFaces > nF)
+            return fail(c, AFVM_ERR_BAD_ARG, "patch face range");
+        if (p.kind == AFVM_PATCH_PROCESSOR) return fail(c, AFVM_ERR_UNSUPPORTED, "processor patch");
+        bool cbc = b.U == AFVM_BC_CBC_UPT || b.T == AFVM_BC_CBC_UPT || b.p == AFVM_BC_CBC_UPT;
+        if (cbc && !(b.U == AFVM_BC_CBC_UPT && b.T == AFVM_BC_CBC_UPT && b.p == AFVM_BC_CBC_UPT))
+            return fail(c, AFVM_ERR_BAD_ARG, "CBC_UPT must be set on U, T and p of a patch");
+        bool cyclic = p.kind == AFVM_PATCH_CYCLIC;
+        if (cyclic) {
+            if (p.neighbourPatch < 0 || p.neighbourPatch >= M->nPatches ||
+                M->patches[p.neighbourPatch].nFaces != p.nFaces)
+                return fail(c, AFVM_ERR_BAD_ARG, "cyclic partner");
+            if (b.U != AFVM_BC_CYCLIC || b.T != AFVM_BC_CYCLIC || b.p != AFVM_BC_CYCLIC)
+                return fail(c, AFVM_ERR_BAD_ARG, "a cyclic patch needs cyclic BCs");
+        }
+        int cU = bc_code(b.U, true), cT = bc_code(b.T, false), cp = bc_code(b.p, false);
+        if (cU < 0 || cT < 0 || cp < 0) return fail(c, AFVM_ERR_BAD_ARG, "unknown BC kind");
+        for (int i = 0; i < p.nFaces; i++) {
+            int f = p.startFace + i, g = f - nIF;
+            h.fkind[g] = (uint8_t)(cyclic ? FACE_COUPLED : (cbc ? FACE_CHARACTERISTIC : FACE_BOUNDARY));
+            h.gsrc[g] = cyclic ? h.own[M->patches[p.neighbourPatch].startFace + i] : h.own[f];
+            h.gkind[g] = cU | (cT << 3) | (cp << 6);
+            if (cU == GK_FIXED) {
+                if (!b.U_value) return fail(c, AFVM_ERR_BAD_ARG, "missing U value");
+                for (int k = 0; k < 3; k++) h.gval[(size_t)k * nG + g] = b.U_value[3 * (size_t)i + k];
+            }
+            if (cT == GK_FIXED) {
+                if (!b.T_value) return fail(c, AFVM_ERR_BAD_ARG, "missing T value");
+                h.gval[3 * (size_t)nG + g] = b.T_value[i];
+            }
+            if (cp == GK_FIXED) {
+                if (!b.p_value) return fail(c, AFVM_ERR_BAD_ARG, "missing p value");
+                h.gval[4 * (size_t)nG + g] = b.p_value[i];
+            }
+            rank[f] = pos + i;
+        }
+        pos += p.nFaces;
+        c->patchStart.push_back(p.startFace);
+        c->patchN.push_back(p.nFaces);
+        c->bcKinds.push_back(b.U); c->bcKinds.push_back(b.T); c->bcKinds.push_back(b.p);
+        if (c->objective == AFVM_OBJ_DRAG && pi == c->objPatch) { c->objStart = p.startFace; c->objN = p.nFaces; }
+    }
+    if (pos != nF) return fail(c, AFVM_ERR_BAD_ARG, "patches do not cover the boundary faces");
+    for (int g = 0; g < nG; g++)
+        if (h.gsrc[g] < 0) return fail(c, AFVM_ERR_BAD_ARG, "boundary face outside every patch");
+    if (c->objective == AFVM_OBJ_DRAG && (c->objPatch < 0 || c->objPatch >= M->nPatches))
+        return fail(c, AFVM_ERR_BAD_ARG, "objective patch");
+
+    // cells: gradient slots in cellFaces order (op.py:45-63)
+    const size_t n = nIC;
+    h.gnb.resize(6 * n); h.gw.resize(6 * n); h.gsn.resize(18 * n);
+    h.rvol.resize(n); h.vol.assign(M->volumes, M->volumes + nIC);
+    h.accf.resize(6 * n); h.accw.resize(6 * n);
+    for (int ci = 0; ci < nIC; ci++) {
+        if (!(M->volumes[ci] > 0)) return fail(c, AFVM_ERR_BAD_ARG, "non-positive cell volume");
+        h.rvol[ci] = 1.0 / M->volumes[ci];
+        int fs[6];
+        for (int s = 0; s < 6; s++) {
+            int f = M->cellFaces[6 * (size_t)ci + s];
+            int O = M->cellOwner[6 * (size_t)ci + s];
+            int nb = M->cellNeighbours[6 * (size_t)ci + s];
+            if (f < 0 || f >= nF || nb < 0 || nb >= nC || (O != 0 && O != 1))
+                return fail(c, AFVM_ERR_BAD_ARG, "cell connectivity out of range");
+            if ((O == 1) != (h.own[f] == ci)) return fail(c, AFVM_ERR_BAD_ARG, "cellOwner disagrees with owner");
+            double Od = (double)O;
+            double w = M->weights[f];
+            double S = M->areas[f];
+            h.gnb[s * n + ci] = nb;
+            h.gw[s * n + ci] = (w + Od) - (2 * w) * Od;
+            for (int k = 0; k < 3; k++) {
+                double Nk = M->normals[3 * (size_t)f + k];
+                h.gsn[(3 * s + k) * n + ci] = S * (((2 * Nk) * Od) - Nk);
+            }
+            fs[s] = f;
+        }
+        // collate order: internal faces by face id, then patches in sorted order
+        std::sort(fs, fs + 6, [&](int a, int b2) { return rank[a] < rank[b2]; });
+        for (int s = 0; s < 6; s++) {
+            int f = fs[s];
+            bool ownerSide = h.own[f] == ci;
+            if (!ownerSide && f >= nIF) return fail(c, AFVM_ERR_BAD_ARG, "boundary face not owned by its cell");
+            h.accf[s * n + ci] = ownerSide ? f : ~f;
+            h.accw[s * n + ci] = ownerSide ? M->areas[f] / M->volumesL[f] : M->areas[f] / M->volumesR[f];
+        }
+    }
+    return AFVM_OK;
+}
+
+template <typename R>
+int alloc_work(Ctx* c) {
+    int st;
+    if ((st = dalloc(c, &c->rec, sizeof(R) * (size_t)c->nC * REC))) return st;
+    if ((st = dalloc(c, &c->fflux, sizeof(R) * (size_t)c->nF * FREC))) return st;
+    size_t n = c->nIC;
+    size_t dims[3] = {1, 3, 1};
+    for (int k = 0; k < 3; k++) {
+        if ((st = dalloc(c, &c->u1[k], sizeof(R) * n * dims[k]))) return st;
+        if ((st = dalloc(c, &c->u2[k], sizeof(R) * n * dims[k]))) return st;
+    }
+    if ((st = dalloc(c, &c->zeroS, sizeof(R) * n * 5))) return st;
+    cudaMemset(c->zeroS, 0, sizeof(R) * n * 5);
+    int np = (int)((std::max(c->nIC, c->nF) + BLOCK - 1) / BLOCK);
+    c->nPartials = np;
+    if ((st = dalloc(c, (void**)&c->partials, sizeof(double) * (size_t)np))) return st;
+    if ((st = dalloc(c, (void**)&c->scal, sizeof(double) * 8))) return st;
+    cudaMemset(c->scal, 0, sizeof(double) * 8);
+    if ((st = dalloc(c, (void**)&c->dtcBits, sizeof(unsigned long long)))) return st;
+    return AFVM_OK;
+}
+
+void release(Ctx* c) {
+    int prev = -1;
+    cudaGetDevice(&prev);
+    cudaSetDevice(c->device);
+    for (auto& e : c->profEntries) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
+    for (auto ev : c->eventPool) cudaEventDestroy(ev);
+    c->profEntries.clear();
+    c->eventPool.clear();
+    for (void* p : c->allocs) cudaFree(p);
+    c->allocs.clear();
+    if (prev >= 0) cudaSetDevice(prev);
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+int get_results(Ctx* c, double* dtc_out, double* obj_out, cudaStream_t s) {
+    if (!dtc_out && !obj_out) return AFVM_OK;
+    double tmp[2];
+    cudaError_t e = cudaMemcpyAsync(tmp, c->scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(c, e, "step results");
+    if (dtc_out) *dtc_out = tmp[0];
+    if (obj_out) *obj_out = tmp[1];
+    if (!std::isfinite(tmp[0]) || !std::isfinite(tmp[1]))
+        return fail(c, AFVM_ERR_NONFINITE, "non-finite CFL sum or objective");
+    return AFVM_OK;
+}
+
+}  // namespace
+}  // namespace afvm
+
+using namespace afvm;
+
+extern "C" {
+
+int afvm_ctx_create(const afvm_mesh_tensors* mesh, const afvm_patch_bc* bcs, const afvm_physics* phys,
+                    int32_t precision, int32_t device, afvm_ctx** out) {
+    if (!out) return AFVM_ERR_BAD_ARG;
+    *out = nullptr;
+    if (!mesh || !phys || (mesh->nPatches > 0 && (!bcs || !mesh->patches))) return AFVM_ERR_BAD_ARG;
+    if (precision != AFVM_FP64 && precision != AFVM_FP32) return AFVM_ERR_BAD_ARG;
+    if (phys->riemann != AFVM_RIEMANN_ROE && phys->riemann != AFVM_RIEMANN_LF) return AFVM_ERR_BAD_ARG;
+    if (phys->boundary_riemann != AFVM_RIEMANN_ROE && phys->boundary_riemann != AFVM_RIEMANN_LF)
+        return AFVM_ERR_BAD_ARG;
+    if (phys->mu_model != AFVM_MU_CONSTANT && phys->mu_model != AFVM_MU_SUTHERLAND) return AFVM_ERR_BAD_ARG;
+    if (phys->objective < AFVM_OBJ_NONE || phys->objective > AFVM_OBJ_SUM_T) return AFVM_ERR_BAD_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return AFVM_ERR_CUDA;
+    }
+    Ctx* c = new (std::nothrow) Ctx();
+    if (!c) return AFVM_ERR_OOM;
+    c->precision = precision;
+    c->device = device;
+    Phys& P = c->phys;
+    P.gamma = phys->gamma;
+    P.gm1 = phys->gamma - 1;
+    P.Cp = phys->Cp;
+    P.Cv = phys->Cp / phys->gamma;
+    P.rCv = 1. / P.Cv;
+    P.kFac = phys->Cp / phys->Pr;
+    P.mu0 = phys->mu0;
+    P.muAs = phys->mu_As;
+    P.muTs = phys->mu_Ts;
+    P.small = precision == AFVM_FP64 ? 1e-30 : 1e-9;   // adFVM/config.py:171-178
+    P.muModel = phys->mu_model;
+    P.riemann = phys->riemann;
+    P.briemann = phys->boundary_riemann;
+    c->objective = phys->objective;
+    c->objPatch = phys->objective_patch;
+    DeviceGuard dg(device);
+    HostTables h;
+    int st = build_tables(c, mesh, bcs, h);
+    if (!st) st = (precision == AFVM_FP64) ? upload_mesh<double>(c, h, c->m64) : upload_mesh<float>(c, h, c->m32);
+    if (!st) st = (precision == AFVM_FP64) ? alloc_work<double>(c) : alloc_work<float>(c);
+    if (!st) {
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) st = cuda_fail(c, e, "context set-up");
+    }
+    if (st) {
+        release(c);
+        delete c;
+        return st;
+    }
+    *out = reinterpret_cast<afvm_ctx*>(c);
+    return AFVM_OK;
+}
+
+int afvm_ctx_destroy(afvm_ctx* ctx) {
+    if (!ctx) return AFVM_OK;
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    release(c);
+    delete c;
+    return AFVM_OK;
+}
+
+const char* afvm_last_error(const afvm_ctx* ctx) {
+    if (!ctx) return "null context";
+    return reinterpret_cast<const Ctx*>(ctx)->err.c_str();
+}
+
+int afvm_profile(afvm_ctx* ctx, int32_t on) {
+    if (!ctx) return AFVM_ERR_BAD_ARG;
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    DeviceGuard dg(c->device);
+    for (auto& e : c->profEntries) { c->eventPool.push_back(e.a); c->eventPool.push_back(e.b); }
+    c->profEntries.clear();
+    c->prof = on != 0;
+    return AFVM_OK;
+}
+
+int afvm_profile_read(afvm_ctx* ctx, int32_t maxKernels, double* ms, int64_t* launches) {
+    if (!ctx || !ms || !launches || maxKernels < KID_COUNT) return AFVM_ERR_BAD_ARG;
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    DeviceGuard dg(c->device);
+    for (int k = 0; k < KID_COUNT; k++) { ms[k] = 0; launches[k] = 0; }
+    for (auto& e : c->profEntries) {
+        cudaError_t err = cudaEventSynchronize(e.b);
+        if (err != cudaSuccess) return cuda_fail(c, err, "profile read");
+        float t = 0;
+        cudaEventElapsedTime(&t, e.a, e.b);
+        ms[e.id] += t;
+        launches[e.id] += 1;
+    }
+    return AFVM_OK;
+}
+
+const char* afvm_profile_kernel_name(int32_t id) {
+    return (id >= 0 && id < KID_COUNT) ? kKernelNames[id] : nullptr;
+}
+
+int afvm_ctx_precision(const afvm_ctx* ctx) {
+    return ctx ? reinterpret_cast<const Ctx*>(ctx)->precision : -1;
+}
+
+int64_t afvm_ctx_device_bytes(const afvm_ctx* ctx) {
+    if (!ctx) return 0;
+    const Ctx* c = reinterpret_cast<const Ctx*>(ctx);
+    return c->bytes + c->adjBytes;
+}
+
+int afvm_set_bc_value(afvm_ctx* ctx, int32_t patch, int32_t field, const double* values) {
+    if (!ctx) return AFVM_ERR_BAD_ARG;
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (patch < 0 || patch >= c->nPatches || field < 0 || field > 2 || !values)
+        return fail(c, AFVM_ERR_BAD_ARG, "afvm_set_bc_value: bad patch/field/values");
+    int kind = c->bcKinds[3 * patch + field];
+    if (kind != AFVM_BC_FIXED_VALUE && kind != AFVM_BC_CBC_UPT)
+        return fail(c, AFVM_ERR_BAD_ARG, "afvm_set_bc_value: the BC has no values");
+    DeviceGuard dg(c->device);
+    int g0 = c->patchStart[patch] - c->nIF, n = c->patchN[patch];
+    int dims = field == 0 ? 3 : 1, comp0 = field == 0 ? 0 : (field == 1 ? 3 : 4);
+    size_t es = c->precision == AFVM_FP64 ? sizeof(double) : sizeof(float);
+    char* base = (char*)(c->precision == AFVM_FP64 ? (const void*)c->m64.gval : (const void*)c->m32.gval);
+    std::vector<char> col(es * (size_t)n);
+    for (int k = 0; k < dims; k++) {
+        for (int i = 0; i < n; i++) {
+            double v = values[(size_t)dims * i + k];
+            if (es == sizeof(double)) memcpy(&col[es * i], &v, es);
+            else { float fv = (float)v; memcpy(&col[es * i], &fv, es); }
+        }
+        cudaError_t e = cudaMemcpy(base + es * ((size_t)(comp0 + k) * c->nG + g0), col.data(), es * (size_t)n,
+                                   cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_fail(c, e, "afvm_set_bc_value");
+    }
+    return AFVM_OK;
+}
+
+int afvm_primal_step(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, double dt,
+                     const void* S_rho, const void* S_rhoU, const void* S_rhoE, void* rhoN, void* rhoUN, void* rhoEN,
+                     double* dtc_out, double* obj_out, void* stream) {
+    if (!ctx) return AFVM_ERR_BAD_ARG;
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!rho || !rhoU || !rhoE || !rhoN || !rhoUN || !rhoEN) return fail(c, AFVM_ERR_BAD_ARG, "null state pointer");
+    if (!std::isfinite(dt)) return fail(c, AFVM_ERR_BAD_ARG, "non-finite dt");
+    DeviceGuard dg(c->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    int st;
+    if (c->precision == AFVM_FP64)
+        st = primal_step_dev<double>(c, (const double*)rho, (const double*)rhoU, (const double*)rhoE, dt, nullptr,
+                                     (const double*)S_rho, (const double*)S_rhoU, (const double*)S_rhoE,
+                                     (double*)rhoN, (double*)rhoUN, (double*)rhoEN, c->scal, c->scal + 1, s);
+    else
+        st = primal_step_dev<float>(c, (const float*)rho, (const float*)rhoU, (const float*)rhoE, dt, nullptr,
+                                    (const float*)S_rho, (const float*)S_rhoU, (const float*)S_rhoE,
+                                    (float*)rhoN, (float*)rhoUN, (float*)rhoEN, c->scal, c->scal + 1, s);
+    if (st) return st;
+    return get_results(c, dtc_out, obj_out, s);
+}
+
+int afvm_primal_step_host(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, double dt,
+                          const void* S_rho, const void* S_rhoU, const void* S_rhoE, void* rhoN, void* rhoUN,
+                          void* rhoEN, double* dtc_out, double* obj_out, void* stream) {
+    if (!ctx) return AFVM_ERR_BAD_ARG;
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!rho || !rhoU || !rhoE || !rhoN || !rhoUN || !rhoEN) return fail(c, AFVM_ERR_BAD_ARG, "null state pointer");
+    DeviceGuard dg(c->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    size_t es = c->precision == AFVM_FP64 ? sizeof(double) : sizeof(float);
+    size_t n = c->nIC;
+    // device staging, allocated on first use: state in (5n), state out (5n), sources (5n)
+    if (!c->stageDev) {
+        int st0 = dalloc(c, &c->stageDev, es * n * 15);
+        if (st0) return st0;
+    }
+    int st = AFVM_OK;
+    void* stage = c->stageDev;
+    char* in = (char*)stage;
+    char* outp = in + es * n * 5;
+    char* src = outp + es * n * 5;
+    void* dIn[3] = {in, in + es * n, in + es * n * 4};
+    void* dOut[3] = {outp, outp + es * n, outp + es * n * 4};
+    const void* hIn[3] = {rho, rhoU, rhoE};
+    void* hOut[3] = {rhoN, rhoUN, rhoEN};
+    size_t cnt[3] = {n, 3 * n, n};
+    for (int k = 0; k < 3; k++) {
+        cudaError_t e = cudaMemcpyAsync(dIn[k], hIn[k], es * cnt[k], cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return cuda_fail(c, e, "state upload");
+    }
+    const void* S[3] = {S_rho, S_rhoU, S_rhoE};
+    void* dS[3] = {nullptr, nullptr, nullptr};
+    void* sbuf[3] = {src, src + es * n, src + es * n * 4};
+    for (int k = 0; k < 3; k++) {
+        if (S[k]) {
+            cudaError_t e = cudaMemcpyAsync(sbuf[k], S[k], es * cnt[k], cudaMemcpyHostToDevice, s);
+            if (e != cudaSuccess) return cuda_fail(c, e, "source upload");
+            dS[k] = sbuf[k];
+        }
+    }
+    st = afvm_primal_step(ctx, dIn[0], dIn[1], dIn[2], dt, dS[0], dS[1], dS[2], dOut[0], dOut[1], dOut[2], nullptr,
+                          nullptr, stream);
+    if (st) return st;
+    for (int k = 0; k < 3; k++) {
+        cudaError_t e = cudaMemcpyAsync(hOut[k], dOut[k], es * cnt[k], cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) return cuda_fail(c, e, "state download");
+    }
+    if (!dtc_out && !obj_out) {
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return cuda_fail(c, e, "host step");
+        return AFVM_OK;
+    }
+    return get_results(c, dtc_out, obj_out, s);
+}
+
+int afvm_primal_run(afvm_ctx* ctx, void* rho, void* rhoU, void* rhoE, int32_t nSteps, double dt0, double CFL,
+                    double stepFactor, int32_t fixed_dt, const void* S_rho, const void* S_rhoU, const void* S_rhoE,
+                    double* dt_hist, double* dtc_hist, double* obj_hist, void* stream) {
+    if (!ctx) return AFVM_ERR_BAD_ARG;
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!rho || !rhoU || !rhoE || nSteps < 0) return fail(c, AFVM_ERR_BAD_ARG, "afvm_primal_run arguments");
+    DeviceGuard dg(c->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (c->precision == AFVM_FP64)
+        return primal_run_dev<double>(c, (double*)rho, (double*)rhoU, (double*)rhoE, nSteps, dt0, CFL, stepFactor,
+                                      fixed_dt, (const double*)S_rho, (const double*)S_rhoU, (const double*)S_rhoE,
+                                      dt_hist, dtc_hist, obj_hist, s);
+    return primal_run_dev<float>(c, (float*)rho, (float*)rhoU, (float*)rhoE, nSteps, dt0, CFL, stepFactor, fixed_dt,
+                                 (const float*)S_rho, (const float*)S_rhoU, (const float*)S_rhoE, dt_hist, dtc_hist,
+                                 obj_hist, s);
+}
+
+int afvm_adjoint_step(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, double dt,
+                      const void* S_rho, const void* S_rhoU, const void* S_rhoE, const void* rhoNa,
+                      const void* rhoUNa, const void* rhoENa, double dtca, double obja, void* rhoa, void* rhoUa,
+                      void* rhoEa, void* S_rhoa, void* S_rhoUa, void* S_rhoEa, void* stream) {
+    if (!ctx) return AFVM_ERR_BAD_ARG;
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    return fail(c, AFVM_ERR_UNSUPPORTED, "adjoint not built yet");
+}
+
+int afvm_sensitivity(afvm_ctx* ctx, int32_t nArrays, const double* const* grad, const double* const* pert,
+                     const int64_t* n, double* out, void* stream) {
+    if (!ctx) return AFVM_ERR_BAD_ARG;
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    return fail(c, AFVM_ERR_UNSUPPORTED, "sensitivity not built yet");
+}
+
+}  // extern "C"

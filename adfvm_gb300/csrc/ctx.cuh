@@ -1,0 +1,129 @@
+// Device context: mesh tables, boundary conditions and work buffers of one solver on one GPU.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+#include "afvm.h"
+#include "physics.cuh"
+
+namespace afvm {
+
+constexpr int BLOCK = 256;
+
+// boundary-condition kind codes stored per ghost cell (3 bits per field: U, T, p)
+constexpr int GK_COPY = 0;     // zeroGradient / empty / cyclic: value of the source cell
+constexpr int GK_FIXED = 1;    // fixedValue or CBC_UPT: stored value
+constexpr int GK_SYM = 2;      // symmetryPlane: U minus its normal component
+
+template <typename R>
+struct MeshDev {
+    int nIC, nIF, nF, nC, nG;
+    // faces
+    const int32_t* own;       // nF
+    const int32_t* nbr;       // nF (ghost ids for boundary faces)
+    const R* nrm;             // 3 x nF (SoA)
+    const R* area;            // nF
+    const R* dlt;             // nF  deltas
+    const R* du;              // 3 x nF deltasUnit
+    const R* lw;              // 2 x nF linearWeights
+    const R* qw;              // 6 x nF quadraticWeights (side0 xyz, side1 xyz)
+    const uint8_t* fkind;     // nF - nIF: FACE_* of each boundary face
+    const int32_t* gsrc;      // nG: source cell of a ghost (owner, or partner owner for cyclic)
+    const int32_t* gkind;     // nG: 3-bit BC codes U | T<<3 | p<<6
+    const R* gval;            // 5 x nG fixed U, T, p (fixedValue / CBC_UPT)
+    // cells: gradient gather slots (cellFaces order), 6 x nIC each
+    const int32_t* gnb;       // cellNeighbours
+    const R* gw;              // w' = w + O - 2 w O
+    const R* gsn;             // 3 x 6 x nIC: S * (2 N O - N)
+    const R* rvol;            // nIC 1/V
+    // cells: flux accumulation in collate order, 6 x nIC
+    const int32_t* accf;      // face id, or ~face id on the neighbour side
+    const R* accw;            // A/V_L (owner side) or A/V_R (neighbour side)
+    const R* vol;             // nIC
+};
+
+// kernel ids for the optional per-launch event timing (afvm_profile_*)
+enum KernelId { KID_PRIM = 0, KID_GRAD, KID_FLUX, KID_UPDATE, KID_OBJECTIVE, KID_FINISH, KID_ADJ_FLUX,
+                KID_ADJ_GATHER, KID_ADJ_GRAD, KID_ADJ_PRIM, KID_ADJ_MISC, KID_SENS, KID_COUNT };
+extern const char* const kKernelNames[KID_COUNT];
+
+struct ProfEntry {
+    int id;
+    cudaEvent_t a, b;
+};
+
+struct Ctx {
+    int precision;            // AFVM_FP64 / AFVM_FP32
+    int device;
+    std::string err;
+    Phys phys;
+    int objective, objPatch;
+    int objStart, objN;       // face range of the objective patch
+    int nIC, nIF, nF, nC, nG, nPatches;
+    std::vector<int> patchStart, patchN, patchKind, patchCellStart;
+    // device allocations
+    std::vector<void*> allocs;
+    int64_t bytes = 0;
+    MeshDev<double> m64;
+    MeshDev<float> m32;
+    // work buffers (element type by precision)
+    void* rec = nullptr;      // nC x REC
+    void* fflux = nullptr;    // nF x FREC
+    void* u1[3] = {nullptr, nullptr, nullptr};   // stage states rho, rhoU, rhoE
+    void* u2[3] = {nullptr, nullptr, nullptr};
+    void* zeroS = nullptr;    // nIC x 5 zeros (absent sources)
+    double* partials = nullptr;   // reduction scratch (block partial sums)
+    int nPartials = 0;
+    double* scal = nullptr;   // device scalars: [0] dtc (stage 1 max), [1] obj, [2] dt, [3] sensitivity
+    unsigned long long* dtcBits = nullptr;
+    // ghost BC values on the host for updates
+    std::vector<int> ghostPatchOffset;   // first ghost index of each patch (sorted order)
+    std::vector<int> bcKinds;            // per patch: U,T,p kinds
+    // adjoint buffers (allocated on first use)
+    void* adj = nullptr;
+    int64_t adjBytes = 0;
+    // device staging of the host-buffer entry point (allocated on first use)
+    void* stageDev = nullptr;
+    // per-launch event timing
+    bool prof = false;
+    std::vector<ProfEntry> profEntries;
+    std::vector<cudaEvent_t> eventPool;
+};
+
+// Event pair around one kernel launch when timing is on (no effect otherwise).
+struct ProfScope {
+    Ctx* c;
+    cudaStream_t s;
+    ProfEntry e;
+    bool on;
+    ProfScope(Ctx* c_, int id, cudaStream_t s_);
+    ~ProfScope();
+};
+
+int fail(Ctx* c, int code, const std::string& msg);
+int cuda_fail(Ctx* c, cudaError_t e, const char* what);
+
+// kernel launchers (primal.cu)
+// dt: by value, or read on the device from dtDev when that is non-NULL
+template <typename R>
+int primal_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double dt, const double* dtDev,
+                    const R* Srho, const R* SrhoU, const R* SrhoE, R* rhoN, R* rhoUN, R* rhoEN,
+                    double* dtcDev, double* objDev, cudaStream_t s);
+template <typename R>
+int primal_run_dev(Ctx* c, R* rho, R* rhoU, R* rhoE, int nSteps, double dt0, double CFL, double stepFactor,
+                   int fixed, const R* Srho, const R* SrhoU, const R* SrhoE, double* dtHist, double* dtcHist,
+                   double* objHist, cudaStream_t s);
+int sensitivity_dev(Ctx* c, int nArrays, const double* const* grad, const double* const* pert,
+                    const int64_t* n, double* out, cudaStream_t s);
+template <typename R>
+int adjoint_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double dt,
+                     const R* Srho, const R* SrhoU, const R* SrhoE,
+                     const R* rhoNa, const R* rhoUNa, const R* rhoENa, double obja,
+                     R* rhoa, R* rhoUa, R* rhoEa, R* Srhoa, R* SrhoUa, R* SrhoEa, cudaStream_t s);
+
+template <typename R> inline const MeshDev<R>& meshOf(const Ctx* c);
+template <> inline const MeshDev<double>& meshOf<double>(const Ctx* c) { return c->m64; }
+template <> inline const MeshDev<float>& meshOf<float>(const Ctx* c) { return c->m32; }
+
+}  // namespace afvm

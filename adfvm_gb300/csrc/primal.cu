@@ -1,0 +1,409 @@
+// Primal residual and SSP-RK3 step on the device (sm_103a).
+//
+// One stage of the reference's time step (adFVM/timestep.py:27-55 over RCF.equation,
+// adFVM/density.py:339-414) is four kernels:
+//   k_prim    cells + ghost cells: conservative -> primitive (density.py:162-171) and the
+//             ghost-cell boundary conditions (BCs.py via Solver.boundary, solver.py:106-114)
+//   k_grad    cells: Green-Gauss gradient, a gather over the 6 cellFaces (op.py:45-63)
+//   k_flux    faces: reconstruction, Riemann flux, viscous flux, CFL term (density.py:253-331)
+//   k_update  cells: gather of the face fluxes in the reference's collate order (no atomics),
+//             the SSP-RK stage combination (timestep.py:35-45) and, at stage 1, the CFL max
+// Data: one record of REC values per cell (primitives + gradients), one FREC record per
+// face, mesh constants in SoA arrays; the conservative state keeps the reference layout
+// (rho (n), rhoU (n x 3), rhoE (n)).
+#include <cuda_runtime.h>
+#include "ctx.cuh"
+
+namespace afvm {
+
+// RCF.primitive (adFVM/density.py:162-171) in double. One out-of-line body, so that a ghost
+// cell and its source cell get bit-identical values.
+__device__ __noinline__ void primitive_d(const Phys& P, double rho, double r0, double r1, double r2, double rhoE,
+                                         double* out) {
+    double U0 = r0 / rho, U1 = r1 / rho, U2 = r2 / rho;
+    double E = rhoE / rho;
+    double e = E - 0.5 * (U0 * U0 + U1 * U1 + U2 * U2);
+    out[0] = U0; out[1] = U1; out[2] = U2;
+    out[4] = (P.gm1 * rho) * e;
+    out[3] = e * P.rCv;
+}
+
+template <typename R>
+__device__ __forceinline__ void load_prim(const Phys& P, const R* rho, const R* rhoU, const R* rhoE, int c, R* out) {
+    double o[5];
+    primitive_d(P, (double)rho[c], (double)rhoU[3 * c], (double)rhoU[3 * c + 1], (double)rhoU[3 * c + 2], (double)rhoE[c], o);
+    for (int k = 0; k < 5; k++) out[k] = (R)o[k];
+}
+
+template <typename R>
+__global__ void __launch_bounds__(BLOCK) k_prim(MeshDev<R> m, Phys P, const R* __restrict__ rho,
+                                                const R* __restrict__ rhoU, const R* __restrict__ rhoE,
+                                                R* __restrict__ rec) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < m.nIC) {
+        R v[5];
+        load_prim<R>(P, rho, rhoU, rhoE, t, v);
+        R* r = rec + (size_t)t * REC;
+        for (int k = 0; k < 5; k++) r[k] = v[k];
+        return;
+    }
+    int g = t - m.nIC;
+    if (g >= m.nG) return;
+    int src = m.gsrc[g];
+    int kind = m.gkind[g];
+    R v[5];
+    load_prim<R>(P, rho, rhoU, rhoE, src, v);
+    int kU = kind & 7, kT = (kind >> 3) & 7, kp = (kind >> 6) & 7;
+    if (kU == GK_FIXED) {
+        for (int k = 0; k < 3; k++) v[k] = m.gval[(size_t)k * m.nG + g];
+    } else if (kU == GK_SYM) {
+        int f = m.nIF + g;
+        R n[3] = {m.nrm[f], m.nrm[(size_t)m.nF + f], m.nrm[2 * (size_t)m.nF + f]};
+        R un = dot3(v, n);
+        for (int k = 0; k < 3; k++) v[k] = v[k] - un * n[k];
+    }
+    if (kT == GK_FIXED) v[3] = m.gval[3 * (size_t)m.nG + g];
+    if (kp == GK_FIXED) v[4] = m.gval[4 * (size_t)m.nG + g];
+    R* r = rec + (size_t)t * REC;
+    for (int k = 0; k < 5; k++) r[k] = v[k];
+}
+
+template <typename R>
+__global__ void __launch_bounds__(BLOCK) k_grad(MeshDev<R> m, R* __restrict__ rec) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m.nIC) return;
+    const R* rc = rec + (size_t)c * REC;
+    R phic[5];
+    for (int k = 0; k < 5; k++) phic[k] = rc[k];
+    R g[15];
+    for (int k = 0; k < 15; k++) g[k] = R(0);
+    const size_t n = m.nIC;
+#pragma unroll
+    for (int s = 0; s < 6; s++) {
+        int nb = m.gnb[s * n + c];
+        R w = m.gw[s * n + c];
+        R omw = -w + R(1);
+        R sn[3] = {m.gsn[(3 * s) * n + c], m.gsn[(3 * s + 1) * n + c], m.gsn[(3 * s + 2) * n + c]};
+        const R* rn = rec + (size_t)nb * REC;
+        R phiF[5];
+        for (int k = 0; k < 5; k++) phiF[k] = phic[k] * omw + rn[k] * w;
+        for (int i = 0; i < 5; i++)
+            for (int j = 0; j < 3; j++) g[3 * i + j] = g[3 * i + j] + phiF[i] * sn[j];
+    }
+    R rv = m.rvol[c];
+    R* out = rec + (size_t)c * REC + R_GU;
+    for (int k = 0; k < 15; k++) out[k] = g[k] * rv;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(BLOCK) k_flux(MeshDev<R> m, Phys P, const R* __restrict__ rec,
+                                                R* __restrict__ fflux, int inviscid) {
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= m.nF) return;
+    const size_t nF = m.nF;
+    int kind = (f < m.nIF) ? FACE_INTERNAL : (int)m.fkind[f - m.nIF];
+    int iP = m.own[f], iN = m.nbr[f];
+    int iNg = (f < m.nIF) ? iN : m.gsrc[iN - m.nIC];   // ghost gradient = copy of its source
+    const R* rP = rec + (size_t)iP * REC;
+    const R* rN = rec + (size_t)iN * REC;
+    const R* rNg = rec + (size_t)iNg * REC;
+    R UP[3] = {rP[0], rP[1], rP[2]}, TP = rP[R_T], pP = rP[R_P];
+    R UN[3] = {rN[0], rN[1], rN[2]}, TN = rN[R_T], pN = rN[R_P];
+    R gUP[9], gUN[9], gTP[3], gTN[3], gpP[3], gpN[3];
+    for (int k = 0; k < 9; k++) { gUP[k] = rP[R_GU + k]; gUN[k] = rNg[R_GU + k]; }
+    for (int k = 0; k < 3; k++) {
+        gTP[k] = rP[R_GT + k]; gTN[k] = rNg[R_GT + k];
+        gpP[k] = rP[R_GP + k]; gpN[k] = rNg[R_GP + k];
+    }
+    R N[3] = {m.nrm[f], m.nrm[nF + f], m.nrm[2 * nF + f]};
+    R F[5];
+    R TF, UF[3];
+    R gTF[3], gUF[9];
+    if (kind == FACE_BOUNDARY) {
+        // RCF.boundaryFlux (density.py:307-331) with RCF.getFlux (density.py:184-190)
+        R rho, rhoU[3], rhoE;
+        conservative<R>(P, UN, TN, pN, rho, rhoU, rhoE);
+        R Un = dot3(UN, N);
+        F[0] = rho * Un;
+        for (int k = 0; k < 3; k++) F[1 + k] = rhoU[k] * Un + pN * N[k];
+        F[4] = (rhoE + pN) * Un;
+        TF = TN;
+        for (int k = 0; k < 3; k++) { UF[k] = UN[k]; gTF[k] = gTN[k]; }
+        for (int k = 0; k < 9; k++) gUF[k] = gUN[k];
+    } else {
+        R lw0 = m.lw[f];
+        R qw0[3] = {m.qw[f], m.qw[nF + f], m.qw[2 * nF + f]};
+        R ULF[3], TLF, pLF;
+        for (int k = 0; k < 3; k++) ULF[k] = recon<R>(UP[k], UN[k], gUP + 3 * k, lw0, qw0);
+        TLF = recon<R>(TP, TN, gTP, lw0, qw0);
+        pLF = recon<R>(pP, pN, gpP, lw0, qw0);
+        R rhoL, rhoUL[3], rhoEL;
+        conservative<R>(P, ULF, TLF, pLF, rhoL, rhoUL, rhoEL);
+        R URF[3], TRF, pRF;
+        int solver;
+        if (kind == FACE_CHARACTERISTIC) {
+            for (int k = 0; k < 3; k++) URF[k] = UN[k];
+            TRF = TN; pRF = pN;
+            solver = P.briemann;
+        } else {
+            R lw1 = m.lw[nF + f];
+            R qw1[3] = {m.qw[3 * nF + f], m.qw[4 * nF + f], m.qw[5 * nF + f]};
+            for (int k = 0; k < 3; k++) URF[k] = recon<R>(UN[k], UP[k], gUN + 3 * k, lw1, qw1);
+            TRF = recon<R>(TN, TP, gTN, lw1, qw1);
+            pRF = recon<R>(pN, pP, gpN, lw1, qw1);
+            solver = P.riemann;
+        }
+        R rhoR, rhoUR[3], rhoER;
+        conservative<R>(P, URF, TRF, pRF, rhoR, rhoUR, rhoER);
+        if (solver == AFVM_RIEMANN_ROE)
+            roe<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, N, F);
+        else
+            laxf<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, rhoUL, rhoUR, rhoEL, rhoER, N, F);
+        if (kind == FACE_CHARACTERISTIC) {
+            TF = TN;
+            for (int k = 0; k < 3; k++) { UF[k] = UN[k]; gTF[k] = gTN[k]; }
+            for (int k = 0; k < 9; k++) gUF[k] = gUN[k];
+        } else {
+            TF = R(0.5) * (TLF + TRF);
+            for (int k = 0; k < 3; k++) { UF[k] = R(0.5) * (ULF[k] + URF[k]); gTF[k] = R(0.5) * (gTP[k] + gTN[k]); }
+            for (int k = 0; k < 9; k++) gUF[k] = R(0.5) * (gUP[k] + gUN[k]);
+        }
+    }
+    if (!inviscid) {
+        R D[3] = {m.du[f], m.du[nF + f], m.du[2 * nF + f]};
+        viscous<R>(P, TP, TN, UP, UN, TF, UF, gTF, gUF, D, N, m.dlt[f], F);
+    }
+    R aF = sqrt(R(P.Cp) * TF * R(P.gm1));
+    R maxaF = fabs(dot3(UF, N)) + aF;
+    R* out = fflux + (size_t)f * FREC;
+    for (int k = 0; k < 5; k++) out[k] = F[k];
+    out[5] = maxaF;
+}
+
+// Gather of the face fluxes (op.div / op.absDiv, op.py:12-29, collated in the order of
+// density.py:390-402) and the SSP-RK3 stage update (timestep.py:35-45).
+template <typename R, int STAGE>
+__global__ void __launch_bounds__(BLOCK) k_update(MeshDev<R> m, const R* __restrict__ fflux, double dtv,
+                                                  const double* dtp,
+                                                  const R* u0r, const R* u0u, const R* u0e,
+                                                  const R* u1r, const R* u1u, const R* u1e,
+                                                  const R* u2r, const R* u2u, const R* u2e,
+                                                  const R* __restrict__ Sr, const R* __restrict__ Su,
+                                                  const R* __restrict__ Se,
+                                                  R* outr, R* outu, R* oute,
+                                                  unsigned long long* dtcBits) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    R dtc = R(0);
+    if (c < m.nIC) {
+        const size_t n = m.nIC;
+        R res[5] = {R(0), R(0), R(0), R(0), R(0)};
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            int e = m.accf[k * n + c];
+            R w = m.accw[k * n + c];
+            bool ownerSide = e >= 0;
+            int f = ownerSide ? e : ~e;
+            const R* F = fflux + (size_t)f * FREC;
+            for (int q = 0; q < 5; q++) {
+                R t = F[q] * w;
+                res[q] = res[q] + (ownerSide ? t : -t);
+            }
+            dtc = dtc + F[5] * w;
+        }
+        R S[5] = {Sr[c], Su[3 * c], Su[3 * c + 1], Su[3 * c + 2], Se[c]};
+        R a[5] = {u0r[c], u0u[3 * c], u0u[3 * c + 1], u0u[3 * c + 2], u0e[c]};
+        R o[5];
+        const R rdt = R(dtp ? *dtp : dtv);
+        if (STAGE == 0) {
+            for (int q = 0; q < 5; q++) o[q] = a[q] + (R(-1.0) * (res[q] - S[q])) * rdt;
+        } else if (STAGE == 1) {
+            R b[5] = {u1r[c], u1u[3 * c], u1u[3 * c + 1], u1u[3 * c + 2], u1e[c]};
+            for (int q = 0; q < 5; q++)
+                o[q] = (R(3. / 4) * a[q] + R(1. / 4) * b[q]) + (R(-(1. / 4)) * (res[q] - S[q])) * rdt;
+        } else {
+            R b[5] = {u2r[c], u2u[3 * c], u2u[3 * c + 1], u2u[3 * c + 2], u2e[c]};
+            for (int q = 0; q < 5; q++)
+                o[q] = (R(1. / 3) * a[q] + R(2. / 3) * b[q]) + (R(-(2. / 3)) * (res[q] - S[q])) * rdt;
+        }
+        outr[c] = o[0];
+        outu[3 * c] = o[1]; outu[3 * c + 1] = o[2]; outu[3 * c + 2] = o[3];
+        oute[c] = o[4];
+    }
+    if (STAGE == 1) {
+        // reduce_max of the CFL sums (density.py:405-410): warp shuffle, block, then an atomic
+        // max on the bit pattern (non-negative doubles order like their bits)
+        double d = (double)dtc;
+        for (int off = 16; off > 0; off >>= 1) d = fmax(d, __shfl_down_sync(0xffffffffu, d, off));
+        __shared__ double wmax[BLOCK / 32];
+        if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = d;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            d = (threadIdx.x < BLOCK / 32) ? wmax[threadIdx.x] : 0.0;
+            for (int off = 16; off > 0; off >>= 1) d = fmax(d, __shfl_down_sync(0xffffffffu, d, off));
+            if (threadIdx.x == 0) atomicMax(dtcBits, (unsigned long long)__double_as_longlong(d));
+        }
+    }
+}
+
+// ---- objectives, evaluated on the ghost-completed primitives of stage 1 ----
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x < 32) {
+        r = (threadIdx.x < BLOCK / 32) ? sh[threadIdx.x] : 0.0;
+        for (int off = 16; off > 0; off >>= 1) r += __shfl_down_sync(0xffffffffu, r, off);
+    }
+    return r;
+}
+
+// per-block partial sums; kinds: AFVM_OBJ_KINETIC_ENERGY, AFVM_OBJ_SUM_T (cells) and
+// AFVM_OBJ_DRAG (faces [start, start+n) of one patch, templates/cylinder_test.py:9-19)
+template <typename R>
+__global__ void __launch_bounds__(BLOCK) k_objective(MeshDev<R> m, Phys P, const R* __restrict__ rec, int kind,
+                                                     int start, int n, double* partials) {
+    __shared__ double sh[BLOCK / 32];
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double v = 0.0;
+    if (t < n) {
+        if (kind == AFVM_OBJ_KINETIC_ENERGY) {
+            const R* r = rec + (size_t)t * REC;
+            double U[3] = {(double)r[0], (double)r[1], (double)r[2]};
+            double T = r[R_T], p = r[R_P];
+            double rho = p / ((P.Cv * T) * P.gm1);
+            v = 0.5 * rho * (U[0] * U[0] + U[1] * U[1] + U[2] * U[2]) * (double)m.vol[t];
+        } else if (kind == AFVM_OBJ_SUM_T) {
+            v = (double)rec[(size_t)t * REC + R_T];
+        } else {
+            int f = start + t;
+            const R* rN = rec + (size_t)m.nbr[f] * REC;
+            const R* rP = rec + (size_t)m.own[f] * REC;
+            double U0 = rN[0], U0i = rP[0], p0 = rN[R_P], T0 = rN[R_T];
+            double nx = m.nrm[f];
+            double mu = (P.muModel == AFVM_MU_SUTHERLAND) ? (P.muAs * (T0 * sqrt(T0))) / (T0 + P.muTs) : P.mu0;
+            double mungUx = mu * (U0 - U0i) / (double)m.dlt[f];
+            v = (p0 * nx - mungUx) * (double)m.area[f];
+        }
+    }
+    double s = block_sum(v, sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+// fixed-order final sum of the partials (deterministic) and the dtc bits -> double
+__global__ void k_finish(const double* partials, int nPartials, const unsigned long long* dtcBits,
+                         double* dtcOut, double* objOut, int haveObj) {
+    __shared__ double sh[BLOCK / 32];
+    double v = 0.0;
+    for (int i = threadIdx.x; i < nPartials; i += BLOCK) v += partials[i];
+    double s = block_sum(haveObj ? v : 0.0, sh);
+    if (threadIdx.x == 0) {
+        if (objOut) *objOut = haveObj ? s : 0.0;
+        if (dtcOut) *dtcOut = __longlong_as_double((long long)*dtcBits);
+    }
+}
+
+static inline int nblocks(long long n) { return (int)((n + BLOCK - 1) / BLOCK); }
+
+template <typename R>
+int primal_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double dt, const double* dtDev,
+                    const R* Srho, const R* SrhoU, const R* SrhoE, R* rhoN, R* rhoUN, R* rhoEN,
+                    double* dtcDev, double* objDev, cudaStream_t s) {
+    const MeshDev<R>& m = meshOf<R>(c);
+    const Phys& P = c->phys;
+    R* rec = (R*)c->rec;
+    R* ff = (R*)c->fflux;
+    const R* zs = (const R*)c->zeroS;
+    if (!Srho) Srho = zs;
+    if (!SrhoU) SrhoU = zs + c->nIC;
+    if (!SrhoE) SrhoE = zs + 4 * (size_t)c->nIC;
+    int inviscid = (P.muModel == AFVM_MU_CONSTANT && P.mu0 == 0.0) ? 1 : 0;
+    R* u1[3] = {(R*)c->u1[0], (R*)c->u1[1], (R*)c->u1[2]};
+    R* u2[3] = {(R*)c->u2[0], (R*)c->u2[1], (R*)c->u2[2]};
+    cudaMemsetAsync(c->dtcBits, 0, sizeof(unsigned long long), s);
+    const R* in[3][3] = {{rho, rhoU, rhoE}, {u1[0], u1[1], u1[2]}, {u2[0], u2[1], u2[2]}};
+    int nObjBlocks = 0;
+    for (int st = 0; st < 3; st++) {
+        {
+            ProfScope ps(c, KID_PRIM, s);
+            k_prim<R><<<nblocks(m.nIC + m.nG), BLOCK, 0, s>>>(m, P, in[st][0], in[st][1], in[st][2], rec);
+        }
+        if (st == 1 && c->objective != AFVM_OBJ_NONE) {
+            int start = 0, n = m.nIC;
+            if (c->objective == AFVM_OBJ_DRAG) { start = c->objStart; n = c->objN; }
+            nObjBlocks = nblocks(n);
+            if (nObjBlocks > c->nPartials) return fail(c, AFVM_ERR_BAD_ARG, "objective partials overflow");
+            if (n > 0) {
+                ProfScope ps(c, KID_OBJECTIVE, s);
+                k_objective<R><<<nObjBlocks, BLOCK, 0, s>>>(m, P, rec, c->objective, start, n, c->partials);
+            }
+        }
+        {
+            ProfScope ps(c, KID_GRAD, s);
+            k_grad<R><<<nblocks(m.nIC), BLOCK, 0, s>>>(m, rec);
+        }
+        {
+            ProfScope ps(c, KID_FLUX, s);
+            k_flux<R><<<nblocks(m.nF), BLOCK, 0, s>>>(m, P, rec, ff, inviscid);
+        }
+        int nb = nblocks(m.nIC);
+        ProfScope ps(c, KID_UPDATE, s);
+        if (st == 0)
+            k_update<R, 0><<<nb, BLOCK, 0, s>>>(m, ff, dt, dtDev, rho, rhoU, rhoE, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                                nullptr, Srho, SrhoU, SrhoE, u1[0], u1[1], u1[2], c->dtcBits);
+        else if (st == 1)
+            k_update<R, 1><<<nb, BLOCK, 0, s>>>(m, ff, dt, dtDev, rho, rhoU, rhoE, u1[0], u1[1], u1[2], nullptr, nullptr,
+                                                nullptr, Srho, SrhoU, SrhoE, u2[0], u2[1], u2[2], c->dtcBits);
+        else
+            k_update<R, 2><<<nb, BLOCK, 0, s>>>(m, ff, dt, dtDev, rho, rhoU, rhoE, nullptr, nullptr, nullptr, u2[0], u2[1],
+                                                u2[2], Srho, SrhoU, SrhoE, rhoN, rhoUN, rhoEN, c->dtcBits);
+    }
+    {
+        ProfScope ps(c, KID_FINISH, s);
+        k_finish<<<1, BLOCK, 0, s>>>(c->partials, nObjBlocks, c->dtcBits, dtcDev, objDev, nObjBlocks > 0);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(c, e, "primal step launch");
+    return AFVM_OK;
+}
+
+// time-step rule of the reference loop, dt <- min(2*CFL/dtc, stepFactor*dt)
+// (adFVM/solver.py:365), kept on the device; records the dt each step used
+__global__ void k_next_dt(double* dt, const double* dtc, double CFL, double stepFactor, int fixed, double* dtHist) {
+    double d = *dt;
+    if (dtHist) *dtHist = d;
+    if (!fixed) *dt = fmin(2 * CFL / *dtc, d * stepFactor);
+}
+
+template <typename R>
+int primal_run_dev(Ctx* c, R* rho, R* rhoU, R* rhoE, int nSteps, double dt0, double CFL, double stepFactor,
+                   int fixed, const R* Srho, const R* SrhoU, const R* SrhoE, double* dtHist, double* dtcHist,
+                   double* objHist, cudaStream_t s) {
+    double* dtDev = c->scal + 2;
+    cudaMemcpyAsync(dtDev, &dt0, sizeof(double), cudaMemcpyHostToDevice, s);
+    for (int n = 0; n < nSteps; n++) {
+        double* dtcOut = dtcHist ? dtcHist + n : c->scal;
+        int st = primal_step_dev<R>(c, rho, rhoU, rhoE, 0.0, dtDev, Srho, SrhoU, SrhoE, rho, rhoU, rhoE, dtcOut,
+                                    objHist ? objHist + n : c->scal + 1, s);
+        if (st != AFVM_OK) return st;
+        k_next_dt<<<1, 1, 0, s>>>(dtDev, dtcOut, CFL, stepFactor, fixed, dtHist ? dtHist + n : nullptr);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(c, e, "primal run launch");
+    return AFVM_OK;
+}
+
+template int primal_step_dev<double>(Ctx*, const double*, const double*, const double*, double, const double*,
+                                     const double*, const double*, const double*, double*, double*, double*,
+                                     double*, double*, cudaStream_t);
+template int primal_step_dev<float>(Ctx*, const float*, const float*, const float*, double, const double*,
+                                    const float*, const float*, const float*, float*, float*, float*, double*,
+                                    double*, cudaStream_t);
+template int primal_run_dev<double>(Ctx*, double*, double*, double*, int, double, double, double, int,
+                                    const double*, const double*, const double*, double*, double*, double*,
+                                    cudaStream_t);
+template int primal_run_dev<float>(Ctx*, float*, float*, float*, int, double, double, double, int, const float*,
+                                   const float*, const float*, double*, double*, double*, cudaStream_t);
+
+}  // namespace afvm

@@ -1,0 +1,313 @@
+"""Host-side mirror of the reference solver's call surface, backed by libafvm on one GPU.
+
+``RCF`` takes the reference's options (adFVM/density.py:22-39, adFVM/solver.py:21-42) and
+exposes:
+
+* ``map(*inputs)`` - the compiled step function the reference's time loop calls
+  (adFVM/solver.py:312-323): the same positional inputs ``[rho, rhoU, rhoE, dt] +
+  mesh.getTensor() + mesh.getScalar() + sources + getBoundaryTensor(1)`` and the same outputs
+  ``[rhoN, rhoUN, rhoEN, dtc (1,1), obj (1,1)]`` as numpy arrays;
+* ``step(...)`` - the same step on device tensors (torch CUDA), no host copies;
+* ``run(...)`` - the reference's ``Solver.run`` loop (time-step rule, ``round(t0+dt, 12)``,
+  objective sum; adFVM/solver.py:210-411) in ``simulation``/``forward`` modes, without
+  file IO;
+* ``run_device(...)`` - n steps resident on the GPU (``afvm_primal_run``).
+The GPU library is mandatory: there is no CPU path.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from .mesh import Mesh, CYCLIC_PATCHES
+
+_BC = {'zeroGradient': L.AFVM_BC_ZERO_GRADIENT, 'empty': L.AFVM_BC_ZERO_GRADIENT,
+       'inletOutlet': L.AFVM_BC_ZERO_GRADIENT, 'calculated': L.AFVM_BC_ZERO_GRADIENT,
+       'fixedValue': L.AFVM_BC_FIXED_VALUE, 'symmetryPlane': L.AFVM_BC_SYMMETRY_PLANE,
+       'slip': L.AFVM_BC_SYMMETRY_PLANE, 'cyclic': L.AFVM_BC_CYCLIC, 'CBC_UPT': L.AFVM_BC_CBC_UPT}
+_RIEMANN = {'eulerRoe': L.AFVM_RIEMANN_ROE, 'eulerLaxFriedrichs': L.AFVM_RIEMANN_LF}
+DEFAULTS = {'Cp': 1004.5, 'gamma': 1.4, 'Pr': 0.7, 'CFL': 1.2, 'stepFactor': 1.2,
+            'riemannSolver': 'eulerRoe', 'boundaryRiemannSolver': 'eulerRoe', 'mu': None,
+            'fixedTimeStep': False, 'timeIntegrator': 'SSPRK', 'nStages': 3,
+            'faceReconstructor': 'secondOrder'}
+SUTHERLAND = (1.4792e-06, 116.)            # adFVM/density.py:27
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class RCF(object):
+    """GB300 drop-in for the reference RCF solver's residual/step evaluation."""
+
+    names = ['rho', 'rhoU', 'rhoE']
+    dimensions = [(1,), (3,), (1,)]
+
+    def __init__(self, mesh, bc, objective='none', precision='fp64', device=0, **config):
+        for k in config:
+            if k not in DEFAULTS:
+                raise ValueError('unknown RCF option %r' % k)
+        cfg = dict(DEFAULTS)
+        cfg.update(config)
+        if cfg['timeIntegrator'] != 'SSPRK' or cfg['faceReconstructor'] != 'secondOrder':
+            raise NotImplementedError('SSPRK with secondOrder reconstruction is the implemented path')
+        self.config = cfg
+        for k, v in cfg.items():
+            setattr(self, k, v)
+        self.Cv = self.Cp / self.gamma
+        self.mesh = mesh if isinstance(mesh, Mesh) else Mesh.create(mesh)
+        self.bc = bc
+        self.objective = objective
+        self.precision = {'fp64': L.AFVM_FP64, 'fp32': L.AFVM_FP32}[precision]
+        self.dtype = np.float64 if self.precision == L.AFVM_FP64 else np.float32
+        self.device = device
+        self._ctx = None
+        self._create()
+
+    # ------------------------------------------------------------------ set-up
+    def _physics(self):
+        mu = self.mu
+        if mu is None:
+            model, mu0 = L.AFVM_MU_SUTHERLAND, 0.0
+        elif callable(mu):
+            raise NotImplementedError('mu must be None (Sutherland) or a constant')
+        else:
+            model, mu0 = L.AFVM_MU_CONSTANT, float(mu)
+        obj, objPatch = L.AFVM_OBJ_NONE, -1
+        if self.objective == 'kinetic_energy':
+            obj = L.AFVM_OBJ_KINETIC_ENERGY
+        elif self.objective == 'sum_T':
+            obj = L.AFVM_OBJ_SUM_T
+        elif self.objective.startswith('drag:'):
+            obj = L.AFVM_OBJ_DRAG
+            objPatch = self.mesh.sortedPatches.index(self.objective.split(':', 1)[1])
+        elif self.objective != 'none':
+            raise ValueError('unknown objective %r' % self.objective)
+        return L.Physics(self.gamma, self.Cp, self.Pr, model, mu0, SUTHERLAND[0], SUTHERLAND[1],
+                         _RIEMANN[self.riemannSolver], _RIEMANN[self.boundaryRiemannSolver], obj, objPatch)
+
+    def _bc_struct(self):
+        m = self.mesh
+        arr = (L.PatchBC * max(1, len(m.sortedPatches)))()
+        keep = []
+        for i, name in enumerate(m.sortedPatches):
+            kinds = {f: self.bc[f][name]['type'] for f in ('U', 'T', 'p')}
+            vals = {}
+            for f, dims in (('U', 3), ('T', 1), ('p', 1)):
+                b = self.bc[f][name]
+                if b['type'] == 'fixedValue':
+                    vals[f] = np.ascontiguousarray(b['value'], np.float64).reshape(-1, dims)
+                elif b['type'] == 'CBC_UPT':
+                    cb = self.bc['p'][name]       # characteristicBoundary uses p's BC (density.py:333-337)
+                    vals[f] = np.ascontiguousarray(cb[f + '0'], np.float64).reshape(-1, dims)
+            keep.append(vals)
+            ptr = lambda f: L.dptr(vals[f]) if f in vals else None
+            arr[i] = L.PatchBC(_BC[kinds['U']], _BC[kinds['T']], _BC[kinds['p']], ptr('U'), ptr('T'), ptr('p'))
+        return arr, keep
+
+    def _create(self):
+        mt, keep = self.mesh.tensorsStruct()
+        bcs, keep2 = self._bc_struct()
+        phys = self._physics()
+        ctx = C.c_void_p()
+        st = L.lib().afvm_ctx_create(C.byref(mt), bcs, C.byref(phys), self.precision, self.device, C.byref(ctx))
+        L.check(st, None, 'afvm_ctx_create')
+        self._ctx = ctx
+        self._bcvals = self.getBoundaryTensor(1)
+
+    def close(self):
+        if self._ctx is not None:
+            L.lib().afvm_ctx_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def device_bytes(self):
+        return int(L.lib().afvm_ctx_device_bytes(self._ctx))
+
+    # ------------------------------------------------------------------ reference call surface
+    def getBoundaryTensor(self, index=1):
+        """BC input values in the reference order (Solver.getBoundaryTensor, solver.py:91-92;
+        CellField.getTensor, field.py:141-146): per field U, T, p, per sorted patch, the
+        fixedValue 'value' or the CBC_UPT U0, T0, p0 arrays."""
+        out = []
+        for f, dims in (('U', 3), ('T', 1), ('p', 1)):
+            for name in self.mesh.sortedPatches:
+                b = self.bc[f][name]
+                if b['type'] == 'fixedValue':
+                    out.append(np.asarray(b['value']).reshape(-1, dims))
+                elif b['type'] == 'CBC_UPT':
+                    out.extend([np.asarray(b['U0']).reshape(-1, 3), np.asarray(b['T0']).reshape(-1, 1),
+                                np.asarray(b['p0']).reshape(-1, 1)])
+        return out
+
+    def _apply_bc_tensors(self, vals):
+        """Upload changed BC values (per-call inputs of the reference's map)."""
+        pos = 0
+        for fi, (f, dims) in enumerate((('U', 3), ('T', 1), ('p', 1))):
+            for pi, name in enumerate(self.mesh.sortedPatches):
+                b = self.bc[f][name]
+                if b['type'] == 'fixedValue':
+                    v = np.ascontiguousarray(vals[pos], np.float64)
+                    if not np.array_equal(v, self._bcvals[pos]):
+                        L.check(L.lib().afvm_set_bc_value(self._ctx, pi, fi, L.dptr(v)), self._ctx)
+                        self._bcvals[pos] = v.copy()
+                    pos += 1
+                elif b['type'] == 'CBC_UPT':
+                    if f == 'p':
+                        for k, (ff, d) in enumerate((('U', 3), ('T', 1), ('p', 1))):
+                            v = np.ascontiguousarray(vals[pos + k], np.float64)
+                            if not np.array_equal(v, self._bcvals[pos + k]):
+                                L.check(L.lib().afvm_set_bc_value(self._ctx, pi, k, L.dptr(v)), self._ctx)
+                                self._bcvals[pos + k] = v.copy()
+                    pos += 3
+        if pos != len(vals):
+            raise ValueError('expected %d boundary tensors, got %d' % (pos, len(vals)))
+
+    def map(self, *inputs, **options):
+        """The reference's primal step function (RCF.compileSolver, density.py:80-105):
+        inputs [rho, rhoU, rhoE, dt] + mesh.getTensor() + mesh.getScalar() + sources +
+        BC tensors; returns [rhoN, rhoUN, rhoEN, dtc, obj] (numpy)."""
+        m = self.mesh
+        nT, nS = len(Mesh.gradFields) + len(Mesh.intFields), len(m.getScalar())
+        base = 4 + nT + nS
+        if len(inputs) < base + 3:
+            raise ValueError('map: expected at least %d inputs, got %d' % (base + 3, len(inputs)))
+        rho, rhoU, rhoE, dt = inputs[:4]
+        scal = list(inputs[4 + nT:base])
+        if scal[:len(Mesh.constants)] != [getattr(m, a) for a in Mesh.constants]:
+            raise ValueError('map: mesh constants differ from the mesh this solver was built on')
+        S = inputs[base:base + 3]
+        self._apply_bc_tensors(list(inputs[base + 3:]))
+        n = m.nInternalCells
+        dt = float(np.asarray(dt).reshape(-1)[0])
+        ins = [np.ascontiguousarray(np.asarray(a).reshape(n, d), self.dtype) for a, d in zip((rho, rhoU, rhoE), (1, 3, 1))]
+        Ss = [np.ascontiguousarray(np.asarray(a).reshape(n, d), self.dtype) if a is not None else None
+              for a, d in zip(S, (1, 3, 1))]
+        if all(s is not None and not s.any() for s in Ss):
+            Ss = [None, None, None]
+        outs = [np.empty((n, d), self.dtype) for d in (1, 3, 1)]
+        dtc = C.c_double()
+        obj = C.c_double()
+        vp = lambda a: None if a is None else C.c_void_p(a.ctypes.data)
+        st = L.lib().afvm_primal_step_host(self._ctx, vp(ins[0]), vp(ins[1]), vp(ins[2]), dt,
+                                           vp(Ss[0]), vp(Ss[1]), vp(Ss[2]), vp(outs[0]), vp(outs[1]), vp(outs[2]),
+                                           C.byref(dtc), C.byref(obj), None)
+        L.check(st, self._ctx, 'afvm_primal_step_host')
+        return outs + [np.array([[dtc.value]]), np.array([[obj.value]])]
+
+    def mapInputs(self, rho, rhoU, rhoE, dt, sources=None):
+        """The positional input list the reference's time loop builds (solver.py:312-317)."""
+        m = self.mesh
+        n = m.nInternalCells
+        if sources is None:
+            sources = [np.zeros((n, 1)), np.zeros((n, 3)), np.zeros((n, 1))]
+        return ([rho, rhoU, rhoE, np.array([[dt]])] + m.getTensor() + m.getScalar() + list(sources) +
+                self.getBoundaryTensor(1))
+
+    def step_host(self, rho, rhoU, rhoE, dt, S=None, out=None):
+        """One step through the host-buffer entry point (afvm_primal_step_host): host arrays in
+        (pinned or pageable), host arrays out, copies inside. Returns (rhoN, rhoUN, rhoEN, dtc, obj)."""
+        n = self.mesh.nInternalCells
+        ins = [np.ascontiguousarray(a, self.dtype) for a in (rho, rhoU, rhoE)]
+        if out is None:
+            out = [np.empty((n, d), self.dtype) for d in (1, 3, 1)]
+        Ss = [None, None, None] if S is None else [np.ascontiguousarray(a, self.dtype) for a in S]
+        vp = lambda a: None if a is None else C.c_void_p(a.ctypes.data)
+        dtc = C.c_double()
+        obj = C.c_double()
+        st = L.lib().afvm_primal_step_host(self._ctx, vp(ins[0]), vp(ins[1]), vp(ins[2]), float(dt),
+                                           vp(Ss[0]), vp(Ss[1]), vp(Ss[2]), vp(out[0]), vp(out[1]), vp(out[2]),
+                                           C.byref(dtc), C.byref(obj), None)
+        L.check(st, self._ctx, 'afvm_primal_step_host')
+        return out[0], out[1], out[2], dtc.value, obj.value
+
+    # ------------------------------------------------------------------ per-kernel timing
+    def profile(self, on=True):
+        L.check(L.lib().afvm_profile(self._ctx, 1 if on else 0), self._ctx)
+
+    def profile_read(self):
+        """{kernel name: (milliseconds, launches)} since profile(True)."""
+        names = L.kernel_names()
+        ms = (C.c_double * len(names))()
+        cnt = (C.c_int64 * len(names))()
+        L.check(L.lib().afvm_profile_read(self._ctx, len(names), ms, cnt), self._ctx)
+        return {n: (ms[i], cnt[i]) for i, n in enumerate(names) if cnt[i]}
+
+    # ------------------------------------------------------------------ device path
+    def step(self, rho, rhoU, rhoE, dt, S=None, out=None, want_scalars=True):
+        """One step on CUDA tensors (reference layouts). Returns (rhoN, rhoUN, rhoEN, dtc, obj)."""
+        torch = _torch()
+        stream = torch.cuda.current_stream(rho.device).cuda_stream
+        if out is None:
+            out = (torch.empty_like(rho), torch.empty_like(rhoU), torch.empty_like(rhoE))
+        Sp = [None, None, None] if S is None else [C.c_void_p(s.data_ptr()) for s in S]
+        dtc = C.c_double()
+        obj = C.c_double()
+        st = L.lib().afvm_primal_step(self._ctx, C.c_void_p(rho.data_ptr()), C.c_void_p(rhoU.data_ptr()),
+                                      C.c_void_p(rhoE.data_ptr()), float(dt), Sp[0], Sp[1], Sp[2],
+                                      C.c_void_p(out[0].data_ptr()), C.c_void_p(out[1].data_ptr()),
+                                      C.c_void_p(out[2].data_ptr()),
+                                      C.byref(dtc) if want_scalars else None, C.byref(obj) if want_scalars else None,
+                                      C.c_void_p(stream))
+        L.check(st, self._ctx, 'afvm_primal_step')
+        return out[0], out[1], out[2], dtc.value, obj.value
+
+    def run_device(self, rho, rhoU, rhoE, nSteps, dt, S=None, record=True):
+        """nSteps steps in place on CUDA tensors, dt control on the device
+        (dt <- min(2*CFL/dtc, stepFactor*dt) unless fixedTimeStep). Returns device histories
+        (dt, dtc, obj) or None."""
+        torch = _torch()
+        stream = torch.cuda.current_stream(rho.device).cuda_stream
+        hist = torch.zeros((3, max(1, nSteps)), dtype=torch.float64, device=rho.device) if record else None
+        hp = [None, None, None] if hist is None else [C.cast(C.c_void_p(hist[k].data_ptr()), L._d) for k in range(3)]
+        Sp = [None, None, None] if S is None else [C.c_void_p(s.data_ptr()) for s in S]
+        st = L.lib().afvm_primal_run(self._ctx, C.c_void_p(rho.data_ptr()), C.c_void_p(rhoU.data_ptr()),
+                                     C.c_void_p(rhoE.data_ptr()), int(nSteps), float(dt), float(self.CFL),
+                                     float(self.stepFactor), 1 if self.fixedTimeStep else 0, Sp[0], Sp[1], Sp[2],
+                                     hp[0], hp[1], hp[2], C.c_void_p(stream))
+        L.check(st, self._ctx, 'afvm_primal_run')
+        return hist
+
+    # ------------------------------------------------------------------ time loop
+    def run(self, fields, nSteps, dt, endTime=np.inf, startTime=0.0, mode='simulation', source=None, avgStart=0):
+        """Solver.run (adFVM/solver.py:210-411) without IO. fields: conservative (rho, rhoU,
+        rhoE) numpy arrays. mode 'forward' returns every step's fields (and the record);
+        otherwise returns the time-summed objective (and the record)."""
+        t = startTime
+        timeIndex = 0
+        result = 0.0
+        sols = [list(fields)]
+        record = []
+        sources = None if source is None else [np.asarray(s) for s in source]
+        while t < endTime and timeIndex < nSteps:
+            inputs = self.mapInputs(*fields, dt, sources)
+            outputs = self.map(*inputs)
+            fields = outputs[:3]
+            dtc, objective = float(outputs[3][0, 0]), float(outputs[4][0, 0])
+            record.append((dt, dtc, objective))
+            timeIndex += 1
+            t = round(t + dt, 12)
+            if not self.fixedTimeStep:
+                dt = min(2 * self.CFL / dtc, dt * self.stepFactor, endTime - t)
+            if timeIndex > avgStart:
+                result += objective
+            if mode == 'forward':
+                sols.append(list(fields))
+        if mode == 'forward':
+            return sols, record
+        return result, record
+
+    def conservative(self, U, T, p):
+        """RCF.conservative (density.py:173-181) on host arrays, for initial conditions."""
+        e = self.Cv * T
+        rho = p / (e * (self.gamma - 1))
+        rhoE = rho * (e + 0.5 * np.sum(U * U, axis=1, keepdims=True))
+        rhoU = U * rho
+        return rho, rhoU, rhoE

@@ -1,0 +1,303 @@
+"""Benchmark of the GB300 finite-volume step (one JSON line on rank 0).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload box128|box64|...] [--precision fp64|fp32]
+
+A step is one SSP-RK3 time step (three residual evaluations) of the periodic jittered box
+(the throughput workload: 128^3 cells, Roe flux, Sutherland viscosity), state resident in
+HBM. ``value`` is whole-job Mcell-steps/s; ``e2e`` is the same metric through the host-buffer
+entry point (afvm_primal_step_host: pinned host state in, host state out, copies inside the
+timed region). Multi-GPU runs are independent replicas (one per rank, weak scaling).
+``--impl reference`` times the CPU oracle (the restated reference path) on the host cores.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'primal+adjoint Mcell-steps/s on 1 GB300 vs plain; sensitivity req/s, p99 @ tol'
+UNIT = 'Mcell-steps/s'
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            d = json.load(f)
+        return float(d['hbm_gbs']), 'measured'
+    except Exception:
+        return 6800.0, 'fallback'
+
+
+# algorithmic (compulsory) bytes per launch of each primal kernel, FP64 / FP32 element size
+# es and int32 indices; see DESIGN.md "Algorithmic bytes"
+def algorithmic_bytes(kernel, nIC, nIF, nF, nG, es):
+    REC, FREC = 20, 6
+    if kernel == 'k_flux':
+        # per face: own+nbr (8), normals 3, deltas 1, deltasUnit 3, linearWeights 2,
+        # quadraticWeights 6 -> 15 values, flux record write 6; cell records read once
+        return nF * (8 + 15 * es + FREC * es) + (nIC + nG) * REC * es
+    if kernel == 'k_grad':
+        # per cell: 6 slots x (nbr 4 + w' + S*N' (3)) + 1/V, primitives of every cell once,
+        # gradient write 15
+        return nIC * (6 * (4 + 4 * es) + es + 15 * es) + (nIC + nG) * 5 * es
+    if kernel == 'k_update':
+        # per cell: 6 x (face id 4 + weight), 2 stage states + source (5 each), write 5;
+        # face flux records read once
+        return nIC * (6 * (4 + es) + 3 * 5 * es + 5 * es) + nF * FREC * es
+    if kernel == 'k_prim':
+        return nIC * 10 * es + nG * (8 + 5 * es + 5 * es)
+    return 0
+
+
+class ClockSampler(object):
+    """nvidia-smi clock/throttle samples during the timed region."""
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+         'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+         'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.gpu), '--query-gpu=' + self.Q,
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(',')]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == 'active':
+                    reasons.add(nm)
+        return {'sm_mhz': statistics.median(sm) if sm else None,
+                'sm_max_mhz': max(smax) if smax else None,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+def make_case(workload):
+    from adfvm_gb300 import cases
+    if workload.startswith('box'):
+        return cases.box(int(workload[3:]), objective='kinetic_energy')
+    if workload.startswith('cylinder'):
+        a, b = workload[8:].split('x')
+        return cases.cylinder(int(a), int(b))
+    if workload.startswith('sod'):
+        return cases.sod(int(workload[3:]))
+    raise ValueError(workload)
+
+
+def describe(case, precision):
+    m = case.mesh
+    return {'workload': '%s: %d cells, %d faces (%d internal), Roe, SSP-RK3, %s, %s' % (
+        case.name, m.nInternalCells, m.nFaces, m.nInternalFaces,
+        'inviscid' if case.config.get('mu') == 0.0 else 'Sutherland viscosity', precision),
+        'cells': int(m.nInternalCells), 'faces': int(m.nFaces)}
+
+
+def cpu_baseline(args, threads):
+    """The oracle (restated reference path, torch CPU float64) on a bounded sample: one step
+    of a 32^3 box of the same recipe, on all host cores."""
+    import torch
+    from adfvm_gb300 import cases
+    from oracle import torch_ref
+    torch.set_num_threads(threads)
+    n = 32
+    case = cases.box(n, objective='kinetic_energy')
+    m = case.build_mesh()
+    prob = torch_ref.Problem(m, case.bc, case.config, case.objective)
+    rho, rhoU, rhoE = [torch.as_tensor(a) for a in cases.conservative(case)]
+    with torch.no_grad():
+        prob.step(rho, rhoU, rhoE, case.dt)       # warm-up
+        t0 = time.perf_counter()
+        steps = 0
+        while True:
+            rho, rhoU, rhoE, _, _ = prob.step(rho, rhoU, rhoE, case.dt)
+            steps += 1
+            if time.perf_counter() - t0 > 10 or steps >= 50:
+                break
+        dt = time.perf_counter() - t0
+    return {'value': m.nInternalCells * steps / dt / 1e6, 'unit': UNIT, 'cores': threads, 'kind': 'port',
+            'sample': '%d steps of the %d^3 box (%d cells) through the torch-CPU float64 oracle' % (
+                steps, n, m.nInternalCells)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    base = cpu_baseline(args, threads)
+    line = {'impl': 'reference', 'metric': METRIC, 'value': base['value'], 'unit': UNIT, 'n_gpus': args.gpus,
+            'steps': args.steps, 'warmup': args.warmup, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
+            'config': {'workload': 'periodic jittered box, Roe, SSP-RK3, Sutherland viscosity, FP64 (CPU sample)'},
+            'cpu_baseline': base,
+            'e2e': {'value': base['value'], 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours')
+    ap.add_argument('--workload', default='box128')
+    ap.add_argument('--precision', default='fp64')
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    args = ap.parse_args()
+    if args.impl == 'reference':
+        return run_reference(args)
+
+    import torch
+    rank = int(os.environ.get('RANK', '0'))
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl' if torch.cuda.is_available() else 'gloo')
+    torch.cuda.set_device(local)
+    from adfvm_gb300.solver import RCF
+
+    case = make_case(args.workload)
+    mesh = case.build_mesh()
+    rcf = RCF(mesh, case.bc, objective=case.objective, precision=args.precision, device=local, **case.config)
+    dt_np = np.float64 if args.precision == 'fp64' else np.float32
+    tdt = torch.float64 if args.precision == 'fp64' else torch.float32
+    from adfvm_gb300 import cases
+    rho0, rhoU0, rhoE0 = cases.conservative(case)
+    x = [torch.as_tensor(np.ascontiguousarray(a, dt_np)).cuda() for a in (rho0, rhoU0, rhoE0)]
+    y = [torch.empty_like(t) for t in x]
+    dt = case.dt
+    nIC, nIF, nF, nG = mesh.nInternalCells, mesh.nInternalFaces, mesh.nFaces, mesh.nGhostCells
+    es = 8 if args.precision == 'fp64' else 4
+
+    def one_step(a, b):
+        return rcf.step(a[0], a[1], a[2], dt, out=b, want_scalars=False)
+
+    for _ in range(args.warmup):
+        one_step(x, y)
+        x, y = y, x
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    rcf.profile(True)
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        one_step(x, y)
+        x, y = y, x
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    prof = rcf.profile_read()
+    rcf.profile(False)
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([ms], device='cuda')
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = nIC * args.steps * world / (ms / 1e3) / 1e6
+
+    # end to end through the host-buffer entry point (pinned host buffers)
+    pin = [torch.empty(tuple(t.shape), dtype=tdt, pin_memory=True).numpy() for t in x]
+    pout = [torch.empty(tuple(t.shape), dtype=tdt, pin_memory=True).numpy() for t in x]
+    for a, b in zip(pin, x):
+        a[...] = b.cpu().numpy()
+    rcf.step_host(pin[0], pin[1], pin[2], dt, out=pout)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    ke = max(1, args.steps // 2)
+    for _ in range(ke):
+        rcf.step_host(pin[0], pin[1], pin[2], dt, out=pout)
+        pin, pout = pout, pin
+    te = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([te], device='cuda')
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        te = float(t.item())
+    e2e = {'value': nIC * ke * world / te / 1e6, 'unit': UNIT,
+           'h2d_bytes_per_step': int(sum(a.nbytes for a in pin)),
+           'd2h_bytes_per_step': int(sum(a.nbytes for a in pout)) + 16,
+           'path': 'afvm_primal_step_host (pinned host state in/out, dtc and objective read back)'}
+
+    launches = sum(v[1] for v in prof.values())
+    kernels = {k: {'ms_total': round(v[0], 4), 'launches': v[1], 'ms_avg': round(v[0] / v[1], 5)}
+               for k, v in prof.items()}
+    top = max(prof.items(), key=lambda kv: kv[1][0])[0]
+    peak, peak_kind = peaks()
+    alg = algorithmic_bytes(top, nIC, nIF, nF, nG, es)
+    avg_s = prof[top][0] / prof[top][1] / 1e3
+    achieved = alg / avg_s / 1e9
+    roofline = {'bound': 'hbm', 'kernel': top, 'achieved': round(achieved, 1), 'peak': peak,
+                'peak_source': peak_kind, 'unit': 'GB/s', 'frac': round(achieved / peak, 4),
+                'algorithmic_bytes_per_launch': int(alg), 'traffic': None}
+    line = {'metric': METRIC, 'value': round(value, 3), 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': round(ms / args.steps, 4), 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64' if args.precision == 'fp64' else 'f32',
+            'data': 'synthetic', 'config': dict(describe(case, args.precision),
+                                                 l2='inputs larger than L2: %.2f GB device working set' % (
+                                                     rcf.device_bytes / 1e9),
+                                                 parallelism='replicas' if world > 1 else 'single GPU',
+                                                 step='primal SSP-RK3 step (adjoint not in this number)'),
+            'roofline': roofline, 'kernels': kernels, 'gpu_launches': int(launches), 'e2e': e2e,
+            'clocks': clk}
+    from adfvm_gb300 import _lib
+    line['fma_peak_tflops'] = {'fp64': round(_lib.fma_peak(local, True), 2), 'fp32': round(_lib.fma_peak(local, False), 2)}
+    if rank == 0 and not args.no_cpu_baseline:
+        line['cpu_baseline'] = cpu_baseline(args, os.cpu_count() or 1)
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == '__main__':
+    sys.exit(main())

@@ -1,0 +1,236 @@
+/*
+ * afvm.h - C ABI of the GB300 compressible finite-volume residual and its discrete adjoint.
+ *
+ * Plain pointers and sizes only. Every call returns an AFVM_* status code and never aborts
+ * the process; afvm_last_error() gives the message of the last failing call on a context.
+ *
+ * The entry points replace, for one GPU, the compiled functions that the reference solver
+ * builds and calls inside its time loops:
+ *   afvm_mesh_build       <- cmesh.build / cmesh.buildBeforeWrite  (adFVM/cpp/cmesh.cpp:3-270,
+ *                            ghost cells adFVM/mesh.py:758-819)
+ *   afvm_ctx_create       <- Function.initialize -> external_init   (adFVM/solver.py:61-71,
+ *                            adFVM/cpp/external.cpp:21-42)
+ *   afvm_ctx_destroy      <- external_exit                          (adFVM/cpp/external.cpp:44-51)
+ *   afvm_primal_step      <- RCF.map(*inputs)                       (adFVM/solver.py:312-323,
+ *                            graph built at adFVM/density.py:80-105)
+ *   afvm_adjoint_step     <- Adjoint.map(*inputs)                   (apps/adjoint.py:268-291,
+ *                            graph built at apps/adjoint.py:94-151)
+ *   afvm_sensitivity      <- cmesh.computeSensitivity               (adFVM/cpp/cmesh.cpp:309-340)
+ */
+#ifndef AFVM_H
+#define AFVM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define AFVM_OK              0
+#define AFVM_ERR_BAD_ARG     1   /* invalid size, pointer, index or option               */
+#define AFVM_ERR_OOM         2   /* device allocation failed                              */
+#define AFVM_ERR_NONFINITE   3   /* a NaN/Inf appeared in a result (reference: MPI.Abort) */
+#define AFVM_ERR_TIMEOUT     4   /* a bounded device-side wait gave up                    */
+#define AFVM_ERR_CUDA        5   /* a CUDA runtime call failed                            */
+#define AFVM_ERR_UNSUPPORTED 6   /* valid input outside what this build implements        */
+
+/* ---- precision of a context ---- */
+#define AFVM_FP64 0              /* all arithmetic and storage in double                  */
+#define AFVM_FP32 1              /* float storage/flux/gradient; double for the pressure
+                                    recovery, the objective and the sensitivity sums       */
+
+/* ---- mesh patch kinds (the 'type' entry of a polyMesh boundary patch) ---- */
+#define AFVM_PATCH_PLAIN     0   /* patch / wall / empty / symmetryPlane                  */
+#define AFVM_PATCH_CYCLIC    1   /* cyclic pair; neighbourPatch names the partner         */
+#define AFVM_PATCH_PROCESSOR 2   /* processor halo: not supported on one GPU              */
+
+typedef struct afvm_patch {
+    int32_t startFace;
+    int32_t nFaces;
+    int32_t kind;            /* AFVM_PATCH_* */
+    int32_t neighbourPatch;  /* index of the cyclic partner in the same table, else -1 */
+} afvm_patch;
+
+/* ---- mesh build (host) ---- */
+typedef struct afvm_mesh_in {
+    int32_t nPoints;
+    const double* points;        /* nPoints x 3 */
+    int32_t nFaces;
+    const int32_t* faces;        /* nFaces x 5: count (4) + point ids */
+    int32_t nInternalFaces;
+    const int32_t* owner;        /* nFaces */
+    const int32_t* neighbour;    /* nInternalFaces */
+    int32_t nInternalCells;
+    int32_t nPatches;
+    const afvm_patch* patches;   /* any order; used for ghost cells */
+} afvm_mesh_in;
+
+typedef struct afvm_mesh_out {   /* all buffers caller-allocated */
+    double* normals;             /* nFaces x 3 */
+    double* faceCentres;         /* nFaces x 3 */
+    double* areas;               /* nFaces */
+    double* cellCentres;         /* nCells x 3 (ghost rows included) */
+    double* volumes;             /* nInternalCells */
+    int32_t* neighbour;          /* nFaces (ghost cell ids appended for boundary faces) */
+    double* deltas;              /* nFaces */
+    double* deltasUnit;          /* nFaces x 3 */
+    double* weights;             /* nFaces */
+    double* linearWeights;       /* nFaces x 2 */
+    double* quadraticWeights;    /* nFaces x 2 x 3 */
+    int32_t* cellFaces;          /* nInternalCells x 6 */
+    int32_t* cellOwner;          /* nInternalCells x 6 */
+    int32_t* cellNeighbours;     /* nInternalCells x 6 (ghost ids included) */
+    int32_t* cellNeighboursMatOp;/* nInternalCells x 6 (-1 for boundary), may be NULL */
+    int32_t nLocalCells;         /* written */
+} afvm_mesh_out;
+
+/* Geometry and connectivity of a hex mesh (host, OpenMP). Replaces cmesh.build /
+ * cmesh.buildBeforeWrite (adFVM/cpp/cmesh.cpp:3-270) and Mesh.createGhostCells for one
+ * rank (adFVM/mesh.py:758-819). */
+int afvm_mesh_build(const afvm_mesh_in* in, afvm_mesh_out* out);
+
+/* ---- solver context ---- */
+
+/* The mesh tensors in the order of Mesh.getTensor() (adFVM/mesh.py:27-32, 870-872) and
+ * the constants of Mesh.getScalar() (adFVM/mesh.py:36-37, 874-881). Host pointers; they are
+ * copied to the device once, at context creation. */
+typedef struct afvm_mesh_tensors {
+    const double* areas;            /* nFaces */
+    const double* volumesL;         /* nFaces */
+    const double* volumesR;         /* nInternalFaces */
+    const double* weights;          /* nFaces */
+    const double* deltas;           /* nFaces */
+    const double* normals;          /* nFaces x 3 */
+    const double* deltasUnit;       /* nFaces x 3 */
+    const double* linearWeights;    /* nFaces x 2 */
+    const double* quadraticWeights; /* nFaces x 2 x 3 */
+    const double* volumes;          /* nInternalCells */
+    const int32_t* owner;           /* nFaces */
+    const int32_t* neighbour;       /* nFaces */
+    const int32_t* cellFaces;       /* nInternalCells x 6 */
+    const int32_t* cellNeighbours;  /* nInternalCells x 6 */
+    const int32_t* cellOwner;       /* nInternalCells x 6 */
+    int32_t nCells, nFaces, nInternalCells, nInternalFaces;
+    int32_t nLocalCells, nRemoteCells, nLocalFaces, nGhostCells;
+    int32_t nPatches;               /* patches in sortedPatches order (alphabetical) */
+    const afvm_patch* patches;      /* kind/neighbourPatch index into this same table */
+} afvm_mesh_tensors;
+
+/* boundary conditions of one field on one patch (adFVM/BCs.py) */
+#define AFVM_BC_ZERO_GRADIENT  0     /* zeroGradient, empty, inletOutlet  (BCs.py:97-104, 136-137) */
+#define AFVM_BC_FIXED_VALUE    1     /* fixedValue                        (BCs.py:111-118)         */
+#define AFVM_BC_SYMMETRY_PLANE 2     /* symmetryPlane, slip               (BCs.py:120-135)         */
+#define AFVM_BC_CYCLIC         3     /* cyclic                            (BCs.py:86-95)           */
+#define AFVM_BC_CBC_UPT        4     /* characteristic U,T,p              (BCs.py:152-161)         */
+
+typedef struct afvm_patch_bc {
+    int32_t U, T, p;                 /* AFVM_BC_* per field; CBC_UPT must be set on all three */
+    const double* U_value;           /* nFaces x 3 for fixedValue U, or U0 for CBC_UPT */
+    const double* T_value;           /* nFaces     for fixedValue T, or T0 for CBC_UPT */
+    const double* p_value;           /* nFaces     for fixedValue p, or p0 for CBC_UPT */
+} afvm_patch_bc;
+
+#define AFVM_RIEMANN_ROE 0           /* riemann.eulerRoe            (adFVM/riemann.py:21-70) */
+#define AFVM_RIEMANN_LF  1           /* riemann.eulerLaxFriedrichs  (adFVM/riemann.py:6-18)  */
+
+#define AFVM_MU_CONSTANT   0         /* mu(T) = mu0                                          */
+#define AFVM_MU_SUTHERLAND 1         /* mu(T) = As*T**1.5/(T+Ts) (adFVM/density.py:27)       */
+
+#define AFVM_OBJ_NONE           0    /* obj = 0 (adFVM/density.py:356-357)                    */
+#define AFVM_OBJ_KINETIC_ENERGY 1    /* sum_c 0.5*rho*|U|^2*V over internal cells            */
+#define AFVM_OBJ_DRAG           2    /* wall drag of templates/cylinder_test.py:9-37          */
+#define AFVM_OBJ_SUM_T          3    /* sum_c T (templates/box.py:10-16)                      */
+
+typedef struct afvm_physics {
+    double gamma, Cp, Pr;            /* defaults 1.4, 1004.5, 0.7 (adFVM/density.py:22-39) */
+    int32_t mu_model;                /* AFVM_MU_* */
+    double mu0;                      /* constant viscosity */
+    double mu_As, mu_Ts;             /* Sutherland constants (1.4792e-06, 116.) */
+    int32_t riemann;                 /* AFVM_RIEMANN_* for internal and coupled faces */
+    int32_t boundary_riemann;        /* AFVM_RIEMANN_* for characteristic patches */
+    int32_t objective;               /* AFVM_OBJ_* evaluated on the stage-1 primitives */
+    int32_t objective_patch;         /* patch index (sorted order) for AFVM_OBJ_DRAG */
+} afvm_physics;
+
+typedef struct afvm_ctx afvm_ctx;
+
+/* Upload the mesh, boundary conditions and physics; allocate all device work buffers.
+ * bcs has mesh->nPatches entries in sortedPatches order. device is a CUDA ordinal. */
+int afvm_ctx_create(const afvm_mesh_tensors* mesh, const afvm_patch_bc* bcs,
+                    const afvm_physics* physics, int32_t precision, int32_t device,
+                    afvm_ctx** out);
+int afvm_ctx_destroy(afvm_ctx* ctx);
+const char* afvm_last_error(const afvm_ctx* ctx);
+int afvm_ctx_precision(const afvm_ctx* ctx);
+/* Device bytes held by the context (mesh + work buffers). */
+int64_t afvm_ctx_device_bytes(const afvm_ctx* ctx);
+
+/* Replace the values of a fixedValue / CBC_UPT boundary input (host pointer, nFaces x dims)
+ * - the per-call BC tensors of Solver.getBoundaryTensor (adFVM/solver.py:91-92). field: 0=U,
+ * 1=T, 2=p. */
+int afvm_set_bc_value(afvm_ctx* ctx, int32_t patch, int32_t field, const double* values);
+
+/* One SSP-RK3 time step (adFVM/timestep.py:27-55 over RCF.equation, density.py:339-414).
+ * State arrays are DEVICE pointers in the reference layout: rho (nInternalCells),
+ * rhoU (nInternalCells x 3), rhoE (nInternalCells); element type double for AFVM_FP64 and
+ * float for AFVM_FP32. Sources may be NULL (zero). Outputs may alias the inputs.
+ * dtc_out / obj_out (host, may be NULL) receive the stage-1 max CFL sum and objective; a
+ * non-NULL one makes the call wait for the step to finish. */
+int afvm_primal_step(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE,
+                     double dt, const void* S_rho, const void* S_rhoU, const void* S_rhoE,
+                     void* rhoN, void* rhoUN, void* rhoEN,
+                     double* dtc_out, double* obj_out, void* stream);
+
+/* Same step with HOST buffers (pinned or pageable): copies in, steps, copies out. */
+int afvm_primal_step_host(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE,
+                          double dt, const void* S_rho, const void* S_rhoU, const void* S_rhoE,
+                          void* rhoN, void* rhoUN, void* rhoEN,
+                          double* dtc_out, double* obj_out, void* stream);
+
+/* nSteps steps resident on the device with the reference's time-step rule
+ * dt <- min(2*CFL/dtc, stepFactor*dt, endTime - t) (adFVM/solver.py:365) unless
+ * fixed_dt != 0. dt_hist/dtc_hist/obj_hist are DEVICE double arrays of nSteps (may be NULL).
+ * The state is advanced in place. No host synchronisation inside. */
+int afvm_primal_run(afvm_ctx* ctx, void* rho, void* rhoU, void* rhoE, int32_t nSteps,
+                    double dt0, double CFL, double stepFactor, int32_t fixed_dt,
+                    const void* S_rho, const void* S_rhoU, const void* S_rhoE,
+                    double* dt_hist, double* dtc_hist, double* obj_hist, void* stream);
+
+/* Vector-Jacobian product of one primal step with dt held fixed - the per-step call of the
+ * adjoint sweep (apps/adjoint.py:268-291). Inputs: the step's input state (device), dt,
+ * sources, the adjoint seeds of the step's outputs (rhoNa, rhoUNa, rhoENa; device) and of
+ * its scalar outputs (dtca, obja). Outputs: the adjoint of the input state and, if non-NULL,
+ * of the three source arrays. Only dtca == 0 is supported (the reference driver always
+ * passes 0, apps/adjoint.py:268). Adjoint outputs may alias the adjoint inputs. */
+int afvm_adjoint_step(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE,
+                      double dt, const void* S_rho, const void* S_rhoU, const void* S_rhoE,
+                      const void* rhoNa, const void* rhoUNa, const void* rhoENa,
+                      double dtca, double obja,
+                      void* rhoa, void* rhoUa, void* rhoEa,
+                      void* S_rhoa, void* S_rhoUa, void* S_rhoEa, void* stream);
+
+/* FP64 sum over k of dot(grad[k], pert[k]) (adFVM/cpp/cmesh.cpp:309-340). DEVICE arrays of
+ * n[k] doubles; result to *out (host) after the stream work completes. */
+int afvm_sensitivity(afvm_ctx* ctx, int32_t nArrays, const double* const* grad,
+                     const double* const* pert, const int64_t* n, double* out, void* stream);
+
+/* ---- per-launch timing (the analogue of the reference's timeFunction decorator and
+ * per-step timers, adFVM/config.py:158-168, adFVM/solver.py:322-346) ----
+ * afvm_profile(ctx, 1) clears the record and brackets every later kernel launch of the
+ * context with a CUDA event pair on the launching stream; afvm_profile_read sums the
+ * elapsed milliseconds and launch counts per kernel id (maxKernels >= the number of ids;
+ * afvm_profile_kernel_name gives an id's name, NULL past the last one). */
+int afvm_profile(afvm_ctx* ctx, int32_t on);
+int afvm_profile_read(afvm_ctx* ctx, int32_t maxKernels, double* ms, int64_t* launches);
+const char* afvm_profile_kernel_name(int32_t id);
+
+/* Measured fused-multiply-add throughput of a device in TFLOP/s (fp64 != 0: double,
+ * else float): the compute ceiling that the FP64 residual kernels meet before the HBM one.
+ * No counterpart in the reference (a measurement aid for the roofline). */
+int afvm_fma_peak(int32_t device, int32_t fp64, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AFVM_H */

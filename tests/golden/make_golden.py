@@ -1,0 +1,175 @@
+"""Generate the golden trajectories in tests/golden/*.npz from the REFERENCE solver itself.
+
+Runs the reference's own RCF residual, SSP-RK3 stepper and time loop (adFVM/density.py,
+interp.py, riemann.py, op.py, timestep.py, BCs.py, solver.py) and its own mesh builder
+(adFVM/cpp/cmesh.cpp, compiled by oracle/build.py), through the adpy/mpi4py stand-ins of
+oracle/refshim, on meshes from adfvm_gb300.meshgen. Needs the reference checkout, so it runs
+in the development container only; the .npz files it writes are committed.
+
+    python tests/golden/make_golden.py            # all cases
+    python tests/golden/make_golden.py sod1000    # one case
+"""
+import hashlib
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from adfvm_gb300 import cases  # noqa: E402
+from oracle import refrun  # noqa: E402
+
+
+def mesh_digest(md):
+    h = hashlib.sha256()
+    for a in md[:4]:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def objective_fn(kind, rcf_cfg):
+    """Objectives written in the adpy style of the reference's case files."""
+    from adpy.tensor import Kernel, Zeros, ExternalFunctionOp
+    if kind == 'none':
+        return None
+    if kind == 'kinetic_energy':
+        def objective(fields, solver):
+            U, T, p = fields
+            mesh = solver.mesh.symMesh
+
+            def _ke(U, T, p, volumes):
+                rho = p / ((solver.Cv * T) * (solver.gamma - 1))
+                return (0.5 * rho * U.magSqr() * volumes).sum()
+            return Kernel(_ke)(mesh.nInternalCells)(U, T, p, mesh.volumes)
+        return objective
+    if kind == 'sum_T':
+        def objective(fields, solver):
+            U, T, p = fields
+            mesh = solver.mesh.symMesh
+            return Kernel(lambda T: (T * 1).sum())(mesh.nInternalCells)(T)
+        return objective
+    if kind.startswith('drag:'):
+        patch_name = kind.split(':', 1)[1]
+
+        # templates/cylinder_test.py:9-37
+        def objectiveDrag(U, T, p, *mesh, **options):
+            from adFVM.mesh import Mesh
+            solver = options['solver']
+            mesh = Mesh.container(mesh)
+            U0 = U.extract(mesh.neighbour)[0]
+            U0i = U.extract(mesh.owner)[0]
+            p0 = p.extract(mesh.neighbour)
+            T0 = T.extract(mesh.neighbour)
+            nx = mesh.normals[0]
+            mungUx = solver.mu(T0) * (U0 - U0i) / mesh.deltas
+            drag = (p0 * nx - mungUx) * mesh.areas
+            return drag.sum()
+
+        def objective(fields, solver):
+            U, T, p = fields
+            mesh = solver.mesh.symMesh
+            patch = mesh.boundary[patch_name]
+            startFace, nFaces = patch['startFace'], patch['nFaces']
+            meshArgs = [x[startFace] for x in mesh.getTensor()]
+            drag = Zeros((1, 1))
+            drag = Kernel(objectiveDrag)(nFaces, (drag,))(U, T, p, *meshArgs, solver=solver)
+            (drag,) = ExternalFunctionOp('mpi_allreduce', (drag,), (drag,)).outputs
+            return drag
+        return objective
+    raise ValueError(kind)
+
+
+def reference_config(case):
+    cfg = dict(case.config)
+    if 'mu' in cfg and not callable(cfg['mu']):
+        v = float(cfg['mu'])
+        cfg['mu'] = lambda T, v=v: v
+    obj = objective_fn(case.objective, cfg)
+    if obj is not None:
+        cfg['objective'] = obj
+    return cfg
+
+
+def run_case(case, nSteps, keep_steps, with_source=False):
+    refrun.load()
+    md = case.meshData
+    with tempfile.TemporaryDirectory() as d:
+        rcf, cons = refrun.make_rcf(md, d, case.bc, case.U, case.T, case.p, **reference_config(case))
+        src = None
+        if with_source:
+            S = cases.source_field(case.build_mesh())
+            src = lambda fields, mesh, t: [x.copy() for x in S]
+        sols, record = refrun.run_forward(rcf, nSteps, case.dt, source=src)
+    out = {
+        'mesh_digest': np.array(mesh_digest(md)),
+        'nSteps': np.array(nSteps),
+        'dt0': np.array(case.dt),
+        'with_source': np.array(with_source),
+        'record': np.array(record),   # per step: dt, dtc (stage-1 max), obj (stage-1)
+        'steps': np.array(keep_steps),
+        'U0': case.U, 'T0': case.T, 'p0': case.p,
+    }
+    for k, name in enumerate(['rho', 'rhoU', 'rhoE']):
+        out[name + '_init'] = np.asarray(cons[k].field)
+        for s in keep_steps:
+            out['%s_%d' % (name, s)] = np.asarray(sols[s][k].field)
+    return out
+
+
+CASES = {
+    'sod1000': lambda: (cases.sod(1000), 200, [1, 2, 10, 50, 100, 200], False),
+    'sod200_sym_lf': lambda: (cases.sod(200, side='symmetryPlane', riemann='eulerLaxFriedrichs'), 60, [1, 20, 60], False),
+    'box8': lambda: (cases.box(8, objective='kinetic_energy'), 5, [1, 2, 5], True),
+    'box6_inviscid_sumT': lambda: (cases.box(6, objective='sum_T', viscous=False), 3, [1, 3], False),
+    'cyl32x16': lambda: (cases.cylinder(32, 16, objective='drag:cylinder'), 5, [1, 2, 5], False),
+}
+
+
+GEOMETRY_FIELDS = ['normals', 'faceCentres', 'areas', 'cellCentres', 'volumes', 'neighbour', 'deltas',
+                   'deltasUnit', 'weights', 'linearWeights', 'quadraticWeights', 'cellFaces', 'cellOwner',
+                   'cellNeighbours', 'volumesL', 'volumesR']
+GEOMETRY_MESHES = {
+    'sod50': lambda: cases.meshgen.sod_tube(50),
+    'box6': lambda: cases.meshgen.periodic_box(6),
+    'cyl16x8': lambda: cases.meshgen.cylinder_ogrid(16, 8),
+}
+
+
+def make_geometry():
+    """Mesh arrays from the reference's own Mesh.build (adFVM/mesh.py:84-127): its compiled
+    cmesh.cpp and its createGhostCells."""
+    refrun.load()
+    out = {}
+    for name, fn in GEOMETRY_MESHES.items():
+        md = fn()
+        with tempfile.TemporaryDirectory() as d:
+            m = refrun.build_mesh(md, d)
+        out[name + '/digest'] = np.array(mesh_digest(md))
+        out[name + '/sortedPatches'] = np.array(m.sortedPatches)
+        for a in GEOMETRY_FIELDS + ['nLocalCells', 'nCells', 'nGhostCells', 'nLocalFaces', 'nRemoteCells']:
+            out[name + '/' + a] = np.asarray(getattr(m, a))
+    path = os.path.join(HERE, 'geometry.npz')
+    np.savez_compressed(path, **out)
+    print('geometry ->', path, os.path.getsize(path), 'bytes')
+
+
+def main(names):
+    for name in names:
+        if name == 'geometry':
+            make_geometry()
+            continue
+        case, nSteps, keep, src = CASES[name]()
+        out = run_case(case, nSteps, keep, src)
+        path = os.path.join(HERE, name + '.npz')
+        np.savez_compressed(path, **out)
+        rec = out['record']
+        print('%s: %d steps, final dt %.6e dtc %.6e obj %.6e -> %s (%d bytes)' % (
+            name, nSteps, rec[-1, 0], rec[-1, 1], rec[-1, 2], path, os.path.getsize(path)))
+
+
+if __name__ == '__main__':
+    main(sys.argv[1:] or (['geometry'] + list(CASES)))
