@@ -1,0 +1,463 @@
+// The flux through one face and its hand-derived vector-Jacobian product.
+//
+// face_flux evaluates RCF.flux / RCF.boundaryFlux (adFVM/density.py:253-331) for one face;
+// face_vjp returns the gradient of <Fbar, F> with respect to every input of the face (the
+// primitives and gradients of the two adjacent cells). The reference differentiates the
+// same arithmetic with adpy's reverse mode (apps/adjoint.py:101); here each forward
+// expression is differentiated by hand, in reverse order. At the kinks of |x| the derivative
+// taken is sign(x) with sign(0) = 0; at max(a, b) with a == b the whole derivative goes to a.
+#pragma once
+#include "physics.cuh"
+
+namespace afvm {
+
+template <typename R>
+struct FaceIn {
+    R UP[3], TP, pP, UN[3], TN, pN;                    // owner cell and neighbour (or ghost) primitives
+    R gUP[9], gTP[3], gpP[3], gUN[9], gTN[3], gpN[3];  // gradients ([component][direction])
+    R N[3], D[3], lw0, lw1, qw0[3], qw1[3], delta;     // normals, deltasUnit, weights, deltas
+};
+
+template <typename R>
+struct FaceBar {
+    R UP[3], TP, pP, UN[3], TN, pN;
+    R gUP[9], gTP[3], gpP[3], gUN[9], gTN[3], gpN[3];
+};
+
+template <typename R>
+AFVM_HD void zero_bar(FaceBar<R>& b) {
+    R* p = &b.UP[0];
+    for (int k = 0; k < 40; k++) p[k] = R(0);
+}
+
+template <typename R>
+AFVM_HD R sgn(R x) { return (x > R(0)) ? R(1) : ((x < R(0)) ? R(-1) : R(0)); }
+
+// flux (rho, rhoU, rhoE) through the face and the CFL term |U.n| + a
+template <typename R>
+AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& in, R* F, R& maxaF) {
+    R TF, UF[3], gTF[3], gUF[9];
+    if (kind == FACE_BOUNDARY) {
+        // RCF.boundaryFlux (density.py:307-331) with RCF.getFlux (density.py:184-190)
+        R rho, rhoU[3], rhoE;
+        conservative<R>(P, in.UN, in.TN, in.pN, rho, rhoU, rhoE);
+        R Un = dot3(in.UN, in.N);
+        F[0] = rho * Un;
+        for (int k = 0; k < 3; k++) F[1 + k] = rhoU[k] * Un + in.pN * in.N[k];
+        F[4] = (rhoE + in.pN) * Un;
+        TF = in.TN;
+        for (int k = 0; k < 3; k++) { UF[k] = in.UN[k]; gTF[k] = in.gTN[k]; }
+        for (int k = 0; k < 9; k++) gUF[k] = in.gUN[k];
+    } else {
+        R ULF[3], TLF, pLF, URF[3], TRF, pRF;
+        for (int k = 0; k < 3; k++) ULF[k] = recon<R>(in.UP[k], in.UN[k], in.gUP + 3 * k, in.lw0, in.qw0);
+        TLF = recon<R>(in.TP, in.TN, in.gTP, in.lw0, in.qw0);
+        pLF = recon<R>(in.pP, in.pN, in.gpP, in.lw0, in.qw0);
+        R rhoL, rhoUL[3], rhoEL;
+        conservative<R>(P, ULF, TLF, pLF, rhoL, rhoUL, rhoEL);
+        int solver;
+        if (kind == FACE_CHARACTERISTIC) {
+            for (int k = 0; k < 3; k++) URF[k] = in.UN[k];
+            TRF = in.TN; pRF = in.pN;
+            solver = P.briemann;
+        } else {
+            for (int k = 0; k < 3; k++) URF[k] = recon<R>(in.UN[k], in.UP[k], in.gUN + 3 * k, in.lw1, in.qw1);
+            TRF = recon<R>(in.TN, in.TP, in.gTN, in.lw1, in.qw1);
+            pRF = recon<R>(in.pN, in.pP, in.gpN, in.lw1, in.qw1);
+            solver = P.riemann;
+        }
+        R rhoR, rhoUR[3], rhoER;
+        conservative<R>(P, URF, TRF, pRF, rhoR, rhoUR, rhoER);
+        if (solver == AFVM_RIEMANN_ROE)
+            roe<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, in.N, F);
+        else
+            laxf<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, rhoUL, rhoUR, rhoEL, rhoER, in.N, F);
+        if (kind == FACE_CHARACTERISTIC) {
+            TF = in.TN;
+            for (int k = 0; k < 3; k++) { UF[k] = in.UN[k]; gTF[k] = in.gTN[k]; }
+            for (int k = 0; k < 9; k++) gUF[k] = in.gUN[k];
+        } else {
+            TF = R(0.5) * (TLF + TRF);
+            for (int k = 0; k < 3; k++) { UF[k] = R(0.5) * (ULF[k] + URF[k]); gTF[k] = R(0.5) * (in.gTP[k] + in.gTN[k]); }
+            for (int k = 0; k < 9; k++) gUF[k] = R(0.5) * (in.gUP[k] + in.gUN[k]);
+        }
+    }
+    if (!inviscid) viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, UF, gTF, gUF, in.D, in.N, in.delta, F);
+    R aF = sqrt(R(P.Cp) * TF * R(P.gm1));
+    maxaF = fabs(dot3(UF, in.N)) + aF;
+}
+
+// ---------------------------------------------------------------------------- adjoints
+
+// RCF.conservative: rho = p/(Cv T (g-1)), rhoU = U rho, rhoE = rho (Cv T + |U|^2/2)
+template <typename R>
+AFVM_HD void conservative_vjp(const Phys& P, const R* U, R T, R p, R rhob, const R* rhoUb, R rhoEb, R* Ub,
+                              R& Tb, R& pb) {
+    R e = R(P.Cv) * T;
+    R d = e * R(P.gm1);
+    R rho = p / d;
+    R q = dot3(U, U);
+    for (int k = 0; k < 3; k++) Ub[k] += rhoUb[k] * rho + rhoEb * rho * U[k];
+    R rhot = rhob + dot3(rhoUb, U) + rhoEb * (e + R(0.5) * q);
+    pb += rhot / d;
+    R eb = -rhot * rho / e + rhoEb * rho;
+    Tb += eb * R(P.Cv);
+}
+
+// interp.secondOrder: phiC + (phiD - phiC) lw + qw.g
+template <typename R>
+AFVM_HD void recon_vjp(R b, R lw, const R* qw, R& phiCb, R& phiDb, R* gb) {
+    phiCb += b * (R(1) - lw);
+    phiDb += b * lw;
+    for (int j = 0; j < 3; j++) gb[j] += b * qw[j];
+}
+
+// riemann.eulerRoe
+template <typename R>
+AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR, const R* N, const R* Fb,
+                     R& pLb, R& pRb, R* ULb, R* URb, R& rhoLb, R& rhoRb) {
+    const R g = R(P.gamma), gm1 = R(P.gm1), h = R(0.5);
+    // ---- forward
+    R UnL = dot3(UL, N), UnR = dot3(UR, N);
+    R rhoUnL = rhoL * UnL, rhoUnR = rhoR * UnR;
+    R qL = dot3(UL, UL), qR = dot3(UR, UR);
+    R hL = g * pL / (gm1 * rhoL) + h * qL;
+    R hR = g * pR / (gm1 * rhoR) + h * qR;
+    R sL = sqrt(rhoL), sR = sqrt(rhoR);
+    R Dn = sL + sR;
+    R UF[3], dU[3];
+    for (int k = 0; k < 3; k++) UF[k] = (UL[k] * sL + UR[k] * sR) / Dn;
+    R hF = (hL * sL + hR * sR) / Dn;
+    R qF = h * dot3(UF, UF);
+    R a2F = gm1 * (hF - qF);
+    R aF = sqrt(a2F);
+    R UnF = dot3(UF, N);
+    R drho = rhoR - rhoL;
+    for (int k = 0; k < 3; k++) dU[k] = rhoR * UR[k] - rhoL * UL[k];
+    R drhoE = (hR * rhoR - pR) - (hL * rhoL - pL);
+    R l1 = fabs(UnF), l2 = fabs(UnF + aF), l3 = fabs(UnF - aF);
+    R ea = rhoUnL / rhoL - rhoUnR / rhoR;
+    R cL = sqrt(g * pL / rhoL), cR = sqrt(g * pR / rhoR);
+    R eb_ = cL - cR;
+    R eps = h * fabs(ea);
+    eps = eps + h * fabs(eb_);
+    eps = (eps < R(0)) ? eps - R(P.small) : eps + R(P.small);
+    bool s1 = l1 < R(2) * eps, s2 = l2 < R(2) * eps, s3 = l3 < R(2) * eps;
+    R L1 = s1 ? R(0.25) * l1 * l1 / eps + eps : l1;
+    R L2 = s2 ? R(0.25) * l2 * l2 / eps + eps : l2;
+    R L3 = s3 ? R(0.25) * l3 * l3 / eps + eps : l3;
+    R abv1 = h * (L2 + L3);
+    R abv2 = h * (L2 - L3);
+    R abv3 = abv1 - L1;
+    R abv4 = gm1 * (qF * drho - dot3(UF, dU) + drhoE);
+    R abv5 = UnF * drho - dot3(dU, N);
+    R abv6 = abv3 * abv4 / a2F - abv2 * abv5 / aF;
+    R abv7 = abv3 * abv5 - abv2 * abv4 / aF;
+    // ---- reverse
+    R Fu[3] = {Fb[1], Fb[2], Fb[3]};
+    R frb = Fb[0], feb = Fb[4];
+    R L1b = -h * (Fb[0] * drho + dot3(Fu, dU) + Fb[4] * drhoE);
+    R drhob = -h * Fb[0] * L1;
+    R dUb[3], UFb[3];
+    for (int k = 0; k < 3; k++) { dUb[k] = -h * Fu[k] * L1; UFb[k] = -h * Fu[k] * abv6; }
+    R drhoEb = -h * Fb[4] * L1;
+    R abv6b = -h * (Fb[0] + dot3(Fu, UF) + Fb[4] * hF);
+    R abv7b = h * (dot3(Fu, N) + Fb[4] * UnF);
+    R hFb = -h * Fb[4] * abv6;
+    R UnFb = h * Fb[4] * abv7;
+    // abv7 = abv3*abv5 - abv2*abv4/aF
+    R abv3b = abv7b * abv5, abv5b = abv7b * abv3, abv2b = -abv7b * abv4 / aF, abv4b = -abv7b * abv2 / aF;
+    R aFb = abv7b * abv2 * abv4 / (aF * aF);
+    // abv6 = abv3*abv4/a2F - abv2*abv5/aF
+    abv3b += abv6b * abv4 / a2F;
+    abv4b += abv6b * abv3 / a2F;
+    R a2Fb = -abv6b * abv3 * abv4 / (a2F * a2F);
+    abv2b += -abv6b * abv5 / aF;
+    abv5b += -abv6b * abv2 / aF;
+    aFb += abv6b * abv2 * abv5 / (aF * aF);
+    // abv5 = UnF*drho - dU.N
+    UnFb += abv5b * drho;
+    drhob += abv5b * UnF;
+    for (int k = 0; k < 3; k++) dUb[k] += -abv5b * N[k];
+    // abv4 = gm1*(qF*drho - UF.dU + drhoE)
+    R tb = gm1 * abv4b;
+    R qFb = tb * drho;
+    drhob += tb * qF;
+    for (int k = 0; k < 3; k++) { UFb[k] += -tb * dU[k]; dUb[k] += -tb * UF[k]; }
+    drhoEb += tb;
+    // abv1..3
+    R abv1b = abv3b;
+    L1b += -abv3b;
+    R L2b = h * (abv1b + abv2b), L3b = h * (abv1b - abv2b);
+    // entropy fix
+    R epsb = R(0), l1b, l2b, l3b;
+    if (s1) { l1b = L1b * h * l1 / eps; epsb += L1b * (R(1) - R(0.25) * l1 * l1 / (eps * eps)); } else l1b = L1b;
+    if (s2) { l2b = L2b * h * l2 / eps; epsb += L2b * (R(1) - R(0.25) * l2 * l2 / (eps * eps)); } else l2b = L2b;
+    if (s3) { l3b = L3b * h * l3 / eps; epsb += L3b * (R(1) - R(0.25) * l3 * l3 / (eps * eps)); } else l3b = L3b;
+    R eab = h * epsb * sgn(ea);
+    R ebb = h * epsb * sgn(eb_);
+    R rhoUnLb = eab / rhoL, rhoUnRb = -eab / rhoR;
+    rhoLb += -eab * rhoUnL / (rhoL * rhoL);
+    rhoRb += eab * rhoUnR / (rhoR * rhoR);
+    R cLb = ebb, cRb = -ebb;
+    pLb += cLb * g / (R(2) * cL * rhoL);
+    rhoLb += -cLb * g * pL / (R(2) * cL * rhoL * rhoL);
+    pRb += cRb * g / (R(2) * cR * rhoR);
+    rhoRb += -cRb * g * pR / (R(2) * cR * rhoR * rhoR);
+    // lam = |UnF|, |UnF + aF|, |UnF - aF|
+    R t2 = sgn(UnF + aF), t3 = sgn(UnF - aF);
+    UnFb += l1b * sgn(UnF) + l2b * t2 + l3b * t3;
+    aFb += l2b * t2 - l3b * t3;
+    // drhoE = (hR rhoR - pR) - (hL rhoL - pL)
+    R hLb = -drhoEb * rhoL, hRb = drhoEb * rhoR;
+    rhoRb += drhoEb * hR;
+    rhoLb += -drhoEb * hL;
+    pRb += -drhoEb;
+    pLb += drhoEb;
+    // dU = rhoR UR - rhoL UL ; drho = rhoR - rhoL
+    rhoRb += dot3(dUb, UR) + drhob;
+    rhoLb += -dot3(dUb, UL) - drhob;
+    for (int k = 0; k < 3; k++) { URb[k] += dUb[k] * rhoR; ULb[k] += -dUb[k] * rhoL; }
+    // UnF = UF.N ; aF = sqrt(a2F) ; a2F = gm1 (hF - qF) ; qF = |UF|^2/2
+    for (int k = 0; k < 3; k++) UFb[k] += UnFb * N[k];
+    a2Fb += aFb / (R(2) * aF);
+    hFb += gm1 * a2Fb;
+    qFb += -gm1 * a2Fb;
+    for (int k = 0; k < 3; k++) UFb[k] += qFb * UF[k];
+    // hF = (hL sL + hR sR)/Dn ; UF = (UL sL + UR sR)/Dn
+    hLb += hFb * sL / Dn;
+    hRb += hFb * sR / Dn;
+    R sLb = hFb * (hL - hF) / Dn, sRb = hFb * (hR - hF) / Dn;
+    for (int k = 0; k < 3; k++) {
+        ULb[k] += UFb[k] * sL / Dn;
+        URb[k] += UFb[k] * sR / Dn;
+        sLb += UFb[k] * (UL[k] - UF[k]) / Dn;
+        sRb += UFb[k] * (UR[k] - UF[k]) / Dn;
+    }
+    rhoLb += sLb / (R(2) * sL);
+    rhoRb += sRb / (R(2) * sR);
+    // fe = (rhoUnL hL + rhoUnR hR)/2 ; fu = (rhoUnL UL + rhoUnR UR + (pL+pR) N)/2 ; fr = (rhoUnL + rhoUnR)/2
+    rhoUnLb += h * feb * hL + h * dot3(Fu, UL) + h * frb;
+    rhoUnRb += h * feb * hR + h * dot3(Fu, UR) + h * frb;
+    hLb += h * feb * rhoUnL;
+    hRb += h * feb * rhoUnR;
+    for (int k = 0; k < 3; k++) { ULb[k] += h * Fu[k] * rhoUnL; URb[k] += h * Fu[k] * rhoUnR; }
+    R pn = h * dot3(Fu, N);
+    pLb += pn;
+    pRb += pn;
+    // hL = g pL/(gm1 rhoL) + qL/2
+    pLb += hLb * g / (gm1 * rhoL);
+    rhoLb += -hLb * g * pL / (gm1 * rhoL * rhoL);
+    pRb += hRb * g / (gm1 * rhoR);
+    rhoRb += -hRb * g * pR / (gm1 * rhoR * rhoR);
+    for (int k = 0; k < 3; k++) { ULb[k] += hLb * UL[k]; URb[k] += hRb * UR[k]; }
+    // rhoUn = rho Un ; Un = U.N
+    rhoLb += rhoUnLb * UnL;
+    rhoRb += rhoUnRb * UnR;
+    R UnLb = rhoUnLb * rhoL, UnRb = rhoUnRb * rhoR;
+    for (int k = 0; k < 3; k++) { ULb[k] += UnLb * N[k]; URb[k] += UnRb * N[k]; }
+}
+
+// riemann.eulerLaxFriedrichs
+template <typename R>
+AFVM_HD void laxf_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR, const R* rhoUL,
+                      const R* rhoUR, R rhoEL, R rhoER, const R* N, const R* Fb, R& pLb, R& pRb, R* ULb, R* URb,
+                      R& rhoLb, R& rhoRb, R* rhoULb, R* rhoURb, R& rhoELb, R& rhoERb) {
+    const R g = R(P.gamma), h = R(0.5);
+    R UnL = dot3(UL, N), UnR = dot3(UR, N);
+    R cL = sqrt(g * pL / rhoL), cR = sqrt(g * pR / rhoR);
+    R A = fabs(UnL) + cL, B = fabs(UnR) + cR;
+    R aF = (A >= B) ? A : B;
+    R ha = h * aF;
+    R Fu[3] = {Fb[1], Fb[2], Fb[3]};
+    R hab = -(Fb[0] * (rhoR - rhoL) + Fu[0] * (rhoUR[0] - rhoUL[0]) + Fu[1] * (rhoUR[1] - rhoUL[1]) +
+              Fu[2] * (rhoUR[2] - rhoUL[2]) + Fb[4] * (rhoER - rhoEL));
+    R aFb = h * hab;
+    rhoLb += h * Fb[0] * UnL + ha * Fb[0];
+    rhoRb += h * Fb[0] * UnR - ha * Fb[0];
+    R UnLb = h * Fb[0] * rhoL + h * dot3(Fu, rhoUL) + h * Fb[4] * (rhoEL + pL);
+    R UnRb = h * Fb[0] * rhoR + h * dot3(Fu, rhoUR) + h * Fb[4] * (rhoER + pR);
+    for (int k = 0; k < 3; k++) {
+        rhoULb[k] += h * Fu[k] * UnL + ha * Fu[k];
+        rhoURb[k] += h * Fu[k] * UnR - ha * Fu[k];
+    }
+    R pn = h * dot3(Fu, N);
+    pLb += pn + h * Fb[4] * UnL;
+    pRb += pn + h * Fb[4] * UnR;
+    rhoELb += h * Fb[4] * UnL + ha * Fb[4];
+    rhoERb += h * Fb[4] * UnR - ha * Fb[4];
+    R Ab = (A >= B) ? aFb : R(0), Bb = (A >= B) ? R(0) : aFb;
+    UnLb += Ab * sgn(UnL);
+    UnRb += Bb * sgn(UnR);
+    pLb += Ab * g / (R(2) * cL * rhoL);
+    rhoLb += -Ab * g * pL / (R(2) * cL * rhoL * rhoL);
+    pRb += Bb * g / (R(2) * cR * rhoR);
+    rhoRb += -Bb * g * pR / (R(2) * cR * rhoR * rhoR);
+    for (int k = 0; k < 3; k++) { ULb[k] += UnLb * N[k]; URb[k] += UnRb * N[k]; }
+}
+
+// RCF.viscousFlux: F[1..3] += -sigma, F[4] += -(q + sigma.UF)
+template <typename R>
+AFVM_HD void viscous_vjp(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, const R* UF, const R* gTF,
+                         const R* gUF, const R* D, const R* N, R delta, const R* Fb, R& TLb, R& TRb, R* ULb, R* URb,
+                         R& TFb, R* UFb, R* gTFb, R* gUFb) {
+    R mu = viscosity<R>(P, TF);
+    R kappa = mu * R(P.kFac);
+    R snT = (TR - TL) / delta;
+    R gTD = dot3(gTF, D);
+    R gT[3];
+    for (int k = 0; k < 3; k++) gT[k] = gTF[k] + snT * D[k] - gTD * D[k];
+    R gU[9];
+    for (int i = 0; i < 3; i++) {
+        R snU = (UR[i] - UL[i]) / delta;
+        R gUD = gUF[3 * i] * D[0] + gUF[3 * i + 1] * D[1] + gUF[3 * i + 2] * D[2];
+        for (int k = 0; k < 3; k++) gU[3 * i + k] = gUF[3 * i + k] + snU * D[k] - gUD * D[k];
+    }
+    R tmp3 = gU[0] + gU[4] + gU[8];
+    R tmp2[3], sigma[3];
+    for (int i = 0; i < 3; i++) {
+        tmp2[i] = (gU[3 * i] + gU[i]) * N[0] + (gU[3 * i + 1] + gU[3 + i]) * N[1] + (gU[3 * i + 2] + gU[6 + i]) * N[2];
+        sigma[i] = mu * (tmp2[i] - R(2.0 / 3) * tmp3 * N[i]);
+    }
+    // reverse
+    R sb[3];
+    for (int i = 0; i < 3; i++) {
+        sb[i] = -Fb[1 + i] - Fb[4] * UF[i];
+        UFb[i] += -Fb[4] * sigma[i];
+    }
+    R qFb = -Fb[4];
+    R mub = R(0);
+    R tmp2b[3];
+    R tmp3b = R(0);
+    for (int i = 0; i < 3; i++) {
+        mub += sb[i] * (tmp2[i] - R(2.0 / 3) * tmp3 * N[i]);
+        tmp2b[i] = sb[i] * mu;
+        tmp3b += -R(2.0 / 3) * mu * sb[i] * N[i];
+    }
+    R kappab = qFb * dot3(gT, N);
+    R gTb[3];
+    for (int k = 0; k < 3; k++) gTb[k] = qFb * kappa * N[k];
+    mub += kappab * R(P.kFac);
+    R gUb[9];
+    for (int i = 0; i < 3; i++)
+        for (int k = 0; k < 3; k++) gUb[3 * i + k] = tmp2b[i] * N[k] + tmp2b[k] * N[i];
+    gUb[0] += tmp3b; gUb[4] += tmp3b; gUb[8] += tmp3b;
+    for (int i = 0; i < 3; i++) {
+        R snUb = R(0), gUDb = R(0);
+        for (int k = 0; k < 3; k++) {
+            gUFb[3 * i + k] += gUb[3 * i + k];
+            snUb += gUb[3 * i + k] * D[k];
+        }
+        gUDb = -snUb;
+        for (int k = 0; k < 3; k++) gUFb[3 * i + k] += gUDb * D[k];
+        URb[i] += snUb / delta;
+        ULb[i] += -snUb / delta;
+    }
+    R snTb = dot3(gTb, D);
+    R gTDb = -snTb;
+    for (int k = 0; k < 3; k++) gTFb[k] += gTb[k] + gTDb * D[k];
+    TRb += snTb / delta;
+    TLb += -snTb / delta;
+    if (P.muModel == AFVM_MU_SUTHERLAND) TFb += mub * mu * (R(1.5) / TF - R(1) / (TF + R(P.muTs)));
+}
+
+// <Fbar, F> differentiated with respect to all 40 inputs of the face (accumulated into out)
+template <typename R>
+AFVM_HD void face_vjp(const Phys& P, int kind, bool inviscid, const FaceIn<R>& in, const R* Fb, FaceBar<R>& o) {
+    if (kind == FACE_BOUNDARY) {
+        R rho, rhoU[3], rhoE;
+        conservative<R>(P, in.UN, in.TN, in.pN, rho, rhoU, rhoE);
+        R Un = dot3(in.UN, in.N);
+        R rhob = Fb[0] * Un, rhoUb[3] = {Fb[1] * Un, Fb[2] * Un, Fb[3] * Un}, rhoEb = Fb[4] * Un;
+        R Fu[3] = {Fb[1], Fb[2], Fb[3]};
+        R Unb = Fb[0] * rho + dot3(Fu, rhoU) + Fb[4] * (rhoE + in.pN);
+        o.pN += dot3(Fu, in.N) + Fb[4] * Un;
+        for (int k = 0; k < 3; k++) o.UN[k] += Unb * in.N[k];
+        conservative_vjp<R>(P, in.UN, in.TN, in.pN, rhob, rhoUb, rhoEb, o.UN, o.TN, o.pN);
+        if (!inviscid) {
+            R TFb = R(0), UFb[3] = {R(0), R(0), R(0)};
+            viscous_vjp<R>(P, in.TP, in.TN, in.UP, in.UN, in.TN, in.UN, in.gTN, in.gUN, in.D, in.N, in.delta, Fb,
+                           o.TP, o.TN, o.UP, o.UN, TFb, UFb, o.gTN, o.gUN);
+            o.TN += TFb;
+            for (int k = 0; k < 3; k++) o.UN[k] += UFb[k];
+        }
+        return;
+    }
+    const bool chr = kind == FACE_CHARACTERISTIC;
+    // forward
+    R ULF[3], TLF, pLF, URF[3], TRF, pRF;
+    for (int k = 0; k < 3; k++) ULF[k] = recon<R>(in.UP[k], in.UN[k], in.gUP + 3 * k, in.lw0, in.qw0);
+    TLF = recon<R>(in.TP, in.TN, in.gTP, in.lw0, in.qw0);
+    pLF = recon<R>(in.pP, in.pN, in.gpP, in.lw0, in.qw0);
+    if (chr) {
+        for (int k = 0; k < 3; k++) URF[k] = in.UN[k];
+        TRF = in.TN; pRF = in.pN;
+    } else {
+        for (int k = 0; k < 3; k++) URF[k] = recon<R>(in.UN[k], in.UP[k], in.gUN + 3 * k, in.lw1, in.qw1);
+        TRF = recon<R>(in.TN, in.TP, in.gTN, in.lw1, in.qw1);
+        pRF = recon<R>(in.pN, in.pP, in.gpN, in.lw1, in.qw1);
+    }
+    R rhoL, rhoUL[3], rhoEL, rhoR, rhoUR[3], rhoER;
+    conservative<R>(P, ULF, TLF, pLF, rhoL, rhoUL, rhoEL);
+    conservative<R>(P, URF, TRF, pRF, rhoR, rhoUR, rhoER);
+    R ULFb[3] = {R(0), R(0), R(0)}, URFb[3] = {R(0), R(0), R(0)};
+    R TLFb = R(0), TRFb = R(0), pLFb = R(0), pRFb = R(0);
+    // viscous part
+    if (!inviscid) {
+        R TF, UF[3], gTF[3], gUF[9];
+        if (chr) {
+            TF = in.TN;
+            for (int k = 0; k < 3; k++) { UF[k] = in.UN[k]; gTF[k] = in.gTN[k]; }
+            for (int k = 0; k < 9; k++) gUF[k] = in.gUN[k];
+        } else {
+            TF = R(0.5) * (TLF + TRF);
+            for (int k = 0; k < 3; k++) { UF[k] = R(0.5) * (ULF[k] + URF[k]); gTF[k] = R(0.5) * (in.gTP[k] + in.gTN[k]); }
+            for (int k = 0; k < 9; k++) gUF[k] = R(0.5) * (in.gUP[k] + in.gUN[k]);
+        }
+        R TFb = R(0), UFb[3] = {R(0), R(0), R(0)}, gTFb[3] = {R(0), R(0), R(0)}, gUFb[9];
+        for (int k = 0; k < 9; k++) gUFb[k] = R(0);
+        viscous_vjp<R>(P, in.TP, in.TN, in.UP, in.UN, TF, UF, gTF, gUF, in.D, in.N, in.delta, Fb, o.TP, o.TN, o.UP,
+                       o.UN, TFb, UFb, gTFb, gUFb);
+        if (chr) {
+            o.TN += TFb;
+            for (int k = 0; k < 3; k++) { o.UN[k] += UFb[k]; o.gTN[k] += gTFb[k]; }
+            for (int k = 0; k < 9; k++) o.gUN[k] += gUFb[k];
+        } else {
+            TLFb += R(0.5) * TFb;
+            TRFb += R(0.5) * TFb;
+            for (int k = 0; k < 3; k++) {
+                ULFb[k] += R(0.5) * UFb[k];
+                URFb[k] += R(0.5) * UFb[k];
+                o.gTP[k] += R(0.5) * gTFb[k];
+                o.gTN[k] += R(0.5) * gTFb[k];
+            }
+            for (int k = 0; k < 9; k++) { o.gUP[k] += R(0.5) * gUFb[k]; o.gUN[k] += R(0.5) * gUFb[k]; }
+        }
+    }
+    // Riemann part
+    R rhoLb = R(0), rhoRb = R(0), rhoULb[3] = {R(0), R(0), R(0)}, rhoURb[3] = {R(0), R(0), R(0)};
+    R rhoELb = R(0), rhoERb = R(0);
+    int solver = chr ? P.briemann : P.riemann;
+    if (solver == AFVM_RIEMANN_ROE)
+        roe_vjp<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, in.N, Fb, pLFb, pRFb, ULFb, URFb, rhoLb, rhoRb);
+    else
+        laxf_vjp<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, rhoUL, rhoUR, rhoEL, rhoER, in.N, Fb, pLFb, pRFb, ULFb, URFb,
+                    rhoLb, rhoRb, rhoULb, rhoURb, rhoELb, rhoERb);
+    conservative_vjp<R>(P, ULF, TLF, pLF, rhoLb, rhoULb, rhoELb, ULFb, TLFb, pLFb);
+    conservative_vjp<R>(P, URF, TRF, pRF, rhoRb, rhoURb, rhoERb, URFb, TRFb, pRFb);
+    // reconstruction
+    for (int k = 0; k < 3; k++) recon_vjp<R>(ULFb[k], in.lw0, in.qw0, o.UP[k], o.UN[k], o.gUP + 3 * k);
+    recon_vjp<R>(TLFb, in.lw0, in.qw0, o.TP, o.TN, o.gTP);
+    recon_vjp<R>(pLFb, in.lw0, in.qw0, o.pP, o.pN, o.gpP);
+    if (chr) {
+        for (int k = 0; k < 3; k++) o.UN[k] += URFb[k];
+        o.TN += TRFb;
+        o.pN += pRFb;
+    } else {
+        for (int k = 0; k < 3; k++) recon_vjp<R>(URFb[k], in.lw1, in.qw1, o.UN[k], o.UP[k], o.gUN + 3 * k);
+        recon_vjp<R>(TRFb, in.lw1, in.qw1, o.TN, o.TP, o.gTN);
+        recon_vjp<R>(pRFb, in.lw1, in.qw1, o.pN, o.pP, o.gpN);
+    }
+}
+
+}  // namespace afvm

@@ -4,9 +4,21 @@
 // reference's order (left to right). FMA contraction is allowed, so results agree with the
 // reference to rounding, not bit for bit.
 #pragma once
-#include <cuda_runtime.h>
 #include <stdint.h>
 #include "afvm.h"
+
+// The face physics is written once for the device and, for the unit tests of the hand-derived
+// adjoint, also compiles as plain host C++.
+#ifdef __CUDACC__
+#include <cuda_runtime.h>
+#define AFVM_HD __host__ __device__ __forceinline__
+#else
+#include <cmath>
+#define AFVM_HD inline
+using std::fabs;
+using std::fmax;
+using std::sqrt;
+#endif
 
 namespace afvm {
 
@@ -26,18 +38,18 @@ struct Phys {
 };
 
 template <typename R>
-__device__ __forceinline__ R dot3(const R* a, const R* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+AFVM_HD R dot3(const R* a, const R* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
 
 // mu(T): constant, or Sutherland 1.4792e-06*T**1.5/(T+116.) (adFVM/density.py:27)
 template <typename R>
-__device__ __forceinline__ R viscosity(const Phys& P, R T) {
+AFVM_HD R viscosity(const Phys& P, R T) {
     if (P.muModel == AFVM_MU_SUTHERLAND) return (R(P.muAs) * (T * sqrt(T))) / (T + R(P.muTs));
     return R(P.mu0);
 }
 
 // RCF.conservative (adFVM/density.py:173-181)
 template <typename R>
-__device__ __forceinline__ void conservative(const Phys& P, const R* U, R T, R p, R& rho, R* rhoU, R& rhoE) {
+AFVM_HD void conservative(const Phys& P, const R* U, R T, R p, R& rho, R* rhoU, R& rhoE) {
     R e = R(P.Cv) * T;
     rho = p / (e * R(P.gm1));
     rhoE = rho * (e + R(0.5) * dot3(U, U));
@@ -46,14 +58,14 @@ __device__ __forceinline__ void conservative(const Phys& P, const R* U, R T, R p
 
 // interp.secondOrder for one side (adFVM/interp.py:20-28): phiC + (phiD-phiC)*lw + qw.grad
 template <typename R>
-__device__ __forceinline__ R recon(R phiC, R phiD, const R* g, R lw, const R* qw) {
+AFVM_HD R recon(R phiC, R phiD, const R* g, R lw, const R* qw) {
     R phiF = phiC + (phiD - phiC) * lw;
     return phiF + (qw[0] * g[0] + qw[1] * g[1] + qw[2] * g[2]);
 }
 
 // riemann.eulerRoe (adFVM/riemann.py:21-70)
 template <typename R>
-__device__ __forceinline__ void roe(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR,
+AFVM_HD void roe(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR,
                                     const R* N, R* F) {
     const R g = R(P.gamma), gm1 = R(P.gm1);
     R rhoUnL = rhoL * dot3(UL, N), rhoUnR = rhoR * dot3(UR, N);
@@ -95,7 +107,7 @@ __device__ __forceinline__ void roe(const Phys& P, R pL, R pR, const R* UL, cons
 
 // riemann.eulerLaxFriedrichs (adFVM/riemann.py:6-18)
 template <typename R>
-__device__ __forceinline__ void laxf(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR,
+AFVM_HD void laxf(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR,
                                      const R* rhoUL, const R* rhoUR, R rhoEL, R rhoER, const R* N, R* F) {
     const R g = R(P.gamma);
     R UnL = dot3(UL, N), UnR = dot3(UR, N);
@@ -111,7 +123,7 @@ __device__ __forceinline__ void laxf(const Phys& P, R pL, R pR, const R* UL, con
 
 // RCF.viscousFlux (adFVM/density.py:192-222): adds -sigma to F[1..3] and -(q + sigma.UF) to F[4]
 template <typename R>
-__device__ __forceinline__ void viscous(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, const R* UF,
+AFVM_HD void viscous(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, const R* UF,
                                         const R* gTF, const R* gUF, const R* D, const R* N, R delta, R* F) {
     R mu = viscosity<R>(P, TF);
     R kappa = mu * R(P.kFac);
