@@ -1,0 +1,303 @@
+// Discrete adjoint of one SSP-RK3 step with dt held fixed (the per-step VJP of the reference's
+// adjoint sweep, apps/adjoint.py:101-126 and 268-291).
+//
+// Forward u0 -> u1 -> u2 -> u3 (timestep.py:27-55) is recomputed, then the three stages are
+// reversed. For stage i with output adjoint abar_{i+1}, the residual seed is
+// Rbar = -beta_ii dt abar_{i+1}, and J_R(u_i)^T Rbar is formed by three kernels, all gathers
+// (no atomics, so every result is bitwise reproducible):
+//   k_adj_flux   faces: Fbar = Rbar_P A/V_P - Rbar_N A/V_N, then the hand-derived face VJP
+//                (face.cuh) -> a 40-value record per face (primitive/gradient adjoints of
+//                both sides)
+//   k_adj_cell1  cells: sum of the face records of the cell's 6 faces (its own side) and of the
+//                gradient adjoints of the ghost cells it is the source of
+//   k_adj_cell2  cells: transpose of the Green-Gauss gradient (own slots and, through the
+//                back-slot weights, the neighbours'), ghost boundary conditions transposed,
+//                objective gradient (stage 1), primitive VJP and the SSP-RK reverse update.
+#include <cuda_runtime.h>
+#include "facedev.cuh"
+
+namespace afvm {
+
+constexpr int FADJ = 40;   // FaceBar layout: UP3 TP pP UN3 TN pN gUP9 gTP3 gpP3 gUN9 gTN3 gpN3
+constexpr int CBAR = 20;   // per cell: primitive adjoint (5) then gradient adjoint (15)
+
+template <typename R>
+__global__ void __launch_bounds__(BLOCK) k_adj_flux(MeshDev<R> m, Phys P, const R* __restrict__ rec, R coef,
+                                                    const R* __restrict__ ar, const R* __restrict__ au,
+                                                    const R* __restrict__ ae, R* __restrict__ fadj, int inviscid) {
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= m.nF) return;
+    int kind = (f < m.nIF) ? FACE_INTERNAL : (int)m.fkind[f - m.nIF];
+    int iP = m.own[f];
+    R wp = m.wpf[f];
+    R Fb[5];
+    Fb[0] = (coef * ar[iP]) * wp;
+    for (int k = 0; k < 3; k++) Fb[1 + k] = (coef * au[3 * iP + k]) * wp;
+    Fb[4] = (coef * ae[iP]) * wp;
+    if (f < m.nIF) {
+        int iN = m.nbr[f];
+        R wn = m.wnf[f];
+        Fb[0] = Fb[0] - (coef * ar[iN]) * wn;
+        for (int k = 0; k < 3; k++) Fb[1 + k] = Fb[1 + k] - (coef * au[3 * iN + k]) * wn;
+        Fb[4] = Fb[4] - (coef * ae[iN]) * wn;
+    }
+    FaceIn<R> in;
+    load_face<R>(m, rec, f, in);
+    FaceBar<R> b;
+    zero_bar(b);
+    face_vjp<R>(P, kind, inviscid != 0, in, Fb, b);
+    const R* src = &b.UP[0];
+    R* out = fadj + (size_t)f * FADJ;
+    for (int k = 0; k < FADJ; k++) out[k] = src[k];
+}
+
+template <typename R>
+__global__ void __launch_bounds__(BLOCK) k_adj_cell1(MeshDev<R> m, const R* __restrict__ fadj, R* __restrict__ cbar) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m.nIC) return;
+    const size_t n = m.nIC;
+    R acc[CBAR];
+    for (int k = 0; k < CBAR; k++) acc[k] = R(0);
+    for (int s = 0; s < 6; s++) {
+        int e = m.accf[s * n + c];
+        bool ownerSide = e >= 0;
+        int f = ownerSide ? e : ~e;
+        const R* r = fadj + (size_t)f * FADJ;
+        int po = ownerSide ? 0 : 5, go = ownerSide ? 10 : 25;
+        for (int k = 0; k < 5; k++) acc[k] += r[po + k];
+        for (int k = 0; k < 15; k++) acc[5 + k] += r[go + k];
+    }
+    // gradient adjoints of the ghosts whose gradient is a copy of this cell's
+    for (int q = m.gsStart[c]; q < m.gsStart[c + 1]; q++) {
+        int g = m.gsList[q];
+        const R* r = fadj + (size_t)(m.nIF + g) * FADJ;
+        for (int k = 0; k < 15; k++) acc[5 + k] += r[25 + k];
+    }
+    R* out = cbar + (size_t)c * CBAR;
+    for (int k = 0; k < CBAR; k++) out[k] = acc[k];
+}
+
+// phiFbar_i = rv * sum_j G[i][j] sn_j  (transpose of grad += phiF (x) S N', scaled by 1/V)
+template <typename R>
+__device__ __forceinline__ void phi_bar(const R* G, const R* sn, R rv, R* pb) {
+    for (int i = 0; i < 5; i++) pb[i] = rv * (G[3 * i] * sn[0] + G[3 * i + 1] * sn[1] + G[3 * i + 2] * sn[2]);
+}
+
+template <typename R, int STAGE>
+__global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const R* __restrict__ rec,
+                                                     const R* __restrict__ fadj, const R* __restrict__ cbar,
+                                                     const R* __restrict__ ur, const R* __restrict__ uu,
+                                                     const R* __restrict__ ue,
+                                                     const R* ainr, const R* ainu, const R* aine,
+                                                     R* a1r, R* a1u, R* a1e, R* a0r, R* a0u, R* a0e, R* sb,
+                                                     double dt, int objective, int objStart, int objN, double obja) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m.nIC) return;
+    const size_t n = m.nIC;
+    const size_t nF = m.nF;
+    const R* cb = cbar + (size_t)c * CBAR;
+    R pbar[5];
+    for (int k = 0; k < 5; k++) pbar[k] = cb[k];
+    const R* G = cb + 5;
+    R rv = m.rvol[c];
+    for (int s = 0; s < 6; s++) {
+        R sn[3] = {m.gsn[(3 * s) * n + c], m.gsn[(3 * s + 1) * n + c], m.gsn[(3 * s + 2) * n + c]};
+        R w = m.gw[s * n + c];
+        R pb[5];
+        phi_bar<R>(G, sn, rv, pb);
+        R omw = -w + R(1);
+        for (int k = 0; k < 5; k++) pbar[k] += omw * pb[k];
+        int nb = m.gnb[s * n + c];
+        if (nb < m.nIC) {
+            // neighbour's gradient: its slot for this face has S N'' = -S N' and weight gwb
+            R msn[3] = {-sn[0], -sn[1], -sn[2]};
+            R pn[5];
+            phi_bar<R>(cbar + (size_t)nb * CBAR + 5, msn, m.rvol[nb], pn);
+            R wb = m.gwb[s * n + c];
+            for (int k = 0; k < 5; k++) pbar[k] += wb * pn[k];
+        }
+    }
+    // ghost cells whose boundary value comes from this cell: transpose of the BC
+    for (int q = m.gsStart[c]; q < m.gsStart[c + 1]; q++) {
+        int g = m.gsList[q];
+        int f = m.nIF + g;
+        int o = m.own[f];
+        int s = m.gslot[g];
+        R gp[5];
+        const R* r = fadj + (size_t)f * FADJ;
+        for (int k = 0; k < 5; k++) gp[k] = r[5 + k];
+        R sn[3] = {m.gsn[(3 * s) * n + o], m.gsn[(3 * s + 1) * n + o], m.gsn[(3 * s + 2) * n + o]};
+        R w = m.gw[s * n + o];
+        R pb[5];
+        phi_bar<R>(cbar + (size_t)o * CBAR + 5, sn, m.rvol[o], pb);
+        for (int k = 0; k < 5; k++) gp[k] += w * pb[k];
+        if (STAGE == 1 && objective == AFVM_OBJ_DRAG && f >= objStart && f < objStart + objN) {
+            // drag = sum (p0 nx - mu(T0) (U0 - U0i)/delta) A, ghost values p0, T0, U0
+            const R* rg = rec + (size_t)(m.nIC + g) * REC;
+            const R* ro = rec + (size_t)o * REC;
+            double T0 = rg[R_T], U0 = rg[0], U0i = ro[0];
+            double A = m.area[f], dl = m.dlt[f], nx = m.nrm[f];
+            double mu = viscosity<double>(P, T0);
+            double dmu = (P.muModel == AFVM_MU_SUTHERLAND) ? mu * (1.5 / T0 - 1.0 / (T0 + P.muTs)) : 0.0;
+            gp[R_P] += (R)(obja * nx * A);
+            gp[R_T] += (R)(-obja * dmu * (U0 - U0i) / dl * A);
+            gp[0] += (R)(-obja * mu / dl * A);
+        }
+        int kind = m.gkind[g];
+        int kU = kind & 7, kT = (kind >> 3) & 7, kp = (kind >> 6) & 7;
+        if (kU == GK_COPY) {
+            for (int k = 0; k < 3; k++) pbar[k] += gp[k];
+        } else if (kU == GK_SYM) {
+            R nr[3] = {m.nrm[f], m.nrm[nF + f], m.nrm[2 * nF + f]};
+            R un = dot3(gp, nr);
+            for (int k = 0; k < 3; k++) pbar[k] += gp[k] - un * nr[k];
+        }
+        if (kT != GK_FIXED) pbar[R_T] += gp[R_T];
+        if (kp != GK_FIXED) pbar[R_P] += gp[R_P];
+    }
+    // objective on the stage-1 primitives
+    if (STAGE == 1 && objective != AFVM_OBJ_NONE) {
+        const R* rc = rec + (size_t)c * REC;
+        if (objective == AFVM_OBJ_KINETIC_ENERGY) {
+            double U[3] = {rc[0], rc[1], rc[2]}, T = rc[R_T], p = rc[R_P], V = m.vol[c];
+            double d = (P.Cv * T) * P.gm1;
+            double rho = p / d;
+            double q = U[0] * U[0] + U[1] * U[1] + U[2] * U[2];
+            for (int k = 0; k < 3; k++) pbar[k] += (R)(obja * rho * U[k] * V);
+            pbar[R_P] += (R)(obja * 0.5 * q * V / d);
+            pbar[R_T] += (R)(-obja * 0.5 * q * V * rho / T);
+        } else if (objective == AFVM_OBJ_SUM_T) {
+            pbar[R_T] += (R)obja;
+        } else if (objective == AFVM_OBJ_DRAG) {
+            for (int s = 0; s < 6; s++) {
+                int e = m.accf[s * n + c];
+                if (e < objStart || e >= objStart + objN) continue;   // owner-side faces of the patch
+                const R* rg = rec + (size_t)m.nbr[e] * REC;
+                double T0 = rg[R_T];
+                double mu = viscosity<double>(P, T0);
+                pbar[0] += (R)(obja * mu / (double)m.dlt[e] * (double)m.area[e]);
+            }
+        }
+    }
+    // primitive VJP (density.py:162-171)
+    double rho = ur[c], rU[3] = {uu[3 * c], uu[3 * c + 1], uu[3 * c + 2]}, rE = ue[c];
+    double U[3] = {rU[0] / rho, rU[1] / rho, rU[2] / rho};
+    double E = rE / rho;
+    double e = E - 0.5 * (U[0] * U[0] + U[1] * U[1] + U[2] * U[2]);
+    double eb = (double)pbar[R_T] * P.rCv + (double)pbar[R_P] * P.gm1 * rho;
+    double rhob = (double)pbar[R_P] * P.gm1 * e;
+    double Ubt[3];
+    for (int k = 0; k < 3; k++) Ubt[k] = (double)pbar[k] - eb * U[k];
+    double J[5];
+    for (int k = 0; k < 3; k++) J[1 + k] = Ubt[k] / rho;
+    J[4] = eb / rho;
+    J[0] = rhob - (Ubt[0] * U[0] + Ubt[1] * U[1] + Ubt[2] * U[2]) / rho - eb * E / rho;
+    // SSP-RK reverse (timestep.py:35-45 transposed)
+    R ain[5] = {ainr[c], ainu[3 * c], ainu[3 * c + 1], ainu[3 * c + 2], aine[c]};
+    R out[5];
+    if (STAGE == 2) {
+        for (int k = 0; k < 5; k++) out[k] = R(2. / 3) * ain[k] + (R)J[k];
+        R z[5];
+        for (int k = 0; k < 5; k++) { z[k] = R(1. / 3) * ain[k]; sb[5 * (size_t)c + k] = R(2. / 3) * R(dt) * ain[k]; }
+        a0r[c] = z[0]; a0u[3 * c] = z[1]; a0u[3 * c + 1] = z[2]; a0u[3 * c + 2] = z[3]; a0e[c] = z[4];
+        a1r[c] = out[0]; a1u[3 * c] = out[1]; a1u[3 * c + 1] = out[2]; a1u[3 * c + 2] = out[3]; a1e[c] = out[4];
+    } else if (STAGE == 1) {
+        for (int k = 0; k < 5; k++) out[k] = R(1. / 4) * ain[k] + (R)J[k];
+        R z[5] = {a0r[c], a0u[3 * c], a0u[3 * c + 1], a0u[3 * c + 2], a0e[c]};
+        for (int k = 0; k < 5; k++) { z[k] += R(3. / 4) * ain[k]; sb[5 * (size_t)c + k] += R(1. / 4) * R(dt) * ain[k]; }
+        a0r[c] = z[0]; a0u[3 * c] = z[1]; a0u[3 * c + 1] = z[2]; a0u[3 * c + 2] = z[3]; a0e[c] = z[4];
+        a1r[c] = out[0]; a1u[3 * c] = out[1]; a1u[3 * c + 1] = out[2]; a1u[3 * c + 2] = out[3]; a1e[c] = out[4];
+    } else {
+        R z[5] = {a0r[c], a0u[3 * c], a0u[3 * c + 1], a0u[3 * c + 2], a0e[c]};
+        for (int k = 0; k < 5; k++) { z[k] += ain[k] + (R)J[k]; sb[5 * (size_t)c + k] += R(dt) * ain[k]; }
+        a0r[c] = z[0]; a0u[3 * c] = z[1]; a0u[3 * c + 1] = z[2]; a0u[3 * c + 2] = z[3]; a0e[c] = z[4];
+    }
+}
+
+// scatter the (nIC x 5) source adjoint into the reference layout
+template <typename R>
+__global__ void k_split5(int n, const R* __restrict__ sb, R* r, R* u, R* e) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const R* s = sb + 5 * (size_t)c;
+    if (r) r[c] = s[0];
+    if (u) { u[3 * c] = s[1]; u[3 * c + 1] = s[2]; u[3 * c + 2] = s[3]; }
+    if (e) e[c] = s[4];
+}
+
+template <typename R>
+int adjoint_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double dt, const R* Srho, const R* SrhoU,
+                     const R* SrhoE, const R* rhoNa, const R* rhoUNa, const R* rhoENa, double obja, R* rhoa,
+                     R* rhoUa, R* rhoEa, R* Srhoa, R* SrhoUa, R* SrhoEa, cudaStream_t s) {
+    const MeshDev<R>& m = meshOf<R>(c);
+    const Phys& P = c->phys;
+    default_sources<R>(c, Srho, SrhoU, SrhoE);
+    int inviscid = (P.muModel == AFVM_MU_CONSTANT && P.mu0 == 0.0) ? 1 : 0;
+    R* u1[3] = {(R*)c->u1[0], (R*)c->u1[1], (R*)c->u1[2]};
+    R* u2[3] = {(R*)c->u2[0], (R*)c->u2[1], (R*)c->u2[2]};
+    const R* u0c[3] = {rho, rhoU, rhoE};
+    const R* u1c[3] = {u1[0], u1[1], u1[2]};
+    const R* u2c[3] = {u2[0], u2[1], u2[2]};
+    // forward recompute of the stage states
+    cudaMemsetAsync(c->dtcBits, 0, sizeof(unsigned long long), s);
+    launch_prim_grad<R>(c, rho, rhoU, rhoE, s);
+    launch_flux_update<R>(c, 0, dt, nullptr, u0c, u1c, u2c, Srho, SrhoU, SrhoE, u1, s);
+    launch_prim_grad<R>(c, u1[0], u1[1], u1[2], s);
+    launch_flux_update<R>(c, 1, dt, nullptr, u0c, u1c, u2c, Srho, SrhoU, SrhoE, u2, s);
+    // reverse sweep
+    R* A1[3] = {(R*)c->a1[0], (R*)c->a1[1], (R*)c->a1[2]};
+    R* A2[3] = {(R*)c->a2[0], (R*)c->a2[1], (R*)c->a2[2]};
+    R* fadj = (R*)c->fadj;
+    R* cbar = (R*)c->cbar;
+    R* sb = (R*)c->sbar;
+    const R* rec = (const R*)c->rec;
+    int nbF = nblocks(m.nF), nbC = nblocks(m.nIC);
+    const double beta[3] = {1.0, 1. / 4, 2. / 3};
+    for (int st = 2; st >= 0; st--) {
+        const R* const* u = st == 0 ? u0c : (st == 1 ? u1c : u2c);
+        launch_prim_grad<R>(c, u[0], u[1], u[2], s);
+        // adjoint of this stage's output: a3 = seeds, a2 = A2, a1 = A1
+        const R* ain[3];
+        if (st == 2) { ain[0] = rhoNa; ain[1] = rhoUNa; ain[2] = rhoENa; }
+        else if (st == 1) { ain[0] = A2[0]; ain[1] = A2[1]; ain[2] = A2[2]; }
+        else { ain[0] = A1[0]; ain[1] = A1[1]; ain[2] = A1[2]; }
+        R coef = (R)(-beta[st] * dt);
+        {
+            ProfScope ps(c, KID_ADJ_FLUX, s);
+            k_adj_flux<R><<<nbF, BLOCK, 0, s>>>(m, P, rec, coef, ain[0], ain[1], ain[2], fadj, inviscid);
+        }
+        {
+            ProfScope ps(c, KID_ADJ_GATHER, s);
+            k_adj_cell1<R><<<nbC, BLOCK, 0, s>>>(m, fadj, cbar);
+        }
+        ProfScope ps(c, KID_ADJ_GRAD, s);
+        if (st == 2)
+            k_adj_cell2<R, 2><<<nbC, BLOCK, 0, s>>>(m, P, rec, fadj, cbar, u[0], u[1], u[2], ain[0], ain[1], ain[2],
+                                                    A2[0], A2[1], A2[2], rhoa, rhoUa, rhoEa, sb, dt, c->objective,
+                                                    c->objStart, c->objN, obja);
+        else if (st == 1)
+            k_adj_cell2<R, 1><<<nbC, BLOCK, 0, s>>>(m, P, rec, fadj, cbar, u[0], u[1], u[2], ain[0], ain[1], ain[2],
+                                                    A1[0], A1[1], A1[2], rhoa, rhoUa, rhoEa, sb, dt, c->objective,
+                                                    c->objStart, c->objN, obja);
+        else
+            k_adj_cell2<R, 0><<<nbC, BLOCK, 0, s>>>(m, P, rec, fadj, cbar, u[0], u[1], u[2], ain[0], ain[1], ain[2],
+                                                    nullptr, nullptr, nullptr, rhoa, rhoUa, rhoEa, sb, dt,
+                                                    c->objective, c->objStart, c->objN, obja);
+    }
+    if (Srhoa || SrhoUa || SrhoEa) {
+        ProfScope ps(c, KID_ADJ_MISC, s);
+        k_split5<R><<<nbC, BLOCK, 0, s>>>(m.nIC, sb, Srhoa, SrhoUa, SrhoEa);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(c, e, "adjoint step launch");
+    return AFVM_OK;
+}
+
+template int adjoint_step_dev<double>(Ctx*, const double*, const double*, const double*, double, const double*,
+                                      const double*, const double*, const double*, const double*, const double*,
+                                      double, double*, double*, double*, double*, double*, double*, cudaStream_t);
+template int adjoint_step_dev<float>(Ctx*, const float*, const float*, const float*, double, const float*,
+                                     const float*, const float*, const float*, const float*, const float*, double,
+                                     float*, float*, float*, float*, float*, float*, cudaStream_t);
+
+}  // namespace afvm

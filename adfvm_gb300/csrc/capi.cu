@@ -91,6 +91,9 @@ struct HostTables {
     // cells
     std::vector<int32_t> gnb, accf;
     std::vector<double> gw, gsn, rvol, accw, vol;
+    // adjoint
+    std::vector<double> wpf, wnf, gwb;
+    std::vector<int32_t> gsStart, gsList, gslot;
 };
 
 template <typename R>
@@ -121,6 +124,12 @@ int upload_mesh(Ctx* c, const HostTables& h, MeshDev<R>& m) {
     if ((st = upload(c, &m.accf, h.accf))) return st;
     if ((st = upload(c, &m.accw, cast<R>(h.accw)))) return st;
     if ((st = upload(c, &m.vol, cast<R>(h.vol)))) return st;
+    if ((st = upload(c, &m.wpf, cast<R>(h.wpf)))) return st;
+    if ((st = upload(c, &m.wnf, cast<R>(h.wnf)))) return st;
+    if ((st = upload(c, &m.gwb, cast<R>(h.gwb)))) return st;
+    if ((st = upload(c, &m.gsStart, h.gsStart))) return st;
+    if ((st = upload(c, &m.gsList, h.gsList))) return st;
+    if ((st = upload(c, &m.gslot, h.gslot))) return st;
     return AFVM_OK;
 }
 
@@ -260,6 +269,36 @@ int build_tables(Ctx* c, const afvm_mesh_tensors* M, const afvm_patch_bc* bcs, H
             h.accw[s * n + ci] = ownerSide ? M->areas[f] / M->volumesL[f] : M->areas[f] / M->volumesR[f];
         }
     }
+    // adjoint tables: face weights, back-slot weights, ghosts grouped by source, ghost slots
+    h.wpf.resize(nF); h.wnf.resize(std::max(nIF, 1));
+    for (int f = 0; f < nF; f++) h.wpf[f] = M->areas[f] / M->volumesL[f];
+    for (int f = 0; f < nIF; f++) h.wnf[f] = M->areas[f] / M->volumesR[f];
+    h.gwb.assign(6 * n, 0.0);
+    h.gslot.assign(std::max(nG, 1), -1);
+    for (int ci = 0; ci < nIC; ci++) {
+        for (int s = 0; s < 6; s++) {
+            int f = M->cellFaces[6 * (size_t)ci + s];
+            int nb = M->cellNeighbours[6 * (size_t)ci + s];
+            if (nb < nIC) {
+                // the slot of f in nb's list has O' = 1 - O: w' = w + O' - 2 w O'
+                double w = M->weights[f];
+                double Ob = (double)(1 - M->cellOwner[6 * (size_t)ci + s]);
+                h.gwb[s * n + ci] = (w + Ob) - (2 * w) * Ob;
+            } else {
+                h.gslot[nb - nIC] = s;
+            }
+        }
+    }
+    for (int g = 0; g < nG; g++)
+        if (h.gslot[g] < 0) return fail(c, AFVM_ERR_BAD_ARG, "ghost without a gradient slot");
+    h.gsStart.assign(nIC + 1, 0);
+    for (int g = 0; g < nG; g++) h.gsStart[h.gsrc[g] + 1]++;
+    for (int ci = 0; ci < nIC; ci++) h.gsStart[ci + 1] += h.gsStart[ci];
+    h.gsList.assign(std::max(nG, 1), 0);
+    {
+        std::vector<int32_t> fillp(h.gsStart.begin(), h.gsStart.end() - 1);
+        for (int g = 0; g < nG; g++) h.gsList[fillp[h.gsrc[g]]++] = g;
+    }
     return AFVM_OK;
 }
 
@@ -282,6 +321,25 @@ int alloc_work(Ctx* c) {
     if ((st = dalloc(c, (void**)&c->scal, sizeof(double) * 8))) return st;
     cudaMemset(c->scal, 0, sizeof(double) * 8);
     if ((st = dalloc(c, (void**)&c->dtcBits, sizeof(unsigned long long)))) return st;
+    return AFVM_OK;
+}
+
+template <typename R>
+int alloc_adjoint(Ctx* c) {
+    if (c->fadj) return AFVM_OK;
+    int64_t before = c->bytes;
+    int st;
+    size_t n = c->nIC;
+    if ((st = dalloc(c, &c->fadj, sizeof(R) * (size_t)c->nF * 40))) return st;
+    if ((st = dalloc(c, &c->cbar, sizeof(R) * n * 20))) return st;
+    size_t dims[3] = {1, 3, 1};
+    for (int k = 0; k < 3; k++) {
+        if ((st = dalloc(c, &c->a1[k], sizeof(R) * n * dims[k]))) return st;
+        if ((st = dalloc(c, &c->a2[k], sizeof(R) * n * dims[k]))) return st;
+    }
+    if ((st = dalloc(c, &c->sbar, sizeof(R) * n * 5))) return st;
+    c->adjBytes = c->bytes - before;
+    c->bytes = before;
     return AFVM_OK;
 }
 
@@ -564,7 +622,25 @@ int afvm_adjoint_step(afvm_ctx* ctx, const void* rho, const void* rhoU, const vo
                       void* rhoEa, void* S_rhoa, void* S_rhoUa, void* S_rhoEa, void* stream) {
     if (!ctx) return AFVM_ERR_BAD_ARG;
     Ctx* c = reinterpret_cast<Ctx*>(ctx);
-    return fail(c, AFVM_ERR_UNSUPPORTED, "adjoint not built yet");
+    if (!rho || !rhoU || !rhoE || !rhoNa || !rhoUNa || !rhoENa || !rhoa || !rhoUa || !rhoEa)
+        return fail(c, AFVM_ERR_BAD_ARG, "null pointer");
+    if (dtca != 0.0) return fail(c, AFVM_ERR_UNSUPPORTED, "dtca != 0 (the CFL-sum output has no adjoint here)");
+    if (!std::isfinite(dt) || !std::isfinite(obja)) return fail(c, AFVM_ERR_BAD_ARG, "non-finite dt or obja");
+    DeviceGuard dg(c->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    int st = (c->precision == AFVM_FP64) ? alloc_adjoint<double>(c) : alloc_adjoint<float>(c);
+    if (st) return st;
+    if (c->precision == AFVM_FP64)
+        return adjoint_step_dev<double>(c, (const double*)rho, (const double*)rhoU, (const double*)rhoE, dt,
+                                        (const double*)S_rho, (const double*)S_rhoU, (const double*)S_rhoE,
+                                        (const double*)rhoNa, (const double*)rhoUNa, (const double*)rhoENa, obja,
+                                        (double*)rhoa, (double*)rhoUa, (double*)rhoEa, (double*)S_rhoa,
+                                        (double*)S_rhoUa, (double*)S_rhoEa, s);
+    return adjoint_step_dev<float>(c, (const float*)rho, (const float*)rhoU, (const float*)rhoE, dt,
+                                   (const float*)S_rho, (const float*)S_rhoU, (const float*)S_rhoE,
+                                   (const float*)rhoNa, (const float*)rhoUNa, (const float*)rhoENa, obja,
+                                   (float*)rhoa, (float*)rhoUa, (float*)rhoEa, (float*)S_rhoa, (float*)S_rhoUa,
+                                   (float*)S_rhoEa, s);
 }
 
 int afvm_sensitivity(afvm_ctx* ctx, int32_t nArrays, const double* const* grad, const double* const* pert,

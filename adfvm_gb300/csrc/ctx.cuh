@@ -41,6 +41,13 @@ struct MeshDev {
     const int32_t* accf;      // face id, or ~face id on the neighbour side
     const R* accw;            // A/V_L (owner side) or A/V_R (neighbour side)
     const R* vol;             // nIC
+    // adjoint tables
+    const R* wpf;             // nF  A/V_L per face
+    const R* wnf;             // nIF A/V_R per internal face
+    const R* gwb;             // 6 x nIC: w' of the neighbour's slot that points back at this cell
+    const int32_t* gsStart;   // nIC + 1: ghosts whose source is the cell, CSR offsets
+    const int32_t* gsList;    // nG ghost ids ordered by source cell
+    const int32_t* gslot;     // nG: slot of the ghost's face in its owner's cellFaces
 };
 
 // kernel ids for the optional per-launch event timing (afvm_profile_*)
@@ -81,7 +88,11 @@ struct Ctx {
     std::vector<int> ghostPatchOffset;   // first ghost index of each patch (sorted order)
     std::vector<int> bcKinds;            // per patch: U,T,p kinds
     // adjoint buffers (allocated on first use)
-    void* adj = nullptr;
+    void* fadj = nullptr;     // nF x 40 face adjoint records
+    void* cbar = nullptr;     // nIC x 20 cell primitive/gradient adjoints
+    void* a1[3] = {nullptr, nullptr, nullptr};
+    void* a2[3] = {nullptr, nullptr, nullptr};
+    void* sbar = nullptr;     // nIC x 5 source adjoint scratch
     int64_t adjBytes = 0;
     // device staging of the host-buffer entry point (allocated on first use)
     void* stageDev = nullptr;
@@ -121,6 +132,15 @@ int adjoint_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double 
                      const R* Srho, const R* SrhoU, const R* SrhoE,
                      const R* rhoNa, const R* rhoUNa, const R* rhoENa, double obja,
                      R* rhoa, R* rhoUa, R* rhoEa, R* Srhoa, R* SrhoUa, R* SrhoEa, cudaStream_t s);
+
+template <typename R>
+void launch_prim_grad(Ctx* c, const R* r, const R* ru, const R* re, cudaStream_t s);
+template <typename R>
+void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const R* const* u0, const R* const* u1,
+                        const R* const* u2, const R* Sr, const R* Su, const R* Se, R* const* out, cudaStream_t s);
+template <typename R>
+void default_sources(Ctx* c, const R*& Srho, const R*& SrhoU, const R*& SrhoE);
+static inline int nblocks(long long n) { return (int)((n + BLOCK - 1) / BLOCK); }
 
 template <typename R> inline const MeshDev<R>& meshOf(const Ctx* c);
 template <> inline const MeshDev<double>& meshOf<double>(const Ctx* c) { return c->m64; }

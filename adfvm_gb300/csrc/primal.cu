@@ -13,6 +13,7 @@
 // (rho (n), rhoU (n x 3), rhoE (n)).
 #include <cuda_runtime.h>
 #include "ctx.cuh"
+#include "facedev.cuh"
 
 namespace afvm {
 
@@ -100,81 +101,11 @@ __global__ void __launch_bounds__(BLOCK) k_flux(MeshDev<R> m, Phys P, const R* _
                                                 R* __restrict__ fflux, int inviscid) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= m.nF) return;
-    const size_t nF = m.nF;
     int kind = (f < m.nIF) ? FACE_INTERNAL : (int)m.fkind[f - m.nIF];
-    int iP = m.own[f], iN = m.nbr[f];
-    int iNg = (f < m.nIF) ? iN : m.gsrc[iN - m.nIC];   // ghost gradient = copy of its source
-    const R* rP = rec + (size_t)iP * REC;
-    const R* rN = rec + (size_t)iN * REC;
-    const R* rNg = rec + (size_t)iNg * REC;
-    R UP[3] = {rP[0], rP[1], rP[2]}, TP = rP[R_T], pP = rP[R_P];
-    R UN[3] = {rN[0], rN[1], rN[2]}, TN = rN[R_T], pN = rN[R_P];
-    R gUP[9], gUN[9], gTP[3], gTN[3], gpP[3], gpN[3];
-    for (int k = 0; k < 9; k++) { gUP[k] = rP[R_GU + k]; gUN[k] = rNg[R_GU + k]; }
-    for (int k = 0; k < 3; k++) {
-        gTP[k] = rP[R_GT + k]; gTN[k] = rNg[R_GT + k];
-        gpP[k] = rP[R_GP + k]; gpN[k] = rNg[R_GP + k];
-    }
-    R N[3] = {m.nrm[f], m.nrm[nF + f], m.nrm[2 * nF + f]};
-    R F[5];
-    R TF, UF[3];
-    R gTF[3], gUF[9];
-    if (kind == FACE_BOUNDARY) {
-        // RCF.boundaryFlux (density.py:307-331) with RCF.getFlux (density.py:184-190)
-        R rho, rhoU[3], rhoE;
-        conservative<R>(P, UN, TN, pN, rho, rhoU, rhoE);
-        R Un = dot3(UN, N);
-        F[0] = rho * Un;
-        for (int k = 0; k < 3; k++) F[1 + k] = rhoU[k] * Un + pN * N[k];
-        F[4] = (rhoE + pN) * Un;
-        TF = TN;
-        for (int k = 0; k < 3; k++) { UF[k] = UN[k]; gTF[k] = gTN[k]; }
-        for (int k = 0; k < 9; k++) gUF[k] = gUN[k];
-    } else {
-        R lw0 = m.lw[f];
-        R qw0[3] = {m.qw[f], m.qw[nF + f], m.qw[2 * nF + f]};
-        R ULF[3], TLF, pLF;
-        for (int k = 0; k < 3; k++) ULF[k] = recon<R>(UP[k], UN[k], gUP + 3 * k, lw0, qw0);
-        TLF = recon<R>(TP, TN, gTP, lw0, qw0);
-        pLF = recon<R>(pP, pN, gpP, lw0, qw0);
-        R rhoL, rhoUL[3], rhoEL;
-        conservative<R>(P, ULF, TLF, pLF, rhoL, rhoUL, rhoEL);
-        R URF[3], TRF, pRF;
-        int solver;
-        if (kind == FACE_CHARACTERISTIC) {
-            for (int k = 0; k < 3; k++) URF[k] = UN[k];
-            TRF = TN; pRF = pN;
-            solver = P.briemann;
-        } else {
-            R lw1 = m.lw[nF + f];
-            R qw1[3] = {m.qw[3 * nF + f], m.qw[4 * nF + f], m.qw[5 * nF + f]};
-            for (int k = 0; k < 3; k++) URF[k] = recon<R>(UN[k], UP[k], gUN + 3 * k, lw1, qw1);
-            TRF = recon<R>(TN, TP, gTN, lw1, qw1);
-            pRF = recon<R>(pN, pP, gpN, lw1, qw1);
-            solver = P.riemann;
-        }
-        R rhoR, rhoUR[3], rhoER;
-        conservative<R>(P, URF, TRF, pRF, rhoR, rhoUR, rhoER);
-        if (solver == AFVM_RIEMANN_ROE)
-            roe<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, N, F);
-        else
-            laxf<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, rhoUL, rhoUR, rhoEL, rhoER, N, F);
-        if (kind == FACE_CHARACTERISTIC) {
-            TF = TN;
-            for (int k = 0; k < 3; k++) { UF[k] = UN[k]; gTF[k] = gTN[k]; }
-            for (int k = 0; k < 9; k++) gUF[k] = gUN[k];
-        } else {
-            TF = R(0.5) * (TLF + TRF);
-            for (int k = 0; k < 3; k++) { UF[k] = R(0.5) * (ULF[k] + URF[k]); gTF[k] = R(0.5) * (gTP[k] + gTN[k]); }
-            for (int k = 0; k < 9; k++) gUF[k] = R(0.5) * (gUP[k] + gUN[k]);
-        }
-    }
-    if (!inviscid) {
-        R D[3] = {m.du[f], m.du[nF + f], m.du[2 * nF + f]};
-        viscous<R>(P, TP, TN, UP, UN, TF, UF, gTF, gUF, D, N, m.dlt[f], F);
-    }
-    R aF = sqrt(R(P.Cp) * TF * R(P.gm1));
-    R maxaF = fabs(dot3(UF, N)) + aF;
+    FaceIn<R> in;
+    load_face<R>(m, rec, f, in);
+    R F[5], maxaF;
+    face_flux<R>(P, kind, inviscid != 0, in, F, maxaF);
     R* out = fflux + (size_t)f * FREC;
     for (int k = 0; k < 5; k++) out[k] = F[k];
     out[5] = maxaF;
@@ -304,7 +235,54 @@ __global__ void k_finish(const double* partials, int nPartials, const unsigned l
     }
 }
 
-static inline int nblocks(long long n) { return (int)((n + BLOCK - 1) / BLOCK); }
+
+template <typename R>
+void launch_prim_grad(Ctx* c, const R* r, const R* ru, const R* re, cudaStream_t s) {
+    const MeshDev<R>& m = meshOf<R>(c);
+    R* rec = (R*)c->rec;
+    {
+        ProfScope ps(c, KID_PRIM, s);
+        k_prim<R><<<nblocks(m.nIC + m.nG), BLOCK, 0, s>>>(m, c->phys, r, ru, re, rec);
+    }
+    {
+        ProfScope ps(c, KID_GRAD, s);
+        k_grad<R><<<nblocks(m.nIC), BLOCK, 0, s>>>(m, rec);
+    }
+}
+
+// faces -> fluxes, then the gather + stage update u_{st+1} = ... (timestep.py:35-45)
+template <typename R>
+void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const R* const* u0, const R* const* u1,
+                        const R* const* u2, const R* Sr, const R* Su, const R* Se, R* const* out, cudaStream_t s) {
+    const MeshDev<R>& m = meshOf<R>(c);
+    const Phys& P = c->phys;
+    R* rec = (R*)c->rec;
+    R* ff = (R*)c->fflux;
+    int inviscid = (P.muModel == AFVM_MU_CONSTANT && P.mu0 == 0.0) ? 1 : 0;
+    {
+        ProfScope ps(c, KID_FLUX, s);
+        k_flux<R><<<nblocks(m.nF), BLOCK, 0, s>>>(m, P, rec, ff, inviscid);
+    }
+    int nb = nblocks(m.nIC);
+    ProfScope ps(c, KID_UPDATE, s);
+    if (st == 0)
+        k_update<R, 0><<<nb, BLOCK, 0, s>>>(m, ff, dt, dtDev, u0[0], u0[1], u0[2], nullptr, nullptr, nullptr, nullptr,
+                                            nullptr, nullptr, Sr, Su, Se, out[0], out[1], out[2], c->dtcBits);
+    else if (st == 1)
+        k_update<R, 1><<<nb, BLOCK, 0, s>>>(m, ff, dt, dtDev, u0[0], u0[1], u0[2], u1[0], u1[1], u1[2], nullptr,
+                                            nullptr, nullptr, Sr, Su, Se, out[0], out[1], out[2], c->dtcBits);
+    else
+        k_update<R, 2><<<nb, BLOCK, 0, s>>>(m, ff, dt, dtDev, u0[0], u0[1], u0[2], nullptr, nullptr, nullptr, u2[0],
+                                            u2[1], u2[2], Sr, Su, Se, out[0], out[1], out[2], c->dtcBits);
+}
+
+template <typename R>
+void default_sources(Ctx* c, const R*& Srho, const R*& SrhoU, const R*& SrhoE) {
+    const R* zs = (const R*)c->zeroS;
+    if (!Srho) Srho = zs;
+    if (!SrhoU) SrhoU = zs + c->nIC;
+    if (!SrhoE) SrhoE = zs + 4 * (size_t)c->nIC;
+}
 
 template <typename R>
 int primal_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double dt, const double* dtDev,
@@ -312,23 +290,18 @@ int primal_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double d
                     double* dtcDev, double* objDev, cudaStream_t s) {
     const MeshDev<R>& m = meshOf<R>(c);
     const Phys& P = c->phys;
-    R* rec = (R*)c->rec;
-    R* ff = (R*)c->fflux;
-    const R* zs = (const R*)c->zeroS;
-    if (!Srho) Srho = zs;
-    if (!SrhoU) SrhoU = zs + c->nIC;
-    if (!SrhoE) SrhoE = zs + 4 * (size_t)c->nIC;
-    int inviscid = (P.muModel == AFVM_MU_CONSTANT && P.mu0 == 0.0) ? 1 : 0;
+    default_sources<R>(c, Srho, SrhoU, SrhoE);
     R* u1[3] = {(R*)c->u1[0], (R*)c->u1[1], (R*)c->u1[2]};
     R* u2[3] = {(R*)c->u2[0], (R*)c->u2[1], (R*)c->u2[2]};
+    R* outN[3] = {rhoN, rhoUN, rhoEN};
+    const R* u0c[3] = {rho, rhoU, rhoE};
+    const R* u1c[3] = {u1[0], u1[1], u1[2]};
+    const R* u2c[3] = {u2[0], u2[1], u2[2]};
     cudaMemsetAsync(c->dtcBits, 0, sizeof(unsigned long long), s);
-    const R* in[3][3] = {{rho, rhoU, rhoE}, {u1[0], u1[1], u1[2]}, {u2[0], u2[1], u2[2]}};
     int nObjBlocks = 0;
     for (int st = 0; st < 3; st++) {
-        {
-            ProfScope ps(c, KID_PRIM, s);
-            k_prim<R><<<nblocks(m.nIC + m.nG), BLOCK, 0, s>>>(m, P, in[st][0], in[st][1], in[st][2], rec);
-        }
+        const R* const* in = st == 0 ? u0c : (st == 1 ? u1c : u2c);
+        launch_prim_grad<R>(c, in[0], in[1], in[2], s);
         if (st == 1 && c->objective != AFVM_OBJ_NONE) {
             int start = 0, n = m.nIC;
             if (c->objective == AFVM_OBJ_DRAG) { start = c->objStart; n = c->objN; }
@@ -336,28 +309,12 @@ int primal_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double d
             if (nObjBlocks > c->nPartials) return fail(c, AFVM_ERR_BAD_ARG, "objective partials overflow");
             if (n > 0) {
                 ProfScope ps(c, KID_OBJECTIVE, s);
-                k_objective<R><<<nObjBlocks, BLOCK, 0, s>>>(m, P, rec, c->objective, start, n, c->partials);
+                k_objective<R><<<nObjBlocks, BLOCK, 0, s>>>(m, P, (const R*)c->rec, c->objective, start, n,
+                                                            c->partials);
             }
         }
-        {
-            ProfScope ps(c, KID_GRAD, s);
-            k_grad<R><<<nblocks(m.nIC), BLOCK, 0, s>>>(m, rec);
-        }
-        {
-            ProfScope ps(c, KID_FLUX, s);
-            k_flux<R><<<nblocks(m.nF), BLOCK, 0, s>>>(m, P, rec, ff, inviscid);
-        }
-        int nb = nblocks(m.nIC);
-        ProfScope ps(c, KID_UPDATE, s);
-        if (st == 0)
-            k_update<R, 0><<<nb, BLOCK, 0, s>>>(m, ff, dt, dtDev, rho, rhoU, rhoE, nullptr, nullptr, nullptr, nullptr, nullptr,
-                                                nullptr, Srho, SrhoU, SrhoE, u1[0], u1[1], u1[2], c->dtcBits);
-        else if (st == 1)
-            k_update<R, 1><<<nb, BLOCK, 0, s>>>(m, ff, dt, dtDev, rho, rhoU, rhoE, u1[0], u1[1], u1[2], nullptr, nullptr,
-                                                nullptr, Srho, SrhoU, SrhoE, u2[0], u2[1], u2[2], c->dtcBits);
-        else
-            k_update<R, 2><<<nb, BLOCK, 0, s>>>(m, ff, dt, dtDev, rho, rhoU, rhoE, nullptr, nullptr, nullptr, u2[0], u2[1],
-                                                u2[2], Srho, SrhoU, SrhoE, rhoN, rhoUN, rhoEN, c->dtcBits);
+        R* const* out = st == 0 ? u1 : (st == 1 ? u2 : outN);
+        launch_flux_update<R>(c, st, dt, dtDev, u0c, u1c, u2c, Srho, SrhoU, SrhoE, out, s);
     }
     {
         ProfScope ps(c, KID_FINISH, s);
@@ -405,5 +362,15 @@ template int primal_run_dev<double>(Ctx*, double*, double*, double*, int, double
                                     cudaStream_t);
 template int primal_run_dev<float>(Ctx*, float*, float*, float*, int, double, double, double, int, const float*,
                                    const float*, const float*, double*, double*, double*, cudaStream_t);
+template void launch_prim_grad<double>(Ctx*, const double*, const double*, const double*, cudaStream_t);
+template void launch_prim_grad<float>(Ctx*, const float*, const float*, const float*, cudaStream_t);
+template void launch_flux_update<double>(Ctx*, int, double, const double*, const double* const*,
+                                         const double* const*, const double* const*, const double*, const double*,
+                                         const double*, double* const*, cudaStream_t);
+template void launch_flux_update<float>(Ctx*, int, double, const double*, const float* const*, const float* const*,
+                                        const float* const*, const float*, const float*, const float*,
+                                        float* const*, cudaStream_t);
+template void default_sources<double>(Ctx*, const double*&, const double*&, const double*&);
+template void default_sources<float>(Ctx*, const float*&, const float*&, const float*&);
 
 }  // namespace afvm

@@ -259,6 +259,24 @@ class RCF(object):
         L.check(st, self._ctx, 'afvm_primal_step')
         return out[0], out[1], out[2], dtc.value, obj.value
 
+    def adjoint_step(self, rho, rhoU, rhoE, dt, seeds, obja=1.0, S=None, out=None, source_grad=True):
+        """VJP of one step on CUDA tensors (afvm_adjoint_step): the adjoint of the input state
+        (and of the sources) given the adjoint seeds of the output state and of the objective.
+        dt is held fixed, the CFL-sum output gets no seed (dtca = 0, apps/adjoint.py:268)."""
+        torch = _torch()
+        stream = torch.cuda.current_stream(rho.device).cuda_stream
+        if out is None:
+            out = (torch.empty_like(rho), torch.empty_like(rhoU), torch.empty_like(rhoE))
+        Sg = (torch.empty_like(rho), torch.empty_like(rhoU), torch.empty_like(rhoE)) if source_grad else None
+        Sp = [None, None, None] if S is None else [C.c_void_p(s.data_ptr()) for s in S]
+        vp = lambda t: C.c_void_p(t.data_ptr())
+        gp = [None, None, None] if Sg is None else [vp(t) for t in Sg]
+        st = L.lib().afvm_adjoint_step(self._ctx, vp(rho), vp(rhoU), vp(rhoE), float(dt), Sp[0], Sp[1], Sp[2],
+                                       vp(seeds[0]), vp(seeds[1]), vp(seeds[2]), 0.0, float(obja),
+                                       vp(out[0]), vp(out[1]), vp(out[2]), gp[0], gp[1], gp[2], C.c_void_p(stream))
+        L.check(st, self._ctx, 'afvm_adjoint_step')
+        return out[0], out[1], out[2], Sg
+
     def run_device(self, rho, rhoU, rhoE, nSteps, dt, S=None, record=True):
         """nSteps steps in place on CUDA tensors, dt control on the device
         (dt <- min(2*CFL/dtc, stepFactor*dt) unless fixedTimeStep). Returns device histories
