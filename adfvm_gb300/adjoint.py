@@ -1,0 +1,116 @@
+"""Adjoint driver: the reference's ``Adjoint`` (apps/adjoint.py:31-404) on the GPU.
+
+* ``Adjoint.map(*inputs)`` is the per-step adjoint function the reference builds with
+  ``primal.map.grad()`` (apps/adjoint.py:94-151): inputs are the primal step's inputs followed
+  by the adjoint seeds ``[rhoNa, rhoUNa, rhoENa, dtca, obja]`` and ``[scaling]``; outputs are
+  ``[rhoa, rhoUa, rhoEa]`` and the gradients of the source terms (``parameters = 'source'``).
+* ``Adjoint.run(...)`` is the checkpointed backward sweep (apps/adjoint.py:176-404): the
+  primal is re-run forward one checkpoint interval at a time (keeping every state of the
+  interval on the device), then the adjoint steps run backwards through it with seeds
+  dtca = 0, obja = 1; after every step the sensitivity to each perturbation is the FP64 dot
+  product of the source gradients with it (cmesh.computeSensitivity), summed over steps past
+  ``avgStart`` and divided by ``nSteps - avgStart`` as writeResult does (apps/problem.py:47-49).
+  Adjoint fields are the plain gradients of the state (the reference keeps them multiplied
+  by the cell volume, apps/adjoint.py:188; divide by the volumes to compare with its files).
+"""
+import numpy as np
+
+from .mesh import Mesh
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class Adjoint(object):
+    def __init__(self, primal, parameters='source'):
+        if parameters != 'source':
+            raise NotImplementedError("parameters other than 'source' are not implemented")
+        self.primal = primal
+        self.mesh = primal.mesh
+        self.names = [n + 'a' for n in primal.names]
+        self.nParams = 3
+
+    # ------------------------------------------------------------ per-step map
+    def map(self, *inputs, **options):
+        """The reference's adjoint step function (apps/adjoint.py:124-126, called at 291)."""
+        torch = _torch()
+        p = self.primal
+        m = self.mesh
+        nT, nS = len(Mesh.gradFields) + len(Mesh.intFields), len(m.getScalar())
+        base = 4 + nT + nS
+        nBC = len(p.getBoundaryTensor(1))
+        primal_in = inputs[:base + 3 + nBC]
+        rest = inputs[base + 3 + nBC:]
+        if len(rest) != 6:
+            raise ValueError('adjoint map: expected 3 adjoint fields, dtca, obja and scaling after the primal inputs')
+        p._apply_bc_tensors(list(primal_in[base + 3:]))
+        n = m.nInternalCells
+        dev = 'cuda:%d' % p.device
+        td = torch.float64 if p.dtype == np.float64 else torch.float32
+        T = lambda a, d: torch.as_tensor(np.ascontiguousarray(np.asarray(a).reshape(n, d)), dtype=td, device=dev)
+        x = [T(primal_in[k], d) for k, d in zip(range(3), (1, 3, 1))]
+        dt = float(np.asarray(primal_in[3]).reshape(-1)[0])
+        S = [T(primal_in[base + k], d) for k, d in zip(range(3), (1, 3, 1))]
+        seeds = [T(rest[k], d) for k, d in zip(range(3), (1, 3, 1))]
+        dtca = float(np.asarray(rest[3]).reshape(-1)[0])
+        obja = float(np.asarray(rest[4]).reshape(-1)[0])
+        if dtca != 0.0:
+            raise NotImplementedError('dtca != 0: the CFL-sum output has no adjoint')
+        r = p.adjoint_step(x[0], x[1], x[2], dt, seeds, obja=obja, S=S)
+        out = [t.cpu().numpy().astype(np.float64) for t in r[:3]]
+        return out + [t.cpu().numpy().astype(np.float64) for t in r[3]]
+
+    # ------------------------------------------------------------ the sweep
+    def run(self, fields, nSteps, dt, writeInterval, perturbations=(), avgStart=0, source=None):
+        """Checkpointed adjoint sweep on the device.
+
+        fields: initial conservative state (host arrays). dt: a float (fixed step) or the
+        per-step dt series of the primal run. perturbations: list of (dS_rho, dS_rhoU,
+        dS_rhoE) host arrays. Returns (sensitivities, adjoint fields at t0 (host), record)."""
+        torch = _torch()
+        p = self.primal
+        if nSteps % writeInterval:
+            raise ValueError('nSteps must be a multiple of writeInterval (apps/problem.py:30-31)')
+        n = self.mesh.nInternalCells
+        dev = 'cuda:%d' % p.device
+        td = torch.float64 if p.dtype == np.float64 else torch.float32
+        T = lambda a, d: torch.as_tensor(np.ascontiguousarray(np.asarray(a).reshape(n, d)), dtype=td, device=dev)
+        x0 = [T(a, d) for a, d in zip(fields, (1, 3, 1))]
+        S = None if source is None else [T(a, d) for a, d in zip(source, (1, 3, 1))]
+        dts = list(dt) if np.ndim(dt) else [float(dt)] * nSteps
+        # primal forward: keep the interval-start states (checkpoints) on the device
+        checkpoints = []
+        x = x0
+        objs = []
+        for k in range(nSteps):
+            if k % writeInterval == 0:
+                checkpoints.append([t.clone() for t in x])
+            r = p.step(x[0], x[1], x[2], dts[k], S=S)
+            objs.append(r[4])
+            x = list(r[:3])
+        perts = [[torch.as_tensor(np.ascontiguousarray(np.asarray(a, np.float64).reshape(-1)), device=dev)
+                  for a in pert] for pert in perturbations]
+        result = [0.0] * len(perts)
+        a = [torch.zeros_like(t) for t in x0]
+        sens_series = []
+        nCk = nSteps // writeInterval
+        for checkpoint in range(nCk):
+            primalIndex = nSteps - (checkpoint + 1) * writeInterval
+            states = [checkpoints[primalIndex // writeInterval]]
+            for k in range(primalIndex, primalIndex + writeInterval - 1):
+                y = states[-1]
+                states.append(list(p.step(y[0], y[1], y[2], dts[k], S=S, want_scalars=False)[:3]))
+            for step in range(writeInterval):
+                adjointIndex = writeInterval - 1 - step
+                y = states[adjointIndex]
+                r = p.adjoint_step(y[0], y[1], y[2], dts[primalIndex + adjointIndex], a, obja=1.0, S=S, out=a)
+                grads = [g.reshape(-1).double() for g in r[3]]
+                sens = [p.sensitivity(grads, pert) for pert in perts]
+                sens_series.append(sens)
+                if (nSteps - (primalIndex + adjointIndex)) > avgStart:
+                    for i, s in enumerate(sens):
+                        result[i] += s
+        out = [r / (nSteps - avgStart) for r in result]
+        return out, [t.cpu().numpy() for t in a], {'objective': objs, 'sensitivity': sens_series}

@@ -353,6 +353,8 @@ void release(Ctx* c) {
     c->eventPool.clear();
     for (void* p : c->allocs) cudaFree(p);
     c->allocs.clear();
+    if (c->sensScratch) cudaFree(c->sensScratch);
+    c->sensScratch = nullptr;
     if (prev >= 0) cudaSetDevice(prev);
 }
 
@@ -647,7 +649,8 @@ int afvm_sensitivity(afvm_ctx* ctx, int32_t nArrays, const double* const* grad, 
                      const int64_t* n, double* out, void* stream) {
     if (!ctx) return AFVM_ERR_BAD_ARG;
     Ctx* c = reinterpret_cast<Ctx*>(ctx);
-    return fail(c, AFVM_ERR_UNSUPPORTED, "sensitivity not built yet");
+    DeviceGuard dg(c->device);
+    return sensitivity_dev(c, nArrays, grad, pert, n, out, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -96,6 +96,9 @@ struct Ctx {
     int64_t adjBytes = 0;
     // device staging of the host-buffer entry point (allocated on first use)
     void* stageDev = nullptr;
+    // sensitivity reduction scratch (grown on demand)
+    void* sensScratch = nullptr;
+    size_t sensBytes = 0;
     // per-launch event timing
     bool prof = false;
     std::vector<ProfEntry> profEntries;

@@ -29,11 +29,31 @@ __device__ __noinline__ void primitive_d(const Phys& P, double rho, double r0, d
     out[3] = e * P.rCv;
 }
 
+// FP32 state: velocity and temperature in float; the internal energy rho*e = rhoE - |rhoU|^2/(2 rho)
+// (the low-Mach cancellation) and the pressure recovered in double from the float state.
+__device__ __noinline__ void primitive_f(const Phys& P, float rho, float r0, float r1, float r2, float rhoE,
+                                         float* out) {
+    float rr = 1.0f / rho;
+    out[0] = r0 * rr; out[1] = r1 * rr; out[2] = r2 * rr;
+    double q = (double)r0 * r0 + (double)r1 * r1 + (double)r2 * r2;
+    double rhoe = (double)rhoE - 0.5 * q * (double)rr;
+    out[4] = (float)(P.gm1 * rhoe);
+    out[3] = (float)(rhoe * (double)rr * P.rCv);
+}
+
 template <typename R>
-__device__ __forceinline__ void load_prim(const Phys& P, const R* rho, const R* rhoU, const R* rhoE, int c, R* out) {
-    double o[5];
-    primitive_d(P, (double)rho[c], (double)rhoU[3 * c], (double)rhoU[3 * c + 1], (double)rhoU[3 * c + 2], (double)rhoE[c], o);
-    for (int k = 0; k < 5; k++) out[k] = (R)o[k];
+__device__ __forceinline__ void load_prim(const Phys& P, const R* rho, const R* rhoU, const R* rhoE, int c, R* out);
+
+template <>
+__device__ __forceinline__ void load_prim<double>(const Phys& P, const double* rho, const double* rhoU,
+                                                  const double* rhoE, int c, double* out) {
+    primitive_d(P, rho[c], rhoU[3 * c], rhoU[3 * c + 1], rhoU[3 * c + 2], rhoE[c], out);
+}
+
+template <>
+__device__ __forceinline__ void load_prim<float>(const Phys& P, const float* rho, const float* rhoU,
+                                                 const float* rhoE, int c, float* out) {
+    primitive_f(P, rho[c], rhoU[3 * c], rhoU[3 * c + 1], rhoU[3 * c + 2], rhoE[c], out);
 }
 
 template <typename R>
@@ -200,11 +220,10 @@ __global__ void __launch_bounds__(BLOCK) k_objective(MeshDev<R> m, Phys P, const
     double v = 0.0;
     if (t < n) {
         if (kind == AFVM_OBJ_KINETIC_ENERGY) {
+            // per-cell term in the working precision R, accumulated in double
             const R* r = rec + (size_t)t * REC;
-            double U[3] = {(double)r[0], (double)r[1], (double)r[2]};
-            double T = r[R_T], p = r[R_P];
-            double rho = p / ((P.Cv * T) * P.gm1);
-            v = 0.5 * rho * (U[0] * U[0] + U[1] * U[1] + U[2] * U[2]) * (double)m.vol[t];
+            R rho = r[R_P] / ((R(P.Cv) * r[R_T]) * R(P.gm1));
+            v = (double)(R(0.5) * rho * (r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) * m.vol[t]);
         } else if (kind == AFVM_OBJ_SUM_T) {
             v = (double)rec[(size_t)t * REC + R_T];
         } else {

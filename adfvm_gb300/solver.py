@@ -277,6 +277,24 @@ class RCF(object):
         L.check(st, self._ctx, 'afvm_adjoint_step')
         return out[0], out[1], out[2], Sg
 
+    def sensitivity(self, grads, perts):
+        """sum_k <grads[k], perts[k]> in FP64 on the device (cmesh.computeSensitivity,
+        cmesh.cpp:309-340); CUDA float64 tensors."""
+        torch = _torch()
+        k = len(grads)
+        gs = [g.contiguous() for g in grads]
+        ps = [p.contiguous() for p in perts]
+        for g, p in zip(gs, ps):
+            if g.dtype != torch.float64 or p.dtype != torch.float64 or g.numel() != p.numel():
+                raise ValueError('sensitivity: float64 arrays of equal size required')
+        ga = (L._d * k)(*[C.cast(C.c_void_p(g.data_ptr()), L._d) for g in gs])
+        pa = (L._d * k)(*[C.cast(C.c_void_p(p.data_ptr()), L._d) for p in ps])
+        na = (C.c_int64 * k)(*[g.numel() for g in gs])
+        out = C.c_double()
+        stream = torch.cuda.current_stream(gs[0].device).cuda_stream
+        L.check(L.lib().afvm_sensitivity(self._ctx, k, ga, pa, na, C.byref(out), C.c_void_p(stream)), self._ctx)
+        return out.value
+
     def run_device(self, rho, rhoU, rhoE, nSteps, dt, S=None, record=True):
         """nSteps steps in place on CUDA tensors, dt control on the device
         (dt <- min(2*CFL/dtc, stepFactor*dt) unless fixedTimeStep). Returns device histories

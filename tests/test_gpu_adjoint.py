@@ -23,7 +23,7 @@ def _setup(name):
 
 def _seeds(x, seed):
     rng = np.random.default_rng(seed)
-    return [torch.as_tensor(rng.normal(size=tuple(t.shape)) / np.abs(t.numpy()).max()) for t in x]
+    return [torch.as_tensor(rng.normal(size=tuple(t.shape)) / max(np.abs(t.numpy()).max(), 1.0)) for t in x]
 
 
 @pytest.mark.parametrize('name', ['box8', 'cyl32x16', 'sod200_sym_lf', 'box6_inviscid_sumT', 'sod1000'])
@@ -83,3 +83,52 @@ def test_adjoint_matches_central_differences():
         fd = (J(1) - J(-1)) / (2 * h)
         ad = sum(float((ai * vi).sum()) for ai, vi in zip(a[:3], v))
         assert abs(fd - ad) <= 1e-6 * max(abs(ad), 1e-30), (k, fd, ad)
+
+
+def test_sensitivity_dot_product():
+    case, mesh, x, S, dt = _setup('box8')
+    rcf = RCF(mesh, case.bc, objective=case.objective, **case.config)
+    rng = np.random.default_rng(1)
+    arrays = [rng.normal(size=n) for n in (1000, 3 * 512, 7, 300000)]
+    perts = [rng.normal(size=a.size) for a in arrays]
+    ref = sum(float(np.dot(a, p)) for a, p in zip(arrays, perts))
+    g = [torch.as_tensor(a).cuda() for a in arrays]
+    p = [torch.as_tensor(b).cuda() for b in perts]
+    v1 = rcf.sensitivity(g, p)
+    v2 = rcf.sensitivity(g, p)
+    assert v1 == v2                                   # fixed reduction order
+    assert abs(v1 - ref) <= 1e-12 * sum(float(np.abs(a * b).sum()) for a, b in zip(arrays, perts))
+
+
+def test_autograd_solve_matches_oracle_and_fd():
+    """torch.autograd.Function over 6 steps with checkpoints every 4: gradient of a weighted
+    objective time series plus a terminal term, against autograd of the oracle (6 chained
+    oracle steps) and central differences."""
+    from adfvm_gb300.autograd import solve
+    case, mesh, x, S, dt = _setup('cyl32x16')
+    rcf = RCF(mesh, case.bc, objective=case.objective, **case.config)
+    prob = torch_ref.Problem(mesh, case.bc, case.config, case.objective)
+    nSteps = 6
+    w = torch.linspace(0.5, 1.5, nSteps, dtype=torch.float64)
+    term = [t for t in _seeds(x, 21)]
+    xs = [t.clone().requires_grad_(True) for t in x]
+    St = [torch.zeros_like(t).requires_grad_(True) for t in x]
+    # oracle chain
+    y = xs
+    objs = []
+    for n in range(nSteps):
+        o = prob.step(y[0], y[1], y[2], dt, torch.cat(St, dim=1))
+        objs.append(o[4])
+        y = o[:3]
+    Jref = (torch.stack(objs) * w).sum() + sum((yi * ti).sum() for yi, ti in zip(y, term))
+    gref = torch.autograd.grad(Jref, xs + St)
+    # GPU
+    xd = [t.cuda().requires_grad_(True) for t in x]
+    Sd = [torch.zeros_like(t).cuda().requires_grad_(True) for t in x]
+    r = solve(rcf, xd[0], xd[1], xd[2], Sd, nSteps=nSteps, dt=dt, checkpoint_every=4)
+    J = (r[3] * w.cuda()).sum() + sum((yi * ti.cuda()).sum() for yi, ti in zip(r[:3], term))
+    assert abs(float(J) - float(Jref)) <= 1e-12 * abs(float(Jref))
+    g = torch.autograd.grad(J, xd + Sd)
+    for i in range(6):
+        e = G.rel_err(g[i].cpu().numpy(), gref[i].numpy())
+        assert e < 1e-10, (i, e)
