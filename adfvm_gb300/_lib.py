@@ -89,6 +89,8 @@ SIGNATURES = {
     'afvm_profile_read': (C.c_int, [_v, C.c_int32, _d, C.POINTER(C.c_int64)]),
     'afvm_profile_kernel_name': (C.c_char_p, [C.c_int32]),
     'afvm_fma_peak': (C.c_int, [C.c_int32, C.c_int32, _d]),
+    'afvm_sensitivity_noalloc': (C.c_int, [C.c_int32, C.c_int32, C.POINTER(_d), C.POINTER(_d),
+                                           C.POINTER(C.c_int64), _d, _v]),
 }
 
 

@@ -6,6 +6,7 @@
 // partials[k * SENS_BLOCKS + b]; one block then adds all partials in a fixed order. The
 // result does not depend on timing, and repeated calls give identical bits.
 #include <cuda_runtime.h>
+#include <mutex>
 #include "ctx.cuh"
 
 namespace afvm {
@@ -111,4 +112,79 @@ int sensitivity_dev(Ctx* c, int nArrays, const double* const* grad, const double
     return AFVM_OK;
 }
 
+// ---------------------------------------------------------------------------------------
+// Allocation-free variant (afvm_sensitivity_noalloc).
+//
+// Some callers cannot allocate device memory: code that runs while a CUDA graph is being
+// captured (cudaMalloc is not capturable), hosts with a fixed device-memory budget that has
+// been handed out up front, or plug-ins that may not touch the allocator of the process that
+// loads them. For them the reduction's scratch (block partials, per-array block counts and
+// the result) is this file-scope device array, sized for at most
+// AFVM_SENSITIVITY_NOALLOC_MAX_ARRAYS arrays. Every GPU that loads the library keeps it
+// (~129 KB) until the process exits. All calls share it: two calls that overlap on the GPU
+// (different streams, or different host threads without ordering) race on it.
+// ---------------------------------------------------------------------------------------
+
+constexpr int NOALLOC_MAX_ARRAYS = AFVM_SENSITIVITY_NOALLOC_MAX_ARRAYS;
+constexpr size_t NOALLOC_PARTIALS = (size_t)NOALLOC_MAX_ARRAYS * SENS_BLOCKS;
+// partials, then the result, then the block counts (as doubles' worth of ints)
+constexpr size_t NOALLOC_DOUBLES = NOALLOC_PARTIALS + 1 + (NOALLOC_MAX_ARRAYS + 1) / 2;
+
+static __device__ __align__(256) double g_sens_noalloc_scratch[NOALLOC_DOUBLES];
+
+// Host code must not use the symbol itself as a device address: the device address of the
+// array is looked up once per device, with that device current, and cached here.
+static std::mutex g_noalloc_mutex;
+static double* g_noalloc_ptr[256] = {nullptr};
+
+static int noalloc_scratch(int device, double** out) {
+    if (device < 0 || device >= 256) return AFVM_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_sens_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            cudaGetLastError();
+            return AFVM_ERR_CUDA;
+        }
+        g_noalloc_ptr[device] = (double*)p;
+    }
+    *out = g_noalloc_ptr[device];
+    return AFVM_OK;
+}
+
 }  // namespace afvm
+
+extern "C" int afvm_sensitivity_noalloc(int32_t device, int32_t nArrays, const double* const* grad,
+                                        const double* const* pert, const int64_t* n, double* out, void* stream) {
+    using namespace afvm;
+    if (nArrays <= 0 || nArrays > NOALLOC_MAX_ARRAYS || !grad || !pert || !n || !out) return AFVM_ERR_BAD_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return AFVM_ERR_BAD_ARG;
+    }
+    int prev = -1;
+    cudaGetDevice(&prev);
+    if (prev != device && cudaSetDevice(device) != cudaSuccess) {
+        cudaGetLastError();
+        return AFVM_ERR_CUDA;
+    }
+    double* scratch = nullptr;
+    int st = noalloc_scratch(device, &scratch);
+    if (st == AFVM_OK) {
+        double* partials = scratch;
+        double* result = scratch + NOALLOC_PARTIALS;
+        int* nUsed = (int*)(result + 1);
+        cudaStream_t s = (cudaStream_t)stream;
+        // every partial and count read below is written earlier in this call, so nothing left by
+        // a previous call is used and nothing needs clearing
+        st = sensitivity_launch(nArrays, grad, pert, n, partials, nUsed, result, s, nullptr);
+        if (st == AFVM_OK && cudaMemcpy(out, result, sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
+            cudaGetLastError();
+            st = AFVM_ERR_CUDA;
+        }
+    }
+    if (prev >= 0 && prev != device) cudaSetDevice(prev);
+    return st;
+}

@@ -215,6 +215,21 @@ int afvm_adjoint_step(afvm_ctx* ctx, const void* rho, const void* rhoU, const vo
 int afvm_sensitivity(afvm_ctx* ctx, int32_t nArrays, const double* const* grad,
                      const double* const* pert, const int64_t* n, double* out, void* stream);
 
+/* Allocation-free form of afvm_sensitivity, for callers that cannot allocate device memory
+ * (code running under CUDA graph capture, where cudaMalloc is not allowed; hosts whose device
+ * memory budget is fixed in advance; plug-ins that must not use the host process's
+ * allocator). No counterpart in the reference. It needs no context: the grad/pert arrays
+ * live on CUDA device `device`; the scratch is a static device array of the library that
+ * holds partial sums for at most AFVM_SENSITIVITY_NOALLOC_MAX_ARRAYS arrays (about 129 KB,
+ * kept on every GPU that loads the library until the process exits). nArrays above that
+ * limit is rejected with AFVM_ERR_BAD_ARG. The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * Calls share the array: calls that overlap on the GPU race and must be ordered by the
+ * caller. Blocks until the result is in *out (host); calls no allocator. */
+#define AFVM_SENSITIVITY_NOALLOC_MAX_ARRAYS 16
+int afvm_sensitivity_noalloc(int32_t device, int32_t nArrays, const double* const* grad,
+                             const double* const* pert, const int64_t* n, double* out, void* stream);
+
 /* ---- per-launch timing (the analogue of the reference's timeFunction decorator and
  * per-step timers, adFVM/config.py:158-168, adFVM/solver.py:322-346) ----
  * afvm_profile(ctx, 1) clears the record and brackets every later kernel launch of the
