@@ -157,6 +157,163 @@ def cpu_baseline(args, threads):
                 steps, n, m.nInternalCells)}
 
 
+def measure(case, precision, args, local, dist, world, clocks):
+    """Timed primal steps and adjoint steps of one precision on the resident workload."""
+    import torch
+    from adfvm_gb300 import cases
+    from adfvm_gb300.solver import RCF
+    mesh = case.mesh
+    rcf = RCF(mesh, case.bc, objective=case.objective, precision=precision, device=local, **case.config)
+    dt_np = np.float64 if precision == 'fp64' else np.float32
+    tdt = torch.float64 if precision == 'fp64' else torch.float32
+    x = [torch.as_tensor(np.ascontiguousarray(a, dt_np)).cuda() for a in cases.conservative(case)]
+    y = [torch.empty_like(t) for t in x]
+    dt = case.dt
+    nIC, nIF, nF, nG = mesh.nInternalCells, mesh.nInternalFaces, mesh.nFaces, mesh.nGhostCells
+    es = 8 if precision == 'fp64' else 4
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        if dist:
+            t = torch.tensor([ms], device='cuda')
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    state = {'x': x, 'y': y}
+
+    def primal():
+        rcf.step(state['x'][0], state['x'][1], state['x'][2], dt, out=state['y'], want_scalars=False)
+        state['x'], state['y'] = state['y'], state['x']
+
+    seeds = [torch.ones_like(t) * 1e-3 for t in x]
+    abuf = [torch.empty_like(t) for t in x]
+
+    def adjoint():
+        xx = state['x']
+        rcf.adjoint_step(xx[0], xx[1], xx[2], dt, seeds, obja=1.0, out=abuf, source_grad=False)
+
+    for _ in range(args.warmup):
+        primal()
+        adjoint()
+    if clocks:
+        clocks.start()
+        time.sleep(0.3)
+    rcf.profile(True)
+    ms_p = timed(primal, args.steps)
+    prof = rcf.profile_read()
+    rcf.profile(True)
+    ms_a = timed(adjoint, args.steps)
+    prof_a = rcf.profile_read()
+    rcf.profile(False)
+    clk = clocks.stop() if clocks else None
+    K = args.steps
+    vp = nIC * K * world / (ms_p / 1e3) / 1e6
+    va = nIC * K * world / (ms_a / 1e3) / 1e6
+    value = nIC * K * world / ((ms_p + ms_a) / 1e3) / 1e6
+
+    # end to end through the host-buffer entry point (pinned host buffers)
+    pin = [torch.empty(tuple(t.shape), dtype=tdt, pin_memory=True).numpy() for t in x]
+    pout = [torch.empty(tuple(t.shape), dtype=tdt, pin_memory=True).numpy() for t in x]
+    for a, b in zip(pin, state['x']):
+        a[...] = b.cpu().numpy()
+    rcf.step_host(pin[0], pin[1], pin[2], dt, out=pout)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    ke = max(1, K // 2)
+    for _ in range(ke):
+        rcf.step_host(pin[0], pin[1], pin[2], dt, out=pout)
+        pin, pout = pout, pin
+    te = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([te], device='cuda')
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        te = float(t.item())
+    # adjoint through the reference-facing Adjoint.map (host arrays in and out)
+    from adfvm_gb300.adjoint import Adjoint
+    adj = Adjoint(rcf)
+    host_x = [np.ascontiguousarray(a, np.float64) for a in pin]
+    host_seeds = [np.full(a.shape, 1e-3) for a in host_x]
+    ainputs = rcf.mapInputs(*host_x, dt) + host_seeds + [np.zeros((1, 1)), np.ones((1, 1)), np.zeros((1, 1))]
+    adj.map(*ainputs)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        aout = adj.map(*ainputs)
+    ta = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([te, ta], device='cuda')
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        te, ta = float(t[0].item()), float(t[1].item())
+    state_bytes = int(sum(a.nbytes for a in pin))
+    e2e = {'value': round(nIC * ke * world / (te + ta) / 1e6, 3), 'unit': UNIT,
+           'h2d_bytes_per_step': state_bytes + int(3 * sum(a.size for a in host_x) * es),
+           'd2h_bytes_per_step': state_bytes + 16 + int(2 * sum(a.size for a in host_x) * es),
+           'path': 'primal: afvm_primal_step_host (pinned host state in/out, dtc and objective read back); '
+                   'adjoint: Adjoint.map (reference input list; state, sources, seeds in; state and source '
+                   'adjoints out)',
+           'primal_only': round(nIC * ke * world / te / 1e6, 3), 'adjoint_only': round(nIC * ke * world / ta / 1e6, 3)}
+    kernels = {k: {'ms_total': round(v[0], 4), 'launches': v[1], 'ms_avg': round(v[0] / v[1], 5)}
+               for k, v in prof.items()}
+    top = max(prof.items(), key=lambda kv: kv[1][0])[0]
+    peak, peak_kind = peaks()
+    alg = algorithmic_bytes(top, nIC, nIF, nF, nG, es)
+    avg_s = prof[top][0] / prof[top][1] / 1e3
+    achieved = alg / avg_s / 1e9
+    roofline = {'bound': 'hbm', 'kernel': top, 'achieved': round(achieved, 1), 'peak': peak,
+                'peak_source': peak_kind, 'unit': 'GB/s', 'frac': round(achieved / peak, 4),
+                'algorithmic_bytes_per_launch': int(alg), 'traffic': None}
+    return {'value': round(value, 3), 'ms_per_step': round((ms_p + ms_a) / K, 4),
+            'primal': {'value': round(vp, 3), 'ms_per_step': round(ms_p / K, 4)},
+            'adjoint': {'value': round(va, 3), 'ms_per_step': round(ms_a / K, 4)},
+            'roofline': roofline, 'kernels': kernels,
+            'adjoint_kernels': {k: {'ms_total': round(v[0], 4), 'launches': v[1], 'ms_avg': round(v[0] / v[1], 5)}
+                                for k, v in prof_a.items()},
+            'gpu_launches': int(sum(v[1] for v in prof.values()) + sum(v[1] for v in prof_a.values())),
+            'e2e': e2e, 'clocks': clk, 'device_bytes': rcf.device_bytes}
+
+
+def serving_bench(local, seconds_budget=60.0, n_requests=48, lam=20.0, seed=4):
+    """Poisson stream of sensitivity requests on boxes {16,24,32,48,64} and cylinders
+    {64x32,128x64} (100 primal + 100 adjoint steps each): served FP32 continuous batching vs
+    the plain FP64 one-at-a-time form on the first requests of the same stream."""
+    from adfvm_gb300 import serving
+    keys = ['box16', 'box24', 'box32', 'box48', 'box64', 'cyl64x32', 'cyl128x64']
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / lam, size=n_requests))
+    ks = [keys[i] for i in rng.integers(0, len(keys), size=n_requests)]
+    lib = serving.MeshLibrary()
+    for k in keys:
+        lib.get(k)
+    srv = serving.SensitivityServer(precision='fp32', device=local, k=10, nPrimal=100, library=lib)
+    srv.warm(keys)
+    reqs = [serving.Request(rid=i, key=k, seed=i, nPrimal=100, arrival=float(a)) for i, (k, a) in enumerate(zip(ks, t))]
+    st = srv.serve(reqs, realtime=True)
+    nplain = 8
+    plain = [serving.Request(rid=i, key=k, seed=i, nPrimal=100) for i, k in enumerate(ks[:nplain])]
+    sp = serving.plain_one_at_a_time(plain, lib, device=local, nPrimal=100)
+    err = max(abs(a.sensitivity - b.sensitivity) / abs(b.sensitivity) for a, b in zip(reqs[:nplain], plain))
+    return {'lambda_req_per_s': lam, 'requests': st['requests'], 'served_req_per_s': round(st['req_per_s'], 3),
+            'p50_s': round(st['p50_s'], 4), 'p99_s': round(st['p99_s'], 4),
+            'plain_fp64_req_per_s': round(sp['req_per_s'], 3),
+            'speedup_vs_plain': round(st['req_per_s'] / sp['req_per_s'], 2),
+            'max_rel_err_fp32_vs_fp64': float('%.3g' % err), 'slots': st['slots'],
+            'meshes': keys, 'steps_per_request': '100 primal + 100 adjoint (checkpoints every 10)'}
+
+
 def run_reference(args):
     rank = int(os.environ.get('RANK', '0'))
     if rank != 0:
@@ -182,6 +339,7 @@ def main():
     ap.add_argument('--workload', default='box128')
     ap.add_argument('--precision', default='fp64')
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--serving', type=int, default=1, help='1: add the serving measurement to the line')
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
@@ -195,98 +353,33 @@ def main():
         import torch.distributed as dist
         dist.init_process_group('nccl' if torch.cuda.is_available() else 'gloo')
     torch.cuda.set_device(local)
-    from adfvm_gb300.solver import RCF
 
     case = make_case(args.workload)
     mesh = case.build_mesh()
-    rcf = RCF(mesh, case.bc, objective=case.objective, precision=args.precision, device=local, **case.config)
-    dt_np = np.float64 if args.precision == 'fp64' else np.float32
-    tdt = torch.float64 if args.precision == 'fp64' else torch.float32
-    from adfvm_gb300 import cases
-    rho0, rhoU0, rhoE0 = cases.conservative(case)
-    x = [torch.as_tensor(np.ascontiguousarray(a, dt_np)).cuda() for a in (rho0, rhoU0, rhoE0)]
-    y = [torch.empty_like(t) for t in x]
-    dt = case.dt
-    nIC, nIF, nF, nG = mesh.nInternalCells, mesh.nInternalFaces, mesh.nFaces, mesh.nGhostCells
-    es = 8 if args.precision == 'fp64' else 4
-
-    def one_step(a, b):
-        return rcf.step(a[0], a[1], a[2], dt, out=b, want_scalars=False)
-
-    for _ in range(args.warmup):
-        one_step(x, y)
-        x, y = y, x
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
     clocks = ClockSampler(local)
-    clocks.start()
-    time.sleep(0.3)
-    rcf.profile(True)
-    stream = torch.cuda.current_stream()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(args.steps):
-        one_step(x, y)
-        x, y = y, x
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    prof = rcf.profile_read()
-    rcf.profile(False)
-    clk = clocks.stop()
-    if dist:
-        t = torch.tensor([ms], device='cuda')
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = nIC * args.steps * world / (ms / 1e3) / 1e6
-
-    # end to end through the host-buffer entry point (pinned host buffers)
-    pin = [torch.empty(tuple(t.shape), dtype=tdt, pin_memory=True).numpy() for t in x]
-    pout = [torch.empty(tuple(t.shape), dtype=tdt, pin_memory=True).numpy() for t in x]
-    for a, b in zip(pin, x):
-        a[...] = b.cpu().numpy()
-    rcf.step_host(pin[0], pin[1], pin[2], dt, out=pout)
-    if dist:
-        dist.barrier()
-    t0 = time.perf_counter()
-    ke = max(1, args.steps // 2)
-    for _ in range(ke):
-        rcf.step_host(pin[0], pin[1], pin[2], dt, out=pout)
-        pin, pout = pout, pin
-    te = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([te], device='cuda')
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        te = float(t.item())
-    e2e = {'value': nIC * ke * world / te / 1e6, 'unit': UNIT,
-           'h2d_bytes_per_step': int(sum(a.nbytes for a in pin)),
-           'd2h_bytes_per_step': int(sum(a.nbytes for a in pout)) + 16,
-           'path': 'afvm_primal_step_host (pinned host state in/out, dtc and objective read back)'}
-
-    launches = sum(v[1] for v in prof.values())
-    kernels = {k: {'ms_total': round(v[0], 4), 'launches': v[1], 'ms_avg': round(v[0] / v[1], 5)}
-               for k, v in prof.items()}
-    top = max(prof.items(), key=lambda kv: kv[1][0])[0]
-    peak, peak_kind = peaks()
-    alg = algorithmic_bytes(top, nIC, nIF, nF, nG, es)
-    avg_s = prof[top][0] / prof[top][1] / 1e3
-    achieved = alg / avg_s / 1e9
-    roofline = {'bound': 'hbm', 'kernel': top, 'achieved': round(achieved, 1), 'peak': peak,
-                'peak_source': peak_kind, 'unit': 'GB/s', 'frac': round(achieved / peak, 4),
-                'algorithmic_bytes_per_launch': int(alg), 'traffic': None}
-    line = {'metric': METRIC, 'value': round(value, 3), 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
-            'warmup': args.warmup, 'ms_per_step': round(ms / args.steps, 4), 'higher_is_better': True,
+    m64 = measure(case, 'fp64', args, local, dist, world, clocks)
+    m32 = measure(case, 'fp32', args, local, dist, world, None) if args.precision == 'fp64' else None
+    clk = m64.pop('clocks')
+    nIC = mesh.nInternalCells
+    line = {'metric': METRIC, 'value': m64['value'], 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': m64['ms_per_step'], 'higher_is_better': True,
             'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64' if args.precision == 'fp64' else 'f32',
-            'data': 'synthetic', 'config': dict(describe(case, args.precision),
-                                                 l2='inputs larger than L2: %.2f GB device working set' % (
-                                                     rcf.device_bytes / 1e9),
-                                                 parallelism='replicas' if world > 1 else 'single GPU',
-                                                 step='primal SSP-RK3 step (adjoint not in this number)'),
-            'roofline': roofline, 'kernels': kernels, 'gpu_launches': int(launches), 'e2e': e2e,
-            'clocks': clk}
+            'data': 'synthetic',
+            'config': dict(describe(case, args.precision),
+                           l2='inputs larger than L2: %.2f GB device working set' % (m64['device_bytes'] / 1e9),
+                           parallelism='replicas' if world > 1 else 'single GPU',
+                           step='one SSP-RK3 primal step plus its adjoint step (value = cells x steps / '
+                                '(primal + adjoint time)); primal and adjoint also reported alone'),
+            'primal': m64['primal'], 'adjoint': m64['adjoint'],
+            'roofline': m64['roofline'], 'kernels': m64['kernels'], 'adjoint_kernels': m64['adjoint_kernels'],
+            'gpu_launches': m64['gpu_launches'],
+            'e2e': m64['e2e'], 'clocks': clk}
+    if m32 is not None:
+        m32.pop('clocks', None)
+        line['fp32'] = {k: m32[k] for k in ('value', 'ms_per_step', 'primal', 'adjoint', 'roofline', 'kernels',
+                                            'adjoint_kernels', 'e2e')}
+    if args.serving and rank == 0:
+        line['serving'] = serving_bench(local)
     from adfvm_gb300 import _lib
     line['fma_peak_tflops'] = {'fp64': round(_lib.fma_peak(local, True), 2), 'fp32': round(_lib.fma_peak(local, False), 2)}
     if rank == 0 and not args.no_cpu_baseline:
