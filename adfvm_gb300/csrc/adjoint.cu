@@ -181,17 +181,18 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const
     }
     // primitive VJP (density.py:162-171)
     double rho = ur[c], rU[3] = {uu[3 * c], uu[3 * c + 1], uu[3 * c + 2]}, rE = ue[c];
-    double U[3] = {rU[0] / rho, rU[1] / rho, rU[2] / rho};
-    double E = rE / rho;
+    double rr = rcp(rho);
+    double U[3] = {rU[0] * rr, rU[1] * rr, rU[2] * rr};
+    double E = rE * rr;
     double e = E - 0.5 * (U[0] * U[0] + U[1] * U[1] + U[2] * U[2]);
     double eb = (double)pbar[R_T] * P.rCv + (double)pbar[R_P] * P.gm1 * rho;
     double rhob = (double)pbar[R_P] * P.gm1 * e;
     double Ubt[3];
     for (int k = 0; k < 3; k++) Ubt[k] = (double)pbar[k] - eb * U[k];
     double J[5];
-    for (int k = 0; k < 3; k++) J[1 + k] = Ubt[k] / rho;
-    J[4] = eb / rho;
-    J[0] = rhob - (Ubt[0] * U[0] + Ubt[1] * U[1] + Ubt[2] * U[2]) / rho - eb * E / rho;
+    for (int k = 0; k < 3; k++) J[1 + k] = Ubt[k] * rr;
+    J[4] = eb * rr;
+    J[0] = rhob - (Ubt[0] * U[0] + Ubt[1] * U[1] + Ubt[2] * U[2]) * rr - eb * E * rr;
     // SSP-RK reverse (timestep.py:35-45 transposed)
     R ain[5] = {ainr[c], ainu[3 * c], ainu[3 * c + 1], ainu[3 * c + 2], aine[c]};
     R out[5];

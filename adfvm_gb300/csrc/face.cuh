@@ -83,7 +83,7 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
         }
     }
     if (!inviscid) viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, UF, gTF, gUF, in.D, in.N, in.delta, F);
-    R aF = sqrt(R(P.Cp) * TF * R(P.gm1));
+    R aF = sqrt_(R(P.Cp) * TF * R(P.gm1));
     maxaF = fabs(dot3(UF, in.N)) + aF;
 }
 
@@ -94,13 +94,13 @@ template <typename R>
 AFVM_HD void conservative_vjp(const Phys& P, const R* U, R T, R p, R rhob, const R* rhoUb, R rhoEb, R* Ub,
                               R& Tb, R& pb) {
     R e = R(P.Cv) * T;
-    R d = e * R(P.gm1);
-    R rho = p / d;
+    R rd = rcp(e * R(P.gm1));
+    R rho = p * rd;
     R q = dot3(U, U);
     for (int k = 0; k < 3; k++) Ub[k] += rhoUb[k] * rho + rhoEb * rho * U[k];
     R rhot = rhob + dot3(rhoUb, U) + rhoEb * (e + R(0.5) * q);
-    pb += rhot / d;
-    R eb = -rhot * rho / e + rhoEb * rho;
+    pb += rhot * rd;
+    R eb = -rhot * rho * rcp(e) + rhoEb * rho;
     Tb += eb * R(P.Cv);
 }
 
@@ -116,43 +116,51 @@ AFVM_HD void recon_vjp(R b, R lw, const R* qw, R& phiCb, R& phiDb, R* gb) {
 template <typename R>
 AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR, const R* N, const R* Fb,
                      R& pLb, R& pRb, R* ULb, R* URb, R& rhoLb, R& rhoRb) {
-    const R g = R(P.gamma), gm1 = R(P.gm1), h = R(0.5);
-    // ---- forward
+    const R g = R(P.gamma), gm1 = R(P.gm1), ggm1 = R(P.gamma / P.gm1), h = R(0.5);
+    // ---- forward (as roe())
     R UnL = dot3(UL, N), UnR = dot3(UR, N);
     R rhoUnL = rhoL * UnL, rhoUnR = rhoR * UnR;
     R qL = dot3(UL, UL), qR = dot3(UR, UR);
-    R hL = g * pL / (gm1 * rhoL) + h * qL;
-    R hR = g * pR / (gm1 * rhoR) + h * qR;
-    R sL = sqrt(rhoL), sR = sqrt(rhoR);
-    R Dn = sL + sR;
+    R rrL = rcp(rhoL), rrR = rcp(rhoR);
+    R hL = ggm1 * pL * rrL + h * qL;
+    R hR = ggm1 * pR * rrR + h * qR;
+    R rsL = rsqrt_(rhoL), rsR = rsqrt_(rhoR);
+    R sL = rhoL * rsL, sR = rhoR * rsR;
+    R rD = rcp(sL + sR);
     R UF[3], dU[3];
-    for (int k = 0; k < 3; k++) UF[k] = (UL[k] * sL + UR[k] * sR) / Dn;
-    R hF = (hL * sL + hR * sR) / Dn;
+    for (int k = 0; k < 3; k++) UF[k] = (UL[k] * sL + UR[k] * sR) * rD;
+    R hF = (hL * sL + hR * sR) * rD;
     R qF = h * dot3(UF, UF);
     R a2F = gm1 * (hF - qF);
-    R aF = sqrt(a2F);
+    R raF = rsqrt_(a2F);
+    R aF = a2F * raF;
+    R ra2F = raF * raF;
     R UnF = dot3(UF, N);
     R drho = rhoR - rhoL;
     for (int k = 0; k < 3; k++) dU[k] = rhoR * UR[k] - rhoL * UL[k];
     R drhoE = (hR * rhoR - pR) - (hL * rhoL - pL);
     R l1 = fabs(UnF), l2 = fabs(UnF + aF), l3 = fabs(UnF - aF);
-    R ea = rhoUnL / rhoL - rhoUnR / rhoR;
-    R cL = sqrt(g * pL / rhoL), cR = sqrt(g * pR / rhoR);
+    R ea = UnL - UnR;
+    R c2L = g * pL * rrL, c2R = g * pR * rrR;
+    R rcL = rsqrt_(c2L), rcR = rsqrt_(c2R);
+    R cL = c2L * rcL, cR = c2R * rcR;
     R eb_ = cL - cR;
     R eps = h * fabs(ea);
     eps = eps + h * fabs(eb_);
     eps = (eps < R(0)) ? eps - R(P.small) : eps + R(P.small);
-    bool s1 = l1 < R(2) * eps, s2 = l2 < R(2) * eps, s3 = l3 < R(2) * eps;
-    R L1 = s1 ? R(0.25) * l1 * l1 / eps + eps : l1;
-    R L2 = s2 ? R(0.25) * l2 * l2 / eps + eps : l2;
-    R L3 = s3 ? R(0.25) * l3 * l3 / eps + eps : l3;
+    R eps2 = R(2) * eps;
+    bool s1 = l1 < eps2, s2 = l2 < eps2, s3 = l3 < eps2;
+    R re = (s1 || s2 || s3) ? rcp(eps) : R(0);
+    R L1 = s1 ? R(0.25) * l1 * l1 * re + eps : l1;
+    R L2 = s2 ? R(0.25) * l2 * l2 * re + eps : l2;
+    R L3 = s3 ? R(0.25) * l3 * l3 * re + eps : l3;
     R abv1 = h * (L2 + L3);
     R abv2 = h * (L2 - L3);
     R abv3 = abv1 - L1;
     R abv4 = gm1 * (qF * drho - dot3(UF, dU) + drhoE);
     R abv5 = UnF * drho - dot3(dU, N);
-    R abv6 = abv3 * abv4 / a2F - abv2 * abv5 / aF;
-    R abv7 = abv3 * abv5 - abv2 * abv4 / aF;
+    R abv6 = abv3 * abv4 * ra2F - abv2 * abv5 * raF;
+    R abv7 = abv3 * abv5 - abv2 * abv4 * raF;
     // ---- reverse
     R Fu[3] = {Fb[1], Fb[2], Fb[3]};
     R frb = Fb[0], feb = Fb[4];
@@ -166,15 +174,15 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL
     R hFb = -h * Fb[4] * abv6;
     R UnFb = h * Fb[4] * abv7;
     // abv7 = abv3*abv5 - abv2*abv4/aF
-    R abv3b = abv7b * abv5, abv5b = abv7b * abv3, abv2b = -abv7b * abv4 / aF, abv4b = -abv7b * abv2 / aF;
-    R aFb = abv7b * abv2 * abv4 / (aF * aF);
+    R abv3b = abv7b * abv5, abv5b = abv7b * abv3, abv2b = -abv7b * abv4 * raF, abv4b = -abv7b * abv2 * raF;
+    R aFb = abv7b * abv2 * abv4 * ra2F;
     // abv6 = abv3*abv4/a2F - abv2*abv5/aF
-    abv3b += abv6b * abv4 / a2F;
-    abv4b += abv6b * abv3 / a2F;
-    R a2Fb = -abv6b * abv3 * abv4 / (a2F * a2F);
-    abv2b += -abv6b * abv5 / aF;
-    abv5b += -abv6b * abv2 / aF;
-    aFb += abv6b * abv2 * abv5 / (aF * aF);
+    abv3b += abv6b * abv4 * ra2F;
+    abv4b += abv6b * abv3 * ra2F;
+    R a2Fb = -abv6b * abv3 * abv4 * ra2F * ra2F;
+    abv2b += -abv6b * abv5 * raF;
+    abv5b += -abv6b * abv2 * raF;
+    aFb += abv6b * abv2 * abv5 * ra2F;
     // abv5 = UnF*drho - dU.N
     UnFb += abv5b * drho;
     drhob += abv5b * UnF;
@@ -191,19 +199,17 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL
     R L2b = h * (abv1b + abv2b), L3b = h * (abv1b - abv2b);
     // entropy fix
     R epsb = R(0), l1b, l2b, l3b;
-    if (s1) { l1b = L1b * h * l1 / eps; epsb += L1b * (R(1) - R(0.25) * l1 * l1 / (eps * eps)); } else l1b = L1b;
-    if (s2) { l2b = L2b * h * l2 / eps; epsb += L2b * (R(1) - R(0.25) * l2 * l2 / (eps * eps)); } else l2b = L2b;
-    if (s3) { l3b = L3b * h * l3 / eps; epsb += L3b * (R(1) - R(0.25) * l3 * l3 / (eps * eps)); } else l3b = L3b;
+    if (s1) { l1b = L1b * h * l1 * re; epsb += L1b * (R(1) - R(0.25) * l1 * l1 * re * re); } else l1b = L1b;
+    if (s2) { l2b = L2b * h * l2 * re; epsb += L2b * (R(1) - R(0.25) * l2 * l2 * re * re); } else l2b = L2b;
+    if (s3) { l3b = L3b * h * l3 * re; epsb += L3b * (R(1) - R(0.25) * l3 * l3 * re * re); } else l3b = L3b;
     R eab = h * epsb * sgn(ea);
     R ebb = h * epsb * sgn(eb_);
-    R rhoUnLb = eab / rhoL, rhoUnRb = -eab / rhoR;
-    rhoLb += -eab * rhoUnL / (rhoL * rhoL);
-    rhoRb += eab * rhoUnR / (rhoR * rhoR);
+    // c = sqrt(g p / rho): dc/dp = c/(2p) = g/(2 c rho), dc/drho = -c/(2 rho)
     R cLb = ebb, cRb = -ebb;
-    pLb += cLb * g / (R(2) * cL * rhoL);
-    rhoLb += -cLb * g * pL / (R(2) * cL * rhoL * rhoL);
-    pRb += cRb * g / (R(2) * cR * rhoR);
-    rhoRb += -cRb * g * pR / (R(2) * cR * rhoR * rhoR);
+    pLb += cLb * g * h * rcL * rrL;
+    rhoLb += -cLb * h * cL * rrL;
+    pRb += cRb * g * h * rcR * rrR;
+    rhoRb += -cRb * h * cR * rrR;
     // lam = |UnF|, |UnF + aF|, |UnF - aF|
     R t2 = sgn(UnF + aF), t3 = sgn(UnF - aF);
     UnFb += l1b * sgn(UnF) + l2b * t2 + l3b * t3;
@@ -220,25 +226,25 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL
     for (int k = 0; k < 3; k++) { URb[k] += dUb[k] * rhoR; ULb[k] += -dUb[k] * rhoL; }
     // UnF = UF.N ; aF = sqrt(a2F) ; a2F = gm1 (hF - qF) ; qF = |UF|^2/2
     for (int k = 0; k < 3; k++) UFb[k] += UnFb * N[k];
-    a2Fb += aFb / (R(2) * aF);
+    a2Fb += aFb * h * raF;
     hFb += gm1 * a2Fb;
     qFb += -gm1 * a2Fb;
     for (int k = 0; k < 3; k++) UFb[k] += qFb * UF[k];
     // hF = (hL sL + hR sR)/Dn ; UF = (UL sL + UR sR)/Dn
-    hLb += hFb * sL / Dn;
-    hRb += hFb * sR / Dn;
-    R sLb = hFb * (hL - hF) / Dn, sRb = hFb * (hR - hF) / Dn;
+    hLb += hFb * sL * rD;
+    hRb += hFb * sR * rD;
+    R sLb = hFb * (hL - hF) * rD, sRb = hFb * (hR - hF) * rD;
     for (int k = 0; k < 3; k++) {
-        ULb[k] += UFb[k] * sL / Dn;
-        URb[k] += UFb[k] * sR / Dn;
-        sLb += UFb[k] * (UL[k] - UF[k]) / Dn;
-        sRb += UFb[k] * (UR[k] - UF[k]) / Dn;
+        ULb[k] += UFb[k] * sL * rD;
+        URb[k] += UFb[k] * sR * rD;
+        sLb += UFb[k] * (UL[k] - UF[k]) * rD;
+        sRb += UFb[k] * (UR[k] - UF[k]) * rD;
     }
-    rhoLb += sLb / (R(2) * sL);
-    rhoRb += sRb / (R(2) * sR);
+    rhoLb += sLb * h * rsL;
+    rhoRb += sRb * h * rsR;
     // fe = (rhoUnL hL + rhoUnR hR)/2 ; fu = (rhoUnL UL + rhoUnR UR + (pL+pR) N)/2 ; fr = (rhoUnL + rhoUnR)/2
-    rhoUnLb += h * feb * hL + h * dot3(Fu, UL) + h * frb;
-    rhoUnRb += h * feb * hR + h * dot3(Fu, UR) + h * frb;
+    R rhoUnLb = h * feb * hL + h * dot3(Fu, UL) + h * frb;
+    R rhoUnRb = h * feb * hR + h * dot3(Fu, UR) + h * frb;
     hLb += h * feb * rhoUnL;
     hRb += h * feb * rhoUnR;
     for (int k = 0; k < 3; k++) { ULb[k] += h * Fu[k] * rhoUnL; URb[k] += h * Fu[k] * rhoUnR; }
@@ -246,15 +252,15 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL
     pLb += pn;
     pRb += pn;
     // hL = g pL/(gm1 rhoL) + qL/2
-    pLb += hLb * g / (gm1 * rhoL);
-    rhoLb += -hLb * g * pL / (gm1 * rhoL * rhoL);
-    pRb += hRb * g / (gm1 * rhoR);
-    rhoRb += -hRb * g * pR / (gm1 * rhoR * rhoR);
+    pLb += hLb * ggm1 * rrL;
+    rhoLb += -hLb * ggm1 * pL * rrL * rrL;
+    pRb += hRb * ggm1 * rrR;
+    rhoRb += -hRb * ggm1 * pR * rrR * rrR;
     for (int k = 0; k < 3; k++) { ULb[k] += hLb * UL[k]; URb[k] += hRb * UR[k]; }
-    // rhoUn = rho Un ; Un = U.N
+    // rhoUn = rho Un ; Un = U.N ; eps term ea = UnL - UnR
     rhoLb += rhoUnLb * UnL;
     rhoRb += rhoUnRb * UnR;
-    R UnLb = rhoUnLb * rhoL, UnRb = rhoUnRb * rhoR;
+    R UnLb = rhoUnLb * rhoL + eab, UnRb = rhoUnRb * rhoR - eab;
     for (int k = 0; k < 3; k++) { ULb[k] += UnLb * N[k]; URb[k] += UnRb * N[k]; }
 }
 
@@ -265,7 +271,10 @@ AFVM_HD void laxf_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rho
                       R& rhoLb, R& rhoRb, R* rhoULb, R* rhoURb, R& rhoELb, R& rhoERb) {
     const R g = R(P.gamma), h = R(0.5);
     R UnL = dot3(UL, N), UnR = dot3(UR, N);
-    R cL = sqrt(g * pL / rhoL), cR = sqrt(g * pR / rhoR);
+    R rrL = rcp(rhoL), rrR = rcp(rhoR);
+    R c2L = g * pL * rrL, c2R = g * pR * rrR;
+    R rcL = rsqrt_(c2L), rcR = rsqrt_(c2R);
+    R cL = c2L * rcL, cR = c2R * rcR;
     R A = fabs(UnL) + cL, B = fabs(UnR) + cR;
     R aF = (A >= B) ? A : B;
     R ha = h * aF;
@@ -289,10 +298,10 @@ AFVM_HD void laxf_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rho
     R Ab = (A >= B) ? aFb : R(0), Bb = (A >= B) ? R(0) : aFb;
     UnLb += Ab * sgn(UnL);
     UnRb += Bb * sgn(UnR);
-    pLb += Ab * g / (R(2) * cL * rhoL);
-    rhoLb += -Ab * g * pL / (R(2) * cL * rhoL * rhoL);
-    pRb += Bb * g / (R(2) * cR * rhoR);
-    rhoRb += -Bb * g * pR / (R(2) * cR * rhoR * rhoR);
+    pLb += Ab * g * h * rcL * rrL;
+    rhoLb += -Ab * h * cL * rrL;
+    pRb += Bb * g * h * rcR * rrR;
+    rhoRb += -Bb * h * cR * rrR;
     for (int k = 0; k < 3; k++) { ULb[k] += UnLb * N[k]; URb[k] += UnRb * N[k]; }
 }
 
@@ -303,13 +312,14 @@ AFVM_HD void viscous_vjp(const Phys& P, R TL, R TR, const R* UL, const R* UR, R 
                          R& TFb, R* UFb, R* gTFb, R* gUFb) {
     R mu = viscosity<R>(P, TF);
     R kappa = mu * R(P.kFac);
-    R snT = (TR - TL) / delta;
+    R rdel = rcp(delta);
+    R snT = (TR - TL) * rdel;
     R gTD = dot3(gTF, D);
     R gT[3];
     for (int k = 0; k < 3; k++) gT[k] = gTF[k] + snT * D[k] - gTD * D[k];
     R gU[9];
     for (int i = 0; i < 3; i++) {
-        R snU = (UR[i] - UL[i]) / delta;
+        R snU = (UR[i] - UL[i]) * rdel;
         R gUD = gUF[3 * i] * D[0] + gUF[3 * i + 1] * D[1] + gUF[3 * i + 2] * D[2];
         for (int k = 0; k < 3; k++) gU[3 * i + k] = gUF[3 * i + k] + snU * D[k] - gUD * D[k];
     }
@@ -350,15 +360,15 @@ AFVM_HD void viscous_vjp(const Phys& P, R TL, R TR, const R* UL, const R* UR, R 
         }
         gUDb = -snUb;
         for (int k = 0; k < 3; k++) gUFb[3 * i + k] += gUDb * D[k];
-        URb[i] += snUb / delta;
-        ULb[i] += -snUb / delta;
+        URb[i] += snUb * rdel;
+        ULb[i] += -snUb * rdel;
     }
     R snTb = dot3(gTb, D);
     R gTDb = -snTb;
     for (int k = 0; k < 3; k++) gTFb[k] += gTb[k] + gTDb * D[k];
-    TRb += snTb / delta;
-    TLb += -snTb / delta;
-    if (P.muModel == AFVM_MU_SUTHERLAND) TFb += mub * mu * (R(1.5) / TF - R(1) / (TF + R(P.muTs)));
+    TRb += snTb * rdel;
+    TLb += -snTb * rdel;
+    if (P.muModel == AFVM_MU_SUTHERLAND) TFb += mub * mu * (R(1.5) * rcp(TF) - rcp(TF + R(P.muTs)));
 }
 
 // <Fbar, F> differentiated with respect to all 40 inputs of the face (accumulated into out)

@@ -40,10 +40,102 @@ struct Phys {
 template <typename R>
 AFVM_HD R dot3(const R* a, const R* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
 
+// ---- reciprocal and reciprocal square root
+//
+// On the GB300 the FP64 pipe runs at 1/57 of the FP32 rate, and an IEEE FP64 division or
+// square root costs about nine FP64 instructions. In double these are built here from a
+// 23-bit FP32 seed (PTX rcp.approx / rsqrt.approx on the mantissa, the exponent handled with
+// integer operations, so no FP64 conversion instruction is issued) and two Newton-Raphson
+// steps - y <- y + y (1 - x y) for 1/x, y <- y + y (1 - x y^2)/2 for 1/sqrt(x) - each of which
+// doubles the number of correct bits (23 -> 46 -> full precision): a relative error of about
+// one unit in the last place, against half a unit for the IEEE operations. Arguments outside
+// 2^[-120, 120] (and 0, inf, NaN) take the IEEE operation. In float the hardware
+// approximations are used directly (about two units in the last place).
+#if defined(__CUDACC__)
+__device__ __forceinline__ double rcp_nr(double x) {
+    int hi = __double2hiint(x);
+    unsigned lo = (unsigned)__double2loint(x);
+    int ex = (hi >> 20) & 0x7ff;
+    if (ex < 1023 - 120 || ex > 1023 + 120) return 1.0 / x;
+    unsigned mb = 0x3f800000u | (((unsigned)hi & 0xfffffu) << 3) | (lo >> 29);
+    float rf;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(__uint_as_float(mb)));
+    unsigned rb = __float_as_uint(rf);
+    long long dexp = (long long)((int)(rb >> 23) - ex + 1919);
+    unsigned long long bits = ((unsigned long long)((unsigned)hi & 0x80000000u) << 32) |
+                              ((unsigned long long)dexp << 52) | ((unsigned long long)(rb & 0x7fffffu) << 29);
+    double y = __longlong_as_double((long long)bits);
+    double e = fma(-x, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-x, y, 1.0);
+    return fma(y, e, y);
+}
+
+__device__ __forceinline__ double rsqrt_nr(double x) {
+    int hi = __double2hiint(x);
+    unsigned lo = (unsigned)__double2loint(x);
+    int ex = (hi >> 20) & 0x7ff;
+    if (hi < 0 || ex < 1023 - 120 || ex > 1023 + 120) return 1.0 / sqrt(x);
+    int u = ex - 1023;
+    int odd = u & 1;
+    // mantissa as a float in [1,2) (u even) or [2,4) (u odd)
+    unsigned mb = ((unsigned)(127 + odd) << 23) | (((unsigned)hi & 0xfffffu) << 3) | (lo >> 29);
+    float rf;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(__uint_as_float(mb)));
+    unsigned rb = __float_as_uint(rf);
+    int half = (u - odd) / 2;                       // exact: u - odd is even
+    long long dexp = (long long)((int)(rb >> 23) - 127 - half + 1023);
+    unsigned long long bits = ((unsigned long long)dexp << 52) | ((unsigned long long)(rb & 0x7fffffu) << 29);
+    double y = __longlong_as_double((long long)bits);
+    double t = y * y;
+    double e = fma(-x, t, 1.0);
+    y = fma(0.5 * y, e, y);
+    t = y * y;
+    e = fma(-x, t, 1.0);
+    return fma(0.5 * y, e, y);
+}
+#endif
+
+AFVM_HD double rcp(double x) {
+#if defined(__CUDA_ARCH__)
+    return rcp_nr(x);
+#else
+    return 1.0 / x;
+#endif
+}
+
+AFVM_HD float rcp(float x) {
+#if defined(__CUDA_ARCH__)
+    return __fdividef(1.0f, x);
+#else
+    return 1.0f / x;
+#endif
+}
+
+AFVM_HD double rsqrt_(double x) {
+#if defined(__CUDA_ARCH__)
+    return rsqrt_nr(x);
+#else
+    return 1.0 / sqrt(x);
+#endif
+}
+
+AFVM_HD float rsqrt_(float x) {
+#if defined(__CUDA_ARCH__)
+    return rsqrtf(x);
+#else
+    return 1.0f / sqrt(x);
+#endif
+}
+
+// sqrt(x) for x >= 0 as x / sqrt(x)
+template <typename R>
+AFVM_HD R sqrt_(R x) { return x > R(0) ? x * rsqrt_(x) : R(0); }
+
 // mu(T): constant, or Sutherland 1.4792e-06*T**1.5/(T+116.) (adFVM/density.py:27)
 template <typename R>
 AFVM_HD R viscosity(const Phys& P, R T) {
-    if (P.muModel == AFVM_MU_SUTHERLAND) return (R(P.muAs) * (T * sqrt(T))) / (T + R(P.muTs));
+    if (P.muModel == AFVM_MU_SUTHERLAND) return (R(P.muAs) * (T * sqrt_(T))) * rcp(T + R(P.muTs));
     return R(P.mu0);
 }
 
@@ -51,7 +143,7 @@ AFVM_HD R viscosity(const Phys& P, R T) {
 template <typename R>
 AFVM_HD void conservative(const Phys& P, const R* U, R T, R p, R& rho, R* rhoU, R& rhoE) {
     R e = R(P.Cv) * T;
-    rho = p / (e * R(P.gm1));
+    rho = p * rcp(e * R(P.gm1));
     rhoE = rho * (e + R(0.5) * dot3(U, U));
     rhoU[0] = U[0] * rho; rhoU[1] = U[1] * rho; rhoU[2] = U[2] * rho;
 }
@@ -63,43 +155,52 @@ AFVM_HD R recon(R phiC, R phiD, const R* g, R lw, const R* qw) {
     return phiF + (qw[0] * g[0] + qw[1] * g[1] + qw[2] * g[2]);
 }
 
-// riemann.eulerRoe (adFVM/riemann.py:21-70)
+// riemann.eulerRoe (adFVM/riemann.py:21-70). Divisions become products with shared
+// reciprocals; rhoUn/rho is Un (the same number in exact arithmetic).
 template <typename R>
 AFVM_HD void roe(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR,
-                                    const R* N, R* F) {
-    const R g = R(P.gamma), gm1 = R(P.gm1);
-    R rhoUnL = rhoL * dot3(UL, N), rhoUnR = rhoR * dot3(UR, N);
-    R hL = g * pL / (gm1 * rhoL) + R(0.5) * dot3(UL, UL);
-    R hR = g * pR / (gm1 * rhoR) + R(0.5) * dot3(UR, UR);
+                 const R* N, R* F) {
+    const R g = R(P.gamma), gm1 = R(P.gm1), ggm1 = R(P.gamma / P.gm1);
+    R UnL = dot3(UL, N), UnR = dot3(UR, N);
+    R rhoUnL = rhoL * UnL, rhoUnR = rhoR * UnR;
+    R rrL = rcp(rhoL), rrR = rcp(rhoR);
+    R hL = ggm1 * pL * rrL + R(0.5) * dot3(UL, UL);
+    R hR = ggm1 * pR * rrR + R(0.5) * dot3(UR, UR);
     R fr = R(0.5) * (rhoUnL + rhoUnR);
     R fu[3], UF[3], dU[3];
     for (int k = 0; k < 3; k++) fu[k] = R(0.5) * (rhoUnL * UL[k] + rhoUnR * UR[k] + (pL + pR) * N[k]);
     R fe = R(0.5) * (rhoUnL * hL + rhoUnR * hR);
-    R sL = sqrt(rhoL), sR = sqrt(rhoR);
-    R divRho = sL + sR;
-    for (int k = 0; k < 3; k++) UF[k] = (UL[k] * sL + UR[k] * sR) / divRho;
-    R hF = (hL * sL + hR * sR) / divRho;
+    R sL = rhoL * rsqrt_(rhoL), sR = rhoR * rsqrt_(rhoR);
+    R rD = rcp(sL + sR);
+    for (int k = 0; k < 3; k++) UF[k] = (UL[k] * sL + UR[k] * sR) * rD;
+    R hF = (hL * sL + hR * sR) * rD;
     R qF = R(0.5) * dot3(UF, UF);
     R a2F = gm1 * (hF - qF);
-    R aF = sqrt(a2F);
+    R raF = rsqrt_(a2F);
+    R aF = a2F * raF;
+    R ra2F = raF * raF;
     R UnF = dot3(UF, N);
     R drho = rhoR - rhoL;
     for (int k = 0; k < 3; k++) dU[k] = rhoR * UR[k] - rhoL * UL[k];
     R drhoE = (hR * rhoR - pR) - (hL * rhoL - pL);
     R lam1 = fabs(UnF), lam2 = fabs(UnF + aF), lam3 = fabs(UnF - aF);
-    R eps = R(0.5) * fabs(rhoUnL / rhoL - rhoUnR / rhoR);
-    eps = eps + R(0.5) * fabs(sqrt(g * pL / rhoL) - sqrt(g * pR / rhoR));
+    R eps = R(0.5) * fabs(UnL - UnR);
+    eps = eps + R(0.5) * fabs(sqrt_(g * pL * rrL) - sqrt_(g * pR * rrR));
     eps = (eps < R(0)) ? eps - R(P.small) : eps + R(P.small);
-    if (lam1 < R(2) * eps) lam1 = R(0.25) * lam1 * lam1 / eps + eps;
-    if (lam2 < R(2) * eps) lam2 = R(0.25) * lam2 * lam2 / eps + eps;
-    if (lam3 < R(2) * eps) lam3 = R(0.25) * lam3 * lam3 / eps + eps;
+    R eps2 = R(2) * eps;
+    if (lam1 < eps2 || lam2 < eps2 || lam3 < eps2) {
+        R re = rcp(eps);
+        if (lam1 < eps2) lam1 = R(0.25) * lam1 * lam1 * re + eps;
+        if (lam2 < eps2) lam2 = R(0.25) * lam2 * lam2 * re + eps;
+        if (lam3 < eps2) lam3 = R(0.25) * lam3 * lam3 * re + eps;
+    }
     R abv1 = R(0.5) * (lam2 + lam3);
     R abv2 = R(0.5) * (lam2 - lam3);
     R abv3 = abv1 - lam1;
     R abv4 = gm1 * (qF * drho - dot3(UF, dU) + drhoE);
     R abv5 = UnF * drho - dot3(dU, N);
-    R abv6 = abv3 * abv4 / a2F - abv2 * abv5 / aF;
-    R abv7 = abv3 * abv5 - abv2 * abv4 / aF;
+    R abv6 = abv3 * abv4 * ra2F - abv2 * abv5 * raF;
+    R abv7 = abv3 * abv5 - abv2 * abv4 * raF;
     F[0] = fr - R(0.5) * (lam1 * drho + abv6);
     for (int k = 0; k < 3; k++) F[1 + k] = fu[k] - R(0.5) * (lam1 * dU[k] + UF[k] * abv6 - abv7 * N[k]);
     F[4] = fe - R(0.5) * (lam1 * drhoE + hF * abv6 - UnF * abv7);
@@ -111,8 +212,8 @@ AFVM_HD void laxf(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R
                                      const R* rhoUL, const R* rhoUR, R rhoEL, R rhoER, const R* N, R* F) {
     const R g = R(P.gamma);
     R UnL = dot3(UL, N), UnR = dot3(UR, N);
-    R cL = sqrt(g * pL / rhoL);
-    R cR = sqrt(g * pR / rhoR);
+    R cL = sqrt_(g * pL * rcp(rhoL));
+    R cR = sqrt_(g * pR * rcp(rhoR));
     R aF = fmax(fabs(UnL) + cL, fabs(UnR) + cR);
     R ha = R(0.5) * aF;
     F[0] = R(0.5) * (rhoL * UnL + rhoR * UnR) - ha * (rhoR - rhoL);
@@ -127,13 +228,14 @@ AFVM_HD void viscous(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, 
                                         const R* gTF, const R* gUF, const R* D, const R* N, R delta, R* F) {
     R mu = viscosity<R>(P, TF);
     R kappa = mu * R(P.kFac);
-    R snT = (TR - TL) / delta;
+    R rdel = rcp(delta);
+    R snT = (TR - TL) * rdel;
     R gTD = dot3(gTF, D);
     R gT[3];
     for (int k = 0; k < 3; k++) gT[k] = gTF[k] + snT * D[k] - gTD * D[k];
     R gU[9];
     for (int i = 0; i < 3; i++) {
-        R snU = (UR[i] - UL[i]) / delta;
+        R snU = (UR[i] - UL[i]) * rdel;
         R gUD = gUF[3 * i] * D[0] + gUF[3 * i + 1] * D[1] + gUF[3 * i + 2] * D[2];
         for (int k = 0; k < 3; k++) gU[3 * i + k] = gUF[3 * i + k] + snU * D[k] - gUD * D[k];
     }

@@ -21,8 +21,9 @@ namespace afvm {
 // cell and its source cell get bit-identical values.
 __device__ __noinline__ void primitive_d(const Phys& P, double rho, double r0, double r1, double r2, double rhoE,
                                          double* out) {
-    double U0 = r0 / rho, U1 = r1 / rho, U2 = r2 / rho;
-    double E = rhoE / rho;
+    double rr = rcp(rho);
+    double U0 = r0 * rr, U1 = r1 * rr, U2 = r2 * rr;
+    double E = rhoE * rr;
     double e = E - 0.5 * (U0 * U0 + U1 * U1 + U2 * U2);
     out[0] = U0; out[1] = U1; out[2] = U2;
     out[4] = (P.gm1 * rho) * e;
@@ -33,7 +34,7 @@ __device__ __noinline__ void primitive_d(const Phys& P, double rho, double r0, d
 // (the low-Mach cancellation) and the pressure recovered in double from the float state.
 __device__ __noinline__ void primitive_f(const Phys& P, float rho, float r0, float r1, float r2, float rhoE,
                                          float* out) {
-    float rr = 1.0f / rho;
+    float rr = rcp(rho);
     out[0] = r0 * rr; out[1] = r1 * rr; out[2] = r2 * rr;
     double q = (double)r0 * r0 + (double)r1 * r1 + (double)r2 * r2;
     double rhoe = (double)rhoE - 0.5 * q * (double)rr;
