@@ -18,7 +18,9 @@
 
 namespace afvm {
 
-constexpr int FADJ = 40;   // FaceBar layout: UP3 TP pP UN3 TN pN gUP9 gTP3 gpP3 gUN9 gTN3 gpN3
+// face adjoint record, one side after the other: owner side [prims 5 | grads 15], then the
+// neighbour (ghost) side [prims 5 | grads 15]
+constexpr int FADJ = 40;
 constexpr int CBAR = 20;   // per cell: primitive adjoint (5) then gradient adjoint (15)
 
 template <typename R>
@@ -48,7 +50,8 @@ __global__ void __launch_bounds__(BLOCK) k_adj_flux(MeshDev<R> m, Phys P, const 
     face_vjp<R>(P, kind, inviscid != 0, in, Fb, b);
     const R* src = &b.UP[0];
     R* out = fadj + (size_t)f * FADJ;
-    for (int k = 0; k < FADJ; k++) out[k] = src[k];
+    for (int k = 0; k < 5; k++) { out[k] = src[k]; out[20 + k] = src[5 + k]; }
+    for (int k = 0; k < 15; k++) { out[5 + k] = src[10 + k]; out[25 + k] = src[25 + k]; }
 }
 
 template <typename R>
@@ -62,10 +65,9 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell1(MeshDev<R> m, const R* __re
         int e = m.accf[s * n + c];
         bool ownerSide = e >= 0;
         int f = ownerSide ? e : ~e;
-        const R* r = fadj + (size_t)f * FADJ;
-        int po = ownerSide ? 0 : 5, go = ownerSide ? 10 : 25;
-        for (int k = 0; k < 5; k++) acc[k] += r[po + k];
-        for (int k = 0; k < 15; k++) acc[5 + k] += r[go + k];
+        R v[20];
+        load_vec(fadj + (size_t)f * FADJ + (ownerSide ? 0 : 20), v, 20);
+        for (int k = 0; k < 20; k++) acc[k] += v[k];
     }
     // gradient adjoints of the ghosts whose gradient is a copy of this cell's
     for (int q = m.gsStart[c]; q < m.gsStart[c + 1]; q++) {
@@ -125,7 +127,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const
         int s = m.gslot[g];
         R gp[5];
         const R* r = fadj + (size_t)f * FADJ;
-        for (int k = 0; k < 5; k++) gp[k] = r[5 + k];
+        for (int k = 0; k < 5; k++) gp[k] = r[20 + k];
         R sn[3] = {m.gsn[(3 * s) * n + o], m.gsn[(3 * s + 1) * n + o], m.gsn[(3 * s + 2) * n + o]};
         R w = m.gw[s * n + o];
         R pb[5];

@@ -5,15 +5,36 @@
 
 namespace afvm {
 
+// 16-byte vector loads of n values (n a multiple of 4 floats / 2 doubles; p 16-byte aligned)
+__device__ __forceinline__ void load_vec(const double* __restrict__ p, double* o, int n) {
+#pragma unroll
+    for (int i = 0; i < n; i += 2) {
+        double2 v = __ldg(reinterpret_cast<const double2*>(p + i));
+        o[i] = v.x; o[i + 1] = v.y;
+    }
+}
+__device__ __forceinline__ void load_vec(const float* __restrict__ p, float* o, int n) {
+#pragma unroll
+    for (int i = 0; i < n; i += 4) {
+        float4 v = __ldg(reinterpret_cast<const float4*>(p + i));
+        o[i] = v.x; o[i + 1] = v.y; o[i + 2] = v.z; o[i + 3] = v.w;
+    }
+}
+
 // the 55 inputs of one face: primitives and gradients of both sides, geometry
 template <typename R>
 __device__ __forceinline__ void load_face(const MeshDev<R>& m, const R* __restrict__ rec, int f, FaceIn<R>& in) {
     const size_t nF = m.nF;
     int iP = m.own[f], iN = m.nbr[f];
     int iNg = (f < m.nIF) ? iN : m.gsrc[iN - m.nIC];   // ghost gradient = copy of its source
-    const R* rP = rec + (size_t)iP * REC;
-    const R* rN = rec + (size_t)iN * REC;
-    const R* rNg = rec + (size_t)iNg * REC;
+    R rP[REC], rN[REC], rNg[REC];
+    load_vec(rec + (size_t)iP * REC, rP, REC);
+    load_vec(rec + (size_t)iN * REC, rN, REC);
+    if (iNg == iN) {
+        for (int k = 0; k < REC; k++) rNg[k] = rN[k];
+    } else {
+        load_vec(rec + (size_t)iNg * REC, rNg, REC);
+    }
     for (int k = 0; k < 3; k++) { in.UP[k] = rP[k]; in.UN[k] = rN[k]; }
     in.TP = rP[R_T]; in.pP = rP[R_P];
     in.TN = rN[R_T]; in.pN = rN[R_P];

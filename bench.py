@@ -28,6 +28,16 @@ METRIC = 'primal+adjoint Mcell-steps/s on 1 GB300 vs plain; sensitivity req/s, p
 UNIT = 'Mcell-steps/s'
 
 
+def max_over_ranks(values, dist, device='cuda'):
+    """Element-wise maximum of per-rank timings (the whole-job time of a replica run)."""
+    import torch
+    if dist is None:
+        return list(values)
+    t = torch.tensor(list(values), dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
@@ -185,11 +195,7 @@ def measure(case, precision, args, local, dist, world, clocks):
         e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
-        if dist:
-            t = torch.tensor([ms], device='cuda')
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms
+        return max_over_ranks([ms], dist)[0]
 
     state = {'x': x, 'y': y}
 
@@ -237,10 +243,6 @@ def measure(case, precision, args, local, dist, world, clocks):
         rcf.step_host(pin[0], pin[1], pin[2], dt, out=pout)
         pin, pout = pout, pin
     te = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([te], device='cuda')
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        te = float(t.item())
     # adjoint through the reference-facing Adjoint.map (host arrays in and out)
     from adfvm_gb300.adjoint import Adjoint
     adj = Adjoint(rcf)
@@ -254,10 +256,7 @@ def measure(case, precision, args, local, dist, world, clocks):
     for _ in range(ke):
         aout = adj.map(*ainputs)
     ta = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([te, ta], device='cuda')
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        te, ta = float(t[0].item()), float(t[1].item())
+    te, ta = max_over_ranks([te, ta], dist)
     state_bytes = int(sum(a.nbytes for a in pin))
     e2e = {'value': round(nIC * ke * world / (te + ta) / 1e6, 3), 'unit': UNIT,
            'h2d_bytes_per_step': state_bytes + int(3 * sum(a.size for a in host_x) * es),
@@ -286,31 +285,39 @@ def measure(case, precision, args, local, dist, world, clocks):
             'e2e': e2e, 'clocks': clk, 'device_bytes': rcf.device_bytes}
 
 
-def serving_bench(local, seconds_budget=60.0, n_requests=48, lam=20.0, seed=4):
-    """Poisson stream of sensitivity requests on boxes {16,24,32,48,64} and cylinders
-    {64x32,128x64} (100 primal + 100 adjoint steps each): served FP32 continuous batching vs
-    the plain FP64 one-at-a-time form on the first requests of the same stream."""
+def serving_bench(local, n_requests=48, lams=(5.0, 20.0, 100.0, 200.0), seed=4, nplain=8):
+    """Poisson streams of sensitivity requests on boxes {16,24,32,48,64} and cylinders
+    {64x32,128x64} (100 primal + 100 adjoint steps each), lambda swept: served FP32
+    continuous batching vs the plain FP64 one-at-a-time form on the same first requests."""
     from adfvm_gb300 import serving
     keys = ['box16', 'box24', 'box32', 'box48', 'box64', 'cyl64x32', 'cyl128x64']
     rng = np.random.default_rng(seed)
-    t = np.cumsum(rng.exponential(1.0 / lam, size=n_requests))
     ks = [keys[i] for i in rng.integers(0, len(keys), size=n_requests)]
+    gaps = rng.exponential(1.0, size=n_requests)
     lib = serving.MeshLibrary()
     for k in keys:
         lib.get(k)
     srv = serving.SensitivityServer(precision='fp32', device=local, k=10, nPrimal=100, library=lib)
     srv.warm(keys)
-    reqs = [serving.Request(rid=i, key=k, seed=i, nPrimal=100, arrival=float(a)) for i, (k, a) in enumerate(zip(ks, t))]
-    st = srv.serve(reqs, realtime=True)
-    nplain = 8
+    sweep = []
+    last = None
+    for lam in lams:
+        t = np.cumsum(gaps / lam)
+        reqs = [serving.Request(rid=i, key=k, seed=i, nPrimal=100, arrival=float(a)) for i, (k, a) in enumerate(zip(ks, t))]
+        st = srv.serve(reqs, realtime=True)
+        sweep.append({'lambda': lam, 'req_per_s': round(st['req_per_s'], 3), 'p50_s': round(st['p50_s'], 4),
+                      'p99_s': round(st['p99_s'], 4)})
+        last = reqs
     plain = [serving.Request(rid=i, key=k, seed=i, nPrimal=100) for i, k in enumerate(ks[:nplain])]
     sp = serving.plain_one_at_a_time(plain, lib, device=local, nPrimal=100)
-    err = max(abs(a.sensitivity - b.sensitivity) / abs(b.sensitivity) for a, b in zip(reqs[:nplain], plain))
-    return {'lambda_req_per_s': lam, 'requests': st['requests'], 'served_req_per_s': round(st['req_per_s'], 3),
-            'p50_s': round(st['p50_s'], 4), 'p99_s': round(st['p99_s'], 4),
-            'plain_fp64_req_per_s': round(sp['req_per_s'], 3),
-            'speedup_vs_plain': round(st['req_per_s'] / sp['req_per_s'], 2),
-            'max_rel_err_fp32_vs_fp64': float('%.3g' % err), 'slots': st['slots'],
+    errs = {}
+    for a, b in zip(last[:nplain], plain):
+        e = abs(a.sensitivity - b.sensitivity) / abs(b.sensitivity)
+        errs[a.key] = max(errs.get(a.key, 0.0), float('%.3g' % e))
+    cap = max(x['req_per_s'] for x in sweep)
+    return {'sweep': sweep, 'requests_per_lambda': n_requests, 'capacity_req_per_s': cap,
+            'plain_fp64_req_per_s': round(sp['req_per_s'], 3), 'speedup_vs_plain': round(cap / sp['req_per_s'], 2),
+            'max_rel_err_fp32_vs_fp64': max(errs.values()), 'rel_err_by_mesh': errs, 'slots': len(srv.slots),
             'meshes': keys, 'steps_per_request': '100 primal + 100 adjoint (checkpoints every 10)'}
 
 
@@ -340,9 +347,14 @@ def main():
     ap.add_argument('--precision', default='fp64')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--serving', type=int, default=1, help='1: add the serving measurement to the line')
+    ap.add_argument('--study', default='', help="'precision': the FP32-vs-FP64 cylinder study (own JSON line)")
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
+    if args.study == 'precision':
+        from adfvm_gb300.studies import precision_study
+        print(json.dumps({'study': 'precision', **precision_study()}))
+        return 0
 
     import torch
     rank = int(os.environ.get('RANK', '0'))
