@@ -2,7 +2,12 @@
 objective the time average of the volume-integrated kinetic energy over the last 200 steps,
 gradient with respect to the initial state by the checkpointed adjoint (checkpoints every 20
 steps), checked against central finite differences (step 1e-6 relative to each field's
-magnitude) on 16 seeded directions."""
+magnitude) on 16 seeded random directions and one along the gradient.
+
+Random directions in a 1.3-million-dimensional state are nearly orthogonal to the gradient
+(|<g,v>| ~ 1e-4 |g| |v|), so their finite differences are dominated by the round-off of J;
+the error is therefore measured against |g| |v| (the Cauchy-Schwarz scale of <g, v>) there,
+and relative to <g, v> itself on the direction along the gradient."""
 import numpy as np
 import pytest
 import torch
@@ -41,16 +46,24 @@ def test_box64_400_steps_adjoint_vs_central_differences():
     assert abs(float(J.detach()) - J_of(x0)) <= 1e-12 * abs(float(J.detach()))
     rng = np.random.default_rng(3)
     scale = [float(t.abs().max()) for t in x0]
+    # gradient norm in the same scaled space as the directions
+    gnorm = float(torch.sqrt(sum((gi * s).pow(2).sum() for gi, s in zip(g, scale))))
     h = 1e-6
+
+    def check(v):
+        fd = (J_of([t + h * vi for t, vi in zip(x0, v)]) - J_of([t - h * vi for t, vi in zip(x0, v)])) / (2 * h)
+        ad = sum(float((gi * vi).sum()) for gi, vi in zip(g, v))
+        return fd, ad
+
     errs = []
     for k in range(16):
         v = [torch.as_tensor(rng.standard_normal(tuple(t.shape))).cuda() * s for t, s in zip(x0, scale)]
         norm = float(torch.sqrt(sum((vi / s).pow(2).sum() for vi, s in zip(v, scale))))
         v = [vi / norm for vi in v]
-        jp = J_of([t + h * vi for t, vi in zip(x0, v)])
-        jm = J_of([t - h * vi for t, vi in zip(x0, v)])
-        fd = (jp - jm) / (2 * h)
-        ad = sum(float((gi * vi).sum()) for gi, vi in zip(g, v))
-        errs.append(abs(fd - ad) / abs(ad))
-    # central differences are O(h^2) accurate; 1e-5 relative on every direction
-    assert max(errs) < 1e-5, errs
+        fd, ad = check(v)
+        errs.append(abs(fd - ad) / gnorm)
+    assert max(errs) < 1e-6, errs
+    # along the gradient: <g, v> = |g|, relative error of the finite difference itself
+    v = [gi * s * s / gnorm for gi, s in zip(g, scale)]
+    fd, ad = check(v)
+    assert abs(fd - ad) <= 1e-6 * abs(ad), (fd, ad)
