@@ -245,7 +245,7 @@ def main():
     case = make_case(args.workload)
     mesh = case.build_mesh()
     clocks = ClockSampler(local)
-    m64 = measure(case, 'fp64', args, local, dist, world, clocks)
+    m64 = measure(case, args.precision, args, local, dist, world, clocks)
     m32 = measure(case, 'fp32', args, local, dist, world, None) if args.precision == 'fp64' else None
     clk = m64.pop('clocks')
     nIC = mesh.nInternalCells
