@@ -15,7 +15,8 @@ STATUS_NAMES = {0: 'OK', 1: 'BAD_ARG', 2: 'OOM', 3: 'NONFINITE', 4: 'TIMEOUT', 5
 
 AFVM_FP64, AFVM_FP32 = 0, 1
 AFVM_PATCH_PLAIN, AFVM_PATCH_CYCLIC, AFVM_PATCH_PROCESSOR = 0, 1, 2
-AFVM_BC_ZERO_GRADIENT, AFVM_BC_FIXED_VALUE, AFVM_BC_SYMMETRY_PLANE, AFVM_BC_CYCLIC, AFVM_BC_CBC_UPT = range(5)
+AFVM_BC_ZERO_GRADIENT, AFVM_BC_FIXED_VALUE, AFVM_BC_SYMMETRY_PLANE, AFVM_BC_CYCLIC, AFVM_BC_CBC_UPT, \
+    AFVM_BC_CBC_TOTAL_PT = range(6)
 AFVM_RIEMANN_ROE, AFVM_RIEMANN_LF = 0, 1
 AFVM_MU_CONSTANT, AFVM_MU_SUTHERLAND = 0, 1
 AFVM_OBJ_NONE, AFVM_OBJ_KINETIC_ENERGY, AFVM_OBJ_DRAG, AFVM_OBJ_SUM_T = range(4)
@@ -85,6 +86,7 @@ SIGNATURES = {
                                     C.c_double, C.c_double, _v, _v, _v, _v, _v, _v, _v]),
     'afvm_sensitivity': (C.c_int, [_v, C.c_int32, C.POINTER(_d), C.POINTER(_d),
                                    C.POINTER(C.c_int64), _d, _v]),
+    'afvm_adjoint_energy': (C.c_int, [_v, _v, _v, _v, _v, _v, _v, _d, _v]),
     'afvm_profile': (C.c_int, [_v, C.c_int32]),
     'afvm_profile_read': (C.c_int, [_v, C.c_int32, _d, C.POINTER(C.c_int64)]),
     'afvm_profile_kernel_name': (C.c_char_p, [C.c_int32]),

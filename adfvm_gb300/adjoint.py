@@ -62,6 +62,10 @@ class Adjoint(object):
         out = [t.cpu().numpy().astype(np.float64) for t in r[:3]]
         return out + [t.cpu().numpy().astype(np.float64) for t in r[3]]
 
+    def computeEnergy(self, adj, state):
+        """sqrt of the adjoint energy (apps/adjoint.py:55 over cmesh.computeEnergy); device tensors."""
+        return self.primal.adjoint_energy(adj, state) ** 0.5
+
     # ------------------------------------------------------------ the sweep
     def run(self, fields, nSteps, dt, writeInterval, perturbations=(), avgStart=0, source=None):
         """Checkpointed adjoint sweep on the device.

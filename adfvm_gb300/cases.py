@@ -146,6 +146,37 @@ def cylinder(n_theta=256, n_r=128, mach=0.3, T0=300.0, p0=1e5, objective='drag:c
     return case
 
 
+def duct(n=100, Tt=310.0, pt=1.05e5, U0=50.0, T0=300.0, p0=1e5, direction=True):
+    """1-D duct on the Sod tube mesh: total-pressure inlet (CBC_TOTAL_PT, BCs.py:164-184) on
+    ``left``, characteristic outlet (CBC_UPT) on ``right``, empty sides; uniform initial flow;
+    Sutherland viscosity, Roe inside and on the characteristic patches."""
+    md = meshgen.sod_tube(n)
+    bnd = md[4]
+
+    def kind(patch, b, f):
+        nf = b['nFaces']
+        if patch == 'left':
+            d = {'type': 'CBC_TOTAL_PT', 'Tt': np.full((nf, 1), Tt), 'pt': np.full((nf, 1), pt)}
+            if direction:
+                dd = np.zeros((nf, 3)); dd[:, 0] = 1.0
+                d['direction'] = dd
+            return d
+        if patch == 'right':
+            u = np.zeros((nf, 3)); u[:, 0] = U0
+            return {'type': 'CBC_UPT', 'U0': u, 'T0': np.full((nf, 1), T0), 'p0': np.full((nf, 1), p0)}
+        return {'type': 'empty'}
+    case = Case('duct%d' % n, md, _uniform_bc(bnd, kind), None, None, None,
+                config={'fixedTimeStep': True}, objective='sum_T')
+    mesh = case.build_mesh()
+    nc = mesh.nInternalCells
+    case.U = np.zeros((nc, 3)); case.U[:, 0] = U0
+    case.T = np.full((nc, 1), T0)
+    case.p = np.full((nc, 1), p0)
+    c = math.sqrt(GAMMA * R_GAS * T0)
+    case.dt = float(0.5 * (1.0 / n) / (U0 + c))
+    return case
+
+
 def conservative(case, gamma=GAMMA, Cp=CP):
     """Initial conservative state of a case: RCF.conservative (adFVM/density.py:173-181)."""
     Cv = Cp / gamma

@@ -147,6 +147,18 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const
         }
         int kind = m.gkind[g];
         int kU = kind & 7, kT = (kind >> 3) & 7, kp = (kind >> 6) & 7;
+        if (kU == GK_TOTALPT) {
+            // transpose of Ub = (U.d) d, Tb = Tt - (U.d)^2/(2 Cp), pb = pt (T/Tt)^kappa
+            const R* rs = rec + (size_t)c * REC;      // this cell is the ghost's source (owner)
+            R d[3] = {m.gval[g], m.gval[(size_t)m.nG + g], m.gval[2 * (size_t)m.nG + g]};
+            R Tt = m.gval[3 * (size_t)m.nG + g], pt = m.gval[4 * (size_t)m.nG + g];
+            R Un = rs[0] * d[0] + rs[1] * d[1] + rs[2] * d[2];
+            R kap = R(P.gamma / P.gm1);
+            R Unb = dot3(gp, d) - gp[R_T] * Un / R(P.Cp);
+            for (int k = 0; k < 3; k++) pbar[k] += Unb * d[k];
+            pbar[R_T] += gp[R_P] * pt * kap * pow(rs[R_T] / Tt, kap - R(1)) / Tt;
+            continue;
+        }
         if (kU == GK_COPY) {
             for (int k = 0; k < 3; k++) pbar[k] += gp[k];
         } else if (kU == GK_SYM) {

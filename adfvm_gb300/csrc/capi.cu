@@ -140,6 +140,7 @@ int bc_code(int kind, bool isU) {
         case AFVM_BC_SYMMETRY_PLANE: return isU ? GK_SYM : GK_COPY;
         case AFVM_BC_FIXED_VALUE: return GK_FIXED;
         case AFVM_BC_CBC_UPT: return GK_FIXED;
+        case AFVM_BC_CBC_TOTAL_PT: return GK_TOTALPT;
         default: return -1;
     }
 }
@@ -188,9 +189,11 @@ int build_tables(Ctx* c, const afvm_mesh_tensors* M, const afvm_patch_bc* bcs, H
         if (p.nFaces < 0 || p.startFace < nIF || p.startFace + p.nFaces > nF)
             return fail(c, AFVM_ERR_BAD_ARG, "patch face range");
         if (p.kind == AFVM_PATCH_PROCESSOR) return fail(c, AFVM_ERR_UNSUPPORTED, "processor patch");
-        bool cbc = b.U == AFVM_BC_CBC_UPT || b.T == AFVM_BC_CBC_UPT || b.p == AFVM_BC_CBC_UPT;
-        if (cbc && !(b.U == AFVM_BC_CBC_UPT && b.T == AFVM_BC_CBC_UPT && b.p == AFVM_BC_CBC_UPT))
-            return fail(c, AFVM_ERR_BAD_ARG, "CBC_UPT must be set on U, T and p of a patch");
+        auto isC = [](int k) { return k == AFVM_BC_CBC_UPT || k == AFVM_BC_CBC_TOTAL_PT; };
+        bool cbc = isC(b.U) || isC(b.T) || isC(b.p);
+        if (cbc && !(b.U == b.T && b.T == b.p))
+            return fail(c, AFVM_ERR_BAD_ARG, "a characteristic BC must be set on U, T and p of a patch");
+        bool totalpt = b.U == AFVM_BC_CBC_TOTAL_PT;
         bool cyclic = p.kind == AFVM_PATCH_CYCLIC;
         if (cyclic) {
             if (p.neighbourPatch < 0 || p.neighbourPatch >= M->nPatches ||
@@ -206,6 +209,16 @@ int build_tables(Ctx* c, const afvm_mesh_tensors* M, const afvm_patch_bc* bcs, H
             h.fkind[g] = (uint8_t)(cyclic ? FACE_COUPLED : (cbc ? FACE_CHARACTERISTIC : FACE_BOUNDARY));
             h.gsrc[g] = cyclic ? h.own[M->patches[p.neighbourPatch].startFace + i] : h.own[f];
             h.gkind[g] = cU | (cT << 3) | (cp << 6);
+            if (totalpt) {
+                if (!b.T_value || !b.p_value) return fail(c, AFVM_ERR_BAD_ARG, "missing Tt or pt");
+                for (int k = 0; k < 3; k++)
+                    h.gval[(size_t)k * nG + g] = b.U_value ? b.U_value[3 * (size_t)i + k] : M->normals[3 * (size_t)f + k];
+                h.gval[3 * (size_t)nG + g] = b.T_value[i];
+                h.gval[4 * (size_t)nG + g] = b.p_value[i];
+                if (!(b.T_value[i] > 0)) return fail(c, AFVM_ERR_BAD_ARG, "Tt must be positive");
+                rank[f] = pos + i;
+                continue;
+            }
             if (cU == GK_FIXED) {
                 if (!b.U_value) return fail(c, AFVM_ERR_BAD_ARG, "missing U value");
                 for (int k = 0; k < 3; k++) h.gval[(size_t)k * nG + g] = b.U_value[3 * (size_t)i + k];
@@ -504,7 +517,7 @@ int afvm_set_bc_value(afvm_ctx* ctx, int32_t patch, int32_t field, const double*
     if (patch < 0 || patch >= c->nPatches || field < 0 || field > 2 || !values)
         return fail(c, AFVM_ERR_BAD_ARG, "afvm_set_bc_value: bad patch/field/values");
     int kind = c->bcKinds[3 * patch + field];
-    if (kind != AFVM_BC_FIXED_VALUE && kind != AFVM_BC_CBC_UPT)
+    if (kind != AFVM_BC_FIXED_VALUE && kind != AFVM_BC_CBC_UPT && kind != AFVM_BC_CBC_TOTAL_PT)
         return fail(c, AFVM_ERR_BAD_ARG, "afvm_set_bc_value: the BC has no values");
     DeviceGuard dg(c->device);
     int g0 = c->patchStart[patch] - c->nIF, n = c->patchN[patch];

@@ -15,6 +15,7 @@ constexpr int BLOCK = 256;
 constexpr int GK_COPY = 0;     // zeroGradient / empty / cyclic: value of the source cell
 constexpr int GK_FIXED = 1;    // fixedValue or CBC_UPT: stored value
 constexpr int GK_SYM = 2;      // symmetryPlane: U minus its normal component
+constexpr int GK_TOTALPT = 3;  // CBC_TOTAL_PT: U, T, p from the source cell and (direction, Tt, pt)
 
 template <typename R>
 struct MeshDev {

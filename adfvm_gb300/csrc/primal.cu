@@ -76,6 +76,20 @@ __global__ void __launch_bounds__(BLOCK) k_prim(MeshDev<R> m, Phys P, const R* _
     R v[5];
     load_prim<R>(P, rho, rhoU, rhoE, src, v);
     int kU = kind & 7, kT = (kind >> 3) & 7, kp = (kind >> 6) & 7;
+    if (kU == GK_TOTALPT) {
+        // CBC_TOTAL_PT (BCs.py:178-184): Un = U.d, Ub = Un d, Tb = Tt - Un^2/(2 Cp),
+        // pb = pt (T/Tt)^(gamma/(gamma-1)) with U, T of the owner cell
+        R d[3] = {m.gval[g], m.gval[(size_t)m.nG + g], m.gval[2 * (size_t)m.nG + g]};
+        R Tt = m.gval[3 * (size_t)m.nG + g], pt = m.gval[4 * (size_t)m.nG + g];
+        R Un = dot3(v, d);
+        R T = v[3];
+        for (int k = 0; k < 3; k++) v[k] = Un * d[k];
+        v[3] = Tt - R(0.5) * Un * Un / R(P.Cp);
+        v[4] = pt * pow(T / Tt, R(P.gamma / P.gm1));
+        R* r = rec + (size_t)t * REC;
+        for (int k = 0; k < 5; k++) r[k] = v[k];
+        return;
+    }
     if (kU == GK_FIXED) {
         for (int k = 0; k < 3; k++) v[k] = m.gval[(size_t)k * m.nG + g];
     } else if (kU == GK_SYM) {

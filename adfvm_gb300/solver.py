@@ -24,7 +24,8 @@ from .mesh import Mesh, CYCLIC_PATCHES
 _BC = {'zeroGradient': L.AFVM_BC_ZERO_GRADIENT, 'empty': L.AFVM_BC_ZERO_GRADIENT,
        'inletOutlet': L.AFVM_BC_ZERO_GRADIENT, 'calculated': L.AFVM_BC_ZERO_GRADIENT,
        'fixedValue': L.AFVM_BC_FIXED_VALUE, 'symmetryPlane': L.AFVM_BC_SYMMETRY_PLANE,
-       'slip': L.AFVM_BC_SYMMETRY_PLANE, 'cyclic': L.AFVM_BC_CYCLIC, 'CBC_UPT': L.AFVM_BC_CBC_UPT}
+       'slip': L.AFVM_BC_SYMMETRY_PLANE, 'cyclic': L.AFVM_BC_CYCLIC, 'CBC_UPT': L.AFVM_BC_CBC_UPT,
+       'CBC_TOTAL_PT': L.AFVM_BC_CBC_TOTAL_PT}
 _RIEMANN = {'eulerRoe': L.AFVM_RIEMANN_ROE, 'eulerLaxFriedrichs': L.AFVM_RIEMANN_LF}
 DEFAULTS = {'Cp': 1004.5, 'gamma': 1.4, 'Pr': 0.7, 'CFL': 1.2, 'stepFactor': 1.2,
             'riemannSolver': 'eulerRoe', 'boundaryRiemannSolver': 'eulerRoe', 'mu': None,
@@ -101,6 +102,11 @@ class RCF(object):
                 elif b['type'] == 'CBC_UPT':
                     cb = self.bc['p'][name]       # characteristicBoundary uses p's BC (density.py:333-337)
                     vals[f] = np.ascontiguousarray(cb[f + '0'], np.float64).reshape(-1, dims)
+                elif b['type'] == 'CBC_TOTAL_PT':
+                    cb = self.bc['p'][name]
+                    key = {'U': 'direction', 'T': 'Tt', 'p': 'pt'}[f]
+                    if key in cb:
+                        vals[f] = np.ascontiguousarray(cb[key], np.float64).reshape(-1, dims)
             keep.append(vals)
             ptr = lambda f: L.dptr(vals[f]) if f in vals else None
             arr[i] = L.PatchBC(_BC[kinds['U']], _BC[kinds['T']], _BC[kinds['p']], ptr('U'), ptr('T'), ptr('p'))
@@ -145,6 +151,11 @@ class RCF(object):
                 elif b['type'] == 'CBC_UPT':
                     out.extend([np.asarray(b['U0']).reshape(-1, 3), np.asarray(b['T0']).reshape(-1, 1),
                                 np.asarray(b['p0']).reshape(-1, 1)])
+                elif b['type'] == 'CBC_TOTAL_PT':
+                    # createInput order of BCs.py:168-175: Tt, pt, then direction when given
+                    out.extend([np.asarray(b['Tt']).reshape(-1, 1), np.asarray(b['pt']).reshape(-1, 1)])
+                    if 'direction' in b:
+                        out.append(np.asarray(b['direction']).reshape(-1, 3))
         return out
 
     def _apply_bc_tensors(self, vals):
@@ -167,6 +178,15 @@ class RCF(object):
                                 L.check(L.lib().afvm_set_bc_value(self._ctx, pi, k, L.dptr(v)), self._ctx)
                                 self._bcvals[pos + k] = v.copy()
                     pos += 3
+                elif b['type'] == 'CBC_TOTAL_PT':
+                    nv = 3 if 'direction' in b else 2
+                    if f == 'p':
+                        for k, field in zip(range(nv), (1, 2, 0)):      # Tt -> T, pt -> p, direction -> U
+                            v = np.ascontiguousarray(vals[pos + k], np.float64)
+                            if not np.array_equal(v, self._bcvals[pos + k]):
+                                L.check(L.lib().afvm_set_bc_value(self._ctx, pi, field, L.dptr(v)), self._ctx)
+                                self._bcvals[pos + k] = v.copy()
+                    pos += nv
         if pos != len(vals):
             raise ValueError('expected %d boundary tensors, got %d' % (pos, len(vals)))
 
@@ -293,6 +313,17 @@ class RCF(object):
         out = C.c_double()
         stream = torch.cuda.current_stream(gs[0].device).cuda_stream
         L.check(L.lib().afvm_sensitivity(self._ctx, k, ga, pa, na, C.byref(out), C.c_void_p(stream)), self._ctx)
+        return out.value
+
+    def adjoint_energy(self, adj, state):
+        """sum_c w^T A(u) w V on the device (cmesh.computeEnergy, cmesh.cpp:342-425); adj and
+        state are (rho, rhoU, rhoE) CUDA tensors. The reference's driver reports sqrt of it."""
+        torch = _torch()
+        vp = lambda t: C.c_void_p(t.data_ptr())
+        out = C.c_double()
+        stream = torch.cuda.current_stream(state[0].device).cuda_stream
+        L.check(L.lib().afvm_adjoint_energy(self._ctx, vp(adj[0]), vp(adj[1]), vp(adj[2]), vp(state[0]),
+                                            vp(state[1]), vp(state[2]), C.byref(out), C.c_void_p(stream)), self._ctx)
         return out.value
 
     def run_device(self, rho, rhoU, rhoE, nSteps, dt, S=None, record=True):

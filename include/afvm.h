@@ -123,12 +123,14 @@ typedef struct afvm_mesh_tensors {
 #define AFVM_BC_SYMMETRY_PLANE 2     /* symmetryPlane, slip               (BCs.py:120-135)         */
 #define AFVM_BC_CYCLIC         3     /* cyclic                            (BCs.py:86-95)           */
 #define AFVM_BC_CBC_UPT        4     /* characteristic U,T,p              (BCs.py:152-161)         */
+#define AFVM_BC_CBC_TOTAL_PT   5     /* characteristic total p, T         (BCs.py:164-184)         */
 
 typedef struct afvm_patch_bc {
-    int32_t U, T, p;                 /* AFVM_BC_* per field; CBC_UPT must be set on all three */
-    const double* U_value;           /* nFaces x 3 for fixedValue U, or U0 for CBC_UPT */
-    const double* T_value;           /* nFaces     for fixedValue T, or T0 for CBC_UPT */
-    const double* p_value;           /* nFaces     for fixedValue p, or p0 for CBC_UPT */
+    int32_t U, T, p;                 /* AFVM_BC_* per field; a CBC kind must be set on all three */
+    const double* U_value;           /* nFaces x 3: fixedValue U; U0 (CBC_UPT); direction
+                                        (CBC_TOTAL_PT; NULL = the face normals) */
+    const double* T_value;           /* nFaces: fixedValue T; T0 (CBC_UPT); Tt (CBC_TOTAL_PT) */
+    const double* p_value;           /* nFaces: fixedValue p; p0 (CBC_UPT); pt (CBC_TOTAL_PT) */
 } afvm_patch_bc;
 
 #define AFVM_RIEMANN_ROE 0           /* riemann.eulerRoe            (adFVM/riemann.py:21-70) */
@@ -214,6 +216,13 @@ int afvm_adjoint_step(afvm_ctx* ctx, const void* rho, const void* rhoU, const vo
  * n[k] doubles; result to *out (host) after the stream work completes. */
 int afvm_sensitivity(afvm_ctx* ctx, int32_t nArrays, const double* const* grad,
                      const double* const* pert, const int64_t* n, double* out, void* stream);
+
+/* Adjoint energy sum_c w^T A(u) w V with w = adjoint / V (cmesh.computeEnergy,
+ * adFVM/cpp/cmesh.cpp:342-425; the reference's adjoint driver reports its square root,
+ * apps/adjoint.py:55). DEVICE arrays in the context's precision: the adjoint state
+ * (rhoa, rhoUa, rhoEa) and the primal state. FP64 sum to *out (host) after the work. */
+int afvm_adjoint_energy(afvm_ctx* ctx, const void* rhoa, const void* rhoUa, const void* rhoEa,
+                        const void* rho, const void* rhoU, const void* rhoE, double* out, void* stream);
 
 /* Allocation-free form of afvm_sensitivity, for callers that cannot allocate device memory
  * (code running under CUDA graph capture, where cudaMalloc is not allowed; hosts whose device

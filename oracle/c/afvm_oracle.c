@@ -25,7 +25,7 @@
 
 #define SMALL 1e-30
 
-enum { K_COPY = 0, K_FIXED = 1, K_SYM = 2 };
+enum { K_COPY = 0, K_FIXED = 1, K_SYM = 2, K_TOTALPT = 3 };
 enum { F_INTERNAL = 0, F_COUPLED = 1, F_CHAR = 2, F_BOUNDARY = 3 };
 
 typedef struct {
@@ -223,6 +223,16 @@ static void equation(const oracle_mesh* M, const double* rho, const double* rU, 
         int kind = M->gkind[g];
         int kU = kind & 7, kT = (kind >> 3) & 7, kp = (kind >> 6) & 7;
         const double* n = M->nrm + 3 * (size_t)(M->nIF + g);
+        if (kU == K_TOTALPT) {
+            /* CBC_TOTAL_PT, BCs.py:178-184 */
+            const double* d = M->gval + 5 * (size_t)g;
+            double Tt = d[3], pt = d[4], T = r[3];
+            double Un = dot3(r, d);
+            for (int k = 0; k < 3; k++) r[k] = Un * d[k];
+            r[3] = Tt - 0.5 * Un * Un / M->Cp;
+            r[4] = pt * pow(T / Tt, M->gamma / (M->gamma - 1));
+            continue;
+        }
         if (kU == K_FIXED) for (int k = 0; k < 3; k++) r[k] = M->gval[5 * (size_t)g + k] * 1;
         else if (kU == K_SYM) {
             double un = dot3(r, n);

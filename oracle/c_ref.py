@@ -62,13 +62,13 @@ class COracle(object):
         pos = nIF
         objStart = objN = 0
         code = {'zeroGradient': 0, 'empty': 0, 'inletOutlet': 0, 'cyclic': 0, 'calculated': 0,
-                'fixedValue': 1, 'CBC_UPT': 1, 'symmetryPlane': 2, 'slip': 2}
+                'fixedValue': 1, 'CBC_UPT': 1, 'symmetryPlane': 2, 'slip': 2, 'CBC_TOTAL_PT': 3}
         for name in m.sortedPatches:
             b = m.boundary[name]
             s, n = int(b['startFace']), int(b['nFaces'])
             g = slice(s - nIF, s - nIF + n)
             kinds = {f: bc[f][name]['type'] for f in ('U', 'T', 'p')}
-            char = 'CBC_UPT' in kinds.values()
+            char = 'CBC_UPT' in kinds.values() or 'CBC_TOTAL_PT' in kinds.values()
             if b['type'] in self.CYCLIC:
                 nb = m.boundary[b['neighbourPatch']]
                 gsrc[g] = owner[int(nb['startFace']):int(nb['startFace']) + n]
@@ -80,7 +80,13 @@ class COracle(object):
             cT = 0 if kinds['T'] in ('symmetryPlane', 'slip') else code[kinds['T']]
             cp = 0 if kinds['p'] in ('symmetryPlane', 'slip') else code[kinds['p']]
             gkind[g] = cU | (cT << 3) | (cp << 6)
-            if char:
+            if kinds['p'] == 'CBC_TOTAL_PT':
+                cb = bc['p'][name]
+                gval[g, 0:3] = (np.asarray(cb['direction']).reshape(-1, 3) if 'direction' in cb
+                                else np.asarray(m.normals).reshape(-1, 3)[s:s + n])
+                gval[g, 3] = np.asarray(cb['Tt']).reshape(-1)
+                gval[g, 4] = np.asarray(cb['pt']).reshape(-1)
+            elif char:
                 cb = bc['p'][name]
                 gval[g, 0:3] = np.asarray(cb['U0']).reshape(-1, 3)
                 gval[g, 3] = np.asarray(cb['T0']).reshape(-1)

@@ -92,7 +92,7 @@ class Problem(object):
             cs = s - self.nIF + self.nIC
             fb = {f: bc[f][name] for f in ('U', 'T', 'p')}
             kinds = {f: fb[f]['type'] for f in fb}
-            char = any(k == 'CBC_UPT' for k in kinds.values())
+            char = any(k in ('CBC_UPT', 'CBC_TOTAL_PT') for k in kinds.values())
             coupled = ptype in ('cyclic', 'slidingPeriodic1D')
             if coupled:
                 nb = m.boundary[b['neighbourPatch']]
@@ -101,11 +101,17 @@ class Problem(object):
                 src = self.owner[s:s + n]
             entry = dict(name=name, start=s, n=n, cellStart=cs, type=ptype, kinds=kinds,
                          coupled=coupled, characteristic=char, src=src, bc=fb)
-            if char:
+            if char and kinds['p'] == 'CBC_UPT':
                 cb = bc['p'][name]      # characteristicBoundary uses p's BC objects (density.py:333-337)
                 entry['U0'] = _t(cb['U0']).reshape(-1, 3)
                 entry['T0'] = _t(cb['T0']).reshape(-1, 1)
                 entry['p0'] = _t(cb['p0']).reshape(-1, 1)
+            if char and kinds['p'] == 'CBC_TOTAL_PT':
+                cb = bc['p'][name]
+                entry['Tt'] = _t(cb['Tt']).reshape(-1, 1)
+                entry['pt'] = _t(cb['pt']).reshape(-1, 1)
+                entry['direction'] = (_t(cb['direction']).reshape(-1, 3) if 'direction' in cb
+                                      else self.normals[s:s + n])
             for f, dims in (('U', 3), ('T', 1), ('p', 1)):
                 if kinds[f] == 'fixedValue':
                     entry[f + '_fixed'] = _t(fb[f]['value']).reshape(-1, dims)
@@ -155,6 +161,16 @@ class Problem(object):
             s, n, src = P['start'], P['n'], P['src']
             k = P['kinds']
             nrm = self.normals[s:s + n]
+            if P['characteristic'] and 'Tt' in P:
+                # CBC_TOTAL_PT (BCs.py:178-184)
+                Uo, To = U[src], T[src]
+                d = P['direction']
+                Un = dot3(Uo, d).unsqueeze(-1)
+                Ub = Un * d
+                Tb = P['Tt'] - 0.5 * Un * Un / self.Cp
+                pb = P['pt'] * (To / P['Tt']) ** (self.gamma / (self.gamma - 1))
+                pieces.append((P['cellStart'], Ub, Tb, pb))
+                continue
             if P['characteristic']:
                 pieces.append((P['cellStart'], P['U0'] * 1, P['T0'] * 1, P['p0'] * 1))
                 continue
@@ -474,3 +490,28 @@ def vjp_step(problem, rho, rhoU, rhoE, dt, S, seeds, obja=1.0):
     g = torch.autograd.grad(J, x + [S], allow_unused=True)
     g = [torch.zeros_like(v) if gi is None else gi for gi, v in zip(g, x + [S])]
     return g[0], g[1], g[2], g[3]
+
+
+def adjoint_energy(volumes, gamma, rhoa, rhoUa, rhoEa, rho, rhoU, rhoE):
+    """cmesh.computeEnergy (adFVM/cpp/cmesh.cpp:342-425) restated in numpy."""
+    g = gamma
+    v = np.asarray(volumes).reshape(-1)
+    rho = np.asarray(rho).reshape(-1)
+    rhoE = np.asarray(rhoE).reshape(-1)
+    rhoU = np.asarray(rhoU).reshape(-1, 3)
+    u1, u2, u3 = rhoU[:, 0] / rho, rhoU[:, 1] / rho, rhoU[:, 2] / rho
+    q2 = u1 * u1 + u2 * u2 + u3 * u3
+    p = (rhoE - rho * q2 / 2) * (g - 1)
+    H = g * p / (rho * (g - 1)) + q2 / 2
+    a = np.asarray(rhoUa).reshape(-1, 3)
+    w1, w2, w3, w4, w5 = (np.asarray(rhoa).reshape(-1) / v, a[:, 0] / v, a[:, 1] / v, a[:, 2] / v,
+                          np.asarray(rhoEa).reshape(-1) / v)
+    A11, A12, A13, A14, A15 = rho, rho * u1, rho * u2, rho * u3, rhoE
+    A22, A23, A24, A25 = rho * u1 * u1 + p, rho * u1 * u2, rho * u1 * u3, rho * H * u1
+    A33, A34, A35 = rho * u2 * u2 + p, rho * u2 * u3, rho * H * u2
+    A44, A45 = rho * u3 * u3 + p, rho * H * u3
+    A55 = rho * H * H - g * p * p / (rho * (g - 1))
+    e = (A11 * w1 * w1 + A22 * w2 * w2 + A33 * w3 * w3 + A44 * w4 * w4 + A55 * w5 * w5 +
+         2 * (A12 * w1 * w2 + A13 * w1 * w3 + A14 * w1 * w4 + A15 * w1 * w5 + A23 * w2 * w3 + A24 * w2 * w4 +
+              A25 * w2 * w5 + A34 * w3 * w4 + A35 * w3 * w5 + A45 * w4 * w5)) * v
+    return float(np.sum(e))

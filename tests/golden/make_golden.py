@@ -126,6 +126,8 @@ CASES = {
     'box8': lambda: (cases.box(8, objective='kinetic_energy'), 5, [1, 2, 5], True),
     'box6_inviscid_sumT': lambda: (cases.box(6, objective='sum_T', viscous=False), 3, [1, 3], False),
     'cyl32x16': lambda: (cases.cylinder(32, 16, objective='drag:cylinder'), 5, [1, 2, 5], False),
+    'duct100_totalpt': lambda: (cases.duct(100), 40, [1, 10, 40], False),
+    'duct60_totalpt_normals': lambda: (cases.duct(60, direction=False, U0=-20.0), 20, [1, 20], False),
 }
 
 
@@ -157,10 +159,42 @@ def make_geometry():
     print('geometry ->', path, os.path.getsize(path), 'bytes')
 
 
+def make_energy():
+    """cmesh.computeEnergy (adFVM/cpp/cmesh.cpp:342-425), the reference's compiled adjoint
+    energy, on seeded adjoint fields over box6 and cyl16x8 states."""
+    refrun.load()
+    from oracle.refrun import load
+    ns = load()
+    import adFVM.mesh as rmesh
+    out = {}
+    for name, mk in [('box6', lambda: cases.box(6, objective='kinetic_energy')),
+                     ('cyl16x8', lambda: cases.cylinder(16, 8))]:
+        case = mk()
+        with tempfile.TemporaryDirectory() as d:
+            refrun.build_mesh(case.meshData, d)     # sets the builder's current mesh
+        rho, rhoU, rhoE = cases.conservative(case)
+        rng = np.random.default_rng(11)
+        n = len(rho)
+        rhoa, rhoUa, rhoEa = rng.normal(size=(n, 1)), rng.normal(size=(n, 3)), rng.normal(size=(n, 1)) * 1e-5
+
+        class Solver:
+            gamma = 1.4
+        e = rmesh.cmesh.computeEnergy(Solver(), rhoa, rhoUa, rhoEa, rho, rhoU, rhoE)
+        out[name + '/energy'] = np.array(e)
+        for k, v in dict(rhoa=rhoa, rhoUa=rhoUa, rhoEa=rhoEa, rho=rho, rhoU=rhoU, rhoE=rhoE).items():
+            out[name + '/' + k] = v
+    path = os.path.join(HERE, 'energy.npz')
+    np.savez_compressed(path, **out)
+    print('energy ->', path, {k: float(v) for k, v in out.items() if k.endswith('/energy')})
+
+
 def main(names):
     for name in names:
         if name == 'geometry':
             make_geometry()
+            continue
+        if name == 'energy':
+            make_energy()
             continue
         case, nSteps, keep, src = CASES[name]()
         out = run_case(case, nSteps, keep, src)
@@ -172,4 +206,4 @@ def main(names):
 
 
 if __name__ == '__main__':
-    main(sys.argv[1:] or (['geometry'] + list(CASES)))
+    main(sys.argv[1:] or (['geometry', 'energy'] + list(CASES)))

@@ -13,6 +13,8 @@ CASES = {
     'box8': lambda: cases.box(8, objective='kinetic_energy'),
     'box6_inviscid_sumT': lambda: cases.box(6, objective='sum_T', viscous=False),
     'cyl32x16': lambda: cases.cylinder(32, 16, objective='drag:cylinder'),
+    'duct100_totalpt': lambda: cases.duct(100),
+    'duct60_totalpt_normals': lambda: cases.duct(60, direction=False, U0=-20.0),
 }
 
 

@@ -26,7 +26,8 @@ def _seeds(x, seed):
     return [torch.as_tensor(rng.normal(size=tuple(t.shape)) / max(np.abs(t.numpy()).max(), 1.0)) for t in x]
 
 
-@pytest.mark.parametrize('name', ['box8', 'cyl32x16', 'sod200_sym_lf', 'box6_inviscid_sumT', 'sod1000'])
+@pytest.mark.parametrize('name', ['box8', 'cyl32x16', 'sod200_sym_lf', 'box6_inviscid_sumT', 'sod1000',
+                                  'duct100_totalpt', 'duct60_totalpt_normals'])
 def test_adjoint_step_matches_autograd(name):
     case, mesh, x, S, dt = _setup(name)
     prob = torch_ref.Problem(mesh, case.bc, case.config, case.objective)
