@@ -196,6 +196,161 @@ def cpu_baseline(args, threads, case=None, seconds=10.0):
                           steps, case.name, m.nInternalCells, na, sm.nInternalCells)}
 
 
+def measure(case, precision, args, local, dist, world, clocks):
+    """Timed primal steps and adjoint steps of one precision on the resident workload."""
+    import torch
+    from adfvm_gb300 import cases
+    from adfvm_gb300.solver import RCF
+    mesh = case.mesh
+    rcf = RCF(mesh, case.bc, objective=case.objective, precision=precision, device=local, **case.config)
+    dt_np = np.float64 if precision == 'fp64' else np.float32
+    tdt = torch.float64 if precision == 'fp64' else torch.float32
+    x = [torch.as_tensor(np.ascontiguousarray(a, dt_np)).cuda() for a in cases.conservative(case)]
+    y = [torch.empty_like(t) for t in x]
+    dt = case.dt
+    nIC, nIF, nF, nG = mesh.nInternalCells, mesh.nInternalFaces, mesh.nFaces, mesh.nGhostCells
+    es = 8 if precision == 'fp64' else 4
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        return max_over_ranks([ms], dist)[0]
+
+    state = {'x': x, 'y': y}
+
+    def primal():
+        rcf.step(state['x'][0], state['x'][1], state['x'][2], dt, out=state['y'], want_scalars=False)
+        state['x'], state['y'] = state['y'], state['x']
+
+    seeds = [torch.ones_like(t) * 1e-3 for t in x]
+    abuf = [torch.empty_like(t) for t in x]
+
+    def adjoint():
+        xx = state['x']
+        rcf.adjoint_step(xx[0], xx[1], xx[2], dt, seeds, obja=1.0, out=abuf, source_grad=False)
+
+    for _ in range(args.warmup):
+        primal()
+        adjoint()
+    if clocks:
+        clocks.start()
+        time.sleep(0.3)
+    rcf.profile(True)
+    ms_p = timed(primal, args.steps)
+    prof = rcf.profile_read()
+    rcf.profile(True)
+    ms_a = timed(adjoint, args.steps)
+    prof_a = rcf.profile_read()
+    rcf.profile(False)
+    clk = clocks.stop() if clocks else None
+    K = args.steps
+    vp = nIC * K * world / (ms_p / 1e3) / 1e6
+    va = nIC * K * world / (ms_a / 1e3) / 1e6
+    value = nIC * K * world / ((ms_p + ms_a) / 1e3) / 1e6
+
+    # end to end through the host-buffer entry point (pinned host buffers)
+    pin = [torch.empty(tuple(t.shape), dtype=tdt, pin_memory=True).numpy() for t in x]
+    pout = [torch.empty(tuple(t.shape), dtype=tdt, pin_memory=True).numpy() for t in x]
+    for a, b in zip(pin, state['x']):
+        a[...] = b.cpu().numpy()
+    rcf.step_host(pin[0], pin[1], pin[2], dt, out=pout)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    ke = max(1, K // 2)
+    for _ in range(ke):
+        rcf.step_host(pin[0], pin[1], pin[2], dt, out=pout)
+        pin, pout = pout, pin
+    te = time.perf_counter() - t0
+    # adjoint through the reference-facing Adjoint.map (host arrays in and out)
+    from adfvm_gb300.adjoint import Adjoint
+    adj = Adjoint(rcf)
+    host_x = [np.ascontiguousarray(a, np.float64) for a in pin]
+    host_seeds = [np.full(a.shape, 1e-3) for a in host_x]
+    ainputs = rcf.mapInputs(*host_x, dt) + host_seeds + [np.zeros((1, 1)), np.ones((1, 1)), np.zeros((1, 1))]
+    adj.map(*ainputs)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        aout = adj.map(*ainputs)
+    ta = time.perf_counter() - t0
+    te, ta = max_over_ranks([te, ta], dist)
+    state_bytes = int(sum(a.nbytes for a in pin))
+    e2e = {'value': round(nIC * ke * world / (te + ta) / 1e6, 3), 'unit': UNIT,
+           'h2d_bytes_per_step': state_bytes + int(3 * sum(a.size for a in host_x) * es),
+           'd2h_bytes_per_step': state_bytes + 16 + int(2 * sum(a.size for a in host_x) * es),
+           'path': 'primal: afvm_primal_step_host (pinned host state in/out, dtc and objective read back); '
+                   'adjoint: Adjoint.map (reference input list; state, sources, seeds in; state and source '
+                   'adjoints out)',
+           'primal_only': round(nIC * ke * world / te / 1e6, 3), 'adjoint_only': round(nIC * ke * world / ta / 1e6, 3)}
+    kernels = {k: {'ms_total': round(v[0], 4), 'launches': v[1], 'ms_avg': round(v[0] / v[1], 5)}
+               for k, v in prof.items()}
+    top = max(prof.items(), key=lambda kv: kv[1][0])[0]
+    peak, peak_kind = peaks()
+    alg = algorithmic_bytes(top, nIC, nIF, nF, nG, es)
+    avg_s = prof[top][0] / prof[top][1] / 1e3
+    achieved = alg / avg_s / 1e9
+    roofline = {'bound': 'hbm', 'kernel': top, 'achieved': round(achieved, 1), 'peak': peak,
+                'peak_source': peak_kind, 'unit': 'GB/s', 'frac': round(achieved / peak, 4),
+                'algorithmic_bytes_per_launch': int(alg), 'traffic': measured_traffic(top, es, nF)}
+    return {'value': round(value, 3), 'ms_per_step': round((ms_p + ms_a) / K, 4),
+            'primal': {'value': round(vp, 3), 'ms_per_step': round(ms_p / K, 4)},
+            'adjoint': {'value': round(va, 3), 'ms_per_step': round(ms_a / K, 4)},
+            'roofline': roofline, 'kernels': kernels,
+            'adjoint_kernels': {k: {'ms_total': round(v[0], 4), 'launches': v[1], 'ms_avg': round(v[0] / v[1], 5)}
+                                for k, v in prof_a.items()},
+            'gpu_launches': int(sum(v[1] for v in prof.values()) + sum(v[1] for v in prof_a.values())),
+            'e2e': e2e, 'clocks': clk, 'device_bytes': rcf.device_bytes}
+
+
+def serving_bench(local, n_requests=48, lams=(5.0, 20.0, 100.0, 200.0), seed=4, nplain=8):
+    """Poisson streams of sensitivity requests on boxes {16,24,32,48,64} and cylinders
+    {64x32,128x64} (100 primal + 100 adjoint steps each), lambda swept: served FP32
+    continuous batching vs the plain FP64 one-at-a-time form on the same first requests."""
+    from adfvm_gb300 import serving
+    keys = ['box16', 'box24', 'box32', 'box48', 'box64', 'cyl64x32', 'cyl128x64']
+    rng = np.random.default_rng(seed)
+    ks = [keys[i] for i in rng.integers(0, len(keys), size=n_requests)]
+    gaps = rng.exponential(1.0, size=n_requests)
+    lib = serving.MeshLibrary()
+    for k in keys:
+        lib.get(k)
+    srv = serving.SensitivityServer(precision='fp32', device=local, k=10, nPrimal=100, library=lib)
+    srv.warm(keys)
+    sweep = []
+    last = None
+    for lam in lams:
+        t = np.cumsum(gaps / lam)
+        reqs = [serving.Request(rid=i, key=k, seed=i, nPrimal=100, arrival=float(a)) for i, (k, a) in enumerate(zip(ks, t))]
+        st = srv.serve(reqs, realtime=True)
+        sweep.append({'lambda': lam, 'req_per_s': round(st['req_per_s'], 3), 'p50_s': round(st['p50_s'], 4),
+                      'p99_s': round(st['p99_s'], 4)})
+        last = reqs
+    plain = [serving.Request(rid=i, key=k, seed=i, nPrimal=100) for i, k in enumerate(ks[:nplain])]
+    sp = serving.plain_one_at_a_time(plain, lib, device=local, nPrimal=100)
+    errs = {}
+    for a, b in zip(last[:nplain], plain):
+        e = abs(a.sensitivity - b.sensitivity) / abs(b.sensitivity)
+        errs[a.key] = max(errs.get(a.key, 0.0), float('%.3g' % e))
+    cap = max(x['req_per_s'] for x in sweep)
+    return {'sweep': sweep, 'requests_per_lambda': n_requests, 'capacity_req_per_s': cap,
+            'plain_fp64_req_per_s': round(sp['req_per_s'], 3), 'speedup_vs_plain': round(cap / sp['req_per_s'], 2),
+            'max_rel_err_fp32_vs_fp64': max(errs.values()), 'rel_err_by_mesh': errs, 'slots': len(srv.slots),
+            'meshes': keys, 'steps_per_request': '100 primal + 100 adjoint (checkpoints every 10)'}
+
+
+
 def run_reference(args):
     rank = int(os.environ.get('RANK', '0'))
     if rank != 0:
