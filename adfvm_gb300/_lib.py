@@ -87,6 +87,7 @@ SIGNATURES = {
     'afvm_sensitivity': (C.c_int, [_v, C.c_int32, C.POINTER(_d), C.POINTER(_d),
                                    C.POINTER(C.c_int64), _d, _v]),
     'afvm_adjoint_energy': (C.c_int, [_v, _v, _v, _v, _v, _v, _v, _d, _v]),
+    'afvm_boundary_values': (C.c_int, [_v, _v, _v, _v, _v, _v]),
     'afvm_profile': (C.c_int, [_v, C.c_int32]),
     'afvm_profile_read': (C.c_int, [_v, C.c_int32, _d, C.POINTER(C.c_int64)]),
     'afvm_profile_kernel_name': (C.c_char_p, [C.c_int32]),

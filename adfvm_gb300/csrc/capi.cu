@@ -658,6 +658,28 @@ int afvm_adjoint_step(afvm_ctx* ctx, const void* rho, const void* rhoU, const vo
                                    (float*)S_rhoEa, s);
 }
 
+int afvm_boundary_values(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, void* out,
+                         void* stream) {
+    if (!ctx) return AFVM_ERR_BAD_ARG;
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!rho || !rhoU || !rhoE || (!out && c->nG > 0)) return fail(c, AFVM_ERR_BAD_ARG, "null pointer");
+    DeviceGuard dg(c->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (c->nG == 0) return AFVM_OK;
+    size_t es = c->precision == AFVM_FP64 ? sizeof(double) : sizeof(float);
+    if (c->precision == AFVM_FP64)
+        launch_prim<double>(c, (const double*)rho, (const double*)rhoU, (const double*)rhoE, s);
+    else
+        launch_prim<float>(c, (const float*)rho, (const float*)rhoU, (const float*)rhoE, s);
+    // ghost rows of the cell record, columns U, T, p
+    const char* src = (const char*)c->rec + es * REC * (size_t)c->nIC;
+    cudaError_t e = cudaMemcpy2DAsync(out, es * 5, src, es * REC, es * 5, (size_t)c->nG, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(c, e, "boundary values copy");
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(c, e, "boundary values launch");
+    return AFVM_OK;
+}
+
 int afvm_sensitivity(afvm_ctx* ctx, int32_t nArrays, const double* const* grad, const double* const* pert,
                      const int64_t* n, double* out, void* stream) {
     if (!ctx) return AFVM_ERR_BAD_ARG;

@@ -138,6 +138,8 @@ int adjoint_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double 
                      R* rhoa, R* rhoUa, R* rhoEa, R* Srhoa, R* SrhoUa, R* SrhoEa, cudaStream_t s);
 
 template <typename R>
+void launch_prim(Ctx* c, const R* r, const R* ru, const R* re, cudaStream_t s);
+template <typename R>
 void launch_prim_grad(Ctx* c, const R* r, const R* ru, const R* re, cudaStream_t s);
 template <typename R>
 void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const R* const* u0, const R* const* u1,

@@ -271,13 +271,17 @@ __global__ void k_finish(const double* partials, int nPartials, const unsigned l
 
 
 template <typename R>
+void launch_prim(Ctx* c, const R* r, const R* ru, const R* re, cudaStream_t s) {
+    const MeshDev<R>& m = meshOf<R>(c);
+    ProfScope ps(c, KID_PRIM, s);
+    k_prim<R><<<nblocks(m.nIC + m.nG), BLOCK, 0, s>>>(m, c->phys, r, ru, re, (R*)c->rec);
+}
+
+template <typename R>
 void launch_prim_grad(Ctx* c, const R* r, const R* ru, const R* re, cudaStream_t s) {
     const MeshDev<R>& m = meshOf<R>(c);
     R* rec = (R*)c->rec;
-    {
-        ProfScope ps(c, KID_PRIM, s);
-        k_prim<R><<<nblocks(m.nIC + m.nG), BLOCK, 0, s>>>(m, c->phys, r, ru, re, rec);
-    }
+    launch_prim<R>(c, r, ru, re, s);
     {
         ProfScope ps(c, KID_GRAD, s);
         k_grad<R><<<nblocks(m.nIC), BLOCK, 0, s>>>(m, rec);
@@ -396,6 +400,8 @@ template int primal_run_dev<double>(Ctx*, double*, double*, double*, int, double
                                     cudaStream_t);
 template int primal_run_dev<float>(Ctx*, float*, float*, float*, int, double, double, double, int, const float*,
                                    const float*, const float*, double*, double*, double*, cudaStream_t);
+template void launch_prim<double>(Ctx*, const double*, const double*, const double*, cudaStream_t);
+template void launch_prim<float>(Ctx*, const float*, const float*, const float*, cudaStream_t);
 template void launch_prim_grad<double>(Ctx*, const double*, const double*, const double*, cudaStream_t);
 template void launch_prim_grad<float>(Ctx*, const float*, const float*, const float*, cudaStream_t);
 template void launch_flux_update<double>(Ctx*, int, double, const double*, const double* const*,

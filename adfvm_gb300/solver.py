@@ -9,16 +9,22 @@ exposes:
   ``[rhoN, rhoUN, rhoEN, dtc (1,1), obj (1,1)]`` as numpy arrays;
 * ``step(...)`` - the same step on device tensors (torch CUDA), no host copies;
 * ``run(...)`` - the reference's ``Solver.run`` loop (time-step rule, ``round(t0+dt, 12)``,
-  objective sum; adFVM/solver.py:210-411) in ``simulation``/``forward`` modes, without
-  file IO;
+  objective sum; adFVM/solver.py:210-411) in ``simulation``/``orig``/``perturb``/``forward``
+  modes; on a case directory it writes the fields every ``writeInterval`` steps together with
+  ``status.pkl``, and resumes from ``startIndex``/``result`` as apps/problem.py:76-80 does;
+* ``fromCase(caseDir)``, ``readFields(t)``, ``writeFields(fields, t)`` - OpenFOAM case files
+  (density.py:113-158): U, T, p are read with their boundary dicts; rho, rhoU, rhoE, U, T, p
+  are written with the ghost-cell values of the boundary map as the patch values;
 * ``run_device(...)`` - n steps resident on the GPU (``afvm_primal_run``).
 The GPU library is mandatory: there is no CPU path.
 """
 import ctypes as C
+import os
 
 import numpy as np
 
 from . import _lib as L
+from . import foam
 from .mesh import Mesh, CYCLIC_PATCHES
 
 _BC = {'zeroGradient': L.AFVM_BC_ZERO_GRADIENT, 'empty': L.AFVM_BC_ZERO_GRADIENT,
@@ -342,16 +348,123 @@ class RCF(object):
         L.check(st, self._ctx, 'afvm_primal_run')
         return hist
 
+    # ------------------------------------------------------------------ case files
+    @classmethod
+    def fromCase(cls, caseDir, time=0.0, objective='none', precision='fp64', device=0, **config):
+        """The solver on an OpenFOAM case directory: the reference's ``RCF(caseDir)`` (mesh from
+        constant/polyMesh, Solver.__init__ solver.py:44-49) with the U, T, p boundary conditions
+        of time ``time``."""
+        meshData = foam.read_mesh(caseDir, time)
+        mesh = Mesh.create(meshData)
+        td = os.path.join(caseDir, foam.time_name(time))
+        bc = {name: foam.read_field(td, name, mesh.boundary, mesh.nInternalCells)[1] for name in ('U', 'T', 'p')}
+        rcf = cls(mesh, bc, objective=objective, precision=precision, device=device, **config)
+        rcf.case = caseDir
+        return rcf
+
+    @property
+    def statusFile(self):
+        return os.path.join(self.case, 'status.pkl')
+
+    def readStatusFile(self):
+        """[timeIndex, t, dt, result] (Solver.readStatusFile, solver.py:185-192); None if absent."""
+        return foam.read_status(self.statusFile)
+
+    def writeStatusFile(self, data):
+        foam.write_status(self.statusFile, data)
+
+    def removeStatusFile(self):
+        try:
+            os.remove(self.statusFile)
+        except OSError:
+            pass
+
+    def readFields(self, t, suffix=''):
+        """U, T, p of time t -> conservative (rho, rhoU, rhoE) host arrays (RCF.readFields,
+        density.py:113-137). The boundary values found there replace the current ones."""
+        m = self.mesh
+        td = os.path.join(self.case, foam.time_name(t))
+        prim = {}
+        for name in ('U', 'T', 'p'):
+            prim[name], b = foam.read_field(td, name + suffix, m.boundary, m.nInternalCells)
+            for patch, entry in b.items():
+                cur = self.bc[name].get(patch)
+                if cur is None or cur.get('type') != entry.get('type'):
+                    raise ValueError('%s: boundary type of patch %s changed between times' % (name, patch))
+                for k, v in entry.items():
+                    if isinstance(v, np.ndarray):
+                        cur[k] = v
+        self._apply_bc_tensors(self.getBoundaryTensor(1))
+        return self.conservative(prim['U'], prim['T'], prim['p'])
+
+    def boundary_values(self, rho, rhoU, rhoE):
+        """Ghost-cell U, T, p (nGhostCells x 5 CUDA tensor, working precision) of a device
+        state: the boundary map (afvm_boundary_values)."""
+        torch = _torch()
+        out = torch.empty((self.mesh.nGhostCells, 5), dtype=rho.dtype, device=rho.device)
+        stream = torch.cuda.current_stream(rho.device).cuda_stream
+        st = L.lib().afvm_boundary_values(self._ctx, C.c_void_p(rho.data_ptr()), C.c_void_p(rhoU.data_ptr()),
+                                          C.c_void_p(rhoE.data_ptr()), C.c_void_p(out.data_ptr()),
+                                          C.c_void_p(stream))
+        L.check(st, self._ctx, 'afvm_boundary_values')
+        return out
+
+    def primitive(self, rho, rhoU, rhoE):
+        """RCF.primitive (density.py:161-170) on host arrays."""
+        U = rhoU / rho
+        E = rhoE / rho
+        e = E - 0.5 * np.sum(U * U, axis=1, keepdims=True)
+        p = (self.gamma - 1) * rho * e
+        T = e * (1. / self.Cv)
+        return U, T, p
+
+    def writeFields(self, fields, t):
+        """Write rho, rhoU, rhoE, U, T, p of time t (RCF.writeFields, density.py:146-158): internal
+        values, and on every patch of a value type (BCs.py:18-23) the ghost-cell values of the
+        boundary map; the conservative fields carry the mesh's default boundary types
+        (IOField without a boundary, field.py:161-168), which hold no values."""
+        torch = _torch()
+        m = self.mesh
+        n = m.nInternalCells
+        dev = 'cuda:%d' % self.device
+        x = [np.asarray(a, np.float64).reshape(n, d) for a, d in zip(fields[:3], (1, 3, 1))]
+        xd = [torch.as_tensor(np.ascontiguousarray(a, self.dtype), device=dev) for a in x]
+        ghost = self.boundary_values(*xd).cpu().numpy().astype(np.float64)
+        gU, gT, gp = ghost[:, 0:3], ghost[:, 3:4], ghost[:, 4:5]
+        U, T, p = self.primitive(*x)
+        td = os.path.join(self.case, foam.time_name(t))
+        nIF = m.nInternalFaces
+
+        def boundary(base, ghost_values):
+            out = {}
+            for patch, entry in base.items():
+                e = dict(entry)
+                if e.get('type') in foam.VALUE_PATCHES:
+                    s = int(m.boundary[patch]['startFace']) - nIF
+                    e['value'] = ghost_values[s:s + int(m.boundary[patch]['nFaces'])]
+                out[patch] = e
+            return out
+        for name, internal in (('rho', x[0]), ('rhoU', x[1]), ('rhoE', x[2])):
+            foam.write_field(td, name, internal, {k: dict(v) for k, v in m.defaultBoundary.items()})
+        for name, internal, g in (('U', U, gU), ('T', T, gT), ('p', p, gp)):
+            foam.write_field(td, name, internal, boundary(self.bc[name], g))
+
     # ------------------------------------------------------------------ time loop
-    def run(self, fields, nSteps, dt, endTime=np.inf, startTime=0.0, mode='simulation', source=None, avgStart=0):
-        """Solver.run (adFVM/solver.py:210-411) without IO. fields: conservative (rho, rhoU,
-        rhoE) numpy arrays. mode 'forward' returns every step's fields (and the record);
-        otherwise returns the time-summed objective (and the record)."""
+    def run(self, fields, nSteps, dt, endTime=np.inf, startTime=0.0, mode='simulation', source=None, avgStart=0,
+            writeInterval=None, startIndex=0, result=0.0):
+        """Solver.run (adFVM/solver.py:210-411). fields: conservative (rho, rhoU, rhoE) numpy
+        arrays. mode 'forward' returns every step's fields (and the record); otherwise returns
+        the time-summed objective (and the record). On a case directory (``fromCase``) the
+        fields and status.pkl are written every writeInterval steps and after the last one in
+        'simulation'/'orig' modes, and 'orig'/'perturb' append the objective series to
+        timeSeries.txt (solver.py:381-396)."""
         t = startTime
-        timeIndex = 0
-        result = 0.0
+        timeIndex = startIndex
         sols = [list(fields)]
         record = []
+        series = []
+        case = getattr(self, 'case', None)
+        every = writeInterval or np.inf
         sources = None if source is None else [np.asarray(s) for s in source]
         while t < endTime and timeIndex < nSteps:
             inputs = self.mapInputs(*fields, dt, sources)
@@ -359,6 +472,7 @@ class RCF(object):
             fields = outputs[:3]
             dtc, objective = float(outputs[3][0, 0]), float(outputs[4][0, 0])
             record.append((dt, dtc, objective))
+            series.append(objective)
             timeIndex += 1
             t = round(t + dt, 12)
             if not self.fixedTimeStep:
@@ -367,6 +481,14 @@ class RCF(object):
                 result += objective
             if mode == 'forward':
                 sols.append(list(fields))
+            elif case is not None and (timeIndex % every == 0 or not (t < endTime and timeIndex < nSteps)):
+                if mode in ('orig', 'simulation'):
+                    self.writeFields(fields, t)
+                if mode in ('orig', 'perturb'):
+                    with open(os.path.join(case, 'timeSeries.txt'), 'ab') as f:
+                        np.savetxt(f, np.array(series))
+                series = []
+                self.writeStatusFile([timeIndex, t, dt, result])
         if mode == 'forward':
             return sols, record
         return result, record

@@ -173,6 +173,14 @@ int64_t afvm_ctx_device_bytes(const afvm_ctx* ctx);
  * 1=T, 2=p. */
 int afvm_set_bc_value(afvm_ctx* ctx, int32_t patch, int32_t field, const double* values);
 
+/* Ghost-cell values of the primitive fields for a conservative state: the boundary map the
+ * reference runs before writing fields (RCF.initFields -> mapBoundary, adFVM/density.py:140-143;
+ * ghost rows per BCs.py:62-184). rho, rhoU, rhoE: DEVICE state as for afvm_primal_step. out:
+ * DEVICE buffer of nGhostCells x 5 in the working precision, rows in ghost-cell order (cell id
+ * minus nInternalCells), columns U(3), T, p. Asynchronous on stream. */
+int afvm_boundary_values(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE,
+                         void* out, void* stream);
+
 /* One SSP-RK3 time step (adFVM/timestep.py:27-55 over RCF.equation, density.py:339-414).
  * State arrays are DEVICE pointers in the reference layout: rho (nInternalCells),
  * rhoU (nInternalCells x 3), rhoE (nInternalCells); element type double for AFVM_FP64 and

@@ -57,6 +57,40 @@ def load():
     return ns
 
 
+class LegacyArray(np.ndarray):
+    """ndarray with NumPy 1's ``tostring`` (removed in NumPy 2), which the reference's file
+    writers call (field.py writeField, mesh.py writeFoamFile)."""
+
+    def tostring(self):
+        return self.tobytes()
+
+
+class _LegacyNumpy(types.ModuleType):
+    """numpy with NumPy 1's binary ``fromstring`` (a copying ``frombuffer``), which the
+    reference's file readers call (mesh.py readFoamFile, extractField)."""
+
+    def __init__(self):
+        super().__init__('numpy')
+
+    def __getattr__(self, name):
+        return getattr(np, name)
+
+    @staticmethod
+    def fromstring(data, dtype=float, count=-1, sep=''):
+        if sep:
+            return np.fromstring(data, dtype, count, sep)
+        return np.frombuffer(data, dtype, count).copy()
+
+
+def legacy_numpy():
+    """Let the reference's mesh/field file IO run on this NumPy (idempotent)."""
+    ns = load()
+    shim = _LegacyNumpy()
+    for mod in (ns.mesh, ns.field):
+        mod.np = shim
+    return ns
+
+
 def build_mesh(meshData, case_dir):
     ns = load()
     points, faces, owner, neighbour, boundary = meshData

@@ -70,5 +70,6 @@ def test_null_arguments_return_status():
     assert lib.afvm_ctx_destroy(None) == L.AFVM_OK
     assert lib.afvm_primal_step(None, None, None, None, 0.0, None, None, None, None, None, None, None, None,
                                 None) == L.AFVM_ERR_BAD_ARG
+    assert lib.afvm_boundary_values(None, None, None, None, None, None) == L.AFVM_ERR_BAD_ARG
     out = C.c_void_p()
     assert lib.afvm_ctx_create(None, None, None, 0, 0, C.byref(out)) == L.AFVM_ERR_BAD_ARG
