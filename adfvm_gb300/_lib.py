@@ -79,11 +79,14 @@ SIGNATURES = {
     'afvm_ctx_device_bytes': (C.c_int64, [_v]),
     'afvm_set_bc_value': (C.c_int, [_v, C.c_int32, C.c_int32, _d]),
     'afvm_primal_step': (C.c_int, [_v, _v, _v, _v, C.c_double, _v, _v, _v, _v, _v, _v, _d, _d, _v]),
+    'afvm_primal_step_stages': (C.c_int, [_v, _v, _v, _v, C.c_double, _v, _v, _v, _v, _v, _v, _v, _d, _d, _v]),
     'afvm_primal_step_host': (C.c_int, [_v, _v, _v, _v, C.c_double, _v, _v, _v, _v, _v, _v, _d, _d, _v]),
     'afvm_primal_run': (C.c_int, [_v, _v, _v, _v, C.c_int32, C.c_double, C.c_double, C.c_double,
                                   C.c_int32, _v, _v, _v, _d, _d, _d, _v]),
     'afvm_adjoint_step': (C.c_int, [_v, _v, _v, _v, C.c_double, _v, _v, _v, _v, _v, _v,
                                     C.c_double, C.c_double, _v, _v, _v, _v, _v, _v, _v]),
+    'afvm_adjoint_step_stages': (C.c_int, [_v, _v, _v, _v, C.c_double, _v, _v, _v, _v, _v, _v, _v,
+                                           C.c_double, C.c_double, _v, _v, _v, _v, _v, _v, _v]),
     'afvm_sensitivity': (C.c_int, [_v, C.c_int32, C.POINTER(_d), C.POINTER(_d),
                                    C.POINTER(C.c_int64), _d, _v]),
     'afvm_adjoint_energy': (C.c_int, [_v, _v, _v, _v, _v, _v, _v, _d, _v]),

@@ -67,12 +67,14 @@ class Adjoint(object):
         return self.primal.adjoint_energy(adj, state) ** 0.5
 
     # ------------------------------------------------------------ the sweep
-    def run(self, fields, nSteps, dt, writeInterval, perturbations=(), avgStart=0, source=None):
+    def run(self, fields, nSteps, dt, writeInterval, perturbations=(), avgStart=0, source=None, keep_stages=True):
         """Checkpointed adjoint sweep on the device.
 
         fields: initial conservative state (host arrays). dt: a float (fixed step) or the
         per-step dt series of the primal run. perturbations: list of (dS_rho, dS_rhoU,
-        dS_rhoE) host arrays. Returns (sensitivities, adjoint fields at t0 (host), record)."""
+        dS_rhoE) host arrays. keep_stages: the interval's forward re-run also keeps every
+        step's RK stage states (10 nInternalCells values a step) so that the adjoint steps
+        do not recompute them. Returns (sensitivities, adjoint fields at t0 (host), record)."""
         torch = _torch()
         p = self.primal
         if nSteps % writeInterval:
@@ -100,16 +102,21 @@ class Adjoint(object):
         a = [torch.zeros_like(t) for t in x0]
         sens_series = []
         nCk = nSteps // writeInterval
+        stages = [p.stage_buffer() for _ in range(writeInterval)] if keep_stages else None
         for checkpoint in range(nCk):
             primalIndex = nSteps - (checkpoint + 1) * writeInterval
             states = [checkpoints[primalIndex // writeInterval]]
-            for k in range(primalIndex, primalIndex + writeInterval - 1):
+            last = primalIndex + writeInterval - (0 if keep_stages else 1)
+            for k in range(primalIndex, last):
                 y = states[-1]
-                states.append(list(p.step(y[0], y[1], y[2], dts[k], S=S, want_scalars=False)[:3]))
+                sb = stages[k - primalIndex] if keep_stages else None
+                states.append(list(p.step(y[0], y[1], y[2], dts[k], S=S, want_scalars=False, stages=sb)[:3]))
             for step in range(writeInterval):
                 adjointIndex = writeInterval - 1 - step
                 y = states[adjointIndex]
-                r = p.adjoint_step(y[0], y[1], y[2], dts[primalIndex + adjointIndex], a, obja=1.0, S=S, out=a)
+                sb = stages[adjointIndex] if keep_stages else None
+                r = p.adjoint_step(y[0], y[1], y[2], dts[primalIndex + adjointIndex], a, obja=1.0, S=S, out=a,
+                                   stages=sb)
                 grads = [g.reshape(-1).double() for g in r[3]]
                 sens = [p.sensitivity(grads, pert) for pert in perts]
                 sens_series.append(sens)

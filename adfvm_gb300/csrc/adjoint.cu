@@ -153,8 +153,8 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const
             R d[3] = {m.gval[g], m.gval[(size_t)m.nG + g], m.gval[2 * (size_t)m.nG + g]};
             R Tt = m.gval[3 * (size_t)m.nG + g], pt = m.gval[4 * (size_t)m.nG + g];
             R Un = rs[0] * d[0] + rs[1] * d[1] + rs[2] * d[2];
-            R kap = R(P.gamma / P.gm1);
-            R Unb = dot3(gp, d) - gp[R_T] * Un / R(P.Cp);
+            R kap = consts<R>(P).ggm1;
+            R Unb = dot3(gp, d) - gp[R_T] * Un / consts<R>(P).Cp;
             for (int k = 0; k < 3; k++) pbar[k] += Unb * d[k];
             pbar[R_T] += gp[R_P] * pt * kap * pow(rs[R_T] / Tt, kap - R(1)) / Tt;
             continue;
@@ -243,7 +243,7 @@ __global__ void k_split5(int n, const R* __restrict__ sb, R* r, R* u, R* e) {
 template <typename R>
 int adjoint_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double dt, const R* Srho, const R* SrhoU,
                      const R* SrhoE, const R* rhoNa, const R* rhoUNa, const R* rhoENa, double obja, R* rhoa,
-                     R* rhoUa, R* rhoEa, R* Srhoa, R* SrhoUa, R* SrhoEa, cudaStream_t s) {
+                     R* rhoUa, R* rhoEa, R* Srhoa, R* SrhoUa, R* SrhoEa, cudaStream_t s, const R* stages) {
     const MeshDev<R>& m = meshOf<R>(c);
     const Phys& P = c->phys;
     default_sources<R>(c, Srho, SrhoU, SrhoE);
@@ -253,12 +253,17 @@ int adjoint_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double 
     const R* u0c[3] = {rho, rhoU, rhoE};
     const R* u1c[3] = {u1[0], u1[1], u1[2]};
     const R* u2c[3] = {u2[0], u2[1], u2[2]};
-    // forward recompute of the stage states
-    cudaMemsetAsync(c->dtcBits, 0, sizeof(unsigned long long), s);
-    launch_prim_grad<R>(c, rho, rhoU, rhoE, s);
-    launch_flux_update<R>(c, 0, dt, nullptr, u0c, u1c, u2c, Srho, SrhoU, SrhoE, u1, s);
-    launch_prim_grad<R>(c, u1[0], u1[1], u1[2], s);
-    launch_flux_update<R>(c, 1, dt, nullptr, u0c, u1c, u2c, Srho, SrhoU, SrhoE, u2, s);
+    if (stages) {
+        // the stage states the primal step kept (afvm_primal_step_stages)
+        stage_views<R, const R>(stages, m.nIC, u1c, u2c);
+    } else {
+        // forward recompute of the stage states
+        cudaMemsetAsync(c->dtcBits, 0, sizeof(unsigned long long), s);
+        launch_prim_grad<R>(c, rho, rhoU, rhoE, s);
+        launch_flux_update<R>(c, 0, dt, nullptr, u0c, u1c, u2c, Srho, SrhoU, SrhoE, u1, s);
+        launch_prim_grad<R>(c, u1[0], u1[1], u1[2], s);
+        launch_flux_update<R>(c, 1, dt, nullptr, u0c, u1c, u2c, Srho, SrhoU, SrhoE, u2, s);
+    }
     // reverse sweep
     R* A1[3] = {(R*)c->a1[0], (R*)c->a1[1], (R*)c->a1[2]};
     R* A2[3] = {(R*)c->a2[0], (R*)c->a2[1], (R*)c->a2[2]};
@@ -310,9 +315,10 @@ int adjoint_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double 
 
 template int adjoint_step_dev<double>(Ctx*, const double*, const double*, const double*, double, const double*,
                                       const double*, const double*, const double*, const double*, const double*,
-                                      double, double*, double*, double*, double*, double*, double*, cudaStream_t);
+                                      double, double*, double*, double*, double*, double*, double*, cudaStream_t,
+                                      const double*);
 template int adjoint_step_dev<float>(Ctx*, const float*, const float*, const float*, double, const float*,
                                      const float*, const float*, const float*, const float*, const float*, double,
-                                     float*, float*, float*, float*, float*, float*, cudaStream_t);
+                                     float*, float*, float*, float*, float*, float*, cudaStream_t, const float*);
 
 }  // namespace afvm

@@ -438,6 +438,7 @@ int afvm_ctx_create(const afvm_mesh_tensors* mesh, const afvm_patch_bc* bcs, con
     P.muModel = phys->mu_model;
     P.riemann = phys->riemann;
     P.briemann = phys->boundary_riemann;
+    finish_phys(P);
     c->objective = phys->objective;
     c->objPatch = phys->objective_patch;
     DeviceGuard dg(device);
@@ -538,9 +539,9 @@ int afvm_set_bc_value(afvm_ctx* ctx, int32_t patch, int32_t field, const double*
     return AFVM_OK;
 }
 
-int afvm_primal_step(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, double dt,
-                     const void* S_rho, const void* S_rhoU, const void* S_rhoE, void* rhoN, void* rhoUN, void* rhoEN,
-                     double* dtc_out, double* obj_out, void* stream) {
+int afvm_primal_step_stages(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, double dt,
+                            const void* S_rho, const void* S_rhoU, const void* S_rhoE, void* rhoN, void* rhoUN,
+                            void* rhoEN, void* stages, double* dtc_out, double* obj_out, void* stream) {
     if (!ctx) return AFVM_ERR_BAD_ARG;
     Ctx* c = reinterpret_cast<Ctx*>(ctx);
     if (!rho || !rhoU || !rhoE || !rhoN || !rhoUN || !rhoEN) return fail(c, AFVM_ERR_BAD_ARG, "null state pointer");
@@ -551,13 +552,22 @@ int afvm_primal_step(afvm_ctx* ctx, const void* rho, const void* rhoU, const voi
     if (c->precision == AFVM_FP64)
         st = primal_step_dev<double>(c, (const double*)rho, (const double*)rhoU, (const double*)rhoE, dt, nullptr,
                                      (const double*)S_rho, (const double*)S_rhoU, (const double*)S_rhoE,
-                                     (double*)rhoN, (double*)rhoUN, (double*)rhoEN, c->scal, c->scal + 1, s);
+                                     (double*)rhoN, (double*)rhoUN, (double*)rhoEN, c->scal, c->scal + 1, s,
+                                     (double*)stages);
     else
         st = primal_step_dev<float>(c, (const float*)rho, (const float*)rhoU, (const float*)rhoE, dt, nullptr,
                                     (const float*)S_rho, (const float*)S_rhoU, (const float*)S_rhoE,
-                                    (float*)rhoN, (float*)rhoUN, (float*)rhoEN, c->scal, c->scal + 1, s);
+                                    (float*)rhoN, (float*)rhoUN, (float*)rhoEN, c->scal, c->scal + 1, s,
+                                    (float*)stages);
     if (st) return st;
     return get_results(c, dtc_out, obj_out, s);
+}
+
+int afvm_primal_step(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, double dt,
+                     const void* S_rho, const void* S_rhoU, const void* S_rhoE, void* rhoN, void* rhoUN, void* rhoEN,
+                     double* dtc_out, double* obj_out, void* stream) {
+    return afvm_primal_step_stages(ctx, rho, rhoU, rhoE, dt, S_rho, S_rhoU, S_rhoE, rhoN, rhoUN, rhoEN, nullptr,
+                                   dtc_out, obj_out, stream);
 }
 
 int afvm_primal_step_host(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, double dt,
@@ -631,10 +641,11 @@ int afvm_primal_run(afvm_ctx* ctx, void* rho, void* rhoU, void* rhoE, int32_t nS
                                  obj_hist, s);
 }
 
-int afvm_adjoint_step(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, double dt,
-                      const void* S_rho, const void* S_rhoU, const void* S_rhoE, const void* rhoNa,
-                      const void* rhoUNa, const void* rhoENa, double dtca, double obja, void* rhoa, void* rhoUa,
-                      void* rhoEa, void* S_rhoa, void* S_rhoUa, void* S_rhoEa, void* stream) {
+int afvm_adjoint_step_stages(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, double dt,
+                             const void* S_rho, const void* S_rhoU, const void* S_rhoE, const void* stages,
+                             const void* rhoNa, const void* rhoUNa, const void* rhoENa, double dtca, double obja,
+                             void* rhoa, void* rhoUa, void* rhoEa, void* S_rhoa, void* S_rhoUa, void* S_rhoEa,
+                             void* stream) {
     if (!ctx) return AFVM_ERR_BAD_ARG;
     Ctx* c = reinterpret_cast<Ctx*>(ctx);
     if (!rho || !rhoU || !rhoE || !rhoNa || !rhoUNa || !rhoENa || !rhoa || !rhoUa || !rhoEa)
@@ -650,12 +661,20 @@ int afvm_adjoint_step(afvm_ctx* ctx, const void* rho, const void* rhoU, const vo
                                         (const double*)S_rho, (const double*)S_rhoU, (const double*)S_rhoE,
                                         (const double*)rhoNa, (const double*)rhoUNa, (const double*)rhoENa, obja,
                                         (double*)rhoa, (double*)rhoUa, (double*)rhoEa, (double*)S_rhoa,
-                                        (double*)S_rhoUa, (double*)S_rhoEa, s);
+                                        (double*)S_rhoUa, (double*)S_rhoEa, s, (const double*)stages);
     return adjoint_step_dev<float>(c, (const float*)rho, (const float*)rhoU, (const float*)rhoE, dt,
                                    (const float*)S_rho, (const float*)S_rhoU, (const float*)S_rhoE,
                                    (const float*)rhoNa, (const float*)rhoUNa, (const float*)rhoENa, obja,
                                    (float*)rhoa, (float*)rhoUa, (float*)rhoEa, (float*)S_rhoa, (float*)S_rhoUa,
-                                   (float*)S_rhoEa, s);
+                                   (float*)S_rhoEa, s, (const float*)stages);
+}
+
+int afvm_adjoint_step(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, double dt,
+                      const void* S_rho, const void* S_rhoU, const void* S_rhoE, const void* rhoNa,
+                      const void* rhoUNa, const void* rhoENa, double dtca, double obja, void* rhoa, void* rhoUa,
+                      void* rhoEa, void* S_rhoa, void* S_rhoUa, void* S_rhoEa, void* stream) {
+    return afvm_adjoint_step_stages(ctx, rho, rhoU, rhoE, dt, S_rho, S_rhoU, S_rhoE, nullptr, rhoNa, rhoUNa, rhoENa,
+                                    dtca, obja, rhoa, rhoUa, rhoEa, S_rhoa, S_rhoUa, S_rhoEa, stream);
 }
 
 int afvm_boundary_values(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, void* out,

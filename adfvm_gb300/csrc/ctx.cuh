@@ -124,7 +124,7 @@ int cuda_fail(Ctx* c, cudaError_t e, const char* what);
 template <typename R>
 int primal_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double dt, const double* dtDev,
                     const R* Srho, const R* SrhoU, const R* SrhoE, R* rhoN, R* rhoUN, R* rhoEN,
-                    double* dtcDev, double* objDev, cudaStream_t s);
+                    double* dtcDev, double* objDev, cudaStream_t s, R* stages = nullptr);
 template <typename R>
 int primal_run_dev(Ctx* c, R* rho, R* rhoU, R* rhoE, int nSteps, double dt0, double CFL, double stepFactor,
                    int fixed, const R* Srho, const R* SrhoU, const R* SrhoE, double* dtHist, double* dtcHist,
@@ -135,7 +135,16 @@ template <typename R>
 int adjoint_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double dt,
                      const R* Srho, const R* SrhoU, const R* SrhoE,
                      const R* rhoNa, const R* rhoUNa, const R* rhoENa, double obja,
-                     R* rhoa, R* rhoUa, R* rhoEa, R* Srhoa, R* SrhoUa, R* SrhoEa, cudaStream_t s);
+                     R* rhoa, R* rhoUa, R* rhoEa, R* Srhoa, R* SrhoUa, R* SrhoEa, cudaStream_t s,
+                     const R* stages = nullptr);
+
+// the RK stage states u1, u2 of one step in a caller's buffer of 10 nIC values:
+// u1 = [rho (n) | rhoU (3n) | rhoE (n)], then u2 in the same layout
+template <typename R, typename P>
+inline void stage_views(P* stages, int n, P** u1, P** u2) {
+    u1[0] = stages; u1[1] = stages + n; u1[2] = stages + 4 * (size_t)n;
+    u2[0] = stages + 5 * (size_t)n; u2[1] = stages + 6 * (size_t)n; u2[2] = stages + 9 * (size_t)n;
+}
 
 template <typename R>
 void launch_prim(Ctx* c, const R* r, const R* ru, const R* re, cudaStream_t s);

@@ -83,7 +83,7 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
         }
     }
     if (!inviscid) viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, UF, gTF, gUF, in.D, in.N, in.delta, F);
-    R aF = sqrt_(R(P.Cp) * TF * R(P.gm1));
+    R aF = sqrt_(consts<R>(P).Cp * TF * consts<R>(P).gm1);
     maxaF = fabs(dot3(UF, in.N)) + aF;
 }
 
@@ -93,15 +93,15 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
 template <typename R>
 AFVM_HD void conservative_vjp(const Phys& P, const R* U, R T, R p, R rhob, const R* rhoUb, R rhoEb, R* Ub,
                               R& Tb, R& pb) {
-    R e = R(P.Cv) * T;
-    R rd = rcp(e * R(P.gm1));
+    R e = consts<R>(P).Cv * T;
+    R rd = rcp(e * consts<R>(P).gm1);
     R rho = p * rd;
     R q = dot3(U, U);
     for (int k = 0; k < 3; k++) Ub[k] += rhoUb[k] * rho + rhoEb * rho * U[k];
     R rhot = rhob + dot3(rhoUb, U) + rhoEb * (e + R(0.5) * q);
     pb += rhot * rd;
     R eb = -rhot * rho * rcp(e) + rhoEb * rho;
-    Tb += eb * R(P.Cv);
+    Tb += eb * consts<R>(P).Cv;
 }
 
 // interp.secondOrder: phiC + (phiD - phiC) lw + qw.g
@@ -116,7 +116,7 @@ AFVM_HD void recon_vjp(R b, R lw, const R* qw, R& phiCb, R& phiDb, R* gb) {
 template <typename R>
 AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR, const R* N, const R* Fb,
                      R& pLb, R& pRb, R* ULb, R* URb, R& rhoLb, R& rhoRb) {
-    const R g = R(P.gamma), gm1 = R(P.gm1), ggm1 = R(P.gamma / P.gm1), h = R(0.5);
+    const R g = consts<R>(P).gamma, gm1 = consts<R>(P).gm1, ggm1 = consts<R>(P).ggm1, h = R(0.5);
     // ---- forward (as roe())
     R UnL = dot3(UL, N), UnR = dot3(UR, N);
     R rhoUnL = rhoL * UnL, rhoUnR = rhoR * UnR;
@@ -147,7 +147,7 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL
     R eb_ = cL - cR;
     R eps = h * fabs(ea);
     eps = eps + h * fabs(eb_);
-    eps = (eps < R(0)) ? eps - R(P.small) : eps + R(P.small);
+    eps = (eps < R(0)) ? eps - consts<R>(P).small : eps + consts<R>(P).small;
     R eps2 = R(2) * eps;
     bool s1 = l1 < eps2, s2 = l2 < eps2, s3 = l3 < eps2;
     R re = (s1 || s2 || s3) ? rcp(eps) : R(0);
@@ -269,7 +269,7 @@ template <typename R>
 AFVM_HD void laxf_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR, const R* rhoUL,
                       const R* rhoUR, R rhoEL, R rhoER, const R* N, const R* Fb, R& pLb, R& pRb, R* ULb, R* URb,
                       R& rhoLb, R& rhoRb, R* rhoULb, R* rhoURb, R& rhoELb, R& rhoERb) {
-    const R g = R(P.gamma), h = R(0.5);
+    const R g = consts<R>(P).gamma, h = R(0.5);
     R UnL = dot3(UL, N), UnR = dot3(UR, N);
     R rrL = rcp(rhoL), rrR = rcp(rhoR);
     R c2L = g * pL * rrL, c2R = g * pR * rrR;
@@ -311,7 +311,7 @@ AFVM_HD void viscous_vjp(const Phys& P, R TL, R TR, const R* UL, const R* UR, R 
                          const R* gUF, const R* D, const R* N, R delta, const R* Fb, R& TLb, R& TRb, R* ULb, R* URb,
                          R& TFb, R* UFb, R* gTFb, R* gUFb) {
     R mu = viscosity<R>(P, TF);
-    R kappa = mu * R(P.kFac);
+    R kappa = mu * consts<R>(P).kFac;
     R rdel = rcp(delta);
     R snT = (TR - TL) * rdel;
     R gTD = dot3(gTF, D);
@@ -347,7 +347,7 @@ AFVM_HD void viscous_vjp(const Phys& P, R TL, R TR, const R* UL, const R* UR, R 
     R kappab = qFb * dot3(gT, N);
     R gTb[3];
     for (int k = 0; k < 3; k++) gTb[k] = qFb * kappa * N[k];
-    mub += kappab * R(P.kFac);
+    mub += kappab * consts<R>(P).kFac;
     R gUb[9];
     for (int i = 0; i < 3; i++)
         for (int k = 0; k < 3; k++) gUb[3 * i + k] = tmp2b[i] * N[k] + tmp2b[k] * N[i];
@@ -368,7 +368,7 @@ AFVM_HD void viscous_vjp(const Phys& P, R TL, R TR, const R* UL, const R* UR, R 
     for (int k = 0; k < 3; k++) gTFb[k] += gTb[k] + gTDb * D[k];
     TRb += snTb * rdel;
     TLb += -snTb * rdel;
-    if (P.muModel == AFVM_MU_SUTHERLAND) TFb += mub * mu * (R(1.5) * rcp(TF) - rcp(TF + R(P.muTs)));
+    if (P.muModel == AFVM_MU_SUTHERLAND) TFb += mub * mu * (R(1.5) * rcp(TF) - rcp(TF + consts<R>(P).muTs));
 }
 
 // <Fbar, F> differentiated with respect to all 40 inputs of the face (accumulated into out)

@@ -32,10 +32,39 @@ constexpr int FREC = 6;
 // kinds of faces
 constexpr int FACE_INTERNAL = 0, FACE_COUPLED = 1, FACE_CHARACTERISTIC = 2, FACE_BOUNDARY = 3;
 
+// the gas constants in the working precision, so that the templated physics issues no FP64
+// conversion or division in FP32 (ggm1 = gamma/(gamma-1))
+template <typename R>
+struct PhysR {
+    R gamma, gm1, ggm1, Cp, Cv, rCv, kFac, mu0, muAs, muTs, small;
+};
+
 struct Phys {
     double gamma, gm1, Cp, Cv, rCv, kFac, mu0, muAs, muTs, small;
     int muModel, riemann, briemann;
+    PhysR<double> d;
+    PhysR<float> f;
 };
+
+template <typename R>
+inline void fill_consts(const Phys& P, PhysR<R>& q) {
+    q.gamma = R(P.gamma); q.gm1 = R(P.gm1); q.ggm1 = R(P.gamma / P.gm1); q.Cp = R(P.Cp); q.Cv = R(P.Cv);
+    q.rCv = R(P.rCv); q.kFac = R(P.kFac); q.mu0 = R(P.mu0); q.muAs = R(P.muAs); q.muTs = R(P.muTs);
+    q.small = R(P.small);
+}
+
+// host: derive the working-precision copies once the double fields are set
+inline void finish_phys(Phys& P) {
+    fill_consts(P, P.d);
+    fill_consts(P, P.f);
+}
+
+template <typename R>
+AFVM_HD const PhysR<R>& consts(const Phys& P);
+template <>
+AFVM_HD const PhysR<double>& consts<double>(const Phys& P) { return P.d; }
+template <>
+AFVM_HD const PhysR<float>& consts<float>(const Phys& P) { return P.f; }
 
 template <typename R>
 AFVM_HD R dot3(const R* a, const R* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
@@ -135,15 +164,15 @@ AFVM_HD R sqrt_(R x) { return x > R(0) ? x * rsqrt_(x) : R(0); }
 // mu(T): constant, or Sutherland 1.4792e-06*T**1.5/(T+116.) (adFVM/density.py:27)
 template <typename R>
 AFVM_HD R viscosity(const Phys& P, R T) {
-    if (P.muModel == AFVM_MU_SUTHERLAND) return (R(P.muAs) * (T * sqrt_(T))) * rcp(T + R(P.muTs));
-    return R(P.mu0);
+    if (P.muModel == AFVM_MU_SUTHERLAND) return (consts<R>(P).muAs * (T * sqrt_(T))) * rcp(T + consts<R>(P).muTs);
+    return consts<R>(P).mu0;
 }
 
 // RCF.conservative (adFVM/density.py:173-181)
 template <typename R>
 AFVM_HD void conservative(const Phys& P, const R* U, R T, R p, R& rho, R* rhoU, R& rhoE) {
-    R e = R(P.Cv) * T;
-    rho = p * rcp(e * R(P.gm1));
+    R e = consts<R>(P).Cv * T;
+    rho = p * rcp(e * consts<R>(P).gm1);
     rhoE = rho * (e + R(0.5) * dot3(U, U));
     rhoU[0] = U[0] * rho; rhoU[1] = U[1] * rho; rhoU[2] = U[2] * rho;
 }
@@ -160,7 +189,7 @@ AFVM_HD R recon(R phiC, R phiD, const R* g, R lw, const R* qw) {
 template <typename R>
 AFVM_HD void roe(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR,
                  const R* N, R* F) {
-    const R g = R(P.gamma), gm1 = R(P.gm1), ggm1 = R(P.gamma / P.gm1);
+    const R g = consts<R>(P).gamma, gm1 = consts<R>(P).gm1, ggm1 = consts<R>(P).ggm1;
     R UnL = dot3(UL, N), UnR = dot3(UR, N);
     R rhoUnL = rhoL * UnL, rhoUnR = rhoR * UnR;
     R rrL = rcp(rhoL), rrR = rcp(rhoR);
@@ -186,7 +215,7 @@ AFVM_HD void roe(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R 
     R lam1 = fabs(UnF), lam2 = fabs(UnF + aF), lam3 = fabs(UnF - aF);
     R eps = R(0.5) * fabs(UnL - UnR);
     eps = eps + R(0.5) * fabs(sqrt_(g * pL * rrL) - sqrt_(g * pR * rrR));
-    eps = (eps < R(0)) ? eps - R(P.small) : eps + R(P.small);
+    eps = (eps < R(0)) ? eps - consts<R>(P).small : eps + consts<R>(P).small;
     R eps2 = R(2) * eps;
     if (lam1 < eps2 || lam2 < eps2 || lam3 < eps2) {
         R re = rcp(eps);
@@ -210,7 +239,7 @@ AFVM_HD void roe(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R 
 template <typename R>
 AFVM_HD void laxf(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR,
                                      const R* rhoUL, const R* rhoUR, R rhoEL, R rhoER, const R* N, R* F) {
-    const R g = R(P.gamma);
+    const R g = consts<R>(P).gamma;
     R UnL = dot3(UL, N), UnR = dot3(UR, N);
     R cL = sqrt_(g * pL * rcp(rhoL));
     R cR = sqrt_(g * pR * rcp(rhoR));
@@ -227,7 +256,7 @@ template <typename R>
 AFVM_HD void viscous(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, const R* UF,
                                         const R* gTF, const R* gUF, const R* D, const R* N, R delta, R* F) {
     R mu = viscosity<R>(P, TF);
-    R kappa = mu * R(P.kFac);
+    R kappa = mu * consts<R>(P).kFac;
     R rdel = rcp(delta);
     R snT = (TR - TL) * rdel;
     R gTD = dot3(gTF, D);

@@ -84,8 +84,8 @@ __global__ void __launch_bounds__(BLOCK) k_prim(MeshDev<R> m, Phys P, const R* _
         R Un = dot3(v, d);
         R T = v[3];
         for (int k = 0; k < 3; k++) v[k] = Un * d[k];
-        v[3] = Tt - R(0.5) * Un * Un / R(P.Cp);
-        v[4] = pt * pow(T / Tt, R(P.gamma / P.gm1));
+        v[3] = Tt - R(0.5) * Un * Un / consts<R>(P).Cp;
+        v[4] = pt * pow(T / Tt, consts<R>(P).ggm1);
         R* r = rec + (size_t)t * REC;
         for (int k = 0; k < 5; k++) r[k] = v[k];
         return;
@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(BLOCK) k_objective(MeshDev<R> m, Phys P, const
         if (kind == AFVM_OBJ_KINETIC_ENERGY) {
             // per-cell term in the working precision R, accumulated in double
             const R* r = rec + (size_t)t * REC;
-            R rho = r[R_P] / ((R(P.Cv) * r[R_T]) * R(P.gm1));
+            R rho = r[R_P] / ((consts<R>(P).Cv * r[R_T]) * consts<R>(P).gm1);
             v = (double)(R(0.5) * rho * (r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) * m.vol[t]);
         } else if (kind == AFVM_OBJ_SUM_T) {
             v = (double)rec[(size_t)t * REC + R_T];
@@ -325,12 +325,13 @@ void default_sources(Ctx* c, const R*& Srho, const R*& SrhoU, const R*& SrhoE) {
 template <typename R>
 int primal_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double dt, const double* dtDev,
                     const R* Srho, const R* SrhoU, const R* SrhoE, R* rhoN, R* rhoUN, R* rhoEN,
-                    double* dtcDev, double* objDev, cudaStream_t s) {
+                    double* dtcDev, double* objDev, cudaStream_t s, R* stages) {
     const MeshDev<R>& m = meshOf<R>(c);
     const Phys& P = c->phys;
     default_sources<R>(c, Srho, SrhoU, SrhoE);
     R* u1[3] = {(R*)c->u1[0], (R*)c->u1[1], (R*)c->u1[2]};
     R* u2[3] = {(R*)c->u2[0], (R*)c->u2[1], (R*)c->u2[2]};
+    if (stages) stage_views<R, R>(stages, m.nIC, u1, u2);
     R* outN[3] = {rhoN, rhoUN, rhoEN};
     const R* u0c[3] = {rho, rhoU, rhoE};
     const R* u1c[3] = {u1[0], u1[1], u1[2]};
@@ -391,10 +392,10 @@ int primal_run_dev(Ctx* c, R* rho, R* rhoU, R* rhoE, int nSteps, double dt0, dou
 
 template int primal_step_dev<double>(Ctx*, const double*, const double*, const double*, double, const double*,
                                      const double*, const double*, const double*, double*, double*, double*,
-                                     double*, double*, cudaStream_t);
+                                     double*, double*, cudaStream_t, double*);
 template int primal_step_dev<float>(Ctx*, const float*, const float*, const float*, double, const double*,
                                     const float*, const float*, const float*, float*, float*, float*, double*,
-                                    double*, cudaStream_t);
+                                    double*, cudaStream_t, float*);
 template int primal_run_dev<double>(Ctx*, double*, double*, double*, int, double, double, double, int,
                                     const double*, const double*, const double*, double*, double*, double*,
                                     cudaStream_t);

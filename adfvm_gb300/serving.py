@@ -105,6 +105,8 @@ class Slot(object):
         self.x = z()
         self.ckpt = [z() for _ in range(self.nck)]
         self.states = [z() for _ in range(k)]
+        self.last = z()                                        # output of the interval's last step
+        self.stages = [self.rcf.stage_buffer() for _ in range(k)]
         self.a = z()
         self.S = z()
         self.dS = [torch.zeros(s, dtype=torch.float64, device=self.dev) for s in shapes]
@@ -123,15 +125,18 @@ class Slot(object):
             r = self.rcf.step(self.x[0], self.x[1], self.x[2], self.dt, S=self.S, out=self.x, want_scalars=False)
 
     def _recompute(self):
-        for j in range(1, self.k):
-            y = self.states[j - 1]
-            self.rcf.step(y[0], y[1], y[2], self.dt, S=self.S, out=self.states[j], want_scalars=False)
+        # the interval's states and each step's RK stage states, for the adjoint steps
+        for j in range(self.k):
+            y = self.states[j]
+            out = self.states[j + 1] if j + 1 < self.k else self.last
+            self.rcf.step(y[0], y[1], y[2], self.dt, S=self.S, out=out, want_scalars=False, stages=self.stages[j])
 
     def _adjoint_k(self):
         torch = _torch()
         for j in range(self.k - 1, -1, -1):
             y = self.states[j]
-            r = self.rcf.adjoint_step(y[0], y[1], y[2], self.dt, self.a, obja=1.0, S=self.S, out=self.a)
+            r = self.rcf.adjoint_step(y[0], y[1], y[2], self.dt, self.a, obja=1.0, S=self.S, out=self.a,
+                                      stages=self.stages[j])
             # FP64 sensitivity accumulation (cmesh.computeSensitivity summed over time)
             s = (r[3][0].double() * self.dS[0]).sum() + (r[3][1].double() * self.dS[1]).sum() + \
                 (r[3][2].double() * self.dS[2]).sum()
@@ -207,7 +212,9 @@ class Slot(object):
         torch = _torch()
         es = 8 if self.td == torch.float64 else 4
         n = self.case.mesh.nInternalCells
-        return int(self.rcf.device_bytes + (self.nck + self.k + 4) * 5 * n * es + 3 * 5 * n * 8)
+        # checkpoints, interval states, last output, x, a, S; the k stage buffers; FP64 dS
+        return int(self.rcf.device_bytes + (self.nck + self.k + 4) * 5 * n * es + self.k * 10 * n * es +
+                   3 * 5 * n * 8)
 
 
 class SensitivityServer(object):

@@ -267,8 +267,16 @@ class RCF(object):
         return {n: (ms[i], cnt[i]) for i, n in enumerate(names) if cnt[i]}
 
     # ------------------------------------------------------------------ device path
-    def step(self, rho, rhoU, rhoE, dt, S=None, out=None, want_scalars=True):
-        """One step on CUDA tensors (reference layouts). Returns (rhoN, rhoUN, rhoEN, dtc, obj)."""
+    def stage_buffer(self):
+        """A device buffer for the two RK stage states of one step (afvm_primal_step_stages)."""
+        torch = _torch()
+        td = torch.float64 if self.dtype == np.float64 else torch.float32
+        return torch.empty(10 * self.mesh.nInternalCells, dtype=td, device='cuda:%d' % self.device)
+
+    def step(self, rho, rhoU, rhoE, dt, S=None, out=None, want_scalars=True, stages=None):
+        """One step on CUDA tensors (reference layouts). Returns (rhoN, rhoUN, rhoEN, dtc, obj).
+        stages: optional stage_buffer() that receives the step's RK stage states, for
+        adjoint_step(..., stages=) on the same state."""
         torch = _torch()
         stream = torch.cuda.current_stream(rho.device).cuda_stream
         if out is None:
@@ -276,19 +284,30 @@ class RCF(object):
         Sp = [None, None, None] if S is None else [C.c_void_p(s.data_ptr()) for s in S]
         dtc = C.c_double()
         obj = C.c_double()
-        st = L.lib().afvm_primal_step(self._ctx, C.c_void_p(rho.data_ptr()), C.c_void_p(rhoU.data_ptr()),
-                                      C.c_void_p(rhoE.data_ptr()), float(dt), Sp[0], Sp[1], Sp[2],
-                                      C.c_void_p(out[0].data_ptr()), C.c_void_p(out[1].data_ptr()),
-                                      C.c_void_p(out[2].data_ptr()),
-                                      C.byref(dtc) if want_scalars else None, C.byref(obj) if want_scalars else None,
-                                      C.c_void_p(stream))
-        L.check(st, self._ctx, 'afvm_primal_step')
+        sp = None if stages is None else C.c_void_p(self._check_stages(stages).data_ptr())
+        st = L.lib().afvm_primal_step_stages(self._ctx, C.c_void_p(rho.data_ptr()), C.c_void_p(rhoU.data_ptr()),
+                                             C.c_void_p(rhoE.data_ptr()), float(dt), Sp[0], Sp[1], Sp[2],
+                                             C.c_void_p(out[0].data_ptr()), C.c_void_p(out[1].data_ptr()),
+                                             C.c_void_p(out[2].data_ptr()), sp,
+                                             C.byref(dtc) if want_scalars else None,
+                                             C.byref(obj) if want_scalars else None, C.c_void_p(stream))
+        L.check(st, self._ctx, 'afvm_primal_step_stages')
         return out[0], out[1], out[2], dtc.value, obj.value
 
-    def adjoint_step(self, rho, rhoU, rhoE, dt, seeds, obja=1.0, S=None, out=None, source_grad=True):
+    def _check_stages(self, stages):
+        torch = _torch()
+        td = torch.float64 if self.dtype == np.float64 else torch.float32
+        if stages.dtype != td or stages.numel() < 10 * self.mesh.nInternalCells or not stages.is_contiguous() \
+                or not stages.is_cuda:
+            raise ValueError('stages: a contiguous device buffer of 10 x nInternalCells %s values' % td)
+        return stages
+
+    def adjoint_step(self, rho, rhoU, rhoE, dt, seeds, obja=1.0, S=None, out=None, source_grad=True, stages=None):
         """VJP of one step on CUDA tensors (afvm_adjoint_step): the adjoint of the input state
         (and of the sources) given the adjoint seeds of the output state and of the objective.
-        dt is held fixed, the CFL-sum output gets no seed (dtca = 0, apps/adjoint.py:268)."""
+        dt is held fixed, the CFL-sum output gets no seed (dtca = 0, apps/adjoint.py:268).
+        stages: the stage_buffer() a step(..., stages=) of this state filled; skips the
+        forward recompute."""
         torch = _torch()
         stream = torch.cuda.current_stream(rho.device).cuda_stream
         if out is None:
@@ -297,10 +316,12 @@ class RCF(object):
         Sp = [None, None, None] if S is None else [C.c_void_p(s.data_ptr()) for s in S]
         vp = lambda t: C.c_void_p(t.data_ptr())
         gp = [None, None, None] if Sg is None else [vp(t) for t in Sg]
-        st = L.lib().afvm_adjoint_step(self._ctx, vp(rho), vp(rhoU), vp(rhoE), float(dt), Sp[0], Sp[1], Sp[2],
-                                       vp(seeds[0]), vp(seeds[1]), vp(seeds[2]), 0.0, float(obja),
-                                       vp(out[0]), vp(out[1]), vp(out[2]), gp[0], gp[1], gp[2], C.c_void_p(stream))
-        L.check(st, self._ctx, 'afvm_adjoint_step')
+        sp = None if stages is None else vp(self._check_stages(stages))
+        st = L.lib().afvm_adjoint_step_stages(self._ctx, vp(rho), vp(rhoU), vp(rhoE), float(dt), Sp[0], Sp[1],
+                                              Sp[2], sp, vp(seeds[0]), vp(seeds[1]), vp(seeds[2]), 0.0, float(obja),
+                                              vp(out[0]), vp(out[1]), vp(out[2]), gp[0], gp[1], gp[2],
+                                              C.c_void_p(stream))
+        L.check(st, self._ctx, 'afvm_adjoint_step_stages')
         return out[0], out[1], out[2], Sg
 
     def sensitivity(self, grads, perts):

@@ -192,6 +192,17 @@ int afvm_primal_step(afvm_ctx* ctx, const void* rho, const void* rhoU, const voi
                      void* rhoN, void* rhoUN, void* rhoEN,
                      double* dtc_out, double* obj_out, void* stream);
 
+/* afvm_primal_step that also keeps the step's two intermediate SSP-RK3 stage states in
+ * stages (DEVICE, 10 x nInternalCells elements of the working precision: u1 then u2, each
+ * rho | rhoU | rhoE), at no extra cost - the step writes them anyway. Handing the same buffer
+ * to afvm_adjoint_step_stages with the same state, sources and dt lets the adjoint skip its
+ * forward recompute of the stages (the reference's reverse mode re-runs the forward,
+ * apps/adjoint.py:124-126 over adpy's generated gradient). No reference counterpart. */
+int afvm_primal_step_stages(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE,
+                            double dt, const void* S_rho, const void* S_rhoU, const void* S_rhoE,
+                            void* rhoN, void* rhoUN, void* rhoEN, void* stages,
+                            double* dtc_out, double* obj_out, void* stream);
+
 /* Same step with HOST buffers (pinned or pageable): copies in, steps, copies out. */
 int afvm_primal_step_host(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE,
                           double dt, const void* S_rho, const void* S_rhoU, const void* S_rhoE,
@@ -219,6 +230,14 @@ int afvm_adjoint_step(afvm_ctx* ctx, const void* rho, const void* rhoU, const vo
                       double dtca, double obja,
                       void* rhoa, void* rhoUa, void* rhoEa,
                       void* S_rhoa, void* S_rhoUa, void* S_rhoEa, void* stream);
+
+/* afvm_adjoint_step with the stage states a preceding afvm_primal_step_stages kept for this
+ * state (stages != NULL), instead of recomputing them: the outputs are bitwise the same. */
+int afvm_adjoint_step_stages(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE,
+                             double dt, const void* S_rho, const void* S_rhoU, const void* S_rhoE,
+                             const void* stages, const void* rhoNa, const void* rhoUNa,
+                             const void* rhoENa, double dtca, double obja, void* rhoa, void* rhoUa,
+                             void* rhoEa, void* S_rhoa, void* S_rhoUa, void* S_rhoEa, void* stream);
 
 /* FP64 sum over k of dot(grad[k], pert[k]) (adFVM/cpp/cmesh.cpp:309-340). DEVICE arrays of
  * n[k] doubles; result to *out (host) after the stream work completes. */

@@ -21,6 +21,7 @@ static Phys make_phys(const double* ph) {
     P.riemann = (int)ph[7];
     P.briemann = (int)ph[8];
     P.small = 1e-30;
+    finish_phys(P);
     return P;
 }
 

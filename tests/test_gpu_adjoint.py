@@ -133,3 +133,31 @@ def test_autograd_solve_matches_oracle_and_fd():
     for i in range(6):
         e = G.rel_err(g[i].cpu().numpy(), gref[i].numpy())
         assert e < 1e-10, (i, e)
+
+
+@pytest.mark.parametrize('name,precision', [('box8', 'fp64'), ('cyl32x16', 'fp64'), ('duct100_totalpt', 'fp64'),
+                                            ('box8', 'fp32')])
+def test_kept_stages_give_the_same_adjoint(name, precision):
+    """afvm_primal_step_stages / afvm_adjoint_step_stages: the adjoint on the stage states the
+    primal step kept is bitwise the adjoint that recomputes them, and the primal step itself is
+    unchanged by keeping them."""
+    case, mesh, x, S, dt = _setup(name)
+    rcf = RCF(mesh, case.bc, objective=case.objective, precision=precision, **case.config)
+    td = torch.float64 if precision == 'fp64' else torch.float32
+    d = [t.to(td).cuda() for t in x]
+    Sd = None if S is None else [torch.as_tensor(s).to(td).cuda() for s in S]
+    seeds = [t.to(td).cuda() for t in _seeds(x, 3)]
+    st = rcf.stage_buffer()
+    p0 = rcf.step(d[0], d[1], d[2], dt, S=Sd)
+    p1 = rcf.step(d[0], d[1], d[2], dt, S=Sd, stages=st)
+    for u, v in zip(p0[:3], p1[:3]):
+        assert torch.equal(u, v)
+    assert p0[3:] == p1[3:]
+    a0 = rcf.adjoint_step(d[0], d[1], d[2], dt, seeds, obja=1.0, S=Sd)
+    a1 = rcf.adjoint_step(d[0], d[1], d[2], dt, seeds, obja=1.0, S=Sd, stages=st)
+    for u, v in zip(a0[:3], a1[:3]):
+        assert torch.equal(u, v)
+    for u, v in zip(a0[3], a1[3]):
+        assert torch.equal(u, v)
+    with pytest.raises(ValueError):
+        rcf.adjoint_step(d[0], d[1], d[2], dt, seeds, S=Sd, stages=st[:10])
