@@ -71,6 +71,7 @@ class Physics(C.Structure):
 # name -> (restype, argtypes); every symbol declared in include/afvm.h
 SIGNATURES = {
     'afvm_mesh_build': (C.c_int, [C.POINTER(MeshIn), C.POINTER(MeshOut)]),
+    'afvm_mesh_build_device': (C.c_int, [C.POINTER(MeshIn), C.POINTER(MeshOut), _v]),
     'afvm_ctx_create': (C.c_int, [C.POINTER(MeshTensors), C.POINTER(PatchBC), C.POINTER(Physics),
                                   C.c_int32, C.c_int32, C.POINTER(_v)]),
     'afvm_ctx_destroy': (C.c_int, [_v]),

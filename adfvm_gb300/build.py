@@ -21,6 +21,8 @@ ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 HOST_FLAGS = ['-O3', '-fPIC', '-fopenmp', '-ffp-contract=off', '-std=c++17']
 NVCC_FLAGS = ARCH + ['-O3', '-lineinfo', '-std=c++17', '--expt-relaxed-constexpr',
                      '-Xcompiler', '-fPIC,-ffp-contract=off', '-I' + INCLUDE, '-I' + CSRC]
+# the device mesh builder rounds every product and sum as the host builder does
+PER_FILE_FLAGS = {'geometry_dev.cu': ['-fmad=false']}
 
 
 def _sources():
@@ -59,7 +61,7 @@ def build(verbose=False, force=False):
         obj = os.path.join(BUILD, f + '.o')
         objs.append(obj)
         if force or _newer(obj, [src] + headers):
-            jobs.append([NVCC] + NVCC_FLAGS + ['-c', src, '-o', obj])
+            jobs.append([NVCC] + NVCC_FLAGS + PER_FILE_FLAGS.get(f, []) + ['-c', src, '-o', obj])
 
     def run(cmd):
         if verbose:

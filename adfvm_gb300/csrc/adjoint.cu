@@ -24,7 +24,7 @@ constexpr int FADJ = 40;
 constexpr int CBAR = 20;   // per cell: primitive adjoint (5) then gradient adjoint (15)
 
 template <typename R>
-__global__ void __launch_bounds__(BLOCK) k_adj_flux(MeshDev<R> m, Phys P, const R* __restrict__ rec, R coef,
+__global__ void __launch_bounds__(FLUX_BLOCK, sizeof(R) == 8 ? 3 : 1) k_adj_flux(MeshDev<R> m, Phys P, const R* __restrict__ rec, R coef,
                                                     const R* __restrict__ ar, const R* __restrict__ au,
                                                     const R* __restrict__ ae, R* __restrict__ fadj, int inviscid) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
@@ -271,7 +271,7 @@ int adjoint_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double 
     R* cbar = (R*)c->cbar;
     R* sb = (R*)c->sbar;
     const R* rec = (const R*)c->rec;
-    int nbF = nblocks(m.nF), nbC = nblocks(m.nIC);
+    int nbC = nblocks(m.nIC);
     const double beta[3] = {1.0, 1. / 4, 2. / 3};
     for (int st = 2; st >= 0; st--) {
         const R* const* u = st == 0 ? u0c : (st == 1 ? u1c : u2c);
@@ -284,7 +284,8 @@ int adjoint_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double 
         R coef = (R)(-beta[st] * dt);
         {
             ProfScope ps(c, KID_ADJ_FLUX, s);
-            k_adj_flux<R><<<nbF, BLOCK, 0, s>>>(m, P, rec, coef, ain[0], ain[1], ain[2], fadj, inviscid);
+            k_adj_flux<R><<<(m.nF + FLUX_BLOCK - 1) / FLUX_BLOCK, FLUX_BLOCK, 0, s>>>(m, P, rec, coef, ain[0], ain[1],
+                                                                                   ain[2], fadj, inviscid);
         }
         {
             ProfScope ps(c, KID_ADJ_GATHER, s);

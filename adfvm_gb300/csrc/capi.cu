@@ -110,6 +110,11 @@ int upload_mesh(Ctx* c, const HostTables& h, MeshDev<R>& m) {
     if ((st = upload(c, &m.nrm, cast<R>(h.nrm)))) return st;
     if ((st = upload(c, &m.area, cast<R>(h.area)))) return st;
     if ((st = upload(c, &m.dlt, cast<R>(h.dlt)))) return st;
+    {
+        std::vector<double> r(h.dlt.size());
+        for (size_t i = 0; i < r.size(); i++) r[i] = 1.0 / h.dlt[i];
+        if ((st = upload(c, &m.rdlt, cast<R>(r)))) return st;
+    }
     if ((st = upload(c, &m.du, cast<R>(h.du)))) return st;
     if ((st = upload(c, &m.lw, cast<R>(h.lw)))) return st;
     if ((st = upload(c, &m.qw, cast<R>(h.qw)))) return st;

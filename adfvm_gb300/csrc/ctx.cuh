@@ -10,6 +10,12 @@
 namespace afvm {
 
 constexpr int BLOCK = 256;
+// the face kernels hold 160-240 registers a thread in FP64: 128-thread blocks capped to three
+// per SM (12 warps, a few registers spilled to L1 in the VJP) keep more FP64 instructions in
+// flight than one 256-thread block (8 warps); in FP32 the forward flux is capped at 64
+// registers (32 warps). Measured at 128^3: FP64 k_flux 5.47 -> 4.93 ms, k_adj_flux 11.08 ->
+// 10.52 ms, FP32 k_flux 0.240 -> 0.217 ms.
+constexpr int FLUX_BLOCK = 128;
 
 // boundary-condition kind codes stored per ghost cell (3 bits per field: U, T, p)
 constexpr int GK_COPY = 0;     // zeroGradient / empty / cyclic: value of the source cell
@@ -26,6 +32,7 @@ struct MeshDev {
     const R* nrm;             // 3 x nF (SoA)
     const R* area;            // nF
     const R* dlt;             // nF  deltas
+    const R* rdlt;            // nF  1/deltas (the viscous snGrad divisor, mesh-only)
     const R* du;              // 3 x nF deltasUnit
     const R* lw;              // 2 x nF linearWeights
     const R* qw;              // 6 x nF quadraticWeights (side0 xyz, side1 xyz)

@@ -15,7 +15,7 @@ template <typename R>
 struct FaceIn {
     R UP[3], TP, pP, UN[3], TN, pN;                    // owner cell and neighbour (or ghost) primitives
     R gUP[9], gTP[3], gpP[3], gUN[9], gTN[3], gpN[3];  // gradients ([component][direction])
-    R N[3], D[3], lw0, lw1, qw0[3], qw1[3], delta;     // normals, deltasUnit, weights, deltas
+    R N[3], D[3], lw0, lw1, qw0[3], qw1[3], rdelta;    // normals, deltasUnit, weights, 1/deltas
 };
 
 template <typename R>
@@ -82,7 +82,7 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
             for (int k = 0; k < 9; k++) gUF[k] = R(0.5) * (in.gUP[k] + in.gUN[k]);
         }
     }
-    if (!inviscid) viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, UF, gTF, gUF, in.D, in.N, in.delta, F);
+    if (!inviscid) viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, UF, gTF, gUF, in.D, in.N, in.rdelta, F);
     R aF = sqrt_(consts<R>(P).Cp * TF * consts<R>(P).gm1);
     maxaF = fabs(dot3(UF, in.N)) + aF;
 }
@@ -308,11 +308,10 @@ AFVM_HD void laxf_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rho
 // RCF.viscousFlux: F[1..3] += -sigma, F[4] += -(q + sigma.UF)
 template <typename R>
 AFVM_HD void viscous_vjp(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, const R* UF, const R* gTF,
-                         const R* gUF, const R* D, const R* N, R delta, const R* Fb, R& TLb, R& TRb, R* ULb, R* URb,
+                         const R* gUF, const R* D, const R* N, R rdel, const R* Fb, R& TLb, R& TRb, R* ULb, R* URb,
                          R& TFb, R* UFb, R* gTFb, R* gUFb) {
     R mu = viscosity<R>(P, TF);
     R kappa = mu * consts<R>(P).kFac;
-    R rdel = rcp(delta);
     R snT = (TR - TL) * rdel;
     R gTD = dot3(gTF, D);
     R gT[3];
@@ -386,7 +385,7 @@ AFVM_HD void face_vjp(const Phys& P, int kind, bool inviscid, const FaceIn<R>& i
         conservative_vjp<R>(P, in.UN, in.TN, in.pN, rhob, rhoUb, rhoEb, o.UN, o.TN, o.pN);
         if (!inviscid) {
             R TFb = R(0), UFb[3] = {R(0), R(0), R(0)};
-            viscous_vjp<R>(P, in.TP, in.TN, in.UP, in.UN, in.TN, in.UN, in.gTN, in.gUN, in.D, in.N, in.delta, Fb,
+            viscous_vjp<R>(P, in.TP, in.TN, in.UP, in.UN, in.TN, in.UN, in.gTN, in.gUN, in.D, in.N, in.rdelta, Fb,
                            o.TP, o.TN, o.UP, o.UN, TFb, UFb, o.gTN, o.gUN);
             o.TN += TFb;
             for (int k = 0; k < 3; k++) o.UN[k] += UFb[k];
@@ -426,7 +425,7 @@ AFVM_HD void face_vjp(const Phys& P, int kind, bool inviscid, const FaceIn<R>& i
         }
         R TFb = R(0), UFb[3] = {R(0), R(0), R(0)}, gTFb[3] = {R(0), R(0), R(0)}, gUFb[9];
         for (int k = 0; k < 9; k++) gUFb[k] = R(0);
-        viscous_vjp<R>(P, in.TP, in.TN, in.UP, in.UN, TF, UF, gTF, gUF, in.D, in.N, in.delta, Fb, o.TP, o.TN, o.UP,
+        viscous_vjp<R>(P, in.TP, in.TN, in.UP, in.UN, TF, UF, gTF, gUF, in.D, in.N, in.rdelta, Fb, o.TP, o.TN, o.UP,
                        o.UN, TFb, UFb, gTFb, gUFb);
         if (chr) {
             o.TN += TFb;

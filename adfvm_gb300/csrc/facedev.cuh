@@ -49,7 +49,7 @@ __device__ __forceinline__ void load_face(const MeshDev<R>& m, const R* __restri
     }
     in.lw0 = m.lw[f];
     in.lw1 = m.lw[nF + f];
-    in.delta = m.dlt[f];
+    in.rdelta = m.rdlt[f];
 }
 
 }  // namespace afvm

@@ -251,13 +251,13 @@ AFVM_HD void laxf(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R
     F[4] = R(0.5) * ((rhoEL + pL) * UnL + (rhoER + pR) * UnR) - ha * (rhoER - rhoEL);
 }
 
-// RCF.viscousFlux (adFVM/density.py:192-222): adds -sigma to F[1..3] and -(q + sigma.UF) to F[4]
+// RCF.viscousFlux (adFVM/density.py:192-222): adds -sigma to F[1..3] and -(q + sigma.UF) to F[4];
+// rdel = 1/deltas (a mesh table), the divisor of snGrad (op.py:66-67)
 template <typename R>
 AFVM_HD void viscous(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, const R* UF,
-                                        const R* gTF, const R* gUF, const R* D, const R* N, R delta, R* F) {
+                                        const R* gTF, const R* gUF, const R* D, const R* N, R rdel, R* F) {
     R mu = viscosity<R>(P, TF);
     R kappa = mu * consts<R>(P).kFac;
-    R rdel = rcp(delta);
     R snT = (TR - TL) * rdel;
     R gTD = dot3(gTF, D);
     R gT[3];

@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(BLOCK) k_grad(MeshDev<R> m, R* __restrict__ re
 }
 
 template <typename R>
-__global__ void __launch_bounds__(BLOCK) k_flux(MeshDev<R> m, Phys P, const R* __restrict__ rec,
+__global__ void __launch_bounds__(FLUX_BLOCK, sizeof(R) == 8 ? 3 : 8) k_flux(MeshDev<R> m, Phys P, const R* __restrict__ rec,
                                                 R* __restrict__ fflux, int inviscid) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= m.nF) return;
@@ -299,7 +299,7 @@ void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const R*
     int inviscid = (P.muModel == AFVM_MU_CONSTANT && P.mu0 == 0.0) ? 1 : 0;
     {
         ProfScope ps(c, KID_FLUX, s);
-        k_flux<R><<<nblocks(m.nF), BLOCK, 0, s>>>(m, P, rec, ff, inviscid);
+        k_flux<R><<<(m.nF + FLUX_BLOCK - 1) / FLUX_BLOCK, FLUX_BLOCK, 0, s>>>(m, P, rec, ff, inviscid);
     }
     int nb = nblocks(m.nIC);
     ProfScope ps(c, KID_UPDATE, s);

@@ -8,6 +8,8 @@ split and alphabetical ``sortedPatches`` (238-249, 100-101), the native geometry
 compiled step function takes them (mesh.py:27-37, 870-881).
 """
 import copy
+import ctypes as C
+
 import numpy as np
 
 from . import _lib as L
@@ -31,12 +33,14 @@ class Mesh(object):
         self.boundary = {}
 
     @classmethod
-    def create(cls, meshData):
+    def create(cls, meshData, device=None):
+        """device: None builds the geometry on the host (afvm_mesh_build, OpenMP); a CUDA
+        ordinal builds it there (afvm_mesh_build_device) - the same bits either way."""
         self = cls()
-        self.build(meshData)
+        self.build(meshData, device)
         return self
 
-    def build(self, meshData):
+    def build(self, meshData, device=None):
         points, faces, owner, neighbour, boundary = meshData
         self.points = np.ascontiguousarray(points, np.float64)
         self.faces = np.ascontiguousarray(faces, np.int32)
@@ -65,7 +69,10 @@ class Mesh(object):
         self.patches = self.localPatches + self.remotePatches
         self.sortedPatches = sorted(self.localPatches)
         self.defaultBoundary = self.getDefaultBoundary()
-        self._geometry(neighbour)
+        if device is None:
+            self._geometry(neighbour)
+        else:
+            self._geometry_device(neighbour, device)
         self.volumesL = self.volumes[self.owner]
         self.volumesR = self.volumes[self.neighbour[:self.nInternalFaces]]
         self.nRemoteCells = self.nCells - self.nLocalCells
@@ -147,3 +154,33 @@ class Mesh(object):
         mt = L.MeshTensors(*([L.dptr(keep[a]) for a in Mesh.gradFields] + [L.iptr(keep[a]) for a in Mesh.intFields]
                              + [getattr(self, a) for a in Mesh.constants] + [len(self.sortedPatches), patches]))
         return mt, (keep, patches)
+
+    def _geometry_device(self, neighbour, device):
+        import torch
+        nF, nIF, nIC, nC = self.nFaces, self.nInternalFaces, self.nInternalCells, self.nCells
+        dev = torch.device('cuda', device)
+        up = lambda a: torch.as_tensor(np.ascontiguousarray(a)).to(dev)
+        points, faces, owner, nbr = up(self.points), up(self.faces), up(self.owner), up(neighbour)
+        shapes = {'normals': ((nF, 3), torch.float64), 'faceCentres': ((nF, 3), torch.float64),
+                  'areas': ((nF, 1), torch.float64), 'cellCentres': ((nC, 3), torch.float64),
+                  'volumes': ((nIC, 1), torch.float64), 'neighbour': ((nF,), torch.int32),
+                  'deltas': ((nF, 1), torch.float64), 'deltasUnit': ((nF, 3), torch.float64),
+                  'weights': ((nF, 1), torch.float64), 'linearWeights': ((nF, 2), torch.float64),
+                  'quadraticWeights': ((nF, 2, 3), torch.float64), 'cellFaces': ((nIC, 6), torch.int32),
+                  'cellOwner': ((nIC, 6), torch.int32), 'cellNeighbours': ((nIC, 6), torch.int32),
+                  'cellNeighboursMatOp': ((nIC, 6), torch.int32)}
+        out = {k: torch.empty(s, dtype=t, device=dev) for k, (s, t) in shapes.items()}
+        vp = lambda t: C.c_void_p(t.data_ptr())
+        patches = self.patchTable(self.patches)
+        mi = L.MeshIn(len(self.points), C.cast(vp(points), L._d), nF, C.cast(vp(faces), L._i), nIF,
+                      C.cast(vp(owner), L._i), C.cast(vp(nbr), L._i), nIC, len(self.patches), patches)
+        d = lambda k: C.cast(vp(out[k]), L._d)
+        i = lambda k: C.cast(vp(out[k]), L._i)
+        mo = L.MeshOut(d('normals'), d('faceCentres'), d('areas'), d('cellCentres'), d('volumes'), i('neighbour'),
+                       d('deltas'), d('deltasUnit'), d('weights'), d('linearWeights'), d('quadraticWeights'),
+                       i('cellFaces'), i('cellOwner'), i('cellNeighbours'), i('cellNeighboursMatOp'), 0)
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        L.check(L.lib().afvm_mesh_build_device(mi, mo, C.c_void_p(stream)), what='afvm_mesh_build_device')
+        for k, t in out.items():
+            setattr(self, k, t.cpu().numpy())
+        self.nLocalCells = int(mo.nLocalCells)

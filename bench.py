@@ -65,13 +65,27 @@ def algorithmic_bytes(kernel, nIC, nIF, nF, nG, es):
         return nIC * (6 * (4 + es) + 3 * 5 * es + 5 * es) + nF * FREC * es
     if kernel == 'k_prim':
         return nIC * 10 * es + nG * (8 + 5 * es + 5 * es)
+    if kernel == 'k_adj_flux':
+        # per face: own+nbr (8), A/V weights 2, geometry 15, 40-value adjoint record write;
+        # cell records and the 5 adjoint seeds of every cell read once
+        return nF * (8 + 17 * es + 40 * es) + (nIC + nG) * REC * es + nIC * 5 * es
     return 0
+
+
+# the cell-step model of compulsory bytes (two passes per stage, every array once a pass): FP64
+# primal 2,904 B, FP32 primal 1,524 B, FP64 adjoint 6,288 B (forward recompute + reverse); the
+# FP32 adjoint scaled from the FP64 one by the primal ratio
+STEP_BYTES = {('primal', 8): 2904, ('primal', 4): 1524, ('adjoint', 8): 6288, ('adjoint', 4): 3300}
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch from an ncu capture of
 # the 64^3 box (798,720 faces, 262,144 cells; profiles/), scaled to a launch of the benchmarked
 # mesh by its number of faces (the kernel's traffic grows in proportion to the faces)
-MEASURED_TRAFFIC = {('k_flux', 8): (174.24e6, 798720)}
+MEASURED_TRAFFIC = {('k_flux', 8): (174.24e6, 798720), ('k_flux', 4): (81.56e6, 798720),
+                    ('k_adj_flux', 8): (387.01e6, 798720)}
+# FP64 thread instructions per face (DADD, DMUL, DFMA) of a launch in the same captures
+# (smsp__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on)
+MEASURED_FP64_INST = {'k_flux': (70.6, 155.4, 216.0), 'k_adj_flux': (117.0, 283.4, 428.9)}
 
 
 def measured_traffic(kernel, es, nF):
@@ -305,22 +319,66 @@ def measure(case, precision, args, local, dist, world, clocks):
            'primal_only': round(nIC * ke * world / te / 1e6, 3), 'adjoint_only': round(nIC * ke * world / ta / 1e6, 3)}
     kernels = {k: {'ms_total': round(v[0], 4), 'launches': v[1], 'ms_avg': round(v[0] / v[1], 5)}
                for k, v in prof.items()}
-    top = max(prof.items(), key=lambda kv: kv[1][0])[0]
+    # the dominant kernel of the primal+adjoint step
+    both = {}
+    for pr in (prof, prof_a):
+        for k, v in pr.items():
+            t = both.setdefault(k, [0.0, 0])
+            t[0] += v[0]
+            t[1] += v[1]
+    top = max(both.items(), key=lambda kv: kv[1][0])[0]
     peak, peak_kind = peaks()
     alg = algorithmic_bytes(top, nIC, nIF, nF, nG, es)
-    avg_s = prof[top][0] / prof[top][1] / 1e3
+    avg_s = both[top][0] / both[top][1] / 1e3
     achieved = alg / avg_s / 1e9
     roofline = {'bound': 'hbm', 'kernel': top, 'achieved': round(achieved, 1), 'peak': peak,
                 'peak_source': peak_kind, 'unit': 'GB/s', 'frac': round(achieved / peak, 4),
-                'algorithmic_bytes_per_launch': int(alg), 'traffic': measured_traffic(top, es, nF)}
+                'algorithmic_bytes_per_launch': int(alg), 'traffic': measured_traffic(top, es, nF),
+                'share_of_step': round(both[top][0] / (ms_p + ms_a), 3)}
+    step_model = {'unit': 'GB/s', 'peak': peak,
+                  'primal': round(vp * 1e6 * STEP_BYTES[('primal', es)] / 1e9, 1),
+                  'adjoint': round(va * 1e6 * STEP_BYTES[('adjoint', es)] / 1e9, 1),
+                  'bytes_per_cell_step': {'primal': STEP_BYTES[('primal', es)],
+                                          'adjoint': STEP_BYTES[('adjoint', es)]}}
+    step_model['primal_frac'] = round(step_model['primal'] / peak, 4)
+    step_model['adjoint_frac'] = round(step_model['adjoint'] / peak, 4)
     return {'value': round(value, 3), 'ms_per_step': round((ms_p + ms_a) / K, 4),
             'primal': {'value': round(vp, 3), 'ms_per_step': round(ms_p / K, 4)},
             'adjoint': {'value': round(va, 3), 'ms_per_step': round(ms_a / K, 4)},
-            'roofline': roofline, 'kernels': kernels,
+            'roofline': roofline, 'kernels': kernels, 'step_model': step_model,
+            '_top': (top, avg_s, nF),
             'adjoint_kernels': {k: {'ms_total': round(v[0], 4), 'launches': v[1], 'ms_avg': round(v[0] / v[1], 5)}
                                 for k, v in prof_a.items()},
             'gpu_launches': int(sum(v[1] for v in prof.values()) + sum(v[1] for v in prof_a.values())),
             'e2e': e2e, 'clocks': clk, 'device_bytes': rcf.device_bytes}
+
+
+def mesh_build_timing(case, local, reps=3):
+    """Geometry/connectivity build of the workload mesh on the host (afvm_mesh_build, all
+    cores) and on the GPU (afvm_mesh_build_device, host arrays in and out), and the solver
+    context set-up (tables + upload) - the admission cost of a new mesh."""
+    import torch
+    from adfvm_gb300.mesh import Mesh
+    from adfvm_gb300.solver import RCF
+    md = case.meshData
+    Mesh.create(md, device=local)
+    th, td = [], []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        Mesh.create(md)
+        th.append(time.perf_counter() - t0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Mesh.create(md, device=local)
+        td.append(time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    rcf = RCF(case.mesh, case.bc, objective=case.objective, device=local, **case.config)
+    tc = time.perf_counter() - t0
+    rcf.close()
+    return {'host_ms': round(1e3 * min(th), 1), 'device_ms': round(1e3 * min(td), 1),
+            'host_threads': os.cpu_count(), 'context_ms': round(1e3 * tc, 1),
+            'note': 'device_ms includes the upload of points/faces/owner/neighbour and the download of '
+                    'every result to host arrays'}
 
 
 def serving_bench(local, n_requests=48, lams=(5.0, 20.0, 100.0, 200.0), seed=4, nplain=8):
@@ -425,17 +483,33 @@ def main():
                                 'the adjoint steps walk them backwards as a sweep does; primal and adjoint '
                                 'also reported alone'),
             'primal': m64['primal'], 'adjoint': m64['adjoint'],
-            'roofline': m64['roofline'], 'kernels': m64['kernels'], 'adjoint_kernels': m64['adjoint_kernels'],
-            'gpu_launches': m64['gpu_launches'],
+            'roofline': m64['roofline'], 'step_model': m64['step_model'], 'kernels': m64['kernels'],
+            'adjoint_kernels': m64['adjoint_kernels'], 'gpu_launches': m64['gpu_launches'],
             'e2e': m64['e2e'], 'clocks': clk}
     if m32 is not None:
         m32.pop('clocks', None)
-        line['fp32'] = {k: m32[k] for k in ('value', 'ms_per_step', 'primal', 'adjoint', 'roofline', 'kernels',
-                                            'adjoint_kernels', 'e2e')}
+        line['fp32'] = {k: m32[k] for k in ('value', 'ms_per_step', 'primal', 'adjoint', 'roofline', 'step_model',
+                                            'kernels', 'adjoint_kernels', 'e2e')}
     if args.serving and rank == 0:
         line['serving'] = serving_bench(local)
+    if rank == 0:
+        line['mesh_build'] = mesh_build_timing(case, local)
     from adfvm_gb300 import _lib
     line['fma_peak_tflops'] = {'fp64': round(_lib.fma_peak(local, True), 2), 'fp32': round(_lib.fma_peak(local, False), 2)}
+    top, avg_s, nF = m64.pop('_top')
+    if args.precision == 'fp64' and top in MEASURED_FP64_INST:
+        # the FP64 kernels are bound by the FP64 pipe, not HBM: counted FP64 instructions per
+        # face (ncu) x faces / the launch's CUDA-event time, against the measured FMA peak
+        da, dm, df = MEASURED_FP64_INST[top]
+        flops = (da + dm + 2 * df) * nF
+        fpk = line['fma_peak_tflops']['fp64']
+        ach = flops / avg_s / 1e12
+        line['compute_roofline'] = {
+            'bound': 'fp64', 'kernel': top, 'achieved': round(ach, 3), 'peak': fpk, 'unit': 'TFLOP/s',
+            'frac': round(ach / fpk, 4), 'flops_per_face': round(da + dm + 2 * df, 1),
+            'issue_frac': round((da + dm + df) * nF / avg_s / (fpk * 1e12 / 2), 4),
+            'peak_source': 'afvm_fma_peak (a DFMA loop on this GPU, FMA = 2 flops)',
+            'note': 'issue_frac counts DADD/DMUL/DFMA as one FP64 pipe issue each'}
     if rank == 0 and not args.no_cpu_baseline:
         line['cpu_baseline'] = cpu_baseline(args, os.cpu_count() or 1, case=case)
     if rank == 0:

@@ -90,6 +90,12 @@ typedef struct afvm_mesh_out {   /* all buffers caller-allocated */
  * rank (adFVM/mesh.py:758-819). */
 int afvm_mesh_build(const afvm_mesh_in* in, afvm_mesh_out* out);
 
+/* The same build on the GPU (one thread per face or cell), bitwise equal to afvm_mesh_build:
+ * in->points, faces, owner, neighbour and every array of out are DEVICE pointers; in->patches
+ * is a host array. Runs on stream and returns when the build is complete. Replaces the same
+ * reference functions as afvm_mesh_build. */
+int afvm_mesh_build_device(const afvm_mesh_in* in, afvm_mesh_out* out, void* stream);
+
 /* ---- solver context ---- */
 
 /* The mesh tensors in the order of Mesh.getTensor() (adFVM/mesh.py:27-32, 870-872) and

@@ -62,6 +62,13 @@ def random_faces(n, seed, char=False):
     return X
 
 
+def native_in(X):
+    """The native face input: slot 54 holds 1/delta (a mesh table of the device path)."""
+    Xn = np.array(X, np.float64)
+    Xn[:, 54] = 1.0 / Xn[:, 54]
+    return Xn
+
+
 def torch_face(kind, X, cfg):
     """The oracle's face physics for a batch of faces (RCF.flux / RCF.boundaryFlux)."""
     obj = types.SimpleNamespace()
@@ -146,7 +153,7 @@ def dp(a):
 def test_face_forward_matches_oracle(host, kind, cfg):
     X = random_faces(64, 11)
     F = np.zeros((64, 6))
-    host.afvm_host_face(64, KINDS[kind], 1 if cfg['mu'] == 0.0 else 0, dp(phys(cfg)), dp(X), dp(F))
+    host.afvm_host_face(64, KINDS[kind], 1 if cfg['mu'] == 0.0 else 0, dp(phys(cfg)), dp(native_in(X)), dp(F))
     ref = torch_face(kind, torch.as_tensor(X), cfg).numpy()
     err = np.abs(F - ref) / (np.abs(ref).max(axis=0) + 1e-300)
     assert err.max() < 1e-12, err.max(axis=0)
@@ -158,7 +165,7 @@ def test_face_adjoint_matches_autograd(host, kind, cfg):
     X = random_faces(n, 12)
     Fb = np.random.default_rng(13).normal(size=(n, 5))
     out = np.zeros((n, 40))
-    host.afvm_host_face_vjp(n, KINDS[kind], 1 if cfg['mu'] == 0.0 else 0, dp(phys(cfg)), dp(X), dp(Fb), dp(out))
+    host.afvm_host_face_vjp(n, KINDS[kind], 1 if cfg['mu'] == 0.0 else 0, dp(phys(cfg)), dp(native_in(X)), dp(Fb), dp(out))
     Xt = torch.as_tensor(X).clone().requires_grad_(True)
     F = torch_face(kind, Xt, cfg)
     J = (F[:, :5] * torch.as_tensor(Fb)).sum()
