@@ -315,10 +315,10 @@ extern "C" int afvm_mesh_build_device(const afvm_mesh_in* in, afvm_mesh_out* out
         e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) {
             status = AFVM_ERR_CUDA;
-        } else if (herr & (E_COUNT | E_SLOTS)) {
-            status = AFVM_ERR_UNSUPPORTED;     // not a quad face / not a hex cell
+        } else if (herr & (E_OWNER | E_POINT | E_NEIGHBOUR)) {
+            status = AFVM_ERR_BAD_ARG;         // an index out of range (its faces claimed no slots)
         } else if (herr) {
-            status = AFVM_ERR_BAD_ARG;
+            status = AFVM_ERR_UNSUPPORTED;     // not a quad face / not a hex cell
         } else {
             k_face_geometry<<<nb(nFaces), TB, 0, s>>>(nFaces, in->faces, in->points, out->normals,
                                                       out->faceCentres, out->areas);
