@@ -19,7 +19,7 @@ AFVM_BC_ZERO_GRADIENT, AFVM_BC_FIXED_VALUE, AFVM_BC_SYMMETRY_PLANE, AFVM_BC_CYCL
     AFVM_BC_CBC_TOTAL_PT = range(6)
 AFVM_RIEMANN_ROE, AFVM_RIEMANN_LF = 0, 1
 AFVM_MU_CONSTANT, AFVM_MU_SUTHERLAND = 0, 1
-AFVM_OBJ_NONE, AFVM_OBJ_KINETIC_ENERGY, AFVM_OBJ_DRAG, AFVM_OBJ_SUM_T = range(4)
+AFVM_OBJ_NONE, AFVM_OBJ_KINETIC_ENERGY, AFVM_OBJ_DRAG, AFVM_OBJ_SUM_T, AFVM_OBJ_VANE = range(5)
 
 _d = C.POINTER(C.c_double)
 _i = C.POINTER(C.c_int32)
@@ -68,6 +68,13 @@ class Physics(C.Structure):
                 ('objective', C.c_int32), ('objective_patch', C.c_int32)]
 
 
+class ObjectiveVane(C.Structure):
+    _fields_ = [('nPlaneCells', C.c_int32), ('planeCells', C.POINTER(C.c_int32)), ('planeAreas', _d),
+                ('normal', C.c_double * 3), ('ptin', C.c_double), ('nHeatPatches', C.c_int32),
+                ('heatPatches', C.POINTER(C.c_int32)), ('heatWeights', C.POINTER(_d)), ('Tw', C.c_double),
+                ('a', C.c_double), ('b', C.c_double)]
+
+
 # name -> (restype, argtypes); every symbol declared in include/afvm.h
 SIGNATURES = {
     'afvm_mesh_build': (C.c_int, [C.POINTER(MeshIn), C.POINTER(MeshOut)]),
@@ -79,6 +86,7 @@ SIGNATURES = {
     'afvm_ctx_precision': (C.c_int, [_v]),
     'afvm_ctx_device_bytes': (C.c_int64, [_v]),
     'afvm_set_bc_value': (C.c_int, [_v, C.c_int32, C.c_int32, _d]),
+    'afvm_set_objective_vane': (C.c_int, [_v, C.POINTER(ObjectiveVane)]),
     'afvm_primal_step': (C.c_int, [_v, _v, _v, _v, C.c_double, _v, _v, _v, _v, _v, _v, _d, _d, _v]),
     'afvm_primal_step_stages': (C.c_int, [_v, _v, _v, _v, C.c_double, _v, _v, _v, _v, _v, _v, _v, _d, _d, _v]),
     'afvm_primal_step_host': (C.c_int, [_v, _v, _v, _v, C.c_double, _v, _v, _v, _v, _v, _v, _d, _d, _v]),

@@ -40,12 +40,14 @@ class Adjoint(object):
         m = self.mesh
         nT, nS = len(Mesh.gradFields) + len(Mesh.intFields), len(m.getScalar())
         base = 4 + nT + nS
-        nBC = len(p.getBoundaryTensor(1))
+        nBC = len(p.getBoundaryTensor(1)) + len(p.extraArgs())
         primal_in = inputs[:base + 3 + nBC]
         rest = inputs[base + 3 + nBC:]
         if len(rest) != 6:
             raise ValueError('adjoint map: expected 3 adjoint fields, dtca, obja and scaling after the primal inputs')
-        p._apply_bc_tensors(list(primal_in[base + 3:]))
+        nB = len(p.getBoundaryTensor(1))
+        p._apply_bc_tensors(list(primal_in[base + 3:base + 3 + nB]))
+        p._apply_extra(list(primal_in[base + 3 + nB:]))
         n = m.nInternalCells
         dev = 'cuda:%d' % p.device
         td = torch.float64 if p.dtype == np.float64 else torch.float32

@@ -177,6 +177,47 @@ def duct(n=100, Tt=310.0, pt=1.05e5, U0=50.0, T0=300.0, p0=1e5, direction=True):
     return case
 
 
+def vane_channel(nx=64, ny=24, Tt=310.0, pt=1.08e5, U0=100.0, T0=300.0, p0=1e5, Tw=350.0, a=0.4, b=1e-5,
+                 stretch=0.3, reference_constants=False):
+    """Channel with the turbine-vane objective (adFVM/objectives/vane.py): the plane x = 0.052641
+    and the ``pressure``/``suction`` walls of that file, a total-pressure inlet (CBC_TOTAL_PT, x
+    direction) and a characteristic outlet (CBC_UPT); no-slip walls (fixedValue U = 0,
+    zeroGradient T, p), empty front/back; Sutherland viscosity, Roe. The objective uses this
+    inlet's total pressure for ptin, a wall temperature of 350 K and weights a = 0.4 (the
+    reference's) and b = 1e-5 (the reference has 0; a non-zero b exercises the heat term).
+    reference_constants=True keeps the constants of objectives/vane.py itself (ptin 175158,
+    Tw 300, a 0.4, b 0), as its own objective function hard-codes them."""
+    from . import vane
+    md = meshgen.channel(nx, ny, stretch=stretch)
+    bnd = md[4]
+
+    def kind(patch, b_, f):
+        nf = b_['nFaces']
+        if patch == 'inlet':
+            d = np.zeros((nf, 3)); d[:, 0] = 1.0
+            return {'type': 'CBC_TOTAL_PT', 'Tt': np.full((nf, 1), Tt), 'pt': np.full((nf, 1), pt), 'direction': d}
+        if patch == 'outlet':
+            u = np.zeros((nf, 3)); u[:, 0] = U0
+            return {'type': 'CBC_UPT', 'U0': u, 'T0': np.full((nf, 1), T0), 'p0': np.full((nf, 1), p0)}
+        if patch in ('pressure', 'suction'):
+            if f == 'U':
+                return {'type': 'fixedValue', 'value': np.zeros((nf, 3))}
+            return {'type': 'zeroGradient'}
+        return {'type': 'empty'}
+    case = Case('vane_channel%dx%d' % (nx, ny), md, _uniform_bc(bnd, kind), None, None, None,
+                config={'fixedTimeStep': True})
+    mesh = case.build_mesh()
+    case.objective = vane.options(mesh) if reference_constants else vane.options(mesh, ptin=pt, Tw=Tw, a=a, b=b)
+    nc = mesh.nInternalCells
+    case.U = np.zeros((nc, 3)); case.U[:, 0] = U0
+    case.T = np.full((nc, 1), T0)
+    case.p = np.full((nc, 1), p0)
+    c = math.sqrt(GAMMA * R_GAS * T0)
+    dx = float(np.min(np.diff(np.unique(np.round(mesh.cellCentres[:nc, 0], 12)))))
+    case.dt = float(0.5 * dx / (U0 + c))
+    return case
+
+
 def conservative(case, gamma=GAMMA, Cp=CP):
     """Initial conservative state of a case: RCF.conservative (adFVM/density.py:173-181)."""
     Cv = Cp / gamma

@@ -15,6 +15,7 @@
 //                objective gradient (stage 1), primitive VJP and the SSP-RK reverse update.
 #include <cuda_runtime.h>
 #include "facedev.cuh"
+#include "vane.cuh"
 
 namespace afvm {
 
@@ -92,7 +93,8 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const
                                                      const R* __restrict__ ue,
                                                      const R* ainr, const R* ainu, const R* aine,
                                                      R* a1r, R* a1u, R* a1e, R* a0r, R* a0u, R* a0e, R* sb,
-                                                     double dt, int objective, int objStart, int objN, double obja) {
+                                                     double dt, int objective, int objStart, int objN, double obja,
+                                                     VaneDev vane) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m.nIC) return;
     const size_t n = m.nIC;
@@ -182,6 +184,23 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const
             pbar[R_T] += (R)(-obja * 0.5 * q * V * rho / T);
         } else if (objective == AFVM_OBJ_SUM_T) {
             pbar[R_T] += (R)obja;
+        } else if (objective == AFVM_OBJ_VANE) {
+            int q = vane.cellPlane[c];
+            if (q >= 0) {
+                double g5[5] = {0, 0, 0, 0, 0};
+                double U[3] = {rc[0], rc[1], rc[2]};
+                vane_cell_grad(P, vane, U, (double)rc[R_T], (double)rc[R_P], vane.planeArea[q], vane.sums[0],
+                               vane.sums[1], obja, g5);
+                for (int k = 0; k < 5; k++) pbar[k] += (R)g5[k];
+            }
+            if (vane.b != 0.0) {
+                for (int s = 0; s < 6; s++) {
+                    int e = m.accf[s * n + c];
+                    if (e < m.nIF) continue;          // owner-side boundary faces only
+                    double k = vane.bHeatCoef[e - m.nIF];
+                    if (k != 0.0) pbar[R_T] += (R)(-obja * vane.b * vane.rw2 * k);
+                }
+            }
         } else if (objective == AFVM_OBJ_DRAG) {
             for (int s = 0; s < 6; s++) {
                 int e = m.accf[s * n + c];
@@ -276,6 +295,7 @@ int adjoint_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double 
     for (int st = 2; st >= 0; st--) {
         const R* const* u = st == 0 ? u0c : (st == 1 ? u1c : u2c);
         launch_prim_grad<R>(c, u[0], u[1], u[2], s);
+        if (st == 1 && c->objective == AFVM_OBJ_VANE) launch_vane_sums<R>(c, s, nullptr, nullptr);
         // adjoint of this stage's output: a3 = seeds, a2 = A2, a1 = A1
         const R* ain[3];
         if (st == 2) { ain[0] = rhoNa; ain[1] = rhoUNa; ain[2] = rhoENa; }
@@ -295,15 +315,15 @@ int adjoint_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double 
         if (st == 2)
             k_adj_cell2<R, 2><<<nbC, BLOCK, 0, s>>>(m, P, rec, fadj, cbar, u[0], u[1], u[2], ain[0], ain[1], ain[2],
                                                     A2[0], A2[1], A2[2], rhoa, rhoUa, rhoEa, sb, dt, c->objective,
-                                                    c->objStart, c->objN, obja);
+                                                    c->objStart, c->objN, obja, c->vane);
         else if (st == 1)
             k_adj_cell2<R, 1><<<nbC, BLOCK, 0, s>>>(m, P, rec, fadj, cbar, u[0], u[1], u[2], ain[0], ain[1], ain[2],
                                                     A1[0], A1[1], A1[2], rhoa, rhoUa, rhoEa, sb, dt, c->objective,
-                                                    c->objStart, c->objN, obja);
+                                                    c->objStart, c->objN, obja, c->vane);
         else
             k_adj_cell2<R, 0><<<nbC, BLOCK, 0, s>>>(m, P, rec, fadj, cbar, u[0], u[1], u[2], ain[0], ain[1], ain[2],
                                                     nullptr, nullptr, nullptr, rhoa, rhoUa, rhoEa, sb, dt,
-                                                    c->objective, c->objStart, c->objN, obja);
+                                                    c->objective, c->objStart, c->objN, obja, c->vane);
     }
     if (Srhoa || SrhoUa || SrhoEa) {
         ProfScope ps(c, KID_ADJ_MISC, s);

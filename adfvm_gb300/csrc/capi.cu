@@ -419,7 +419,7 @@ int afvm_ctx_create(const afvm_mesh_tensors* mesh, const afvm_patch_bc* bcs, con
     if (phys->boundary_riemann != AFVM_RIEMANN_ROE && phys->boundary_riemann != AFVM_RIEMANN_LF)
         return AFVM_ERR_BAD_ARG;
     if (phys->mu_model != AFVM_MU_CONSTANT && phys->mu_model != AFVM_MU_SUTHERLAND) return AFVM_ERR_BAD_ARG;
-    if (phys->objective < AFVM_OBJ_NONE || phys->objective > AFVM_OBJ_SUM_T) return AFVM_ERR_BAD_ARG;
+    if (phys->objective < AFVM_OBJ_NONE || phys->objective > AFVM_OBJ_VANE) return AFVM_ERR_BAD_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
         cudaGetLastError();
@@ -515,6 +515,93 @@ int64_t afvm_ctx_device_bytes(const afvm_ctx* ctx) {
     if (!ctx) return 0;
     const Ctx* c = reinterpret_cast<const Ctx*>(ctx);
     return c->bytes + c->adjBytes;
+}
+
+int afvm_set_objective_vane(afvm_ctx* ctx, const afvm_objective_vane* v) {
+    if (!ctx) return AFVM_ERR_BAD_ARG;
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!v) return fail(c, AFVM_ERR_BAD_ARG, "afvm_set_objective_vane: null description");
+    if (c->objective != AFVM_OBJ_VANE) return fail(c, AFVM_ERR_BAD_ARG, "the context's objective is not AFVM_OBJ_VANE");
+    if (v->nPlaneCells < 0 || (v->nPlaneCells > 0 && (!v->planeCells || !v->planeAreas)))
+        return fail(c, AFVM_ERR_BAD_ARG, "afvm_set_objective_vane: plane cells");
+    if (v->nHeatPatches < 0 || (v->nHeatPatches > 0 && (!v->heatPatches || !v->heatWeights)))
+        return fail(c, AFVM_ERR_BAD_ARG, "afvm_set_objective_vane: heat patches");
+    if (!(v->ptin != 0.0) || !std::isfinite(v->ptin) || !std::isfinite(v->Tw) || !std::isfinite(v->a) ||
+        !std::isfinite(v->b))
+        return fail(c, AFVM_ERR_BAD_ARG, "afvm_set_objective_vane: constants");
+    DeviceGuard dg(c->device);
+    int np = v->nPlaneCells;
+    std::vector<int32_t> cells(np > 0 ? np : 1), cellPlane(c->nIC, -1);
+    std::vector<double> areas(np > 0 ? np : 1);
+    for (int q = 0; q < np; q++) {
+        int cc = v->planeCells[q];
+        if (cc < 0 || cc >= c->nIC || cellPlane[cc] >= 0)
+            return fail(c, AFVM_ERR_BAD_ARG, "afvm_set_objective_vane: plane cell out of range or repeated");
+        cells[q] = cc;
+        areas[q] = v->planeAreas[q];
+        cellPlane[cc] = q;
+    }
+    // heat-transfer coefficients k A w / delta from the context's mesh tables
+    std::vector<double> A(c->nF), dl(c->nF);
+    cudaError_t e;
+    if (c->precision == AFVM_FP64) {
+        e = cudaMemcpy(A.data(), c->m64.area, sizeof(double) * c->nF, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(dl.data(), c->m64.dlt, sizeof(double) * c->nF, cudaMemcpyDeviceToHost);
+    } else {
+        std::vector<float> a32(c->nF), d32(c->nF);
+        e = cudaMemcpy(a32.data(), c->m32.area, sizeof(float) * c->nF, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(d32.data(), c->m32.dlt, sizeof(float) * c->nF, cudaMemcpyDeviceToHost);
+        for (int f = 0; f < c->nF; f++) { A[f] = a32[f]; dl[f] = d32[f]; }
+    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "afvm_set_objective_vane: mesh tables");
+    const Phys& P = c->phys;
+    double mu = (P.muModel == AFVM_MU_SUTHERLAND) ? P.muAs * std::pow(v->Tw, 1.5) / (v->Tw + P.muTs) : P.mu0;
+    double k = mu * P.kFac;
+    std::vector<int32_t> hf;
+    std::vector<double> hc, bhc(c->nG > 0 ? c->nG : 1, 0.0);
+    double w2 = 0.0;
+    for (int q = 0; q < v->nHeatPatches; q++) {
+        int pi = v->heatPatches[q];
+        if (pi < 0 || pi >= c->nPatches || !v->heatWeights[q])
+            return fail(c, AFVM_ERR_BAD_ARG, "afvm_set_objective_vane: heat patch index or weights");
+        for (int i = 0; i < c->patchN[pi]; i++) {
+            int f = c->patchStart[pi] + i;
+            double w = v->heatWeights[q][i];
+            w2 += A[f] * w;
+            if (w == 0.0) continue;
+            double cf = k * A[f] * w / dl[f];
+            hf.push_back(f);
+            hc.push_back(cf);
+            bhc[f - c->nIF] += cf;
+        }
+    }
+    int nh = (int)hf.size();
+    if (hf.empty()) { hf.push_back(0); hc.push_back(0.0); }   // one placeholder, never read
+    VaneDev d{};
+    int st;
+    if ((st = upload(c, &d.planeCells, cells))) return st;
+    if ((st = upload(c, &d.planeArea, areas))) return st;
+    if ((st = upload(c, &d.cellPlane, cellPlane))) return st;
+    if ((st = upload(c, &d.heatFaces, hf))) return st;
+    if ((st = upload(c, &d.heatCoef, hc))) return st;
+    if ((st = upload(c, &d.bHeatCoef, bhc))) return st;
+    int nb = nblocks((long long)np + nh);
+    if (nb < 1) nb = 1;
+    if ((st = dalloc(c, (void**)&c->vanePartials, sizeof(double) * 3 * (size_t)nb))) return st;
+    if ((st = dalloc(c, (void**)&c->vaneSums, sizeof(double) * 4))) return st;
+    cudaMemset(c->vaneSums, 0, sizeof(double) * 4);
+    d.sums = c->vaneSums;
+    d.nPlane = np;
+    d.nHeat = nh;
+    double nn = std::sqrt(v->normal[0] * v->normal[0] + v->normal[1] * v->normal[1] + v->normal[2] * v->normal[2]);
+    if (!(nn > 0)) return fail(c, AFVM_ERR_BAD_ARG, "afvm_set_objective_vane: zero normal");
+    d.n0 = v->normal[0]; d.n1 = v->normal[1]; d.n2 = v->normal[2];
+    d.ptin = v->ptin; d.Tw = v->Tw; d.a = v->a; d.b = v->b;
+    d.rw2 = (w2 != 0.0) ? 1.0 / w2 : 0.0;
+    c->vane = d;
+    c->nVaneBlocks = nb;
+    c->vaneSet = true;
+    return AFVM_OK;
 }
 
 int afvm_set_bc_value(afvm_ctx* ctx, int32_t patch, int32_t field, const double* values) {

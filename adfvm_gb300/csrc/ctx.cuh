@@ -68,6 +68,19 @@ struct ProfEntry {
     cudaEvent_t a, b;
 };
 
+// device view of the turbine-vane objective (AFVM_OBJ_VANE)
+struct VaneDev {
+    const int32_t* planeCells;   // nPlane internal cells cut by the plane
+    const double* planeArea;     // nPlane cut areas
+    const int32_t* cellPlane;    // nIC: index into the plane arrays, or -1
+    const int32_t* heatFaces;    // nHeat boundary faces of the heat-transfer patches
+    const double* heatCoef;      // nHeat: k A w / delta
+    const double* bHeatCoef;     // nG (by boundary face): the same coefficient, 0 elsewhere
+    const double* sums;          // [0] sum of pressure-loss terms, [1] sum of rhoUn A, [2] heat sum
+    int nPlane, nHeat;
+    double n0, n1, n2, ptin, Tw, a, b, rw2;   // rw2 = 1 / sum_f A_f w_f
+};
+
 struct Ctx {
     int precision;            // AFVM_FP64 / AFVM_FP32
     int device;
@@ -107,6 +120,12 @@ struct Ctx {
     // sensitivity reduction scratch (grown on demand)
     void* sensScratch = nullptr;
     size_t sensBytes = 0;
+    // turbine-vane objective inputs (afvm_set_objective_vane)
+    bool vaneSet = false;
+    VaneDev vane{};
+    double* vanePartials = nullptr;   // 3 x nVaneBlocks
+    int nVaneBlocks = 0;
+    double* vaneSums = nullptr;       // 3 doubles
     // per-launch event timing
     bool prof = false;
     std::vector<ProfEntry> profEntries;
@@ -153,6 +172,9 @@ inline void stage_views(P* stages, int n, P** u1, P** u2) {
     u2[0] = stages + 5 * (size_t)n; u2[1] = stages + 6 * (size_t)n; u2[2] = stages + 9 * (size_t)n;
 }
 
+// turbine-vane objective partial sums of the stage-1 record now in c->rec into c->vaneSums
+template <typename R>
+void launch_vane_sums(Ctx* c, cudaStream_t s, double* dtcOut, double* objOut);
 template <typename R>
 void launch_prim(Ctx* c, const R* r, const R* ru, const R* re, cudaStream_t s);
 template <typename R>

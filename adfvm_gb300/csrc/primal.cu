@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 #include "ctx.cuh"
 #include "facedev.cuh"
+#include "vane.cuh"
 
 namespace afvm {
 
@@ -256,6 +257,66 @@ __global__ void __launch_bounds__(BLOCK) k_objective(MeshDev<R> m, Phys P, const
     if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
 
+// turbine-vane objective on the stage-1 primitives (adFVM/objectives/vane.py:7-60): threads
+// [0, nPlane) take the plane cells (pressure-loss and weighting terms), the next nHeat threads
+// the heat-transfer faces; three block partial sums (FP64) in partials[0|1|2][block]
+template <typename R>
+__global__ void __launch_bounds__(BLOCK) k_obj_vane(MeshDev<R> m, Phys P, const R* __restrict__ rec, VaneDev v,
+                                                    int nBlocks, double* partials) {
+    __shared__ double sh0[BLOCK / 32], sh1[BLOCK / 32], sh2[BLOCK / 32];
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double l = 0.0, w = 0.0, h = 0.0;
+    if (t < v.nPlane) {
+        const R* r = rec + (size_t)v.planeCells[t] * REC;
+        double U[3] = {r[0], r[1], r[2]};
+        vane_cell(P, v, U, (double)r[R_T], (double)r[R_P], v.planeArea[t], l, w);
+    } else if (t < v.nPlane + v.nHeat) {
+        int q = t - v.nPlane;
+        int f = v.heatFaces[q];
+        h = v.heatCoef[q] * (v.Tw - (double)rec[(size_t)m.own[f] * REC + R_T]);
+    }
+    double s0 = block_sum(l, sh0), s1 = block_sum(w, sh1), s2 = block_sum(h, sh2);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = s0;
+        partials[nBlocks + blockIdx.x] = s1;
+        partials[2 * nBlocks + blockIdx.x] = s2;
+    }
+}
+
+// fixed-order sums of the vane partials into sums[0..2]; with objOut, also the objective
+// a L/W + b H/sum(A w) and the dtc bits, as k_finish does
+__global__ void k_vane_finish(const double* partials, int nBlocks, VaneDev v, double* sums,
+                              const unsigned long long* dtcBits, double* dtcOut, double* objOut) {
+    __shared__ double sh0[BLOCK / 32], sh1[BLOCK / 32], sh2[BLOCK / 32];
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (int i = threadIdx.x; i < nBlocks; i += BLOCK) {
+        a += partials[i];
+        b += partials[nBlocks + i];
+        c += partials[2 * nBlocks + i];
+    }
+    double L = block_sum(a, sh0), W = block_sum(b, sh1), H = block_sum(c, sh2);
+    if (threadIdx.x == 0) {
+        sums[0] = L;
+        sums[1] = W;
+        sums[2] = H;
+        if (objOut) *objOut = v.a * (L / W) + v.b * (H * v.rw2);
+        if (dtcOut) *dtcOut = __longlong_as_double((long long)*dtcBits);
+    }
+}
+
+template <typename R>
+void launch_vane_sums(Ctx* c, cudaStream_t s, double* dtcOut, double* objOut) {
+    const MeshDev<R>& m = meshOf<R>(c);
+    {
+        ProfScope ps(c, KID_OBJECTIVE, s);
+        k_obj_vane<R><<<c->nVaneBlocks, BLOCK, 0, s>>>(m, c->phys, (const R*)c->rec, c->vane, c->nVaneBlocks,
+                                                      c->vanePartials);
+    }
+    ProfScope ps(c, KID_FINISH, s);
+    k_vane_finish<<<1, BLOCK, 0, s>>>(c->vanePartials, c->nVaneBlocks, c->vane, c->vaneSums, c->dtcBits, dtcOut,
+                                      objOut);
+}
+
 // fixed-order final sum of the partials (deterministic) and the dtc bits -> double
 __global__ void k_finish(const double* partials, int nPartials, const unsigned long long* dtcBits,
                          double* dtcOut, double* objOut, int haveObj) {
@@ -338,10 +399,20 @@ int primal_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double d
     const R* u2c[3] = {u2[0], u2[1], u2[2]};
     cudaMemsetAsync(c->dtcBits, 0, sizeof(unsigned long long), s);
     int nObjBlocks = 0;
+    bool vaneDone = false;
+    if (c->objective == AFVM_OBJ_VANE && !c->vaneSet)
+        return fail(c, AFVM_ERR_BAD_ARG, "AFVM_OBJ_VANE needs afvm_set_objective_vane before the first step");
     for (int st = 0; st < 3; st++) {
         const R* const* in = st == 0 ? u0c : (st == 1 ? u1c : u2c);
         launch_prim_grad<R>(c, in[0], in[1], in[2], s);
-        if (st == 1 && c->objective != AFVM_OBJ_NONE) {
+        if (st == 1 && c->objective == AFVM_OBJ_VANE) {
+            // the partial sums now, while rec holds the stage-1 primitives; combined at the end
+            const MeshDev<R>& mm = meshOf<R>(c);
+            ProfScope ps(c, KID_OBJECTIVE, s);
+            k_obj_vane<R><<<c->nVaneBlocks, BLOCK, 0, s>>>(mm, P, (const R*)c->rec, c->vane, c->nVaneBlocks,
+                                                          c->vanePartials);
+            vaneDone = true;
+        } else if (st == 1 && c->objective != AFVM_OBJ_NONE) {
             int start = 0, n = m.nIC;
             if (c->objective == AFVM_OBJ_DRAG) { start = c->objStart; n = c->objN; }
             nObjBlocks = nblocks(n);
@@ -355,7 +426,11 @@ int primal_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double d
         R* const* out = st == 0 ? u1 : (st == 1 ? u2 : outN);
         launch_flux_update<R>(c, st, dt, dtDev, u0c, u1c, u2c, Srho, SrhoU, SrhoE, out, s);
     }
-    {
+    if (vaneDone) {
+        ProfScope ps(c, KID_FINISH, s);
+        k_vane_finish<<<1, BLOCK, 0, s>>>(c->vanePartials, c->nVaneBlocks, c->vane, c->vaneSums, c->dtcBits, dtcDev,
+                                          objDev);
+    } else {
         ProfScope ps(c, KID_FINISH, s);
         k_finish<<<1, BLOCK, 0, s>>>(c->partials, nObjBlocks, c->dtcBits, dtcDev, objDev, nObjBlocks > 0);
     }
@@ -401,6 +476,8 @@ template int primal_run_dev<double>(Ctx*, double*, double*, double*, int, double
                                     cudaStream_t);
 template int primal_run_dev<float>(Ctx*, float*, float*, float*, int, double, double, double, int, const float*,
                                    const float*, const float*, double*, double*, double*, cudaStream_t);
+template void launch_vane_sums<double>(Ctx*, cudaStream_t, double*, double*);
+template void launch_vane_sums<float>(Ctx*, cudaStream_t, double*, double*);
 template void launch_prim<double>(Ctx*, const double*, const double*, const double*, cudaStream_t);
 template void launch_prim<float>(Ctx*, const float*, const float*, const float*, cudaStream_t);
 template void launch_prim_grad<double>(Ctx*, const double*, const double*, const double*, cudaStream_t);

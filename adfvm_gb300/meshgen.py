@@ -268,3 +268,56 @@ def cylinder_ogrid(n_theta=256, n_r=128, diameter=1.0, far=20.0, span=None, grow
           ('back', 'empty', fb_own, back_q, {})]
     faces, owner, neighbour, boundary = _assemble(A, B, Q, bp)
     return P, faces, owner, neighbour, boundary
+
+
+def channel(nx=64, ny=32, x0=0.0, x1=0.1, y0=0.0, y1=0.044, dz=None, stretch=0.0):
+    """2-D channel of nx x ny hex cells extruded one cell in z, for the pressure-loss and
+    heat-transfer objective of adFVM/objectives/vane.py (whose plane and wall patches it names).
+
+    x in [x0, x1] (optionally stretched towards both ends by ``stretch``), y in [y0, y1].
+    Patches (file order): ``inlet`` (x = x0) and ``outlet`` (x = x1) of type ``patch``,
+    ``pressure`` (y = y0) and ``suction`` (y = y1) of type ``wall``, ``front``/``back`` ``empty``.
+    """
+    s = np.linspace(0.0, 1.0, nx + 1)
+    if stretch:
+        s = s + stretch * np.sin(2 * np.pi * s) / (2 * np.pi)
+    xs = x0 + (x1 - x0) * s
+    xs[0], xs[-1] = x0, x1
+    ys = np.linspace(y0, y1, ny + 1)
+    if dz is None:
+        dz = (y1 - y0) / ny
+    pid = lambda i, j, k: i + (nx + 1) * (j + (ny + 1) * k)
+    I, J = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), indexing='ij')
+    P = np.zeros(((nx + 1) * (ny + 1) * 2, 3))
+    for k in range(2):
+        ids = pid(I, J, k).ravel()
+        P[ids, 0] = xs[I].ravel()
+        P[ids, 1] = ys[J].ravel()
+        P[ids, 2] = k * dz
+    cell = lambda i, j: i + nx * j
+
+    def qx(i, j):    # normal +x
+        return np.stack([pid(i, j, 0), pid(i, j + 1, 0), pid(i, j + 1, 1), pid(i, j, 1)], -1)
+
+    def qy(i, j):    # normal +y
+        return np.stack([pid(i, j, 0), pid(i, j, 1), pid(i + 1, j, 1), pid(i + 1, j, 0)], -1)
+
+    def qz(i, j, k):  # normal +z
+        return np.stack([pid(i, j, k), pid(i + 1, j, k), pid(i + 1, j + 1, k), pid(i, j + 1, k)], -1)
+
+    Ii, Jj = np.meshgrid(np.arange(1, nx), np.arange(ny), indexing='ij')
+    A = [cell(Ii - 1, Jj).ravel()]; B = [cell(Ii, Jj).ravel()]; Q = [qx(Ii, Jj).reshape(-1, 4)]
+    Ii, Jj = np.meshgrid(np.arange(nx), np.arange(1, ny), indexing='ij')
+    A.append(cell(Ii, Jj - 1).ravel()); B.append(cell(Ii, Jj).ravel()); Q.append(qy(Ii, Jj).reshape(-1, 4))
+    A = np.concatenate(A); B = np.concatenate(B); Q = np.concatenate(Q)
+    j = np.arange(ny)
+    i = np.arange(nx)
+    Ii, Jj = np.meshgrid(np.arange(nx), np.arange(ny), indexing='ij')
+    bp = [('inlet', 'patch', cell(0, j), qx(0, j)[:, ::-1], {}),
+          ('outlet', 'patch', cell(nx - 1, j), qx(nx, j), {}),
+          ('pressure', 'wall', cell(i, 0), qy(i, 0)[:, ::-1], {}),
+          ('suction', 'wall', cell(i, ny - 1), qy(i, ny), {}),
+          ('front', 'empty', cell(Ii, Jj).ravel(), qz(Ii, Jj, 1).reshape(-1, 4), {}),
+          ('back', 'empty', cell(Ii, Jj).ravel(), qz(Ii, Jj, 0).reshape(-1, 4)[:, ::-1], {})]
+    faces, owner, neighbour, boundary = _assemble(A, B, Q, bp)
+    return P, faces, owner, neighbour, boundary

@@ -65,6 +65,13 @@ class RCF(object):
         self.Cv = self.Cp / self.gamma
         self.mesh = mesh if isinstance(mesh, Mesh) else Mesh.create(mesh)
         self.bc = bc
+        # the turbine-vane objective: 'vane' (adFVM/objectives/vane.py's own plane and weights)
+        # or a description from adfvm_gb300.vane.options(...)
+        self.vane = None
+        if isinstance(objective, dict) or objective == 'vane':
+            from . import vane as _vane
+            self.vane = dict(objective) if isinstance(objective, dict) else _vane.options(self.mesh)
+            objective = 'vane'
         self.objective = objective
         self.precision = {'fp64': L.AFVM_FP64, 'fp32': L.AFVM_FP32}[precision]
         self.dtype = np.float64 if self.precision == L.AFVM_FP64 else np.float32
@@ -82,7 +89,9 @@ class RCF(object):
         else:
             model, mu0 = L.AFVM_MU_CONSTANT, float(mu)
         obj, objPatch = L.AFVM_OBJ_NONE, -1
-        if self.objective == 'kinetic_energy':
+        if self.vane is not None:
+            obj = L.AFVM_OBJ_VANE
+        elif self.objective == 'kinetic_energy':
             obj = L.AFVM_OBJ_KINETIC_ENERGY
         elif self.objective == 'sum_T':
             obj = L.AFVM_OBJ_SUM_T
@@ -127,6 +136,53 @@ class RCF(object):
         L.check(st, None, 'afvm_ctx_create')
         self._ctx = ctx
         self._bcvals = self.getBoundaryTensor(1)
+        if self.vane is not None:
+            self._set_vane(self.vane)
+
+    def _set_vane(self, v):
+        m = self.mesh
+        cells = np.ascontiguousarray(v['planeCells'], np.int32).reshape(-1)
+        areas = np.ascontiguousarray(v['planeAreas'], np.float64).reshape(-1)
+        names = [p for p in m.sortedPatches if p in v['heat']]
+        idx = np.array([m.sortedPatches.index(p) for p in names], np.int32)
+        ws = [np.ascontiguousarray(v['heat'][p], np.float64).reshape(-1) for p in names]
+        wp = (L._d * max(1, len(ws)))(*[L.dptr(w) for w in ws])
+        d = L.ObjectiveVane(len(cells), L.iptr(cells), L.dptr(areas), (C.c_double * 3)(*[float(x) for x in v['normal']]),
+                            float(v['ptin']), len(names), L.iptr(idx) if len(idx) else None, wp, float(v['Tw']),
+                            float(v['a']), float(v['b']))
+        L.check(L.lib().afvm_set_objective_vane(self._ctx, C.byref(d)), self._ctx, 'afvm_set_objective_vane')
+        self.vane = dict(v, planeCells=cells, planeAreas=areas.reshape(-1, 1))
+
+    def extraArgs(self):
+        """The objective's extra step inputs, as the reference's getPlane/getWeights append them
+        to solver.extraArgs (vane.py:33-37, 79-80): [nPlaneCells, cells, areas] + a weight array
+        per heat patch (in the order of objectives/vane.py's ``patches``)."""
+        if self.vane is None:
+            return []
+        v = self.vane
+        from .vane import HEAT_PATCHES
+        order = [p for p in HEAT_PATCHES if p in v['heat']] + [p for p in v['heat'] if p not in HEAT_PATCHES]
+        return ([np.int32(len(v['planeCells'])), np.asarray(v['planeCells'], np.int32).reshape(-1, 1),
+                 np.asarray(v['planeAreas'], np.float64).reshape(-1, 1)] +
+                [np.asarray(v['heat'][p], np.float64).reshape(-1, 1) for p in order])
+
+    def _apply_extra(self, extra):
+        """Re-upload the vane inputs when the extra step inputs differ from the current ones."""
+        if self.vane is None:
+            if len(extra):
+                raise ValueError('map: %d inputs past the boundary tensors, the objective takes none' % len(extra))
+            return
+        cur = self.extraArgs()
+        if len(extra) != len(cur):
+            raise ValueError('map: expected %d objective inputs, got %d' % (len(cur), len(extra)))
+        if all(np.array_equal(np.asarray(a), np.asarray(b)) for a, b in zip(extra, cur)):
+            return
+        from .vane import HEAT_PATCHES
+        order = [p for p in HEAT_PATCHES if p in self.vane['heat']] + \
+            [p for p in self.vane['heat'] if p not in HEAT_PATCHES]
+        v = dict(self.vane, planeCells=np.asarray(extra[1]).reshape(-1), planeAreas=np.asarray(extra[2]),
+                 heat={p: np.asarray(w) for p, w in zip(order, extra[3:])})
+        self._set_vane(v)
 
     def close(self):
         if self._ctx is not None:
@@ -210,7 +266,9 @@ class RCF(object):
         if scal[:len(Mesh.constants)] != [getattr(m, a) for a in Mesh.constants]:
             raise ValueError('map: mesh constants differ from the mesh this solver was built on')
         S = inputs[base:base + 3]
-        self._apply_bc_tensors(list(inputs[base + 3:]))
+        nBC = len(self._bcvals)
+        self._apply_bc_tensors(list(inputs[base + 3:base + 3 + nBC]))
+        self._apply_extra(list(inputs[base + 3 + nBC:]))
         n = m.nInternalCells
         dt = float(np.asarray(dt).reshape(-1)[0])
         ins = [np.ascontiguousarray(np.asarray(a).reshape(n, d), self.dtype) for a, d in zip((rho, rhoU, rhoE), (1, 3, 1))]
@@ -235,7 +293,7 @@ class RCF(object):
         if sources is None:
             sources = [np.zeros((n, 1)), np.zeros((n, 3)), np.zeros((n, 1))]
         return ([rho, rhoU, rhoE, np.array([[dt]])] + m.getTensor() + m.getScalar() + list(sources) +
-                self.getBoundaryTensor(1))
+                self.getBoundaryTensor(1) + self.extraArgs())
 
     def step_host(self, rho, rhoU, rhoE, dt, S=None, out=None):
         """One step through the host-buffer entry point (afvm_primal_step_host): host arrays in

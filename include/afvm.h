@@ -149,6 +149,8 @@ typedef struct afvm_patch_bc {
 #define AFVM_OBJ_KINETIC_ENERGY 1    /* sum_c 0.5*rho*|U|^2*V over internal cells            */
 #define AFVM_OBJ_DRAG           2    /* wall drag of templates/cylinder_test.py:9-37          */
 #define AFVM_OBJ_SUM_T          3    /* sum_c T (templates/box.py:10-16)                      */
+#define AFVM_OBJ_VANE           4    /* plane pressure loss + wall heat transfer, set with
+                                        afvm_set_objective_vane (adFVM/objectives/vane.py)     */
 
 typedef struct afvm_physics {
     double gamma, Cp, Pr;            /* defaults 1.4, 1004.5, 0.7 (adFVM/density.py:22-39) */
@@ -178,6 +180,27 @@ int64_t afvm_ctx_device_bytes(const afvm_ctx* ctx);
  * - the per-call BC tensors of Solver.getBoundaryTensor (adFVM/solver.py:91-92). field: 0=U,
  * 1=T, 2=p. */
 int afvm_set_bc_value(afvm_ctx* ctx, int32_t patch, int32_t field, const double* values);
+
+/* The turbine-vane objective (adFVM/objectives/vane.py:7-140), for a context created with
+ * objective AFVM_OBJ_VANE (which must be given these inputs before its first step):
+ *   J = a * sum_c (ptin - pt_c) rhoUn_c A_c / ptin / sum_c rhoUn_c A_c
+ *     + b * sum_f k (Tw - T_owner) / delta_f A_f w_f / sum_f A_f w_f,   k = Cp mu(Tw) / Pr,
+ * over the plane cells c (the reference's getPlane extraArgs, vane.py:23-37) and the faces f of
+ * the heat-transfer patches with weights w (getWeights, vane.py:68-80). All arrays are host
+ * arrays, copied. */
+typedef struct afvm_objective_vane {
+    int32_t nPlaneCells;
+    const int32_t* planeCells;      /* internal cell ids cut by the plane */
+    const double* planeAreas;       /* the cut area of each */
+    double normal[3];               /* direction of rho U.n (vane.py: (1, 0, 0)) */
+    double ptin;                    /* inlet total pressure (vane.py: 175158) */
+    int32_t nHeatPatches;
+    const int32_t* heatPatches;     /* patch indices in sortedPatches order */
+    const double* const* heatWeights;   /* per heat patch, nFaces weights */
+    double Tw;                      /* wall temperature (vane.py: 300) */
+    double a, b;                    /* weights of the two terms (vane.py: 0.4, 0) */
+} afvm_objective_vane;
+int afvm_set_objective_vane(afvm_ctx* ctx, const afvm_objective_vane* v);
 
 /* Ghost-cell values of the primitive fields for a conservative state: the boundary map the
  * reference runs before writing fields (RCF.initFields -> mapBoundary, adFVM/density.py:140-143;

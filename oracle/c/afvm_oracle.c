@@ -42,7 +42,11 @@ typedef struct {
     double gamma, Cp, Pr;
     int muModel; double mu0, muAs, muTs;
     int riemann, briemann;
-    int objective, objStart, objN;                 /* 0 none 1 KE 2 drag 3 sumT */
+    int objective, objStart, objN;                 /* 0 none 1 KE 2 drag 3 sumT 4 vane */
+    /* turbine-vane objective (adFVM/objectives/vane.py:7-60, 118-131) */
+    int nPlane; const int32_t* planeCells; const double* planeAreas;
+    double vn[3], ptin, Tw, va, vb;
+    int nHeat; const int32_t* heatFaces; const double* heatW; /* faces of the heat patches, weights */
 } oracle_mesh;
 
 static inline double dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
@@ -259,6 +263,33 @@ static void equation(const oracle_mesh* M, const double* rho, const double* rU, 
                 double mung = mu_of(M, rN[3]) * (rN[0] - rP[0]) / M->dlt[f];
                 v = v + (rN[4] * M->nrm[3 * (size_t)f] - mung) * M->area[f];
             }
+        } else if (M->objective == 4) {
+            /* pressure loss over the plane cells, normalised by the mass flux through them */
+            double g = M->gamma, Cv = M->Cp / M->gamma, w = 0.0, pl = 0.0, w2 = 0.0, ht = 0.0;
+            for (int q = 0; q < M->nPlane; q++) {
+                const double* r = rec + 20 * (size_t)M->planeCells[q];
+                double rh = r[4] / (Cv * r[3] * (g - 1));
+                double rUn = 0.0 + rh * r[0] * M->vn[0] + rh * r[1] * M->vn[1] + rh * r[2] * M->vn[2];
+                w = w + rUn * M->planeAreas[q];
+            }
+            for (int q = 0; q < M->nPlane; q++) {
+                const double* r = rec + 20 * (size_t)M->planeCells[q];
+                double rh = r[4] / (Cv * r[3] * (g - 1));
+                double c = sqrt(g * r[4] / rh);
+                double rUn = 0.0 + rh * r[0] * M->vn[0] + rh * r[1] * M->vn[1] + rh * r[2] * M->vn[2];
+                double Mi = sqrt(dot3(r, r)) / c;
+                double pt = r[4] * pow(1 + 0.5 * (g - 1) * Mi * Mi, g / (g - 1));
+                pl = pl + (M->ptin - pt) * rUn * M->planeAreas[q] / M->ptin / w;
+            }
+            /* weighted wall heat transfer k (Tw - T_owner)/delta A w / sum A w */
+            double k = M->Cp * mu_of(M, M->Tw) / M->Pr;
+            for (int q = 0; q < M->nHeat; q++) w2 = w2 + M->area[M->heatFaces[q]] * M->heatW[q];
+            for (int q = 0; q < M->nHeat; q++) {
+                int f = M->heatFaces[q];
+                double dtdn = (M->Tw - rec[20 * (size_t)M->own[f] + 3]) / M->dlt[f];
+                ht = ht + k * dtdn * M->area[f] * M->heatW[q] / w2;
+            }
+            v = M->va * pl + M->vb * ht;
         }
         *obj = v;
     }

@@ -25,7 +25,10 @@ class OracleMesh(C.Structure):
                 ('gamma', C.c_double), ('Cp', C.c_double), ('Pr', C.c_double),
                 ('muModel', C.c_int), ('mu0', C.c_double), ('muAs', C.c_double), ('muTs', C.c_double),
                 ('riemann', C.c_int), ('briemann', C.c_int),
-                ('objective', C.c_int), ('objStart', C.c_int), ('objN', C.c_int)]
+                ('objective', C.c_int), ('objStart', C.c_int), ('objN', C.c_int),
+                ('nPlane', C.c_int), ('planeCells', C.c_void_p), ('planeAreas', C.c_void_p),
+                ('vn', C.c_double * 3), ('ptin', C.c_double), ('Tw', C.c_double), ('va', C.c_double),
+                ('vb', C.c_double), ('nHeat', C.c_int), ('heatFaces', C.c_void_p), ('heatW', C.c_void_p)]
 
 
 def lib():
@@ -104,7 +107,11 @@ class COracle(object):
         accF = np.take_along_axis(cf, order, axis=1)
         own = owner[accF] == np.arange(nIC)[:, None]
         accf = np.where(own, accF, ~accF).astype(np.int32)
-        obj = {'none': 0, 'kinetic_energy': 1, 'sum_T': 3}.get(objective, 2 if objective.startswith('drag:') else 0)
+        vane = objective if isinstance(objective, dict) else None
+        if vane is not None:
+            obj = 4
+        else:
+            obj = {'none': 0, 'kinetic_energy': 1, 'sum_T': 3}.get(objective, 2 if objective.startswith('drag:') else 0)
         mu = cfg['mu']
         keep = dict(own=owner, nbr=np.asarray(m.neighbour, np.int32).reshape(-1),
                     nrm=np.ascontiguousarray(m.normals, np.float64), area=np.ascontiguousarray(m.areas, np.float64),
@@ -125,6 +132,26 @@ class COracle(object):
                             1 if mu is None else 0, 0.0 if mu is None else float(mu), 1.4792e-06, 116.,
                             0 if cfg['riemannSolver'] == 'eulerRoe' else 1,
                             0 if cfg['boundaryRiemannSolver'] == 'eulerRoe' else 1, obj, objStart, objN)
+        if vane is not None:
+            hf, hw = [], []
+            # heat faces in the order of objectives/vane.py's patch list
+            for name in [p for p in ('pressure', 'suction') if p in vane['heat']] + \
+                    [p for p in vane['heat'] if p not in ('pressure', 'suction')]:
+                b = m.boundary[name]
+                s, n = int(b['startFace']), int(b['nFaces'])
+                hf.append(np.arange(s, s + n, dtype=np.int32))
+                hw.append(np.asarray(vane['heat'][name], np.float64).reshape(-1))
+            keep['planeCells'] = np.ascontiguousarray(vane['planeCells'], np.int32).reshape(-1)
+            keep['planeAreas'] = np.ascontiguousarray(vane['planeAreas'], np.float64).reshape(-1)
+            keep['heatFaces'] = np.ascontiguousarray(np.concatenate(hf) if hf else np.zeros(1, np.int32), np.int32)
+            keep['heatW'] = np.ascontiguousarray(np.concatenate(hw) if hw else np.zeros(1), np.float64)
+            M = self.M
+            M.nPlane = len(keep['planeCells'])
+            M.planeCells, M.planeAreas = ptr('planeCells'), ptr('planeAreas')
+            M.vn = (C.c_double * 3)(*[float(x) for x in vane['normal']])
+            M.ptin, M.Tw, M.va, M.vb = float(vane['ptin']), float(vane['Tw']), float(vane['a']), float(vane['b'])
+            M.nHeat = int(sum(len(h) for h in hf))
+            M.heatFaces, M.heatW = ptr('heatFaces'), ptr('heatW')
         self.nIC = nIC
         self.work = np.zeros(lib().oracle_work_doubles(C.byref(self.M)))
 

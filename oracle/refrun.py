@@ -102,12 +102,14 @@ def build_mesh(meshData, case_dir):
     return m
 
 
-def make_rcf(meshData, case_dir, fields_bc, U, T, p, **rcf_config):
+def make_rcf(meshData, case_dir, fields_bc, U, T, p, before_compile=None, **rcf_config):
     """Construct the reference RCF solver on a generated mesh.
 
     fields_bc: {'U': {patch: bcdict}, 'T': ..., 'p': ...} in the reference's boundary-dict
     form ({'type': ..., 'value'/'U0'/'T0'/'p0': ndarray}). U, T, p: internal-cell values.
     Returns (rcf, conservative_fields) where the latter is what readFields returns.
+    before_compile(rcf), if given, runs before the step function is compiled (where a case file
+    calls helpers that append solver.extraArgs, e.g. objectives/vane.py getPlane/getWeights).
     """
     ns = load()
     density = ns.density
@@ -137,6 +139,8 @@ def make_rcf(meshData, case_dir, fields_bc, U, T, p, **rcf_config):
     rcf.firstRun = False
     cons = list(rcf.conservative(*rcf.fields))
     rcf.readFields = lambda t, suffix='': cons
+    if before_compile is not None:
+        before_compile(rcf)
     rcf.compileInit()
     rcf.compileSolver()
     return rcf, cons

@@ -152,12 +152,14 @@ class OffsetView(Node):
 
 
 class KernelOutput(Node):
-    def __init__(self, call, index, dummy):
+    def __init__(self, call, index, dummy, shape=None):
         super().__init__()
         self.call = call
         self.index = index
         self.dummy = dummy
-        self.shape = (None,) + tuple(dummy[0].shape[1:])
+        # an output written into a given array has that array's shape (a reduction into a
+        # Zeros((1, 1)) is (1, 1)); otherwise one row per element of the range
+        self.shape = tuple(shape) if shape is not None else (None,) + tuple(dummy[0].shape[1:])
 
     def _eval(self, env):
         return env.kernel(self.call)[self.index]
@@ -430,7 +432,9 @@ class Kernel(object):
         def call(*args, **kwargs):
             kc = KernelCall(self.func, n, outputs, args, kwargs)
             single, dummies = kc.dry()
-            outs = tuple(KernelOutput(kc, k, d) for k, d in enumerate(dummies))
+            shapes = [getattr(o, 'shape', None) for o in outputs] if outputs else [None] * len(dummies)
+            outs = tuple(KernelOutput(kc, k, d, shapes[k] if k < len(shapes) else None)
+                         for k, d in enumerate(dummies))
             # one result is returned bare (BCs.py:65-71, density.py:410 use it so)
             if len(outs) == 1:
                 return outs[0]
@@ -439,11 +443,12 @@ class Kernel(object):
 
 
 class ExternalFunctionOp(object):
-    """MPI halo / allreduce ops: on one rank the outputs are the given output arrays
-    unchanged (every call site passes the field itself as its output)."""
+    """MPI halo / allreduce ops on one rank: a halo op's outputs are the given output arrays
+    unchanged (its call sites pass the field itself as its output); an allreduce over one rank
+    is its inputs (objectives/vane.py:108-110 passes fresh zeros as the outputs)."""
     def __init__(self, name, inputs, outputs, empty=False):
         self.name = name
-        self.outputs = tuple(outputs)
+        self.outputs = tuple(inputs) if name == 'mpi_allreduce' else tuple(outputs)
 
 
 class ConstantOp(object):

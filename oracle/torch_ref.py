@@ -392,6 +392,8 @@ class Problem(object):
         """Objective on the (ghost-completed) primitives of RK stage 1."""
         o = self.objective
         nIC = self.nIC
+        if isinstance(o, dict):
+            return self._vane(o, U, T, p)
         if o == 'none':
             return torch.zeros((), dtype=T64)
         if o == 'kinetic_energy':
@@ -415,6 +417,43 @@ class Problem(object):
             drag = (p0 * nx - mungUx) * self.areas[sl]
             return torch.cumsum(drag.reshape(-1), 0)[-1]
         raise ValueError(o)
+
+    def _vane(self, v, U, T, p):
+        """adFVM/objectives/vane.py:7-60, 118-131: a * pressure loss over the plane cells
+        (objectivePressureLoss / objectivePressureLossWeighting) + b * weighted wall heat
+        transfer (objectiveHeatTransfer / objectiveHeatTransferWeighting)."""
+        g = self.gamma
+        cells = _t(v['planeCells'], torch.int64).reshape(-1)
+        areas = _t(v['planeAreas']).reshape(-1, 1)
+        n = [float(x) for x in v['normal']]
+        pi, Ti, Ui = p[cells], T[cells], U[cells]
+        rhoi = pi / (self.Cv * Ti * (g - 1))
+        ci = (g * pi / rhoi).sqrt()
+        rhoUni = sum([rhoi * Ui[:, i:i + 1] * n[i] for i in range(3)])
+        w = torch.cumsum((rhoUni * areas).reshape(-1), 0)[-1]
+        Umagi = dot3(Ui, Ui).unsqueeze(-1)
+        Mi = Umagi.sqrt() / ci
+        pti = pi * (1 + 0.5 * (g - 1) * Mi * Mi) ** (g / (g - 1))
+        pl = (v['ptin'] - pti) * rhoUni * areas / v['ptin']
+        pl = torch.cumsum((pl / w).reshape(-1), 0)[-1]
+        ht = torch.zeros((), dtype=T64)
+        w2 = 0.0
+        k = self.Cp * self.mu(torch.tensor(float(v['Tw']), dtype=T64)) / self.Pr
+        for P in self.patches:
+            if P['name'] not in v['heat']:
+                continue
+            sl = slice(P['start'], P['start'] + P['n'])
+            wt = _t(v['heat'][P['name']]).reshape(-1, 1)
+            w2 = w2 + float((self.areas[sl] * wt).sum())
+        for P in self.patches:
+            if P['name'] not in v['heat']:
+                continue
+            sl = slice(P['start'], P['start'] + P['n'])
+            wt = _t(v['heat'][P['name']]).reshape(-1, 1)
+            Tin = T[self.owner[sl]]
+            dtdn = (v['Tw'] - Tin) / self.deltas[sl]
+            ht = ht + torch.cumsum((k * dtdn * self.areas[sl] * wt / w2).reshape(-1), 0)[-1]
+        return v['a'] * pl + v['b'] * ht
 
     # ------------------------------------------------------------ residual and step
     def equation(self, rho, rhoU, rhoE, want_objective=False):

@@ -84,21 +84,37 @@ def objective_fn(kind, rcf_cfg):
 
 
 def reference_config(case):
+    """(RCF options, hook run before the step function is compiled)."""
     cfg = dict(case.config)
     if 'mu' in cfg and not callable(cfg['mu']):
         v = float(cfg['mu'])
         cfg['mu'] = lambda T, v=v: v
+    if isinstance(case.objective, dict):
+        # the reference's own turbine-vane objective (adFVM/objectives/vane.py) with its own
+        # getPlane/getWeights; the compiled compat.intersectPlane it calls is replaced by the
+        # plane cells and areas of adfvm_gb300.vane (the only input not computed by that file)
+        import adFVM.objectives.vane as V
+        cells = np.asarray(case.objective['planeCells'], np.int32)
+        areas = np.asarray(case.objective['planeAreas'], np.float64).reshape(-1, 1)
+        V.intersectPlane = lambda mesh, point, normal: (cells, areas)
+        cfg['objective'] = V.objective
+
+        def hook(rcf):
+            V.getPlane(rcf)
+            V.getWeights(rcf)
+        return cfg, hook
     obj = objective_fn(case.objective, cfg)
     if obj is not None:
         cfg['objective'] = obj
-    return cfg
+    return cfg, None
 
 
 def run_case(case, nSteps, keep_steps, with_source=False):
     refrun.load()
     md = case.meshData
     with tempfile.TemporaryDirectory() as d:
-        rcf, cons = refrun.make_rcf(md, d, case.bc, case.U, case.T, case.p, **reference_config(case))
+        cfg, hook = reference_config(case)
+        rcf, cons = refrun.make_rcf(md, d, case.bc, case.U, case.T, case.p, before_compile=hook, **cfg)
         src = None
         if with_source:
             S = cases.source_field(case.build_mesh())
@@ -128,6 +144,7 @@ CASES = {
     'cyl32x16': lambda: (cases.cylinder(32, 16, objective='drag:cylinder'), 5, [1, 2, 5], False),
     'duct100_totalpt': lambda: (cases.duct(100), 40, [1, 10, 40], False),
     'duct60_totalpt_normals': lambda: (cases.duct(60, direction=False, U0=-20.0), 20, [1, 20], False),
+    'vane32x12': lambda: (cases.vane_channel(32, 12, reference_constants=True), 20, [1, 5, 20], False),
 }
 
 

@@ -15,6 +15,7 @@ CASES = {
     'cyl32x16': lambda: cases.cylinder(32, 16, objective='drag:cylinder'),
     'duct100_totalpt': lambda: cases.duct(100),
     'duct60_totalpt_normals': lambda: cases.duct(60, direction=False, U0=-20.0),
+    'vane32x12': lambda: cases.vane_channel(32, 12, reference_constants=True),
 }
 
 

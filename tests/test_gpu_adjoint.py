@@ -27,7 +27,7 @@ def _seeds(x, seed):
 
 
 @pytest.mark.parametrize('name', ['box8', 'cyl32x16', 'sod200_sym_lf', 'box6_inviscid_sumT', 'sod1000',
-                                  'duct100_totalpt', 'duct60_totalpt_normals'])
+                                  'duct100_totalpt', 'duct60_totalpt_normals', 'vane32x12'])
 def test_adjoint_step_matches_autograd(name):
     case, mesh, x, S, dt = _setup(name)
     prob = torch_ref.Problem(mesh, case.bc, case.config, case.objective)
@@ -161,3 +161,31 @@ def test_kept_stages_give_the_same_adjoint(name, precision):
         assert torch.equal(u, v)
     with pytest.raises(ValueError):
         rcf.adjoint_step(d[0], d[1], d[2], dt, seeds, S=Sd, stages=st[:10])
+
+
+@pytest.mark.parametrize('b', [0.0, 1e-5])
+def test_vane_objective_adjoint_with_heat_term(b):
+    """The turbine-vane objective with its heat-transfer term switched on (the reference's own
+    file has b = 0): value and VJP against the oracle and its autograd, FP64."""
+    case = cases.vane_channel(24, 10, b=b)
+    mesh = case.build_mesh()
+    x = [torch.as_tensor(a) for a in cases.conservative(case)]
+    rng = np.random.default_rng(5)
+    x = [t * (1 + 0.01 * torch.as_tensor(rng.standard_normal(tuple(t.shape)))) for t in x]
+    prob = torch_ref.Problem(mesh, case.bc, case.config, case.objective)
+    ref_step = prob.step(x[0], x[1], x[2], case.dt)
+    rcf = RCF(mesh, case.bc, objective=case.objective, **case.config)
+    d = [t.cuda() for t in x]
+    r = rcf.step(d[0], d[1], d[2], case.dt)
+    assert abs(r[4] - float(ref_step[4])) <= 1e-12 * abs(float(ref_step[4]))
+    seeds = _seeds(x, 9)
+    ref = torch_ref.vjp_step(prob, x[0], x[1], x[2], case.dt, None, seeds, obja=1.0)
+    a = rcf.adjoint_step(d[0], d[1], d[2], case.dt, [t.cuda() for t in seeds], obja=1.0)
+    for i in range(3):
+        assert G.rel_err(a[i].cpu().numpy(), ref[i].numpy()) < 1e-11, i
+    # the objective's own gradient (no state seeds) is the part that changes with b
+    z = [torch.zeros_like(t) for t in seeds]
+    ref0 = torch_ref.vjp_step(prob, x[0], x[1], x[2], case.dt, None, z, obja=1.0)
+    a0 = rcf.adjoint_step(d[0], d[1], d[2], case.dt, [t.cuda() for t in z], obja=1.0)
+    for i in range(3):
+        assert G.rel_err(a0[i].cpu().numpy(), ref0[i].numpy()) < 1e-11, i
