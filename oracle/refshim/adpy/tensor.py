@@ -195,6 +195,16 @@ class Tensor(object):
     __array_priority__ = 1000
 
     def __init__(self, value=None, full=None, off=0, n=None):
+        if isinstance(value, tuple) and isinstance(full, list):
+            # Tensor(shape, [elements]): an element tensor assembled from scalars per element
+            # (postpro.py:564-612 builds 5x5 matrices so), constants broadcast to the rows
+            shape, elems = value, full
+            vals = [np.asarray(Tensor._v(e), np.float64) for e in elems]
+            rows = max([v.shape[0] for v in vals if v.ndim >= 1] + [1])
+            cols = [np.broadcast_to(v.reshape(-1, 1) if v.ndim else np.full((1, 1), float(v)), (rows, 1))
+                    for v in vals]
+            value = np.concatenate(cols, axis=1).reshape((rows,) + tuple(shape))
+            full, off, n = None, 0, None
         self._value = value
         self.full = full
         self.off = off
@@ -251,7 +261,7 @@ class Tensor(object):
         return Tensor(np.sqrt(self.value))
 
     def __getitem__(self, i):
-        v = self.value[:, i]
+        v = self.value[(slice(None),) + i] if isinstance(i, tuple) else self.value[:, i]
         if v.ndim == 1:
             v = v.reshape(-1, 1)
         return Tensor(v)
@@ -442,17 +452,55 @@ class Kernel(object):
         return call
 
 
+class ExternalNode(Node):
+    """Output k of a compiled external operation, computed when the graph is evaluated."""
+    def __init__(self, fn, inputs, k, shape):
+        super().__init__()
+        self.fn = fn
+        self.inputs = inputs
+        self.k = k
+        self.shape = shape
+
+    def _eval(self, env):
+        key = ('ext', id(self.fn))
+        if key not in env.cache:
+            vals = []
+            for x in self.inputs:
+                arr, off = env.value(x)
+                vals.append(np.asarray(arr)[off:])
+            env.cache[key] = self.fn(*vals)
+        return (env.cache[key][self.k], 0)
+
+    def _dummy(self):
+        return (np.zeros([1] + [int(s) if isinstance(s, (int, np.integer)) else 1 for s in self.shape[1:]]), 0)
+
+
+# compiled external operations other than the one-rank MPI ones: name -> fn(*input arrays) ->
+# output arrays; registered by the test infrastructure that restates them
+EXTERNAL = {}
+
+
 class ExternalFunctionOp(object):
     """MPI halo / allreduce ops on one rank: a halo op's outputs are the given output arrays
     unchanged (its call sites pass the field itself as its output); an allreduce over one rank
-    is its inputs (objectives/vane.py:108-110 passes fresh zeros as the outputs)."""
+    is its inputs (objectives/vane.py:108-110 passes fresh zeros as the outputs). Other names
+    are looked up in EXTERNAL."""
     def __init__(self, name, inputs, outputs, empty=False):
         self.name = name
-        self.outputs = tuple(inputs) if name == 'mpi_allreduce' else tuple(outputs)
+        if name in EXTERNAL:
+            fn = EXTERNAL[name]
+            ins = tuple(inputs)
+
+            def run(*vals):
+                return fn(*vals)
+            self.outputs = tuple(ExternalNode(run, ins, k, getattr(o, 'shape', None)) for k, o in enumerate(outputs))
+        else:
+            self.outputs = tuple(inputs) if name == 'mpi_allreduce' else tuple(outputs)
 
 
-class ConstantOp(object):
-    pass
+def ConstantOp(value=0.0):
+    """A constant element (postpro.py:562)."""
+    return float(value)
 
 
 class Function(object):

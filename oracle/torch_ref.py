@@ -554,3 +554,168 @@ def adjoint_energy(volumes, gamma, rhoa, rhoUa, rhoEa, rho, rhoU, rhoE):
          2 * (A12 * w1 * w2 + A13 * w1 * w3 + A14 * w1 * w4 + A15 * w1 * w5 + A23 * w2 * w3 + A24 * w2 * w4 +
               A25 * w2 * w5 + A34 * w3 * w4 + A35 * w3 * w5 + A45 * w4 * w5)) * v
     return float(np.sum(e))
+
+
+# ---------------------------------------------------------------- adjoint stabilisation
+
+def _max_eig_sym(MS):
+    """Largest eigenvalue of each symmetric 5x5 (LAPACK's ascending w[4], scaling.cpp:84-104)."""
+    return np.linalg.eigvalsh(MS)[:, -1]
+
+
+def viscosity_matrix(kind, g, U, T, p, Cv, gradU, divU, gradp, gradc, Uref=33., pref=1e5):
+    """The symmetric part MS = (M + M^T)/2 of getMaxEigenvalue (adFVM/postpro.py:549-634) per
+    cell, numpy float64: U (n,3), T, p (n,), gradU (n,3,3), divU (n,), gradp, gradc (n,3)."""
+    n = len(T)
+    rho = p / ((Cv * T) * (g - 1))
+    c = np.sqrt(g * p / rho)
+    gradrho = g * (gradp - (c * p)[:, None]) / (c * c)[:, None]
+    Z = np.zeros(n)
+    M = np.zeros((n, 5, 5))
+    g1 = g - 1
+    if kind == 'turkel':
+        M1 = np.zeros((n, 5, 5))
+        for k in range(5):
+            M1[:, k, k] = divU
+        for k in range(3):
+            M1[:, 0, 1 + k] = gradc[:, k]
+            M1[:, 1 + k, 0] = gradc[:, k]
+        tmp1 = gradp / (rho * c)[:, None]
+        tmp2 = g1 * gradp / (2 * rho * c)[:, None]
+        tmp3 = gradp * pref / (2 * g * p * rho * Uref)[:, None]
+        tmp4 = (gradp - (c * c)[:, None] * gradrho) * Uref / pref
+        M2 = np.zeros((n, 5, 5))
+        M2[:, 0, 0] = g1 * divU / 2
+        M2[:, 0, 1:4] = tmp1
+        M2[:, 0, 4] = divU * pref / (2 * rho * c * Uref)
+        M2[:, 1:4, 0] = tmp2
+        M2[:, 1:4, 1:4] = gradU
+        M2[:, 1:4, 4] = tmp3
+        M2[:, 4, 1:4] = tmp4
+        M2[:, 4, 4] = g1 * divU / 2
+        M = M1 / 2 - M2
+    elif kind == 'abarbanel':
+        sg, sg1 = np.sqrt(g), np.sqrt(g1)
+        b = c / sg
+        a = sg1 * c / sg
+        gradb = gradc / sg
+        grada = gradc * sg1 / sg
+        M1 = np.zeros((n, 5, 5))
+        for k in range(5):
+            M1[:, k, k] = divU
+        for k in range(3):
+            M1[:, 0, 1 + k] = gradb[:, k]
+            M1[:, 1 + k, 0] = gradb[:, k]
+            M1[:, 1 + k, 4] = grada[:, k]
+            M1[:, 4, 1 + k] = grada[:, k]
+        tmp1 = b[:, None] * gradrho / rho[:, None]
+        tmp2 = a[:, None] * gradp / (2 * p)[:, None]
+        tmp3 = 2 * grada / g1
+        M2 = np.zeros((n, 5, 5))
+        M2[:, 0, 1:4] = tmp1
+        M2[:, 0, 4] = sg1 * divU / 2
+        M2[:, 1:4, 1:4] = gradU
+        M2[:, 1:4, 4] = tmp2
+        M2[:, 4, 1:4] = tmp3
+        M2[:, 4, 4] = g1 * divU / 2
+        M = M1 / 2 - M2
+    else:
+        raise ValueError(kind)
+    del Z
+    return (M + np.swapaxes(M, 1, 2)) / 2
+
+
+def adjoint_viscosity(problem, rho, rhoU, rhoE, kind, scaling, Uref=33., pref=1e5):
+    """postpro.computeAdjointViscosity (adFVM/postpro.py:491-697): the per-cell viscosity
+    M_2norm (max eigenvalue of the symmetrised 5x5 of each cell, normalised to
+    scaling * M / sqrt(sum M^2 V / sum V)) and its central interpolation DT on every face.
+    Returns (M_2norm (nCells,) with ghost values, DT (nFaces,)), numpy float64."""
+    P = problem
+    g = P.gamma
+    Rg = P.Cp - P.Cv
+    with torch.no_grad():
+        U, T, p = P.ghosts(*P.primitive(torch.as_tensor(rho), torch.as_tensor(rhoU), torch.as_tensor(rhoE)))
+    U, T, p = U.numpy(), T.numpy().reshape(-1), p.numpy().reshape(-1)
+    own, nbr = P.owner.numpy(), P.neighbour.numpy()
+    w = P.weights.numpy().reshape(-1)
+    A = P.areas.numpy().reshape(-1)
+    N = P.normals.numpy()
+    V = P.volumes.numpy().reshape(-1)
+    nIC, nIF, nF = P.nIC, P.nIF, P.nF
+    # face values (postpro.py:500-516): central on internal and coupled faces, ghost values on
+    # the other boundary faces
+    UF = np.zeros((nF, 3)); pF = np.zeros(nF); cF = np.zeros(nF)
+    central = np.zeros(nF, bool)
+    central[:nIF] = True
+    for Pt in P.patches:
+        if Pt['coupled']:
+            central[Pt['start']:Pt['start'] + Pt['n']] = True
+    cc = np.sqrt(g * T * Rg)
+    wc = w[:, None]
+    UF[central] = (U[own] * wc + U[nbr] * (1 - wc))[central]
+    pF[central] = (p[own] * w + p[nbr] * (1 - w))[central]
+    cF[central] = (cc[nbr] * (1 - w) + cc[own] * w)[central]
+    UF[~central] = U[nbr][~central]
+    pF[~central] = p[nbr][~central]
+    cF[~central] = np.sqrt(g * T[nbr][~central] * Rg)
+    # op.grad / op.div (op.py:12-43): + A/V_L to the owner, - A/V_R to the internal neighbour,
+    # accumulated in collate order (internal faces, then the patches in sortedPatches order)
+    gradU = np.zeros((nIC, 3, 3)); divU = np.zeros(nIC); gradp = np.zeros((nIC, 3)); gradc = np.zeros((nIC, 3))
+    acc = P.accFaces.numpy()
+    side = P.accOwnerSide.numpy()
+    for s in range(6):
+        f = acc[:, s]
+        sgn = np.where(side[:, s], 1.0, -1.0)
+        wgt = sgn * A[f] / V
+        gradU += UF[f][:, :, None] * N[f][:, None, :] * wgt[:, None, None]
+        divU += (UF[f] * N[f]).sum(axis=1) * wgt
+        gradp += (pF[f][:, None] * N[f]) * wgt[:, None]
+        gradc += (cF[f][:, None] * N[f]) * wgt[:, None]
+    if kind == 'uniform':
+        M = np.ones(nIC)
+    else:
+        MS = viscosity_matrix(kind, g, U[:nIC], T[:nIC], p[:nIC], P.Cv, gradU, divU, gradp, gradc, Uref, pref)
+        M = _max_eig_sym(MS)
+    Vt = V.sum()
+    Nrm = (M * M * V / Vt).sum()
+    M = M * scaling / np.sqrt(Nrm)
+    # ghost values by the default boundary (cyclic: partner's owner, others: owner) and the
+    # central interpolation to every face (postpro.py:680-697)
+    Mc = np.concatenate([M, M[P.gradSrc.numpy()]])
+    DT = Mc[own] * w + Mc[nbr] * (1 - w)
+    return Mc, DT
+
+
+def viscosity_solve(problem, DT, dt, rhoa, rhoUa, rhoEa):
+    """postpro.viscositySolver (adFVM/postpro.py:699-718) with the implicit heat equation of
+    apply_adjoint_viscosity (scaling.cpp:135-159, matop_petsc.cpp:230-372) solved exactly: per
+    component x of the adjoint per unit volume,
+        (1 + sum_k DTF_k dt/V) x_c - sum_k DTF_k dt/V x_nbr(k) = x0_c,  DTF = A DT / delta,
+    over the faces k of cell c that have an internal neighbour (cellNeighboursMatOp >= 0).
+    Returns the smoothed (rhoa, rhoUa, rhoEa) times the volumes again."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    P = problem
+    nIC = P.nIC
+    V = P.volumes.numpy().reshape(-1)
+    A = P.areas.numpy().reshape(-1)
+    dl = P.deltas.numpy().reshape(-1)
+    DTF = A * np.asarray(DT).reshape(-1) / dl
+    cf = P.cellFaces.numpy()
+    cn = P.cellNeighbours.numpy()
+    rows, cols, vals = [], [], []
+    diag = np.ones(nIC)
+    for k in range(6):
+        f = cf[:, k]
+        nb = cn[:, k]
+        ok = nb < nIC
+        coef = DTF[f] * dt / V
+        diag += np.where(ok, coef, 0.0)
+        rows.append(np.arange(nIC)[ok]); cols.append(nb[ok]); vals.append(-coef[ok])
+    Amat = sp.csr_matrix((np.concatenate(vals + [diag]), (np.concatenate(rows + [np.arange(nIC)]),
+                                                         np.concatenate(cols + [np.arange(nIC)]))), shape=(nIC, nIC))
+    X = np.concatenate([np.asarray(rhoa).reshape(nIC, 1), np.asarray(rhoUa).reshape(nIC, 3),
+                        np.asarray(rhoEa).reshape(nIC, 1)], axis=1) / V[:, None]
+    lu = spla.splu(Amat.tocsc())
+    Y = np.stack([lu.solve(X[:, k]) for k in range(5)], axis=1) * V[:, None]
+    return Y[:, 0:1], Y[:, 1:4], Y[:, 4:5]

@@ -205,6 +205,86 @@ def make_energy():
     print('energy ->', path, {k: float(v) for k, v in out.items() if k.endswith('/energy')})
 
 
+VISCOSITY_CASES = {'cyl16x8': lambda: cases.cylinder(16, 8), 'box6': lambda: cases.box(6),
+                   'vane16x8': lambda: cases.vane_channel(16, 8)}
+
+
+def make_viscosity():
+    """The adjoint stabilisation of the reference itself: postpro.computeAdjointViscosity
+    (adFVM/postpro.py:491-697) for the 'turkel', 'abarbanel' and 'uniform' symmetrisers and
+    postpro.viscositySolver (postpro.py:699-718), on seeded states. Their two compiled helpers
+    are restated for the stand-in: get_max_eigenvalue (scaling.cpp:84-104, the largest
+    eigenvalue of each symmetric 5x5) and apply_adjoint_viscosity (scaling.cpp:135-159: the
+    implicit heat equation of matop_petsc.cpp:230-372, here solved exactly by sparse LU)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    ns = refrun.load()
+    import adpy.tensor as AT
+    from adpy.tensor import Variable, Function
+    from adFVM import postpro
+    out = {}
+    AT.EXTERNAL['get_max_eigenvalue'] = lambda MS: [np.linalg.eigvalsh(MS.reshape(-1, 5, 5))[:, -1].reshape(-1, 1)]
+    for name, mk in VISCOSITY_CASES.items():
+        case = mk()
+        cfg, hook = reference_config(case)
+        with tempfile.TemporaryDirectory() as d:
+            rcf, cons = refrun.make_rcf(case.meshData, d, case.bc, case.U, case.T, case.p, before_compile=hook, **cfg)
+        m = rcf.mesh
+        n = m.nInternalCells
+        V = np.asarray(m.volumes).reshape(-1)
+        cf = np.asarray(m.cellFaces).reshape(-1, 6)
+        cn = np.asarray(m.cellNeighboursMatOp).reshape(-1, 6)
+
+        def heat(u0, u1, u2, u3, u4, rho, rhoU, rhoE, DTF, dt):
+            dtv = float(np.asarray(dt).reshape(-1)[0])
+            DTF = np.asarray(DTF).reshape(-1)
+            rows, cols, vals = [], [], []
+            diag = np.ones(n)
+            for k in range(6):
+                ok = cn[:, k] > -1
+                coef = -DTF[cf[:, k]] / V * dtv
+                diag -= np.where(ok, coef, 0.0)
+                rows.append(np.arange(n)[ok]); cols.append(cn[ok, k]); vals.append(coef[ok])
+            A = sp.csr_matrix((np.concatenate(vals + [diag]), (np.concatenate(rows + [np.arange(n)]),
+                                                              np.concatenate(cols + [np.arange(n)]))), shape=(n, n))
+            lu = spla.splu(A.tocsc())
+            return [lu.solve(np.asarray(u).reshape(-1)).reshape(-1, 1) for u in (u0, u1, u2, u3, u4)]
+        AT.EXTERNAL['apply_adjoint_viscosity'] = heat
+        rng = np.random.default_rng(21)
+        x = [a * (1 + 0.01 * rng.standard_normal(a.shape)) for a in cases.conservative(case)]
+        sm = m.symMesh
+        meshIn = sm.getTensor() + sm.getScalar() + rcf.getBoundaryTensor(0) + [v[0] for v in rcf.extraArgs]
+        meshVal = m.getTensor() + m.getScalar() + rcf.getBoundaryTensor(1) + [v[1] for v in rcf.extraArgs]
+        for k, nm in enumerate(['rho', 'rhoU', 'rhoE']):
+            out['%s/%s' % (name, nm)] = x[k]
+        for kind, scale in (('turkel', 1e-3), ('abarbanel', 0.5), ('uniform', 2.0)):
+            rho, rhoU, rhoE = Variable((n, 1)), Variable((n, 3)), Variable((n, 1))
+            scaling = Variable((1, 1))
+            M2, DT = postpro.computeAdjointViscosity(rcf, kind, rho, rhoU, rhoE, scaling)
+            F = Function('viscosity', [rho, rhoU, rhoE, scaling] + meshIn, [M2, DT])
+            M2v, DTv = F(x[0], x[1], x[2], np.array([[scale]]), *meshVal)
+            out['%s/%s/scaling' % (name, kind)] = np.array(scale)
+            out['%s/%s/M' % (name, kind)] = M2v.reshape(-1)
+            out['%s/%s/DT' % (name, kind)] = DTv.reshape(-1)
+        # the smoother on seeded adjoint fields with the 'abarbanel' DT and a large dt
+        a = [rng.standard_normal((n, 1)), rng.standard_normal((n, 3)), rng.standard_normal((n, 1))]
+        rho, rhoU, rhoE = Variable((n, 1)), Variable((n, 3)), Variable((n, 1))
+        ra, rUa, rEa = Variable((n, 1)), Variable((n, 3)), Variable((n, 1))
+        DT = Variable((m.nFaces, 1))
+        outs = postpro.viscositySolver(rcf, rho, rhoU, rhoE, ra, rUa, rEa, DT)
+        dt = 1e-2 if name != 'vane16x8' else 1e-6
+        F = Function('smooth', [rho, rhoU, rhoE, ra, rUa, rEa, DT, rcf.dt] + meshIn, list(outs))
+        res = F(x[0], x[1], x[2], a[0], a[1], a[2], out['%s/abarbanel/DT' % name].reshape(-1, 1),
+                np.array([[dt]]), *meshVal)
+        out['%s/smooth/dt' % name] = np.array(dt)
+        for k, nm in enumerate(['rhoa', 'rhoUa', 'rhoEa']):
+            out['%s/smooth/in_%s' % (name, nm)] = a[k]
+            out['%s/smooth/out_%s' % (name, nm)] = res[k]
+    path = os.path.join(HERE, 'viscosity.npz')
+    np.savez_compressed(path, **out)
+    print('viscosity ->', path, os.path.getsize(path), 'bytes')
+
+
 def main(names):
     for name in names:
         if name == 'geometry':
@@ -212,6 +292,9 @@ def main(names):
             continue
         if name == 'energy':
             make_energy()
+            continue
+        if name == 'viscosity':
+            make_viscosity()
             continue
         case, nSteps, keep, src = CASES[name]()
         out = run_case(case, nSteps, keep, src)
@@ -223,4 +306,4 @@ def main(names):
 
 
 if __name__ == '__main__':
-    main(sys.argv[1:] or (['geometry', 'energy'] + list(CASES)))
+    main(sys.argv[1:] or (['geometry', 'energy', 'viscosity'] + list(CASES)))
