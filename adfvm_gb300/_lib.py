@@ -20,6 +20,7 @@ AFVM_BC_ZERO_GRADIENT, AFVM_BC_FIXED_VALUE, AFVM_BC_SYMMETRY_PLANE, AFVM_BC_CYCL
 AFVM_RIEMANN_ROE, AFVM_RIEMANN_LF = 0, 1
 AFVM_MU_CONSTANT, AFVM_MU_SUTHERLAND = 0, 1
 AFVM_OBJ_NONE, AFVM_OBJ_KINETIC_ENERGY, AFVM_OBJ_DRAG, AFVM_OBJ_SUM_T, AFVM_OBJ_VANE = range(5)
+AFVM_VISC = {'uniform': 1, 'turkel': 2, 'abarbanel': 3}
 
 _d = C.POINTER(C.c_double)
 _i = C.POINTER(C.c_int32)
@@ -100,6 +101,8 @@ SIGNATURES = {
                                    C.POINTER(C.c_int64), _d, _v]),
     'afvm_adjoint_energy': (C.c_int, [_v, _v, _v, _v, _v, _v, _v, _d, _v]),
     'afvm_boundary_values': (C.c_int, [_v, _v, _v, _v, _v, _v]),
+    'afvm_adjoint_viscosity': (C.c_int, [_v, _v, _v, _v, C.c_int32, C.c_double, C.c_double, _v, _v, _v, _d, _d,
+                                         C.POINTER(C.c_int32), _v]),
     'afvm_profile': (C.c_int, [_v, C.c_int32]),
     'afvm_profile_read': (C.c_int, [_v, C.c_int32, _d, C.POINTER(C.c_int64)]),
     'afvm_profile_kernel_name': (C.c_char_p, [C.c_int32]),

@@ -24,10 +24,17 @@ def _torch():
 
 
 class Adjoint(object):
-    def __init__(self, primal, parameters='source'):
+    def __init__(self, primal, parameters='source', adjParams=None, viscousInterval=1):
+        """adjParams = [scaling, viscosityType, scaler] as in a case file (templates/vane.py:68):
+        with a viscosityType ('turkel', 'abarbanel', 'uniform') every viscousInterval-th step of
+        the sweep is followed by the artificial-viscosity smoothing (apps/adjoint.py:127-139,
+        250, 288-289)."""
         if parameters != 'source':
             raise NotImplementedError("parameters other than 'source' are not implemented")
         self.primal = primal
+        self.scaling = adjParams[0] if adjParams else None
+        self.viscosityType = adjParams[1] if adjParams else None
+        self.viscousInterval = viscousInterval
         self.mesh = primal.mesh
         self.names = [n + 'a' for n in primal.names]
         self.nParams = 3
@@ -119,6 +126,9 @@ class Adjoint(object):
                 sb = stages[adjointIndex] if keep_stages else None
                 r = p.adjoint_step(y[0], y[1], y[2], dts[primalIndex + adjointIndex], a, obja=1.0, S=S, out=a,
                                    stages=sb)
+                if self.viscosityType and (step + 1) % self.viscousInterval == 0:
+                    p.adjoint_viscosity(y[0], y[1], y[2], a, dts[primalIndex + adjointIndex], self.viscosityType,
+                                        self.scaling)
                 grads = [g.reshape(-1).double() for g in r[3]]
                 sens = [p.sensitivity(grads, pert) for pert in perts]
                 sens_series.append(sens)

@@ -28,7 +28,7 @@ int cuda_fail(Ctx* c, cudaError_t e, const char* what) {
 
 const char* const kKernelNames[KID_COUNT] = {"k_prim", "k_grad", "k_flux", "k_update", "k_objective",
                                              "k_finish", "k_adj_flux", "k_adj_gather", "k_adj_grad",
-                                             "k_adj_prim", "k_adj_misc", "k_sensitivity"};
+                                             "k_adj_prim", "k_adj_misc", "k_sensitivity", "k_adj_viscosity"};
 
 static cudaEvent_t take_event(Ctx* c) {
     if (!c->eventPool.empty()) {
@@ -70,6 +70,12 @@ int dalloc(Ctx* c, void** p, size_t bytes) {
     return AFVM_OK;
 }
 
+}  // namespace
+
+int ctx_alloc(Ctx* c, void** p, size_t bytes) { return dalloc(c, p, bytes); }
+
+namespace {
+
 template <typename T>
 int upload(Ctx* c, const T** dst, const std::vector<T>& v) {
     void* p = nullptr;
@@ -84,7 +90,7 @@ int upload(Ctx* c, const T** dst, const std::vector<T>& v) {
 struct HostTables {
     // faces
     std::vector<int32_t> own, nbr;
-    std::vector<double> nrm, area, dlt, du, lw, qw;
+    std::vector<double> nrm, area, dlt, du, lw, qw, wts;
     std::vector<uint8_t> fkind;
     std::vector<int32_t> gsrc, gkind;
     std::vector<double> gval;
@@ -116,6 +122,7 @@ int upload_mesh(Ctx* c, const HostTables& h, MeshDev<R>& m) {
         if ((st = upload(c, &m.rdlt, cast<R>(r)))) return st;
     }
     if ((st = upload(c, &m.du, cast<R>(h.du)))) return st;
+    if ((st = upload(c, &m.wts, cast<R>(h.wts)))) return st;
     if ((st = upload(c, &m.lw, cast<R>(h.lw)))) return st;
     if ((st = upload(c, &m.qw, cast<R>(h.qw)))) return st;
     if ((st = upload(c, &m.fkind, h.fkind))) return st;
@@ -171,6 +178,9 @@ int build_tables(Ctx* c, const afvm_mesh_tensors* M, const afvm_patch_bc* bcs, H
     h.lw.resize(2 * (size_t)nF); h.qw.resize(6 * (size_t)nF);
     h.area.assign(M->areas, M->areas + nF);
     h.dlt.assign(M->deltas, M->deltas + nF);
+    h.wts.assign(M->weights, M->weights + nF);
+    c->volTotal = 0.0;
+    for (int i = 0; i < nIC; i++) c->volTotal += M->volumes[i];
     for (int f = 0; f < nF; f++) {
         for (int k = 0; k < 3; k++) {
             h.nrm[(size_t)k * nF + f] = M->normals[3 * (size_t)f + k];
@@ -767,6 +777,29 @@ int afvm_adjoint_step(afvm_ctx* ctx, const void* rho, const void* rhoU, const vo
                       void* rhoEa, void* S_rhoa, void* S_rhoUa, void* S_rhoEa, void* stream) {
     return afvm_adjoint_step_stages(ctx, rho, rhoU, rhoE, dt, S_rho, S_rhoU, S_rhoE, nullptr, rhoNa, rhoUNa, rhoENa,
                                     dtca, obja, rhoa, rhoUa, rhoEa, S_rhoa, S_rhoUa, S_rhoEa, stream);
+}
+
+int afvm_adjoint_viscosity(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, int32_t kind,
+                           double scaling, double dt, void* rhoa, void* rhoUa, void* rhoEa, double* M_out,
+                           double* DT_out, int32_t* iterations_out, void* stream) {
+    if (!ctx) return AFVM_ERR_BAD_ARG;
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!rho || !rhoU || !rhoE || !rhoa || !rhoUa || !rhoEa) return fail(c, AFVM_ERR_BAD_ARG, "null pointer");
+    if (kind < AFVM_VISC_UNIFORM || kind > AFVM_VISC_ABARBANEL) return fail(c, AFVM_ERR_BAD_ARG, "viscosity kind");
+    if (!std::isfinite(scaling) || !std::isfinite(dt) || dt < 0) return fail(c, AFVM_ERR_BAD_ARG, "scaling or dt");
+    DeviceGuard dg(c->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    int it = 0, st;
+    if (c->precision == AFVM_FP64)
+        st = adjoint_viscosity_dev<double>(c, (const double*)rho, (const double*)rhoU, (const double*)rhoE, kind,
+                                           scaling, dt, (double*)rhoa, (double*)rhoUa, (double*)rhoEa, M_out, DT_out,
+                                           &it, s);
+    else
+        st = adjoint_viscosity_dev<float>(c, (const float*)rho, (const float*)rhoU, (const float*)rhoE, kind,
+                                          scaling, dt, (float*)rhoa, (float*)rhoUa, (float*)rhoEa, M_out, DT_out,
+                                          &it, s);
+    if (iterations_out) *iterations_out = it;
+    return st;
 }
 
 int afvm_boundary_values(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, void* out,

@@ -34,6 +34,7 @@ struct MeshDev {
     const R* dlt;             // nF  deltas
     const R* rdlt;            // nF  1/deltas (the viscous snGrad divisor, mesh-only)
     const R* du;              // 3 x nF deltasUnit
+    const R* wts;             // nF  weights (central interpolation, interp.py:15-18)
     const R* lw;              // 2 x nF linearWeights
     const R* qw;              // 6 x nF quadraticWeights (side0 xyz, side1 xyz)
     const uint8_t* fkind;     // nF - nIF: FACE_* of each boundary face
@@ -60,7 +61,7 @@ struct MeshDev {
 
 // kernel ids for the optional per-launch event timing (afvm_profile_*)
 enum KernelId { KID_PRIM = 0, KID_GRAD, KID_FLUX, KID_UPDATE, KID_OBJECTIVE, KID_FINISH, KID_ADJ_FLUX,
-                KID_ADJ_GATHER, KID_ADJ_GRAD, KID_ADJ_PRIM, KID_ADJ_MISC, KID_SENS, KID_COUNT };
+                KID_ADJ_GATHER, KID_ADJ_GRAD, KID_ADJ_PRIM, KID_ADJ_MISC, KID_SENS, KID_ADJ_VISC, KID_COUNT };
 extern const char* const kKernelNames[KID_COUNT];
 
 struct ProfEntry {
@@ -126,6 +127,9 @@ struct Ctx {
     double* vanePartials = nullptr;   // 3 x nVaneBlocks
     int nVaneBlocks = 0;
     double* vaneSums = nullptr;       // 3 doubles
+    // adjoint stabilisation work (allocated on first use) and the total volume
+    double* viscWork = nullptr;
+    double volTotal = 0.0;
     // per-launch event timing
     bool prof = false;
     std::vector<ProfEntry> profEntries;
@@ -144,6 +148,11 @@ struct ProfScope {
 
 int fail(Ctx* c, int code, const std::string& msg);
 int cuda_fail(Ctx* c, cudaError_t e, const char* what);
+// device allocation owned by the context (freed by afvm_ctx_destroy)
+int ctx_alloc(Ctx* c, void** p, size_t bytes);
+template <typename R>
+int adjoint_viscosity_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, int kind, double scaling, double dt,
+                          R* ar, R* au, R* ae, double* Mout, double* DTout, int* iters, cudaStream_t s);
 
 // kernel launchers (primal.cu)
 // dt: by value, or read on the device from dtDev when that is non-NULL

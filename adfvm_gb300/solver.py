@@ -382,6 +382,30 @@ class RCF(object):
         L.check(st, self._ctx, 'afvm_adjoint_step_stages')
         return out[0], out[1], out[2], Sg
 
+    def adjoint_viscosity(self, rho, rhoU, rhoE, adj, dt, kind='turkel', scaling=1e-3, want_fields=False):
+        """Artificial-viscosity stabilisation of the adjoint fields ``adj`` (three CUDA tensors,
+        smoothed in place) for the primal state (rho, rhoU, rhoE) and time step dt
+        (afvm_adjoint_viscosity; postpro.computeAdjointViscosity + viscositySolver). kind:
+        'turkel', 'abarbanel' or 'uniform'. Returns the CG iterations, and with want_fields
+        also the viscosity (nCells) and its face values (nFaces) as FP64 CUDA tensors."""
+        torch = _torch()
+        stream = torch.cuda.current_stream(rho.device).cuda_stream
+        vp = lambda t: C.c_void_p(t.data_ptr())
+        Mt = DTt = None
+        if want_fields:
+            Mt = torch.empty(self.mesh.nCells, dtype=torch.float64, device=rho.device)
+            DTt = torch.empty(self.mesh.nFaces, dtype=torch.float64, device=rho.device)
+        it = C.c_int32()
+        st = L.lib().afvm_adjoint_viscosity(self._ctx, vp(rho), vp(rhoU), vp(rhoE), L.AFVM_VISC[kind], float(scaling),
+                                            float(dt), vp(adj[0]), vp(adj[1]), vp(adj[2]),
+                                            None if Mt is None else C.cast(vp(Mt), L._d),
+                                            None if DTt is None else C.cast(vp(DTt), L._d), C.byref(it),
+                                            C.c_void_p(stream))
+        L.check(st, self._ctx, 'afvm_adjoint_viscosity')
+        if want_fields:
+            return it.value, Mt, DTt
+        return it.value
+
     def sensitivity(self, grads, perts):
         """sum_k <grads[k], perts[k]> in FP64 on the device (cmesh.computeSensitivity,
         cmesh.cpp:309-340); CUDA float64 tensors."""

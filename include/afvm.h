@@ -270,6 +270,25 @@ int afvm_adjoint_step_stages(afvm_ctx* ctx, const void* rho, const void* rhoU, c
 
 /* FP64 sum over k of dot(grad[k], pert[k]) (adFVM/cpp/cmesh.cpp:309-340). DEVICE arrays of
  * n[k] doubles; result to *out (host) after the stream work completes. */
+/* Adjoint stabilisation by artificial viscosity (adFVM/postpro.py:491-718, the viscous
+ * adjoint step of apps/adjoint.py:127-139 and 288-289): from the primal state (DEVICE, as
+ * afvm_adjoint_step) the per-cell viscosity M = the largest eigenvalue of the symmetrised 5x5
+ * of the chosen kind, normalised to scaling * M / sqrt(sum M^2 V / sum V) (computeAdjoint-
+ * Viscosity), its central face values DT, and then the implicit heat-equation smoothing of
+ * the adjoint fields rhoa, rhoUa, rhoEa (DEVICE, in place; plain gradients of the state) over
+ * the time step dt (viscositySolver with scaling.cpp:135-159): per component, x = a / V solves
+ * (1 + sum_k c_k) x_c - sum_k c_k x_nbr = a_c / V_c, c_k = dt A_k DT_k / (delta_k V_c), over
+ * the faces with an internal neighbour, and a <- V x. Solved by conjugate gradients to a
+ * relative residual of 1e-13 (AFVM_ERR_TIMEOUT after 500 iterations). M_out (nCells) and
+ * DT_out (nFaces) are optional DEVICE double buffers; iterations_out (host) the CG count. */
+#define AFVM_VISC_UNIFORM   1        /* M = 1                                   */
+#define AFVM_VISC_TURKEL    2        /* postpro.py:586-602                      */
+#define AFVM_VISC_ABARBANEL 3        /* postpro.py:571-585                      */
+int afvm_adjoint_viscosity(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE,
+                           int32_t kind, double scaling, double dt, void* rhoa, void* rhoUa,
+                           void* rhoEa, double* M_out, double* DT_out, int32_t* iterations_out,
+                           void* stream);
+
 int afvm_sensitivity(afvm_ctx* ctx, int32_t nArrays, const double* const* grad,
                      const double* const* pert, const int64_t* n, double* out, void* stream);
 

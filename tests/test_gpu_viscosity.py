@@ -1,0 +1,52 @@
+"""Adjoint stabilisation on the GPU (afvm_adjoint_viscosity) against the reference's own
+postpro.computeAdjointViscosity / viscositySolver (tests/golden/viscosity.npz).
+
+Tolerances: the viscosity and its face values within 1e-12 relative in FP64 (the largest
+eigenvalue comes from Jacobi rotations here and LAPACK there); the smoothed adjoint within
+1e-10 (CG to a relative residual of 1e-13 here, a direct solve there); FP32 contexts (whose
+mesh tables and state are FP32) within 1e-5."""
+import numpy as np
+import pytest
+import torch
+
+from adfvm_gb300.solver import RCF
+from tests import golden_cases as G
+from tests.test_viscosity import CASES, PATH
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(name, precision='fp64'):
+    g = np.load(PATH)
+    case = CASES[name]()
+    m = case.build_mesh()
+    rcf = RCF(m, case.bc, objective=case.objective, precision=precision, **case.config)
+    td = torch.float64 if precision == 'fp64' else torch.float32
+    x = [torch.as_tensor(g['%s/%s' % (name, k)]).to(td).cuda() for k in ('rho', 'rhoU', 'rhoE')]
+    return g, m, rcf, x, td
+
+
+@pytest.mark.parametrize('name', list(CASES))
+@pytest.mark.parametrize('kind', ['turkel', 'abarbanel', 'uniform'])
+def test_viscosity_fields_match_reference(name, kind):
+    g, m, rcf, x, td = _setup(name)
+    s = float(g['%s/%s/scaling' % (name, kind)])
+    a = [torch.zeros_like(t) for t in x]
+    it, M, DT = rcf.adjoint_viscosity(x[0], x[1], x[2], a, 1e-6, kind, s, want_fields=True)
+    assert G.rel_err(M.cpu().numpy()[:m.nInternalCells], g['%s/%s/M' % (name, kind)][:m.nInternalCells]) < 1e-12
+    assert G.rel_err(DT.cpu().numpy(), g['%s/%s/DT' % (name, kind)]) < 1e-12
+    for t in a:
+        assert torch.count_nonzero(t) == 0          # zero stays zero
+
+
+@pytest.mark.parametrize('name', list(CASES))
+@pytest.mark.parametrize('precision', ['fp64', 'fp32'])
+def test_smoother_matches_reference(name, precision):
+    g, m, rcf, x, td = _setup(name, precision)
+    dt = float(g['%s/smooth/dt' % name])
+    a = [torch.as_tensor(g['%s/smooth/in_%s' % (name, k)]).to(td).cuda() for k in ('rhoa', 'rhoUa', 'rhoEa')]
+    it = rcf.adjoint_viscosity(x[0], x[1], x[2], a, dt, 'abarbanel', float(g['%s/abarbanel/scaling' % name]))
+    tol = 1e-10 if precision == 'fp64' else 1e-5
+    for k, nm in enumerate(['rhoa', 'rhoUa', 'rhoEa']):
+        assert G.rel_err(a[k].double().cpu().numpy(), g['%s/smooth/out_%s' % (name, nm)]) < tol, (nm, it)
+    assert 0 < it < 500
