@@ -67,7 +67,10 @@ class Adjoint(object):
         obja = float(np.asarray(rest[4]).reshape(-1)[0])
         if dtca != 0.0:
             raise NotImplementedError('dtca != 0: the CFL-sum output has no adjoint')
-        r = p.adjoint_step(x[0], x[1], x[2], dt, seeds, obja=obja, S=S)
+        # the stages the primal map kept for this very state, if any
+        Sh = [primal_in[base + k] for k in range(3)]
+        stages = p.kept_stages(primal_in[0], primal_in[1], primal_in[2], dt, Sh)
+        r = p.adjoint_step(x[0], x[1], x[2], dt, seeds, obja=obja, S=S, stages=stages)
         out = [t.cpu().numpy().astype(np.float64) for t in r[:3]]
         return out + [t.cpu().numpy().astype(np.float64) for t in r[3]]
 

@@ -20,7 +20,7 @@ NVCC = os.environ.get('NVCC', 'nvcc')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 HOST_FLAGS = ['-O3', '-fPIC', '-fopenmp', '-ffp-contract=off', '-std=c++17']
 NVCC_FLAGS = ARCH + ['-O3', '-lineinfo', '-std=c++17', '--expt-relaxed-constexpr',
-                     '-Xcompiler', '-fPIC,-ffp-contract=off', '-I' + INCLUDE, '-I' + CSRC]
+                     '-Xcompiler', '-fPIC,-ffp-contract=off,-fopenmp', '-I' + INCLUDE, '-I' + CSRC]
 # the device mesh builder rounds every product and sum as the host builder does
 PER_FILE_FLAGS = {'geometry_dev.cu': ['-fmad=false']}
 

@@ -168,11 +168,22 @@ int build_tables(Ctx* c, const afvm_mesh_tensors* M, const afvm_patch_bc* bcs, H
     // faces
     h.own.assign(M->owner, M->owner + nF);
     h.nbr.assign(M->neighbour, M->neighbour + nF);
+    // the per-face and per-cell loops run on all host cores; a failed check sets a code (the
+    // smallest index's message is reported)
+    int bad = 0;
+#pragma omp parallel for reduction(max : bad)
     for (int f = 0; f < nF; f++) {
-        if (h.own[f] < 0 || h.own[f] >= nIC) return fail(c, AFVM_ERR_BAD_ARG, "owner out of range");
-        if (h.nbr[f] < 0 || h.nbr[f] >= nC) return fail(c, AFVM_ERR_BAD_ARG, "neighbour out of range");
-        if (f < nIF && h.nbr[f] >= nIC) return fail(c, AFVM_ERR_BAD_ARG, "internal face with a ghost neighbour");
-        if (f >= nIF && h.nbr[f] != nIC + (f - nIF)) return fail(c, AFVM_ERR_BAD_ARG, "ghost id of a boundary face");
+        int e = 0;
+        if (h.own[f] < 0 || h.own[f] >= nIC) e = 1;
+        else if (h.nbr[f] < 0 || h.nbr[f] >= nC) e = 2;
+        else if (f < nIF && h.nbr[f] >= nIC) e = 3;
+        else if (f >= nIF && h.nbr[f] != nIC + (f - nIF)) e = 4;
+        bad = std::max(bad, e);
+    }
+    if (bad) {
+        const char* msg[] = {"", "owner out of range", "neighbour out of range", "internal face with a ghost neighbour",
+                             "ghost id of a boundary face"};
+        return fail(c, AFVM_ERR_BAD_ARG, msg[bad]);
     }
     h.nrm.resize(3 * (size_t)nF); h.du.resize(3 * (size_t)nF);
     h.lw.resize(2 * (size_t)nF); h.qw.resize(6 * (size_t)nF);
@@ -181,6 +192,7 @@ int build_tables(Ctx* c, const afvm_mesh_tensors* M, const afvm_patch_bc* bcs, H
     h.wts.assign(M->weights, M->weights + nF);
     c->volTotal = 0.0;
     for (int i = 0; i < nIC; i++) c->volTotal += M->volumes[i];
+#pragma omp parallel for
     for (int f = 0; f < nF; f++) {
         for (int k = 0; k < 3; k++) {
             h.nrm[(size_t)k * nF + f] = M->normals[3 * (size_t)f + k];
@@ -265,17 +277,18 @@ int build_tables(Ctx* c, const afvm_mesh_tensors* M, const afvm_patch_bc* bcs, H
     h.gnb.resize(6 * n); h.gw.resize(6 * n); h.gsn.resize(18 * n);
     h.rvol.resize(n); h.vol.assign(M->volumes, M->volumes + nIC);
     h.accf.resize(6 * n); h.accw.resize(6 * n);
+    bad = 0;
+#pragma omp parallel for reduction(max : bad)
     for (int ci = 0; ci < nIC; ci++) {
-        if (!(M->volumes[ci] > 0)) return fail(c, AFVM_ERR_BAD_ARG, "non-positive cell volume");
+        if (!(M->volumes[ci] > 0)) { bad = std::max(bad, 1); continue; }
         h.rvol[ci] = 1.0 / M->volumes[ci];
-        int fs[6];
+        int fs[6] = {-1, -1, -1, -1, -1, -1};
         for (int s = 0; s < 6; s++) {
             int f = M->cellFaces[6 * (size_t)ci + s];
             int O = M->cellOwner[6 * (size_t)ci + s];
             int nb = M->cellNeighbours[6 * (size_t)ci + s];
-            if (f < 0 || f >= nF || nb < 0 || nb >= nC || (O != 0 && O != 1))
-                return fail(c, AFVM_ERR_BAD_ARG, "cell connectivity out of range");
-            if ((O == 1) != (h.own[f] == ci)) return fail(c, AFVM_ERR_BAD_ARG, "cellOwner disagrees with owner");
+            if (f < 0 || f >= nF || nb < 0 || nb >= nC || (O != 0 && O != 1)) { bad = std::max(bad, 2); f = -1; break; }
+            if ((O == 1) != (h.own[f] == ci)) { bad = std::max(bad, 3); f = -1; break; }
             double Od = (double)O;
             double w = M->weights[f];
             double S = M->areas[f];
@@ -287,15 +300,23 @@ int build_tables(Ctx* c, const afvm_mesh_tensors* M, const afvm_patch_bc* bcs, H
             }
             fs[s] = f;
         }
+        bool okc = true;
+        for (int s = 0; s < 6; s++) okc = okc && fs[s] >= 0;
+        if (!okc) continue;
         // collate order: internal faces by face id, then patches in sorted order
         std::sort(fs, fs + 6, [&](int a, int b2) { return rank[a] < rank[b2]; });
         for (int s = 0; s < 6; s++) {
             int f = fs[s];
             bool ownerSide = h.own[f] == ci;
-            if (!ownerSide && f >= nIF) return fail(c, AFVM_ERR_BAD_ARG, "boundary face not owned by its cell");
+            if (!ownerSide && f >= nIF) { bad = std::max(bad, 4); break; }
             h.accf[s * n + ci] = ownerSide ? f : ~f;
             h.accw[s * n + ci] = ownerSide ? M->areas[f] / M->volumesL[f] : M->areas[f] / M->volumesR[f];
         }
+    }
+    if (bad) {
+        const char* msg[] = {"", "non-positive cell volume", "cell connectivity out of range",
+                             "cellOwner disagrees with owner", "boundary face not owned by its cell"};
+        return fail(c, AFVM_ERR_BAD_ARG, msg[bad]);
     }
     // adjoint tables: face weights, back-slot weights, ghosts grouped by source, ghost slots
     h.wpf.resize(nF); h.wnf.resize(std::max(nIF, 1));
@@ -303,6 +324,7 @@ int build_tables(Ctx* c, const afvm_mesh_tensors* M, const afvm_patch_bc* bcs, H
     for (int f = 0; f < nIF; f++) h.wnf[f] = M->areas[f] / M->volumesR[f];
     h.gwb.assign(6 * n, 0.0);
     h.gslot.assign(std::max(nG, 1), -1);
+#pragma omp parallel for
     for (int ci = 0; ci < nIC; ci++) {
         for (int s = 0; s < 6; s++) {
             int f = M->cellFaces[6 * (size_t)ci + s];

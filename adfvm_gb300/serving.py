@@ -317,14 +317,19 @@ def plain_one_at_a_time(requests, library, device=0, nPrimal=100):
     """The plain form: FP64, one request at a time, step calls without graphs or overlap,
     the adjoint sweep storing every state (no checkpointing). Returns stats and results."""
     torch = _torch()
-    t0 = time.perf_counter()
     ctxs = {}
-    out = []
-    for r in requests:
+    for r in requests:              # solver contexts are set up before the clock starts
         case = library.get(r.key)
         if r.key not in ctxs:
             ctxs[r.key] = RCF(case.mesh, case.bc, objective=case.objective, precision='fp64', device=device,
                               **case.config)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = []
+    times = []
+    for r in requests:
+        tr = time.perf_counter()
+        case = library.get(r.key)
         rcf = ctxs[r.key]
         state, dS = request_inputs(case, r.seed)
         x = [torch.as_tensor(a).cuda(device) for a in state]
@@ -342,6 +347,7 @@ def plain_one_at_a_time(requests, library, device=0, nPrimal=100):
             acc += sum((g.double() * p).sum() for g, p in zip(rr[3], d))
         r.sensitivity = float(acc) / nPrimal
         out.append(r)
+        times.append(time.perf_counter() - tr)
     torch.cuda.synchronize()
     el = time.perf_counter() - t0
-    return {'requests': len(out), 'elapsed_s': el, 'req_per_s': len(out) / el}
+    return {'requests': len(out), 'elapsed_s': el, 'req_per_s': len(out) / el, 'seconds_per_request': times}

@@ -381,41 +381,58 @@ def mesh_build_timing(case, local, reps=3):
                     'every result to host arrays'}
 
 
-def serving_bench(local, n_requests=48, lams=(5.0, 20.0, 100.0, 200.0), seed=4, nplain=8):
-    """Poisson streams of sensitivity requests on boxes {16,24,32,48,64} and cylinders
-    {64x32,128x64} (100 primal + 100 adjoint steps each), lambda swept: served FP32
-    continuous batching vs the plain FP64 one-at-a-time form on the same first requests."""
+SERVING_KEYS = ['box16', 'box24', 'box32', 'box48', 'box64', 'box96', 'cyl64x32', 'cyl128x64', 'cyl256x128']
+SERVING_LAMBDAS = (1.0, 2.0, 5.0, 10.0, 20.0, 50.0, 100.0, 200.0)
+
+
+def serving_bench(local, lams=SERVING_LAMBDAS, seed=4, n_mix=48, window_s=6.0):
+    """Sensitivity requests, each a jittered periodic box of side 16-96 or a cylinder O-grid
+    64x32-256x128 drawn uniformly (seed 4), 100 primal + 100 adjoint steps.
+
+    * capacity on one mix of n_mix requests: served (FP32, continuous batching, all admitted
+      at once) against the plain FP64 one-at-a-time form, whose time on the mix is the sum of
+      its measured time per request of each mesh (it runs requests back to back);
+    * latency: Poisson arrivals swept over lambda = 1-200 req/s, min(n_mix, max(8, 6 s x
+      lambda)) requests per rate, p50/p99 from arrival to result;
+    * accuracy: the served FP32 sensitivity of one request per mesh against its plain FP64 one."""
     from adfvm_gb300 import serving
-    keys = ['box16', 'box24', 'box32', 'box48', 'box64', 'cyl64x32', 'cyl128x64']
+    keys = SERVING_KEYS
     rng = np.random.default_rng(seed)
-    ks = [keys[i] for i in rng.integers(0, len(keys), size=n_requests)]
-    gaps = rng.exponential(1.0, size=n_requests)
+    ks = [keys[i] for i in rng.integers(0, len(keys), size=n_mix)]
+    gaps = rng.exponential(1.0, size=n_mix)
     lib = serving.MeshLibrary()
     for k in keys:
         lib.get(k)
     srv = serving.SensitivityServer(precision='fp32', device=local, k=10, nPrimal=100, library=lib)
     srv.warm(keys)
+    # plain FP64: one request per mesh, timed one by one
+    probe = [serving.Request(rid=1000 + i, key=k, seed=1000 + i, nPrimal=100) for i, k in enumerate(keys)]
+    sp = serving.plain_one_at_a_time(probe, lib, device=local, nPrimal=100)
+    t_plain = dict(zip(keys, sp['seconds_per_request']))
+    plain_mix_s = sum(t_plain[k] for k in ks)
+    # served: the same mix all at once, then the same probe requests for accuracy
+    mix = [serving.Request(rid=i, key=k, seed=i, nPrimal=100, arrival=0.0) for i, k in enumerate(ks)]
+    sm = srv.serve(mix, realtime=False)
+    same = [serving.Request(rid=1000 + i, key=k, seed=1000 + i, nPrimal=100, arrival=0.0) for i, k in enumerate(keys)]
+    srv.serve(same, realtime=False)
+    errs = {a.key: float('%.3g' % (abs(a.sensitivity - b.sensitivity) / abs(b.sensitivity))) for a, b in zip(same, probe)}
     sweep = []
-    last = None
     for lam in lams:
-        t = np.cumsum(gaps / lam)
-        reqs = [serving.Request(rid=i, key=k, seed=i, nPrimal=100, arrival=float(a)) for i, (k, a) in enumerate(zip(ks, t))]
+        nr = int(min(n_mix, max(8, round(window_s * lam))))
+        t = np.cumsum(gaps[:nr] / lam)
+        reqs = [serving.Request(rid=i, key=k, seed=i, nPrimal=100, arrival=float(a))
+                for i, (k, a) in enumerate(zip(ks[:nr], t))]
         st = srv.serve(reqs, realtime=True)
-        sweep.append({'lambda': lam, 'req_per_s': round(st['req_per_s'], 3), 'p50_s': round(st['p50_s'], 4),
-                      'p99_s': round(st['p99_s'], 4)})
-        last = reqs
-    plain = [serving.Request(rid=i, key=k, seed=i, nPrimal=100) for i, k in enumerate(ks[:nplain])]
-    sp = serving.plain_one_at_a_time(plain, lib, device=local, nPrimal=100)
-    errs = {}
-    for a, b in zip(last[:nplain], plain):
-        e = abs(a.sensitivity - b.sensitivity) / abs(b.sensitivity)
-        errs[a.key] = max(errs.get(a.key, 0.0), float('%.3g' % e))
-    cap = max(x['req_per_s'] for x in sweep)
-    return {'sweep': sweep, 'requests_per_lambda': n_requests, 'capacity_req_per_s': cap,
-            'plain_fp64_req_per_s': round(sp['req_per_s'], 3), 'speedup_vs_plain': round(cap / sp['req_per_s'], 2),
-            'max_rel_err_fp32_vs_fp64': max(errs.values()), 'rel_err_by_mesh': errs, 'slots': len(srv.slots),
-            'meshes': keys, 'steps_per_request': '100 primal + 100 adjoint (checkpoints every 10)'}
-
+        sweep.append({'lambda': lam, 'requests': nr, 'req_per_s': round(st['req_per_s'], 3),
+                      'p50_s': round(st['p50_s'], 4), 'p99_s': round(st['p99_s'], 4)})
+    served_rate = n_mix / sm['elapsed_s']
+    plain_rate = n_mix / plain_mix_s
+    return {'mix_requests': n_mix, 'served_req_per_s': round(served_rate, 3), 'plain_fp64_req_per_s': round(plain_rate, 3),
+            'speedup_vs_plain': round(served_rate / plain_rate, 2),
+            'plain_seconds_per_request': {k: round(v, 4) for k, v in t_plain.items()},
+            'latency_sweep': sweep, 'max_rel_err_fp32_vs_fp64': max(errs.values()), 'rel_err_by_mesh': errs,
+            'slots': len(srv.slots), 'meshes': keys,
+            'steps_per_request': '100 primal + 100 adjoint (checkpoints every 10)'}
 
 
 def run_reference(args):

@@ -26,8 +26,12 @@ def _seeds(x, seed):
     return [torch.as_tensor(rng.normal(size=tuple(t.shape)) / max(np.abs(t.numpy()).max(), 1.0)) for t in x]
 
 
+# (the vane channel's golden state is uniform, which puts every wall-parallel face exactly at
+# |U.n| = 0, the kink of the Roe entropy fix: there the VJP is decided by roundoff of the
+# face velocity, in the reference as here, and no two evaluation orders agree; the vane channel
+# is compared at a perturbed state in test_vane_objective_adjoint_with_heat_term)
 @pytest.mark.parametrize('name', ['box8', 'cyl32x16', 'sod200_sym_lf', 'box6_inviscid_sumT', 'sod1000',
-                                  'duct100_totalpt', 'duct60_totalpt_normals', 'vane32x12'])
+                                  'duct100_totalpt', 'duct60_totalpt_normals'])
 def test_adjoint_step_matches_autograd(name):
     case, mesh, x, S, dt = _setup(name)
     prob = torch_ref.Problem(mesh, case.bc, case.config, case.objective)
@@ -163,11 +167,12 @@ def test_kept_stages_give_the_same_adjoint(name, precision):
         rcf.adjoint_step(d[0], d[1], d[2], dt, seeds, S=Sd, stages=st[:10])
 
 
-@pytest.mark.parametrize('b', [0.0, 1e-5])
-def test_vane_objective_adjoint_with_heat_term(b):
-    """The turbine-vane objective with its heat-transfer term switched on (the reference's own
-    file has b = 0): value and VJP against the oracle and its autograd, FP64."""
-    case = cases.vane_channel(24, 10, b=b)
+@pytest.mark.parametrize('nx,ny,b,ref', [(24, 10, 0.0, False), (24, 10, 1e-5, False), (32, 12, 0.0, True)])
+def test_vane_objective_adjoint_with_heat_term(nx, ny, b, ref):
+    """The turbine-vane objective, with its heat-transfer term switched on (the reference's own
+    file has b = 0) and with the reference's own constants on the golden mesh: value and VJP
+    against the oracle and its autograd, FP64, at a perturbed state."""
+    case = cases.vane_channel(nx, ny, reference_constants=True) if ref else cases.vane_channel(nx, ny, b=b)
     mesh = case.build_mesh()
     x = [torch.as_tensor(a) for a in cases.conservative(case)]
     rng = np.random.default_rng(5)
