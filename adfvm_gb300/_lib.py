@@ -13,7 +13,7 @@ AFVM_OK, AFVM_ERR_BAD_ARG, AFVM_ERR_OOM, AFVM_ERR_NONFINITE, AFVM_ERR_TIMEOUT, \
     AFVM_ERR_CUDA, AFVM_ERR_UNSUPPORTED = range(7)
 STATUS_NAMES = {0: 'OK', 1: 'BAD_ARG', 2: 'OOM', 3: 'NONFINITE', 4: 'TIMEOUT', 5: 'CUDA', 6: 'UNSUPPORTED'}
 
-AFVM_FP64, AFVM_FP32 = 0, 1
+AFVM_FP64, AFVM_FP32, AFVM_FP32_STATE64 = 0, 1, 2
 AFVM_PATCH_PLAIN, AFVM_PATCH_CYCLIC, AFVM_PATCH_PROCESSOR = 0, 1, 2
 AFVM_BC_ZERO_GRADIENT, AFVM_BC_FIXED_VALUE, AFVM_BC_SYMMETRY_PLANE, AFVM_BC_CYCLIC, AFVM_BC_CBC_UPT, \
     AFVM_BC_CBC_TOTAL_PT = range(6)

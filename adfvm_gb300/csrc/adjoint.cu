@@ -24,25 +24,25 @@ namespace afvm {
 constexpr int FADJ = 40;
 constexpr int CBAR = 20;   // per cell: primitive adjoint (5) then gradient adjoint (15)
 
-template <typename R>
+template <typename R, typename S>
 __global__ void __launch_bounds__(FLUX_BLOCK, sizeof(R) == 8 ? 3 : 1) k_adj_flux(MeshDev<R> m, Phys P, const R* __restrict__ rec, R coef,
-                                                    const R* __restrict__ ar, const R* __restrict__ au,
-                                                    const R* __restrict__ ae, R* __restrict__ fadj, int inviscid) {
+                                                    const S* __restrict__ ar, const S* __restrict__ au,
+                                                    const S* __restrict__ ae, R* __restrict__ fadj, int inviscid) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= m.nF) return;
     int kind = (f < m.nIF) ? FACE_INTERNAL : (int)m.fkind[f - m.nIF];
     int iP = m.own[f];
     R wp = m.wpf[f];
     R Fb[5];
-    Fb[0] = (coef * ar[iP]) * wp;
-    for (int k = 0; k < 3; k++) Fb[1 + k] = (coef * au[3 * iP + k]) * wp;
-    Fb[4] = (coef * ae[iP]) * wp;
+    Fb[0] = (coef * R(ar[iP])) * wp;
+    for (int k = 0; k < 3; k++) Fb[1 + k] = (coef * R(au[3 * iP + k])) * wp;
+    Fb[4] = (coef * R(ae[iP])) * wp;
     if (f < m.nIF) {
         int iN = m.nbr[f];
         R wn = m.wnf[f];
-        Fb[0] = Fb[0] - (coef * ar[iN]) * wn;
-        for (int k = 0; k < 3; k++) Fb[1 + k] = Fb[1 + k] - (coef * au[3 * iN + k]) * wn;
-        Fb[4] = Fb[4] - (coef * ae[iN]) * wn;
+        Fb[0] = Fb[0] - (coef * R(ar[iN])) * wn;
+        for (int k = 0; k < 3; k++) Fb[1 + k] = Fb[1 + k] - (coef * R(au[3 * iN + k])) * wn;
+        Fb[4] = Fb[4] - (coef * R(ae[iN])) * wn;
     }
     FaceIn<R> in;
     load_face<R>(m, rec, f, in);
@@ -86,13 +86,13 @@ __device__ __forceinline__ void phi_bar(const R* G, const R* sn, R rv, R* pb) {
     for (int i = 0; i < 5; i++) pb[i] = rv * (G[3 * i] * sn[0] + G[3 * i + 1] * sn[1] + G[3 * i + 2] * sn[2]);
 }
 
-template <typename R, int STAGE>
+template <typename R, typename S, int STAGE>
 __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const R* __restrict__ rec,
                                                      const R* __restrict__ fadj, const R* __restrict__ cbar,
-                                                     const R* __restrict__ ur, const R* __restrict__ uu,
-                                                     const R* __restrict__ ue,
-                                                     const R* ainr, const R* ainu, const R* aine,
-                                                     R* a1r, R* a1u, R* a1e, R* a0r, R* a0u, R* a0e, R* sb,
+                                                     const S* __restrict__ ur, const S* __restrict__ uu,
+                                                     const S* __restrict__ ue,
+                                                     const S* ainr, const S* ainu, const S* aine,
+                                                     S* a1r, S* a1u, S* a1e, S* a0r, S* a0u, S* a0e, S* sb,
                                                      double dt, int objective, int objStart, int objN, double obja,
                                                      VaneDev vane) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -226,24 +226,24 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const
     for (int k = 0; k < 3; k++) J[1 + k] = Ubt[k] * rr;
     J[4] = eb * rr;
     J[0] = rhob - (Ubt[0] * U[0] + Ubt[1] * U[1] + Ubt[2] * U[2]) * rr - eb * E * rr;
-    // SSP-RK reverse (timestep.py:35-45 transposed)
-    R ain[5] = {ainr[c], ainu[3 * c], ainu[3 * c + 1], ainu[3 * c + 2], aine[c]};
-    R out[5];
+    // SSP-RK reverse (timestep.py:35-45 transposed), in the state's type S
+    S ain[5] = {ainr[c], ainu[3 * c], ainu[3 * c + 1], ainu[3 * c + 2], aine[c]};
+    S out[5];
     if (STAGE == 2) {
-        for (int k = 0; k < 5; k++) out[k] = R(2. / 3) * ain[k] + (R)J[k];
-        R z[5];
-        for (int k = 0; k < 5; k++) { z[k] = R(1. / 3) * ain[k]; sb[5 * (size_t)c + k] = R(2. / 3) * R(dt) * ain[k]; }
+        for (int k = 0; k < 5; k++) out[k] = S(2. / 3) * ain[k] + (S)J[k];
+        S z[5];
+        for (int k = 0; k < 5; k++) { z[k] = S(1. / 3) * ain[k]; sb[5 * (size_t)c + k] = S(2. / 3) * S(dt) * ain[k]; }
         a0r[c] = z[0]; a0u[3 * c] = z[1]; a0u[3 * c + 1] = z[2]; a0u[3 * c + 2] = z[3]; a0e[c] = z[4];
         a1r[c] = out[0]; a1u[3 * c] = out[1]; a1u[3 * c + 1] = out[2]; a1u[3 * c + 2] = out[3]; a1e[c] = out[4];
     } else if (STAGE == 1) {
-        for (int k = 0; k < 5; k++) out[k] = R(1. / 4) * ain[k] + (R)J[k];
-        R z[5] = {a0r[c], a0u[3 * c], a0u[3 * c + 1], a0u[3 * c + 2], a0e[c]};
-        for (int k = 0; k < 5; k++) { z[k] += R(3. / 4) * ain[k]; sb[5 * (size_t)c + k] += R(1. / 4) * R(dt) * ain[k]; }
+        for (int k = 0; k < 5; k++) out[k] = S(1. / 4) * ain[k] + (S)J[k];
+        S z[5] = {a0r[c], a0u[3 * c], a0u[3 * c + 1], a0u[3 * c + 2], a0e[c]};
+        for (int k = 0; k < 5; k++) { z[k] += S(3. / 4) * ain[k]; sb[5 * (size_t)c + k] += S(1. / 4) * S(dt) * ain[k]; }
         a0r[c] = z[0]; a0u[3 * c] = z[1]; a0u[3 * c + 1] = z[2]; a0u[3 * c + 2] = z[3]; a0e[c] = z[4];
         a1r[c] = out[0]; a1u[3 * c] = out[1]; a1u[3 * c + 1] = out[2]; a1u[3 * c + 2] = out[3]; a1e[c] = out[4];
     } else {
-        R z[5] = {a0r[c], a0u[3 * c], a0u[3 * c + 1], a0u[3 * c + 2], a0e[c]};
-        for (int k = 0; k < 5; k++) { z[k] += ain[k] + (R)J[k]; sb[5 * (size_t)c + k] += R(dt) * ain[k]; }
+        S z[5] = {a0r[c], a0u[3 * c], a0u[3 * c + 1], a0u[3 * c + 2], a0e[c]};
+        for (int k = 0; k < 5; k++) { z[k] += ain[k] + (S)J[k]; sb[5 * (size_t)c + k] += S(dt) * ain[k]; }
         a0r[c] = z[0]; a0u[3 * c] = z[1]; a0u[3 * c + 1] = z[2]; a0u[3 * c + 2] = z[3]; a0e[c] = z[4];
     }
 }
@@ -259,52 +259,52 @@ __global__ void k_split5(int n, const R* __restrict__ sb, R* r, R* u, R* e) {
     if (e) e[c] = s[4];
 }
 
-template <typename R>
-int adjoint_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double dt, const R* Srho, const R* SrhoU,
-                     const R* SrhoE, const R* rhoNa, const R* rhoUNa, const R* rhoENa, double obja, R* rhoa,
-                     R* rhoUa, R* rhoEa, R* Srhoa, R* SrhoUa, R* SrhoEa, cudaStream_t s, const R* stages) {
+template <typename R, typename S>
+int adjoint_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double dt, const S* Srho, const S* SrhoU,
+                     const S* SrhoE, const S* rhoNa, const S* rhoUNa, const S* rhoENa, double obja, S* rhoa,
+                     S* rhoUa, S* rhoEa, S* Srhoa, S* SrhoUa, S* SrhoEa, cudaStream_t s, const S* stages) {
     const MeshDev<R>& m = meshOf<R>(c);
     const Phys& P = c->phys;
-    default_sources<R>(c, Srho, SrhoU, SrhoE);
+    default_sources<S>(c, Srho, SrhoU, SrhoE);
     int inviscid = (P.muModel == AFVM_MU_CONSTANT && P.mu0 == 0.0) ? 1 : 0;
-    R* u1[3] = {(R*)c->u1[0], (R*)c->u1[1], (R*)c->u1[2]};
-    R* u2[3] = {(R*)c->u2[0], (R*)c->u2[1], (R*)c->u2[2]};
-    const R* u0c[3] = {rho, rhoU, rhoE};
-    const R* u1c[3] = {u1[0], u1[1], u1[2]};
-    const R* u2c[3] = {u2[0], u2[1], u2[2]};
+    S* u1[3] = {(S*)c->u1[0], (S*)c->u1[1], (S*)c->u1[2]};
+    S* u2[3] = {(S*)c->u2[0], (S*)c->u2[1], (S*)c->u2[2]};
+    const S* u0c[3] = {rho, rhoU, rhoE};
+    const S* u1c[3] = {u1[0], u1[1], u1[2]};
+    const S* u2c[3] = {u2[0], u2[1], u2[2]};
     if (stages) {
         // the stage states the primal step kept (afvm_primal_step_stages)
-        stage_views<R, const R>(stages, m.nIC, u1c, u2c);
+        stage_views<S, const S>(stages, m.nIC, u1c, u2c);
     } else {
         // forward recompute of the stage states
         cudaMemsetAsync(c->dtcBits, 0, sizeof(unsigned long long), s);
-        launch_prim_grad<R>(c, rho, rhoU, rhoE, s);
-        launch_flux_update<R>(c, 0, dt, nullptr, u0c, u1c, u2c, Srho, SrhoU, SrhoE, u1, s);
-        launch_prim_grad<R>(c, u1[0], u1[1], u1[2], s);
-        launch_flux_update<R>(c, 1, dt, nullptr, u0c, u1c, u2c, Srho, SrhoU, SrhoE, u2, s);
+        launch_prim_grad<R, S>(c, rho, rhoU, rhoE, s);
+        launch_flux_update<R, S>(c, 0, dt, nullptr, u0c, u1c, u2c, Srho, SrhoU, SrhoE, u1, s);
+        launch_prim_grad<R, S>(c, u1[0], u1[1], u1[2], s);
+        launch_flux_update<R, S>(c, 1, dt, nullptr, u0c, u1c, u2c, Srho, SrhoU, SrhoE, u2, s);
     }
     // reverse sweep
-    R* A1[3] = {(R*)c->a1[0], (R*)c->a1[1], (R*)c->a1[2]};
-    R* A2[3] = {(R*)c->a2[0], (R*)c->a2[1], (R*)c->a2[2]};
+    S* A1[3] = {(S*)c->a1[0], (S*)c->a1[1], (S*)c->a1[2]};
+    S* A2[3] = {(S*)c->a2[0], (S*)c->a2[1], (S*)c->a2[2]};
     R* fadj = (R*)c->fadj;
     R* cbar = (R*)c->cbar;
-    R* sb = (R*)c->sbar;
+    S* sb = (S*)c->sbar;
     const R* rec = (const R*)c->rec;
     int nbC = nblocks(m.nIC);
     const double beta[3] = {1.0, 1. / 4, 2. / 3};
     for (int st = 2; st >= 0; st--) {
-        const R* const* u = st == 0 ? u0c : (st == 1 ? u1c : u2c);
-        launch_prim_grad<R>(c, u[0], u[1], u[2], s);
+        const S* const* u = st == 0 ? u0c : (st == 1 ? u1c : u2c);
+        launch_prim_grad<R, S>(c, u[0], u[1], u[2], s);
         if (st == 1 && c->objective == AFVM_OBJ_VANE) launch_vane_sums<R>(c, s, nullptr, nullptr);
         // adjoint of this stage's output: a3 = seeds, a2 = A2, a1 = A1
-        const R* ain[3];
+        const S* ain[3];
         if (st == 2) { ain[0] = rhoNa; ain[1] = rhoUNa; ain[2] = rhoENa; }
         else if (st == 1) { ain[0] = A2[0]; ain[1] = A2[1]; ain[2] = A2[2]; }
         else { ain[0] = A1[0]; ain[1] = A1[1]; ain[2] = A1[2]; }
         R coef = (R)(-beta[st] * dt);
         {
             ProfScope ps(c, KID_ADJ_FLUX, s);
-            k_adj_flux<R><<<(m.nF + FLUX_BLOCK - 1) / FLUX_BLOCK, FLUX_BLOCK, 0, s>>>(m, P, rec, coef, ain[0], ain[1],
+            k_adj_flux<R, S><<<(m.nF + FLUX_BLOCK - 1) / FLUX_BLOCK, FLUX_BLOCK, 0, s>>>(m, P, rec, coef, ain[0], ain[1],
                                                                                    ain[2], fadj, inviscid);
         }
         {
@@ -313,33 +313,33 @@ int adjoint_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double 
         }
         ProfScope ps(c, KID_ADJ_GRAD, s);
         if (st == 2)
-            k_adj_cell2<R, 2><<<nbC, BLOCK, 0, s>>>(m, P, rec, fadj, cbar, u[0], u[1], u[2], ain[0], ain[1], ain[2],
+            k_adj_cell2<R, S, 2><<<nbC, BLOCK, 0, s>>>(m, P, rec, fadj, cbar, u[0], u[1], u[2], ain[0], ain[1], ain[2],
                                                     A2[0], A2[1], A2[2], rhoa, rhoUa, rhoEa, sb, dt, c->objective,
                                                     c->objStart, c->objN, obja, c->vane);
         else if (st == 1)
-            k_adj_cell2<R, 1><<<nbC, BLOCK, 0, s>>>(m, P, rec, fadj, cbar, u[0], u[1], u[2], ain[0], ain[1], ain[2],
+            k_adj_cell2<R, S, 1><<<nbC, BLOCK, 0, s>>>(m, P, rec, fadj, cbar, u[0], u[1], u[2], ain[0], ain[1], ain[2],
                                                     A1[0], A1[1], A1[2], rhoa, rhoUa, rhoEa, sb, dt, c->objective,
                                                     c->objStart, c->objN, obja, c->vane);
         else
-            k_adj_cell2<R, 0><<<nbC, BLOCK, 0, s>>>(m, P, rec, fadj, cbar, u[0], u[1], u[2], ain[0], ain[1], ain[2],
+            k_adj_cell2<R, S, 0><<<nbC, BLOCK, 0, s>>>(m, P, rec, fadj, cbar, u[0], u[1], u[2], ain[0], ain[1], ain[2],
                                                     nullptr, nullptr, nullptr, rhoa, rhoUa, rhoEa, sb, dt,
                                                     c->objective, c->objStart, c->objN, obja, c->vane);
     }
     if (Srhoa || SrhoUa || SrhoEa) {
         ProfScope ps(c, KID_ADJ_MISC, s);
-        k_split5<R><<<nbC, BLOCK, 0, s>>>(m.nIC, sb, Srhoa, SrhoUa, SrhoEa);
+        k_split5<S><<<nbC, BLOCK, 0, s>>>(m.nIC, sb, Srhoa, SrhoUa, SrhoEa);
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(c, e, "adjoint step launch");
     return AFVM_OK;
 }
 
-template int adjoint_step_dev<double>(Ctx*, const double*, const double*, const double*, double, const double*,
-                                      const double*, const double*, const double*, const double*, const double*,
-                                      double, double*, double*, double*, double*, double*, double*, cudaStream_t,
-                                      const double*);
-template int adjoint_step_dev<float>(Ctx*, const float*, const float*, const float*, double, const float*,
-                                     const float*, const float*, const float*, const float*, const float*, double,
-                                     float*, float*, float*, float*, float*, float*, cudaStream_t, const float*);
+#define AFVM_ADJ_INST(R, S)                                                                                    \
+    template int adjoint_step_dev<R, S>(Ctx*, const S*, const S*, const S*, double, const S*, const S*, const S*, \
+                                        const S*, const S*, const S*, double, S*, S*, S*, S*, S*, S*,             \
+                                        cudaStream_t, const S*);
+AFVM_ADJ_INST(double, double)
+AFVM_ADJ_INST(float, float)
+AFVM_ADJ_INST(float, double)
 
 }  // namespace afvm

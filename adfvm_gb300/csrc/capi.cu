@@ -352,7 +352,9 @@ int build_tables(Ctx* c, const afvm_mesh_tensors* M, const afvm_patch_bc* bcs, H
     return AFVM_OK;
 }
 
-template <typename R>
+// R: element type of the mesh tables, cell records and face fluxes; S: element type of the
+// conservative state, its RK stages, sources and adjoints
+template <typename R, typename S>
 int alloc_work(Ctx* c) {
     int st;
     if ((st = dalloc(c, &c->rec, sizeof(R) * (size_t)c->nC * REC))) return st;
@@ -360,11 +362,11 @@ int alloc_work(Ctx* c) {
     size_t n = c->nIC;
     size_t dims[3] = {1, 3, 1};
     for (int k = 0; k < 3; k++) {
-        if ((st = dalloc(c, &c->u1[k], sizeof(R) * n * dims[k]))) return st;
-        if ((st = dalloc(c, &c->u2[k], sizeof(R) * n * dims[k]))) return st;
+        if ((st = dalloc(c, &c->u1[k], sizeof(S) * n * dims[k]))) return st;
+        if ((st = dalloc(c, &c->u2[k], sizeof(S) * n * dims[k]))) return st;
     }
-    if ((st = dalloc(c, &c->zeroS, sizeof(R) * n * 5))) return st;
-    cudaMemset(c->zeroS, 0, sizeof(R) * n * 5);
+    if ((st = dalloc(c, &c->zeroS, sizeof(S) * n * 5))) return st;
+    cudaMemset(c->zeroS, 0, sizeof(S) * n * 5);
     int np = (int)((std::max(c->nIC, c->nF) + BLOCK - 1) / BLOCK);
     c->nPartials = np;
     if ((st = dalloc(c, (void**)&c->partials, sizeof(double) * (size_t)np))) return st;
@@ -374,7 +376,7 @@ int alloc_work(Ctx* c) {
     return AFVM_OK;
 }
 
-template <typename R>
+template <typename R, typename S>
 int alloc_adjoint(Ctx* c) {
     if (c->fadj) return AFVM_OK;
     int64_t before = c->bytes;
@@ -384,10 +386,10 @@ int alloc_adjoint(Ctx* c) {
     if ((st = dalloc(c, &c->cbar, sizeof(R) * n * 20))) return st;
     size_t dims[3] = {1, 3, 1};
     for (int k = 0; k < 3; k++) {
-        if ((st = dalloc(c, &c->a1[k], sizeof(R) * n * dims[k]))) return st;
-        if ((st = dalloc(c, &c->a2[k], sizeof(R) * n * dims[k]))) return st;
+        if ((st = dalloc(c, &c->a1[k], sizeof(S) * n * dims[k]))) return st;
+        if ((st = dalloc(c, &c->a2[k], sizeof(S) * n * dims[k]))) return st;
     }
-    if ((st = dalloc(c, &c->sbar, sizeof(R) * n * 5))) return st;
+    if ((st = dalloc(c, &c->sbar, sizeof(S) * n * 5))) return st;
     c->adjBytes = c->bytes - before;
     c->bytes = before;
     return AFVM_OK;
@@ -421,6 +423,18 @@ struct DeviceGuard {
     }
 };
 
+// calls f(R{}, S{}) with the element types of the context's precision mode
+template <typename F>
+int dispatch(const Ctx* c, F&& f) {
+    if (c->precision == AFVM_FP64) return f(double{}, double{});
+    if (c->precision == AFVM_FP32) return f(float{}, float{});
+    return f(float{}, double{});
+}
+
+// bytes of one state value (S) and of one mesh/record value (R)
+inline size_t state_size(const Ctx* c) { return c->precision == AFVM_FP32 ? sizeof(float) : sizeof(double); }
+inline size_t record_size(const Ctx* c) { return c->precision == AFVM_FP64 ? sizeof(double) : sizeof(float); }
+
 int get_results(Ctx* c, double* dtc_out, double* obj_out, cudaStream_t s) {
     if (!dtc_out && !obj_out) return AFVM_OK;
     double tmp[2];
@@ -446,7 +460,7 @@ int afvm_ctx_create(const afvm_mesh_tensors* mesh, const afvm_patch_bc* bcs, con
     if (!out) return AFVM_ERR_BAD_ARG;
     *out = nullptr;
     if (!mesh || !phys || (mesh->nPatches > 0 && (!bcs || !mesh->patches))) return AFVM_ERR_BAD_ARG;
-    if (precision != AFVM_FP64 && precision != AFVM_FP32) return AFVM_ERR_BAD_ARG;
+    if (precision != AFVM_FP64 && precision != AFVM_FP32 && precision != AFVM_FP32_STATE64) return AFVM_ERR_BAD_ARG;
     if (phys->riemann != AFVM_RIEMANN_ROE && phys->riemann != AFVM_RIEMANN_LF) return AFVM_ERR_BAD_ARG;
     if (phys->boundary_riemann != AFVM_RIEMANN_ROE && phys->boundary_riemann != AFVM_RIEMANN_LF)
         return AFVM_ERR_BAD_ARG;
@@ -482,7 +496,8 @@ int afvm_ctx_create(const afvm_mesh_tensors* mesh, const afvm_patch_bc* bcs, con
     HostTables h;
     int st = build_tables(c, mesh, bcs, h);
     if (!st) st = (precision == AFVM_FP64) ? upload_mesh<double>(c, h, c->m64) : upload_mesh<float>(c, h, c->m32);
-    if (!st) st = (precision == AFVM_FP64) ? alloc_work<double>(c) : alloc_work<float>(c);
+    if (!st)
+        st = dispatch(c, [&](auto r, auto sv) { return alloc_work<decltype(r), decltype(sv)>(c); });
     if (!st) {
         cudaError_t e = cudaDeviceSynchronize();
         if (e != cudaSuccess) st = cuda_fail(c, e, "context set-up");
@@ -672,17 +687,13 @@ int afvm_primal_step_stages(afvm_ctx* ctx, const void* rho, const void* rhoU, co
     if (!std::isfinite(dt)) return fail(c, AFVM_ERR_BAD_ARG, "non-finite dt");
     DeviceGuard dg(c->device);
     cudaStream_t s = (cudaStream_t)stream;
-    int st;
-    if (c->precision == AFVM_FP64)
-        st = primal_step_dev<double>(c, (const double*)rho, (const double*)rhoU, (const double*)rhoE, dt, nullptr,
-                                     (const double*)S_rho, (const double*)S_rhoU, (const double*)S_rhoE,
-                                     (double*)rhoN, (double*)rhoUN, (double*)rhoEN, c->scal, c->scal + 1, s,
-                                     (double*)stages);
-    else
-        st = primal_step_dev<float>(c, (const float*)rho, (const float*)rhoU, (const float*)rhoE, dt, nullptr,
-                                    (const float*)S_rho, (const float*)S_rhoU, (const float*)S_rhoE,
-                                    (float*)rhoN, (float*)rhoUN, (float*)rhoEN, c->scal, c->scal + 1, s,
-                                    (float*)stages);
+    int st = dispatch(c, [&](auto r, auto sv) {
+        using R = decltype(r);
+        using S = decltype(sv);
+        return primal_step_dev<R, S>(c, (const S*)rho, (const S*)rhoU, (const S*)rhoE, dt, nullptr, (const S*)S_rho,
+                                     (const S*)S_rhoU, (const S*)S_rhoE, (S*)rhoN, (S*)rhoUN, (S*)rhoEN, c->scal,
+                                     c->scal + 1, s, (S*)stages);
+    });
     if (st) return st;
     return get_results(c, dtc_out, obj_out, s);
 }
@@ -702,7 +713,7 @@ int afvm_primal_step_host(afvm_ctx* ctx, const void* rho, const void* rhoU, cons
     if (!rho || !rhoU || !rhoE || !rhoN || !rhoUN || !rhoEN) return fail(c, AFVM_ERR_BAD_ARG, "null state pointer");
     DeviceGuard dg(c->device);
     cudaStream_t s = (cudaStream_t)stream;
-    size_t es = c->precision == AFVM_FP64 ? sizeof(double) : sizeof(float);
+    size_t es = state_size(c);
     size_t n = c->nIC;
     // device staging, allocated on first use: state in (5n), state out (5n), sources (5n)
     if (!c->stageDev) {
@@ -756,13 +767,13 @@ int afvm_primal_run(afvm_ctx* ctx, void* rho, void* rhoU, void* rhoE, int32_t nS
     if (!rho || !rhoU || !rhoE || nSteps < 0) return fail(c, AFVM_ERR_BAD_ARG, "afvm_primal_run arguments");
     DeviceGuard dg(c->device);
     cudaStream_t s = (cudaStream_t)stream;
-    if (c->precision == AFVM_FP64)
-        return primal_run_dev<double>(c, (double*)rho, (double*)rhoU, (double*)rhoE, nSteps, dt0, CFL, stepFactor,
-                                      fixed_dt, (const double*)S_rho, (const double*)S_rhoU, (const double*)S_rhoE,
-                                      dt_hist, dtc_hist, obj_hist, s);
-    return primal_run_dev<float>(c, (float*)rho, (float*)rhoU, (float*)rhoE, nSteps, dt0, CFL, stepFactor, fixed_dt,
-                                 (const float*)S_rho, (const float*)S_rhoU, (const float*)S_rhoE, dt_hist, dtc_hist,
-                                 obj_hist, s);
+    return dispatch(c, [&](auto r, auto sv) {
+        using R = decltype(r);
+        using S = decltype(sv);
+        return primal_run_dev<R, S>(c, (S*)rho, (S*)rhoU, (S*)rhoE, nSteps, dt0, CFL, stepFactor, fixed_dt,
+                                    (const S*)S_rho, (const S*)S_rhoU, (const S*)S_rhoE, dt_hist, dtc_hist, obj_hist,
+                                    s);
+    });
 }
 
 int afvm_adjoint_step_stages(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, double dt,
@@ -778,19 +789,16 @@ int afvm_adjoint_step_stages(afvm_ctx* ctx, const void* rho, const void* rhoU, c
     if (!std::isfinite(dt) || !std::isfinite(obja)) return fail(c, AFVM_ERR_BAD_ARG, "non-finite dt or obja");
     DeviceGuard dg(c->device);
     cudaStream_t s = (cudaStream_t)stream;
-    int st = (c->precision == AFVM_FP64) ? alloc_adjoint<double>(c) : alloc_adjoint<float>(c);
-    if (st) return st;
-    if (c->precision == AFVM_FP64)
-        return adjoint_step_dev<double>(c, (const double*)rho, (const double*)rhoU, (const double*)rhoE, dt,
-                                        (const double*)S_rho, (const double*)S_rhoU, (const double*)S_rhoE,
-                                        (const double*)rhoNa, (const double*)rhoUNa, (const double*)rhoENa, obja,
-                                        (double*)rhoa, (double*)rhoUa, (double*)rhoEa, (double*)S_rhoa,
-                                        (double*)S_rhoUa, (double*)S_rhoEa, s, (const double*)stages);
-    return adjoint_step_dev<float>(c, (const float*)rho, (const float*)rhoU, (const float*)rhoE, dt,
-                                   (const float*)S_rho, (const float*)S_rhoU, (const float*)S_rhoE,
-                                   (const float*)rhoNa, (const float*)rhoUNa, (const float*)rhoENa, obja,
-                                   (float*)rhoa, (float*)rhoUa, (float*)rhoEa, (float*)S_rhoa, (float*)S_rhoUa,
-                                   (float*)S_rhoEa, s, (const float*)stages);
+    return dispatch(c, [&](auto r, auto sv) {
+        using R = decltype(r);
+        using S = decltype(sv);
+        int st = alloc_adjoint<R, S>(c);
+        if (st) return st;
+        return adjoint_step_dev<R, S>(c, (const S*)rho, (const S*)rhoU, (const S*)rhoE, dt, (const S*)S_rho,
+                                      (const S*)S_rhoU, (const S*)S_rhoE, (const S*)rhoNa, (const S*)rhoUNa,
+                                      (const S*)rhoENa, obja, (S*)rhoa, (S*)rhoUa, (S*)rhoEa, (S*)S_rhoa,
+                                      (S*)S_rhoUa, (S*)S_rhoEa, s, (const S*)stages);
+    });
 }
 
 int afvm_adjoint_step(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, double dt,
@@ -811,15 +819,13 @@ int afvm_adjoint_viscosity(afvm_ctx* ctx, const void* rho, const void* rhoU, con
     if (!std::isfinite(scaling) || !std::isfinite(dt) || dt < 0) return fail(c, AFVM_ERR_BAD_ARG, "scaling or dt");
     DeviceGuard dg(c->device);
     cudaStream_t s = (cudaStream_t)stream;
-    int it = 0, st;
-    if (c->precision == AFVM_FP64)
-        st = adjoint_viscosity_dev<double>(c, (const double*)rho, (const double*)rhoU, (const double*)rhoE, kind,
-                                           scaling, dt, (double*)rhoa, (double*)rhoUa, (double*)rhoEa, M_out, DT_out,
-                                           &it, s);
-    else
-        st = adjoint_viscosity_dev<float>(c, (const float*)rho, (const float*)rhoU, (const float*)rhoE, kind,
-                                          scaling, dt, (float*)rhoa, (float*)rhoUa, (float*)rhoEa, M_out, DT_out,
-                                          &it, s);
+    int it = 0;
+    int st = dispatch(c, [&](auto r, auto sv) {
+        using R = decltype(r);
+        using S = decltype(sv);
+        return adjoint_viscosity_dev<R, S>(c, (const S*)rho, (const S*)rhoU, (const S*)rhoE, kind, scaling, dt,
+                                           (S*)rhoa, (S*)rhoUa, (S*)rhoEa, M_out, DT_out, &it, s);
+    });
     if (iterations_out) *iterations_out = it;
     return st;
 }
@@ -832,11 +838,13 @@ int afvm_boundary_values(afvm_ctx* ctx, const void* rho, const void* rhoU, const
     DeviceGuard dg(c->device);
     cudaStream_t s = (cudaStream_t)stream;
     if (c->nG == 0) return AFVM_OK;
-    size_t es = c->precision == AFVM_FP64 ? sizeof(double) : sizeof(float);
-    if (c->precision == AFVM_FP64)
-        launch_prim<double>(c, (const double*)rho, (const double*)rhoU, (const double*)rhoE, s);
-    else
-        launch_prim<float>(c, (const float*)rho, (const float*)rhoU, (const float*)rhoE, s);
+    size_t es = record_size(c);
+    dispatch(c, [&](auto r, auto sv) {
+        using R = decltype(r);
+        using S = decltype(sv);
+        launch_prim<R, S>(c, (const S*)rho, (const S*)rhoU, (const S*)rhoE, s);
+        return 0;
+    });
     // ghost rows of the cell record, columns U, T, p
     const char* src = (const char*)c->rec + es * REC * (size_t)c->nIC;
     cudaError_t e = cudaMemcpy2DAsync(out, es * 5, src, es * REC, es * 5, (size_t)c->nG, cudaMemcpyDeviceToDevice, s);

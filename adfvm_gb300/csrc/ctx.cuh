@@ -150,28 +150,29 @@ int fail(Ctx* c, int code, const std::string& msg);
 int cuda_fail(Ctx* c, cudaError_t e, const char* what);
 // device allocation owned by the context (freed by afvm_ctx_destroy)
 int ctx_alloc(Ctx* c, void** p, size_t bytes);
-template <typename R>
-int adjoint_viscosity_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, int kind, double scaling, double dt,
-                          R* ar, R* au, R* ae, double* Mout, double* DTout, int* iters, cudaStream_t s);
+template <typename R, typename S = R>
+int adjoint_viscosity_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, int kind, double scaling, double dt,
+                          S* ar, S* au, S* ae, double* Mout, double* DTout, int* iters, cudaStream_t s);
 
-// kernel launchers (primal.cu)
-// dt: by value, or read on the device from dtDev when that is non-NULL
-template <typename R>
-int primal_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double dt, const double* dtDev,
-                    const R* Srho, const R* SrhoU, const R* SrhoE, R* rhoN, R* rhoUN, R* rhoEN,
-                    double* dtcDev, double* objDev, cudaStream_t s, R* stages = nullptr);
-template <typename R>
-int primal_run_dev(Ctx* c, R* rho, R* rhoU, R* rhoE, int nSteps, double dt0, double CFL, double stepFactor,
-                   int fixed, const R* Srho, const R* SrhoU, const R* SrhoE, double* dtHist, double* dtcHist,
+// kernel launchers (primal.cu). R: the record/flux type (double or float); S: the state type
+// (R, or double under FP32 fluxes with an FP64 state). dt: by value, or read on the device from
+// dtDev when that is non-NULL
+template <typename R, typename S = R>
+int primal_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double dt, const double* dtDev,
+                    const S* Srho, const S* SrhoU, const S* SrhoE, S* rhoN, S* rhoUN, S* rhoEN,
+                    double* dtcDev, double* objDev, cudaStream_t s, S* stages = nullptr);
+template <typename R, typename S = R>
+int primal_run_dev(Ctx* c, S* rho, S* rhoU, S* rhoE, int nSteps, double dt0, double CFL, double stepFactor,
+                   int fixed, const S* Srho, const S* SrhoU, const S* SrhoE, double* dtHist, double* dtcHist,
                    double* objHist, cudaStream_t s);
 int sensitivity_dev(Ctx* c, int nArrays, const double* const* grad, const double* const* pert,
                     const int64_t* n, double* out, cudaStream_t s);
-template <typename R>
-int adjoint_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double dt,
-                     const R* Srho, const R* SrhoU, const R* SrhoE,
-                     const R* rhoNa, const R* rhoUNa, const R* rhoENa, double obja,
-                     R* rhoa, R* rhoUa, R* rhoEa, R* Srhoa, R* SrhoUa, R* SrhoEa, cudaStream_t s,
-                     const R* stages = nullptr);
+template <typename R, typename S = R>
+int adjoint_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double dt,
+                     const S* Srho, const S* SrhoU, const S* SrhoE,
+                     const S* rhoNa, const S* rhoUNa, const S* rhoENa, double obja,
+                     S* rhoa, S* rhoUa, S* rhoEa, S* Srhoa, S* SrhoUa, S* SrhoEa, cudaStream_t s,
+                     const S* stages = nullptr);
 
 // the RK stage states u1, u2 of one step in a caller's buffer of 10 nIC values:
 // u1 = [rho (n) | rhoU (3n) | rhoE (n)], then u2 in the same layout
@@ -184,15 +185,15 @@ inline void stage_views(P* stages, int n, P** u1, P** u2) {
 // turbine-vane objective partial sums of the stage-1 record now in c->rec into c->vaneSums
 template <typename R>
 void launch_vane_sums(Ctx* c, cudaStream_t s, double* dtcOut, double* objOut);
-template <typename R>
-void launch_prim(Ctx* c, const R* r, const R* ru, const R* re, cudaStream_t s);
-template <typename R>
-void launch_prim_grad(Ctx* c, const R* r, const R* ru, const R* re, cudaStream_t s);
-template <typename R>
-void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const R* const* u0, const R* const* u1,
-                        const R* const* u2, const R* Sr, const R* Su, const R* Se, R* const* out, cudaStream_t s);
-template <typename R>
-void default_sources(Ctx* c, const R*& Srho, const R*& SrhoU, const R*& SrhoE);
+template <typename R, typename S = R>
+void launch_prim(Ctx* c, const S* r, const S* ru, const S* re, cudaStream_t s);
+template <typename R, typename S = R>
+void launch_prim_grad(Ctx* c, const S* r, const S* ru, const S* re, cudaStream_t s);
+template <typename R, typename S = R>
+void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const S* const* u0, const S* const* u1,
+                        const S* const* u2, const S* Sr, const S* Su, const S* Se, S* const* out, cudaStream_t s);
+template <typename S>
+void default_sources(Ctx* c, const S*& Srho, const S*& SrhoU, const S*& SrhoE);
 static inline int nblocks(long long n) { return (int)((n + BLOCK - 1) / BLOCK); }
 
 template <typename R> inline const MeshDev<R>& meshOf(const Ctx* c);

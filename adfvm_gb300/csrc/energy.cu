@@ -19,11 +19,11 @@ __device__ __forceinline__ double e_block_sum(double v, double* sh) {
     return r;
 }
 
-template <typename R>
-__global__ void __launch_bounds__(BLOCK) k_energy(MeshDev<R> m, double g, const R* __restrict__ ra,
-                                                  const R* __restrict__ rua, const R* __restrict__ rea,
-                                                  const R* __restrict__ r, const R* __restrict__ ru,
-                                                  const R* __restrict__ re, double* partials) {
+template <typename R, typename S>
+__global__ void __launch_bounds__(BLOCK) k_energy(MeshDev<R> m, double g, const S* __restrict__ ra,
+                                                  const S* __restrict__ rua, const S* __restrict__ rea,
+                                                  const S* __restrict__ r, const S* __restrict__ ru,
+                                                  const S* __restrict__ re, double* partials) {
     __shared__ double sh[BLOCK / 32];
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     double e = 0.0;
@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(BLOCK) k_energy_finish(const double* __restric
     if (threadIdx.x == 0) *out = s;
 }
 
-template <typename R>
+template <typename R, typename S>
 int energy_dev(Ctx* c, const void* ra, const void* rua, const void* rea, const void* r, const void* ru,
                const void* re, double* out, cudaStream_t s) {
     const MeshDev<R>& m = meshOf<R>(c);
@@ -64,8 +64,8 @@ int energy_dev(Ctx* c, const void* ra, const void* rua, const void* rea, const v
     if (nb > c->nPartials) return fail(c, AFVM_ERR_BAD_ARG, "energy partials overflow");
     {
         ProfScope ps(c, KID_ADJ_MISC, s);
-        k_energy<R><<<nb, BLOCK, 0, s>>>(m, c->phys.gamma, (const R*)ra, (const R*)rua, (const R*)rea, (const R*)r,
-                                         (const R*)ru, (const R*)re, c->partials);
+        k_energy<R, S><<<nb, BLOCK, 0, s>>>(m, c->phys.gamma, (const S*)ra, (const S*)rua, (const S*)rea,
+                                            (const S*)r, (const S*)ru, (const S*)re, c->partials);
         k_energy_finish<<<1, BLOCK, 0, s>>>(c->partials, nb, c->scal + 4);
     }
     cudaError_t e = cudaMemcpyAsync(out, c->scal + 4, sizeof(double), cudaMemcpyDeviceToHost, s);
@@ -87,8 +87,10 @@ extern "C" int afvm_adjoint_energy(afvm_ctx* ctx, const void* rhoa, const void* 
     cudaGetDevice(&prev);
     if (prev != c->device) cudaSetDevice(c->device);
     int st = (c->precision == AFVM_FP64)
-                 ? energy_dev<double>(c, rhoa, rhoUa, rhoEa, rho, rhoU, rhoE, out, (cudaStream_t)stream)
-                 : energy_dev<float>(c, rhoa, rhoUa, rhoEa, rho, rhoU, rhoE, out, (cudaStream_t)stream);
+                 ? energy_dev<double, double>(c, rhoa, rhoUa, rhoEa, rho, rhoU, rhoE, out, (cudaStream_t)stream)
+                 : (c->precision == AFVM_FP32)
+                       ? energy_dev<float, float>(c, rhoa, rhoUa, rhoEa, rho, rhoU, rhoE, out, (cudaStream_t)stream)
+                       : energy_dev<float, double>(c, rhoa, rhoUa, rhoEa, rho, rhoU, rhoE, out, (cudaStream_t)stream);
     if (prev >= 0 && prev != c->device) cudaSetDevice(prev);
     return st;
 }

@@ -43,29 +43,39 @@ __device__ __noinline__ void primitive_f(const Phys& P, float rho, float r0, flo
     out[3] = (float)(rhoe * (double)rr * P.rCv);
 }
 
-template <typename R>
-__device__ __forceinline__ void load_prim(const Phys& P, const R* rho, const R* rhoU, const R* rhoE, int c, R* out);
+// primitives of cell c from the state (element type S) into the record type R
+template <typename R, typename S>
+__device__ __forceinline__ void load_prim(const Phys& P, const S* rho, const S* rhoU, const S* rhoE, int c, R* out);
 
 template <>
-__device__ __forceinline__ void load_prim<double>(const Phys& P, const double* rho, const double* rhoU,
-                                                  const double* rhoE, int c, double* out) {
+__device__ __forceinline__ void load_prim<double, double>(const Phys& P, const double* rho, const double* rhoU,
+                                                          const double* rhoE, int c, double* out) {
     primitive_d(P, rho[c], rhoU[3 * c], rhoU[3 * c + 1], rhoU[3 * c + 2], rhoE[c], out);
 }
 
 template <>
-__device__ __forceinline__ void load_prim<float>(const Phys& P, const float* rho, const float* rhoU,
-                                                 const float* rhoE, int c, float* out) {
+__device__ __forceinline__ void load_prim<float, float>(const Phys& P, const float* rho, const float* rhoU,
+                                                        const float* rhoE, int c, float* out) {
     primitive_f(P, rho[c], rhoU[3 * c], rhoU[3 * c + 1], rhoU[3 * c + 2], rhoE[c], out);
 }
 
-template <typename R>
-__global__ void __launch_bounds__(BLOCK) k_prim(MeshDev<R> m, Phys P, const R* __restrict__ rho,
-                                                const R* __restrict__ rhoU, const R* __restrict__ rhoE,
+// FP64 state, FP32 record: the primitives in double, then rounded once
+template <>
+__device__ __forceinline__ void load_prim<float, double>(const Phys& P, const double* rho, const double* rhoU,
+                                                         const double* rhoE, int c, float* out) {
+    double v[5];
+    primitive_d(P, rho[c], rhoU[3 * c], rhoU[3 * c + 1], rhoU[3 * c + 2], rhoE[c], v);
+    for (int k = 0; k < 5; k++) out[k] = (float)v[k];
+}
+
+template <typename R, typename S>
+__global__ void __launch_bounds__(BLOCK) k_prim(MeshDev<R> m, Phys P, const S* __restrict__ rho,
+                                                const S* __restrict__ rhoU, const S* __restrict__ rhoE,
                                                 R* __restrict__ rec) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < m.nIC) {
         R v[5];
-        load_prim<R>(P, rho, rhoU, rhoE, t, v);
+        load_prim<R, S>(P, rho, rhoU, rhoE, t, v);
         R* r = rec + (size_t)t * REC;
         for (int k = 0; k < 5; k++) r[k] = v[k];
         return;
@@ -75,7 +85,7 @@ __global__ void __launch_bounds__(BLOCK) k_prim(MeshDev<R> m, Phys P, const R* _
     int src = m.gsrc[g];
     int kind = m.gkind[g];
     R v[5];
-    load_prim<R>(P, rho, rhoU, rhoE, src, v);
+    load_prim<R, S>(P, rho, rhoU, rhoE, src, v);
     int kU = kind & 7, kT = (kind >> 3) & 7, kp = (kind >> 6) & 7;
     if (kU == GK_TOTALPT) {
         // CBC_TOTAL_PT (BCs.py:178-184): Un = U.d, Ub = Un d, Tb = Tt - Un^2/(2 Cp),
@@ -149,21 +159,23 @@ __global__ void __launch_bounds__(FLUX_BLOCK, sizeof(R) == 8 ? 3 : 8) k_flux(Mes
 
 // Gather of the face fluxes (op.div / op.absDiv, op.py:12-29, collated in the order of
 // density.py:390-402) and the SSP-RK3 stage update (timestep.py:35-45).
-template <typename R, int STAGE>
+template <typename R, typename S, int STAGE>
 __global__ void __launch_bounds__(BLOCK) k_update(MeshDev<R> m, const R* __restrict__ fflux, double dtv,
                                                   const double* dtp,
-                                                  const R* u0r, const R* u0u, const R* u0e,
-                                                  const R* u1r, const R* u1u, const R* u1e,
-                                                  const R* u2r, const R* u2u, const R* u2e,
-                                                  const R* __restrict__ Sr, const R* __restrict__ Su,
-                                                  const R* __restrict__ Se,
-                                                  R* outr, R* outu, R* oute,
+                                                  const S* u0r, const S* u0u, const S* u0e,
+                                                  const S* u1r, const S* u1u, const S* u1e,
+                                                  const S* u2r, const S* u2u, const S* u2e,
+                                                  const S* __restrict__ Sr, const S* __restrict__ Su,
+                                                  const S* __restrict__ Se,
+                                                  S* outr, S* outu, S* oute,
                                                   unsigned long long* dtcBits) {
+    // the gather and the update run in the state's type S (double for an FP64 state under
+    // FP32 fluxes); the CFL sum in the flux type R
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     R dtc = R(0);
     if (c < m.nIC) {
         const size_t n = m.nIC;
-        R res[5] = {R(0), R(0), R(0), R(0), R(0)};
+        S res[5] = {S(0), S(0), S(0), S(0), S(0)};
 #pragma unroll
         for (int k = 0; k < 6; k++) {
             int e = m.accf[k * n + c];
@@ -172,25 +184,25 @@ __global__ void __launch_bounds__(BLOCK) k_update(MeshDev<R> m, const R* __restr
             int f = ownerSide ? e : ~e;
             const R* F = fflux + (size_t)f * FREC;
             for (int q = 0; q < 5; q++) {
-                R t = F[q] * w;
+                S t = (S)F[q] * (S)w;
                 res[q] = res[q] + (ownerSide ? t : -t);
             }
             dtc = dtc + F[5] * w;
         }
-        R S[5] = {Sr[c], Su[3 * c], Su[3 * c + 1], Su[3 * c + 2], Se[c]};
-        R a[5] = {u0r[c], u0u[3 * c], u0u[3 * c + 1], u0u[3 * c + 2], u0e[c]};
-        R o[5];
-        const R rdt = R(dtp ? *dtp : dtv);
+        S Sv[5] = {Sr[c], Su[3 * c], Su[3 * c + 1], Su[3 * c + 2], Se[c]};
+        S a[5] = {u0r[c], u0u[3 * c], u0u[3 * c + 1], u0u[3 * c + 2], u0e[c]};
+        S o[5];
+        const S rdt = S(dtp ? *dtp : dtv);
         if (STAGE == 0) {
-            for (int q = 0; q < 5; q++) o[q] = a[q] + (R(-1.0) * (res[q] - S[q])) * rdt;
+            for (int q = 0; q < 5; q++) o[q] = a[q] + (S(-1.0) * (res[q] - Sv[q])) * rdt;
         } else if (STAGE == 1) {
-            R b[5] = {u1r[c], u1u[3 * c], u1u[3 * c + 1], u1u[3 * c + 2], u1e[c]};
+            S b[5] = {u1r[c], u1u[3 * c], u1u[3 * c + 1], u1u[3 * c + 2], u1e[c]};
             for (int q = 0; q < 5; q++)
-                o[q] = (R(3. / 4) * a[q] + R(1. / 4) * b[q]) + (R(-(1. / 4)) * (res[q] - S[q])) * rdt;
+                o[q] = (S(3. / 4) * a[q] + S(1. / 4) * b[q]) + (S(-(1. / 4)) * (res[q] - Sv[q])) * rdt;
         } else {
-            R b[5] = {u2r[c], u2u[3 * c], u2u[3 * c + 1], u2u[3 * c + 2], u2e[c]};
+            S b[5] = {u2r[c], u2u[3 * c], u2u[3 * c + 1], u2u[3 * c + 2], u2e[c]};
             for (int q = 0; q < 5; q++)
-                o[q] = (R(1. / 3) * a[q] + R(2. / 3) * b[q]) + (R(-(2. / 3)) * (res[q] - S[q])) * rdt;
+                o[q] = (S(1. / 3) * a[q] + S(2. / 3) * b[q]) + (S(-(2. / 3)) * (res[q] - Sv[q])) * rdt;
         }
         outr[c] = o[0];
         outu[3 * c] = o[1]; outu[3 * c + 1] = o[2]; outu[3 * c + 2] = o[3];
@@ -331,18 +343,18 @@ __global__ void k_finish(const double* partials, int nPartials, const unsigned l
 }
 
 
-template <typename R>
-void launch_prim(Ctx* c, const R* r, const R* ru, const R* re, cudaStream_t s) {
+template <typename R, typename S>
+void launch_prim(Ctx* c, const S* r, const S* ru, const S* re, cudaStream_t s) {
     const MeshDev<R>& m = meshOf<R>(c);
     ProfScope ps(c, KID_PRIM, s);
-    k_prim<R><<<nblocks(m.nIC + m.nG), BLOCK, 0, s>>>(m, c->phys, r, ru, re, (R*)c->rec);
+    k_prim<R, S><<<nblocks(m.nIC + m.nG), BLOCK, 0, s>>>(m, c->phys, r, ru, re, (R*)c->rec);
 }
 
-template <typename R>
-void launch_prim_grad(Ctx* c, const R* r, const R* ru, const R* re, cudaStream_t s) {
+template <typename R, typename S>
+void launch_prim_grad(Ctx* c, const S* r, const S* ru, const S* re, cudaStream_t s) {
     const MeshDev<R>& m = meshOf<R>(c);
     R* rec = (R*)c->rec;
-    launch_prim<R>(c, r, ru, re, s);
+    launch_prim<R, S>(c, r, ru, re, s);
     {
         ProfScope ps(c, KID_GRAD, s);
         k_grad<R><<<nblocks(m.nIC), BLOCK, 0, s>>>(m, rec);
@@ -350,9 +362,9 @@ void launch_prim_grad(Ctx* c, const R* r, const R* ru, const R* re, cudaStream_t
 }
 
 // faces -> fluxes, then the gather + stage update u_{st+1} = ... (timestep.py:35-45)
-template <typename R>
-void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const R* const* u0, const R* const* u1,
-                        const R* const* u2, const R* Sr, const R* Su, const R* Se, R* const* out, cudaStream_t s) {
+template <typename R, typename S>
+void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const S* const* u0, const S* const* u1,
+                        const S* const* u2, const S* Sr, const S* Su, const S* Se, S* const* out, cudaStream_t s) {
     const MeshDev<R>& m = meshOf<R>(c);
     const Phys& P = c->phys;
     R* rec = (R*)c->rec;
@@ -365,46 +377,46 @@ void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const R*
     int nb = nblocks(m.nIC);
     ProfScope ps(c, KID_UPDATE, s);
     if (st == 0)
-        k_update<R, 0><<<nb, BLOCK, 0, s>>>(m, ff, dt, dtDev, u0[0], u0[1], u0[2], nullptr, nullptr, nullptr, nullptr,
+        k_update<R, S, 0><<<nb, BLOCK, 0, s>>>(m, ff, dt, dtDev, u0[0], u0[1], u0[2], nullptr, nullptr, nullptr, nullptr,
                                             nullptr, nullptr, Sr, Su, Se, out[0], out[1], out[2], c->dtcBits);
     else if (st == 1)
-        k_update<R, 1><<<nb, BLOCK, 0, s>>>(m, ff, dt, dtDev, u0[0], u0[1], u0[2], u1[0], u1[1], u1[2], nullptr,
+        k_update<R, S, 1><<<nb, BLOCK, 0, s>>>(m, ff, dt, dtDev, u0[0], u0[1], u0[2], u1[0], u1[1], u1[2], nullptr,
                                             nullptr, nullptr, Sr, Su, Se, out[0], out[1], out[2], c->dtcBits);
     else
-        k_update<R, 2><<<nb, BLOCK, 0, s>>>(m, ff, dt, dtDev, u0[0], u0[1], u0[2], nullptr, nullptr, nullptr, u2[0],
+        k_update<R, S, 2><<<nb, BLOCK, 0, s>>>(m, ff, dt, dtDev, u0[0], u0[1], u0[2], nullptr, nullptr, nullptr, u2[0],
                                             u2[1], u2[2], Sr, Su, Se, out[0], out[1], out[2], c->dtcBits);
 }
 
-template <typename R>
-void default_sources(Ctx* c, const R*& Srho, const R*& SrhoU, const R*& SrhoE) {
-    const R* zs = (const R*)c->zeroS;
+template <typename S>
+void default_sources(Ctx* c, const S*& Srho, const S*& SrhoU, const S*& SrhoE) {
+    const S* zs = (const S*)c->zeroS;
     if (!Srho) Srho = zs;
     if (!SrhoU) SrhoU = zs + c->nIC;
     if (!SrhoE) SrhoE = zs + 4 * (size_t)c->nIC;
 }
 
-template <typename R>
-int primal_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double dt, const double* dtDev,
-                    const R* Srho, const R* SrhoU, const R* SrhoE, R* rhoN, R* rhoUN, R* rhoEN,
-                    double* dtcDev, double* objDev, cudaStream_t s, R* stages) {
+template <typename R, typename S>
+int primal_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double dt, const double* dtDev,
+                    const S* Srho, const S* SrhoU, const S* SrhoE, S* rhoN, S* rhoUN, S* rhoEN,
+                    double* dtcDev, double* objDev, cudaStream_t s, S* stages) {
     const MeshDev<R>& m = meshOf<R>(c);
     const Phys& P = c->phys;
-    default_sources<R>(c, Srho, SrhoU, SrhoE);
-    R* u1[3] = {(R*)c->u1[0], (R*)c->u1[1], (R*)c->u1[2]};
-    R* u2[3] = {(R*)c->u2[0], (R*)c->u2[1], (R*)c->u2[2]};
-    if (stages) stage_views<R, R>(stages, m.nIC, u1, u2);
-    R* outN[3] = {rhoN, rhoUN, rhoEN};
-    const R* u0c[3] = {rho, rhoU, rhoE};
-    const R* u1c[3] = {u1[0], u1[1], u1[2]};
-    const R* u2c[3] = {u2[0], u2[1], u2[2]};
+    default_sources<S>(c, Srho, SrhoU, SrhoE);
+    S* u1[3] = {(S*)c->u1[0], (S*)c->u1[1], (S*)c->u1[2]};
+    S* u2[3] = {(S*)c->u2[0], (S*)c->u2[1], (S*)c->u2[2]};
+    if (stages) stage_views<S, S>(stages, m.nIC, u1, u2);
+    S* outN[3] = {rhoN, rhoUN, rhoEN};
+    const S* u0c[3] = {rho, rhoU, rhoE};
+    const S* u1c[3] = {u1[0], u1[1], u1[2]};
+    const S* u2c[3] = {u2[0], u2[1], u2[2]};
     cudaMemsetAsync(c->dtcBits, 0, sizeof(unsigned long long), s);
     int nObjBlocks = 0;
     bool vaneDone = false;
     if (c->objective == AFVM_OBJ_VANE && !c->vaneSet)
         return fail(c, AFVM_ERR_BAD_ARG, "AFVM_OBJ_VANE needs afvm_set_objective_vane before the first step");
     for (int st = 0; st < 3; st++) {
-        const R* const* in = st == 0 ? u0c : (st == 1 ? u1c : u2c);
-        launch_prim_grad<R>(c, in[0], in[1], in[2], s);
+        const S* const* in = st == 0 ? u0c : (st == 1 ? u1c : u2c);
+        launch_prim_grad<R, S>(c, in[0], in[1], in[2], s);
         if (st == 1 && c->objective == AFVM_OBJ_VANE) {
             // the partial sums now, while rec holds the stage-1 primitives; combined at the end
             const MeshDev<R>& mm = meshOf<R>(c);
@@ -423,8 +435,8 @@ int primal_step_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, double d
                                                             c->partials);
             }
         }
-        R* const* out = st == 0 ? u1 : (st == 1 ? u2 : outN);
-        launch_flux_update<R>(c, st, dt, dtDev, u0c, u1c, u2c, Srho, SrhoU, SrhoE, out, s);
+        S* const* out = st == 0 ? u1 : (st == 1 ? u2 : outN);
+        launch_flux_update<R, S>(c, st, dt, dtDev, u0c, u1c, u2c, Srho, SrhoU, SrhoE, out, s);
     }
     if (vaneDone) {
         ProfScope ps(c, KID_FINISH, s);
@@ -447,15 +459,15 @@ __global__ void k_next_dt(double* dt, const double* dtc, double CFL, double step
     if (!fixed) *dt = fmin(2 * CFL / *dtc, d * stepFactor);
 }
 
-template <typename R>
-int primal_run_dev(Ctx* c, R* rho, R* rhoU, R* rhoE, int nSteps, double dt0, double CFL, double stepFactor,
-                   int fixed, const R* Srho, const R* SrhoU, const R* SrhoE, double* dtHist, double* dtcHist,
+template <typename R, typename S>
+int primal_run_dev(Ctx* c, S* rho, S* rhoU, S* rhoE, int nSteps, double dt0, double CFL, double stepFactor,
+                   int fixed, const S* Srho, const S* SrhoU, const S* SrhoE, double* dtHist, double* dtcHist,
                    double* objHist, cudaStream_t s) {
     double* dtDev = c->scal + 2;
     cudaMemcpyAsync(dtDev, &dt0, sizeof(double), cudaMemcpyHostToDevice, s);
     for (int n = 0; n < nSteps; n++) {
         double* dtcOut = dtcHist ? dtcHist + n : c->scal;
-        int st = primal_step_dev<R>(c, rho, rhoU, rhoE, 0.0, dtDev, Srho, SrhoU, SrhoE, rho, rhoU, rhoE, dtcOut,
+        int st = primal_step_dev<R, S>(c, rho, rhoU, rhoE, 0.0, dtDev, Srho, SrhoU, SrhoE, rho, rhoU, rhoE, dtcOut,
                                     objHist ? objHist + n : c->scal + 1, s);
         if (st != AFVM_OK) return st;
         k_next_dt<<<1, 1, 0, s>>>(dtDev, dtcOut, CFL, stepFactor, fixed, dtHist ? dtHist + n : nullptr);
@@ -465,30 +477,21 @@ int primal_run_dev(Ctx* c, R* rho, R* rhoU, R* rhoE, int nSteps, double dt0, dou
     return AFVM_OK;
 }
 
-template int primal_step_dev<double>(Ctx*, const double*, const double*, const double*, double, const double*,
-                                     const double*, const double*, const double*, double*, double*, double*,
-                                     double*, double*, cudaStream_t, double*);
-template int primal_step_dev<float>(Ctx*, const float*, const float*, const float*, double, const double*,
-                                    const float*, const float*, const float*, float*, float*, float*, double*,
-                                    double*, cudaStream_t, float*);
-template int primal_run_dev<double>(Ctx*, double*, double*, double*, int, double, double, double, int,
-                                    const double*, const double*, const double*, double*, double*, double*,
-                                    cudaStream_t);
-template int primal_run_dev<float>(Ctx*, float*, float*, float*, int, double, double, double, int, const float*,
-                                   const float*, const float*, double*, double*, double*, cudaStream_t);
-template void launch_vane_sums<double>(Ctx*, cudaStream_t, double*, double*);
-template void launch_vane_sums<float>(Ctx*, cudaStream_t, double*, double*);
-template void launch_prim<double>(Ctx*, const double*, const double*, const double*, cudaStream_t);
-template void launch_prim<float>(Ctx*, const float*, const float*, const float*, cudaStream_t);
-template void launch_prim_grad<double>(Ctx*, const double*, const double*, const double*, cudaStream_t);
-template void launch_prim_grad<float>(Ctx*, const float*, const float*, const float*, cudaStream_t);
-template void launch_flux_update<double>(Ctx*, int, double, const double*, const double* const*,
-                                         const double* const*, const double* const*, const double*, const double*,
-                                         const double*, double* const*, cudaStream_t);
-template void launch_flux_update<float>(Ctx*, int, double, const double*, const float* const*, const float* const*,
-                                        const float* const*, const float*, const float*, const float*,
-                                        float* const*, cudaStream_t);
+#define AFVM_PRIMAL_INST(R, S)                                                                                 \
+    template int primal_step_dev<R, S>(Ctx*, const S*, const S*, const S*, double, const double*, const S*,       \
+                                       const S*, const S*, S*, S*, S*, double*, double*, cudaStream_t, S*);       \
+    template int primal_run_dev<R, S>(Ctx*, S*, S*, S*, int, double, double, double, int, const S*, const S*,     \
+                                      const S*, double*, double*, double*, cudaStream_t);                         \
+    template void launch_prim<R, S>(Ctx*, const S*, const S*, const S*, cudaStream_t);                           \
+    template void launch_prim_grad<R, S>(Ctx*, const S*, const S*, const S*, cudaStream_t);                      \
+    template void launch_flux_update<R, S>(Ctx*, int, double, const double*, const S* const*, const S* const*,   \
+                                           const S* const*, const S*, const S*, const S*, S* const*, cudaStream_t);
+AFVM_PRIMAL_INST(double, double)
+AFVM_PRIMAL_INST(float, float)
+AFVM_PRIMAL_INST(float, double)
 template void default_sources<double>(Ctx*, const double*&, const double*&, const double*&);
 template void default_sources<float>(Ctx*, const float*&, const float*&, const float*&);
+template void launch_vane_sums<double>(Ctx*, cudaStream_t, double*, double*);
+template void launch_vane_sums<float>(Ctx*, cudaStream_t, double*, double*);
 
 }  // namespace afvm

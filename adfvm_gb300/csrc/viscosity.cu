@@ -347,8 +347,8 @@ __global__ void k_cg_shift(double* sc) {
     if (threadIdx.x < 5) sc[threadIdx.x] = sc[10 + threadIdx.x];
 }
 
-template <typename R>
-__global__ void k_heat_rhs(int n, const R* __restrict__ ar, const R* __restrict__ au, const R* __restrict__ ae,
+template <typename S>
+__global__ void k_heat_rhs(int n, const S* __restrict__ ar, const S* __restrict__ au, const S* __restrict__ ae,
                            double* __restrict__ rhs, double* __restrict__ partials, int nb) {
     __shared__ double sh[5][BLOCK / 32];
     int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -373,23 +373,23 @@ __global__ void k_heat_x0(MeshDev<R> m, const double* __restrict__ rhs, double* 
     for (int k = 0; k < 5; k++) x[k * n + c] = rhs[k * n + c] / V;
 }
 
-template <typename R>
-__global__ void k_heat_out(MeshDev<R> m, const double* __restrict__ x, R* __restrict__ ar, R* __restrict__ au,
-                           R* __restrict__ ae) {
+template <typename R, typename S>
+__global__ void k_heat_out(MeshDev<R> m, const double* __restrict__ x, S* __restrict__ ar, S* __restrict__ au,
+                           S* __restrict__ ae) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     const size_t n = m.nIC;
     if (c >= m.nIC) return;
     double V = m.vol[c];
-    ar[c] = (R)(x[c] * V);
-    for (int k = 0; k < 3; k++) au[3 * c + k] = (R)(x[(1 + k) * n + c] * V);
-    ae[c] = (R)(x[4 * n + c] * V);
+    ar[c] = (S)(x[c] * V);
+    for (int k = 0; k < 3; k++) au[3 * c + k] = (S)(x[(1 + k) * n + c] * V);
+    ae[c] = (S)(x[4 * n + c] * V);
 }
 
 }  // namespace
 
-template <typename R>
-int adjoint_viscosity_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, int kind, double scaling, double dt,
-                          R* ar, R* au, R* ae, double* Mout, double* DTout, int* iters, cudaStream_t s) {
+template <typename R, typename S>
+int adjoint_viscosity_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, int kind, double scaling, double dt,
+                          S* ar, S* au, S* ae, double* Mout, double* DTout, int* iters, cudaStream_t s) {
     const MeshDev<R>& m = meshOf<R>(c);
     const Phys& P = c->phys;
     const size_t n = c->nIC;
@@ -412,14 +412,14 @@ int adjoint_viscosity_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, in
     double* partials = diag + 5 * n;         // 15 x nb
     double* sc = partials + 15 * (size_t)nb; // 64 scalars
     ProfScope ps(c, KID_ADJ_VISC, s);
-    launch_prim<R>(c, rho, rhoU, rhoE, s);
+    launch_prim<R, S>(c, rho, rhoU, rhoE, s);
     k_visc_cell<R><<<nb, BLOCK, 0, s>>>(m, P, (const R*)c->rec, kind, M, partials);
     k_visc_norm<<<1, BLOCK, 0, s>>>(partials, nb, c->volTotal, scaling, sc + 40);
     k_visc_scale<R><<<nb, BLOCK, 0, s>>>(m, M, sc + 40);
     if (c->nG > 0) k_visc_ghost<R><<<nblocks(c->nG), BLOCK, 0, s>>>(m, M);
     k_visc_face<R><<<nblocks(c->nF), BLOCK, 0, s>>>(m, M, dt, DT, coef);
     // PCG on (V + dt L) x = a, from x0 = a / V (the unsmoothed field per unit volume)
-    k_heat_rhs<R><<<nb, BLOCK, 0, s>>>(c->nIC, ar, au, ae, rhs, partials, nb);
+    k_heat_rhs<S><<<nb, BLOCK, 0, s>>>(c->nIC, ar, au, ae, rhs, partials, nb);
     k_sum5<<<1, BLOCK, 0, s>>>(partials, nb, sc + 20);
     k_heat_x0<R><<<nb, BLOCK, 0, s>>>(m, rhs, x);
     k_heat_apply<R><<<nb, BLOCK, 0, s>>>(m, coef, x, r, diag, nullptr, nullptr, nb);
@@ -446,7 +446,7 @@ int adjoint_viscosity_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, in
         k_cg_shift<<<1, 32, 0, s>>>(sc);
     }
     if (iters) *iters = it;
-    k_heat_out<R><<<nb, BLOCK, 0, s>>>(m, x, ar, au, ae);
+    k_heat_out<R, S><<<nb, BLOCK, 0, s>>>(m, x, ar, au, ae);
     if (Mout) cudaMemcpyAsync(Mout, M, sizeof(double) * c->nC, cudaMemcpyDeviceToDevice, s);
     if (DTout) cudaMemcpyAsync(DTout, DT, sizeof(double) * c->nF, cudaMemcpyDeviceToDevice, s);
     cudaError_t e = cudaGetLastError();
@@ -455,9 +455,13 @@ int adjoint_viscosity_dev(Ctx* c, const R* rho, const R* rhoU, const R* rhoE, in
     return AFVM_OK;
 }
 
-template int adjoint_viscosity_dev<double>(Ctx*, const double*, const double*, const double*, int, double, double,
-                                           double*, double*, double*, double*, double*, int*, cudaStream_t);
-template int adjoint_viscosity_dev<float>(Ctx*, const float*, const float*, const float*, int, double, double,
-                                          float*, float*, float*, double*, double*, int*, cudaStream_t);
+template int adjoint_viscosity_dev<double, double>(Ctx*, const double*, const double*, const double*, int, double,
+                                                   double, double*, double*, double*, double*, double*, int*,
+                                                   cudaStream_t);
+template int adjoint_viscosity_dev<float, float>(Ctx*, const float*, const float*, const float*, int, double, double,
+                                                 float*, float*, float*, double*, double*, int*, cudaStream_t);
+template int adjoint_viscosity_dev<float, double>(Ctx*, const double*, const double*, const double*, int, double,
+                                                  double, double*, double*, double*, double*, double*, int*,
+                                                  cudaStream_t);
 
 }  // namespace afvm

@@ -98,7 +98,7 @@ class Slot(object):
         self.dev = torch.device('cuda', device)
         self.rcf = RCF(case.mesh, case.bc, objective=case.objective, precision=precision, device=device,
                        **case.config)
-        self.td = torch.float64 if precision == 'fp64' else torch.float32
+        self.td = torch.float32 if precision == 'fp32' else torch.float64      # state type
         n = case.mesh.nInternalCells
         shapes = [(n, 1), (n, 3), (n, 1)]
         z = lambda: [torch.zeros(s, dtype=self.td, device=self.dev) for s in shapes]
@@ -231,31 +231,50 @@ class SensitivityServer(object):
         self.bytes_of = {}
         self.used = 0
 
+    def close(self):
+        """Release every slot's device context."""
+        for s in self.slots:
+            s.rcf.close()
+        self.slots = []
+        self.used = 0
+
     def warm(self, keys):
-        """Create (and capture) one slot per mesh key ahead of traffic."""
-        for key in keys:
-            if not any(s.key == key for s in self.slots):
-                s = self._slot_for(key)
-                if s is None:
-                    raise RuntimeError('HBM budget too small for a slot of %s' % key)
+        """Create (and capture) slots ahead of traffic: as many slots of each mesh key as the
+        key appears in ``keys`` (one per distinct key for a list of distinct keys), within
+        the HBM budget and the slot limit; no slot is evicted for this. Returns the number of
+        slots created."""
+        made = 0
+        for key, count in collections.Counter(keys).items():
+            while sum(s.key == key for s in self.slots) < count:
+                if self._new_slot(key, evict=False) is None:
+                    if not any(s.key == key for s in self.slots):
+                        raise RuntimeError('HBM budget too small for a slot of %s' % key)
+                    break
+                made += 1
+        return made
 
     def _estimate(self, key):
         if key in self.bytes_of:
             return self.bytes_of[key]
         m = self.lib.get(key).mesh
-        es = 8 if self.precision == 'fp64' else 4
-        # mesh tables + records + face fluxes + adjoint records + checkpoints (see DESIGN.md)
-        return int(m.nFaces * (60 + 28 * es + 40 * es) + m.nInternalCells * (150 + 80 * es
-                   + (self.nPrimal // self.k + self.k + 8) * 5 * es))
+        er = 8 if self.precision == 'fp64' else 4      # mesh tables, records, face fluxes
+        es = 4 if self.precision == 'fp32' else 8      # states, stages, checkpoints, adjoints
+        # per face: tables, flux records, adjoint face records; per cell: tables and cell
+        # records, RK and adjoint work states, checkpoints, interval states and stage buffers
+        return int(m.nFaces * (60 + 28 * er + 40 * er) + m.nInternalCells * (150 + 40 * er + 40 * es
+                   + (self.nPrimal // self.k + 3 * self.k + 8) * 5 * es))
 
     def _slot_for(self, key):
         for s in self.slots:
             if s.key == key and not s.busy:
                 return s
+        return self._new_slot(key)
+
+    def _new_slot(self, key, evict=True):
         need = self._estimate(key)
         while self.used + need > self.budget or len(self.slots) >= self.max_slots:
             idle = [s for s in self.slots if not s.busy]
-            if not idle:
+            if not idle or not evict:
                 return None
             victim = idle[0]
             self.slots.remove(victim)

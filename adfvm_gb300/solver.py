@@ -74,8 +74,11 @@ class RCF(object):
             self.vane = dict(objective) if isinstance(objective, dict) else _vane.options(self.mesh)
             objective = 'vane'
         self.objective = objective
-        self.precision = {'fp64': L.AFVM_FP64, 'fp32': L.AFVM_FP32}[precision]
-        self.dtype = np.float64 if self.precision == L.AFVM_FP64 else np.float32
+        # 'fp64'; 'fp32'; 'mixed': FP32 mesh tables, records, face fluxes and face arithmetic
+        # with the conservative state, RK stages, sources and adjoints in FP64
+        self.precision = {'fp64': L.AFVM_FP64, 'fp32': L.AFVM_FP32, 'mixed': L.AFVM_FP32_STATE64}[precision]
+        self.dtype = np.float32 if self.precision == L.AFVM_FP32 else np.float64                # state
+        self.record_dtype = np.float64 if self.precision == L.AFVM_FP64 else np.float32         # records
         self.device = device
         self._ctx = None
         self._create()
@@ -564,10 +567,11 @@ class RCF(object):
         return self.conservative(prim['U'], prim['T'], prim['p'])
 
     def boundary_values(self, rho, rhoU, rhoE):
-        """Ghost-cell U, T, p (nGhostCells x 5 CUDA tensor, working precision) of a device
-        state: the boundary map (afvm_boundary_values)."""
+        """Ghost-cell U, T, p (nGhostCells x 5 CUDA tensor of the record type: FP64 for 'fp64',
+        FP32 otherwise) of a device state: the boundary map (afvm_boundary_values)."""
         torch = _torch()
-        out = torch.empty((self.mesh.nGhostCells, 5), dtype=rho.dtype, device=rho.device)
+        rd = torch.float64 if self.record_dtype == np.float64 else torch.float32
+        out = torch.empty((self.mesh.nGhostCells, 5), dtype=rd, device=rho.device)
         stream = torch.cuda.current_stream(rho.device).cuda_stream
         st = L.lib().afvm_boundary_values(self._ctx, C.c_void_p(rho.data_ptr()), C.c_void_p(rhoU.data_ptr()),
                                           C.c_void_p(rhoE.data_ptr()), C.c_void_p(out.data_ptr()),

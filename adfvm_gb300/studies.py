@@ -1,8 +1,9 @@
-"""Precision study of the FP32 form (the cylinder workload).
+"""Precision study of the FP32 and mixed forms (the cylinder workload).
 
 Cylinder O-grid 256x128 extruded one cell, inflow Mach 0.3, T = 300 K, p = 1e5 Pa, viscous
 no-slip wall, characteristic far field; 2000 steps. FP32 storage and flux/gradient
-arithmetic with FP64 objective and sensitivity accumulation against the FP64 run: the
+arithmetic with FP64 objective and sensitivity accumulation ('fp32'), and the same face
+arithmetic with the state, RK stages and adjoints in FP64 ('mixed'), against the FP64 run: the
 time-averaged drag (templates/cylinder_test.py:9-37) and its sensitivity to a source
 perturbation near the cylinder (the perturbation of templates/cylinder_test.py:45-55, scaled
 to this mesh) by the checkpointed adjoint sweep.
@@ -32,7 +33,7 @@ def precision_study(n_theta=256, n_r=128, nSteps=2000, writeInterval=100, device
     pert = source_near_cylinder(mesh)
     out = {'workload': 'cylinder %dx%d, %d steps, dt %.3e s' % (n_theta, n_r, nSteps, case.dt)}
     res = {}
-    for prec in ('fp64', 'fp32'):
+    for prec in ('fp64', 'fp32', 'mixed'):
         rcf = RCF(mesh, case.bc, objective=case.objective, precision=prec, device=device, **case.config)
         adj = Adjoint(rcf)
         t0 = time.perf_counter()
@@ -42,6 +43,8 @@ def precision_study(n_theta=256, n_r=128, nSteps=2000, writeInterval=100, device
         res[prec] = {'drag': drag, 'sensitivity': sens[0], 'seconds': round(el, 2)}
         rcf.close()
     out.update(res)
-    out['drag_rel_err'] = abs(res['fp32']['drag'] - res['fp64']['drag']) / abs(res['fp64']['drag'])
-    out['sensitivity_rel_err'] = abs(res['fp32']['sensitivity'] - res['fp64']['sensitivity']) / abs(res['fp64']['sensitivity'])
+    for prec in ('fp32', 'mixed'):
+        out['%s_drag_rel_err' % prec] = abs(res[prec]['drag'] - res['fp64']['drag']) / abs(res['fp64']['drag'])
+        out['%s_sensitivity_rel_err' % prec] = (abs(res[prec]['sensitivity'] - res['fp64']['sensitivity'])
+                                                / abs(res['fp64']['sensitivity']))
     return out

@@ -48,7 +48,7 @@ def peaks():
 
 
 # algorithmic (compulsory) bytes per launch of each primal kernel, FP64 / FP32 element size
-# es and int32 indices; see DESIGN.md "Algorithmic bytes"
+# es and int32 indices (per-unit counts in the comments below)
 def algorithmic_bytes(kernel, nIC, nIF, nF, nG, es):
     REC, FREC = 20, 6
     if kernel == 'k_flux':
@@ -385,16 +385,19 @@ SERVING_KEYS = ['box16', 'box24', 'box32', 'box48', 'box64', 'box96', 'cyl64x32'
 SERVING_LAMBDAS = (1.0, 2.0, 5.0, 10.0, 20.0, 50.0, 100.0, 200.0)
 
 
-def serving_bench(local, lams=SERVING_LAMBDAS, seed=4, n_mix=48, window_s=6.0):
+def serving_bench(local, lams=SERVING_LAMBDAS, seed=4, n_mix=48, window_s=6.0, precision='mixed'):
     """Sensitivity requests, each a jittered periodic box of side 16-96 or a cylinder O-grid
     64x32-256x128 drawn uniformly (seed 4), 100 primal + 100 adjoint steps.
 
-    * capacity on one mix of n_mix requests: served (FP32, continuous batching, all admitted
-      at once) against the plain FP64 one-at-a-time form, whose time on the mix is the sum of
-      its measured time per request of each mesh (it runs requests back to back);
+    * capacity on one mix of n_mix requests: served (``precision``: 'mixed' = FP32 face
+      arithmetic with FP64 state and adjoints; continuous batching, all admitted at once)
+      against the plain FP64 one-at-a-time form, whose time on the mix is the sum of its
+      measured time per request of each mesh (it runs requests back to back); the same mix
+      served in FP32 as well, for comparison;
     * latency: Poisson arrivals swept over lambda = 1-200 req/s, min(n_mix, max(8, 6 s x
       lambda)) requests per rate, p50/p99 from arrival to result;
-    * accuracy: the served FP32 sensitivity of one request per mesh against its plain FP64 one."""
+    * accuracy: the served sensitivity of one request per mesh against its plain FP64 one, in
+      both served precisions."""
     from adfvm_gb300 import serving
     keys = SERVING_KEYS
     rng = np.random.default_rng(seed)
@@ -403,7 +406,11 @@ def serving_bench(local, lams=SERVING_LAMBDAS, seed=4, n_mix=48, window_s=6.0):
     lib = serving.MeshLibrary()
     for k in keys:
         lib.get(k)
-    srv = serving.SensitivityServer(precision='fp32', device=local, k=10, nPrimal=100, library=lib)
+    # a server that stays up keeps its slots: contexts and graphs of the mix's meshes are made
+    # before the timed serving, as the plain form's contexts are made before its timing
+    srv = serving.SensitivityServer(precision=precision, device=local, k=10, nPrimal=100, library=lib,
+                                     hbm_budget=120e9, max_slots=64)
+    srv.warm(ks)
     srv.warm(keys)
     # plain FP64: one request per mesh, timed one by one
     probe = [serving.Request(rid=1000 + i, key=k, seed=1000 + i, nPrimal=100) for i, k in enumerate(keys)]
@@ -415,7 +422,9 @@ def serving_bench(local, lams=SERVING_LAMBDAS, seed=4, n_mix=48, window_s=6.0):
     sm = srv.serve(mix, realtime=False)
     same = [serving.Request(rid=1000 + i, key=k, seed=1000 + i, nPrimal=100, arrival=0.0) for i, k in enumerate(keys)]
     srv.serve(same, realtime=False)
-    errs = {a.key: float('%.3g' % (abs(a.sensitivity - b.sensitivity) / abs(b.sensitivity))) for a, b in zip(same, probe)}
+    rel = lambda rs: {a.key: float('%.3g' % (abs(a.sensitivity - b.sensitivity) / abs(b.sensitivity)))
+                      for a, b in zip(rs, probe)}
+    errs = rel(same)
     sweep = []
     for lam in lams:
         nr = int(min(n_mix, max(8, round(window_s * lam))))
@@ -425,13 +434,31 @@ def serving_bench(local, lams=SERVING_LAMBDAS, seed=4, n_mix=48, window_s=6.0):
         st = srv.serve(reqs, realtime=True)
         sweep.append({'lambda': lam, 'requests': nr, 'req_per_s': round(st['req_per_s'], 3),
                       'p50_s': round(st['p50_s'], 4), 'p99_s': round(st['p99_s'], 4)})
+    nslots = len(srv.slots)
+    srv.close()
+    other = None
+    if precision != 'fp32':
+        # the same mix and probes served in FP32 (state and adjoints FP32 too)
+        s32 = serving.SensitivityServer(precision='fp32', device=local, k=10, nPrimal=100, library=lib,
+                                        hbm_budget=120e9, max_slots=64)
+        s32.warm(ks)
+        s32.warm(keys)
+        mix32 = [serving.Request(rid=i, key=k, seed=i, nPrimal=100, arrival=0.0) for i, k in enumerate(ks)]
+        sm32 = s32.serve(mix32, realtime=False)
+        same32 = [serving.Request(rid=1000 + i, key=k, seed=1000 + i, nPrimal=100, arrival=0.0)
+                  for i, k in enumerate(keys)]
+        s32.serve(same32, realtime=False)
+        e32 = rel(same32)
+        other = {'precision': 'fp32', 'served_req_per_s': round(n_mix / sm32['elapsed_s'], 3),
+                 'max_rel_err_vs_fp64': max(e32.values()), 'rel_err_by_mesh': e32}
+        s32.close()
     served_rate = n_mix / sm['elapsed_s']
     plain_rate = n_mix / plain_mix_s
-    return {'mix_requests': n_mix, 'served_req_per_s': round(served_rate, 3), 'plain_fp64_req_per_s': round(plain_rate, 3),
-            'speedup_vs_plain': round(served_rate / plain_rate, 2),
+    return {'precision': precision, 'mix_requests': n_mix, 'served_req_per_s': round(served_rate, 3),
+            'plain_fp64_req_per_s': round(plain_rate, 3), 'speedup_vs_plain': round(served_rate / plain_rate, 2),
             'plain_seconds_per_request': {k: round(v, 4) for k, v in t_plain.items()},
-            'latency_sweep': sweep, 'max_rel_err_fp32_vs_fp64': max(errs.values()), 'rel_err_by_mesh': errs,
-            'slots': len(srv.slots), 'meshes': keys,
+            'latency_sweep': sweep, 'max_rel_err_vs_fp64': max(errs.values()), 'rel_err_by_mesh': errs,
+            'fp32': other, 'slots': nslots, 'meshes': keys,
             'steps_per_request': '100 primal + 100 adjoint (checkpoints every 10)'}
 
 

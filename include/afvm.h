@@ -39,6 +39,10 @@ extern "C" {
 #define AFVM_FP64 0              /* all arithmetic and storage in double                  */
 #define AFVM_FP32 1              /* float storage/flux/gradient; double for the pressure
                                     recovery, the objective and the sensitivity sums       */
+#define AFVM_FP32_STATE64 2      /* AFVM_FP32's float mesh tables, cell records, face
+                                    fluxes and face arithmetic, with the conservative
+                                    state, RK stages, sources and adjoints in double: the
+                                    RK update and its reverse accumulate in double          */
 
 /* ---- mesh patch kinds (the 'type' entry of a polyMesh boundary patch) ---- */
 #define AFVM_PATCH_PLAIN     0   /* patch / wall / empty / symmetryPlane                  */
@@ -166,7 +170,8 @@ typedef struct afvm_physics {
 typedef struct afvm_ctx afvm_ctx;
 
 /* Upload the mesh, boundary conditions and physics; allocate all device work buffers.
- * bcs has mesh->nPatches entries in sortedPatches order. device is a CUDA ordinal. */
+ * bcs has mesh->nPatches entries in sortedPatches order. precision is AFVM_FP64, AFVM_FP32 or
+ * AFVM_FP32_STATE64. device is a CUDA ordinal. */
 int afvm_ctx_create(const afvm_mesh_tensors* mesh, const afvm_patch_bc* bcs,
                     const afvm_physics* physics, int32_t precision, int32_t device,
                     afvm_ctx** out);
@@ -205,7 +210,8 @@ int afvm_set_objective_vane(afvm_ctx* ctx, const afvm_objective_vane* v);
 /* Ghost-cell values of the primitive fields for a conservative state: the boundary map the
  * reference runs before writing fields (RCF.initFields -> mapBoundary, adFVM/density.py:140-143;
  * ghost rows per BCs.py:62-184). rho, rhoU, rhoE: DEVICE state as for afvm_primal_step. out:
- * DEVICE buffer of nGhostCells x 5 in the working precision, rows in ghost-cell order (cell id
+ * DEVICE buffer of nGhostCells x 5 in the record type (double for AFVM_FP64, float for the
+ * other two modes), rows in ghost-cell order (cell id
  * minus nInternalCells), columns U(3), T, p. Asynchronous on stream. */
 int afvm_boundary_values(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE,
                          void* out, void* stream);
@@ -213,7 +219,9 @@ int afvm_boundary_values(afvm_ctx* ctx, const void* rho, const void* rhoU, const
 /* One SSP-RK3 time step (adFVM/timestep.py:27-55 over RCF.equation, density.py:339-414).
  * State arrays are DEVICE pointers in the reference layout: rho (nInternalCells),
  * rhoU (nInternalCells x 3), rhoE (nInternalCells); element type double for AFVM_FP64 and
- * float for AFVM_FP32. Sources may be NULL (zero). Outputs may alias the inputs.
+ * AFVM_FP32_STATE64, float for AFVM_FP32 (the "state type"; every state, source, stage and
+ * adjoint array of this interface has it). Sources may be NULL (zero). Outputs may alias
+ * the inputs.
  * dtc_out / obj_out (host, may be NULL) receive the stage-1 max CFL sum and objective; a
  * non-NULL one makes the call wait for the step to finish. */
 int afvm_primal_step(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE,
@@ -222,7 +230,7 @@ int afvm_primal_step(afvm_ctx* ctx, const void* rho, const void* rhoU, const voi
                      double* dtc_out, double* obj_out, void* stream);
 
 /* afvm_primal_step that also keeps the step's two intermediate SSP-RK3 stage states in
- * stages (DEVICE, 10 x nInternalCells elements of the working precision: u1 then u2, each
+ * stages (DEVICE, 10 x nInternalCells elements of the state type: u1 then u2, each
  * rho | rhoU | rhoE), at no extra cost - the step writes them anyway. Handing the same buffer
  * to afvm_adjoint_step_stages with the same state, sources and dt lets the adjoint skip its
  * forward recompute of the stages (the reference's reverse mode re-runs the forward,
@@ -294,7 +302,7 @@ int afvm_sensitivity(afvm_ctx* ctx, int32_t nArrays, const double* const* grad,
 
 /* Adjoint energy sum_c w^T A(u) w V with w = adjoint / V (cmesh.computeEnergy,
  * adFVM/cpp/cmesh.cpp:342-425; the reference's adjoint driver reports its square root,
- * apps/adjoint.py:55). DEVICE arrays in the context's precision: the adjoint state
+ * apps/adjoint.py:55). DEVICE arrays of the context's state type: the adjoint state
  * (rhoa, rhoUa, rhoEa) and the primal state. FP64 sum to *out (host) after the work. */
 int afvm_adjoint_energy(afvm_ctx* ctx, const void* rhoa, const void* rhoUa, const void* rhoEa,
                         const void* rho, const void* rhoU, const void* rhoE, double* out, void* stream);

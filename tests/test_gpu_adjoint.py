@@ -51,6 +51,27 @@ def test_adjoint_step_matches_autograd(name):
     assert e < 1e-11, (name, 'source', e)
 
 
+@pytest.mark.parametrize('precision,tol', [('fp32', 1e-4), ('mixed', 1e-6)])
+@pytest.mark.parametrize('name', ['box8', 'cyl32x16', 'duct100_totalpt'])
+def test_reduced_precision_adjoint_against_fp64_autograd(name, precision, tol):
+    """FP32 contexts and mixed ones (FP32 records and face arithmetic, FP64 state, stages and
+    adjoints) against the FP64 autograd VJP of one step: max|x-ref|/max|ref| per field."""
+    case, mesh, x, S, dt = _setup(name)
+    prob = torch_ref.Problem(mesh, case.bc, case.config, case.objective)
+    seeds = _seeds(x, 7)
+    St = None if S is None else [torch.as_tensor(s) for s in S]
+    ref = torch_ref.vjp_step(prob, x[0], x[1], x[2], dt, St, seeds, obja=1.0)
+    rcf = RCF(mesh, case.bc, objective=case.objective, precision=precision, **case.config)
+    td = torch.float32 if precision == 'fp32' else torch.float64
+    d = [t.to(td).cuda() for t in x]
+    Sd = None if S is None else [torch.as_tensor(s).to(td).cuda() for s in S]
+    a = rcf.adjoint_step(d[0], d[1], d[2], dt, [t.to(td).cuda() for t in seeds], obja=1.0, S=Sd)
+    for i in range(3):
+        assert a[i].dtype == td
+        e = G.rel_err(a[i].double().cpu().numpy(), ref[i].numpy())
+        assert e < tol, (name, i, e)
+
+
 def test_adjoint_deterministic_and_aliasing():
     case, mesh, x, S, dt = _setup('cyl32x16')
     rcf = RCF(mesh, case.bc, objective=case.objective, **case.config)
@@ -140,14 +161,14 @@ def test_autograd_solve_matches_oracle_and_fd():
 
 
 @pytest.mark.parametrize('name,precision', [('box8', 'fp64'), ('cyl32x16', 'fp64'), ('duct100_totalpt', 'fp64'),
-                                            ('box8', 'fp32')])
+                                            ('box8', 'fp32'), ('cyl32x16', 'mixed')])
 def test_kept_stages_give_the_same_adjoint(name, precision):
     """afvm_primal_step_stages / afvm_adjoint_step_stages: the adjoint on the stage states the
     primal step kept is bitwise the adjoint that recomputes them, and the primal step itself is
     unchanged by keeping them."""
     case, mesh, x, S, dt = _setup(name)
     rcf = RCF(mesh, case.bc, objective=case.objective, precision=precision, **case.config)
-    td = torch.float64 if precision == 'fp64' else torch.float32
+    td = torch.float32 if precision == 'fp32' else torch.float64
     d = [t.to(td).cuda() for t in x]
     Sd = None if S is None else [torch.as_tensor(s).to(td).cuda() for s in S]
     seeds = [t.to(td).cuda() for t in _seeds(x, 3)]

@@ -77,20 +77,25 @@ def test_device_run_matches_step_loop_and_is_deterministic():
     assert G.rel_err(hist[0].cpu().numpy(), np.array(record)[:, 0]) < 1e-13
 
 
+@pytest.mark.parametrize('precision', ['fp32', 'mixed'])
 @pytest.mark.parametrize('name', ['box8', 'cyl32x16'])
-def test_fp32_against_fp64_oracle(name):
+def test_fp32_against_fp64_oracle(name, precision):
     case, g = G.load(name)
     mesh = case.build_mesh()
     prob = torch_ref.Problem(mesh, case.bc, case.config, case.objective)
     x = [torch.as_tensor(a) for a in _init(g)]
     ref = prob.step(x[0], x[1], x[2], float(g['dt0']))
-    rcf = _solver(case, 'fp32')
-    d = [a.float().cuda() for a in x]
+    rcf = _solver(case, precision)
+    td = torch.float32 if precision == 'fp32' else torch.float64
+    d = [a.to(td).cuda() for a in x]
     out = rcf.step(d[0], d[1], d[2], float(g['dt0']))
-    # FP32 storage and flux arithmetic: one step stays within 1e-5 of FP64 per field
+    assert out[0].dtype == td
+    # FP32 records and flux arithmetic: one step stays within 1e-5 of FP64 per field; with
+    # the state in FP64 ('mixed') only the step's increment carries FP32 rounding: 1e-7
+    tol = 1e-5 if precision == 'fp32' else 1e-7
     for i in range(3):
         e = G.rel_err(out[i].double().cpu().numpy(), ref[i].numpy())
-        assert e < 1e-5, (i, e)
+        assert e < tol, (i, e)
     assert abs(out[4] - float(ref[4])) <= 1e-5 * max(1.0, abs(float(ref[4])))
 
 

@@ -1,6 +1,6 @@
 """Continuous-batching sensitivity server: a request's result is the same alone and in a
-mix; the served FP64 result equals the plain one-at-a-time computation; FP32 is within the
-stated bound of FP64."""
+mix; the served FP64 result equals the plain one-at-a-time computation; FP32 and mixed
+(FP32 records and fluxes, FP64 state) are within their stated bounds of FP64."""
 import numpy as np
 import pytest
 
@@ -42,3 +42,15 @@ def test_fp32_served_within_bound_of_fp64():
         # FP32 storage and flux arithmetic, FP64 sensitivity accumulation: 1e-3 relative over
         # 8 primal + 8 adjoint steps
         assert abs(a.sensitivity - b.sensitivity) <= 1e-3 * abs(b.sensitivity), (a.key, a.sensitivity, b.sensitivity)
+
+
+def test_mixed_served_within_bound_of_fp64():
+    lib = serving.MeshLibrary()
+    r64 = _reqs(KEYS, [7, 8, 9], 8)
+    serving.plain_one_at_a_time(r64, lib, nPrimal=8)
+    rm = _reqs(KEYS, [7, 8, 9], 8)
+    srv = serving.SensitivityServer(precision='mixed', k=4, nPrimal=8, library=lib)
+    srv.serve(rm, realtime=False)
+    for a, b in zip(rm, r64):
+        # FP32 face arithmetic, FP64 state, stages, adjoints and sums: 1e-5 relative
+        assert abs(a.sensitivity - b.sensitivity) <= 1e-5 * abs(b.sensitivity), (a.key, a.sensitivity, b.sensitivity)

@@ -4,7 +4,8 @@ postpro.computeAdjointViscosity / viscositySolver (tests/golden/viscosity.npz).
 Tolerances: the viscosity and its face values within 1e-12 relative in FP64 (the largest
 eigenvalue comes from Jacobi rotations here and LAPACK there); the smoothed adjoint within
 1e-10 (CG to a relative residual of 1e-13 here, a direct solve there); FP32 contexts (whose
-mesh tables and state are FP32) within 1e-5."""
+mesh tables and state are FP32) and mixed ones (FP32 mesh tables and records, FP64 state)
+within 1e-5."""
 import numpy as np
 import pytest
 import torch
@@ -21,7 +22,7 @@ def _setup(name, precision='fp64'):
     case = CASES[name]()
     m = case.build_mesh()
     rcf = RCF(m, case.bc, objective=case.objective, precision=precision, **case.config)
-    td = torch.float64 if precision == 'fp64' else torch.float32
+    td = torch.float32 if precision == 'fp32' else torch.float64
     x = [torch.as_tensor(g['%s/%s' % (name, k)]).to(td).cuda() for k in ('rho', 'rhoU', 'rhoE')]
     return g, m, rcf, x, td
 
@@ -40,7 +41,7 @@ def test_viscosity_fields_match_reference(name, kind):
 
 
 @pytest.mark.parametrize('name', list(CASES))
-@pytest.mark.parametrize('precision', ['fp64', 'fp32'])
+@pytest.mark.parametrize('precision', ['fp64', 'fp32', 'mixed'])
 def test_smoother_matches_reference(name, precision):
     g, m, rcf, x, td = _setup(name, precision)
     dt = float(g['%s/smooth/dt' % name])
