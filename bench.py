@@ -385,15 +385,15 @@ SERVING_KEYS = ['box16', 'box24', 'box32', 'box48', 'box64', 'box96', 'cyl64x32'
 SERVING_LAMBDAS = (1.0, 2.0, 5.0, 10.0, 20.0, 50.0, 100.0, 200.0)
 
 
-def serving_bench(local, lams=SERVING_LAMBDAS, seed=4, n_mix=48, window_s=6.0, precision='mixed'):
+def serving_bench(local, lams=SERVING_LAMBDAS, seed=4, n_mix=48, window_s=6.0, precision='fp32', compare='mixed'):
     """Sensitivity requests, each a jittered periodic box of side 16-96 or a cylinder O-grid
     64x32-256x128 drawn uniformly (seed 4), 100 primal + 100 adjoint steps.
 
-    * capacity on one mix of n_mix requests: served (``precision``: 'mixed' = FP32 face
-      arithmetic with FP64 state and adjoints; continuous batching, all admitted at once)
-      against the plain FP64 one-at-a-time form, whose time on the mix is the sum of its
-      measured time per request of each mesh (it runs requests back to back); the same mix
-      served in FP32 as well, for comparison;
+    * capacity on one mix of n_mix requests: served (``precision``; continuous batching, all
+      admitted at once) against the plain FP64 one-at-a-time form, whose time on the mix is
+      the sum of its measured time per request of each mesh (it runs requests back to back);
+      the same mix served in the ``compare`` precision as well ('mixed' = FP32 face
+      arithmetic with FP64 state, stages and adjoints);
     * latency: Poisson arrivals swept over lambda = 1-200 req/s, min(n_mix, max(8, 6 s x
       lambda)) requests per rate, p50/p99 from arrival to result;
     * accuracy: the served sensitivity of one request per mesh against its plain FP64 one, in
@@ -437,9 +437,9 @@ def serving_bench(local, lams=SERVING_LAMBDAS, seed=4, n_mix=48, window_s=6.0, p
     nslots = len(srv.slots)
     srv.close()
     other = None
-    if precision != 'fp32':
-        # the same mix and probes served in FP32 (state and adjoints FP32 too)
-        s32 = serving.SensitivityServer(precision='fp32', device=local, k=10, nPrimal=100, library=lib,
+    if compare and compare != precision:
+        # the same mix and probes served in the comparison precision
+        s32 = serving.SensitivityServer(precision=compare, device=local, k=10, nPrimal=100, library=lib,
                                         hbm_budget=120e9, max_slots=64)
         s32.warm(ks)
         s32.warm(keys)
@@ -449,7 +449,7 @@ def serving_bench(local, lams=SERVING_LAMBDAS, seed=4, n_mix=48, window_s=6.0, p
                   for i, k in enumerate(keys)]
         s32.serve(same32, realtime=False)
         e32 = rel(same32)
-        other = {'precision': 'fp32', 'served_req_per_s': round(n_mix / sm32['elapsed_s'], 3),
+        other = {'precision': compare, 'served_req_per_s': round(n_mix / sm32['elapsed_s'], 3),
                  'max_rel_err_vs_fp64': max(e32.values()), 'rel_err_by_mesh': e32}
         s32.close()
     served_rate = n_mix / sm['elapsed_s']
@@ -458,7 +458,7 @@ def serving_bench(local, lams=SERVING_LAMBDAS, seed=4, n_mix=48, window_s=6.0, p
             'plain_fp64_req_per_s': round(plain_rate, 3), 'speedup_vs_plain': round(served_rate / plain_rate, 2),
             'plain_seconds_per_request': {k: round(v, 4) for k, v in t_plain.items()},
             'latency_sweep': sweep, 'max_rel_err_vs_fp64': max(errs.values()), 'rel_err_by_mesh': errs,
-            'fp32': other, 'slots': nslots, 'meshes': keys,
+            'compare': other, 'slots': nslots, 'meshes': keys,
             'steps_per_request': '100 primal + 100 adjoint (checkpoints every 10)'}
 
 

@@ -91,8 +91,8 @@ def test_fp32_against_fp64_oracle(name, precision):
     out = rcf.step(d[0], d[1], d[2], float(g['dt0']))
     assert out[0].dtype == td
     # FP32 records and flux arithmetic: one step stays within 1e-5 of FP64 per field; with
-    # the state in FP64 ('mixed') only the step's increment carries FP32 rounding: 1e-7
-    tol = 1e-5 if precision == 'fp32' else 1e-7
+    # the state in FP64 ('mixed') only the step's increment carries FP32 rounding: 1e-6
+    tol = 1e-5 if precision == 'fp32' else 1e-6
     for i in range(3):
         e = G.rel_err(out[i].double().cpu().numpy(), ref[i].numpy())
         assert e < tol, (i, e)
