@@ -80,6 +80,7 @@ class ObjectiveVane(C.Structure):
 SIGNATURES = {
     'afvm_mesh_build': (C.c_int, [C.POINTER(MeshIn), C.POINTER(MeshOut)]),
     'afvm_mesh_build_device': (C.c_int, [C.POINTER(MeshIn), C.POINTER(MeshOut), _v]),
+    'afvm_mesh_reorder_device': (C.c_int, [C.POINTER(MeshIn), _i, _i, _i, _i, _i, _i, _v]),
     'afvm_ctx_create': (C.c_int, [C.POINTER(MeshTensors), C.POINTER(PatchBC), C.POINTER(Physics),
                                   C.c_int32, C.c_int32, C.POINTER(_v)]),
     'afvm_ctx_destroy': (C.c_int, [_v]),

@@ -184,3 +184,41 @@ class Mesh(object):
         for k, t in out.items():
             setattr(self, k, t.cpu().numpy())
         self.nLocalCells = int(mo.nLocalCells)
+
+
+def reorder(meshData, device=0):
+    """Bandwidth (reverse Cuthill-McKee) renumbering of a mesh's cells on the GPU
+    (afvm_mesh_reorder_device), for meshes admitted in any cell order.
+
+    meshData = (points, faces, owner, neighbour, boundary). Returns (meshData', cellNew,
+    faceOld, (bandwidth before, after)): cellNew[old cell] = new id (a field ``x`` of the old
+    mesh is ``x_new[cellNew] = x`` on the new one), faceOld[new face] = old face, ~old where
+    the face was flipped. Points and boundary patches are unchanged."""
+    import torch
+    points, faces, owner, neighbour, boundary = meshData
+    faces = np.ascontiguousarray(faces, np.int32)
+    owner = np.ascontiguousarray(owner, np.int32).reshape(-1)
+    neighbour = np.ascontiguousarray(neighbour, np.int32).reshape(-1)
+    nF, nIF = len(owner), len(neighbour)
+    nIC = int(owner.max()) + 1
+    m = Mesh()
+    m.boundary = copy.deepcopy(boundary)
+    order = sorted(m.boundary.keys(), key=lambda x: (m.boundary[x]['startFace'], m.boundary[x]['nFaces']))
+    patches = m.patchTable(order)
+    dev = torch.device('cuda', device)
+    up = lambda a: torch.as_tensor(a).to(dev)
+    df, do, dn = up(faces), up(owner), up(neighbour if nIF > 0 else np.zeros(1, np.int32))
+    fo = torch.empty_like(df)
+    oo = torch.empty_like(do)
+    no = torch.empty_like(dn)
+    cn = torch.empty(nIC, dtype=torch.int32, device=dev)
+    fold = torch.empty(nF, dtype=torch.int32, device=dev)
+    ip = lambda t: C.cast(C.c_void_p(t.data_ptr()), L._i)
+    mi = L.MeshIn(0, None, nF, ip(df), nIF, ip(do), ip(dn), nIC, len(order), patches)
+    bw = (C.c_int32 * 2)()
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    L.check(L.lib().afvm_mesh_reorder_device(mi, ip(fo), ip(oo), ip(no), ip(cn), ip(fold),
+                                             C.cast(bw, L._i), C.c_void_p(stream)),
+            what='afvm_mesh_reorder_device')
+    out = (np.asarray(points), fo.cpu().numpy(), oo.cpu().numpy(), no.cpu().numpy()[:nIF], copy.deepcopy(boundary))
+    return out, cn.cpu().numpy(), fold.cpu().numpy(), (int(bw[0]), int(bw[1]))

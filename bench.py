@@ -381,6 +381,44 @@ def mesh_build_timing(case, local, reps=3):
                     'every result to host arrays'}
 
 
+def reorder_timing(n, local, steps=5):
+    """The shuffled n^3 box (cells in random order, seed 1): the device renumbering
+    (afvm_mesh_reorder_device, host arrays in and out) and the FP64 primal step on the mesh
+    before and after it (CUDA events over ``steps`` steps) - what a mesh admitted in an
+    arbitrary cell order costs without and with the renumbering."""
+    import torch
+    from adfvm_gb300 import cases, meshgen
+    from adfvm_gb300.mesh import Mesh, reorder
+    from adfvm_gb300.solver import RCF
+    md = meshgen.periodic_box(n, reorder=False)
+    reorder(meshgen.periodic_box(8, reorder=False), device=local)      # load and warm the path
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    md2, cn, _, bw = reorder(md, device=local)
+    t_re = time.perf_counter() - t0
+    ref = cases.box(n)
+    out = {'mesh': 'box%d shuffled' % n, 'cells': int(len(cn)), 'reorder_ms': round(1e3 * t_re, 1),
+           'bandwidth_before': bw[0], 'bandwidth_after': bw[1]}
+    for tag, data in (('shuffled', md), ('reordered', md2)):
+        mesh = Mesh.create(data, device=local)
+        rcf = RCF(mesh, ref.bc, objective=ref.objective, device=local, **ref.config)
+        x = [torch.as_tensor(a).cuda(local) for a in rcf.conservative(np.zeros((mesh.nInternalCells, 3)),
+                                                                      np.full((mesh.nInternalCells, 1), 300.0),
+                                                                      np.full((mesh.nInternalCells, 1), 1.0332e5))]
+        for _ in range(2):
+            rcf.step(x[0], x[1], x[2], ref.dt, out=x, want_scalars=False)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(steps):
+            rcf.step(x[0], x[1], x[2], ref.dt, out=x, want_scalars=False)
+        e1.record()
+        torch.cuda.synchronize()
+        out[tag + '_ms_per_step'] = round(e0.elapsed_time(e1) / steps, 3)
+        rcf.close()
+    return out
+
+
 SERVING_KEYS = ['box16', 'box24', 'box32', 'box48', 'box64', 'box96', 'cyl64x32', 'cyl128x64', 'cyl256x128']
 SERVING_LAMBDAS = (1.0, 2.0, 5.0, 10.0, 20.0, 50.0, 100.0, 200.0)
 
@@ -538,6 +576,8 @@ def main():
         line['serving'] = serving_bench(local)
     if rank == 0:
         line['mesh_build'] = mesh_build_timing(case, local)
+        if case.name.startswith('box'):
+            line['mesh_reorder'] = reorder_timing(int(case.name[3:]), local)
     from adfvm_gb300 import _lib
     line['fma_peak_tflops'] = {'fp64': round(_lib.fma_peak(local, True), 2), 'fp32': round(_lib.fma_peak(local, False), 2)}
     top, avg_s, nF = m64.pop('_top')

@@ -100,6 +100,27 @@ int afvm_mesh_build(const afvm_mesh_in* in, afvm_mesh_out* out);
  * reference functions as afvm_mesh_build. */
 int afvm_mesh_build_device(const afvm_mesh_in* in, afvm_mesh_out* out, void* stream);
 
+/* Bandwidth renumbering of a hex mesh's cells on the GPU, for meshes admitted in any cell
+ * order: reverse Cuthill-McKee over the cell graph (edges: internal faces and cyclic patch
+ * face pairs), each component started from the cell of least (degree, id), neighbours
+ * appended in increasing (degree, id), new id = nInternalCells - 1 - position; the highest
+ * id then goes to a cell owning a boundary face (the reader's cell count is max(owner) + 1,
+ * adFVM/mesh.py:521). Internal faces take the new ids, a face whose new owner id exceeds its
+ * new neighbour id is flipped (ids swapped, points listed p2 p1 p0 p3 so that the normal of
+ * adFVM/cpp/cmesh.cpp:72-87 is exactly negated), and internal faces are ordered by (owner,
+ * neighbour, old face); boundary faces keep their places. No reference counterpart (the
+ * reference takes meshes in file order, adFVM/mesh.py:84-127).
+ * in->faces, owner, neighbour: DEVICE (points unused); in->patches: host. Outputs, DEVICE,
+ * caller-allocated: facesOut (nFaces x 5), ownerOut (nFaces), neighbourOut (nInternalFaces),
+ * cellNew (nInternalCells: new id of each old cell), faceOld (nFaces: old face of each new
+ * face, ~old where flipped). bandwidth (host, may be NULL): max |id difference| over the
+ * graph's edges before and after. Returns when done. AFVM_ERR_BAD_ARG for an index out of
+ * range, a face between a cell and itself or a cell without faces, AFVM_ERR_UNSUPPORTED for a cell with more than six graph edges or processor
+ * patches. */
+int afvm_mesh_reorder_device(const afvm_mesh_in* in, int32_t* facesOut, int32_t* ownerOut,
+                             int32_t* neighbourOut, int32_t* cellNew, int32_t* faceOld,
+                             int32_t* bandwidth, void* stream);
+
 /* ---- solver context ---- */
 
 /* The mesh tensors in the order of Mesh.getTensor() (adFVM/mesh.py:27-32, 870-872) and

@@ -4,8 +4,9 @@
   lie (adFVM/cpp/cmesh.cpp and adFVM/cpp/mesh.cpp under the reference checkout), against the
   stand-in headers in oracle/refshim, into the Python extension ``oracle/_ref/cmesh``. It
   runs only where the reference checkout exists (``AFVM_REFERENCE`` or /root/reference).
-* ``build_c()`` compiles the C restatement of the residual (oracle/c/afvm_oracle.c) into
-  ``oracle/_ref/liboracle.so`` for the timed CPU baseline.
+* ``build_c()`` compiles the C restatements of the residual (oracle/c/afvm_oracle.c, also the
+  timed CPU baseline) and of the cell renumbering (oracle/c/reorder_oracle.c) into
+  ``oracle/_ref/liboracle.so``.
 Both use -ffp-contract=off so that x86 and Arm give identical results.
 """
 import os
@@ -48,15 +49,16 @@ def build_ref():
 
 
 def build_c():
-    """Compile the C restatement of the residual into oracle/_ref/liboracle.so."""
+    """Compile the C restatements (the residual, oracle/c/afvm_oracle.c; the cell renumbering,
+    oracle/c/reorder_oracle.c) into oracle/_ref/liboracle.so."""
     os.makedirs(OUT, exist_ok=True)
-    src = os.path.join(HERE, 'c', 'afvm_oracle.c')
-    if not os.path.exists(src):
+    srcs = [os.path.join(HERE, 'c', f) for f in ('afvm_oracle.c', 'reorder_oracle.c')]
+    if not all(os.path.exists(s) for s in srcs):
         return None
     target = os.path.join(OUT, 'liboracle.so')
-    if os.path.exists(target) and os.path.getmtime(target) > os.path.getmtime(src):
+    if os.path.exists(target) and all(os.path.getmtime(target) > os.path.getmtime(s) for s in srcs):
         return target
-    _run(['gcc', '-O3', '-std=c11', '-shared', '-fPIC', '-fopenmp', '-ffp-contract=off', src, '-o', target, '-lm'])
+    _run(['gcc', '-O3', '-std=c11', '-shared', '-fPIC', '-fopenmp', '-ffp-contract=off'] + srcs + ['-o', target, '-lm'])
     return target
 
 

@@ -42,6 +42,9 @@ def lib():
         L.oracle_step.restype = None
         L.oracle_work_doubles.argtypes = [C.POINTER(OracleMesh)]
         L.oracle_work_doubles.restype = C.c_size_t
+        L.oracle_mesh_reorder.argtypes = [C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 3 + [C.c_int] + \
+            [C.c_void_p] * 3 + [C.c_void_p] * 6
+        L.oracle_mesh_reorder.restype = C.c_int
         _lib = L
     return _lib
 
@@ -166,3 +169,34 @@ class COracle(object):
         lib().oracle_step(C.byref(self.M), v(x[0]), v(x[1]), v(x[2]), float(dt), v(Sp), v(out[0]), v(out[1]),
                           v(out[2]), C.byref(dtc), C.byref(obj), v(self.work))
         return out[0], out[1], out[2], dtc.value, obj.value
+
+
+def mesh_reorder(meshData):
+    """Reverse Cuthill-McKee renumbering of a mesh's cells (oracle/c/reorder_oracle.c).
+
+    meshData = (points, faces, owner, neighbour, boundary) as read from a polyMesh. Returns
+    ((points, faces', owner', neighbour', boundary), cellNew, faceOld, (bandwidth before,
+    after)); cellNew[old cell] = new id, faceOld[new face] = old face (~old where flipped)."""
+    points, faces, owner, neighbour, boundary = meshData
+    faces = np.ascontiguousarray(faces, np.int32)
+    owner = np.ascontiguousarray(owner, np.int32).reshape(-1)
+    neighbour = np.ascontiguousarray(neighbour, np.int32).reshape(-1)
+    nF, nIF = len(owner), len(neighbour)
+    nIC = int(owner.max()) + 1
+    names = list(boundary.keys())
+    start = np.array([int(boundary[p]['startFace']) for p in names], np.int32)
+    count = np.array([int(boundary[p]['nFaces']) for p in names], np.int32)
+    partner = np.array([int(boundary[boundary[p]['neighbourPatch']]['startFace'])
+                        if boundary[p]['type'] in COracle.CYCLIC else -1 for p in names], np.int32)
+    fo = np.empty_like(faces)
+    oo = np.empty_like(owner)
+    no = np.empty_like(neighbour)
+    cn = np.empty(nIC, np.int32)
+    fold = np.empty(nF, np.int32)
+    bw = np.zeros(2, np.int32)
+    p = lambda a: a.ctypes.data_as(C.c_void_p)
+    rc = lib().oracle_mesh_reorder(nIC, nF, nIF, p(faces), p(owner), p(neighbour), len(names), p(start), p(count),
+                                   p(partner), p(fo), p(oo), p(no), p(cn), p(fold), p(bw))
+    if rc != 0:
+        raise ValueError('oracle_mesh_reorder: index out of range or a cell with more than six edges')
+    return (points, fo, oo, no, boundary), cn, fold, (int(bw[0]), int(bw[1]))
