@@ -416,12 +416,14 @@ extern "C" int afvm_mesh_reorder_device(const afvm_mesh_in* in, int32_t* facesOu
     cudaStream_t s = (cudaStream_t)stream;
     const size_t n = (size_t)nIC;
     const int nScan = (nIC + SCAN_BLOCK - 1) / SCAN_BLOCK + 1;
-    // ints: fill, deg, lev, ppos, order, cnt, off (n each); adj (6n); bucket (nIF); scan block
-    // sums; small: err, total, mx, bw(2); then the 64-bit seed key
+    // the 64-bit seed key first (cudaMalloc's alignment keeps it 8-byte aligned for its
+    // atomicMin), then ints: fill, deg, lev, ppos, order, cnt, off (n each); adj (6n); bucket
+    // (nIF); scan block sums; small: err, total, mx, bw(2)
+    const size_t keyBytes = 16;
     size_t nInts = 7 * n + 6 * n + (size_t)(nIF > 0 ? nIF : 1) + (size_t)nScan + 8;
     char* base = nullptr;
     DevPatch* dp = nullptr;
-    cudaError_t e = cudaMalloc(&base, sizeof(int) * nInts + sizeof(unsigned long long) * 2);
+    cudaError_t e = cudaMalloc(&base, keyBytes + sizeof(int) * nInts);
     if (e == cudaSuccess) e = cudaMalloc(&dp, sizeof(DevPatch) * pt.size());
     if (e != cudaSuccess) {
         cudaFree(base);
@@ -429,7 +431,8 @@ extern "C" int afvm_mesh_reorder_device(const afvm_mesh_in* in, int32_t* facesOu
         cudaGetLastError();
         return AFVM_ERR_OOM;
     }
-    int* ip = (int*)base;
+    unsigned long long* best = (unsigned long long*)base;
+    int* ip = (int*)(base + keyBytes);
     int* fill = ip;
     int* deg = fill + n;
     int* lev = deg + n;
@@ -445,7 +448,6 @@ extern "C" int afvm_mesh_reorder_device(const afvm_mesh_in* in, int32_t* facesOu
     int* total = small + 1;
     int* mx = small + 2;
     int* bw = small + 3;          // [0] before, [1] after
-    unsigned long long* best = (unsigned long long*)(base + sizeof(int) * nInts);
     int status = AFVM_OK;
     int herr = 0;
     cudaMemcpyAsync(dp, pt.data(), sizeof(DevPatch) * pt.size(), cudaMemcpyHostToDevice, s);
