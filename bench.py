@@ -383,9 +383,9 @@ def mesh_build_timing(case, local, reps=3):
 
 def reorder_timing(n, local, steps=5):
     """The shuffled n^3 box (cells in random order, seed 1): the device renumbering
-    (afvm_mesh_reorder_device, host arrays in and out) and the FP64 primal step on the mesh
-    before and after it (CUDA events over ``steps`` steps) - what a mesh admitted in an
-    arbitrary cell order costs without and with the renumbering."""
+    (afvm_mesh_reorder_device, host arrays in and out) and the FP32 and FP64 primal steps on
+    the mesh before and after it (CUDA events over ``steps`` steps) - what a mesh admitted in
+    an arbitrary cell order costs without and with the renumbering."""
     import torch
     from adfvm_gb300 import cases, meshgen
     from adfvm_gb300.mesh import Mesh, reorder
@@ -401,21 +401,22 @@ def reorder_timing(n, local, steps=5):
            'bandwidth_before': bw[0], 'bandwidth_after': bw[1]}
     for tag, data in (('shuffled', md), ('reordered', md2)):
         mesh = Mesh.create(data, device=local)
-        rcf = RCF(mesh, ref.bc, objective=ref.objective, device=local, **ref.config)
-        x = [torch.as_tensor(a).cuda(local) for a in rcf.conservative(np.zeros((mesh.nInternalCells, 3)),
-                                                                      np.full((mesh.nInternalCells, 1), 300.0),
-                                                                      np.full((mesh.nInternalCells, 1), 1.0332e5))]
-        for _ in range(2):
-            rcf.step(x[0], x[1], x[2], ref.dt, out=x, want_scalars=False)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        e0.record()
-        for _ in range(steps):
-            rcf.step(x[0], x[1], x[2], ref.dt, out=x, want_scalars=False)
-        e1.record()
-        torch.cuda.synchronize()
-        out[tag + '_ms_per_step'] = round(e0.elapsed_time(e1) / steps, 3)
-        rcf.close()
+        for prec, td in (('fp32', torch.float32), ('fp64', torch.float64)):
+            rcf = RCF(mesh, ref.bc, objective=ref.objective, precision=prec, device=local, **ref.config)
+            x = [torch.as_tensor(a).to(td).cuda(local)
+                 for a in rcf.conservative(np.zeros((mesh.nInternalCells, 3)), np.full((mesh.nInternalCells, 1), 300.0),
+                                           np.full((mesh.nInternalCells, 1), 1.0332e5))]
+            for _ in range(2):
+                rcf.step(x[0], x[1], x[2], ref.dt, out=x, want_scalars=False)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            for _ in range(steps):
+                rcf.step(x[0], x[1], x[2], ref.dt, out=x, want_scalars=False)
+            e1.record()
+            torch.cuda.synchronize()
+            out['%s_%s_ms_per_step' % (tag, prec)] = round(e0.elapsed_time(e1) / steps, 3)
+            rcf.close()
     return out
 
 
