@@ -24,12 +24,11 @@ namespace afvm {
 constexpr int FADJ = 40;
 constexpr int CBAR = 20;   // per cell: primitive adjoint (5) then gradient adjoint (15)
 
+// one face's record of k_adj_flux into row[0..39]
 template <typename R, typename S>
-__global__ void __launch_bounds__(FLUX_BLOCK, sizeof(R) == 8 ? 3 : 1) k_adj_flux(MeshDev<R> m, Phys P, const R* __restrict__ rec, R coef,
-                                                    const S* __restrict__ ar, const S* __restrict__ au,
-                                                    const S* __restrict__ ae, R* __restrict__ fadj, int inviscid) {
-    int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= m.nF) return;
+__device__ __forceinline__ void adj_face(const MeshDev<R>& m, const Phys& P, const R* __restrict__ rec, R coef,
+                                         const S* __restrict__ ar, const S* __restrict__ au,
+                                         const S* __restrict__ ae, int inviscid, int f, R* row) {
     int kind = (f < m.nIF) ? FACE_INTERNAL : (int)m.fkind[f - m.nIF];
     int iP = m.own[f];
     R wp = m.wpf[f];
@@ -50,9 +49,28 @@ __global__ void __launch_bounds__(FLUX_BLOCK, sizeof(R) == 8 ? 3 : 1) k_adj_flux
     zero_bar(b);
     face_vjp<R>(P, kind, inviscid != 0, in, Fb, b);
     const R* src = &b.UP[0];
-    R* out = fadj + (size_t)f * FADJ;
-    for (int k = 0; k < 5; k++) { out[k] = src[k]; out[20 + k] = src[5 + k]; }
-    for (int k = 0; k < 15; k++) { out[5 + k] = src[10 + k]; out[25 + k] = src[25 + k]; }
+    for (int k = 0; k < 5; k++) { row[k] = src[k]; row[20 + k] = src[5 + k]; }
+    for (int k = 0; k < 15; k++) { row[5 + k] = src[10 + k]; row[25 + k] = src[25 + k]; }
+}
+
+template <typename R, typename S>
+__global__ void __launch_bounds__(FLUX_BLOCK, sizeof(R) == 8 ? 3 : 4) k_adj_flux(MeshDev<R> m, Phys P, const R* __restrict__ rec, R coef,
+                                                    const S* __restrict__ ar, const S* __restrict__ au,
+                                                    const S* __restrict__ ae, R* __restrict__ fadj, int inviscid) {
+    // the block's 40-value face records are staged here and written out contiguously: one
+    // thread's 40 scalar stores at a 40-value stride would touch a new 32-byte sector each and
+    // load L2 with eight partial writes per sector
+    __shared__ R stage[FLUX_BLOCK * (FADJ + 1)];
+    const int f0 = blockIdx.x * FLUX_BLOCK;
+    const int f = f0 + threadIdx.x;
+    if (f < m.nF) adj_face<R, S>(m, P, rec, coef, ar, au, ae, inviscid, f, stage + threadIdx.x * (FADJ + 1));
+    __syncthreads();
+    const int nb = min(FLUX_BLOCK, m.nF - f0);
+    R* out = fadj + (size_t)f0 * FADJ;
+    for (int i = threadIdx.x; i < nb * FADJ; i += FLUX_BLOCK) {
+        int r = i / FADJ;
+        out[i] = stage[r * (FADJ + 1) + (i - r * FADJ)];
+    }
 }
 
 template <typename R>
