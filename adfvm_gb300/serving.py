@@ -66,6 +66,9 @@ class Request:
     seed: int = 0
     nPrimal: int = 100
     arrival: float = 0.0
+    # the request's payload: (state, source perturbation) as pinned host tensors, made by the
+    # client (``prepare``); the server makes them itself when absent
+    inputs: tuple = None
     # results
     sensitivity: float = None
     objective: float = None
@@ -75,6 +78,19 @@ class Request:
     @property
     def latency(self):
         return None if self.t_done is None else self.t_done - self.arrival
+
+
+def prepare(requests, library):
+    """Client side: the payload of each request (seeded initial state and source perturbation,
+    ``request_inputs``) as FP64 tensors in pinned host memory, so the server's copies to the
+    device are asynchronous."""
+    torch = _torch()
+    for r in requests:
+        if r.inputs is None:
+            state, dS = request_inputs(library.get(r.key), r.seed)
+            pin = lambda a: torch.as_tensor(np.ascontiguousarray(a, np.float64)).pin_memory()
+            r.inputs = ([pin(a) for a in state], [pin(a) for a in dS])
+    return requests
 
 
 def request_inputs(case, seed):
@@ -161,14 +177,18 @@ class Slot(object):
 
     # ---- a request's work as a list of small host closures, run one per engine pass
     def start(self, req, state, dS):
+        """state, dS: host arrays, or pinned host tensors (copied asynchronously)."""
         torch = _torch()
         self.req = req
         self.busy = True
+        host = lambda v: v if isinstance(v, torch.Tensor) else torch.as_tensor(np.ascontiguousarray(v, np.float64))
         with torch.cuda.stream(self.stream):
             for t, v in zip(self.x, state):
-                t.copy_(torch.as_tensor(np.ascontiguousarray(v), dtype=self.td), non_blocking=False)
+                v = host(v)
+                t.copy_(v, non_blocking=v.is_pinned())
             for t, v in zip(self.dS, dS):
-                t.copy_(torch.as_tensor(np.ascontiguousarray(v), dtype=torch.float64))
+                v = host(v)
+                t.copy_(v, non_blocking=v.is_pinned())
             for t in self.a:
                 t.zero_()
             self.acc.zero_()
@@ -306,7 +326,7 @@ class SensitivityServer(object):
                 if s is None:
                     break
                 waiting.popleft()
-                state, dS = request_inputs(s.case, r.seed)
+                state, dS = r.inputs if r.inputs is not None else request_inputs(s.case, r.seed)
                 s.start(r, state, dS)
                 r.t_admit = time.perf_counter() - t0
                 active.append(s)
@@ -350,7 +370,7 @@ def plain_one_at_a_time(requests, library, device=0, nPrimal=100):
         tr = time.perf_counter()
         case = library.get(r.key)
         rcf = ctxs[r.key]
-        state, dS = request_inputs(case, r.seed)
+        state, dS = r.inputs if r.inputs is not None else request_inputs(case, r.seed)
         x = [torch.as_tensor(a).cuda(device) for a in state]
         d = [torch.as_tensor(a).cuda(device) for a in dS]
         states = [x]

@@ -82,7 +82,7 @@ STEP_BYTES = {('primal', 8): 2904, ('primal', 4): 1524, ('adjoint', 8): 6288, ('
 # the 64^3 box (798,720 faces, 262,144 cells; profiles/), scaled to a launch of the benchmarked
 # mesh by its number of faces (the kernel's traffic grows in proportion to the faces)
 MEASURED_TRAFFIC = {('k_flux', 8): (172.68e6, 798720), ('k_flux', 4): (81.56e6, 798720),
-                    ('k_adj_flux', 8): (407.63e6, 798720)}
+                    ('k_adj_flux', 8): (407.63e6, 798720), ('k_adj_flux', 4): (170.37e6, 798720)}
 # FP64 thread instructions per face (DADD, DMUL, DFMA) of a launch in the same captures
 # (smsp__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on)
 MEASURED_FP64_INST = {'k_flux': (76.0, 149.4, 186.9), 'k_adj_flux': (108.0, 307.9, 456.9)}
@@ -452,14 +452,19 @@ def serving_bench(local, lams=SERVING_LAMBDAS, seed=4, n_mix=48, window_s=6.0, p
     srv.warm(ks)
     srv.warm(keys)
     # plain FP64: one request per mesh, timed one by one
-    probe = [serving.Request(rid=1000 + i, key=k, seed=1000 + i, nPrimal=100) for i, k in enumerate(keys)]
+    # request payloads (initial state, source perturbation) are the clients' work: made before
+    # the clocks of both forms start
+    probe = serving.prepare([serving.Request(rid=1000 + i, key=k, seed=1000 + i, nPrimal=100)
+                             for i, k in enumerate(keys)], lib)
     sp = serving.plain_one_at_a_time(probe, lib, device=local, nPrimal=100)
     t_plain = dict(zip(keys, sp['seconds_per_request']))
     plain_mix_s = sum(t_plain[k] for k in ks)
     # served: the same mix all at once, then the same probe requests for accuracy
-    mix = [serving.Request(rid=i, key=k, seed=i, nPrimal=100, arrival=0.0) for i, k in enumerate(ks)]
+    mix = serving.prepare([serving.Request(rid=i, key=k, seed=i, nPrimal=100, arrival=0.0)
+                           for i, k in enumerate(ks)], lib)
     sm = srv.serve(mix, realtime=False)
-    same = [serving.Request(rid=1000 + i, key=k, seed=1000 + i, nPrimal=100, arrival=0.0) for i, k in enumerate(keys)]
+    same = serving.prepare([serving.Request(rid=1000 + i, key=k, seed=1000 + i, nPrimal=100, arrival=0.0)
+                            for i, k in enumerate(keys)], lib)
     srv.serve(same, realtime=False)
     rel = lambda rs: {a.key: float('%.3g' % (abs(a.sensitivity - b.sensitivity) / abs(b.sensitivity)))
                       for a, b in zip(rs, probe)}
@@ -468,8 +473,8 @@ def serving_bench(local, lams=SERVING_LAMBDAS, seed=4, n_mix=48, window_s=6.0, p
     for lam in lams:
         nr = int(min(n_mix, max(8, round(window_s * lam))))
         t = np.cumsum(gaps[:nr] / lam)
-        reqs = [serving.Request(rid=i, key=k, seed=i, nPrimal=100, arrival=float(a))
-                for i, (k, a) in enumerate(zip(ks[:nr], t))]
+        reqs = serving.prepare([serving.Request(rid=i, key=k, seed=i, nPrimal=100, arrival=float(a))
+                                for i, (k, a) in enumerate(zip(ks[:nr], t))], lib)
         st = srv.serve(reqs, realtime=True)
         sweep.append({'lambda': lam, 'requests': nr, 'req_per_s': round(st['req_per_s'], 3),
                       'p50_s': round(st['p50_s'], 4), 'p99_s': round(st['p99_s'], 4)})
@@ -482,10 +487,11 @@ def serving_bench(local, lams=SERVING_LAMBDAS, seed=4, n_mix=48, window_s=6.0, p
                                         hbm_budget=120e9, max_slots=64)
         s32.warm(ks)
         s32.warm(keys)
-        mix32 = [serving.Request(rid=i, key=k, seed=i, nPrimal=100, arrival=0.0) for i, k in enumerate(ks)]
+        mix32 = serving.prepare([serving.Request(rid=i, key=k, seed=i, nPrimal=100, arrival=0.0)
+                                 for i, k in enumerate(ks)], lib)
         sm32 = s32.serve(mix32, realtime=False)
-        same32 = [serving.Request(rid=1000 + i, key=k, seed=1000 + i, nPrimal=100, arrival=0.0)
-                  for i, k in enumerate(keys)]
+        same32 = serving.prepare([serving.Request(rid=1000 + i, key=k, seed=1000 + i, nPrimal=100, arrival=0.0)
+                                  for i, k in enumerate(keys)], lib)
         s32.serve(same32, realtime=False)
         e32 = rel(same32)
         other = {'precision': compare, 'served_req_per_s': round(n_mix / sm32['elapsed_s'], 3),
