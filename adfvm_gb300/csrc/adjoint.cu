@@ -73,10 +73,9 @@ __global__ void __launch_bounds__(FLUX_BLOCK, sizeof(R) == 8 ? 3 : 4) k_adj_flux
     }
 }
 
+// one cell's sum of its faces' adjoint records (and of the ghosts whose gradient is its own)
 template <typename R>
-__global__ void __launch_bounds__(BLOCK) k_adj_cell1(MeshDev<R> m, const R* __restrict__ fadj, R* __restrict__ cbar) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= m.nIC) return;
+__device__ __forceinline__ void adj_cell_gather(const MeshDev<R>& m, const R* __restrict__ fadj, int c, R* row) {
     const size_t n = m.nIC;
     R acc[CBAR];
     for (int k = 0; k < CBAR; k++) acc[k] = R(0);
@@ -94,9 +93,19 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell1(MeshDev<R> m, const R* __re
         const R* r = fadj + (size_t)(m.nIF + g) * FADJ;
         for (int k = 0; k < 15; k++) acc[5 + k] += r[25 + k];
     }
-    R* out = cbar + (size_t)c * CBAR;
-    for (int k = 0; k < CBAR; k++) out[k] = acc[k];
+    for (int k = 0; k < CBAR; k++) row[k] = acc[k];
 }
+
+template <typename R>
+__global__ void __launch_bounds__(BLOCK) k_adj_cell1(MeshDev<R> m, const R* __restrict__ fadj, R* __restrict__ cbar) {
+    __shared__ R stage[BLOCK * (CBAR + 1)];
+    const int c0 = blockIdx.x * BLOCK;
+    const int c = c0 + threadIdx.x;
+    if (c < m.nIC) adj_cell_gather<R>(m, fadj, c, stage + threadIdx.x * (CBAR + 1));
+    __syncthreads();
+    if (c0 < m.nIC) store_staged<R, CBAR, BLOCK>(cbar, c0, min(BLOCK, m.nIC - c0), stage);
+}
+
 
 // phiFbar_i = rv * sum_j G[i][j] sn_j  (transpose of grad += phiF (x) S N', scaled by 1/V)
 template <typename R>

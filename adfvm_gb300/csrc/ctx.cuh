@@ -17,6 +17,21 @@ constexpr int BLOCK = 256;
 // 10.52 ms, FP32 k_flux 0.240 -> 0.217 ms.
 constexpr int FLUX_BLOCK = 128;
 
+// Writes the W-value records a block of NT threads staged in shared memory (row r at
+// stage + r (W + 1); the padding keeps the staging stores free of bank conflicts) to
+// out[(first + r) W + k] for the block's nValid rows, as contiguous runs of the output. A thread
+// storing its own W-value record at a W-value stride would make each scalar store a separate L2
+// write request into a partly written sector. Callers __syncthreads() before.
+template <typename T, int W, int NT>
+__device__ __forceinline__ void store_staged(T* __restrict__ out, size_t first, int nValid,
+                                             const T* __restrict__ stage) {
+    T* o = out + first * W;
+    for (int i = threadIdx.x; i < nValid * W; i += NT) {
+        int r = i / W;
+        o[i] = stage[r * (W + 1) + (i - r * W)];
+    }
+}
+
 // boundary-condition kind codes stored per ghost cell (3 bits per field: U, T, p)
 constexpr int GK_COPY = 0;     // zeroGradient / empty / cyclic: value of the source cell
 constexpr int GK_FIXED = 1;    // fixedValue or CBC_UPT: stored value

@@ -116,9 +116,7 @@ __global__ void __launch_bounds__(BLOCK) k_prim(MeshDev<R> m, Phys P, const S* _
 }
 
 template <typename R>
-__global__ void __launch_bounds__(BLOCK) k_grad(MeshDev<R> m, R* __restrict__ rec) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= m.nIC) return;
+__device__ __forceinline__ void grad_cell(const MeshDev<R>& m, const R* __restrict__ rec, int c, R* row) {
     const R* rc = rec + (size_t)c * REC;
     R phic[5];
     for (int k = 0; k < 5; k++) phic[k] = rc[k];
@@ -138,23 +136,41 @@ __global__ void __launch_bounds__(BLOCK) k_grad(MeshDev<R> m, R* __restrict__ re
             for (int j = 0; j < 3; j++) g[3 * i + j] = g[3 * i + j] + phiF[i] * sn[j];
     }
     R rv = m.rvol[c];
-    R* out = rec + (size_t)c * REC + R_GU;
-    for (int k = 0; k < 15; k++) out[k] = g[k] * rv;
+    for (int k = 0; k < 5; k++) row[k] = phic[k];
+    for (int k = 0; k < 15; k++) row[R_GU + k] = g[k] * rv;
 }
+
+// the cell's whole record (its primitives again, then the gradients) is staged and the block's
+// records written contiguously
+template <typename R>
+__global__ void __launch_bounds__(BLOCK) k_grad(MeshDev<R> m, R* __restrict__ rec) {
+    __shared__ R stage[BLOCK * (REC + 1)];
+    const int c0 = blockIdx.x * BLOCK;
+    const int c = c0 + threadIdx.x;
+    if (c < m.nIC) grad_cell<R>(m, rec, c, stage + threadIdx.x * (REC + 1));
+    __syncthreads();
+    if (c0 < m.nIC) store_staged<R, REC, BLOCK>(rec, c0, min(BLOCK, m.nIC - c0), stage);
+}
+
 
 template <typename R>
 __global__ void __launch_bounds__(FLUX_BLOCK, sizeof(R) == 8 ? 3 : 8) k_flux(MeshDev<R> m, Phys P, const R* __restrict__ rec,
                                                 R* __restrict__ fflux, int inviscid) {
-    int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= m.nF) return;
-    int kind = (f < m.nIF) ? FACE_INTERNAL : (int)m.fkind[f - m.nIF];
-    FaceIn<R> in;
-    load_face<R>(m, rec, f, in);
-    R F[5], maxaF;
-    face_flux<R>(P, kind, inviscid != 0, in, F, maxaF);
-    R* out = fflux + (size_t)f * FREC;
-    for (int k = 0; k < 5; k++) out[k] = F[k];
-    out[5] = maxaF;
+    __shared__ R stage[FLUX_BLOCK * (FREC + 1)];
+    const int f0 = blockIdx.x * FLUX_BLOCK;
+    const int f = f0 + threadIdx.x;
+    if (f < m.nF) {
+        int kind = (f < m.nIF) ? FACE_INTERNAL : (int)m.fkind[f - m.nIF];
+        FaceIn<R> in;
+        load_face<R>(m, rec, f, in);
+        R F[5], maxaF;
+        face_flux<R>(P, kind, inviscid != 0, in, F, maxaF);
+        R* row = stage + threadIdx.x * (FREC + 1);
+        for (int k = 0; k < 5; k++) row[k] = F[k];
+        row[5] = maxaF;
+    }
+    __syncthreads();
+    store_staged<R, FREC, FLUX_BLOCK>(fflux, f0, min(FLUX_BLOCK, m.nF - f0), stage);
 }
 
 // Gather of the face fluxes (op.div / op.absDiv, op.py:12-29, collated in the order of
