@@ -126,7 +126,9 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const
     if (c >= m.nIC) return;
     const size_t n = m.nIC;
     const size_t nF = m.nF;
-    const R* cb = cbar + (size_t)c * CBAR;
+    // cell adjoint records in 16-byte loads (a record is 80 / 160 bytes, 16-byte aligned)
+    R cb[CBAR];
+    load_vec(cbar + (size_t)c * CBAR, cb, CBAR);
     R pbar[5];
     for (int k = 0; k < 5; k++) pbar[k] = cb[k];
     const R* G = cb + 5;
@@ -142,8 +144,9 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const
         if (nb < m.nIC) {
             // neighbour's gradient: its slot for this face has S N'' = -S N' and weight gwb
             R msn[3] = {-sn[0], -sn[1], -sn[2]};
-            R pn[5];
-            phi_bar<R>(cbar + (size_t)nb * CBAR + 5, msn, m.rvol[nb], pn);
+            R pn[5], cn[CBAR];
+            load_vec(cbar + (size_t)nb * CBAR, cn, CBAR);
+            phi_bar<R>(cn + 5, msn, m.rvol[nb], pn);
             R wb = m.gwb[s * n + c];
             for (int k = 0; k < 5; k++) pbar[k] += wb * pn[k];
         }

@@ -117,9 +117,11 @@ __global__ void __launch_bounds__(BLOCK) k_prim(MeshDev<R> m, Phys P, const S* _
 
 template <typename R>
 __device__ __forceinline__ void grad_cell(const MeshDev<R>& m, const R* __restrict__ rec, int c, R* row) {
-    const R* rc = rec + (size_t)c * REC;
+    // the five primitives of a record as one 16-byte load and a scalar (records are 16-byte
+    // aligned)
     R phic[5];
-    for (int k = 0; k < 5; k++) phic[k] = rc[k];
+    load_vec(rec + (size_t)c * REC, phic, 4);
+    phic[4] = rec[(size_t)c * REC + 4];
     R g[15];
     for (int k = 0; k < 15; k++) g[k] = R(0);
     const size_t n = m.nIC;
@@ -129,7 +131,9 @@ __device__ __forceinline__ void grad_cell(const MeshDev<R>& m, const R* __restri
         R w = m.gw[s * n + c];
         R omw = -w + R(1);
         R sn[3] = {m.gsn[(3 * s) * n + c], m.gsn[(3 * s + 1) * n + c], m.gsn[(3 * s + 2) * n + c]};
-        const R* rn = rec + (size_t)nb * REC;
+        R rn[5];
+        load_vec(rec + (size_t)nb * REC, rn, 4);
+        rn[4] = rec[(size_t)nb * REC + 4];
         R phiF[5];
         for (int k = 0; k < 5; k++) phiF[k] = phic[k] * omw + rn[k] * w;
         for (int i = 0; i < 5; i++)
@@ -156,21 +160,19 @@ __global__ void __launch_bounds__(BLOCK) k_grad(MeshDev<R> m, R* __restrict__ re
 template <typename R>
 __global__ void __launch_bounds__(FLUX_BLOCK, sizeof(R) == 8 ? 3 : 8) k_flux(MeshDev<R> m, Phys P, const R* __restrict__ rec,
                                                 R* __restrict__ fflux, int inviscid) {
-    __shared__ R stage[FLUX_BLOCK * (FREC + 1)];
-    const int f0 = blockIdx.x * FLUX_BLOCK;
-    const int f = f0 + threadIdx.x;
-    if (f < m.nF) {
-        int kind = (f < m.nIF) ? FACE_INTERNAL : (int)m.fkind[f - m.nIF];
-        FaceIn<R> in;
-        load_face<R>(m, rec, f, in);
-        R F[5], maxaF;
-        face_flux<R>(P, kind, inviscid != 0, in, F, maxaF);
-        R* row = stage + threadIdx.x * (FREC + 1);
-        for (int k = 0; k < 5; k++) row[k] = F[k];
-        row[5] = maxaF;
-    }
-    __syncthreads();
-    store_staged<R, FREC, FLUX_BLOCK>(fflux, f0, min(FLUX_BLOCK, m.nF - f0), stage);
+    // (the 6-value face records are stored directly: staging them through shared memory, as
+    // the 20- and 40-value records are, made this kernel slower - 0.217 -> 0.269 ms at 128^3 in
+    // FP32 - the barrier costs more than the six partly coalesced stores)
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= m.nF) return;
+    int kind = (f < m.nIF) ? FACE_INTERNAL : (int)m.fkind[f - m.nIF];
+    FaceIn<R> in;
+    load_face<R>(m, rec, f, in);
+    R F[5], maxaF;
+    face_flux<R>(P, kind, inviscid != 0, in, F, maxaF);
+    R* out = fflux + (size_t)f * FREC;
+    for (int k = 0; k < 5; k++) out[k] = F[k];
+    out[5] = maxaF;
 }
 
 // Gather of the face fluxes (op.div / op.absDiv, op.py:12-29, collated in the order of
