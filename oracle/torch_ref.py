@@ -377,8 +377,10 @@ class Problem(object):
             sideOwn = self.accOwnerSide[:, k:k + 1]
             Ff = F[f]
             wpf = self.wp[f]
-            wnf = torch.where(f < self.nIF, f, torch.zeros_like(f))
-            wnf = self.wnAbs[wnf]
+            if self.nIF > 0:
+                wnf = self.wnAbs[torch.where(f < self.nIF, f, torch.zeros_like(f))]
+            else:                                         # no internal faces: owner sides only
+                wnf = torch.zeros_like(wpf)
             w = torch.where(sideOwn, wpf, wnf)
             c5 = Ff[:, :5] * w
             c5 = torch.where(sideOwn, c5, -c5)            # phi*(-A/V_R) == -(phi*(A/V_R))

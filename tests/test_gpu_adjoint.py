@@ -215,3 +215,21 @@ def test_vane_objective_adjoint_with_heat_term(nx, ny, b, ref):
     a0 = rcf.adjoint_step(d[0], d[1], d[2], case.dt, [t.cuda() for t in z], obja=1.0)
     for i in range(3):
         assert G.rel_err(a0[i].cpu().numpy(), ref0[i].numpy()) < 1e-11, i
+
+
+@pytest.mark.parametrize('name', ['sod1', 'box1', 'box2', 'vane2x1', 'cyl4x2'])
+def test_tiny_meshes_adjoint_matches_autograd(name):
+    """The adjoint step on the smallest meshes (one cell cyclic to itself, ...) within 1e-11 of
+    the oracle's autograd VJP."""
+    from tests.test_oracle_c import TINY
+    case = TINY[name]()
+    mesh = case.build_mesh()
+    x = [torch.as_tensor(np.asarray(a)) for a in cases.conservative(case)]
+    prob = torch_ref.Problem(mesh, case.bc, case.config, case.objective)
+    seeds = _seeds(x, 11)
+    ref = torch_ref.vjp_step(prob, x[0], x[1], x[2], case.dt, None, seeds, obja=1.0)
+    rcf = RCF(mesh, case.bc, objective=case.objective, **case.config)
+    a = rcf.adjoint_step(*[t.cuda() for t in x], case.dt, [t.cuda() for t in seeds], obja=1.0)
+    for i in range(3):
+        e = G.rel_err(a[i].cpu().numpy(), ref[i].numpy())
+        assert e < 1e-11, (name, i, e)

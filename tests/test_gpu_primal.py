@@ -8,9 +8,11 @@ import numpy as np
 import pytest
 import torch
 
+from adfvm_gb300 import cases
 from adfvm_gb300.solver import RCF
 from oracle import torch_ref
 from tests import golden_cases as G
+from tests.test_oracle_c import TINY
 
 pytestmark = pytest.mark.gpu
 
@@ -115,3 +117,25 @@ def test_map_signature_matches_reference_inputs():
     assert not np.array_equal(out[2], out2[2])
     out3 = rcf.map(*inputs)
     assert np.array_equal(out[2], out3[2])
+
+
+@pytest.mark.parametrize('name', sorted(TINY))
+def test_tiny_meshes_against_oracle(name):
+    """One cell (no internal face; a periodic cube cyclic to itself), two cells, a one-cell-thick
+    channel, the smallest O-grid: FP64 within 1e-12 of the oracle; FP32 and mixed run and stay
+    within their one-step bounds."""
+    case = TINY[name]()
+    mesh = case.build_mesh()
+    x = [np.asarray(a) for a in cases.conservative(case)]
+    ref = torch_ref.Problem(mesh, case.bc, case.config, case.objective).step(
+        *[torch.as_tensor(a) for a in x], case.dt)
+    for precision, tol in (('fp64', 1e-12), ('fp32', 1e-5), ('mixed', 1e-6)):
+        rcf = RCF(mesh, case.bc, objective=case.objective, precision=precision, **case.config)
+        td = torch.float32 if precision == 'fp32' else torch.float64
+        d = [torch.as_tensor(a).to(td).cuda() for a in x]
+        out = rcf.step(d[0], d[1], d[2], case.dt)
+        for i in range(3):
+            e = G.rel_err(out[i].double().cpu().numpy(), ref[i].numpy())
+            assert e < tol, (name, precision, i, e)
+        assert abs(out[3] - float(ref[3])) <= max(tol, 1e-12) * abs(float(ref[3])), (name, precision)
+        rcf.close()

@@ -2,6 +2,7 @@
 import numpy as np
 import pytest
 
+from adfvm_gb300 import cases
 from oracle.c_ref import COracle
 from tests import golden_cases as G
 
@@ -34,3 +35,27 @@ def test_c_oracle_matches_reference_trajectory(name):
     rec = np.array(rec)
     for k in range(3):
         assert G.rel_err(rec[:, k], g['record'][:, k]) < 1e-12
+
+
+# edge cases of the mesh: one cell (no internal face; a periodic cube whose six faces are cyclic
+# to itself), two cells, a one-cell-thick channel, the smallest O-grid
+TINY = {'sod1': lambda: cases.sod(1), 'sod2': lambda: cases.sod(2), 'box1': lambda: cases.box(1),
+        'box2': lambda: cases.box(2), 'vane2x1': lambda: cases.vane_channel(2, 1),
+        'cyl4x2': lambda: cases.cylinder(4, 2)}
+
+
+@pytest.mark.parametrize('name', sorted(TINY))
+def test_tiny_meshes_c_oracle_equals_torch_oracle(name):
+    """Both oracles agree to 1e-12 on the smallest meshes."""
+    import torch
+    from oracle import torch_ref
+    case = TINY[name]()
+    mesh = case.build_mesh()
+    x = [np.asarray(a) for a in cases.conservative(case)]
+    r0 = torch_ref.Problem(mesh, case.bc, case.config, case.objective).step(
+        *[torch.as_tensor(a) for a in x], case.dt)
+    r1 = COracle(mesh, case.bc, case.config, case.objective).step(x[0], x[1], x[2], case.dt, None)
+    for i in range(3):
+        assert G.rel_err(r1[i], r0[i].numpy()) < 1e-12, (name, i)
+    assert abs(r1[3] - float(r0[3])) <= 1e-12 * abs(float(r0[3]))
+    assert abs(r1[4] - float(r0[4])) <= 1e-12 * max(1.0, abs(float(r0[4])))
