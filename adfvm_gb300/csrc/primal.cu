@@ -68,6 +68,18 @@ __device__ __forceinline__ void load_prim<float, double>(const Phys& P, const do
     for (int k = 0; k < 5; k++) out[k] = (float)v[k];
 }
 
+// the five primitives at the head of a 16-byte aligned record: a 16-byte store and a scalar
+// (two L2 write requests a cell instead of five)
+__device__ __forceinline__ void store_prims(float* r, const float* v) {
+    *reinterpret_cast<float4*>(r) = make_float4(v[0], v[1], v[2], v[3]);
+    r[4] = v[4];
+}
+__device__ __forceinline__ void store_prims(double* r, const double* v) {
+    *reinterpret_cast<double2*>(r) = make_double2(v[0], v[1]);
+    *reinterpret_cast<double2*>(r + 2) = make_double2(v[2], v[3]);
+    r[4] = v[4];
+}
+
 template <typename R, typename S>
 __global__ void __launch_bounds__(BLOCK) k_prim(MeshDev<R> m, Phys P, const S* __restrict__ rho,
                                                 const S* __restrict__ rhoU, const S* __restrict__ rhoE,
@@ -76,8 +88,7 @@ __global__ void __launch_bounds__(BLOCK) k_prim(MeshDev<R> m, Phys P, const S* _
     if (t < m.nIC) {
         R v[5];
         load_prim<R, S>(P, rho, rhoU, rhoE, t, v);
-        R* r = rec + (size_t)t * REC;
-        for (int k = 0; k < 5; k++) r[k] = v[k];
+        store_prims(rec + (size_t)t * REC, v);
         return;
     }
     int g = t - m.nIC;
@@ -97,8 +108,7 @@ __global__ void __launch_bounds__(BLOCK) k_prim(MeshDev<R> m, Phys P, const S* _
         for (int k = 0; k < 3; k++) v[k] = Un * d[k];
         v[3] = Tt - R(0.5) * Un * Un / consts<R>(P).Cp;
         v[4] = pt * pow(T / Tt, consts<R>(P).ggm1);
-        R* r = rec + (size_t)t * REC;
-        for (int k = 0; k < 5; k++) r[k] = v[k];
+        store_prims(rec + (size_t)t * REC, v);
         return;
     }
     if (kU == GK_FIXED) {
@@ -111,8 +121,7 @@ __global__ void __launch_bounds__(BLOCK) k_prim(MeshDev<R> m, Phys P, const S* _
     }
     if (kT == GK_FIXED) v[3] = m.gval[3 * (size_t)m.nG + g];
     if (kp == GK_FIXED) v[4] = m.gval[4 * (size_t)m.nG + g];
-    R* r = rec + (size_t)t * REC;
-    for (int k = 0; k < 5; k++) r[k] = v[k];
+    store_prims(rec + (size_t)t * REC, v);
 }
 
 template <typename R>
@@ -175,6 +184,23 @@ __global__ void __launch_bounds__(FLUX_BLOCK, sizeof(R) == 8 ? 3 : 8) k_flux(Mes
     out[5] = maxaF;
 }
 
+// a 6-value face flux record in three 8- (FP32) or 16-byte (FP64) loads; records start on
+// multiples of 24 / 48 bytes
+__device__ __forceinline__ void load_flux_record(const float* __restrict__ p, float* o) {
+#pragma unroll
+    for (int i = 0; i < FREC; i += 2) {
+        float2 v = __ldg(reinterpret_cast<const float2*>(p + i));
+        o[i] = v.x; o[i + 1] = v.y;
+    }
+}
+__device__ __forceinline__ void load_flux_record(const double* __restrict__ p, double* o) {
+#pragma unroll
+    for (int i = 0; i < FREC; i += 2) {
+        double2 v = __ldg(reinterpret_cast<const double2*>(p + i));
+        o[i] = v.x; o[i + 1] = v.y;
+    }
+}
+
 // Gather of the face fluxes (op.div / op.absDiv, op.py:12-29, collated in the order of
 // density.py:390-402) and the SSP-RK3 stage update (timestep.py:35-45).
 template <typename R, typename S, int STAGE>
@@ -200,7 +226,8 @@ __global__ void __launch_bounds__(BLOCK) k_update(MeshDev<R> m, const R* __restr
             R w = m.accw[k * n + c];
             bool ownerSide = e >= 0;
             int f = ownerSide ? e : ~e;
-            const R* F = fflux + (size_t)f * FREC;
+            R F[FREC];
+            load_flux_record(fflux + (size_t)f * FREC, F);
             for (int q = 0; q < 5; q++) {
                 S t = (S)F[q] * (S)w;
                 res[q] = res[q] + (ownerSide ? t : -t);
