@@ -204,9 +204,12 @@ template <typename R, typename S = R>
 void launch_prim(Ctx* c, const S* r, const S* ru, const S* re, cudaStream_t s);
 template <typename R, typename S = R>
 void launch_prim_grad(Ctx* c, const S* r, const S* ru, const S* re, cudaStream_t s);
+// nextPrims: the update also writes the primitives of the state it produces into the cell
+// records (the next stage's k_prim, fused)
 template <typename R, typename S = R>
 void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const S* const* u0, const S* const* u1,
-                        const S* const* u2, const S* Sr, const S* Su, const S* Se, S* const* out, cudaStream_t s);
+                        const S* const* u2, const S* Sr, const S* Su, const S* Se, S* const* out, cudaStream_t s,
+                        bool nextPrims = false);
 template <typename S>
 void default_sources(Ctx* c, const S*& Srho, const S*& SrhoU, const S*& SrhoE);
 static inline int nblocks(long long n) { return (int)((n + BLOCK - 1) / BLOCK); }

@@ -43,29 +43,27 @@ __device__ __noinline__ void primitive_f(const Phys& P, float rho, float r0, flo
     out[3] = (float)(rhoe * (double)rr * P.rCv);
 }
 
-// primitives of cell c from the state (element type S) into the record type R
-template <typename R, typename S>
-__device__ __forceinline__ void load_prim(const Phys& P, const S* rho, const S* rhoU, const S* rhoE, int c, R* out);
-
-template <>
-__device__ __forceinline__ void load_prim<double, double>(const Phys& P, const double* rho, const double* rhoU,
-                                                          const double* rhoE, int c, double* out) {
-    primitive_d(P, rho[c], rhoU[3 * c], rhoU[3 * c + 1], rhoU[3 * c + 2], rhoE[c], out);
+// primitives of one state (element type S) into the record type R
+__device__ __forceinline__ void prim_values(const Phys& P, double r, double u0, double u1, double u2, double e,
+                                            double* out) {
+    primitive_d(P, r, u0, u1, u2, e, out);
 }
-
-template <>
-__device__ __forceinline__ void load_prim<float, float>(const Phys& P, const float* rho, const float* rhoU,
-                                                        const float* rhoE, int c, float* out) {
-    primitive_f(P, rho[c], rhoU[3 * c], rhoU[3 * c + 1], rhoU[3 * c + 2], rhoE[c], out);
+__device__ __forceinline__ void prim_values(const Phys& P, float r, float u0, float u1, float u2, float e,
+                                            float* out) {
+    primitive_f(P, r, u0, u1, u2, e, out);
 }
-
 // FP64 state, FP32 record: the primitives in double, then rounded once
-template <>
-__device__ __forceinline__ void load_prim<float, double>(const Phys& P, const double* rho, const double* rhoU,
-                                                         const double* rhoE, int c, float* out) {
+__device__ __forceinline__ void prim_values(const Phys& P, double r, double u0, double u1, double u2, double e,
+                                            float* out) {
     double v[5];
-    primitive_d(P, rho[c], rhoU[3 * c], rhoU[3 * c + 1], rhoU[3 * c + 2], rhoE[c], v);
+    primitive_d(P, r, u0, u1, u2, e, v);
     for (int k = 0; k < 5; k++) out[k] = (float)v[k];
+}
+
+// primitives of cell c from the state arrays
+template <typename R, typename S>
+__device__ __forceinline__ void load_prim(const Phys& P, const S* rho, const S* rhoU, const S* rhoE, int c, R* out) {
+    prim_values(P, rho[c], rhoU[3 * c], rhoU[3 * c + 1], rhoU[3 * c + 2], rhoE[c], out);
 }
 
 // the five primitives at the head of a 16-byte aligned record: a 16-byte store and a scalar
@@ -78,6 +76,36 @@ __device__ __forceinline__ void store_prims(double* r, const double* v) {
     *reinterpret_cast<double2*>(r) = make_double2(v[0], v[1]);
     *reinterpret_cast<double2*>(r + 2) = make_double2(v[2], v[3]);
     r[4] = v[4];
+}
+
+// ghost cell g's primitives from its source cell's (v, replaced in place): the boundary
+// conditions of BCs.py:62-184
+template <typename R>
+__device__ __forceinline__ void ghost_prims(const MeshDev<R>& m, const Phys& P, int g, R* v) {
+    int kind = m.gkind[g];
+    int kU = kind & 7, kT = (kind >> 3) & 7, kp = (kind >> 6) & 7;
+    if (kU == GK_TOTALPT) {
+        // CBC_TOTAL_PT (BCs.py:178-184): Un = U.d, Ub = Un d, Tb = Tt - Un^2/(2 Cp),
+        // pb = pt (T/Tt)^(gamma/(gamma-1)) with U, T of the owner cell
+        R d[3] = {m.gval[g], m.gval[(size_t)m.nG + g], m.gval[2 * (size_t)m.nG + g]};
+        R Tt = m.gval[3 * (size_t)m.nG + g], pt = m.gval[4 * (size_t)m.nG + g];
+        R Un = dot3(v, d);
+        R T = v[3];
+        for (int k = 0; k < 3; k++) v[k] = Un * d[k];
+        v[3] = Tt - R(0.5) * Un * Un / consts<R>(P).Cp;
+        v[4] = pt * pow(T / Tt, consts<R>(P).ggm1);
+        return;
+    }
+    if (kU == GK_FIXED) {
+        for (int k = 0; k < 3; k++) v[k] = m.gval[(size_t)k * m.nG + g];
+    } else if (kU == GK_SYM) {
+        int f = m.nIF + g;
+        R n[3] = {m.nrm[f], m.nrm[(size_t)m.nF + f], m.nrm[2 * (size_t)m.nF + f]};
+        R un = dot3(v, n);
+        for (int k = 0; k < 3; k++) v[k] = v[k] - un * n[k];
+    }
+    if (kT == GK_FIXED) v[3] = m.gval[3 * (size_t)m.nG + g];
+    if (kp == GK_FIXED) v[4] = m.gval[4 * (size_t)m.nG + g];
 }
 
 template <typename R, typename S>
@@ -93,34 +121,9 @@ __global__ void __launch_bounds__(BLOCK) k_prim(MeshDev<R> m, Phys P, const S* _
     }
     int g = t - m.nIC;
     if (g >= m.nG) return;
-    int src = m.gsrc[g];
-    int kind = m.gkind[g];
     R v[5];
-    load_prim<R, S>(P, rho, rhoU, rhoE, src, v);
-    int kU = kind & 7, kT = (kind >> 3) & 7, kp = (kind >> 6) & 7;
-    if (kU == GK_TOTALPT) {
-        // CBC_TOTAL_PT (BCs.py:178-184): Un = U.d, Ub = Un d, Tb = Tt - Un^2/(2 Cp),
-        // pb = pt (T/Tt)^(gamma/(gamma-1)) with U, T of the owner cell
-        R d[3] = {m.gval[g], m.gval[(size_t)m.nG + g], m.gval[2 * (size_t)m.nG + g]};
-        R Tt = m.gval[3 * (size_t)m.nG + g], pt = m.gval[4 * (size_t)m.nG + g];
-        R Un = dot3(v, d);
-        R T = v[3];
-        for (int k = 0; k < 3; k++) v[k] = Un * d[k];
-        v[3] = Tt - R(0.5) * Un * Un / consts<R>(P).Cp;
-        v[4] = pt * pow(T / Tt, consts<R>(P).ggm1);
-        store_prims(rec + (size_t)t * REC, v);
-        return;
-    }
-    if (kU == GK_FIXED) {
-        for (int k = 0; k < 3; k++) v[k] = m.gval[(size_t)k * m.nG + g];
-    } else if (kU == GK_SYM) {
-        int f = m.nIF + g;
-        R n[3] = {m.nrm[f], m.nrm[(size_t)m.nF + f], m.nrm[2 * (size_t)m.nF + f]};
-        R un = dot3(v, n);
-        for (int k = 0; k < 3; k++) v[k] = v[k] - un * n[k];
-    }
-    if (kT == GK_FIXED) v[3] = m.gval[3 * (size_t)m.nG + g];
-    if (kp == GK_FIXED) v[4] = m.gval[4 * (size_t)m.nG + g];
+    load_prim<R, S>(P, rho, rhoU, rhoE, m.gsrc[g], v);
+    ghost_prims<R>(m, P, g, v);
     store_prims(rec + (size_t)t * REC, v);
 }
 
@@ -212,7 +215,7 @@ __global__ void __launch_bounds__(BLOCK) k_update(MeshDev<R> m, const R* __restr
                                                   const S* __restrict__ Sr, const S* __restrict__ Su,
                                                   const S* __restrict__ Se,
                                                   S* outr, S* outu, S* oute,
-                                                  unsigned long long* dtcBits) {
+                                                  unsigned long long* dtcBits, Phys P, R* __restrict__ recNext) {
     // the gather and the update run in the state's type S (double for an FP64 state under
     // FP32 fluxes); the CFL sum in the flux type R
     int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -252,6 +255,20 @@ __global__ void __launch_bounds__(BLOCK) k_update(MeshDev<R> m, const R* __restr
         outr[c] = o[0];
         outu[3 * c] = o[1]; outu[3 * c + 1] = o[2]; outu[3 * c + 2] = o[3];
         oute[c] = o[4];
+        if (recNext) {
+            // the next stage's k_prim, fused: this cell's primitives and those of the ghost
+            // cells whose source it is, from the values just stored (the same bits k_prim
+            // would read back)
+            R v[5];
+            prim_values(P, o[0], o[1], o[2], o[3], o[4], v);
+            store_prims(recNext + (size_t)c * REC, v);
+            for (int q = m.gsStart[c]; q < m.gsStart[c + 1]; q++) {
+                int g = m.gsList[q];
+                R w[5] = {v[0], v[1], v[2], v[3], v[4]};
+                ghost_prims<R>(m, P, g, w);
+                store_prims(recNext + (size_t)(m.nIC + g) * REC, w);
+            }
+        }
     }
     if (STAGE == 1) {
         // reduce_max of the CFL sums (density.py:405-410): warp shuffle, block, then an atomic
@@ -409,7 +426,8 @@ void launch_prim_grad(Ctx* c, const S* r, const S* ru, const S* re, cudaStream_t
 // faces -> fluxes, then the gather + stage update u_{st+1} = ... (timestep.py:35-45)
 template <typename R, typename S>
 void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const S* const* u0, const S* const* u1,
-                        const S* const* u2, const S* Sr, const S* Su, const S* Se, S* const* out, cudaStream_t s) {
+                        const S* const* u2, const S* Sr, const S* Su, const S* Se, S* const* out, cudaStream_t s,
+                        bool nextPrims) {
     const MeshDev<R>& m = meshOf<R>(c);
     const Phys& P = c->phys;
     R* rec = (R*)c->rec;
@@ -420,16 +438,20 @@ void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const S*
         k_flux<R><<<(m.nF + FLUX_BLOCK - 1) / FLUX_BLOCK, FLUX_BLOCK, 0, s>>>(m, P, rec, ff, inviscid);
     }
     int nb = nblocks(m.nIC);
+    R* recNext = nextPrims ? rec : nullptr;
     ProfScope ps(c, KID_UPDATE, s);
     if (st == 0)
         k_update<R, S, 0><<<nb, BLOCK, 0, s>>>(m, ff, dt, dtDev, u0[0], u0[1], u0[2], nullptr, nullptr, nullptr, nullptr,
-                                            nullptr, nullptr, Sr, Su, Se, out[0], out[1], out[2], c->dtcBits);
+                                            nullptr, nullptr, Sr, Su, Se, out[0], out[1], out[2], c->dtcBits, P,
+                                            recNext);
     else if (st == 1)
         k_update<R, S, 1><<<nb, BLOCK, 0, s>>>(m, ff, dt, dtDev, u0[0], u0[1], u0[2], u1[0], u1[1], u1[2], nullptr,
-                                            nullptr, nullptr, Sr, Su, Se, out[0], out[1], out[2], c->dtcBits);
+                                            nullptr, nullptr, Sr, Su, Se, out[0], out[1], out[2], c->dtcBits, P,
+                                            recNext);
     else
         k_update<R, S, 2><<<nb, BLOCK, 0, s>>>(m, ff, dt, dtDev, u0[0], u0[1], u0[2], nullptr, nullptr, nullptr, u2[0],
-                                            u2[1], u2[2], Sr, Su, Se, out[0], out[1], out[2], c->dtcBits);
+                                            u2[1], u2[2], Sr, Su, Se, out[0], out[1], out[2], c->dtcBits, P,
+                                            recNext);
 }
 
 template <typename S>
@@ -461,7 +483,13 @@ int primal_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double d
         return fail(c, AFVM_ERR_BAD_ARG, "AFVM_OBJ_VANE needs afvm_set_objective_vane before the first step");
     for (int st = 0; st < 3; st++) {
         const S* const* in = st == 0 ? u0c : (st == 1 ? u1c : u2c);
-        launch_prim_grad<R, S>(c, in[0], in[1], in[2], s);
+        if (st == 0) {
+            launch_prim_grad<R, S>(c, in[0], in[1], in[2], s);
+        } else {
+            // the primitives of stages 1 and 2 were written by the previous stage's update
+            ProfScope ps(c, KID_GRAD, s);
+            k_grad<R><<<nblocks(m.nIC), BLOCK, 0, s>>>(m, (R*)c->rec);
+        }
         if (st == 1 && c->objective == AFVM_OBJ_VANE) {
             // the partial sums now, while rec holds the stage-1 primitives; combined at the end
             const MeshDev<R>& mm = meshOf<R>(c);
@@ -481,7 +509,7 @@ int primal_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double d
             }
         }
         S* const* out = st == 0 ? u1 : (st == 1 ? u2 : outN);
-        launch_flux_update<R, S>(c, st, dt, dtDev, u0c, u1c, u2c, Srho, SrhoU, SrhoE, out, s);
+        launch_flux_update<R, S>(c, st, dt, dtDev, u0c, u1c, u2c, Srho, SrhoU, SrhoE, out, s, st < 2);
     }
     if (vaneDone) {
         ProfScope ps(c, KID_FINISH, s);
@@ -530,7 +558,8 @@ int primal_run_dev(Ctx* c, S* rho, S* rhoU, S* rhoE, int nSteps, double dt0, dou
     template void launch_prim<R, S>(Ctx*, const S*, const S*, const S*, cudaStream_t);                           \
     template void launch_prim_grad<R, S>(Ctx*, const S*, const S*, const S*, cudaStream_t);                      \
     template void launch_flux_update<R, S>(Ctx*, int, double, const double*, const S* const*, const S* const*,   \
-                                           const S* const*, const S*, const S*, const S*, S* const*, cudaStream_t);
+                                           const S* const*, const S*, const S*, const S*, S* const*, cudaStream_t,  \
+                                           bool);
 AFVM_PRIMAL_INST(double, double)
 AFVM_PRIMAL_INST(float, float)
 AFVM_PRIMAL_INST(float, double)
