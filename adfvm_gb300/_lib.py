@@ -98,6 +98,11 @@ SIGNATURES = {
                                     C.c_double, C.c_double, _v, _v, _v, _v, _v, _v, _v]),
     'afvm_adjoint_step_stages': (C.c_int, [_v, _v, _v, _v, C.c_double, _v, _v, _v, _v, _v, _v, _v,
                                            C.c_double, C.c_double, _v, _v, _v, _v, _v, _v, _v]),
+    'afvm_tape_elements': (C.c_int64, [_v]),
+    'afvm_primal_step_tape': (C.c_int, [_v, _v, _v, _v, C.c_double, _v, _v, _v, _v, _v, _v, _v, _v,
+                                        C.POINTER(C.c_double), C.POINTER(C.c_double), _v]),
+    'afvm_adjoint_step_tape': (C.c_int, [_v, _v, _v, _v, C.c_double, _v, _v, _v, _v, _v, _v, _v, _v,
+                                         C.c_double, C.c_double, _v, _v, _v, _v, _v, _v, _v]),
     'afvm_sensitivity': (C.c_int, [_v, C.c_int32, C.POINTER(_d), C.POINTER(_d),
                                    C.POINTER(C.c_int64), _d, _v]),
     'afvm_adjoint_energy': (C.c_int, [_v, _v, _v, _v, _v, _v, _v, _d, _v]),

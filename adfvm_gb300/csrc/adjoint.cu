@@ -24,11 +24,13 @@ namespace afvm {
 constexpr int FADJ = 40;
 constexpr int CBAR = 20;   // per cell: primitive adjoint (5) then gradient adjoint (15)
 
-// one face's record of k_adj_flux into row[0..39]
-template <typename R, typename S>
+// one face's record of k_adj_flux into row[0..39]; TAPED: the forward values of a
+// non-boundary face come from its tape column instead of a re-evaluation of the face flux
+template <typename R, typename S, bool TAPED>
 __device__ __forceinline__ void adj_face(const MeshDev<R>& m, const Phys& P, const R* __restrict__ rec, R coef,
                                          const S* __restrict__ ar, const S* __restrict__ au,
-                                         const S* __restrict__ ae, int inviscid, int f, R* row) {
+                                         const S* __restrict__ ae, int inviscid, int f, R* row,
+                                         const R* __restrict__ tape) {
     int kind = (f < m.nIF) ? FACE_INTERNAL : (int)m.fkind[f - m.nIF];
     int iP = m.own[f];
     R wp = m.wpf[f];
@@ -44,26 +46,32 @@ __device__ __forceinline__ void adj_face(const MeshDev<R>& m, const Phys& P, con
         Fb[4] = Fb[4] - (coef * R(ae[iN])) * wn;
     }
     FaceIn<R> in;
-    load_face<R>(m, rec, f, in);
     FaceBar<R> b;
     zero_bar(b);
-    face_vjp<R>(P, kind, inviscid != 0, in, Fb, b);
+    if (TAPED && kind != FACE_BOUNDARY) {
+        load_face_geometry<R>(m, f, in);
+        face_vjp_t<R>(P, kind, inviscid != 0, in, TapeLoad<R>{tape + f, (size_t)m.nF}, Fb, b);
+    } else {
+        load_face<R>(m, rec, f, in);
+        face_vjp<R>(P, kind, inviscid != 0, in, Fb, b);
+    }
     const R* src = &b.UP[0];
     for (int k = 0; k < 5; k++) { row[k] = src[k]; row[20 + k] = src[5 + k]; }
     for (int k = 0; k < 15; k++) { row[5 + k] = src[10 + k]; row[25 + k] = src[25 + k]; }
 }
 
-template <typename R, typename S>
+template <typename R, typename S, bool TAPED>
 __global__ void __launch_bounds__(FLUX_BLOCK, sizeof(R) == 8 ? 3 : 4) k_adj_flux(MeshDev<R> m, Phys P, const R* __restrict__ rec, R coef,
                                                     const S* __restrict__ ar, const S* __restrict__ au,
-                                                    const S* __restrict__ ae, R* __restrict__ fadj, int inviscid) {
+                                                    const S* __restrict__ ae, R* __restrict__ fadj, int inviscid,
+                                                    const R* __restrict__ tape) {
     // the block's 40-value face records are staged here and written out contiguously: one
     // thread's 40 scalar stores at a 40-value stride would touch a new 32-byte sector each and
     // load L2 with eight partial writes per sector
     __shared__ R stage[FLUX_BLOCK * (FADJ + 1)];
     const int f0 = blockIdx.x * FLUX_BLOCK;
     const int f = f0 + threadIdx.x;
-    if (f < m.nF) adj_face<R, S>(m, P, rec, coef, ar, au, ae, inviscid, f, stage + threadIdx.x * (FADJ + 1));
+    if (f < m.nF) adj_face<R, S, TAPED>(m, P, rec, coef, ar, au, ae, inviscid, f, stage + threadIdx.x * (FADJ + 1), tape);
     __syncthreads();
     const int nb = min(FLUX_BLOCK, m.nF - f0);
     R* out = fadj + (size_t)f0 * FADJ;
@@ -292,7 +300,8 @@ __global__ void k_split5(int n, const R* __restrict__ sb, R* r, R* u, R* e) {
 template <typename R, typename S>
 int adjoint_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double dt, const S* Srho, const S* SrhoU,
                      const S* SrhoE, const S* rhoNa, const S* rhoUNa, const S* rhoENa, double obja, S* rhoa,
-                     S* rhoUa, S* rhoEa, S* Srhoa, S* SrhoUa, S* SrhoEa, cudaStream_t s, const S* stages) {
+                     S* rhoUa, S* rhoEa, S* Srhoa, S* SrhoUa, S* SrhoEa, cudaStream_t s, const S* stages,
+                     const R* tape) {
     const MeshDev<R>& m = meshOf<R>(c);
     const Phys& P = c->phys;
     default_sources<S>(c, Srho, SrhoU, SrhoE);
@@ -334,8 +343,13 @@ int adjoint_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double 
         R coef = (R)(-beta[st] * dt);
         {
             ProfScope ps(c, KID_ADJ_FLUX, s);
-            k_adj_flux<R, S><<<(m.nF + FLUX_BLOCK - 1) / FLUX_BLOCK, FLUX_BLOCK, 0, s>>>(m, P, rec, coef, ain[0], ain[1],
-                                                                                   ain[2], fadj, inviscid);
+            int nbF = (m.nF + FLUX_BLOCK - 1) / FLUX_BLOCK;
+            if (tape)
+                k_adj_flux<R, S, true><<<nbF, FLUX_BLOCK, 0, s>>>(m, P, rec, coef, ain[0], ain[1], ain[2], fadj,
+                                                                  inviscid, tape + (size_t)st * TAPE * m.nF);
+            else
+                k_adj_flux<R, S, false><<<nbF, FLUX_BLOCK, 0, s>>>(m, P, rec, coef, ain[0], ain[1], ain[2], fadj,
+                                                                   inviscid, nullptr);
         }
         {
             ProfScope ps(c, KID_ADJ_GATHER, s);
@@ -367,7 +381,7 @@ int adjoint_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double 
 #define AFVM_ADJ_INST(R, S)                                                                                    \
     template int adjoint_step_dev<R, S>(Ctx*, const S*, const S*, const S*, double, const S*, const S*, const S*, \
                                         const S*, const S*, const S*, double, S*, S*, S*, S*, S*, S*,             \
-                                        cudaStream_t, const S*);
+                                        cudaStream_t, const S*, const R*);
 AFVM_ADJ_INST(double, double)
 AFVM_ADJ_INST(float, float)
 AFVM_ADJ_INST(float, double)

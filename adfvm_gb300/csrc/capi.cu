@@ -678,13 +678,19 @@ int afvm_set_bc_value(afvm_ctx* ctx, int32_t patch, int32_t field, const double*
     return AFVM_OK;
 }
 
-int afvm_primal_step_stages(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, double dt,
-                            const void* S_rho, const void* S_rhoU, const void* S_rhoE, void* rhoN, void* rhoUN,
-                            void* rhoEN, void* stages, double* dtc_out, double* obj_out, void* stream) {
+int64_t afvm_tape_elements(const afvm_ctx* ctx) {
+    if (!ctx) return 0;
+    return (int64_t)tape_elements(reinterpret_cast<const Ctx*>(ctx)->nF);
+}
+
+int afvm_primal_step_tape(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, double dt,
+                          const void* S_rho, const void* S_rhoU, const void* S_rhoE, void* rhoN, void* rhoUN,
+                          void* rhoEN, void* stages, void* tape, double* dtc_out, double* obj_out, void* stream) {
     if (!ctx) return AFVM_ERR_BAD_ARG;
     Ctx* c = reinterpret_cast<Ctx*>(ctx);
     if (!rho || !rhoU || !rhoE || !rhoN || !rhoUN || !rhoEN) return fail(c, AFVM_ERR_BAD_ARG, "null state pointer");
     if (!std::isfinite(dt)) return fail(c, AFVM_ERR_BAD_ARG, "non-finite dt");
+    if (tape && !stages) return fail(c, AFVM_ERR_BAD_ARG, "a face tape is kept together with the stage states");
     DeviceGuard dg(c->device);
     cudaStream_t s = (cudaStream_t)stream;
     int st = dispatch(c, [&](auto r, auto sv) {
@@ -692,10 +698,17 @@ int afvm_primal_step_stages(afvm_ctx* ctx, const void* rho, const void* rhoU, co
         using S = decltype(sv);
         return primal_step_dev<R, S>(c, (const S*)rho, (const S*)rhoU, (const S*)rhoE, dt, nullptr, (const S*)S_rho,
                                      (const S*)S_rhoU, (const S*)S_rhoE, (S*)rhoN, (S*)rhoUN, (S*)rhoEN, c->scal,
-                                     c->scal + 1, s, (S*)stages);
+                                     c->scal + 1, s, (S*)stages, (R*)tape);
     });
     if (st) return st;
     return get_results(c, dtc_out, obj_out, s);
+}
+
+int afvm_primal_step_stages(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, double dt,
+                            const void* S_rho, const void* S_rhoU, const void* S_rhoE, void* rhoN, void* rhoUN,
+                            void* rhoEN, void* stages, double* dtc_out, double* obj_out, void* stream) {
+    return afvm_primal_step_tape(ctx, rho, rhoU, rhoE, dt, S_rho, S_rhoU, S_rhoE, rhoN, rhoUN, rhoEN, stages, nullptr,
+                                 dtc_out, obj_out, stream);
 }
 
 int afvm_primal_step(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, double dt,
@@ -781,11 +794,21 @@ int afvm_adjoint_step_stages(afvm_ctx* ctx, const void* rho, const void* rhoU, c
                              const void* rhoNa, const void* rhoUNa, const void* rhoENa, double dtca, double obja,
                              void* rhoa, void* rhoUa, void* rhoEa, void* S_rhoa, void* S_rhoUa, void* S_rhoEa,
                              void* stream) {
+    return afvm_adjoint_step_tape(ctx, rho, rhoU, rhoE, dt, S_rho, S_rhoU, S_rhoE, stages, nullptr, rhoNa, rhoUNa,
+                                  rhoENa, dtca, obja, rhoa, rhoUa, rhoEa, S_rhoa, S_rhoUa, S_rhoEa, stream);
+}
+
+int afvm_adjoint_step_tape(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, double dt,
+                           const void* S_rho, const void* S_rhoU, const void* S_rhoE, const void* stages,
+                           const void* tape, const void* rhoNa, const void* rhoUNa, const void* rhoENa, double dtca,
+                           double obja, void* rhoa, void* rhoUa, void* rhoEa, void* S_rhoa, void* S_rhoUa,
+                           void* S_rhoEa, void* stream) {
     if (!ctx) return AFVM_ERR_BAD_ARG;
     Ctx* c = reinterpret_cast<Ctx*>(ctx);
     if (!rho || !rhoU || !rhoE || !rhoNa || !rhoUNa || !rhoENa || !rhoa || !rhoUa || !rhoEa)
         return fail(c, AFVM_ERR_BAD_ARG, "null pointer");
     if (dtca != 0.0) return fail(c, AFVM_ERR_UNSUPPORTED, "dtca != 0 (the CFL-sum output has no adjoint here)");
+    if (tape && !stages) return fail(c, AFVM_ERR_BAD_ARG, "a face tape is read together with the stage states");
     if (!std::isfinite(dt) || !std::isfinite(obja)) return fail(c, AFVM_ERR_BAD_ARG, "non-finite dt or obja");
     DeviceGuard dg(c->device);
     cudaStream_t s = (cudaStream_t)stream;
@@ -797,7 +820,7 @@ int afvm_adjoint_step_stages(afvm_ctx* ctx, const void* rho, const void* rhoU, c
         return adjoint_step_dev<R, S>(c, (const S*)rho, (const S*)rhoU, (const S*)rhoE, dt, (const S*)S_rho,
                                       (const S*)S_rhoU, (const S*)S_rhoE, (const S*)rhoNa, (const S*)rhoUNa,
                                       (const S*)rhoENa, obja, (S*)rhoa, (S*)rhoUa, (S*)rhoEa, (S*)S_rhoa,
-                                      (S*)S_rhoUa, (S*)S_rhoEa, s, (const S*)stages);
+                                      (S*)S_rhoUa, (S*)S_rhoEa, s, (const S*)stages, (const R*)tape);
     });
 }
 

@@ -175,7 +175,7 @@ int adjoint_viscosity_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, in
 template <typename R, typename S = R>
 int primal_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double dt, const double* dtDev,
                     const S* Srho, const S* SrhoU, const S* SrhoE, S* rhoN, S* rhoUN, S* rhoEN,
-                    double* dtcDev, double* objDev, cudaStream_t s, S* stages = nullptr);
+                    double* dtcDev, double* objDev, cudaStream_t s, S* stages = nullptr, R* tape = nullptr);
 template <typename R, typename S = R>
 int primal_run_dev(Ctx* c, S* rho, S* rhoU, S* rhoE, int nSteps, double dt0, double CFL, double stepFactor,
                    int fixed, const S* Srho, const S* SrhoU, const S* SrhoE, double* dtHist, double* dtcHist,
@@ -187,7 +187,11 @@ int adjoint_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double 
                      const S* Srho, const S* SrhoU, const S* SrhoE,
                      const S* rhoNa, const S* rhoUNa, const S* rhoENa, double obja,
                      S* rhoa, S* rhoUa, S* rhoEa, S* Srhoa, S* SrhoUa, S* SrhoEa, cudaStream_t s,
-                     const S* stages = nullptr);
+                     const S* stages = nullptr, const R* tape = nullptr);
+
+// a step's face tapes: one per RK stage, TAPE values a face each (value k of face f of stage st
+// at tape[(st TAPE + k) nF + f]), written by the primal step and read by its adjoint step
+inline size_t tape_elements(int nF) { return (size_t)3 * TAPE * (size_t)nF; }
 
 // the RK stage states u1, u2 of one step in a caller's buffer of 10 nIC values:
 // u1 = [rho (n) | rhoU (3n) | rhoE (n)], then u2 in the same layout
@@ -206,10 +210,11 @@ template <typename R, typename S = R>
 void launch_prim_grad(Ctx* c, const S* r, const S* ru, const S* re, cudaStream_t s);
 // nextPrims: the update also writes the primitives of the state it produces into the cell
 // records (the next stage's k_prim, fused)
+// tape: the stage's face tape to write (NULL: none)
 template <typename R, typename S = R>
 void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const S* const* u0, const S* const* u1,
                         const S* const* u2, const S* Sr, const S* Su, const S* Se, S* const* out, cudaStream_t s,
-                        bool nextPrims = false);
+                        bool nextPrims = false, R* tape = nullptr);
 template <typename S>
 void default_sources(Ctx* c, const S*& Srho, const S*& SrhoU, const S*& SrhoE);
 static inline int nblocks(long long n) { return (int)((n + BLOCK - 1) / BLOCK); }

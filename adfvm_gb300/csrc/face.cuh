@@ -33,9 +33,11 @@ AFVM_HD void zero_bar(FaceBar<R>& b) {
 template <typename R>
 AFVM_HD R sgn(R x) { return (x > R(0)) ? R(1) : ((x < R(0)) ? R(-1) : R(0)); }
 
-// flux (rho, rhoU, rhoE) through the face and the CFL term |U.n| + a
-template <typename R>
-AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& in, R* F, R& maxaF) {
+// flux (rho, rhoU, rhoE) through the face and the CFL term |U.n| + a; the tape values of a
+// non-boundary face go to tp
+template <typename R, typename Sink = TapeNone>
+AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& in, R* F, R& maxaF,
+                       Sink&& tp = Sink()) {
     R TF, UF[3], gTF[3], gUF[9];
     if (kind == FACE_BOUNDARY) {
         // RCF.boundaryFlux (density.py:307-331) with RCF.getFlux (density.py:184-190)
@@ -53,8 +55,8 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
         for (int k = 0; k < 3; k++) ULF[k] = recon<R>(in.UP[k], in.UN[k], in.gUP + 3 * k, in.lw0, in.qw0);
         TLF = recon<R>(in.TP, in.TN, in.gTP, in.lw0, in.qw0);
         pLF = recon<R>(in.pP, in.pN, in.gpP, in.lw0, in.qw0);
-        R rhoL, rhoUL[3], rhoEL;
-        conservative<R>(P, ULF, TLF, pLF, rhoL, rhoUL, rhoEL);
+        R rhoL, rhoUL[3], rhoEL, rdL, rdR;
+        conservative<R>(P, ULF, TLF, pLF, rhoL, rhoUL, rhoEL, &rdL);
         int solver;
         if (kind == FACE_CHARACTERISTIC) {
             for (int k = 0; k < 3; k++) URF[k] = in.UN[k];
@@ -67,11 +69,14 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
             solver = P.riemann;
         }
         R rhoR, rhoUR[3], rhoER;
-        conservative<R>(P, URF, TRF, pRF, rhoR, rhoUR, rhoER);
+        conservative<R>(P, URF, TRF, pRF, rhoR, rhoUR, rhoER, &rdR);
+        for (int k = 0; k < 3; k++) { tp.put(T_ULF + k, ULF[k]); tp.put(T_URF + k, URF[k]); }
+        tp.put(T_TLF, TLF); tp.put(T_PLF, pLF); tp.put(T_TRF, TRF); tp.put(T_PRF, pRF);
+        tp.put(T_RDL, rdL); tp.put(T_RDR, rdR);
         if (solver == AFVM_RIEMANN_ROE)
-            roe<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, in.N, F);
+            roe<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, in.N, F, tp);
         else
-            laxf<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, rhoUL, rhoUR, rhoEL, rhoER, in.N, F);
+            laxf<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, rhoUL, rhoUR, rhoEL, rhoER, in.N, F, tp);
         if (kind == FACE_CHARACTERISTIC) {
             TF = in.TN;
             for (int k = 0; k < 3; k++) { UF[k] = in.UN[k]; gTF[k] = in.gTN[k]; }
@@ -82,7 +87,7 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
             for (int k = 0; k < 9; k++) gUF[k] = R(0.5) * (in.gUP[k] + in.gUN[k]);
         }
     }
-    if (!inviscid) viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, UF, gTF, gUF, in.D, in.N, in.rdelta, F);
+    if (!inviscid) viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, UF, gTF, gUF, in.D, in.N, in.rdelta, F, tp);
     R aF = sqrt_(consts<R>(P).Cp * TF * consts<R>(P).gm1);
     maxaF = fabs(dot3(UF, in.N)) + aF;
 }
@@ -90,11 +95,11 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
 // ---------------------------------------------------------------------------- adjoints
 
 // RCF.conservative: rho = p/(Cv T (g-1)), rhoU = U rho, rhoE = rho (Cv T + |U|^2/2)
+// (rd = 1/(e (g-1)), the forward's reciprocal)
 template <typename R>
-AFVM_HD void conservative_vjp(const Phys& P, const R* U, R T, R p, R rhob, const R* rhoUb, R rhoEb, R* Ub,
-                              R& Tb, R& pb) {
+AFVM_HD void conservative_vjp_t(const Phys& P, const R* U, R T, R p, R rd, R rhob, const R* rhoUb, R rhoEb,
+                                R* Ub, R& Tb, R& pb) {
     R e = consts<R>(P).Cv * T;
-    R rd = rcp(e * consts<R>(P).gm1);
     R rho = p * rd;
     R q = dot3(U, U);
     for (int k = 0; k < 3; k++) Ub[k] += rhoUb[k] * rho + rhoEb * rho * U[k];
@@ -102,6 +107,13 @@ AFVM_HD void conservative_vjp(const Phys& P, const R* U, R T, R p, R rhob, const
     pb += rhot * rd;
     R eb = -rhot * rho * rcp(e) + rhoEb * rho;
     Tb += eb * consts<R>(P).Cv;
+}
+
+template <typename R>
+AFVM_HD void conservative_vjp(const Phys& P, const R* U, R T, R p, R rhob, const R* rhoUb, R rhoEb, R* Ub,
+                              R& Tb, R& pb) {
+    R rd = rcp(consts<R>(P).Cv * T * consts<R>(P).gm1);
+    conservative_vjp_t<R>(P, U, T, p, rd, rhob, rhoUb, rhoEb, Ub, Tb, pb);
 }
 
 // interp.secondOrder: phiC + (phiD - phiC) lw + qw.g
@@ -112,27 +124,27 @@ AFVM_HD void recon_vjp(R b, R lw, const R* qw, R& phiCb, R& phiDb, R* gb) {
     for (int j = 0; j < 3; j++) gb[j] += b * qw[j];
 }
 
-// riemann.eulerRoe
-template <typename R>
+// riemann.eulerRoe; the forward's reciprocals and reciprocal square roots come from the tape
+template <typename R, typename Src>
 AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR, const R* N, const R* Fb,
-                     R& pLb, R& pRb, R* ULb, R* URb, R& rhoLb, R& rhoRb) {
+                     const Src& t, R& pLb, R& pRb, R* ULb, R* URb, R& rhoLb, R& rhoRb) {
     const R g = consts<R>(P).gamma, gm1 = consts<R>(P).gm1, ggm1 = consts<R>(P).ggm1, h = R(0.5);
     // ---- forward (as roe())
     R UnL = dot3(UL, N), UnR = dot3(UR, N);
     R rhoUnL = rhoL * UnL, rhoUnR = rhoR * UnR;
     R qL = dot3(UL, UL), qR = dot3(UR, UR);
-    R rrL = rcp(rhoL), rrR = rcp(rhoR);
+    R rrL = t.get(T_RRL), rrR = t.get(T_RRR);
     R hL = ggm1 * pL * rrL + h * qL;
     R hR = ggm1 * pR * rrR + h * qR;
-    R rsL = rsqrt_(rhoL), rsR = rsqrt_(rhoR);
+    R rsL = t.get(T_RSL), rsR = t.get(T_RSR);
     R sL = rhoL * rsL, sR = rhoR * rsR;
-    R rD = rcp(sL + sR);
+    R rD = t.get(T_RD);
     R UF[3], dU[3];
     for (int k = 0; k < 3; k++) UF[k] = (UL[k] * sL + UR[k] * sR) * rD;
     R hF = (hL * sL + hR * sR) * rD;
     R qF = h * dot3(UF, UF);
     R a2F = gm1 * (hF - qF);
-    R raF = rsqrt_(a2F);
+    R raF = t.get(T_RAF);
     R aF = a2F * raF;
     R ra2F = raF * raF;
     R UnF = dot3(UF, N);
@@ -142,15 +154,15 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL
     R l1 = fabs(UnF), l2 = fabs(UnF + aF), l3 = fabs(UnF - aF);
     R ea = UnL - UnR;
     R c2L = g * pL * rrL, c2R = g * pR * rrR;
-    R rcL = rsqrt_(c2L), rcR = rsqrt_(c2R);
-    R cL = c2L * rcL, cR = c2R * rcR;
+    R rcL = t.get(T_RCL), rcR = t.get(T_RCR);
+    R cL = c2L > R(0) ? c2L * rcL : R(0), cR = c2R > R(0) ? c2R * rcR : R(0);
     R eb_ = cL - cR;
     R eps = h * fabs(ea);
     eps = eps + h * fabs(eb_);
     eps = (eps < R(0)) ? eps - consts<R>(P).small : eps + consts<R>(P).small;
     R eps2 = R(2) * eps;
     bool s1 = l1 < eps2, s2 = l2 < eps2, s3 = l3 < eps2;
-    R re = (s1 || s2 || s3) ? rcp(eps) : R(0);
+    R re = t.get(T_RE);
     R L1 = s1 ? R(0.25) * l1 * l1 * re + eps : l1;
     R L2 = s2 ? R(0.25) * l2 * l2 * re + eps : l2;
     R L3 = s3 ? R(0.25) * l3 * l3 * re + eps : l3;
@@ -265,16 +277,16 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL
 }
 
 // riemann.eulerLaxFriedrichs
-template <typename R>
+template <typename R, typename Src>
 AFVM_HD void laxf_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR, const R* rhoUL,
-                      const R* rhoUR, R rhoEL, R rhoER, const R* N, const R* Fb, R& pLb, R& pRb, R* ULb, R* URb,
-                      R& rhoLb, R& rhoRb, R* rhoULb, R* rhoURb, R& rhoELb, R& rhoERb) {
+                      const R* rhoUR, R rhoEL, R rhoER, const R* N, const R* Fb, const Src& t, R& pLb, R& pRb,
+                      R* ULb, R* URb, R& rhoLb, R& rhoRb, R* rhoULb, R* rhoURb, R& rhoELb, R& rhoERb) {
     const R g = consts<R>(P).gamma, h = R(0.5);
     R UnL = dot3(UL, N), UnR = dot3(UR, N);
-    R rrL = rcp(rhoL), rrR = rcp(rhoR);
+    R rrL = t.get(T_RRL), rrR = t.get(T_RRR);
     R c2L = g * pL * rrL, c2R = g * pR * rrR;
-    R rcL = rsqrt_(c2L), rcR = rsqrt_(c2R);
-    R cL = c2L * rcL, cR = c2R * rcR;
+    R rcL = t.get(T_RCL), rcR = t.get(T_RCR);
+    R cL = c2L > R(0) ? c2L * rcL : R(0), cR = c2R > R(0) ? c2R * rcR : R(0);
     R A = fabs(UnL) + cL, B = fabs(UnR) + cR;
     R aF = (A >= B) ? A : B;
     R ha = h * aF;
@@ -306,22 +318,12 @@ AFVM_HD void laxf_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rho
 }
 
 // RCF.viscousFlux: F[1..3] += -sigma, F[4] += -(q + sigma.UF)
+// (mu = mu(TF), gT and gU the corrected face gradients: the forward's values)
 template <typename R>
-AFVM_HD void viscous_vjp(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, const R* UF, const R* gTF,
-                         const R* gUF, const R* D, const R* N, R rdel, const R* Fb, R& TLb, R& TRb, R* ULb, R* URb,
-                         R& TFb, R* UFb, R* gTFb, R* gUFb) {
-    R mu = viscosity<R>(P, TF);
+AFVM_HD void viscous_vjp_t(const Phys& P, R TF, const R* UF, R mu, const R* gT, const R* gU, const R* D,
+                           const R* N, R rdel, const R* Fb, R& TLb, R& TRb, R* ULb, R* URb, R& TFb, R* UFb,
+                           R* gTFb, R* gUFb) {
     R kappa = mu * consts<R>(P).kFac;
-    R snT = (TR - TL) * rdel;
-    R gTD = dot3(gTF, D);
-    R gT[3];
-    for (int k = 0; k < 3; k++) gT[k] = gTF[k] + snT * D[k] - gTD * D[k];
-    R gU[9];
-    for (int i = 0; i < 3; i++) {
-        R snU = (UR[i] - UL[i]) * rdel;
-        R gUD = gUF[3 * i] * D[0] + gUF[3 * i + 1] * D[1] + gUF[3 * i + 2] * D[2];
-        for (int k = 0; k < 3; k++) gU[3 * i + k] = gUF[3 * i + k] + snU * D[k] - gUD * D[k];
-    }
     R tmp3 = gU[0] + gU[4] + gU[8];
     R tmp2[3], sigma[3];
     for (int i = 0; i < 3; i++) {
@@ -370,6 +372,28 @@ AFVM_HD void viscous_vjp(const Phys& P, R TL, R TR, const R* UL, const R* UR, R 
     if (P.muModel == AFVM_MU_SUTHERLAND) TFb += mub * mu * (R(1.5) * rcp(TF) - rcp(TF + consts<R>(P).muTs));
 }
 
+template <typename R>
+AFVM_HD void viscous_vjp(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, const R* UF, const R* gTF,
+                         const R* gUF, const R* D, const R* N, R rdel, const R* Fb, R& TLb, R& TRb, R* ULb, R* URb,
+                         R& TFb, R* UFb, R* gTFb, R* gUFb) {
+    R mu = viscosity<R>(P, TF);
+    R snT = (TR - TL) * rdel;
+    R gTD = dot3(gTF, D);
+    R gT[3];
+    for (int k = 0; k < 3; k++) gT[k] = gTF[k] + snT * D[k] - gTD * D[k];
+    R gU[9];
+    for (int i = 0; i < 3; i++) {
+        R snU = (UR[i] - UL[i]) * rdel;
+        R gUD = gUF[3 * i] * D[0] + gUF[3 * i + 1] * D[1] + gUF[3 * i + 2] * D[2];
+        for (int k = 0; k < 3; k++) gU[3 * i + k] = gUF[3 * i + k] + snU * D[k] - gUD * D[k];
+    }
+    viscous_vjp_t<R>(P, TF, UF, mu, gT, gU, D, N, rdel, Fb, TLb, TRb, ULb, URb, TFb, UFb, gTFb, gUFb);
+}
+
+template <typename R, typename Src>
+AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>& in, const Src& t, const R* Fb,
+                        FaceBar<R>& o);
+
 // <Fbar, F> differentiated with respect to all 40 inputs of the face (accumulated into out)
 template <typename R>
 AFVM_HD void face_vjp(const Phys& P, int kind, bool inviscid, const FaceIn<R>& in, const R* Fb, FaceBar<R>& o) {
@@ -392,41 +416,42 @@ AFVM_HD void face_vjp(const Phys& P, int kind, bool inviscid, const FaceIn<R>& i
         }
         return;
     }
+    TapeLocal<R> t;
+    R F[5], maxaF;   // dead after inlining: only the tape values are used
+    face_flux<R>(P, kind, inviscid, in, F, maxaF, t);
+    face_vjp_t<R>(P, kind, inviscid, in, t, Fb, o);
+}
+
+// the VJP of a non-boundary face from the tape of its forward evaluation: of the face inputs
+// only the geometry (N, D, lw, qw, 1/deltas) is read from in
+template <typename R, typename Src>
+AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>& in, const Src& t, const R* Fb,
+                        FaceBar<R>& o) {
     const bool chr = kind == FACE_CHARACTERISTIC;
-    // forward
-    R ULF[3], TLF, pLF, URF[3], TRF, pRF;
-    for (int k = 0; k < 3; k++) ULF[k] = recon<R>(in.UP[k], in.UN[k], in.gUP + 3 * k, in.lw0, in.qw0);
-    TLF = recon<R>(in.TP, in.TN, in.gTP, in.lw0, in.qw0);
-    pLF = recon<R>(in.pP, in.pN, in.gpP, in.lw0, in.qw0);
-    if (chr) {
-        for (int k = 0; k < 3; k++) URF[k] = in.UN[k];
-        TRF = in.TN; pRF = in.pN;
-    } else {
-        for (int k = 0; k < 3; k++) URF[k] = recon<R>(in.UN[k], in.UP[k], in.gUN + 3 * k, in.lw1, in.qw1);
-        TRF = recon<R>(in.TN, in.TP, in.gTN, in.lw1, in.qw1);
-        pRF = recon<R>(in.pN, in.pP, in.gpN, in.lw1, in.qw1);
-    }
-    R rhoL, rhoUL[3], rhoEL, rhoR, rhoUR[3], rhoER;
-    conservative<R>(P, ULF, TLF, pLF, rhoL, rhoUL, rhoEL);
-    conservative<R>(P, URF, TRF, pRF, rhoR, rhoUR, rhoER);
+    // forward values
+    R ULF[3], TLF = t.get(T_TLF), pLF = t.get(T_PLF), URF[3], TRF = t.get(T_TRF), pRF = t.get(T_PRF);
+    for (int k = 0; k < 3; k++) { ULF[k] = t.get(T_ULF + k); URF[k] = t.get(T_URF + k); }
+    R rdL = t.get(T_RDL), rdR = t.get(T_RDR);
+    R rhoL = pLF * rdL, rhoR = pRF * rdR;      // conservative(): rho = p * rd
     R ULFb[3] = {R(0), R(0), R(0)}, URFb[3] = {R(0), R(0), R(0)};
     R TLFb = R(0), TRFb = R(0), pLFb = R(0), pRFb = R(0);
     // viscous part
     if (!inviscid) {
-        R TF, UF[3], gTF[3], gUF[9];
+        R TF, UF[3];
         if (chr) {
-            TF = in.TN;
-            for (int k = 0; k < 3; k++) { UF[k] = in.UN[k]; gTF[k] = in.gTN[k]; }
-            for (int k = 0; k < 9; k++) gUF[k] = in.gUN[k];
+            TF = TRF;                            // the ghost's values (in.TN, in.UN)
+            for (int k = 0; k < 3; k++) UF[k] = URF[k];
         } else {
             TF = R(0.5) * (TLF + TRF);
-            for (int k = 0; k < 3; k++) { UF[k] = R(0.5) * (ULF[k] + URF[k]); gTF[k] = R(0.5) * (in.gTP[k] + in.gTN[k]); }
-            for (int k = 0; k < 9; k++) gUF[k] = R(0.5) * (in.gUP[k] + in.gUN[k]);
+            for (int k = 0; k < 3; k++) UF[k] = R(0.5) * (ULF[k] + URF[k]);
         }
+        R gT[3], gU[9];
+        for (int k = 0; k < 3; k++) gT[k] = t.get(T_GT + k);
+        for (int k = 0; k < 9; k++) gU[k] = t.get(T_GU + k);
         R TFb = R(0), UFb[3] = {R(0), R(0), R(0)}, gTFb[3] = {R(0), R(0), R(0)}, gUFb[9];
         for (int k = 0; k < 9; k++) gUFb[k] = R(0);
-        viscous_vjp<R>(P, in.TP, in.TN, in.UP, in.UN, TF, UF, gTF, gUF, in.D, in.N, in.rdelta, Fb, o.TP, o.TN, o.UP,
-                       o.UN, TFb, UFb, gTFb, gUFb);
+        viscous_vjp_t<R>(P, TF, UF, t.get(T_MU), gT, gU, in.D, in.N, in.rdelta, Fb, o.TP, o.TN, o.UP, o.UN, TFb,
+                         UFb, gTFb, gUFb);
         if (chr) {
             o.TN += TFb;
             for (int k = 0; k < 3; k++) { o.UN[k] += UFb[k]; o.gTN[k] += gTFb[k]; }
@@ -447,13 +472,19 @@ AFVM_HD void face_vjp(const Phys& P, int kind, bool inviscid, const FaceIn<R>& i
     R rhoLb = R(0), rhoRb = R(0), rhoULb[3] = {R(0), R(0), R(0)}, rhoURb[3] = {R(0), R(0), R(0)};
     R rhoELb = R(0), rhoERb = R(0);
     int solver = chr ? P.briemann : P.riemann;
-    if (solver == AFVM_RIEMANN_ROE)
-        roe_vjp<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, in.N, Fb, pLFb, pRFb, ULFb, URFb, rhoLb, rhoRb);
-    else
-        laxf_vjp<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, rhoUL, rhoUR, rhoEL, rhoER, in.N, Fb, pLFb, pRFb, ULFb, URFb,
-                    rhoLb, rhoRb, rhoULb, rhoURb, rhoELb, rhoERb);
-    conservative_vjp<R>(P, ULF, TLF, pLF, rhoLb, rhoULb, rhoELb, ULFb, TLFb, pLFb);
-    conservative_vjp<R>(P, URF, TRF, pRF, rhoRb, rhoURb, rhoERb, URFb, TRFb, pRFb);
+    if (solver == AFVM_RIEMANN_ROE) {
+        roe_vjp<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, in.N, Fb, t, pLFb, pRFb, ULFb, URFb, rhoLb, rhoRb);
+    } else {
+        // conservative()'s rhoU and rhoE of each side
+        R eL = consts<R>(P).Cv * TLF, eR = consts<R>(P).Cv * TRF;
+        R rhoEL = rhoL * (eL + R(0.5) * dot3(ULF, ULF)), rhoER = rhoR * (eR + R(0.5) * dot3(URF, URF));
+        R rhoUL[3], rhoUR[3];
+        for (int k = 0; k < 3; k++) { rhoUL[k] = ULF[k] * rhoL; rhoUR[k] = URF[k] * rhoR; }
+        laxf_vjp<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, rhoUL, rhoUR, rhoEL, rhoER, in.N, Fb, t, pLFb, pRFb, ULFb,
+                    URFb, rhoLb, rhoRb, rhoULb, rhoURb, rhoELb, rhoERb);
+    }
+    conservative_vjp_t<R>(P, ULF, TLF, pLF, rdL, rhoLb, rhoULb, rhoELb, ULFb, TLFb, pLFb);
+    conservative_vjp_t<R>(P, URF, TRF, pRF, rdR, rhoRb, rhoURb, rhoERb, URFb, TRFb, pRFb);
     // reconstruction
     for (int k = 0; k < 3; k++) recon_vjp<R>(ULFb[k], in.lw0, in.qw0, o.UP[k], o.UN[k], o.gUP + 3 * k);
     recon_vjp<R>(TLFb, in.lw0, in.qw0, o.TP, o.TN, o.gTP);

@@ -52,4 +52,33 @@ __device__ __forceinline__ void load_face(const MeshDev<R>& m, const R* __restri
     in.rdelta = m.rdlt[f];
 }
 
+// a face's column of a device tape (value k of face f at tape[k nF + f]; p = tape + f)
+template <typename R>
+struct TapeStore {
+    R* p;
+    size_t stride;
+    __device__ __forceinline__ void put(int k, R x) const { p[(size_t)k * stride] = x; }
+};
+template <typename R>
+struct TapeLoad {
+    const R* p;
+    size_t stride;
+    __device__ __forceinline__ R get(int k) const { return __ldg(p + (size_t)k * stride); }
+};
+
+// the geometry inputs of a face only (what the VJP reads besides the tape)
+template <typename R>
+__device__ __forceinline__ void load_face_geometry(const MeshDev<R>& m, int f, FaceIn<R>& in) {
+    const size_t nF = m.nF;
+    for (int k = 0; k < 3; k++) {
+        in.N[k] = m.nrm[k * nF + f];
+        in.D[k] = m.du[k * nF + f];
+        in.qw0[k] = m.qw[k * nF + f];
+        in.qw1[k] = m.qw[(3 + k) * nF + f];
+    }
+    in.lw0 = m.lw[f];
+    in.lw1 = m.lw[nF + f];
+    in.rdelta = m.rdlt[f];
+}
+
 }  // namespace afvm

@@ -32,6 +32,33 @@ constexpr int FREC = 6;
 // kinds of faces
 constexpr int FACE_INTERNAL = 0, FACE_COUPLED = 1, FACE_CHARACTERISTIC = 2, FACE_BOUNDARY = 3;
 
+// The face tape: the values of the forward face flux that its VJP would otherwise recompute
+// at the highest FP64 cost - the reconstructed face states, the reciprocals and reciprocal
+// square roots, mu(T_F) and the corrected face gradients. The forward flux writes them through
+// a sink (nothing, a local array, or a column of a device tape); the VJP reads them back.
+constexpr int T_ULF = 0, T_TLF = 3, T_PLF = 4, T_URF = 5, T_TRF = 8, T_PRF = 9;   // face states
+constexpr int T_RDL = 10, T_RDR = 11;            // 1/(Cv T (g-1)) of each side (conservative)
+constexpr int T_RRL = 12, T_RRR = 13;            // 1/rho
+constexpr int T_RSL = 14, T_RSR = 15;            // 1/sqrt(rho)
+constexpr int T_RD = 16, T_RAF = 17;             // 1/(sL + sR), 1/a_F (Roe average)
+constexpr int T_RCL = 18, T_RCR = 19;            // 1/c of each side
+constexpr int T_RE = 20;                         // 1/eps of the entropy fix (0 when inactive)
+constexpr int T_MU = 21;                         // mu(T_F)
+constexpr int T_GT = 22, T_GU = 25;              // corrected face gradients of T (3) and U (9)
+constexpr int TAPE = 34;
+
+struct TapeNone {
+    template <typename R>
+    AFVM_HD void put(int, R) const {}
+};
+
+template <typename R>
+struct TapeLocal {
+    R v[TAPE];
+    AFVM_HD void put(int k, R x) { v[k] = x; }
+    AFVM_HD R get(int k) const { return v[k]; }
+};
+
 // the gas constants in the working precision, so that the templated physics issues no FP64
 // conversion or division in FP32 (ggm1 = gamma/(gamma-1))
 template <typename R>
@@ -170,9 +197,11 @@ AFVM_HD R viscosity(const Phys& P, R T) {
 
 // RCF.conservative (adFVM/density.py:173-181)
 template <typename R>
-AFVM_HD void conservative(const Phys& P, const R* U, R T, R p, R& rho, R* rhoU, R& rhoE) {
+AFVM_HD void conservative(const Phys& P, const R* U, R T, R p, R& rho, R* rhoU, R& rhoE, R* rdOut = nullptr) {
     R e = consts<R>(P).Cv * T;
-    rho = p * rcp(e * consts<R>(P).gm1);
+    R rd = rcp(e * consts<R>(P).gm1);
+    if (rdOut) *rdOut = rd;
+    rho = p * rd;
     rhoE = rho * (e + R(0.5) * dot3(U, U));
     rhoU[0] = U[0] * rho; rhoU[1] = U[1] * rho; rhoU[2] = U[2] * rho;
 }
@@ -186,26 +215,33 @@ AFVM_HD R recon(R phiC, R phiD, const R* g, R lw, const R* qw) {
 
 // riemann.eulerRoe (adFVM/riemann.py:21-70). Divisions become products with shared
 // reciprocals; rhoUn/rho is Un (the same number in exact arithmetic).
-template <typename R>
+template <typename R, typename Sink = TapeNone>
 AFVM_HD void roe(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR,
-                 const R* N, R* F) {
+                 const R* N, R* F, Sink&& tp = Sink()) {
     const R g = consts<R>(P).gamma, gm1 = consts<R>(P).gm1, ggm1 = consts<R>(P).ggm1;
     R UnL = dot3(UL, N), UnR = dot3(UR, N);
     R rhoUnL = rhoL * UnL, rhoUnR = rhoR * UnR;
     R rrL = rcp(rhoL), rrR = rcp(rhoR);
+    tp.put(T_RRL, rrL);
+    tp.put(T_RRR, rrR);
     R hL = ggm1 * pL * rrL + R(0.5) * dot3(UL, UL);
     R hR = ggm1 * pR * rrR + R(0.5) * dot3(UR, UR);
     R fr = R(0.5) * (rhoUnL + rhoUnR);
     R fu[3], UF[3], dU[3];
     for (int k = 0; k < 3; k++) fu[k] = R(0.5) * (rhoUnL * UL[k] + rhoUnR * UR[k] + (pL + pR) * N[k]);
     R fe = R(0.5) * (rhoUnL * hL + rhoUnR * hR);
-    R sL = rhoL * rsqrt_(rhoL), sR = rhoR * rsqrt_(rhoR);
+    R rsL = rsqrt_(rhoL), rsR = rsqrt_(rhoR);
+    R sL = rhoL * rsL, sR = rhoR * rsR;
     R rD = rcp(sL + sR);
+    tp.put(T_RSL, rsL);
+    tp.put(T_RSR, rsR);
+    tp.put(T_RD, rD);
     for (int k = 0; k < 3; k++) UF[k] = (UL[k] * sL + UR[k] * sR) * rD;
     R hF = (hL * sL + hR * sR) * rD;
     R qF = R(0.5) * dot3(UF, UF);
     R a2F = gm1 * (hF - qF);
     R raF = rsqrt_(a2F);
+    tp.put(T_RAF, raF);
     R aF = a2F * raF;
     R ra2F = raF * raF;
     R UnF = dot3(UF, N);
@@ -213,16 +249,24 @@ AFVM_HD void roe(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R 
     for (int k = 0; k < 3; k++) dU[k] = rhoR * UR[k] - rhoL * UL[k];
     R drhoE = (hR * rhoR - pR) - (hL * rhoL - pL);
     R lam1 = fabs(UnF), lam2 = fabs(UnF + aF), lam3 = fabs(UnF - aF);
+    // sound speeds c = sqrt(g p / rho) as c^2 / c with the reciprocal kept for the VJP
+    R c2L = g * pL * rrL, c2R = g * pR * rrR;
+    R rcL = rsqrt_(c2L), rcR = rsqrt_(c2R);
+    tp.put(T_RCL, rcL);
+    tp.put(T_RCR, rcR);
+    R cL = c2L > R(0) ? c2L * rcL : R(0), cR = c2R > R(0) ? c2R * rcR : R(0);
     R eps = R(0.5) * fabs(UnL - UnR);
-    eps = eps + R(0.5) * fabs(sqrt_(g * pL * rrL) - sqrt_(g * pR * rrR));
+    eps = eps + R(0.5) * fabs(cL - cR);
     eps = (eps < R(0)) ? eps - consts<R>(P).small : eps + consts<R>(P).small;
     R eps2 = R(2) * eps;
+    R re = R(0);
     if (lam1 < eps2 || lam2 < eps2 || lam3 < eps2) {
-        R re = rcp(eps);
+        re = rcp(eps);
         if (lam1 < eps2) lam1 = R(0.25) * lam1 * lam1 * re + eps;
         if (lam2 < eps2) lam2 = R(0.25) * lam2 * lam2 * re + eps;
         if (lam3 < eps2) lam3 = R(0.25) * lam3 * lam3 * re + eps;
     }
+    tp.put(T_RE, re);
     R abv1 = R(0.5) * (lam2 + lam3);
     R abv2 = R(0.5) * (lam2 - lam3);
     R abv3 = abv1 - lam1;
@@ -236,13 +280,21 @@ AFVM_HD void roe(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R 
 }
 
 // riemann.eulerLaxFriedrichs (adFVM/riemann.py:6-18)
-template <typename R>
+template <typename R, typename Sink = TapeNone>
 AFVM_HD void laxf(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR,
-                                     const R* rhoUL, const R* rhoUR, R rhoEL, R rhoER, const R* N, R* F) {
+                                     const R* rhoUL, const R* rhoUR, R rhoEL, R rhoER, const R* N, R* F,
+                                     Sink&& tp = Sink()) {
     const R g = consts<R>(P).gamma;
     R UnL = dot3(UL, N), UnR = dot3(UR, N);
-    R cL = sqrt_(g * pL * rcp(rhoL));
-    R cR = sqrt_(g * pR * rcp(rhoR));
+    R rrL = rcp(rhoL), rrR = rcp(rhoR);
+    R c2L = g * pL * rrL, c2R = g * pR * rrR;
+    R rcL = rsqrt_(c2L), rcR = rsqrt_(c2R);
+    tp.put(T_RRL, rrL);
+    tp.put(T_RRR, rrR);
+    tp.put(T_RCL, rcL);
+    tp.put(T_RCR, rcR);
+    R cL = c2L > R(0) ? c2L * rcL : R(0);
+    R cR = c2R > R(0) ? c2R * rcR : R(0);
     R aF = fmax(fabs(UnL) + cL, fabs(UnR) + cR);
     R ha = R(0.5) * aF;
     F[0] = R(0.5) * (rhoL * UnL + rhoR * UnR) - ha * (rhoR - rhoL);
@@ -253,10 +305,12 @@ AFVM_HD void laxf(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R
 
 // RCF.viscousFlux (adFVM/density.py:192-222): adds -sigma to F[1..3] and -(q + sigma.UF) to F[4];
 // rdel = 1/deltas (a mesh table), the divisor of snGrad (op.py:66-67)
-template <typename R>
+template <typename R, typename Sink = TapeNone>
 AFVM_HD void viscous(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, const R* UF,
-                                        const R* gTF, const R* gUF, const R* D, const R* N, R rdel, R* F) {
+                                        const R* gTF, const R* gUF, const R* D, const R* N, R rdel, R* F,
+                                        Sink&& tp = Sink()) {
     R mu = viscosity<R>(P, TF);
+    tp.put(T_MU, mu);
     R kappa = mu * consts<R>(P).kFac;
     R snT = (TR - TL) * rdel;
     R gTD = dot3(gTF, D);
@@ -268,6 +322,8 @@ AFVM_HD void viscous(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, 
         R gUD = gUF[3 * i] * D[0] + gUF[3 * i + 1] * D[1] + gUF[3 * i + 2] * D[2];
         for (int k = 0; k < 3; k++) gU[3 * i + k] = gUF[3 * i + k] + snU * D[k] - gUD * D[k];
     }
+    for (int k = 0; k < 3; k++) tp.put(T_GT + k, gT[k]);
+    for (int k = 0; k < 9; k++) tp.put(T_GU + k, gU[k]);
     R qF = kappa * dot3(gT, N);
     R tmp3 = gU[0] + gU[4] + gU[8];
     R sigma[3];

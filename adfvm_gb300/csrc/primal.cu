@@ -169,9 +169,11 @@ __global__ void __launch_bounds__(BLOCK) k_grad(MeshDev<R> m, R* __restrict__ re
 }
 
 
-template <typename R>
+// TAPED: also writes the face tape (TAPE values a face, column-major: tape[k nF + f]) that
+// k_adj_flux<..., true> reads back instead of re-evaluating the forward flux
+template <typename R, bool TAPED>
 __global__ void __launch_bounds__(FLUX_BLOCK, sizeof(R) == 8 ? 3 : 8) k_flux(MeshDev<R> m, Phys P, const R* __restrict__ rec,
-                                                R* __restrict__ fflux, int inviscid) {
+                                                R* __restrict__ fflux, int inviscid, R* __restrict__ tape) {
     // (the 6-value face records are stored directly: staging them through shared memory, as
     // the 20- and 40-value records are, made this kernel slower - 0.217 -> 0.269 ms at 128^3 in
     // FP32 - the barrier costs more than the six partly coalesced stores)
@@ -181,7 +183,10 @@ __global__ void __launch_bounds__(FLUX_BLOCK, sizeof(R) == 8 ? 3 : 8) k_flux(Mes
     FaceIn<R> in;
     load_face<R>(m, rec, f, in);
     R F[5], maxaF;
-    face_flux<R>(P, kind, inviscid != 0, in, F, maxaF);
+    if (TAPED)
+        face_flux<R>(P, kind, inviscid != 0, in, F, maxaF, TapeStore<R>{tape + f, (size_t)m.nF});
+    else
+        face_flux<R>(P, kind, inviscid != 0, in, F, maxaF);
     R* out = fflux + (size_t)f * FREC;
     for (int k = 0; k < 5; k++) out[k] = F[k];
     out[5] = maxaF;
@@ -427,7 +432,7 @@ void launch_prim_grad(Ctx* c, const S* r, const S* ru, const S* re, cudaStream_t
 template <typename R, typename S>
 void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const S* const* u0, const S* const* u1,
                         const S* const* u2, const S* Sr, const S* Su, const S* Se, S* const* out, cudaStream_t s,
-                        bool nextPrims) {
+                        bool nextPrims, R* tape) {
     const MeshDev<R>& m = meshOf<R>(c);
     const Phys& P = c->phys;
     R* rec = (R*)c->rec;
@@ -435,7 +440,11 @@ void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const S*
     int inviscid = (P.muModel == AFVM_MU_CONSTANT && P.mu0 == 0.0) ? 1 : 0;
     {
         ProfScope ps(c, KID_FLUX, s);
-        k_flux<R><<<(m.nF + FLUX_BLOCK - 1) / FLUX_BLOCK, FLUX_BLOCK, 0, s>>>(m, P, rec, ff, inviscid);
+        int nbF = (m.nF + FLUX_BLOCK - 1) / FLUX_BLOCK;
+        if (tape)
+            k_flux<R, true><<<nbF, FLUX_BLOCK, 0, s>>>(m, P, rec, ff, inviscid, tape);
+        else
+            k_flux<R, false><<<nbF, FLUX_BLOCK, 0, s>>>(m, P, rec, ff, inviscid, nullptr);
     }
     int nb = nblocks(m.nIC);
     R* recNext = nextPrims ? rec : nullptr;
@@ -465,7 +474,7 @@ void default_sources(Ctx* c, const S*& Srho, const S*& SrhoU, const S*& SrhoE) {
 template <typename R, typename S>
 int primal_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double dt, const double* dtDev,
                     const S* Srho, const S* SrhoU, const S* SrhoE, S* rhoN, S* rhoUN, S* rhoEN,
-                    double* dtcDev, double* objDev, cudaStream_t s, S* stages) {
+                    double* dtcDev, double* objDev, cudaStream_t s, S* stages, R* tape) {
     const MeshDev<R>& m = meshOf<R>(c);
     const Phys& P = c->phys;
     default_sources<S>(c, Srho, SrhoU, SrhoE);
@@ -509,7 +518,8 @@ int primal_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double d
             }
         }
         S* const* out = st == 0 ? u1 : (st == 1 ? u2 : outN);
-        launch_flux_update<R, S>(c, st, dt, dtDev, u0c, u1c, u2c, Srho, SrhoU, SrhoE, out, s, st < 2);
+        launch_flux_update<R, S>(c, st, dt, dtDev, u0c, u1c, u2c, Srho, SrhoU, SrhoE, out, s, st < 2,
+                                 tape ? tape + (size_t)st * TAPE * m.nF : nullptr);
     }
     if (vaneDone) {
         ProfScope ps(c, KID_FINISH, s);
@@ -552,14 +562,14 @@ int primal_run_dev(Ctx* c, S* rho, S* rhoU, S* rhoE, int nSteps, double dt0, dou
 
 #define AFVM_PRIMAL_INST(R, S)                                                                                 \
     template int primal_step_dev<R, S>(Ctx*, const S*, const S*, const S*, double, const double*, const S*,       \
-                                       const S*, const S*, S*, S*, S*, double*, double*, cudaStream_t, S*);       \
+                                       const S*, const S*, S*, S*, S*, double*, double*, cudaStream_t, S*, R*);   \
     template int primal_run_dev<R, S>(Ctx*, S*, S*, S*, int, double, double, double, int, const S*, const S*,     \
                                       const S*, double*, double*, double*, cudaStream_t);                         \
     template void launch_prim<R, S>(Ctx*, const S*, const S*, const S*, cudaStream_t);                           \
     template void launch_prim_grad<R, S>(Ctx*, const S*, const S*, const S*, cudaStream_t);                      \
     template void launch_flux_update<R, S>(Ctx*, int, double, const double*, const S* const*, const S* const*,   \
                                            const S* const*, const S*, const S*, const S*, S* const*, cudaStream_t,  \
-                                           bool);
+                                           bool, R*);
 AFVM_PRIMAL_INST(double, double)
 AFVM_PRIMAL_INST(float, float)
 AFVM_PRIMAL_INST(float, double)

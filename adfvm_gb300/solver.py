@@ -397,10 +397,28 @@ class RCF(object):
         td = torch.float64 if self.dtype == np.float64 else torch.float32
         return torch.empty(10 * self.mesh.nInternalCells, dtype=td, device='cuda:%d' % self.device)
 
-    def step(self, rho, rhoU, rhoE, dt, S=None, out=None, want_scalars=True, stages=None):
+    def tape_buffer(self):
+        """A device buffer for the face tape of one step (afvm_primal_step_tape): the forward
+        values the adjoint step would otherwise re-evaluate; kept together with a stage_buffer."""
+        torch = _torch()
+        td = torch.float64 if self.record_dtype == np.float64 else torch.float32
+        return torch.empty(int(L.lib().afvm_tape_elements(self._ctx)), dtype=td, device='cuda:%d' % self.device)
+
+    def _check_tape(self, tape, stages):
+        torch = _torch()
+        td = torch.float64 if self.record_dtype == np.float64 else torch.float32
+        if stages is None:
+            raise ValueError('tape: kept together with stages')
+        if tape.dtype != td or tape.numel() < int(L.lib().afvm_tape_elements(self._ctx)) or \
+                not tape.is_contiguous() or not tape.is_cuda:
+            raise ValueError('tape: a contiguous device buffer of afvm_tape_elements %s values' % td)
+        return tape
+
+    def step(self, rho, rhoU, rhoE, dt, S=None, out=None, want_scalars=True, stages=None, tape=None):
         """One step on CUDA tensors (reference layouts). Returns (rhoN, rhoUN, rhoEN, dtc, obj).
         stages: optional stage_buffer() that receives the step's RK stage states, for
-        adjoint_step(..., stages=) on the same state."""
+        adjoint_step(..., stages=) on the same state; tape: optional tape_buffer() (with stages)
+        that receives the step's face tape, for adjoint_step(..., tape=)."""
         torch = _torch()
         stream = torch.cuda.current_stream(rho.device).cuda_stream
         if out is None:
@@ -409,13 +427,14 @@ class RCF(object):
         dtc = C.c_double()
         obj = C.c_double()
         sp = None if stages is None else C.c_void_p(self._check_stages(stages).data_ptr())
-        st = L.lib().afvm_primal_step_stages(self._ctx, C.c_void_p(rho.data_ptr()), C.c_void_p(rhoU.data_ptr()),
-                                             C.c_void_p(rhoE.data_ptr()), float(dt), Sp[0], Sp[1], Sp[2],
-                                             C.c_void_p(out[0].data_ptr()), C.c_void_p(out[1].data_ptr()),
-                                             C.c_void_p(out[2].data_ptr()), sp,
-                                             C.byref(dtc) if want_scalars else None,
-                                             C.byref(obj) if want_scalars else None, C.c_void_p(stream))
-        L.check(st, self._ctx, 'afvm_primal_step_stages')
+        tp = None if tape is None else C.c_void_p(self._check_tape(tape, stages).data_ptr())
+        st = L.lib().afvm_primal_step_tape(self._ctx, C.c_void_p(rho.data_ptr()), C.c_void_p(rhoU.data_ptr()),
+                                           C.c_void_p(rhoE.data_ptr()), float(dt), Sp[0], Sp[1], Sp[2],
+                                           C.c_void_p(out[0].data_ptr()), C.c_void_p(out[1].data_ptr()),
+                                           C.c_void_p(out[2].data_ptr()), sp, tp,
+                                           C.byref(dtc) if want_scalars else None,
+                                           C.byref(obj) if want_scalars else None, C.c_void_p(stream))
+        L.check(st, self._ctx, 'afvm_primal_step_tape')
         return out[0], out[1], out[2], dtc.value, obj.value
 
     def _check_stages(self, stages):
@@ -426,12 +445,14 @@ class RCF(object):
             raise ValueError('stages: a contiguous device buffer of 10 x nInternalCells %s values' % td)
         return stages
 
-    def adjoint_step(self, rho, rhoU, rhoE, dt, seeds, obja=1.0, S=None, out=None, source_grad=True, stages=None):
+    def adjoint_step(self, rho, rhoU, rhoE, dt, seeds, obja=1.0, S=None, out=None, source_grad=True, stages=None,
+                     tape=None):
         """VJP of one step on CUDA tensors (afvm_adjoint_step): the adjoint of the input state
         (and of the sources) given the adjoint seeds of the output state and of the objective.
         dt is held fixed, the CFL-sum output gets no seed (dtca = 0, apps/adjoint.py:268).
         stages: the stage_buffer() a step(..., stages=) of this state filled; skips the
-        forward recompute."""
+        forward recompute. tape: the tape_buffer() the same step filled; skips the face
+        flux's re-evaluation inside the VJP."""
         torch = _torch()
         stream = torch.cuda.current_stream(rho.device).cuda_stream
         if out is None:
@@ -441,11 +462,12 @@ class RCF(object):
         vp = lambda t: C.c_void_p(t.data_ptr())
         gp = [None, None, None] if Sg is None else [vp(t) for t in Sg]
         sp = None if stages is None else vp(self._check_stages(stages))
-        st = L.lib().afvm_adjoint_step_stages(self._ctx, vp(rho), vp(rhoU), vp(rhoE), float(dt), Sp[0], Sp[1],
-                                              Sp[2], sp, vp(seeds[0]), vp(seeds[1]), vp(seeds[2]), 0.0, float(obja),
-                                              vp(out[0]), vp(out[1]), vp(out[2]), gp[0], gp[1], gp[2],
-                                              C.c_void_p(stream))
-        L.check(st, self._ctx, 'afvm_adjoint_step_stages')
+        tp = None if tape is None else vp(self._check_tape(tape, stages))
+        st = L.lib().afvm_adjoint_step_tape(self._ctx, vp(rho), vp(rhoU), vp(rhoE), float(dt), Sp[0], Sp[1],
+                                            Sp[2], sp, tp, vp(seeds[0]), vp(seeds[1]), vp(seeds[2]), 0.0, float(obja),
+                                            vp(out[0]), vp(out[1]), vp(out[2]), gp[0], gp[1], gp[2],
+                                            C.c_void_p(stream))
+        L.check(st, self._ctx, 'afvm_adjoint_step_tape')
         return out[0], out[1], out[2], Sg
 
     def adjoint_viscosity(self, rho, rhoU, rhoE, adj, dt, kind='turkel', scaling=1e-3, want_fields=False):

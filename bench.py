@@ -239,18 +239,22 @@ def measure(case, precision, args, local, dist, world, clocks):
         ms = e0.elapsed_time(e1)
         return max_over_ranks([ms], dist)[0]
 
-    # a sweep: the primal steps keep their states and RK stage states in rings of the last
-    # R steps; the adjoint steps walk those steps backwards (cycling when K > R), each on the
-    # state and stages of one primal step, carrying the adjoint field as a real sweep does
-    R = max(1, min(args.steps, 32))
+    # a sweep: the primal steps keep their states, RK stage states and face tapes in rings of
+    # the last R steps; the adjoint steps walk those steps backwards (cycling when K > R), each
+    # on the state, stages and tape of one primal step, carrying the adjoint field as a real
+    # sweep does. The ring is capped at 60 GB of tapes.
+    use_tape = args.tape
+    tape_bytes = int(rcf.tape_buffer().numel()) * es if use_tape else 0
+    R = max(1, min(args.steps, 32, int(60e9 // tape_bytes) if tape_bytes else 32))
     ring = [x] + [[torch.empty_like(t) for t in x] for _ in range(R)]
     stg = [rcf.stage_buffer() for _ in range(R)]
+    tps = [rcf.tape_buffer() for _ in range(R)] if use_tape else [None] * R
     cnt = {'p': 0, 'a': 0}
 
     def primal():
         j = cnt['p']
         xi, xo = ring[j % (R + 1)], ring[(j + 1) % (R + 1)]
-        rcf.step(xi[0], xi[1], xi[2], dt, out=xo, want_scalars=False, stages=stg[j % R])
+        rcf.step(xi[0], xi[1], xi[2], dt, out=xo, want_scalars=False, stages=stg[j % R], tape=tps[j % R])
         cnt['p'] = j + 1
 
     abuf = [torch.ones_like(t) * 1e-3 for t in x]
@@ -260,7 +264,8 @@ def measure(case, precision, args, local, dist, world, clocks):
         cnt['a'] = q + 1
         j = cnt['p'] - 1 - (q % min(R, cnt['p']))
         xi = ring[j % (R + 1)]
-        rcf.adjoint_step(xi[0], xi[1], xi[2], dt, abuf, obja=1.0, out=abuf, source_grad=False, stages=stg[j % R])
+        rcf.adjoint_step(xi[0], xi[1], xi[2], dt, abuf, obja=1.0, out=abuf, source_grad=False, stages=stg[j % R],
+                         tape=tps[j % R])
 
     for _ in range(args.warmup):
         primal()
@@ -534,6 +539,8 @@ def main():
     ap.add_argument('--precision', default='fp64')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--serving', type=int, default=1, help='1: add the serving measurement to the line')
+    ap.add_argument('--tape', type=int, default=1,
+                    help='1: the primal steps keep their face tapes for the adjoint steps (afvm_primal_step_tape)')
     ap.add_argument('--study', default='', help="'precision': the FP32-vs-FP64 cylinder study (own JSON line)")
     args = ap.parse_args()
     if args.impl == 'reference':
@@ -568,9 +575,10 @@ def main():
                            l2='inputs larger than L2: %.2f GB device working set' % (m64['device_bytes'] / 1e9),
                            parallelism='replicas' if world > 1 else 'single GPU',
                            step='one SSP-RK3 primal step plus its adjoint step (value = cells x steps / '
-                                '(primal + adjoint time)); the primal steps keep their RK stage states and '
+                                '(primal + adjoint time)); the primal steps keep their RK stage states%s and '
                                 'the adjoint steps walk them backwards as a sweep does; primal and adjoint '
-                                'also reported alone'),
+                                'also reported alone' % (' and face tapes' if args.tape else ''),
+                           tape=bool(args.tape)),
             'primal': m64['primal'], 'adjoint': m64['adjoint'],
             'roofline': m64['roofline'], 'step_model': m64['step_model'], 'kernels': m64['kernels'],
             'adjoint_kernels': m64['adjoint_kernels'], 'gpu_launches': m64['gpu_launches'],

@@ -297,6 +297,32 @@ int afvm_adjoint_step_stages(afvm_ctx* ctx, const void* rho, const void* rhoU, c
                              const void* rhoENa, double dtca, double obja, void* rhoa, void* rhoUa,
                              void* rhoEa, void* S_rhoa, void* S_rhoUa, void* S_rhoEa, void* stream);
 
+/* The face tape of a step: per RK stage and face, the 34 values of the forward face flux
+ * that its VJP would otherwise re-evaluate at the highest FP64 cost (the reconstructed face
+ * states, the reciprocals and reciprocal square roots of the Roe / Rusanov flux and of the
+ * conservative variables, mu(T_F) and the corrected face gradients). Element type: the
+ * record type (double for AFVM_FP64, float otherwise); afvm_tape_elements values a step,
+ * 3 x 34 x nFaces. Worth keeping in FP64, where the face VJP is bound by the FP64 pipe and
+ * HBM is idle; no reference counterpart (adpy's reverse mode re-runs the forward). */
+int64_t afvm_tape_elements(const afvm_ctx* ctx);
+
+/* afvm_primal_step_stages that also writes the step's face tape (DEVICE, afvm_tape_elements
+ * values; tape needs stages). */
+int afvm_primal_step_tape(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE,
+                          double dt, const void* S_rho, const void* S_rhoU, const void* S_rhoE,
+                          void* rhoN, void* rhoUN, void* rhoEN, void* stages, void* tape,
+                          double* dtc_out, double* obj_out, void* stream);
+
+/* afvm_adjoint_step_stages that reads the face tape the primal step wrote for this state
+ * (tape needs stages; NULL: re-evaluate the forward). The result agrees with the re-evaluating
+ * step to rounding (the forward kernel may contract products into FMAs differently). */
+int afvm_adjoint_step_tape(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE,
+                           double dt, const void* S_rho, const void* S_rhoU, const void* S_rhoE,
+                           const void* stages, const void* tape, const void* rhoNa,
+                           const void* rhoUNa, const void* rhoENa, double dtca, double obja,
+                           void* rhoa, void* rhoUa, void* rhoEa, void* S_rhoa, void* S_rhoUa,
+                           void* S_rhoEa, void* stream);
+
 /* FP64 sum over k of dot(grad[k], pert[k]) (adFVM/cpp/cmesh.cpp:309-340). DEVICE arrays of
  * n[k] doubles; result to *out (host) after the stream work completes. */
 /* Adjoint stabilisation by artificial viscosity (adFVM/postpro.py:491-718, the viscous
