@@ -49,12 +49,13 @@ def peaks():
 
 # algorithmic (compulsory) bytes per launch of each primal kernel, FP64 / FP32 element size
 # es and int32 indices (per-unit counts in the comments below)
-def algorithmic_bytes(kernel, nIC, nIF, nF, nG, es):
-    REC, FREC = 20, 6
+def algorithmic_bytes(kernel, nIC, nIF, nF, nG, es, taped=False):
+    REC, FREC, TAPE = 20, 6, 34
     if kernel == 'k_flux':
         # per face: own+nbr (8), normals 3, deltas 1, deltasUnit 3, linearWeights 2,
-        # quadraticWeights 6 -> 15 values, flux record write 6; cell records read once
-        return nF * (8 + 15 * es + FREC * es) + (nIC + nG) * REC * es
+        # quadraticWeights 6 -> 15 values, flux record write 6 (and the 34-value face tape when
+        # taped); cell records read once
+        return nF * (8 + 15 * es + FREC * es + (TAPE * es if taped else 0)) + (nIC + nG) * REC * es
     if kernel == 'k_grad':
         # per cell: 6 slots x (nbr 4 + w' + S*N' (3)) + 1/V, primitives of every cell once,
         # gradient write 15
@@ -65,6 +66,11 @@ def algorithmic_bytes(kernel, nIC, nIF, nF, nG, es):
         return nIC * (6 * (4 + es) + 3 * 5 * es + 5 * es) + nF * FREC * es
     if kernel == 'k_prim':
         return nIC * 10 * es + nG * (8 + 5 * es + 5 * es)
+    if kernel == 'k_adj_flux' and taped:
+        # per face: own+nbr (8), A/V weights 2, geometry 15, the 34-value face tape, 40-value
+        # adjoint record write; the 5 adjoint seeds of every cell once; the two cell records of
+        # each boundary face (boundary faces are not taped)
+        return nF * (8 + (17 + TAPE + 40) * es) + nIC * 5 * es + (nF - nIF) * 2 * REC * es
     if kernel == 'k_adj_flux':
         # per face: own+nbr (8), A/V weights 2, geometry 15, 40-value adjoint record write;
         # cell records and the 5 adjoint seeds of every cell read once
@@ -243,7 +249,9 @@ def measure(case, precision, args, local, dist, world, clocks):
     # the last R steps; the adjoint steps walk those steps backwards (cycling when K > R), each
     # on the state, stages and tape of one primal step, carrying the adjoint field as a real
     # sweep does. The ring is capped at 60 GB of tapes.
-    use_tape = args.tape
+    # (FP64 only: there the face VJP is bound by the FP64 pipe and HBM is idle; in FP32 the tape's
+    # bytes cost more than the re-evaluation)
+    use_tape = bool(args.tape) and precision == 'fp64'
     tape_bytes = int(rcf.tape_buffer().numel()) * es if use_tape else 0
     R = max(1, min(args.steps, 32, int(60e9 // tape_bytes) if tape_bytes else 32))
     ring = [x] + [[torch.empty_like(t) for t in x] for _ in range(R)]
@@ -333,12 +341,13 @@ def measure(case, precision, args, local, dist, world, clocks):
             t[1] += v[1]
     top = max(both.items(), key=lambda kv: kv[1][0])[0]
     peak, peak_kind = peaks()
-    alg = algorithmic_bytes(top, nIC, nIF, nF, nG, es)
+    alg = algorithmic_bytes(top, nIC, nIF, nF, nG, es, taped=use_tape)
+    topkey = top + ('+tape' if use_tape and top in ('k_flux', 'k_adj_flux') else '')
     avg_s = both[top][0] / both[top][1] / 1e3
     achieved = alg / avg_s / 1e9
-    roofline = {'bound': 'hbm', 'kernel': top, 'achieved': round(achieved, 1), 'peak': peak,
+    roofline = {'bound': 'hbm', 'kernel': topkey, 'achieved': round(achieved, 1), 'peak': peak,
                 'peak_source': peak_kind, 'unit': 'GB/s', 'frac': round(achieved / peak, 4),
-                'algorithmic_bytes_per_launch': int(alg), 'traffic': measured_traffic(top, es, nF),
+                'algorithmic_bytes_per_launch': int(alg), 'traffic': measured_traffic(topkey, es, nF),
                 'share_of_step': round(both[top][0] / (ms_p + ms_a), 3)}
     step_model = {'unit': 'GB/s', 'peak': peak,
                   'primal': round(vp * 1e6 * STEP_BYTES[('primal', es)] / 1e9, 1),
@@ -351,7 +360,7 @@ def measure(case, precision, args, local, dist, world, clocks):
             'primal': {'value': round(vp, 3), 'ms_per_step': round(ms_p / K, 4)},
             'adjoint': {'value': round(va, 3), 'ms_per_step': round(ms_a / K, 4)},
             'roofline': roofline, 'kernels': kernels, 'step_model': step_model,
-            '_top': (top, avg_s, nF),
+            '_top': (topkey, avg_s, nF), 'tape': use_tape,
             'adjoint_kernels': {k: {'ms_total': round(v[0], 4), 'launches': v[1], 'ms_avg': round(v[0] / v[1], 5)}
                                 for k, v in prof_a.items()},
             'gpu_launches': int(sum(v[1] for v in prof.values()) + sum(v[1] for v in prof_a.values())),
@@ -577,8 +586,8 @@ def main():
                            step='one SSP-RK3 primal step plus its adjoint step (value = cells x steps / '
                                 '(primal + adjoint time)); the primal steps keep their RK stage states%s and '
                                 'the adjoint steps walk them backwards as a sweep does; primal and adjoint '
-                                'also reported alone' % (' and face tapes' if args.tape else ''),
-                           tape=bool(args.tape)),
+                                'also reported alone' % (' and face tapes' if m64['tape'] else ''),
+                           tape=bool(m64['tape'])),
             'primal': m64['primal'], 'adjoint': m64['adjoint'],
             'roofline': m64['roofline'], 'step_model': m64['step_model'], 'kernels': m64['kernels'],
             'adjoint_kernels': m64['adjoint_kernels'], 'gpu_launches': m64['gpu_launches'],
