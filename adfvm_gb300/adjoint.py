@@ -79,14 +79,18 @@ class Adjoint(object):
         return self.primal.adjoint_energy(adj, state) ** 0.5
 
     # ------------------------------------------------------------ the sweep
-    def run(self, fields, nSteps, dt, writeInterval, perturbations=(), avgStart=0, source=None, keep_stages=True):
+    def run(self, fields, nSteps, dt, writeInterval, perturbations=(), avgStart=0, source=None, keep_stages=True,
+            keep_tapes=None):
         """Checkpointed adjoint sweep on the device.
 
         fields: initial conservative state (host arrays). dt: a float (fixed step) or the
         per-step dt series of the primal run. perturbations: list of (dS_rho, dS_rhoU,
         dS_rhoE) host arrays. keep_stages: the interval's forward re-run also keeps every
         step's RK stage states (10 nInternalCells values a step) so that the adjoint steps
-        do not recompute them. Returns (sensitivities, adjoint fields at t0 (host), record)."""
+        do not recompute them. keep_tapes: with keep_stages, also keep every step's face tape
+        (the forward values the face VJP would re-evaluate); None: for FP64 contexts whose
+        interval of tapes fits in 32 GB. Returns (sensitivities, adjoint fields at t0 (host),
+        record)."""
         torch = _torch()
         p = self.primal
         if nSteps % writeInterval:
@@ -115,6 +119,9 @@ class Adjoint(object):
         sens_series = []
         nCk = nSteps // writeInterval
         stages = [p.stage_buffer() for _ in range(writeInterval)] if keep_stages else None
+        if keep_tapes is None:
+            keep_tapes = p.record_dtype == np.float64 and writeInterval * p.tape_bytes <= 32e9
+        tapes = [p.tape_buffer() for _ in range(writeInterval)] if keep_stages and keep_tapes else None
         for checkpoint in range(nCk):
             primalIndex = nSteps - (checkpoint + 1) * writeInterval
             states = [checkpoints[primalIndex // writeInterval]]
@@ -122,13 +129,16 @@ class Adjoint(object):
             for k in range(primalIndex, last):
                 y = states[-1]
                 sb = stages[k - primalIndex] if keep_stages else None
-                states.append(list(p.step(y[0], y[1], y[2], dts[k], S=S, want_scalars=False, stages=sb)[:3]))
+                tb = tapes[k - primalIndex] if tapes else None
+                states.append(list(p.step(y[0], y[1], y[2], dts[k], S=S, want_scalars=False, stages=sb,
+                                          tape=tb)[:3]))
             for step in range(writeInterval):
                 adjointIndex = writeInterval - 1 - step
                 y = states[adjointIndex]
                 sb = stages[adjointIndex] if keep_stages else None
+                tb = tapes[adjointIndex] if tapes else None
                 r = p.adjoint_step(y[0], y[1], y[2], dts[primalIndex + adjointIndex], a, obja=1.0, S=S, out=a,
-                                   stages=sb)
+                                   stages=sb, tape=tb)
                 if self.viscosityType and (step + 1) % self.viscousInterval == 0:
                     p.adjoint_viscosity(y[0], y[1], y[2], a, dts[primalIndex + adjointIndex], self.viscosityType,
                                         self.scaling)

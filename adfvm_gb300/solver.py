@@ -397,6 +397,11 @@ class RCF(object):
         td = torch.float64 if self.dtype == np.float64 else torch.float32
         return torch.empty(10 * self.mesh.nInternalCells, dtype=td, device='cuda:%d' % self.device)
 
+    @property
+    def tape_bytes(self):
+        """Bytes of one step's face tape (afvm_tape_elements values of the record type)."""
+        return int(L.lib().afvm_tape_elements(self._ctx)) * np.dtype(self.record_dtype).itemsize
+
     def tape_buffer(self):
         """A device buffer for the face tape of one step (afvm_primal_step_tape): the forward
         values the adjoint step would otherwise re-evaluate; kept together with a stage_buffer."""
