@@ -71,8 +71,9 @@ class Adjoint(object):
         Sh = [primal_in[base + k] for k in range(3)]
         stages = p.kept_stages(primal_in[0], primal_in[1], primal_in[2], dt, Sh)
         r = p.adjoint_step(x[0], x[1], x[2], dt, seeds, obja=obja, S=S, stages=stages)
-        out = [t.cpu().numpy().astype(np.float64) for t in r[:3]]
-        return out + [t.cpu().numpy().astype(np.float64) for t in r[3]]
+        # (FP64 results are returned as they come off the device; FP32 ones widened)
+        host = lambda t: t.cpu().numpy().astype(np.float64, copy=False)
+        return [host(t) for t in r[:3]] + [host(t) for t in r[3]]
 
     def computeEnergy(self, adj, state):
         """sqrt of the adjoint energy (apps/adjoint.py:55 over cmesh.computeEnergy); device tensors."""

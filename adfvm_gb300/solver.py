@@ -626,7 +626,7 @@ class RCF(object):
         dev = 'cuda:%d' % self.device
         x = [np.asarray(a, np.float64).reshape(n, d) for a, d in zip(fields[:3], (1, 3, 1))]
         xd = [torch.as_tensor(np.ascontiguousarray(a, self.dtype), device=dev) for a in x]
-        ghost = self.boundary_values(*xd).cpu().numpy().astype(np.float64)
+        ghost = self.boundary_values(*xd).cpu().numpy().astype(np.float64, copy=False)
         gU, gT, gp = ghost[:, 0:3], ghost[:, 3:4], ghost[:, 4:5]
         U, T, p = self.primitive(*x)
         td = os.path.join(self.case, foam.time_name(t))
