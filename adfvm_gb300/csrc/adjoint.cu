@@ -56,8 +56,10 @@ __device__ __forceinline__ void adj_face(const MeshDev<R>& m, const Phys& P, con
         face_vjp<R>(P, kind, inviscid != 0, in, Fb, b);
     }
     const R* src = &b.UP[0];
-    for (int k = 0; k < 5; k++) { row[k] = src[k]; row[20 + k] = src[5 + k]; }
-    for (int k = 0; k < 15; k++) { row[5 + k] = src[10 + k]; row[25 + k] = src[25 + k]; }
+    R v[FADJ];
+    for (int k = 0; k < 5; k++) { v[k] = src[k]; v[20 + k] = src[5 + k]; }
+    for (int k = 0; k < 15; k++) { v[5 + k] = src[10 + k]; v[25 + k] = src[25 + k]; }
+    stage_row<R, FADJ>(row, v);
 }
 
 template <typename R, typename S, bool TAPED>
@@ -68,17 +70,12 @@ __global__ void __launch_bounds__(FLUX_BLOCK, sizeof(R) == 8 ? 3 : 4) k_adj_flux
     // the block's 40-value face records are staged here and written out contiguously: one
     // thread's 40 scalar stores at a 40-value stride would touch a new 32-byte sector each and
     // load L2 with eight partial writes per sector
-    __shared__ R stage[FLUX_BLOCK * (FADJ + 1)];
+    __shared__ __align__(16) R stage[FLUX_BLOCK * FADJ];
     const int f0 = blockIdx.x * FLUX_BLOCK;
     const int f = f0 + threadIdx.x;
-    if (f < m.nF) adj_face<R, S, TAPED>(m, P, rec, coef, ar, au, ae, inviscid, f, stage + threadIdx.x * (FADJ + 1), tape);
+    if (f < m.nF) adj_face<R, S, TAPED>(m, P, rec, coef, ar, au, ae, inviscid, f, stage + threadIdx.x * FADJ, tape);
     __syncthreads();
-    const int nb = min(FLUX_BLOCK, m.nF - f0);
-    R* out = fadj + (size_t)f0 * FADJ;
-    for (int i = threadIdx.x; i < nb * FADJ; i += FLUX_BLOCK) {
-        int r = i / FADJ;
-        out[i] = stage[r * (FADJ + 1) + (i - r * FADJ)];
-    }
+    store_staged<R, FADJ, FLUX_BLOCK>(fadj, f0, min(FLUX_BLOCK, m.nF - f0), stage);
 }
 
 // one cell's sum of its faces' adjoint records (and of the ghosts whose gradient is its own)
@@ -101,15 +98,15 @@ __device__ __forceinline__ void adj_cell_gather(const MeshDev<R>& m, const R* __
         const R* r = fadj + (size_t)(m.nIF + g) * FADJ;
         for (int k = 0; k < 15; k++) acc[5 + k] += r[25 + k];
     }
-    for (int k = 0; k < CBAR; k++) row[k] = acc[k];
+    stage_row<R, CBAR>(row, acc);
 }
 
 template <typename R>
 __global__ void __launch_bounds__(BLOCK) k_adj_cell1(MeshDev<R> m, const R* __restrict__ fadj, R* __restrict__ cbar) {
-    __shared__ R stage[BLOCK * (CBAR + 1)];
+    __shared__ __align__(16) R stage[BLOCK * CBAR];
     const int c0 = blockIdx.x * BLOCK;
     const int c = c0 + threadIdx.x;
-    if (c < m.nIC) adj_cell_gather<R>(m, fadj, c, stage + threadIdx.x * (CBAR + 1));
+    if (c < m.nIC) adj_cell_gather<R>(m, fadj, c, stage + threadIdx.x * CBAR);
     __syncthreads();
     if (c0 < m.nIC) store_staged<R, CBAR, BLOCK>(cbar, c0, min(BLOCK, m.nIC - c0), stage);
 }

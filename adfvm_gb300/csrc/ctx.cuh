@@ -17,19 +17,43 @@ constexpr int BLOCK = 256;
 // 10.52 ms, FP32 k_flux 0.240 -> 0.217 ms.
 constexpr int FLUX_BLOCK = 128;
 
-// Writes the W-value records a block of NT threads staged in shared memory (row r at
-// stage + r (W + 1); the padding keeps the staging stores free of bank conflicts) to
-// out[(first + r) W + k] for the block's nValid rows, as contiguous runs of the output. A thread
-// storing its own W-value record at a W-value stride would make each scalar store a separate L2
-// write request into a partly written sector. Callers __syncthreads() before.
+// Block-staged record stores. A thread that stores its own W-value record at a W-value stride
+// makes each scalar store a separate L2 write request into a partly written sector; instead
+// each thread writes its record into the block's shared-memory stage (stage_row: 16-byte
+// stores, rows of W values unpadded - W a multiple of 16 bytes, so a quarter-warp's 16-byte
+// stores land in distinct banks for W = 20 floats and in two for W = 40), and after a
+// __syncthreads() the block's records - one contiguous range of the output - are copied out
+// as 16-byte vectors (store_staged).
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> { using type = float4; };
+template <>
+struct Vec16<double> { using type = double2; };
+
+template <typename T, int W>
+__device__ __forceinline__ void stage_row(T* __restrict__ row, const T* v) {
+    using V = typename Vec16<T>::type;
+    constexpr int PER = 16 / sizeof(T);
+    static_assert(W % PER == 0, "record rows are whole 16-byte vectors");
+#pragma unroll
+    for (int j = 0; j < W / PER; j++) {
+        V x;
+        if constexpr (PER == 4) x = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+        else x = make_double2(v[2 * j], v[2 * j + 1]);
+        reinterpret_cast<V*>(row)[j] = x;
+    }
+}
+
 template <typename T, int W, int NT>
 __device__ __forceinline__ void store_staged(T* __restrict__ out, size_t first, int nValid,
                                              const T* __restrict__ stage) {
-    T* o = out + first * W;
-    for (int i = threadIdx.x; i < nValid * W; i += NT) {
-        int r = i / W;
-        o[i] = stage[r * (W + 1) + (i - r * W)];
-    }
+    using V = typename Vec16<T>::type;
+    constexpr int PER = 16 / sizeof(T);
+    const V* s = reinterpret_cast<const V*>(stage);
+    V* o = reinterpret_cast<V*>(out + first * W);
+    const int n = nValid * (W / PER);
+    for (int i = threadIdx.x; i < n; i += NT) o[i] = s[i];
 }
 
 // boundary-condition kind codes stored per ghost cell (3 bits per field: U, T, p)

@@ -152,18 +152,20 @@ __device__ __forceinline__ void grad_cell(const MeshDev<R>& m, const R* __restri
             for (int j = 0; j < 3; j++) g[3 * i + j] = g[3 * i + j] + phiF[i] * sn[j];
     }
     R rv = m.rvol[c];
-    for (int k = 0; k < 5; k++) row[k] = phic[k];
-    for (int k = 0; k < 15; k++) row[R_GU + k] = g[k] * rv;
+    R v[REC];
+    for (int k = 0; k < 5; k++) v[k] = phic[k];
+    for (int k = 0; k < 15; k++) v[R_GU + k] = g[k] * rv;
+    stage_row<R, REC>(row, v);
 }
 
 // the cell's whole record (its primitives again, then the gradients) is staged and the block's
 // records written contiguously
 template <typename R>
 __global__ void __launch_bounds__(BLOCK) k_grad(MeshDev<R> m, R* __restrict__ rec) {
-    __shared__ R stage[BLOCK * (REC + 1)];
+    __shared__ __align__(16) R stage[BLOCK * REC];
     const int c0 = blockIdx.x * BLOCK;
     const int c = c0 + threadIdx.x;
-    if (c < m.nIC) grad_cell<R>(m, rec, c, stage + threadIdx.x * (REC + 1));
+    if (c < m.nIC) grad_cell<R>(m, rec, c, stage + threadIdx.x * REC);
     __syncthreads();
     if (c0 < m.nIC) store_staged<R, REC, BLOCK>(rec, c0, min(BLOCK, m.nIC - c0), stage);
 }
