@@ -267,31 +267,31 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const
     if (STAGE == 2) {
         for (int k = 0; k < 5; k++) out[k] = S(2. / 3) * ain[k] + (S)J[k];
         S z[5];
-        for (int k = 0; k < 5; k++) { z[k] = S(1. / 3) * ain[k]; sb[5 * (size_t)c + k] = S(2. / 3) * S(dt) * ain[k]; }
+        for (int k = 0; k < 5; k++) { z[k] = S(1. / 3) * ain[k]; sb[k * n + c] = S(2. / 3) * S(dt) * ain[k]; }
         a0r[c] = z[0]; a0u[3 * c] = z[1]; a0u[3 * c + 1] = z[2]; a0u[3 * c + 2] = z[3]; a0e[c] = z[4];
         a1r[c] = out[0]; a1u[3 * c] = out[1]; a1u[3 * c + 1] = out[2]; a1u[3 * c + 2] = out[3]; a1e[c] = out[4];
     } else if (STAGE == 1) {
         for (int k = 0; k < 5; k++) out[k] = S(1. / 4) * ain[k] + (S)J[k];
         S z[5] = {a0r[c], a0u[3 * c], a0u[3 * c + 1], a0u[3 * c + 2], a0e[c]};
-        for (int k = 0; k < 5; k++) { z[k] += S(3. / 4) * ain[k]; sb[5 * (size_t)c + k] += S(1. / 4) * S(dt) * ain[k]; }
+        for (int k = 0; k < 5; k++) { z[k] += S(3. / 4) * ain[k]; sb[k * n + c] += S(1. / 4) * S(dt) * ain[k]; }
         a0r[c] = z[0]; a0u[3 * c] = z[1]; a0u[3 * c + 1] = z[2]; a0u[3 * c + 2] = z[3]; a0e[c] = z[4];
         a1r[c] = out[0]; a1u[3 * c] = out[1]; a1u[3 * c + 1] = out[2]; a1u[3 * c + 2] = out[3]; a1e[c] = out[4];
     } else {
         S z[5] = {a0r[c], a0u[3 * c], a0u[3 * c + 1], a0u[3 * c + 2], a0e[c]};
-        for (int k = 0; k < 5; k++) { z[k] += ain[k] + (S)J[k]; sb[5 * (size_t)c + k] += S(dt) * ain[k]; }
+        for (int k = 0; k < 5; k++) { z[k] += ain[k] + (S)J[k]; sb[k * n + c] += S(dt) * ain[k]; }
         a0r[c] = z[0]; a0u[3 * c] = z[1]; a0u[3 * c + 1] = z[2]; a0u[3 * c + 2] = z[3]; a0e[c] = z[4];
     }
 }
 
-// scatter the (nIC x 5) source adjoint into the reference layout
+// the source adjoint (5 x nIC, one coalesced row per component) into the reference layout
 template <typename R>
 __global__ void k_split5(int n, const R* __restrict__ sb, R* r, R* u, R* e) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n) return;
-    const R* s = sb + 5 * (size_t)c;
-    if (r) r[c] = s[0];
-    if (u) { u[3 * c] = s[1]; u[3 * c + 1] = s[2]; u[3 * c + 2] = s[3]; }
-    if (e) e[c] = s[4];
+    const size_t m = n;
+    if (r) r[c] = sb[c];
+    if (u) { u[3 * c] = sb[m + c]; u[3 * c + 1] = sb[2 * m + c]; u[3 * c + 2] = sb[3 * m + c]; }
+    if (e) e[c] = sb[4 * m + c];
 }
 
 template <typename R, typename S>

@@ -153,7 +153,7 @@ struct Ctx {
     void* cbar = nullptr;     // nIC x 20 cell primitive/gradient adjoints
     void* a1[3] = {nullptr, nullptr, nullptr};
     void* a2[3] = {nullptr, nullptr, nullptr};
-    void* sbar = nullptr;     // nIC x 5 source adjoint scratch
+    void* sbar = nullptr;     // 5 x nIC source adjoint scratch (component-major)
     int64_t adjBytes = 0;
     // device staging of the host-buffer entry point (allocated on first use)
     void* stageDev = nullptr;
