@@ -328,9 +328,15 @@ int adjoint_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double 
     const R* rec = (const R*)c->rec;
     int nbC = nblocks(m.nIC);
     const double beta[3] = {1.0, 1. / 4, 2. / 3};
+    // with the face tape only the VJPs of physical boundary faces read cell gradients (their
+    // viscous flux); without such faces the stage's primitives are all the records needed
+    const bool needGrad = !tape || (!inviscid && c->nBoundaryFlux > 0);
     for (int st = 2; st >= 0; st--) {
         const S* const* u = st == 0 ? u0c : (st == 1 ? u1c : u2c);
-        launch_prim_grad<R, S>(c, u[0], u[1], u[2], s);
+        if (needGrad)
+            launch_prim_grad<R, S>(c, u[0], u[1], u[2], s);
+        else
+            launch_prim<R, S>(c, u[0], u[1], u[2], s);
         if (st == 1 && c->objective == AFVM_OBJ_VANE) launch_vane_sums<R>(c, s, nullptr, nullptr);
         // adjoint of this stage's output: a3 = seeds, a2 = A2, a1 = A1
         const S* ain[3];

@@ -126,6 +126,8 @@ int upload_mesh(Ctx* c, const HostTables& h, MeshDev<R>& m) {
     if ((st = upload(c, &m.lw, cast<R>(h.lw)))) return st;
     if ((st = upload(c, &m.qw, cast<R>(h.qw)))) return st;
     if ((st = upload(c, &m.fkind, h.fkind))) return st;
+    c->nBoundaryFlux = 0;
+    for (uint8_t k : h.fkind) c->nBoundaryFlux += (k == FACE_BOUNDARY);
     if ((st = upload(c, &m.gsrc, h.gsrc))) return st;
     if ((st = upload(c, &m.gkind, h.gkind))) return st;
     if ((st = upload(c, &m.gval, cast<R>(h.gval)))) return st;

@@ -129,6 +129,7 @@ struct Ctx {
     int objective, objPatch;
     int objStart, objN;       // face range of the objective patch
     int nIC, nIF, nF, nC, nG, nPatches;
+    int nBoundaryFlux = 0;    // faces with FACE_BOUNDARY (the physical boundary flux)
     std::vector<int> patchStart, patchN, patchKind, patchCellStart;
     // device allocations
     std::vector<void*> allocs;
