@@ -223,13 +223,15 @@ __global__ void __launch_bounds__(BLOCK) k_update(MeshDev<R> m, const R* __restr
                                                   const S* __restrict__ Se,
                                                   S* outr, S* outu, S* oute,
                                                   unsigned long long* dtcBits, Phys P, R* __restrict__ recNext) {
-    // the gather and the update run in the state's type S (double for an FP64 state under
-    // FP32 fluxes); the CFL sum in the flux type R
+    // the gather (and the CFL sum) in the flux type R, the stage update in the state's type S:
+    // under FP32 fluxes with an FP64 state the six fluxes are summed in FP32 (each carries FP32
+    // rounding already; summing them in FP64 cost six FP64 conversions, products and sums a
+    // cell and component) and the state is updated in FP64
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     R dtc = R(0);
     if (c < m.nIC) {
         const size_t n = m.nIC;
-        S res[5] = {S(0), S(0), S(0), S(0), S(0)};
+        R res[5] = {R(0), R(0), R(0), R(0), R(0)};
 #pragma unroll
         for (int k = 0; k < 6; k++) {
             int e = m.accf[k * n + c];
@@ -239,7 +241,7 @@ __global__ void __launch_bounds__(BLOCK) k_update(MeshDev<R> m, const R* __restr
             R F[FREC];
             load_flux_record(fflux + (size_t)f * FREC, F);
             for (int q = 0; q < 5; q++) {
-                S t = (S)F[q] * (S)w;
+                R t = F[q] * w;
                 res[q] = res[q] + (ownerSide ? t : -t);
             }
             dtc = dtc + F[5] * w;
@@ -249,15 +251,15 @@ __global__ void __launch_bounds__(BLOCK) k_update(MeshDev<R> m, const R* __restr
         S o[5];
         const S rdt = S(dtp ? *dtp : dtv);
         if (STAGE == 0) {
-            for (int q = 0; q < 5; q++) o[q] = a[q] + (S(-1.0) * (res[q] - Sv[q])) * rdt;
+            for (int q = 0; q < 5; q++) o[q] = a[q] + (S(-1.0) * (S(res[q]) - Sv[q])) * rdt;
         } else if (STAGE == 1) {
             S b[5] = {u1r[c], u1u[3 * c], u1u[3 * c + 1], u1u[3 * c + 2], u1e[c]};
             for (int q = 0; q < 5; q++)
-                o[q] = (S(3. / 4) * a[q] + S(1. / 4) * b[q]) + (S(-(1. / 4)) * (res[q] - Sv[q])) * rdt;
+                o[q] = (S(3. / 4) * a[q] + S(1. / 4) * b[q]) + (S(-(1. / 4)) * (S(res[q]) - Sv[q])) * rdt;
         } else {
             S b[5] = {u2r[c], u2u[3 * c], u2u[3 * c + 1], u2u[3 * c + 2], u2e[c]};
             for (int q = 0; q < 5; q++)
-                o[q] = (S(1. / 3) * a[q] + S(2. / 3) * b[q]) + (S(-(2. / 3)) * (res[q] - Sv[q])) * rdt;
+                o[q] = (S(1. / 3) * a[q] + S(2. / 3) * b[q]) + (S(-(2. / 3)) * (S(res[q]) - Sv[q])) * rdt;
         }
         outr[c] = o[0];
         outu[3 * c] = o[1]; outu[3 * c + 1] = o[2]; outu[3 * c + 2] = o[3];
