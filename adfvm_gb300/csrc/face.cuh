@@ -105,7 +105,7 @@ AFVM_HD void conservative_vjp_t(const Phys& P, const R* U, R T, R p, R rd, R rho
     for (int k = 0; k < 3; k++) Ub[k] += rhoUb[k] * rho + rhoEb * rho * U[k];
     R rhot = rhob + dot3(rhoUb, U) + rhoEb * (e + R(0.5) * q);
     pb += rhot * rd;
-    R eb = -rhot * rho * rcp(e) + rhoEb * rho;
+    R eb = -rhot * rho * (rd * consts<R>(P).gm1) + rhoEb * rho;    // 1/e = rd (g-1)
     Tb += eb * consts<R>(P).Cv;
 }
 
@@ -369,7 +369,11 @@ AFVM_HD void viscous_vjp_t(const Phys& P, R TF, const R* UF, R mu, const R* gT, 
     for (int k = 0; k < 3; k++) gTFb[k] += gTb[k] + gTDb * D[k];
     TRb += snTb * rdel;
     TLb += -snTb * rdel;
-    if (P.muModel == AFVM_MU_SUTHERLAND) TFb += mub * mu * (R(1.5) * rcp(TF) - rcp(TF + consts<R>(P).muTs));
+    // d mu/dT = mu (1.5/T - 1/(T + Ts)) = mu (0.5 T + 1.5 Ts) / (T (T + Ts)): one reciprocal
+    if (P.muModel == AFVM_MU_SUTHERLAND) {
+        R Ts = consts<R>(P).muTs;
+        TFb += mub * mu * ((R(0.5) * TF + R(1.5) * Ts) * rcp(TF * (TF + Ts)));
+    }
 }
 
 template <typename R>
