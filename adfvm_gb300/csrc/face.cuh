@@ -129,50 +129,38 @@ template <typename R, typename Src>
 AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR, const R* N, const R* Fb,
                      const Src& t, R& pLb, R& pRb, R* ULb, R* URb, R& rhoLb, R& rhoRb) {
     const R g = consts<R>(P).gamma, gm1 = consts<R>(P).gm1, ggm1 = consts<R>(P).ggm1, h = R(0.5);
-    // ---- forward (as roe())
+    // ---- forward values: those dear to recompute from the tape, the cheap ones again (as roe())
     R UnL = dot3(UL, N), UnR = dot3(UR, N);
     R rhoUnL = rhoL * UnL, rhoUnR = rhoR * UnR;
-    R qL = dot3(UL, UL), qR = dot3(UR, UR);
     R rrL = t.get(T_RRL), rrR = t.get(T_RRR);
-    R hL = ggm1 * pL * rrL + h * qL;
-    R hR = ggm1 * pR * rrR + h * qR;
+    R hL = t.get(T_HL), hR = t.get(T_HR);
     R rsL = t.get(T_RSL), rsR = t.get(T_RSR);
     R sL = rhoL * rsL, sR = rhoR * rsR;
     R rD = t.get(T_RD);
     R UF[3], dU[3];
-    for (int k = 0; k < 3; k++) UF[k] = (UL[k] * sL + UR[k] * sR) * rD;
-    R hF = (hL * sL + hR * sR) * rD;
-    R qF = h * dot3(UF, UF);
+    for (int k = 0; k < 3; k++) { UF[k] = t.get(T_UFR + k); dU[k] = t.get(T_DU + k); }
+    R hF = t.get(T_HF), qF = t.get(T_QF);
     R a2F = gm1 * (hF - qF);
     R raF = t.get(T_RAF);
     R aF = a2F * raF;
     R ra2F = raF * raF;
-    R UnF = dot3(UF, N);
+    R UnF = t.get(T_UNF);
     R drho = rhoR - rhoL;
-    for (int k = 0; k < 3; k++) dU[k] = rhoR * UR[k] - rhoL * UL[k];
-    R drhoE = (hR * rhoR - pR) - (hL * rhoL - pL);
+    R drhoE = t.get(T_DRHOE);
     R l1 = fabs(UnF), l2 = fabs(UnF + aF), l3 = fabs(UnF - aF);
     R ea = UnL - UnR;
     R c2L = g * pL * rrL, c2R = g * pR * rrR;
     R rcL = t.get(T_RCL), rcR = t.get(T_RCR);
     R cL = c2L > R(0) ? c2L * rcL : R(0), cR = c2R > R(0) ? c2R * rcR : R(0);
     R eb_ = cL - cR;
-    R eps = h * fabs(ea);
-    eps = eps + h * fabs(eb_);
-    eps = (eps < R(0)) ? eps - consts<R>(P).small : eps + consts<R>(P).small;
+    R eps = t.get(T_EPS);
     R eps2 = R(2) * eps;
     bool s1 = l1 < eps2, s2 = l2 < eps2, s3 = l3 < eps2;
     R re = t.get(T_RE);
-    R L1 = s1 ? R(0.25) * l1 * l1 * re + eps : l1;
-    R L2 = s2 ? R(0.25) * l2 * l2 * re + eps : l2;
-    R L3 = s3 ? R(0.25) * l3 * l3 * re + eps : l3;
-    R abv1 = h * (L2 + L3);
+    R L1 = t.get(T_L1), L2 = t.get(T_L2), L3 = t.get(T_L3);
     R abv2 = h * (L2 - L3);
-    R abv3 = abv1 - L1;
-    R abv4 = gm1 * (qF * drho - dot3(UF, dU) + drhoE);
-    R abv5 = UnF * drho - dot3(dU, N);
-    R abv6 = abv3 * abv4 * ra2F - abv2 * abv5 * raF;
-    R abv7 = abv3 * abv5 - abv2 * abv4 * raF;
+    R abv3 = h * (L2 + L3) - L1;
+    R abv4 = t.get(T_ABV4), abv5 = t.get(T_ABV5), abv6 = t.get(T_ABV6), abv7 = t.get(T_ABV7);
     // ---- reverse
     R Fu[3] = {Fb[1], Fb[2], Fb[3]};
     R frb = Fb[0], feb = Fb[4];
@@ -320,16 +308,10 @@ AFVM_HD void laxf_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rho
 // RCF.viscousFlux: F[1..3] += -sigma, F[4] += -(q + sigma.UF)
 // (mu = mu(TF), gT and gU the corrected face gradients: the forward's values)
 template <typename R>
-AFVM_HD void viscous_vjp_t(const Phys& P, R TF, const R* UF, R mu, const R* gT, const R* gU, const R* D,
-                           const R* N, R rdel, const R* Fb, R& TLb, R& TRb, R* ULb, R* URb, R& TFb, R* UFb,
-                           R* gTFb, R* gUFb) {
+AFVM_HD void viscous_vjp_t(const Phys& P, R TF, const R* UF, R mu, R gTn, const R* tmp2, R tmp3, const R* sigma,
+                           const R* D, const R* N, R rdel, const R* Fb, R& TLb, R& TRb, R* ULb, R* URb, R& TFb,
+                           R* UFb, R* gTFb, R* gUFb) {
     R kappa = mu * consts<R>(P).kFac;
-    R tmp3 = gU[0] + gU[4] + gU[8];
-    R tmp2[3], sigma[3];
-    for (int i = 0; i < 3; i++) {
-        tmp2[i] = (gU[3 * i] + gU[i]) * N[0] + (gU[3 * i + 1] + gU[3 + i]) * N[1] + (gU[3 * i + 2] + gU[6 + i]) * N[2];
-        sigma[i] = mu * (tmp2[i] - R(2.0 / 3) * tmp3 * N[i]);
-    }
     // reverse
     R sb[3];
     for (int i = 0; i < 3; i++) {
@@ -345,7 +327,7 @@ AFVM_HD void viscous_vjp_t(const Phys& P, R TF, const R* UF, R mu, const R* gT, 
         tmp2b[i] = sb[i] * mu;
         tmp3b += -R(2.0 / 3) * mu * sb[i] * N[i];
     }
-    R kappab = qFb * dot3(gT, N);
+    R kappab = qFb * gTn;
     R gTb[3];
     for (int k = 0; k < 3; k++) gTb[k] = qFb * kappa * N[k];
     mub += kappab * consts<R>(P).kFac;
@@ -391,7 +373,14 @@ AFVM_HD void viscous_vjp(const Phys& P, R TL, R TR, const R* UL, const R* UR, R 
         R gUD = gUF[3 * i] * D[0] + gUF[3 * i + 1] * D[1] + gUF[3 * i + 2] * D[2];
         for (int k = 0; k < 3; k++) gU[3 * i + k] = gUF[3 * i + k] + snU * D[k] - gUD * D[k];
     }
-    viscous_vjp_t<R>(P, TF, UF, mu, gT, gU, D, N, rdel, Fb, TLb, TRb, ULb, URb, TFb, UFb, gTFb, gUFb);
+    R tmp3 = gU[0] + gU[4] + gU[8];
+    R tmp2[3], sigma[3];
+    for (int i = 0; i < 3; i++) {
+        tmp2[i] = (gU[3 * i] + gU[i]) * N[0] + (gU[3 * i + 1] + gU[3 + i]) * N[1] + (gU[3 * i + 2] + gU[6 + i]) * N[2];
+        sigma[i] = mu * (tmp2[i] - R(2.0 / 3) * tmp3 * N[i]);
+    }
+    viscous_vjp_t<R>(P, TF, UF, mu, dot3(gT, N), tmp2, tmp3, sigma, D, N, rdel, Fb, TLb, TRb, ULb, URb, TFb, UFb,
+                     gTFb, gUFb);
 }
 
 template <typename R, typename Src>
@@ -449,13 +438,13 @@ AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>&
             TF = R(0.5) * (TLF + TRF);
             for (int k = 0; k < 3; k++) UF[k] = R(0.5) * (ULF[k] + URF[k]);
         }
-        R gT[3], gU[9];
-        for (int k = 0; k < 3; k++) gT[k] = t.get(T_GT + k);
-        for (int k = 0; k < 9; k++) gU[k] = t.get(T_GU + k);
+
         R TFb = R(0), UFb[3] = {R(0), R(0), R(0)}, gTFb[3] = {R(0), R(0), R(0)}, gUFb[9];
         for (int k = 0; k < 9; k++) gUFb[k] = R(0);
-        viscous_vjp_t<R>(P, TF, UF, t.get(T_MU), gT, gU, in.D, in.N, in.rdelta, Fb, o.TP, o.TN, o.UP, o.UN, TFb,
-                         UFb, gTFb, gUFb);
+        R tmp2[3], sigma[3];
+        for (int k = 0; k < 3; k++) { tmp2[k] = t.get(T_TMP2 + k); sigma[k] = t.get(T_SIG + k); }
+        viscous_vjp_t<R>(P, TF, UF, t.get(T_MU), t.get(T_GTN), tmp2, t.get(T_TMP3), sigma, in.D, in.N, in.rdelta, Fb,
+                         o.TP, o.TN, o.UP, o.UN, TFb, UFb, gTFb, gUFb);
         if (chr) {
             o.TN += TFb;
             for (int k = 0; k < 3; k++) { o.UN[k] += UFb[k]; o.gTN[k] += gTFb[k]; }

@@ -34,7 +34,7 @@ constexpr int FACE_INTERNAL = 0, FACE_COUPLED = 1, FACE_CHARACTERISTIC = 2, FACE
 
 // The face tape: the values of the forward face flux that its VJP would otherwise recompute
 // at the highest FP64 cost - the reconstructed face states, the reciprocals and reciprocal
-// square roots, mu(T_F) and the corrected face gradients. The forward flux writes them through
+// square roots, mu(T_F), the Roe and viscous intermediates. The forward flux writes them through
 // a sink (nothing, a local array, or a column of a device tape); the VJP reads them back.
 constexpr int T_ULF = 0, T_TLF = 3, T_PLF = 4, T_URF = 5, T_TRF = 8, T_PRF = 9;   // face states
 constexpr int T_RDL = 10, T_RDR = 11;            // 1/(Cv T (g-1)) of each side (conservative)
@@ -44,8 +44,17 @@ constexpr int T_RD = 16, T_RAF = 17;             // 1/(sL + sR), 1/a_F (Roe aver
 constexpr int T_RCL = 18, T_RCR = 19;            // 1/c of each side
 constexpr int T_RE = 20;                         // 1/eps of the entropy fix (0 when inactive)
 constexpr int T_MU = 21;                         // mu(T_F)
-constexpr int T_GT = 22, T_GU = 25;              // corrected face gradients of T (3) and U (9)
-constexpr int TAPE = 34;
+constexpr int T_GTN = 22;                        // (corrected face grad T).n
+// Roe intermediates the reverse sweep uses (eulerRoe's names, riemann.py:21-70)
+constexpr int T_HL = 23, T_HR = 24;              // total enthalpies
+constexpr int T_UFR = 25, T_HF = 28, T_QF = 29;  // Roe-averaged U (3), H, |U|^2/2
+constexpr int T_UNF = 30, T_DU = 31;             // U_F.n, the jump of rho U (3)
+constexpr int T_DRHOE = 34, T_EPS = 35;          // the jump of rho E, the entropy-fix width
+constexpr int T_L1 = 36, T_L2 = 37, T_L3 = 38;   // |eigenvalues| after the entropy fix
+constexpr int T_ABV4 = 39, T_ABV5 = 40, T_ABV6 = 41, T_ABV7 = 42;
+// viscous intermediates: (grad U + grad U^T).n (3), sigma (3), tr grad U (corrected face gradient)
+constexpr int T_TMP2 = 43, T_SIG = 46, T_TMP3 = 49;
+constexpr int TAPE = 50;
 
 struct TapeNone {
     template <typename R>
@@ -226,6 +235,8 @@ AFVM_HD void roe(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R 
     tp.put(T_RRR, rrR);
     R hL = ggm1 * pL * rrL + R(0.5) * dot3(UL, UL);
     R hR = ggm1 * pR * rrR + R(0.5) * dot3(UR, UR);
+    tp.put(T_HL, hL);
+    tp.put(T_HR, hR);
     R fr = R(0.5) * (rhoUnL + rhoUnR);
     R fu[3], UF[3], dU[3];
     for (int k = 0; k < 3; k++) fu[k] = R(0.5) * (rhoUnL * UL[k] + rhoUnR * UR[k] + (pL + pR) * N[k]);
@@ -248,6 +259,11 @@ AFVM_HD void roe(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R 
     R drho = rhoR - rhoL;
     for (int k = 0; k < 3; k++) dU[k] = rhoR * UR[k] - rhoL * UL[k];
     R drhoE = (hR * rhoR - pR) - (hL * rhoL - pL);
+    for (int k = 0; k < 3; k++) { tp.put(T_UFR + k, UF[k]); tp.put(T_DU + k, dU[k]); }
+    tp.put(T_HF, hF);
+    tp.put(T_QF, qF);
+    tp.put(T_UNF, UnF);
+    tp.put(T_DRHOE, drhoE);
     R lam1 = fabs(UnF), lam2 = fabs(UnF + aF), lam3 = fabs(UnF - aF);
     // sound speeds c = sqrt(g p / rho) as c^2 / c with the reciprocal kept for the VJP
     R c2L = g * pL * rrL, c2R = g * pR * rrR;
@@ -267,6 +283,10 @@ AFVM_HD void roe(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R 
         if (lam3 < eps2) lam3 = R(0.25) * lam3 * lam3 * re + eps;
     }
     tp.put(T_RE, re);
+    tp.put(T_EPS, eps);
+    tp.put(T_L1, lam1);
+    tp.put(T_L2, lam2);
+    tp.put(T_L3, lam3);
     R abv1 = R(0.5) * (lam2 + lam3);
     R abv2 = R(0.5) * (lam2 - lam3);
     R abv3 = abv1 - lam1;
@@ -274,6 +294,10 @@ AFVM_HD void roe(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R 
     R abv5 = UnF * drho - dot3(dU, N);
     R abv6 = abv3 * abv4 * ra2F - abv2 * abv5 * raF;
     R abv7 = abv3 * abv5 - abv2 * abv4 * raF;
+    tp.put(T_ABV4, abv4);
+    tp.put(T_ABV5, abv5);
+    tp.put(T_ABV6, abv6);
+    tp.put(T_ABV7, abv7);
     F[0] = fr - R(0.5) * (lam1 * drho + abv6);
     for (int k = 0; k < 3; k++) F[1 + k] = fu[k] - R(0.5) * (lam1 * dU[k] + UF[k] * abv6 - abv7 * N[k]);
     F[4] = fe - R(0.5) * (lam1 * drhoE + hF * abv6 - UnF * abv7);
@@ -322,14 +346,17 @@ AFVM_HD void viscous(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, 
         R gUD = gUF[3 * i] * D[0] + gUF[3 * i + 1] * D[1] + gUF[3 * i + 2] * D[2];
         for (int k = 0; k < 3; k++) gU[3 * i + k] = gUF[3 * i + k] + snU * D[k] - gUD * D[k];
     }
-    for (int k = 0; k < 3; k++) tp.put(T_GT + k, gT[k]);
-    for (int k = 0; k < 9; k++) tp.put(T_GU + k, gU[k]);
-    R qF = kappa * dot3(gT, N);
+    R gTn = dot3(gT, N);
+    tp.put(T_GTN, gTn);
+    R qF = kappa * gTn;
     R tmp3 = gU[0] + gU[4] + gU[8];
+    tp.put(T_TMP3, tmp3);
     R sigma[3];
     for (int i = 0; i < 3; i++) {
         R tmp2 = (gU[3 * i] + gU[i]) * N[0] + (gU[3 * i + 1] + gU[3 + i]) * N[1] + (gU[3 * i + 2] + gU[6 + i]) * N[2];
         sigma[i] = mu * (tmp2 - R(2.0 / 3) * tmp3 * N[i]);
+        tp.put(T_TMP2 + i, tmp2);
+        tp.put(T_SIG + i, sigma[i]);
     }
     F[1] = F[1] + (-sigma[0]);
     F[2] = F[2] + (-sigma[1]);

@@ -50,10 +50,10 @@ def peaks():
 # algorithmic (compulsory) bytes per launch of each primal kernel, FP64 / FP32 element size
 # es and int32 indices (per-unit counts in the comments below)
 def algorithmic_bytes(kernel, nIC, nIF, nF, nG, es, taped=False):
-    REC, FREC, TAPE = 20, 6, 34
+    REC, FREC, TAPE = 20, 6, 50
     if kernel == 'k_flux':
         # per face: own+nbr (8), normals 3, deltas 1, deltasUnit 3, linearWeights 2,
-        # quadraticWeights 6 -> 15 values, flux record write 6 (and the 34-value face tape when
+        # quadraticWeights 6 -> 15 values, flux record write 6 (and the 50-value face tape when
         # taped); cell records read once
         return nF * (8 + 15 * es + FREC * es + (TAPE * es if taped else 0)) + (nIC + nG) * REC * es
     if kernel == 'k_grad':
@@ -67,7 +67,7 @@ def algorithmic_bytes(kernel, nIC, nIF, nF, nG, es, taped=False):
     if kernel == 'k_prim':
         return nIC * 10 * es + nG * (8 + 5 * es + 5 * es)
     if kernel == 'k_adj_flux' and taped:
-        # per face: own+nbr (8), A/V weights 2, geometry 15, the 34-value face tape, 40-value
+        # per face: own+nbr (8), A/V weights 2, geometry 15, the 50-value face tape, 40-value
         # adjoint record write; the 5 adjoint seeds of every cell once; the two cell records of
         # each boundary face (boundary faces are not taped)
         return nF * (8 + (17 + TAPE + 40) * es) + nIC * 5 * es + (nF - nIF) * 2 * REC * es
@@ -250,12 +250,12 @@ def measure(case, precision, args, local, dist, world, clocks):
     # a sweep: the primal steps keep their states, RK stage states and face tapes in rings of
     # the last R steps; the adjoint steps walk those steps backwards (cycling when K > R), each
     # on the state, stages and tape of one primal step, carrying the adjoint field as a real
-    # sweep does. The ring is capped at 60 GB of tapes.
+    # sweep does. The ring is capped at 100 GB of tapes.
     # (FP64 only: there the face VJP is bound by the FP64 pipe and HBM is idle; in FP32 the tape's
     # bytes cost more than the re-evaluation)
     use_tape = bool(args.tape) and precision == 'fp64'
     tape_bytes = int(rcf.tape_buffer().numel()) * es if use_tape else 0
-    R = max(1, min(args.steps, 32, int(60e9 // tape_bytes) if tape_bytes else 32))
+    R = max(1, min(args.steps, 32, int(100e9 // tape_bytes) if tape_bytes else 32))
     ring = [x] + [[torch.empty_like(t) for t in x] for _ in range(R)]
     stg = [rcf.stage_buffer() for _ in range(R)]
     tps = [rcf.tape_buffer() for _ in range(R)] if use_tape else [None] * R

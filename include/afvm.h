@@ -297,12 +297,12 @@ int afvm_adjoint_step_stages(afvm_ctx* ctx, const void* rho, const void* rhoU, c
                              const void* rhoENa, double dtca, double obja, void* rhoa, void* rhoUa,
                              void* rhoEa, void* S_rhoa, void* S_rhoUa, void* S_rhoEa, void* stream);
 
-/* The face tape of a step: per RK stage and face, the 34 values of the forward face flux
- * that its VJP would otherwise re-evaluate at the highest FP64 cost (the reconstructed face
- * states, the reciprocals and reciprocal square roots of the Roe / Rusanov flux and of the
- * conservative variables, mu(T_F) and the corrected face gradients). Element type: the
- * record type (double for AFVM_FP64, float otherwise); afvm_tape_elements values a step,
- * 3 x 34 x nFaces. Worth keeping in FP64, where the face VJP is bound by the FP64 pipe and
+/* The face tape of a step: per RK stage and face, the 50 values of the forward face flux
+ * that its VJP would otherwise re-evaluate (the reconstructed face states, the reciprocals
+ * and reciprocal square roots of the Roe / Rusanov flux and of the conservative variables,
+ * mu(T_F), the Roe average and eigenvalue intermediates, the viscous stress intermediates).
+ * Element type: the record type (double for AFVM_FP64, float otherwise); afvm_tape_elements
+ * values a step, 3 x 50 x nFaces. Worth keeping in FP64, where the face VJP is bound by the FP64 pipe and
  * HBM is idle; no reference counterpart (adpy's reverse mode re-runs the forward). */
 int64_t afvm_tape_elements(const afvm_ctx* ctx);
 
