@@ -129,38 +129,69 @@ template <typename R, typename Src>
 AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR, const R* N, const R* Fb,
                      const Src& t, R& pLb, R& pRb, R* ULb, R* URb, R& rhoLb, R& rhoRb) {
     const R g = consts<R>(P).gamma, gm1 = consts<R>(P).gm1, ggm1 = consts<R>(P).ggm1, h = R(0.5);
-    // ---- forward values: those dear to recompute from the tape, the cheap ones again (as roe())
+    // ---- forward values: those dear to recompute from the tape, the cheap ones again (as roe());
+    // a lean tape (Src::kFull false) holds only the reciprocals, and the Roe intermediates are
+    // re-evaluated here
     R UnL = dot3(UL, N), UnR = dot3(UR, N);
     R rhoUnL = rhoL * UnL, rhoUnR = rhoR * UnR;
     R rrL = t.get(T_RRL), rrR = t.get(T_RRR);
-    R hL = t.get(T_HL), hR = t.get(T_HR);
     R rsL = t.get(T_RSL), rsR = t.get(T_RSR);
     R sL = rhoL * rsL, sR = rhoR * rsR;
     R rD = t.get(T_RD);
-    R UF[3], dU[3];
-    for (int k = 0; k < 3; k++) { UF[k] = t.get(T_UFR + k); dU[k] = t.get(T_DU + k); }
-    R hF = t.get(T_HF), qF = t.get(T_QF);
-    R a2F = gm1 * (hF - qF);
     R raF = t.get(T_RAF);
-    R aF = a2F * raF;
-    R ra2F = raF * raF;
-    R UnF = t.get(T_UNF);
-    R drho = rhoR - rhoL;
-    R drhoE = t.get(T_DRHOE);
-    R l1 = fabs(UnF), l2 = fabs(UnF + aF), l3 = fabs(UnF - aF);
-    R ea = UnL - UnR;
-    R c2L = g * pL * rrL, c2R = g * pR * rrR;
     R rcL = t.get(T_RCL), rcR = t.get(T_RCR);
+    R re = t.get(T_RE);
+    R c2L = g * pL * rrL, c2R = g * pR * rrR;
     R cL = c2L > R(0) ? c2L * rcL : R(0), cR = c2R > R(0) ? c2R * rcR : R(0);
     R eb_ = cL - cR;
-    R eps = t.get(T_EPS);
+    R ea = UnL - UnR;
+    R drho = rhoR - rhoL;
+    R hL, hR, UF[3], dU[3], hF, qF, UnF, drhoE, eps, L1, L2, L3, abv4, abv5, abv6, abv7;
+    if constexpr (Src::kFull) {
+        hL = t.get(T_HL);
+        hR = t.get(T_HR);
+        for (int k = 0; k < 3; k++) { UF[k] = t.get(T_UFR + k); dU[k] = t.get(T_DU + k); }
+        hF = t.get(T_HF);
+        qF = t.get(T_QF);
+        UnF = t.get(T_UNF);
+        drhoE = t.get(T_DRHOE);
+        eps = t.get(T_EPS);
+        L1 = t.get(T_L1); L2 = t.get(T_L2); L3 = t.get(T_L3);
+        abv4 = t.get(T_ABV4); abv5 = t.get(T_ABV5); abv6 = t.get(T_ABV6); abv7 = t.get(T_ABV7);
+    }
+    R a2F = gm1 * (hF - qF);
+    if constexpr (!Src::kFull) {
+        hL = ggm1 * pL * rrL + h * dot3(UL, UL);
+        hR = ggm1 * pR * rrR + h * dot3(UR, UR);
+        for (int k = 0; k < 3; k++) UF[k] = (UL[k] * sL + UR[k] * sR) * rD;
+        hF = (hL * sL + hR * sR) * rD;
+        qF = h * dot3(UF, UF);
+        a2F = gm1 * (hF - qF);
+        UnF = dot3(UF, N);
+        for (int k = 0; k < 3; k++) dU[k] = rhoR * UR[k] - rhoL * UL[k];
+        drhoE = (hR * rhoR - pR) - (hL * rhoL - pL);
+        eps = h * fabs(ea);
+        eps = eps + h * fabs(eb_);
+        eps = (eps < R(0)) ? eps - consts<R>(P).small : eps + consts<R>(P).small;
+    }
+    R aF = a2F * raF;
+    R ra2F = raF * raF;
+    R l1 = fabs(UnF), l2 = fabs(UnF + aF), l3 = fabs(UnF - aF);
     R eps2 = R(2) * eps;
     bool s1 = l1 < eps2, s2 = l2 < eps2, s3 = l3 < eps2;
-    R re = t.get(T_RE);
-    R L1 = t.get(T_L1), L2 = t.get(T_L2), L3 = t.get(T_L3);
+    if constexpr (!Src::kFull) {
+        L1 = s1 ? R(0.25) * l1 * l1 * re + eps : l1;
+        L2 = s2 ? R(0.25) * l2 * l2 * re + eps : l2;
+        L3 = s3 ? R(0.25) * l3 * l3 * re + eps : l3;
+    }
     R abv2 = h * (L2 - L3);
     R abv3 = h * (L2 + L3) - L1;
-    R abv4 = t.get(T_ABV4), abv5 = t.get(T_ABV5), abv6 = t.get(T_ABV6), abv7 = t.get(T_ABV7);
+    if constexpr (!Src::kFull) {
+        abv4 = gm1 * (qF * drho - dot3(UF, dU) + drhoE);
+        abv5 = UnF * drho - dot3(dU, N);
+        abv6 = abv3 * abv4 * ra2F - abv2 * abv5 * raF;
+        abv7 = abv3 * abv5 - abv2 * abv4 * raF;
+    }
     // ---- reverse
     R Fu[3] = {Fb[1], Fb[2], Fb[3]};
     R frb = Fb[0], feb = Fb[4];
@@ -387,6 +418,19 @@ template <typename R, typename Src>
 AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>& in, const Src& t, const R* Fb,
                         FaceBar<R>& o);
 
+// the corrected face gradient of U that viscous() forms (face-averaged cell gradients, or the
+// ghost's on a characteristic face, with the normal component replaced by snGrad)
+template <typename R>
+AFVM_HD void corrected_gradU(const FaceIn<R>& in, bool chr, R* gU) {
+    R gUF[9];
+    for (int k = 0; k < 9; k++) gUF[k] = chr ? in.gUN[k] : R(0.5) * (in.gUP[k] + in.gUN[k]);
+    for (int i = 0; i < 3; i++) {
+        R snU = (in.UN[i] - in.UP[i]) * in.rdelta;
+        R gUD = gUF[3 * i] * in.D[0] + gUF[3 * i + 1] * in.D[1] + gUF[3 * i + 2] * in.D[2];
+        for (int k = 0; k < 3; k++) gU[3 * i + k] = gUF[3 * i + k] + snU * in.D[k] - gUD * in.D[k];
+    }
+}
+
 // <Fbar, F> differentiated with respect to all 40 inputs of the face (accumulated into out)
 template <typename R>
 AFVM_HD void face_vjp(const Phys& P, int kind, bool inviscid, const FaceIn<R>& in, const R* Fb, FaceBar<R>& o) {
@@ -409,7 +453,7 @@ AFVM_HD void face_vjp(const Phys& P, int kind, bool inviscid, const FaceIn<R>& i
         }
         return;
     }
-    TapeLocal<R> t;
+    TapeLocal<R, sizeof(R) == 8> t;
     R F[5], maxaF;   // dead after inlining: only the tape values are used
     face_flux<R>(P, kind, inviscid, in, F, maxaF, t);
     face_vjp_t<R>(P, kind, inviscid, in, t, Fb, o);
@@ -441,10 +485,23 @@ AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>&
 
         R TFb = R(0), UFb[3] = {R(0), R(0), R(0)}, gTFb[3] = {R(0), R(0), R(0)}, gUFb[9];
         for (int k = 0; k < 9; k++) gUFb[k] = R(0);
-        R tmp2[3], sigma[3];
-        for (int k = 0; k < 3; k++) { tmp2[k] = t.get(T_TMP2 + k); sigma[k] = t.get(T_SIG + k); }
-        viscous_vjp_t<R>(P, TF, UF, t.get(T_MU), t.get(T_GTN), tmp2, t.get(T_TMP3), sigma, in.D, in.N, in.rdelta, Fb,
-                         o.TP, o.TN, o.UP, o.UN, TFb, UFb, gTFb, gUFb);
+        R tmp2[3], sigma[3], tmp3, mu = t.get(T_MU);
+        if constexpr (Src::kFull) {
+            for (int k = 0; k < 3; k++) { tmp2[k] = t.get(T_TMP2 + k); sigma[k] = t.get(T_SIG + k); }
+            tmp3 = t.get(T_TMP3);
+        } else {
+            // the stress terms from the corrected face gradient, as viscous() forms them
+            R gUl[9];
+            corrected_gradU<R>(in, chr, gUl);
+            tmp3 = gUl[0] + gUl[4] + gUl[8];
+            for (int i = 0; i < 3; i++) {
+                tmp2[i] = (gUl[3 * i] + gUl[i]) * in.N[0] + (gUl[3 * i + 1] + gUl[3 + i]) * in.N[1] +
+                          (gUl[3 * i + 2] + gUl[6 + i]) * in.N[2];
+                sigma[i] = mu * (tmp2[i] - R(2.0 / 3) * tmp3 * in.N[i]);
+            }
+        }
+        viscous_vjp_t<R>(P, TF, UF, mu, t.get(T_GTN), tmp2, tmp3, sigma, in.D, in.N, in.rdelta, Fb, o.TP, o.TN, o.UP,
+                         o.UN, TFb, UFb, gTFb, gUFb);
         if (chr) {
             o.TN += TFb;
             for (int k = 0; k < 3; k++) { o.UN[k] += UFb[k]; o.gTN[k] += gTFb[k]; }

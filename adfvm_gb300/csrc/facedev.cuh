@@ -61,6 +61,7 @@ struct TapeStore {
 };
 template <typename R>
 struct TapeLoad {
+    static constexpr bool kFull = true;
     const R* p;
     size_t stride;
     __device__ __forceinline__ R get(int k) const { return __ldg(p + (size_t)k * stride); }

@@ -55,16 +55,23 @@ constexpr int T_ABV4 = 39, T_ABV5 = 40, T_ABV6 = 41, T_ABV7 = 42;
 // viscous intermediates: (grad U + grad U^T).n (3), sigma (3), tr grad U (corrected face gradient)
 constexpr int T_TMP2 = 43, T_SIG = 46, T_TMP3 = 49;
 constexpr int TAPE = 50;
+constexpr int T_LEAN = 23;   // the values up to here: those that cost the most to re-evaluate
 
 struct TapeNone {
     template <typename R>
     AFVM_HD void put(int, R) const {}
 };
 
-template <typename R>
+// A sink/source in registers for the untaped VJP. FULL: all TAPE values (FP64: the VJP then
+// re-evaluates nothing); otherwise the first T_LEAN and the VJP re-evaluates the Roe and
+// viscous intermediates (FP32: fewer values live across the forward, faster)
+template <typename R, bool FULL>
 struct TapeLocal {
-    R v[TAPE];
-    AFVM_HD void put(int k, R x) { v[k] = x; }
+    static constexpr bool kFull = FULL;
+    R v[FULL ? TAPE : T_LEAN];
+    AFVM_HD void put(int k, R x) {
+        if (FULL || k < T_LEAN) v[k] = x;
+    }
     AFVM_HD R get(int k) const { return v[k]; }
 };
 

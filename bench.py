@@ -89,11 +89,11 @@ STEP_BYTES = {('primal', 8): 2904, ('primal', 4): 1524, ('adjoint', 8): 6288, ('
 # mesh by its number of faces (the kernel's traffic grows in proportion to the faces)
 MEASURED_TRAFFIC = {('k_flux', 8): (172.68e6, 798720), ('k_flux', 4): (81.56e6, 798720),
                     ('k_adj_flux', 8): (407.63e6, 798720), ('k_adj_flux', 4): (170.37e6, 798720),
-                    ('k_flux+tape', 8): (355.04e6, 798720), ('k_adj_flux+tape', 8): (577.73e6, 798720)}
+                    ('k_flux+tape', 8): (453.94e6, 798720), ('k_adj_flux+tape', 8): (677.39e6, 798720)}
 # FP64 thread instructions per face (DADD, DMUL, DFMA) of a launch in the same captures
 # (smsp__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on)
 MEASURED_FP64_INST = {'k_flux': (76.0, 149.4, 186.9), 'k_adj_flux': (108.0, 307.9, 456.9),
-                      'k_flux+tape': (75.0, 148.4, 187.9), 'k_adj_flux+tape': (73.0, 221.9, 321.9)}
+                      'k_flux+tape': (74.0, 148.4, 188.9), 'k_adj_flux+tape': (60.0, 173.9, 262.9)}
 
 
 def measured_traffic(kernel, es, nF):

@@ -51,3 +51,23 @@ extern "C" void afvm_host_face_vjp(int n, int kind, int inviscid, const double* 
         memcpy(out + 40 * (size_t)i, &b, sizeof(b));
     }
 }
+
+// the same VJP in FP32 (the lean local tape: the Roe and viscous intermediates re-evaluated)
+extern "C" void afvm_host_face_vjp_f32(int n, int kind, int inviscid, const double* ph, const double* in,
+                                       const double* Fb, double* out) {
+    Phys P = make_phys(ph);
+    P.small = 1e-9;
+    finish_phys(P);
+    for (int i = 0; i < n; i++) {
+        FaceIn<float> fi;
+        float* f = &fi.UP[0];
+        for (int k = 0; k < 55; k++) f[k] = (float)in[55 * (size_t)i + k];
+        float fb[5];
+        for (int k = 0; k < 5; k++) fb[k] = (float)Fb[5 * (size_t)i + k];
+        FaceBar<float> b;
+        zero_bar(b);
+        face_vjp<float>(P, kind, inviscid != 0, fi, fb, b);
+        const float* bo = &b.UP[0];
+        for (int k = 0; k < 40; k++) out[40 * (size_t)i + k] = bo[k];
+    }
+}

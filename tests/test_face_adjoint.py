@@ -33,6 +33,7 @@ def host():
     d = C.POINTER(C.c_double)
     lib.afvm_host_face.argtypes = [C.c_int, C.c_int, C.c_int, d, d, d]
     lib.afvm_host_face_vjp.argtypes = [C.c_int, C.c_int, C.c_int, d, d, d, d]
+    lib.afvm_host_face_vjp_f32.argtypes = [C.c_int, C.c_int, C.c_int, d, d, d, d]
     return lib
 
 
@@ -174,4 +175,22 @@ def test_face_adjoint_matches_autograd(host, kind, cfg):
     scale = np.abs(ref).max(axis=0) + 1e-300
     err = np.abs(out - ref) / scale
     bad = [(NAMES_IN[k], float(err[:, k].max())) for k in range(40) if err[:, k].max() > 1e-10]
+    assert not bad, bad
+
+
+@pytest.mark.parametrize('kind,cfg', CONFIGS)
+def test_fp32_face_adjoint_matches_fp64(host, kind, cfg):
+    """The FP32 VJP (a lean local tape: the Roe and viscous intermediates re-evaluated in the
+    reverse sweep) against the FP64 one (the full tape) on the same faces: within FP32 rounding
+    (1e-3 of each input's largest adjoint; a wrong term would be O(1))."""
+    n = 64
+    X = random_faces(n, 14)
+    Fb = np.random.default_rng(15).normal(size=(n, 5))
+    o64, o32 = np.zeros((n, 40)), np.zeros((n, 40))
+    inv = 1 if cfg['mu'] == 0.0 else 0
+    host.afvm_host_face_vjp(n, KINDS[kind], inv, dp(phys(cfg)), dp(native_in(X)), dp(Fb), dp(o64))
+    host.afvm_host_face_vjp_f32(n, KINDS[kind], inv, dp(phys(cfg)), dp(native_in(X)), dp(Fb), dp(o32))
+    scale = np.abs(o64).max(axis=0) + 1e-300
+    err = np.abs(o32 - o64) / scale
+    bad = [(NAMES_IN[k], float(err[:, k].max())) for k in range(40) if err[:, k].max() > 1e-3]
     assert not bad, bad
