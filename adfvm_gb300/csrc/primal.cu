@@ -159,7 +159,10 @@ __device__ __forceinline__ void grad_cell(const MeshDev<R>& m, const R* __restri
 }
 
 // the cell's whole record (its primitives again, then the gradients) is staged and the block's
-// records written contiguously
+// records written contiguously. Other blocks read the primitives of these records while they
+// are rewritten: the rewrite stores the bits already there (each cell's primitives are read
+// from its own record and written back unchanged), so every read sees the same value whether
+// it lands before or after the store.
 template <typename R>
 __global__ void __launch_bounds__(BLOCK) k_grad(MeshDev<R> m, R* __restrict__ rec) {
     __shared__ __align__(16) R stage[BLOCK * REC];
