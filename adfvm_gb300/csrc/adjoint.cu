@@ -138,13 +138,15 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const
     for (int k = 0; k < 5; k++) pbar[k] = cb[k];
     const R* G = cb + 5;
     R rv = m.rvol[c];
+    {
+        // the cell's own slots at once: sum_s (1 - w'_s) (G . S N'_s) = G . sum_s (1 - w'_s) S N'_s
+        R A[3] = {m.gA[c], m.gA[n + c], m.gA[2 * n + c]};
+        R pb[5];
+        phi_bar<R>(G, A, rv, pb);
+        for (int k = 0; k < 5; k++) pbar[k] += pb[k];
+    }
     for (int s = 0; s < 6; s++) {
         R sn[3] = {m.gsn[(3 * s) * n + c], m.gsn[(3 * s + 1) * n + c], m.gsn[(3 * s + 2) * n + c]};
-        R w = m.gw[s * n + c];
-        R pb[5];
-        phi_bar<R>(G, sn, rv, pb);
-        R omw = -w + R(1);
-        for (int k = 0; k < 5; k++) pbar[k] += omw * pb[k];
         int nb = m.gnb[s * n + c];
         if (nb < m.nIC) {
             // neighbour's gradient: its slot for this face has S N'' = -S N' and weight gwb

@@ -98,7 +98,7 @@ struct HostTables {
     std::vector<int32_t> gnb, accf;
     std::vector<double> gw, gsn, rvol, accw, vol;
     // adjoint
-    std::vector<double> wpf, wnf, gwb;
+    std::vector<double> wpf, wnf, gwb, gA;
     std::vector<int32_t> gsStart, gsList, gslot;
 };
 
@@ -141,6 +141,7 @@ int upload_mesh(Ctx* c, const HostTables& h, MeshDev<R>& m) {
     if ((st = upload(c, &m.wpf, cast<R>(h.wpf)))) return st;
     if ((st = upload(c, &m.wnf, cast<R>(h.wnf)))) return st;
     if ((st = upload(c, &m.gwb, cast<R>(h.gwb)))) return st;
+    if ((st = upload(c, &m.gA, cast<R>(h.gA)))) return st;
     if ((st = upload(c, &m.gsStart, h.gsStart))) return st;
     if ((st = upload(c, &m.gsList, h.gsList))) return st;
     if ((st = upload(c, &m.gslot, h.gslot))) return st;
@@ -343,6 +344,15 @@ int build_tables(Ctx* c, const afvm_mesh_tensors* M, const afvm_patch_bc* bcs, H
     }
     for (int g = 0; g < nG; g++)
         if (h.gslot[g] < 0) return fail(c, AFVM_ERR_BAD_ARG, "ghost without a gradient slot");
+    // the cell's own share of the gradient transpose, sum_s (1 - w'_s) S N'_s (mesh-only): the
+    // adjoint applies it once instead of slot by slot
+    h.gA.assign(3 * n, 0.0);
+    for (int ci = 0; ci < nIC; ci++)
+        for (int k = 0; k < 3; k++) {
+            double a = 0.0;
+            for (int s = 0; s < 6; s++) a += (1.0 - h.gw[s * n + ci]) * h.gsn[(3 * s + k) * n + ci];
+            h.gA[k * n + ci] = a;
+        }
     h.gsStart.assign(nIC + 1, 0);
     for (int g = 0; g < nG; g++) h.gsStart[h.gsrc[g] + 1]++;
     for (int ci = 0; ci < nIC; ci++) h.gsStart[ci + 1] += h.gsStart[ci];

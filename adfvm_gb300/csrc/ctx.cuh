@@ -93,6 +93,7 @@ struct MeshDev {
     const R* wpf;             // nF  A/V_L per face
     const R* wnf;             // nIF A/V_R per internal face
     const R* gwb;             // 6 x nIC: w' of the neighbour's slot that points back at this cell
+    const R* gA;              // 3 x nIC: sum over the slots of (1 - w') S N
     const int32_t* gsStart;   // nIC + 1: ghosts whose source is the cell, CSR offsets
     const int32_t* gsList;    // nG ghost ids ordered by source cell
     const int32_t* gslot;     // nG: slot of the ghost's face in its owner's cellFaces
