@@ -63,7 +63,7 @@ __device__ __forceinline__ void adj_face(const MeshDev<R>& m, const Phys& P, con
 }
 
 template <typename R, typename S, bool TAPED>
-__global__ void __launch_bounds__(FLUX_BLOCK, sizeof(R) == 8 ? 3 : 4) k_adj_flux(MeshDev<R> m, Phys P, const R* __restrict__ rec, R coef,
+__global__ void __launch_bounds__(FLUX_BLOCK, sizeof(R) == 8 ? 3 : 5) k_adj_flux(MeshDev<R> m, Phys P, const R* __restrict__ rec, R coef,
                                                     const S* __restrict__ ar, const S* __restrict__ au,
                                                     const S* __restrict__ ae, R* __restrict__ fadj, int inviscid,
                                                     const R* __restrict__ tape) {

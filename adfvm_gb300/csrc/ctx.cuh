@@ -13,8 +13,9 @@ constexpr int BLOCK = 256;
 // the face kernels hold 160-240 registers a thread in FP64: 128-thread blocks capped to three
 // per SM (12 warps, a few registers spilled to L1 in the VJP) keep more FP64 instructions in
 // flight than one 256-thread block (8 warps); in FP32 the forward flux is capped at 64
-// registers (32 warps). Measured at 128^3: FP64 k_flux 5.47 -> 4.93 ms, k_adj_flux 11.08 ->
-// 10.52 ms, FP32 k_flux 0.240 -> 0.217 ms.
+// registers (32 warps) and the VJP at five blocks (96 registers, 20 warps). Measured at 128^3:
+// FP64 k_flux 5.47 -> 4.93 ms, k_adj_flux 11.08 -> 10.52 ms (untaped), FP32 k_flux 0.240 ->
+// 0.217 ms, FP32 k_adj_flux 0.471 (4 blocks) -> 0.445 (5) / 0.456 ms (6).
 constexpr int FLUX_BLOCK = 128;
 
 // Block-staged record stores. A thread that stores its own W-value record at a W-value stride
