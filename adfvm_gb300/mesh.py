@@ -65,7 +65,7 @@ class Mesh(object):
             else:
                 self.localPatches.append(patchID)
         if self.remotePatches:
-            raise NotImplementedError('processor patches: this build runs one partition per GPU')
+            raise NotImplementedError('processor patches: one partition per GPU is supported')
         self.patches = self.localPatches + self.remotePatches
         self.sortedPatches = sorted(self.localPatches)
         self.defaultBoundary = self.getDefaultBoundary()

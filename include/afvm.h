@@ -33,7 +33,7 @@ extern "C" {
 #define AFVM_ERR_NONFINITE   3   /* a NaN/Inf appeared in a result (reference: MPI.Abort) */
 #define AFVM_ERR_TIMEOUT     4   /* a bounded device-side wait gave up                    */
 #define AFVM_ERR_CUDA        5   /* a CUDA runtime call failed                            */
-#define AFVM_ERR_UNSUPPORTED 6   /* valid input outside what this build implements        */
+#define AFVM_ERR_UNSUPPORTED 6   /* valid input outside what this library implements      */
 
 /* ---- precision of a context ---- */
 #define AFVM_FP64 0              /* all arithmetic and storage in double                  */
