@@ -225,12 +225,14 @@ def measure(case, precision, args, local, dist, world, clocks):
     from adfvm_gb300.solver import RCF
     mesh = case.mesh
     rcf = RCF(mesh, case.bc, objective=case.objective, precision=precision, device=local, **case.config)
-    dt_np = np.float64 if precision == 'fp64' else np.float32
-    tdt = torch.float64 if precision == 'fp64' else torch.float32
+    # state type (FP64 for 'fp64' and 'mixed') and record type (es: FP32 unless 'fp64')
+    dt_np = np.float32 if precision == 'fp32' else np.float64
+    tdt = torch.float32 if precision == 'fp32' else torch.float64
     x = [torch.as_tensor(np.ascontiguousarray(a, dt_np)).cuda() for a in cases.conservative(case)]
     dt = case.dt
     nIC, nIF, nF, nG = mesh.nInternalCells, mesh.nInternalFaces, mesh.nFaces, mesh.nGhostCells
     es = 8 if precision == 'fp64' else 4
+    ss = 4 if precision == 'fp32' else 8
     stream = torch.cuda.current_stream()
 
     def timed(fn, steps):
@@ -326,8 +328,8 @@ def measure(case, precision, args, local, dist, world, clocks):
     te, ta = max_over_ranks([te, ta], dist)
     state_bytes = int(sum(a.nbytes for a in pin))
     e2e = {'value': round(nIC * ke * world / (te + ta) / 1e6, 3), 'unit': UNIT,
-           'h2d_bytes_per_step': state_bytes + int(3 * sum(a.size for a in host_x) * es),
-           'd2h_bytes_per_step': state_bytes + 16 + int(2 * sum(a.size for a in host_x) * es),
+           'h2d_bytes_per_step': state_bytes + int(3 * sum(a.size for a in host_x) * ss),
+           'd2h_bytes_per_step': state_bytes + 16 + int(2 * sum(a.size for a in host_x) * ss),
            'path': 'primal: afvm_primal_step_host (pinned host state in/out, dtc and objective read back); '
                    'adjoint: Adjoint.map (reference input list; state, sources, seeds in; state and source '
                    'adjoints out)',
@@ -576,6 +578,7 @@ def main():
     clocks = ClockSampler(local)
     m64 = measure(case, args.precision, args, local, dist, world, clocks)
     m32 = measure(case, 'fp32', args, local, dist, world, None) if args.precision == 'fp64' else None
+    mmx = measure(case, 'mixed', args, local, dist, world, None) if args.precision == 'fp64' else None
     clk = m64.pop('clocks')
     nIC = mesh.nInternalCells
     line = {'metric': METRIC, 'value': m64['value'], 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
@@ -594,6 +597,8 @@ def main():
             'roofline': m64['roofline'], 'step_model': m64['step_model'], 'kernels': m64['kernels'],
             'adjoint_kernels': m64['adjoint_kernels'], 'gpu_launches': m64['gpu_launches'],
             'e2e': m64['e2e'], 'clocks': clk}
+    if mmx is not None:
+        line['mixed'] = {k: mmx[k] for k in ('value', 'ms_per_step', 'primal', 'adjoint', 'kernels', 'adjoint_kernels')}
     if m32 is not None:
         m32.pop('clocks', None)
         line['fp32'] = {k: m32[k] for k in ('value', 'ms_per_step', 'primal', 'adjoint', 'roofline', 'step_model',
