@@ -4,12 +4,14 @@
 steps on the GPU and returns the final state and the per-step objective (evaluated on the
 stage-1 primitives, adFVM/density.py:412-413). Its backward pass is the reference's
 checkpointed adjoint sweep (apps/adjoint.py:176-404): the forward keeps only every k-th state;
-the backward recomputes the k states of a segment from its checkpoint, then runs the
+the backward recomputes the k states of a segment from its checkpoint, keeping each step's RK
+stage states (and, in FP64 when a segment's tapes fit in 32 GB, its face tape), then runs the
 hand-written adjoint kernels (``afvm_adjoint_step``) through the segment in reverse, with the
 objective seed of step n equal to the incoming gradient of objective n. dt is held fixed per
 step (a fixed-step run, or the dt series recorded by the forward of an adaptive run), as in
 the reference's adjoint. Gradients flow to the initial state and to the source terms.
 """
+import numpy as np
 import torch
 
 
@@ -46,17 +48,22 @@ class _Solve(torch.autograd.Function):
         g_obj = torch.zeros(nSteps, dtype=torch.float64) if g_obj is None else g_obj.detach().double().cpu()
         Sbar = [torch.zeros_like(s) for s in S]
         starts = sorted(ctx.checkpoints)
+        stages = [solver.stage_buffer() for _ in range(k)]
+        taped = solver.record_dtype == np.float64 and k * solver.tape_bytes <= 32e9
+        tapes = [solver.tape_buffer() for _ in range(k)] if taped else [None] * k
         for s0 in reversed(starts):
             s1 = min(s0 + k, nSteps)
-            # recompute the segment's input states
+            # recompute the segment's input states, keeping each step's stages (and tape)
             states = [ctx.checkpoints[s0]]
-            for n in range(s0, s1 - 1):
+            for n in range(s0, s1):
                 x = states[-1]
-                r = solver.step(x[0], x[1], x[2], dts[n], S=S, want_scalars=False)
+                r = solver.step(x[0], x[1], x[2], dts[n], S=S, want_scalars=False, stages=stages[n - s0],
+                                tape=tapes[n - s0])
                 states.append(r[:3])
             for n in range(s1 - 1, s0 - 1, -1):
                 x = states[n - s0]
-                r = solver.adjoint_step(x[0], x[1], x[2], dts[n], a, obja=float(g_obj[n]), S=S, out=a)
+                r = solver.adjoint_step(x[0], x[1], x[2], dts[n], a, obja=float(g_obj[n]), S=S, out=a,
+                                        stages=stages[n - s0], tape=tapes[n - s0])
                 for sb, g in zip(Sbar, r[3]):
                     sb += g
         return a[0], a[1], a[2], Sbar[0], Sbar[1], Sbar[2], None, None, None, None
