@@ -176,7 +176,9 @@ __global__ void __launch_bounds__(BLOCK) k_grad(MeshDev<R> m, R* __restrict__ re
 
 // TAPED: also writes the face tape (TAPE values a face, column-major: tape[k nF + f]) that
 // k_adj_flux<..., true> reads back instead of re-evaluating the forward flux
-template <typename R, bool TAPED>
+// CFL: the stage whose CFL sum is taken (the second, density.py:405-413); the other stages
+// store 0 in the CFL slot and skip its square root
+template <typename R, bool TAPED, bool CFL>
 __global__ void __launch_bounds__(FLUX_BLOCK, sizeof(R) == 8 ? 3 : 8) k_flux(MeshDev<R> m, Phys P, const R* __restrict__ rec,
                                                 R* __restrict__ fflux, int inviscid, R* __restrict__ tape) {
     // (the 6-value face records are stored directly: staging them through shared memory, as
@@ -194,7 +196,7 @@ __global__ void __launch_bounds__(FLUX_BLOCK, sizeof(R) == 8 ? 3 : 8) k_flux(Mes
         face_flux<R>(P, kind, inviscid != 0, in, F, maxaF);
     R* out = fflux + (size_t)f * FREC;
     for (int k = 0; k < 5; k++) out[k] = F[k];
-    out[5] = maxaF;
+    out[5] = CFL ? maxaF : R(0);
 }
 
 // a 6-value face flux record in three 8- (FP32) or 16-byte (FP64) loads; records start on
@@ -448,10 +450,14 @@ void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const S*
     {
         ProfScope ps(c, KID_FLUX, s);
         int nbF = (m.nF + FLUX_BLOCK - 1) / FLUX_BLOCK;
-        if (tape)
-            k_flux<R, true><<<nbF, FLUX_BLOCK, 0, s>>>(m, P, rec, ff, inviscid, tape);
+        if (tape && st == 1)
+            k_flux<R, true, true><<<nbF, FLUX_BLOCK, 0, s>>>(m, P, rec, ff, inviscid, tape);
+        else if (tape)
+            k_flux<R, true, false><<<nbF, FLUX_BLOCK, 0, s>>>(m, P, rec, ff, inviscid, tape);
+        else if (st == 1)
+            k_flux<R, false, true><<<nbF, FLUX_BLOCK, 0, s>>>(m, P, rec, ff, inviscid, nullptr);
         else
-            k_flux<R, false><<<nbF, FLUX_BLOCK, 0, s>>>(m, P, rec, ff, inviscid, nullptr);
+            k_flux<R, false, false><<<nbF, FLUX_BLOCK, 0, s>>>(m, P, rec, ff, inviscid, nullptr);
     }
     int nb = nblocks(m.nIC);
     R* recNext = nextPrims ? rec : nullptr;
