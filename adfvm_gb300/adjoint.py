@@ -88,10 +88,9 @@ class Adjoint(object):
         per-step dt series of the primal run. perturbations: list of (dS_rho, dS_rhoU,
         dS_rhoE) host arrays. keep_stages: the interval's forward re-run also keeps every
         step's RK stage states (10 nInternalCells values a step) so that the adjoint steps
-        do not recompute them. keep_tapes: with keep_stages, also keep every step's face tape
-        (the forward values the face VJP would re-evaluate); None: for FP64 contexts whose
-        interval of tapes fits in 32 GB. Returns (sensitivities, adjoint fields at t0 (host),
-        record)."""
+        do not recompute them. keep_tapes: with keep_stages, also keep every step's tape (its
+        stages' cell records and, in FP64, the face tape); None: when the interval's tapes fit
+        in 32 GB. Returns (sensitivities, adjoint fields at t0 (host), record)."""
         torch = _torch()
         p = self.primal
         if nSteps % writeInterval:
@@ -121,7 +120,7 @@ class Adjoint(object):
         nCk = nSteps // writeInterval
         stages = [p.stage_buffer() for _ in range(writeInterval)] if keep_stages else None
         if keep_tapes is None:
-            keep_tapes = p.record_dtype == np.float64 and writeInterval * p.tape_bytes <= 32e9
+            keep_tapes = writeInterval * p.tape_bytes <= 32e9
         tapes = [p.tape_buffer() for _ in range(writeInterval)] if keep_stages and keep_tapes else None
         for checkpoint in range(nCk):
             primalIndex = nSteps - (checkpoint + 1) * writeInterval

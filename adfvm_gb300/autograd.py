@@ -5,13 +5,12 @@ steps on the GPU and returns the final state and the per-step objective (evaluat
 stage-1 primitives, adFVM/density.py:412-413). Its backward pass is the reference's
 checkpointed adjoint sweep (apps/adjoint.py:176-404): the forward keeps only every k-th state;
 the backward recomputes the k states of a segment from its checkpoint, keeping each step's RK
-stage states (and, in FP64 when a segment's tapes fit in 32 GB, its face tape), then runs the
+stage states and, when a segment's tapes fit in 32 GB, its tape, then runs the
 hand-written adjoint kernels (``afvm_adjoint_step``) through the segment in reverse, with the
 objective seed of step n equal to the incoming gradient of objective n. dt is held fixed per
 step (a fixed-step run, or the dt series recorded by the forward of an adaptive run), as in
 the reference's adjoint. Gradients flow to the initial state and to the source terms.
 """
-import numpy as np
 import torch
 
 
@@ -49,7 +48,7 @@ class _Solve(torch.autograd.Function):
         Sbar = [torch.zeros_like(s) for s in S]
         starts = sorted(ctx.checkpoints)
         stages = [solver.stage_buffer() for _ in range(k)]
-        taped = solver.record_dtype == np.float64 and k * solver.tape_bytes <= 32e9
+        taped = k * solver.tape_bytes <= 32e9
         tapes = [solver.tape_buffer() for _ in range(k)] if taped else [None] * k
         for s0 in reversed(starts):
             s1 = min(s0 + k, nSteps)

@@ -327,19 +327,18 @@ int adjoint_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double 
     R* fadj = (R*)c->fadj;
     R* cbar = (R*)c->cbar;
     S* sb = (S*)c->sbar;
-    const R* rec = (const R*)c->rec;
     int nbC = nblocks(m.nIC);
     const double beta[3] = {1.0, 1. / 4, 2. / 3};
-    // with the face tape only the VJPs of physical boundary faces read cell gradients (their
-    // viscous flux); without such faces the stage's primitives are all the records needed
-    const bool needGrad = !tape || (!inviscid && c->nBoundaryFlux > 0);
+    // a tape holds the stage's cell records the primal step built (no primitive or gradient
+    // launches here) and, in FP64, its face tape
+    const R* faceTape = nullptr;
+    const R* recTape = nullptr;
+    split_tape<const R>(c, tape, faceTape, recTape);
     for (int st = 2; st >= 0; st--) {
         const S* const* u = st == 0 ? u0c : (st == 1 ? u1c : u2c);
-        if (needGrad)
-            launch_prim_grad<R, S>(c, u[0], u[1], u[2], s);
-        else
-            launch_prim<R, S>(c, u[0], u[1], u[2], s);
-        if (st == 1 && c->objective == AFVM_OBJ_VANE) launch_vane_sums<R>(c, s, nullptr, nullptr);
+        const R* rec = recTape ? recTape + (size_t)st * m.nC * REC : (const R*)c->rec;
+        if (!recTape) launch_prim_grad<R, S>(c, u[0], u[1], u[2], s);
+        if (st == 1 && c->objective == AFVM_OBJ_VANE) launch_vane_sums<R>(c, s, nullptr, nullptr, rec);
         // adjoint of this stage's output: a3 = seeds, a2 = A2, a1 = A1
         const S* ain[3];
         if (st == 2) { ain[0] = rhoNa; ain[1] = rhoUNa; ain[2] = rhoENa; }
@@ -349,9 +348,9 @@ int adjoint_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double 
         {
             ProfScope ps(c, KID_ADJ_FLUX, s);
             int nbF = (m.nF + FLUX_BLOCK - 1) / FLUX_BLOCK;
-            if (tape)
+            if (faceTape)
                 k_adj_flux<R, S, true><<<nbF, FLUX_BLOCK, 0, s>>>(m, P, rec, coef, ain[0], ain[1], ain[2], fadj,
-                                                                  inviscid, tape + (size_t)st * TAPE * m.nF);
+                                                                  inviscid, faceTape + (size_t)st * TAPE * m.nF);
             else
                 k_adj_flux<R, S, false><<<nbF, FLUX_BLOCK, 0, s>>>(m, P, rec, coef, ain[0], ain[1], ain[2], fadj,
                                                                    inviscid, nullptr);

@@ -692,7 +692,7 @@ int afvm_set_bc_value(afvm_ctx* ctx, int32_t patch, int32_t field, const double*
 
 int64_t afvm_tape_elements(const afvm_ctx* ctx) {
     if (!ctx) return 0;
-    return (int64_t)tape_elements(reinterpret_cast<const Ctx*>(ctx)->nF);
+    return (int64_t)tape_elements(reinterpret_cast<const Ctx*>(ctx));
 }
 
 int afvm_primal_step_tape(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, double dt,

@@ -216,9 +216,14 @@ int adjoint_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double 
                      S* rhoa, S* rhoUa, S* rhoEa, S* Srhoa, S* SrhoUa, S* SrhoEa, cudaStream_t s,
                      const S* stages = nullptr, const R* tape = nullptr);
 
-// a step's face tapes: one per RK stage, TAPE values a face each (value k of face f of stage st
-// at tape[(st TAPE + k) nF + f]), written by the primal step and read by its adjoint step
-inline size_t tape_elements(int nF) { return (size_t)3 * TAPE * (size_t)nF; }
+// a step's tape, written by the primal step and read by its adjoint step: in FP64 first the
+// face tapes, one per RK stage, TAPE values a face each (value k of face f of stage st at
+// [(st TAPE + k) nF + f]); then, in every precision, the three stages' cell records (REC values
+// a cell, nCells rows each), which spare the adjoint its primitive and gradient launches
+inline size_t face_tape_elements(const Ctx* c);
+inline size_t tape_elements(const Ctx* c);
+template <typename R>
+inline void split_tape(const Ctx* c, R* tape, R*& face, R*& recs);
 
 // the RK stage states u1, u2 of one step in a caller's buffer of 10 nIC values:
 // u1 = [rho (n) | rhoU (3n) | rhoE (n)], then u2 in the same layout
@@ -229,19 +234,20 @@ inline void stage_views(P* stages, int n, P** u1, P** u2) {
 }
 
 // turbine-vane objective partial sums of the stage-1 record now in c->rec into c->vaneSums
+// rec: the cell records to read/write (NULL: the context's)
 template <typename R>
-void launch_vane_sums(Ctx* c, cudaStream_t s, double* dtcOut, double* objOut);
+void launch_vane_sums(Ctx* c, cudaStream_t s, double* dtcOut, double* objOut, const R* rec = nullptr);
 template <typename R, typename S = R>
-void launch_prim(Ctx* c, const S* r, const S* ru, const S* re, cudaStream_t s);
+void launch_prim(Ctx* c, const S* r, const S* ru, const S* re, cudaStream_t s, R* rec = nullptr);
 template <typename R, typename S = R>
-void launch_prim_grad(Ctx* c, const S* r, const S* ru, const S* re, cudaStream_t s);
+void launch_prim_grad(Ctx* c, const S* r, const S* ru, const S* re, cudaStream_t s, R* rec = nullptr);
 // nextPrims: the update also writes the primitives of the state it produces into the cell
 // records (the next stage's k_prim, fused)
 // tape: the stage's face tape to write (NULL: none)
 template <typename R, typename S = R>
 void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const S* const* u0, const S* const* u1,
                         const S* const* u2, const S* Sr, const S* Su, const S* Se, S* const* out, cudaStream_t s,
-                        bool nextPrims = false, R* tape = nullptr);
+                        bool nextPrims = false, R* tape = nullptr, R* recIn = nullptr, R* recOut = nullptr);
 template <typename S>
 void default_sources(Ctx* c, const S*& Srho, const S*& SrhoU, const S*& SrhoE);
 static inline int nblocks(long long n) { return (int)((n + BLOCK - 1) / BLOCK); }
@@ -249,5 +255,19 @@ static inline int nblocks(long long n) { return (int)((n + BLOCK - 1) / BLOCK); 
 template <typename R> inline const MeshDev<R>& meshOf(const Ctx* c);
 template <> inline const MeshDev<double>& meshOf<double>(const Ctx* c) { return c->m64; }
 template <> inline const MeshDev<float>& meshOf<float>(const Ctx* c) { return c->m32; }
+
+inline size_t face_tape_elements(const Ctx* c) {
+    return c->precision == AFVM_FP64 ? (size_t)3 * TAPE * (size_t)c->nF : 0;
+}
+inline size_t tape_elements(const Ctx* c) { return face_tape_elements(c) + (size_t)3 * REC * (size_t)c->nC; }
+template <typename R>
+inline void split_tape(const Ctx* c, R* tape, R*& face, R*& recs) {
+    face = nullptr;
+    recs = nullptr;
+    if (!tape) return;
+    size_t nface = face_tape_elements(c);
+    face = nface ? tape : nullptr;
+    recs = tape + nface;
+}
 
 }  // namespace afvm

@@ -393,12 +393,12 @@ __global__ void k_vane_finish(const double* partials, int nBlocks, VaneDev v, do
 }
 
 template <typename R>
-void launch_vane_sums(Ctx* c, cudaStream_t s, double* dtcOut, double* objOut) {
+void launch_vane_sums(Ctx* c, cudaStream_t s, double* dtcOut, double* objOut, const R* rec) {
     const MeshDev<R>& m = meshOf<R>(c);
     {
         ProfScope ps(c, KID_OBJECTIVE, s);
-        k_obj_vane<R><<<c->nVaneBlocks, BLOCK, 0, s>>>(m, c->phys, (const R*)c->rec, c->vane, c->nVaneBlocks,
-                                                      c->vanePartials);
+        k_obj_vane<R><<<c->nVaneBlocks, BLOCK, 0, s>>>(m, c->phys, rec ? rec : (const R*)c->rec, c->vane,
+                                                      c->nVaneBlocks, c->vanePartials);
     }
     ProfScope ps(c, KID_FINISH, s);
     k_vane_finish<<<1, BLOCK, 0, s>>>(c->vanePartials, c->nVaneBlocks, c->vane, c->vaneSums, c->dtcBits, dtcOut,
@@ -420,17 +420,17 @@ __global__ void k_finish(const double* partials, int nPartials, const unsigned l
 
 
 template <typename R, typename S>
-void launch_prim(Ctx* c, const S* r, const S* ru, const S* re, cudaStream_t s) {
+void launch_prim(Ctx* c, const S* r, const S* ru, const S* re, cudaStream_t s, R* rec) {
     const MeshDev<R>& m = meshOf<R>(c);
     ProfScope ps(c, KID_PRIM, s);
-    k_prim<R, S><<<nblocks(m.nIC + m.nG), BLOCK, 0, s>>>(m, c->phys, r, ru, re, (R*)c->rec);
+    k_prim<R, S><<<nblocks(m.nIC + m.nG), BLOCK, 0, s>>>(m, c->phys, r, ru, re, rec ? rec : (R*)c->rec);
 }
 
 template <typename R, typename S>
-void launch_prim_grad(Ctx* c, const S* r, const S* ru, const S* re, cudaStream_t s) {
+void launch_prim_grad(Ctx* c, const S* r, const S* ru, const S* re, cudaStream_t s, R* rec) {
     const MeshDev<R>& m = meshOf<R>(c);
-    R* rec = (R*)c->rec;
-    launch_prim<R, S>(c, r, ru, re, s);
+    if (!rec) rec = (R*)c->rec;
+    launch_prim<R, S>(c, r, ru, re, s, rec);
     {
         ProfScope ps(c, KID_GRAD, s);
         k_grad<R><<<nblocks(m.nIC), BLOCK, 0, s>>>(m, rec);
@@ -441,10 +441,10 @@ void launch_prim_grad(Ctx* c, const S* r, const S* ru, const S* re, cudaStream_t
 template <typename R, typename S>
 void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const S* const* u0, const S* const* u1,
                         const S* const* u2, const S* Sr, const S* Su, const S* Se, S* const* out, cudaStream_t s,
-                        bool nextPrims, R* tape) {
+                        bool nextPrims, R* tape, R* recIn, R* recOut) {
     const MeshDev<R>& m = meshOf<R>(c);
     const Phys& P = c->phys;
-    R* rec = (R*)c->rec;
+    R* rec = recIn ? recIn : (R*)c->rec;
     R* ff = (R*)c->fflux;
     int inviscid = (P.muModel == AFVM_MU_CONSTANT && P.mu0 == 0.0) ? 1 : 0;
     {
@@ -460,7 +460,7 @@ void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const S*
             k_flux<R, false, false><<<nbF, FLUX_BLOCK, 0, s>>>(m, P, rec, ff, inviscid, nullptr);
     }
     int nb = nblocks(m.nIC);
-    R* recNext = nextPrims ? rec : nullptr;
+    R* recNext = nextPrims ? (recOut ? recOut : rec) : nullptr;
     ProfScope ps(c, KID_UPDATE, s);
     if (st == 0)
         k_update<R, S, 0><<<nb, BLOCK, 0, s>>>(m, ff, dt, dtDev, u0[0], u0[1], u0[2], nullptr, nullptr, nullptr, nullptr,
@@ -503,20 +503,27 @@ int primal_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double d
     bool vaneDone = false;
     if (c->objective == AFVM_OBJ_VANE && !c->vaneSet)
         return fail(c, AFVM_ERR_BAD_ARG, "AFVM_OBJ_VANE needs afvm_set_objective_vane before the first step");
+    // with a tape each stage's cell records are built in the tape's record part (kept for the
+    // adjoint step), else in the context's one record buffer
+    R* faceTape = nullptr;
+    R* recTape = nullptr;
+    split_tape<R>(c, tape, faceTape, recTape);
+    R* recs[3];
+    for (int st = 0; st < 3; st++) recs[st] = recTape ? recTape + (size_t)st * m.nC * REC : (R*)c->rec;
     for (int st = 0; st < 3; st++) {
         const S* const* in = st == 0 ? u0c : (st == 1 ? u1c : u2c);
         if (st == 0) {
-            launch_prim_grad<R, S>(c, in[0], in[1], in[2], s);
+            launch_prim_grad<R, S>(c, in[0], in[1], in[2], s, recs[0]);
         } else {
             // the primitives of stages 1 and 2 were written by the previous stage's update
             ProfScope ps(c, KID_GRAD, s);
-            k_grad<R><<<nblocks(m.nIC), BLOCK, 0, s>>>(m, (R*)c->rec);
+            k_grad<R><<<nblocks(m.nIC), BLOCK, 0, s>>>(m, recs[st]);
         }
         if (st == 1 && c->objective == AFVM_OBJ_VANE) {
             // the partial sums now, while rec holds the stage-1 primitives; combined at the end
             const MeshDev<R>& mm = meshOf<R>(c);
             ProfScope ps(c, KID_OBJECTIVE, s);
-            k_obj_vane<R><<<c->nVaneBlocks, BLOCK, 0, s>>>(mm, P, (const R*)c->rec, c->vane, c->nVaneBlocks,
+            k_obj_vane<R><<<c->nVaneBlocks, BLOCK, 0, s>>>(mm, P, (const R*)recs[1], c->vane, c->nVaneBlocks,
                                                           c->vanePartials);
             vaneDone = true;
         } else if (st == 1 && c->objective != AFVM_OBJ_NONE) {
@@ -526,13 +533,14 @@ int primal_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double d
             if (nObjBlocks > c->nPartials) return fail(c, AFVM_ERR_BAD_ARG, "objective partials overflow");
             if (n > 0) {
                 ProfScope ps(c, KID_OBJECTIVE, s);
-                k_objective<R><<<nObjBlocks, BLOCK, 0, s>>>(m, P, (const R*)c->rec, c->objective, start, n,
+                k_objective<R><<<nObjBlocks, BLOCK, 0, s>>>(m, P, (const R*)recs[1], c->objective, start, n,
                                                             c->partials);
             }
         }
         S* const* out = st == 0 ? u1 : (st == 1 ? u2 : outN);
         launch_flux_update<R, S>(c, st, dt, dtDev, u0c, u1c, u2c, Srho, SrhoU, SrhoE, out, s, st < 2,
-                                 tape ? tape + (size_t)st * TAPE * m.nF : nullptr);
+                                 faceTape ? faceTape + (size_t)st * TAPE * m.nF : nullptr, recs[st],
+                                 st < 2 ? recs[st + 1] : nullptr);
     }
     if (vaneDone) {
         ProfScope ps(c, KID_FINISH, s);
@@ -578,17 +586,17 @@ int primal_run_dev(Ctx* c, S* rho, S* rhoU, S* rhoE, int nSteps, double dt0, dou
                                        const S*, const S*, S*, S*, S*, double*, double*, cudaStream_t, S*, R*);   \
     template int primal_run_dev<R, S>(Ctx*, S*, S*, S*, int, double, double, double, int, const S*, const S*,     \
                                       const S*, double*, double*, double*, cudaStream_t);                         \
-    template void launch_prim<R, S>(Ctx*, const S*, const S*, const S*, cudaStream_t);                           \
-    template void launch_prim_grad<R, S>(Ctx*, const S*, const S*, const S*, cudaStream_t);                      \
+    template void launch_prim<R, S>(Ctx*, const S*, const S*, const S*, cudaStream_t, R*);                       \
+    template void launch_prim_grad<R, S>(Ctx*, const S*, const S*, const S*, cudaStream_t, R*);                  \
     template void launch_flux_update<R, S>(Ctx*, int, double, const double*, const S* const*, const S* const*,   \
                                            const S* const*, const S*, const S*, const S*, S* const*, cudaStream_t,  \
-                                           bool, R*);
+                                           bool, R*, R*, R*);
 AFVM_PRIMAL_INST(double, double)
 AFVM_PRIMAL_INST(float, float)
 AFVM_PRIMAL_INST(float, double)
 template void default_sources<double>(Ctx*, const double*&, const double*&, const double*&);
 template void default_sources<float>(Ctx*, const float*&, const float*&, const float*&);
-template void launch_vane_sums<double>(Ctx*, cudaStream_t, double*, double*);
-template void launch_vane_sums<float>(Ctx*, cudaStream_t, double*, double*);
+template void launch_vane_sums<double>(Ctx*, cudaStream_t, double*, double*, const double*);
+template void launch_vane_sums<float>(Ctx*, cudaStream_t, double*, double*, const float*);
 
 }  // namespace afvm

@@ -123,6 +123,7 @@ class Slot(object):
         self.states = [z() for _ in range(k)]
         self.last = z()                                        # output of the interval's last step
         self.stages = [self.rcf.stage_buffer() for _ in range(k)]
+        self.tapes = [self.rcf.tape_buffer() for _ in range(k)]        # the stages' cell records
         self.a = z()
         self.S = z()
         self.dS = [torch.zeros(s, dtype=torch.float64, device=self.dev) for s in shapes]
@@ -145,14 +146,15 @@ class Slot(object):
         for j in range(self.k):
             y = self.states[j]
             out = self.states[j + 1] if j + 1 < self.k else self.last
-            self.rcf.step(y[0], y[1], y[2], self.dt, S=self.S, out=out, want_scalars=False, stages=self.stages[j])
+            self.rcf.step(y[0], y[1], y[2], self.dt, S=self.S, out=out, want_scalars=False, stages=self.stages[j],
+                          tape=self.tapes[j])
 
     def _adjoint_k(self):
         torch = _torch()
         for j in range(self.k - 1, -1, -1):
             y = self.states[j]
             r = self.rcf.adjoint_step(y[0], y[1], y[2], self.dt, self.a, obja=1.0, S=self.S, out=self.a,
-                                      stages=self.stages[j])
+                                      stages=self.stages[j], tape=self.tapes[j])
             # FP64 sensitivity accumulation (cmesh.computeSensitivity summed over time)
             s = (r[3][0].double() * self.dS[0]).sum() + (r[3][1].double() * self.dS[1]).sum() + \
                 (r[3][2].double() * self.dS[2]).sum()
@@ -232,9 +234,9 @@ class Slot(object):
         torch = _torch()
         es = 8 if self.td == torch.float64 else 4
         n = self.case.mesh.nInternalCells
-        # checkpoints, interval states, last output, x, a, S; the k stage buffers; FP64 dS
+        # checkpoints, interval states, last output, x, a, S; the k stage buffers and tapes; FP64 dS
         return int(self.rcf.device_bytes + (self.nck + self.k + 4) * 5 * n * es + self.k * 10 * n * es +
-                   3 * 5 * n * 8)
+                   self.k * self.rcf.tape_bytes + 3 * 5 * n * 8)
 
 
 class SensitivityServer(object):
@@ -279,10 +281,12 @@ class SensitivityServer(object):
         m = self.lib.get(key).mesh
         er = 8 if self.precision == 'fp64' else 4      # mesh tables, records, face fluxes
         es = 4 if self.precision == 'fp32' else 8      # states, stages, checkpoints, adjoints
-        # per face: tables, flux records, adjoint face records; per cell: tables and cell
-        # records, RK and adjoint work states, checkpoints, interval states and stage buffers
-        return int(m.nFaces * (60 + 28 * er + 40 * er) + m.nInternalCells * (150 + 40 * er + 40 * es
-                   + (self.nPrimal // self.k + 3 * self.k + 8) * 5 * es))
+        # per face: tables, flux records, adjoint face records (and FP64 face tapes); per cell:
+        # tables and cell records, RK and adjoint work states, checkpoints, interval states,
+        # stage buffers and the tapes' cell records
+        face_tape = 3 * 50 * 8 * self.k if self.precision == 'fp64' else 0
+        return int(m.nFaces * (60 + 28 * er + 40 * er + face_tape) + m.nInternalCells * (150 + 40 * er + 40 * es
+                   + (self.nPrimal // self.k + 3 * self.k + 8) * 5 * es) + m.nCells * 3 * 20 * er * self.k)
 
     def _slot_for(self, key):
         for s in self.slots:

@@ -253,9 +253,9 @@ def measure(case, precision, args, local, dist, world, clocks):
     # the last R steps; the adjoint steps walk those steps backwards (cycling when K > R), each
     # on the state, stages and tape of one primal step, carrying the adjoint field as a real
     # sweep does. The ring is capped at 100 GB of tapes.
-    # (FP64 only: there the face VJP is bound by the FP64 pipe and HBM is idle; in FP32 the tape's
-    # bytes cost more than the re-evaluation)
-    use_tape = bool(args.tape) and precision == 'fp64'
+    # (a tape holds each stage's cell records, and in FP64 the face tape as well)
+    use_tape = bool(args.tape)
+    face_taped = use_tape and precision == 'fp64'
     tape_bytes = int(rcf.tape_buffer().numel()) * es if use_tape else 0
     R = max(1, min(args.steps, 32, int(100e9 // tape_bytes) if tape_bytes else 32))
     ring = [x] + [[torch.empty_like(t) for t in x] for _ in range(R)]
@@ -345,8 +345,8 @@ def measure(case, precision, args, local, dist, world, clocks):
             t[1] += v[1]
     top = max(both.items(), key=lambda kv: kv[1][0])[0]
     peak, peak_kind = peaks()
-    alg = algorithmic_bytes(top, nIC, nIF, nF, nG, es, taped=use_tape)
-    topkey = top + ('+tape' if use_tape and top in ('k_flux', 'k_adj_flux') else '')
+    alg = algorithmic_bytes(top, nIC, nIF, nF, nG, es, taped=face_taped)
+    topkey = top + ('+tape' if face_taped and top in ('k_flux', 'k_adj_flux') else '')
     avg_s = both[top][0] / both[top][1] / 1e3
     achieved = alg / avg_s / 1e9
     roofline = {'bound': 'hbm', 'kernel': topkey, 'achieved': round(achieved, 1), 'peak': peak,
@@ -364,7 +364,7 @@ def measure(case, precision, args, local, dist, world, clocks):
             'primal': {'value': round(vp, 3), 'ms_per_step': round(ms_p / K, 4)},
             'adjoint': {'value': round(va, 3), 'ms_per_step': round(ms_a / K, 4)},
             'roofline': roofline, 'kernels': kernels, 'step_model': step_model,
-            '_top': (topkey, avg_s, nF), 'tape': use_tape,
+            '_top': (topkey, avg_s, nF), 'tape': face_taped,
             'adjoint_kernels': {k: {'ms_total': round(v[0], 4), 'launches': v[1], 'ms_avg': round(v[0] / v[1], 5)}
                                 for k, v in prof_a.items()},
             'gpu_launches': int(sum(v[1] for v in prof.values()) + sum(v[1] for v in prof_a.values())),
@@ -589,9 +589,10 @@ def main():
                            l2='inputs larger than L2: %.2f GB device working set' % (m64['device_bytes'] / 1e9),
                            parallelism='replicas' if world > 1 else 'single GPU',
                            step='one SSP-RK3 primal step plus its adjoint step (value = cells x steps / '
-                                '(primal + adjoint time)); the primal steps keep their RK stage states%s and '
-                                'the adjoint steps walk them backwards as a sweep does; primal and adjoint '
-                                'also reported alone' % (' and face tapes' if m64['tape'] else ''),
+                                '(primal + adjoint time)); the primal steps keep their RK stage states and '
+                                'tapes (each stage\'s cell records%s) and the adjoint steps walk them backwards '
+                                'as a sweep does; primal and adjoint also reported alone'
+                                % (', FP64 face tapes' if m64['tape'] else ''),
                            tape=bool(m64['tape'])),
             'primal': m64['primal'], 'adjoint': m64['adjoint'],
             'roofline': m64['roofline'], 'step_model': m64['step_model'], 'kernels': m64['kernels'],

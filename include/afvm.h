@@ -297,23 +297,27 @@ int afvm_adjoint_step_stages(afvm_ctx* ctx, const void* rho, const void* rhoU, c
                              const void* rhoENa, double dtca, double obja, void* rhoa, void* rhoUa,
                              void* rhoEa, void* S_rhoa, void* S_rhoUa, void* S_rhoEa, void* stream);
 
-/* The face tape of a step: per RK stage and face, the 50 values of the forward face flux
- * that its VJP would otherwise re-evaluate (the reconstructed face states, the reciprocals
- * and reciprocal square roots of the Roe / Rusanov flux and of the conservative variables,
- * mu(T_F), the Roe average and eigenvalue intermediates, the viscous stress intermediates).
- * Element type: the record type (double for AFVM_FP64, float otherwise); afvm_tape_elements
- * values a step, 3 x 50 x nFaces. Worth keeping in FP64, where the face VJP is bound by the FP64 pipe and
- * HBM is idle; no reference counterpart (adpy's reverse mode re-runs the forward). */
+/* The tape of a step: what the primal step computed that its adjoint step would otherwise
+ * compute again. In every precision the three RK stages' cell records (20 values a cell:
+ * primitives and gradients), which spare the adjoint its primitive and gradient launches; in
+ * AFVM_FP64 first also the face tape: per stage and face the 50 values of the forward face
+ * flux that its VJP would otherwise re-evaluate (the reconstructed face states, the
+ * reciprocals and reciprocal square roots of the Roe / Rusanov flux and of the conservative
+ * variables, mu(T_F), the Roe average and eigenvalue terms, the viscous stress terms), the
+ * face VJP being bound by the FP64 pipe there while HBM idles. Element type: the record type
+ * (double for AFVM_FP64, float otherwise); afvm_tape_elements values a step (3 x 50 x nFaces
+ * + 3 x 20 x nCells in FP64, 3 x 20 x nCells otherwise). No reference counterpart (adpy's
+ * reverse mode re-runs the forward). */
 int64_t afvm_tape_elements(const afvm_ctx* ctx);
 
-/* afvm_primal_step_stages that also writes the step's face tape (DEVICE, afvm_tape_elements
+/* afvm_primal_step_stages that also writes the step's tape (DEVICE, afvm_tape_elements
  * values; tape needs stages). */
 int afvm_primal_step_tape(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE,
                           double dt, const void* S_rho, const void* S_rhoU, const void* S_rhoE,
                           void* rhoN, void* rhoUN, void* rhoEN, void* stages, void* tape,
                           double* dtc_out, double* obj_out, void* stream);
 
-/* afvm_adjoint_step_stages that reads the face tape the primal step wrote for this state
+/* afvm_adjoint_step_stages that reads the tape the primal step wrote for this state
  * (tape needs stages; NULL: re-evaluate the forward). The result agrees with the re-evaluating
  * step to rounding (the forward kernel may contract products into FMAs differently). */
 int afvm_adjoint_step_tape(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE,
