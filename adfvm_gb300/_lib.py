@@ -115,6 +115,8 @@ SIGNATURES = {
     'afvm_fma_peak': (C.c_int, [C.c_int32, C.c_int32, _d]),
     'afvm_sensitivity_noalloc': (C.c_int, [C.c_int32, C.c_int32, C.POINTER(_d), C.POINTER(_d),
                                            C.POINTER(C.c_int64), _d, _v]),
+    'afvm_copy_to_device': (C.c_int, [C.c_int32, _v, C.c_int32, _v, C.c_int32, C.c_int64, _v]),
+    'afvm_copy_to_host': (C.c_int, [C.c_int32, _v, C.c_int32, _v, C.c_int32, C.c_int64, _v]),
 }
 
 
@@ -166,6 +168,40 @@ def check(status, ctx=None, what=''):
             if m:
                 msg = (what + ': ' if what else '') + m.decode()
         raise AfvmError(status, msg)
+
+
+def to_device(a, t):
+    """Host array `a` (numpy, float64 or float32, any host memory) into the CUDA tensor `t`
+    (same number of values, float64 or float32), converted when the types differ; ordered on
+    t's device's current stream (afvm_copy_to_device)."""
+    import numpy as np
+    import torch
+    a = np.ascontiguousarray(a)
+    if (a.dtype not in (np.float64, np.float32) or t.dtype not in (torch.float64, torch.float32)
+            or a.size != t.numel() or not t.is_contiguous() or t.device.type != 'cuda'):
+        raise ValueError('to_device: %s array of %d values into a %s tensor of %d' % (a.dtype, a.size, t.dtype, t.numel()))
+    stream = torch.cuda.current_stream(t.device).cuda_stream
+    check(lib().afvm_copy_to_device(t.device.index, C.c_void_p(t.data_ptr()), t.element_size(),
+                                    C.c_void_p(a.ctypes.data), a.itemsize, a.size, C.c_void_p(stream)),
+          None, 'afvm_copy_to_device')
+    return t
+
+
+def to_host(t, out):
+    """The CUDA tensor `t` (float64 or float32) into the numpy array `out` (float64 or float32,
+    C-contiguous, same number of values), converted when the types differ; returns once `out`
+    holds the values (afvm_copy_to_host)."""
+    import numpy as np
+    import torch
+    t = t.contiguous()
+    if (out.dtype not in (np.float64, np.float32) or t.dtype not in (torch.float64, torch.float32)
+            or out.size != t.numel() or not out.flags['C_CONTIGUOUS'] or t.device.type != 'cuda'):
+        raise ValueError('to_host: %s tensor of %d values into a %s array of %d' % (t.dtype, t.numel(), out.dtype, out.size))
+    stream = torch.cuda.current_stream(t.device).cuda_stream
+    check(lib().afvm_copy_to_host(t.device.index, C.c_void_p(out.ctypes.data), out.itemsize,
+                                  C.c_void_p(t.data_ptr()), t.element_size(), out.size, C.c_void_p(stream)),
+          None, 'afvm_copy_to_host')
+    return out
 
 
 def dptr(a):

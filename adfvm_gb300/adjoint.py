@@ -42,7 +42,6 @@ class Adjoint(object):
     # ------------------------------------------------------------ per-step map
     def map(self, *inputs, **options):
         """The reference's adjoint step function (apps/adjoint.py:124-126, called at 291)."""
-        torch = _torch()
         p = self.primal
         m = self.mesh
         nT, nS = len(Mesh.gradFields) + len(Mesh.intFields), len(m.getScalar())
@@ -55,14 +54,10 @@ class Adjoint(object):
         nB = len(p.getBoundaryTensor(1))
         p._apply_bc_tensors(list(primal_in[base + 3:base + 3 + nB]))
         p._apply_extra(list(primal_in[base + 3 + nB:]))
-        n = m.nInternalCells
-        dev = 'cuda:%d' % p.device
-        td = torch.float64 if p.dtype == np.float64 else torch.float32
-        T = lambda a, d: torch.as_tensor(np.ascontiguousarray(np.asarray(a).reshape(n, d)), dtype=td, device=dev)
-        x = [T(primal_in[k], d) for k, d in zip(range(3), (1, 3, 1))]
+        x = p.upload(primal_in[:3])
         dt = float(np.asarray(primal_in[3]).reshape(-1)[0])
-        S = [T(primal_in[base + k], d) for k, d in zip(range(3), (1, 3, 1))]
-        seeds = [T(rest[k], d) for k, d in zip(range(3), (1, 3, 1))]
+        S = p.upload(primal_in[base:base + 3])
+        seeds = p.upload(rest[:3])
         dtca = float(np.asarray(rest[3]).reshape(-1)[0])
         obja = float(np.asarray(rest[4]).reshape(-1)[0])
         if dtca != 0.0:
@@ -71,9 +66,8 @@ class Adjoint(object):
         Sh = [primal_in[base + k] for k in range(3)]
         stages = p.kept_stages(primal_in[0], primal_in[1], primal_in[2], dt, Sh)
         r = p.adjoint_step(x[0], x[1], x[2], dt, seeds, obja=obja, S=S, stages=stages)
-        # (FP64 results are returned as they come off the device; FP32 ones widened)
-        host = lambda t: t.cpu().numpy().astype(np.float64, copy=False)
-        return [host(t) for t in r[:3]] + [host(t) for t in r[3]]
+        # float64 host arrays (FP32 results widened on the way)
+        return p.download(list(r[:3]) + list(r[3]))
 
     def computeEnergy(self, adj, state):
         """sqrt of the adjoint energy (apps/adjoint.py:55 over cmesh.computeEnergy); device tensors."""

@@ -755,17 +755,18 @@ int afvm_primal_step_host(afvm_ctx* ctx, const void* rho, const void* rhoU, cons
     const void* hIn[3] = {rho, rhoU, rhoE};
     void* hOut[3] = {rhoN, rhoUN, rhoEN};
     size_t cnt[3] = {n, 3 * n, n};
+    // pinned buffers are copied asynchronously; pageable ones through the pipelined host copy
     for (int k = 0; k < 3; k++) {
-        cudaError_t e = cudaMemcpyAsync(dIn[k], hIn[k], es * cnt[k], cudaMemcpyHostToDevice, s);
-        if (e != cudaSuccess) return cuda_fail(c, e, "state upload");
+        st = host_copy(c->device, dIn[k], (int)es, hIn[k], (int)es, (int64_t)cnt[k], stream, true, false);
+        if (st) return fail(c, st, "state upload");
     }
     const void* S[3] = {S_rho, S_rhoU, S_rhoE};
     void* dS[3] = {nullptr, nullptr, nullptr};
     void* sbuf[3] = {src, src + es * n, src + es * n * 4};
     for (int k = 0; k < 3; k++) {
         if (S[k]) {
-            cudaError_t e = cudaMemcpyAsync(sbuf[k], S[k], es * cnt[k], cudaMemcpyHostToDevice, s);
-            if (e != cudaSuccess) return cuda_fail(c, e, "source upload");
+            st = host_copy(c->device, sbuf[k], (int)es, S[k], (int)es, (int64_t)cnt[k], stream, true, false);
+            if (st) return fail(c, st, "source upload");
             dS[k] = sbuf[k];
         }
     }
@@ -773,8 +774,8 @@ int afvm_primal_step_host(afvm_ctx* ctx, const void* rho, const void* rhoU, cons
                           nullptr, stream);
     if (st) return st;
     for (int k = 0; k < 3; k++) {
-        cudaError_t e = cudaMemcpyAsync(hOut[k], dOut[k], es * cnt[k], cudaMemcpyDeviceToHost, s);
-        if (e != cudaSuccess) return cuda_fail(c, e, "state download");
+        st = host_copy(c->device, hOut[k], (int)es, dOut[k], (int)es, (int64_t)cnt[k], stream, false, false);
+        if (st) return fail(c, st, "state download");
     }
     if (!dtc_out && !obj_out) {
         cudaError_t e = cudaStreamSynchronize(s);

@@ -250,6 +250,12 @@ void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const S*
                         bool nextPrims = false, R* tape = nullptr, R* recIn = nullptr, R* recOut = nullptr);
 template <typename S>
 void default_sources(Ctx* c, const S*& Srho, const S*& SrhoU, const S*& SrhoE);
+// count values between host memory of any kind and the device (element sizes 4 or 8, converted
+// when they differ; hostcopy.cu). toDevice: returns once src has been read. Otherwise returns
+// once dst holds the values, except for a pinned dst of the same type with syncPinned false
+// (then the copy is only queued on the stream).
+int host_copy(int32_t device, void* dst, int32_t dstBytes, const void* src, int32_t srcBytes, int64_t count,
+              void* stream, bool toDevice, bool syncPinned);
 static inline int nblocks(long long n) { return (int)((n + BLOCK - 1) / BLOCK); }
 
 template <typename R> inline const MeshDev<R>& meshOf(const Ctx* c);

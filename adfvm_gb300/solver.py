@@ -279,13 +279,14 @@ class RCF(object):
         self._apply_extra(list(inputs[base + 3 + nBC:]))
         n = m.nInternalCells
         dt = float(np.asarray(dt).reshape(-1)[0])
-        ins = [np.ascontiguousarray(np.asarray(a).reshape(n, d), self.dtype) for a, d in zip((rho, rhoU, rhoE), (1, 3, 1))]
-        Ss = [np.ascontiguousarray(np.asarray(a).reshape(n, d), self.dtype) if a is not None else None
-              for a, d in zip(S, (1, 3, 1))]
+        ins = self._host_fields((rho, rhoU, rhoE))
+        Ss = self._host_fields(S)
         if all(s is not None and not s.any() for s in Ss):
             Ss = [None, None, None]
         if self.keep_stages:
             return self._map_keeping_stages((rho, rhoU, rhoE), ins, Ss, dt)
+        ins = [np.ascontiguousarray(a, self.dtype) for a in ins]
+        Ss = [None if a is None else np.ascontiguousarray(a, self.dtype) for a in Ss]
         outs = [np.empty((n, d), self.dtype) for d in (1, 3, 1)]
         dtc = C.c_double()
         obj = C.c_double()
@@ -303,6 +304,34 @@ class RCF(object):
     # identity, dt and a sample of their values), for the last keep_stages calls; Adjoint.map
     # then skips the forward recompute. keep_stages = 0 turns this off.
     keep_stages = 32
+
+    def _host_fields(self, arrays):
+        """(rho, rhoU, rhoE)-shaped host arrays as (n,1), (n,3), (n,1) views, float64 or float32
+        as given (other types become float64); None stays None."""
+        n = self.mesh.nInternalCells
+        out = []
+        for a, d in zip(arrays, (1, 3, 1)):
+            if a is None:
+                out.append(None)
+                continue
+            a = np.asarray(a)
+            if a.dtype not in (np.float64, np.float32):
+                a = a.astype(np.float64)
+            out.append(np.ascontiguousarray(a.reshape(n, d)))
+        return out
+
+    def upload(self, arrays):
+        """Device tensors of the state type from (rho, rhoU, rhoE)-shaped host arrays of any
+        float type in any host memory, through the library's pipelined host copy."""
+        torch = _torch()
+        td = torch.float64 if self.dtype == np.float64 else torch.float32
+        dev = 'cuda:%d' % self.device
+        return [L.to_device(a, torch.empty(a.shape, dtype=td, device=dev)) for a in self._host_fields(arrays)]
+
+    @staticmethod
+    def download(tensors, dtype=np.float64):
+        """New host arrays of `dtype` holding the device tensors (pipelined host copy)."""
+        return [L.to_host(t, np.empty(tuple(t.shape), dtype)) for t in tensors]
 
     def _fingerprint(self, arrays, dt):
         parts = [repr(float(dt)).encode(), str(getattr(self, '_bcVersion', 0)).encode()]
@@ -329,11 +358,11 @@ class RCF(object):
             buf = self._stageCache.popitem(last=False)[1][1]
         else:
             buf = self.stage_buffer()
-        x = [torch.from_numpy(a).to(dev) for a in ins]
-        Sd = None if Ss[0] is None else [torch.from_numpy(a).to(dev) for a in Ss]
+        x = self.upload(ins)
+        Sd = None if Ss[0] is None else self.upload(Ss)
         r = self.step(x[0], x[1], x[2], dt, S=Sd, out=x, stages=buf)
         self._stageCache[key] = (fp, buf)
-        outs = [t.cpu().numpy() for t in r[:3]]
+        outs = self.download(r[:3], self.dtype)
         return outs + [np.array([[r[3]]]), np.array([[r[4]]])]
 
     def kept_stages(self, rho, rhoU, rhoE, dt, S=None):
@@ -344,10 +373,8 @@ class RCF(object):
         hit = cache.get((id(rho), id(rhoU), id(rhoE)))
         if hit is None:
             return None
-        n = self.mesh.nInternalCells
-        ins = [np.ascontiguousarray(np.asarray(a).reshape(n, d), self.dtype) for a, d in zip((rho, rhoU, rhoE), (1, 3, 1))]
-        Ss = [None, None, None] if S is None else [np.ascontiguousarray(np.asarray(a).reshape(n, d), self.dtype)
-                                                   for a, d in zip(S, (1, 3, 1))]
+        ins = self._host_fields((rho, rhoU, rhoE))
+        Ss = [None, None, None] if S is None else self._host_fields(S)
         if all(s is not None and not s.any() for s in Ss):
             Ss = [None, None, None]
         return hit[1] if hit[0] == self._fingerprint(list(ins) + list(Ss), dt) else None

@@ -373,6 +373,22 @@ int afvm_adjoint_energy(afvm_ctx* ctx, const void* rhoa, const void* rhoUa, cons
 int afvm_sensitivity_noalloc(int32_t device, int32_t nArrays, const double* const* grad,
                              const double* const* pert, const int64_t* n, double* out, void* stream);
 
+/* ---- field arrays between any host memory and the device ----
+ * The reference passes its compiled step numpy arrays (pageable host memory) every call and
+ * gets numpy arrays back (adFVM/solver.py:312-323 inputs and outputs of self.map;
+ * apps/adjoint.py:268-291 for the adjoint map); these two calls are that transfer. `count`
+ * values of srcBytes bytes each (8: double, 4: float) become `count` values of dstBytes bytes,
+ * converted (round to nearest) when the sizes differ. Host memory may be pageable or pinned;
+ * device arrays live on CUDA device `device`, and the copy is ordered on `stream`.
+ * Pageable or converted data moves through two pinned 8 MB staging chunks per device, filled
+ * or drained by all OpenMP threads while the other chunk is on the link; calls on one device
+ * are serialised by a lock. afvm_copy_to_device returns once `src` has been read (the device
+ * data is ready in stream order); afvm_copy_to_host returns when `dst` holds the values. */
+int afvm_copy_to_device(int32_t device, void* dst, int32_t dstBytes, const void* src, int32_t srcBytes,
+                        int64_t count, void* stream);
+int afvm_copy_to_host(int32_t device, void* dst, int32_t dstBytes, const void* src, int32_t srcBytes,
+                      int64_t count, void* stream);
+
 /* ---- per-launch timing (the analogue of the reference's timeFunction decorator and
  * per-step timers, adFVM/config.py:158-168, adFVM/solver.py:322-346) ----
  * afvm_profile(ctx, 1) clears the record and brackets every later kernel launch of the
