@@ -37,6 +37,7 @@ class Adjoint(object):
         self.viscousInterval = viscousInterval
         self.mesh = primal.mesh
         self.names = [n + 'a' for n in primal.names]
+        self._fwd = None   # map's forward buffers: None (not sized yet), False (do not fit)
         self.nParams = 3
 
     # ------------------------------------------------------------ per-step map
@@ -65,9 +66,31 @@ class Adjoint(object):
         # the stages the primal map kept for this very state, if any
         Sh = [primal_in[base + k] for k in range(3)]
         stages = p.kept_stages(primal_in[0], primal_in[1], primal_in[2], dt, Sh)
-        r = p.adjoint_step(x[0], x[1], x[2], dt, seeds, obja=obja, S=S, stages=stages)
+        tape = None
+        if stages is None:
+            stages, tape = self._forward_with_tape(x, dt, S)
+        r = p.adjoint_step(x[0], x[1], x[2], dt, seeds, obja=obja, S=S, stages=stages, tape=tape)
         # float64 host arrays (FP32 results widened on the way)
         return p.download(list(r[:3]) + list(r[3]))
+
+    def _forward_with_tape(self, x, dt, S):
+        """The primal step of the map's state run once more with its stage states and tape kept
+        (buffers reused across calls), so that the adjoint step reads the forward's cell records
+        (and, in FP64, its face values) instead of re-evaluating them: the re-evaluation inside
+        the FP64 face VJP costs more FP64 instructions than the forward flux that writes the
+        tape. (None, None) - the adjoint step then recomputes its forward itself - when the
+        buffers would take more than a quarter of the device's free memory."""
+        p = self.primal
+        if self._fwd is None:
+            torch = _torch()
+            free = torch.cuda.mem_get_info(p.device)[0]
+            need = p.tape_bytes + 10 * self.mesh.nInternalCells * np.dtype(p.dtype).itemsize
+            self._fwd = (p.stage_buffer(), p.tape_buffer()) if need <= free // 4 else False
+        if not self._fwd:
+            return None, None
+        st, tp = self._fwd
+        p.step(x[0], x[1], x[2], dt, S=S, want_scalars=False, stages=st, tape=tp)
+        return st, tp
 
     def computeEnergy(self, adj, state):
         """sqrt of the adjoint energy (apps/adjoint.py:55 over cmesh.computeEnergy); device tensors."""

@@ -74,6 +74,10 @@ def test_bad_arguments():
 
 @pytest.mark.parametrize('precision', ['fp64', 'fp32', 'mixed'])
 def test_adjoint_map_matches_adjoint_step(precision):
+    """Adjoint.map runs the forward with its stages and tape kept and then the taped adjoint
+    step: bit for bit that device path; without room for the tape (forced here), bit for bit
+    the adjoint step that recomputes its forward. The two agree within the taped adjoint's
+    tolerances (FMA contraction differs between the kernels)."""
     case, g = G.load('cyl32x16')
     rcf = RCF(case.build_mesh(), case.bc, objective=case.objective, precision=precision, **case.config)
     n = rcf.mesh.nInternalCells
@@ -83,17 +87,28 @@ def test_adjoint_map_matches_adjoint_step(precision):
     rng = np.random.default_rng(3)
     seeds = [rng.standard_normal((n, d)) * 1e-3 for d in (1, 3, 1)]
     inputs = rcf.mapInputs(*x, dt) + seeds + [np.zeros((1, 1)), np.ones((1, 1)), np.zeros((1, 1))]
-    got = Adjoint(rcf).map(*inputs)
+    adj = Adjoint(rcf)
+    got = adj.map(*inputs)
+    assert adj._fwd
+    adj._fwd = False
+    got_untaped = adj.map(*inputs)
     td = torch.float64 if rcf.dtype == np.float64 else torch.float32
     xd = [torch.as_tensor(a.astype(rcf.dtype), device='cuda:0') for a in x]
     sd = [torch.as_tensor(a.astype(rcf.dtype), device='cuda:0') for a in seeds]
     zero = [torch.zeros((n, d), dtype=td, device='cuda:0') for d in (1, 3, 1)]
-    r = rcf.adjoint_step(xd[0], xd[1], xd[2], dt, sd, obja=1.0, S=zero)
+    st, tp = rcf.stage_buffer(), rcf.tape_buffer()
+    rcf.step(xd[0], xd[1], xd[2], dt, S=zero, stages=st, tape=tp)
+    r = rcf.adjoint_step(xd[0], xd[1], xd[2], dt, sd, obja=1.0, S=zero, stages=st, tape=tp)
     want = [t.double().cpu().numpy() for t in list(r[:3]) + list(r[3])]
-    assert len(got) == len(want)
-    for a, b in zip(got, want):
+    r0 = rcf.adjoint_step(xd[0], xd[1], xd[2], dt, sd, obja=1.0, S=zero)
+    want_untaped = [t.double().cpu().numpy() for t in list(r0[:3]) + list(r0[3])]
+    tol = 1e-5 if precision == 'fp32' else (1e-6 if precision == 'mixed' else 1e-13)
+    assert len(got) == len(want) == len(got_untaped) == 6
+    for a, b, c, d in zip(got, want, got_untaped, want_untaped):
         assert a.dtype == np.float64 and a.shape == b.shape
         assert np.array_equal(a, b)
+        assert np.array_equal(c, d)
+        assert G.rel_err(a, c) <= tol
     # the primal map (which keeps its stages for the adjoint map) returns the device step's state
     out = rcf.map(*rcf.mapInputs(*x, dt))
     y = rcf.step(xd[0], xd[1], xd[2], dt, S=zero)
