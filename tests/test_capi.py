@@ -73,3 +73,19 @@ def test_null_arguments_return_status():
     assert lib.afvm_boundary_values(None, None, None, None, None, None) == L.AFVM_ERR_BAD_ARG
     out = C.c_void_p()
     assert lib.afvm_ctx_create(None, None, None, 0, 0, C.byref(out)) == L.AFVM_ERR_BAD_ARG
+
+
+def test_host_copy_argument_checks():
+    """afvm_copy_to_device / afvm_copy_to_host reject bad element sizes, negative counts, null
+    pointers and negative devices before any CUDA call; an empty copy is a no-op."""
+    lib = L.lib()
+    a = np.zeros(4)
+    hp = C.c_void_p(a.ctypes.data)
+    for fn in (lib.afvm_copy_to_device, lib.afvm_copy_to_host):
+        assert fn(0, None, 8, None, 8, 0, None) == L.AFVM_OK
+        assert fn(0, None, 8, hp, 8, 4, None) == L.AFVM_ERR_BAD_ARG
+        assert fn(0, hp, 8, None, 8, 4, None) == L.AFVM_ERR_BAD_ARG
+        assert fn(0, hp, 2, hp, 8, 4, None) == L.AFVM_ERR_BAD_ARG
+        assert fn(0, hp, 8, hp, 16, 4, None) == L.AFVM_ERR_BAD_ARG
+        assert fn(0, hp, 8, hp, 8, -1, None) == L.AFVM_ERR_BAD_ARG
+        assert fn(-1, hp, 8, hp, 8, 4, None) == L.AFVM_ERR_BAD_ARG
