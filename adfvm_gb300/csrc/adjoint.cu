@@ -250,19 +250,37 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const
         }
     }
     // primitive VJP (density.py:162-171)
-    double rho = ur[c], rU[3] = {uu[3 * c], uu[3 * c + 1], uu[3 * c + 2]}, rE = ue[c];
-    double rr = rcp(rho);
-    double U[3] = {rU[0] * rr, rU[1] * rr, rU[2] * rr};
-    double E = rE * rr;
-    double e = E - 0.5 * (U[0] * U[0] + U[1] * U[1] + U[2] * U[2]);
-    double eb = (double)pbar[R_T] * P.rCv + (double)pbar[R_P] * P.gm1 * rho;
-    double rhob = (double)pbar[R_P] * P.gm1 * e;
-    double Ubt[3];
-    for (int k = 0; k < 3; k++) Ubt[k] = (double)pbar[k] - eb * U[k];
-    double J[5];
-    for (int k = 0; k < 3; k++) J[1 + k] = Ubt[k] * rr;
-    J[4] = eb * rr;
-    J[0] = rhob - (Ubt[0] * U[0] + Ubt[1] * U[1] + Ubt[2] * U[2]) * rr - eb * E * rr;
+    S J[5];
+    if constexpr (sizeof(S) == 4) {
+        // float state: the density row without the low-Mach cancellation of the form below
+        // (rhob and eb E/rho both hold pbar_p (g-1) E): with q = |U|^2/2 and e = E - q,
+        //   J_rho = pbar_p (g-1) q - (pbar_U . U)/rho + (pbar_T/Cv) (q - e)/rho,
+        // which float evaluates to its own rounding, so the FP32 context needs no FP64 here
+        const PhysR<float>& Q = consts<float>(P);
+        float rho = ur[c], rr = rcp(rho);
+        float U[3] = {uu[3 * c] * rr, uu[3 * c + 1] * rr, uu[3 * c + 2] * rr};
+        float E = ue[c] * rr;
+        float q = 0.5f * (U[0] * U[0] + U[1] * U[1] + U[2] * U[2]);
+        float e = E - q;
+        float pT = pbar[R_T] * Q.rCv, pp = pbar[R_P] * Q.gm1;
+        float eb = pT + pp * rho;
+        for (int k = 0; k < 3; k++) J[1 + k] = (pbar[k] - eb * U[k]) * rr;
+        J[4] = eb * rr;
+        J[0] = pp * q - (pbar[0] * U[0] + pbar[1] * U[1] + pbar[2] * U[2]) * rr + pT * (q - e) * rr;
+    } else {
+        double rho = ur[c], rU[3] = {uu[3 * c], uu[3 * c + 1], uu[3 * c + 2]}, rE = ue[c];
+        double rr = rcp(rho);
+        double U[3] = {rU[0] * rr, rU[1] * rr, rU[2] * rr};
+        double E = rE * rr;
+        double e = E - 0.5 * (U[0] * U[0] + U[1] * U[1] + U[2] * U[2]);
+        double eb = (double)pbar[R_T] * P.rCv + (double)pbar[R_P] * P.gm1 * rho;
+        double rhob = (double)pbar[R_P] * P.gm1 * e;
+        double Ubt[3];
+        for (int k = 0; k < 3; k++) Ubt[k] = (double)pbar[k] - eb * U[k];
+        for (int k = 0; k < 3; k++) J[1 + k] = Ubt[k] * rr;
+        J[4] = eb * rr;
+        J[0] = rhob - (Ubt[0] * U[0] + Ubt[1] * U[1] + Ubt[2] * U[2]) * rr - eb * E * rr;
+    }
     // SSP-RK reverse (timestep.py:35-45 transposed), in the state's type S
     S ain[5] = {ainr[c], ainu[3 * c], ainu[3 * c + 1], ainu[3 * c + 2], aine[c]};
     S out[5];
