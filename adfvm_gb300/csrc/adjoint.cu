@@ -82,15 +82,19 @@ __global__ void __launch_bounds__(FLUX_BLOCK, sizeof(R) == 8 ? 3 : 5) k_adj_flux
 template <typename R>
 __device__ __forceinline__ void adj_cell_gather(const MeshDev<R>& m, const R* __restrict__ fadj, int c, R* row) {
     const size_t n = m.nIC;
+    // the first slot initialises the sums: adding it to zeros would cost 20 more adds (FP64
+    // pipe issues in double) and changes nothing but the sign of a zero
     R acc[CBAR];
-    for (int k = 0; k < CBAR; k++) acc[k] = R(0);
     for (int s = 0; s < 6; s++) {
         int e = m.accf[s * n + c];
         bool ownerSide = e >= 0;
         int f = ownerSide ? e : ~e;
-        R v[20];
-        load_vec(fadj + (size_t)f * FADJ + (ownerSide ? 0 : 20), v, 20);
-        for (int k = 0; k < 20; k++) acc[k] += v[k];
+        R v[CBAR];
+        load_vec(fadj + (size_t)f * FADJ + (ownerSide ? 0 : CBAR), v, CBAR);
+        if (s == 0)
+            for (int k = 0; k < CBAR; k++) acc[k] = v[k];
+        else
+            for (int k = 0; k < CBAR; k++) acc[k] += v[k];
     }
     // gradient adjoints of the ghosts whose gradient is a copy of this cell's
     for (int q = m.gsStart[c]; q < m.gsStart[c + 1]; q++) {
