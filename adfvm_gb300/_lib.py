@@ -76,6 +76,12 @@ class ObjectiveVane(C.Structure):
                 ('a', C.c_double), ('b', C.c_double)]
 
 
+class ParamGrad(C.Structure):
+    _fields_ = [('areas', _d), ('volumesL', _d), ('volumesR', _d), ('weights', _d), ('deltas', _d),
+                ('normals', _d), ('deltasUnit', _d), ('linearWeights', _d), ('quadraticWeights', _d),
+                ('volumes', _d), ('bcPatch', C.c_int32), ('bcField', C.c_int32), ('bc', _d)]
+
+
 # name -> (restype, argtypes); every symbol declared in include/afvm.h
 SIGNATURES = {
     'afvm_mesh_build': (C.c_int, [C.POINTER(MeshIn), C.POINTER(MeshOut)]),
@@ -89,6 +95,8 @@ SIGNATURES = {
     'afvm_ctx_device_bytes': (C.c_int64, [_v]),
     'afvm_set_bc_value': (C.c_int, [_v, C.c_int32, C.c_int32, _d]),
     'afvm_set_objective_vane': (C.c_int, [_v, C.POINTER(ObjectiveVane)]),
+    'afvm_set_objective_sink': (C.c_int, [_v, _v]),
+    'afvm_set_objective_seed': (C.c_int, [_v, _v]),
     'afvm_primal_step': (C.c_int, [_v, _v, _v, _v, C.c_double, _v, _v, _v, _v, _v, _v, _d, _d, _v]),
     'afvm_primal_step_stages': (C.c_int, [_v, _v, _v, _v, C.c_double, _v, _v, _v, _v, _v, _v, _v, _d, _d, _v]),
     'afvm_primal_step_host': (C.c_int, [_v, _v, _v, _v, C.c_double, _v, _v, _v, _v, _v, _v, _d, _d, _v]),
@@ -103,6 +111,9 @@ SIGNATURES = {
                                         C.POINTER(C.c_double), C.POINTER(C.c_double), _v]),
     'afvm_adjoint_step_tape': (C.c_int, [_v, _v, _v, _v, C.c_double, _v, _v, _v, _v, _v, _v, _v, _v,
                                          C.c_double, C.c_double, _v, _v, _v, _v, _v, _v, _v]),
+    'afvm_adjoint_step_params': (C.c_int, [_v, _v, _v, _v, C.c_double, _v, _v, _v, _v, _v, _v, _v, _v,
+                                           C.c_double, C.c_double, _v, _v, _v, _v, _v, _v,
+                                           C.POINTER(ParamGrad), _v]),
     'afvm_sensitivity': (C.c_int, [_v, C.c_int32, C.POINTER(_d), C.POINTER(_d),
                                    C.POINTER(C.c_int64), _d, _v]),
     'afvm_adjoint_energy': (C.c_int, [_v, _v, _v, _v, _v, _v, _v, _d, _v]),

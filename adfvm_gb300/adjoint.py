@@ -3,12 +3,14 @@
 * ``Adjoint.map(*inputs)`` is the per-step adjoint function the reference builds with
   ``primal.map.grad()`` (apps/adjoint.py:94-151): inputs are the primal step's inputs followed
   by the adjoint seeds ``[rhoNa, rhoUNa, rhoENa, dtca, obja]`` and ``[scaling]``; outputs are
-  ``[rhoa, rhoUa, rhoEa]`` and the gradients of the source terms (``parameters = 'source'``).
+  ``[rhoa, rhoUa, rhoEa]`` and the gradients of the parameters: the three source terms
+  (``parameters = 'source'``), the ten Mesh.gradFields tensors (``'mesh'``), or one boundary
+  input (``('BCs', field, patch, key)``), apps/adjoint.py:104-121.
 * ``Adjoint.run(...)`` is the checkpointed backward sweep (apps/adjoint.py:176-404): the
   primal is re-run forward one checkpoint interval at a time (keeping every state of the
   interval on the device), then the adjoint steps run backwards through it with seeds
   dtca = 0, obja = 1; after every step the sensitivity to each perturbation is the FP64 dot
-  product of the source gradients with it (cmesh.computeSensitivity), summed over steps past
+  product of the parameter gradients with it (cmesh.computeSensitivity), summed over steps past
   ``avgStart`` and divided by ``nSteps - avgStart`` as writeResult does (apps/problem.py:47-49).
   Adjoint fields are the plain gradients of the state (the reference keeps them multiplied
   by the cell volume, apps/adjoint.py:188; divide by the volumes to compare with its files).
@@ -29,8 +31,14 @@ class Adjoint(object):
         with a viscosityType ('turkel', 'abarbanel', 'uniform') every viscousInterval-th step of
         the sweep is followed by the artificial-viscosity smoothing (apps/adjoint.py:127-139,
         250, 288-289)."""
-        if parameters != 'source':
-            raise NotImplementedError("parameters other than 'source' are not implemented")
+        self.parameters = parameters
+        if parameters == 'source':
+            self.nParams = 3
+        elif parameters == 'mesh':
+            self.nParams = len(primal.MESH_GRAD_FIELDS)
+        else:
+            primal._bc_param(parameters)          # raises for anything else
+            self.nParams = 1
         self.primal = primal
         self.scaling = adjParams[0] if adjParams else None
         self.viscosityType = adjParams[1] if adjParams else None
@@ -38,7 +46,16 @@ class Adjoint(object):
         self.mesh = primal.mesh
         self.names = [n + 'a' for n in primal.names]
         self._fwd = None   # map's forward buffers: None (not sized yet), False (do not fit)
-        self.nParams = 3
+
+    def _step(self, y, dt, a, S, out=None, stages=None, tape=None, obja=1.0):
+        """One adjoint step; returns (state adjoints, parameter gradients as device tensors)."""
+        p = self.primal
+        if self.parameters == 'source':
+            r = p.adjoint_step(y[0], y[1], y[2], dt, a, obja=obja, S=S, out=out, stages=stages, tape=tape)
+            return r[:3], list(r[3])
+        r = p.adjoint_step(y[0], y[1], y[2], dt, a, obja=obja, S=S, out=out, source_grad=False, stages=stages,
+                           tape=tape, params=self.parameters)
+        return r[:3], r[4]
 
     # ------------------------------------------------------------ per-step map
     def map(self, *inputs, **options):
@@ -69,9 +86,9 @@ class Adjoint(object):
         tape = None
         if stages is None:
             stages, tape = self._forward_with_tape(x, dt, S)
-        r = p.adjoint_step(x[0], x[1], x[2], dt, seeds, obja=obja, S=S, stages=stages, tape=tape)
+        adj, grads = self._step(x, dt, seeds, S, stages=stages, tape=tape, obja=obja)
         # float64 host arrays (FP32 results widened on the way)
-        return p.download(list(r[:3]) + list(r[3]))
+        return p.download(list(adj) + list(grads))
 
     def _forward_with_tape(self, x, dt, S):
         """The primal step of the map's state run once more with its stage states and tape kept
@@ -102,8 +119,10 @@ class Adjoint(object):
         """Checkpointed adjoint sweep on the device.
 
         fields: initial conservative state (host arrays). dt: a float (fixed step) or the
-        per-step dt series of the primal run. perturbations: list of (dS_rho, dS_rhoU,
-        dS_rhoE) host arrays. keep_stages: the interval's forward re-run also keeps every
+        per-step dt series of the primal run. perturbations: list of perturbations of the
+        parameters, each a tuple of host arrays shaped like the parameter gradients ((dS_rho,
+        dS_rhoU, dS_rhoE) for 'source', the ten mesh tensors for 'mesh', the one boundary
+        input otherwise). keep_stages: the interval's forward re-run also keeps every
         step's RK stage states (10 nInternalCells values a step) so that the adjoint steps
         do not recompute them. keep_tapes: with keep_stages, also keep every step's tape (its
         stages' cell records and, in FP64, the face tape); None: when the interval's tapes fit
@@ -154,12 +173,11 @@ class Adjoint(object):
                 y = states[adjointIndex]
                 sb = stages[adjointIndex] if keep_stages else None
                 tb = tapes[adjointIndex] if tapes else None
-                r = p.adjoint_step(y[0], y[1], y[2], dts[primalIndex + adjointIndex], a, obja=1.0, S=S, out=a,
-                                   stages=sb, tape=tb)
+                _, pgrads = self._step(y, dts[primalIndex + adjointIndex], a, S, out=a, stages=sb, tape=tb)
                 if self.viscosityType and (step + 1) % self.viscousInterval == 0:
                     p.adjoint_viscosity(y[0], y[1], y[2], a, dts[primalIndex + adjointIndex], self.viscosityType,
                                         self.scaling)
-                grads = [g.reshape(-1).double() for g in r[3]]
+                grads = [g.reshape(-1).double() for g in pgrads]
                 sens = [p.sensitivity(grads, pert) for pert in perts]
                 sens_series.append(sens)
                 if (nSteps - (primalIndex + adjointIndex)) > avgStart:

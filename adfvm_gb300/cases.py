@@ -66,10 +66,13 @@ def sod(n=1000, side='empty', riemann='eulerRoe', cfl=0.5, smooth_cells=2.0):
                 dt=1e-7)
     mesh = case.build_mesh()
     x = mesh.cellCentres[:mesh.nInternalCells, 0:1]
-    # the jump is spread over ~2 cells (tanh): with a one-cell jump the reference's unlimited
-    # second-order reconstruction (adFVM/interp.py:20-28) gives a negative face pressure in
-    # the first stage and its solver stops with NaN
-    s = 0.5 * (1.0 - np.tanh((x - 0.5) / (smooth_cells / n)))
+    # the jump is spread over ~2 cells (tanh): with a one-cell jump (smooth_cells=None) the
+    # reference's unlimited second-order reconstruction (adFVM/interp.py:20-28) gives a
+    # negative face pressure in the first stage and its solver stops with NaN
+    if smooth_cells is None:
+        s = (x < 0.5).astype(np.float64)
+    else:
+        s = 0.5 * (1.0 - np.tanh((x - 0.5) / (smooth_cells / n)))
     case.U = np.zeros((mesh.nInternalCells, 3))
     case.T = 278.7 + (348.4 - 278.7) * s
     case.p = 1e4 + (1e5 - 1e4) * s

@@ -14,6 +14,7 @@
 //                back-slot weights, the neighbours'), ghost boundary conditions transposed,
 //                objective gradient (stage 1), primitive VJP and the SSP-RK reverse update.
 #include <cuda_runtime.h>
+#include <type_traits>
 #include "facedev.cuh"
 #include "vane.cuh"
 
@@ -130,7 +131,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const
                                                      const S* ainr, const S* ainu, const S* aine,
                                                      S* a1r, S* a1u, S* a1e, S* a0r, S* a0u, S* a0e, S* sb,
                                                      double dt, int objective, int objStart, int objN, double obja,
-                                                     VaneDev vane) {
+                                                     VaneDev vane, const double* __restrict__ objSeed) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m.nIC) return;
     const size_t n = m.nIC;
@@ -188,6 +189,8 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const
             gp[R_T] += (R)(-obja * dmu * (U0 - U0i) / dl * A);
             gp[0] += (R)(-obja * mu / dl * A);
         }
+        if (STAGE == 1 && objSeed)
+            for (int k = 0; k < 5; k++) gp[k] += (R)(obja * objSeed[(size_t)(m.nIC + g) * 5 + k]);
         int kind = m.gkind[g];
         int kU = kind & 7, kT = (kind >> 3) & 7, kp = (kind >> 6) & 7;
         if (kU == GK_TOTALPT) {
@@ -212,6 +215,9 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const
         if (kT != GK_FIXED) pbar[R_T] += gp[R_T];
         if (kp != GK_FIXED) pbar[R_P] += gp[R_P];
     }
+    // an objective evaluated by the caller: its gradient with respect to this cell's primitives
+    if (STAGE == 1 && objSeed)
+        for (int k = 0; k < 5; k++) pbar[k] += (R)(obja * objSeed[(size_t)c * 5 + k]);
     // objective on the stage-1 primitives
     if (STAGE == 1 && objective != AFVM_OBJ_NONE) {
         const R* rc = rec + (size_t)c * REC;
@@ -322,7 +328,7 @@ template <typename R, typename S>
 int adjoint_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double dt, const S* Srho, const S* SrhoU,
                      const S* SrhoE, const S* rhoNa, const S* rhoUNa, const S* rhoENa, double obja, S* rhoa,
                      S* rhoUa, S* rhoEa, S* Srhoa, S* SrhoUa, S* SrhoEa, cudaStream_t s, const S* stages,
-                     const R* tape) {
+                     const R* tape, const ParamDev* params) {
     const MeshDev<R>& m = meshOf<R>(c);
     const Phys& P = c->phys;
     default_sources<S>(c, Srho, SrhoU, SrhoE);
@@ -381,19 +387,23 @@ int adjoint_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double 
             ProfScope ps(c, KID_ADJ_GATHER, s);
             k_adj_cell1<R><<<nbC, BLOCK, 0, s>>>(m, fadj, cbar);
         }
+        // the stage's share of the mesh / boundary-input gradients (before the cell kernel: the
+        // adjoint outputs it writes may alias this stage's input adjoints)
+        if constexpr (std::is_same<R, double>::value && std::is_same<S, double>::value)
+            if (params) launch_param_grads<R, S>(c, *params, rec, coef, ain[0], ain[1], ain[2], st == 1, obja, s);
         ProfScope ps(c, KID_ADJ_GRAD, s);
         if (st == 2)
             k_adj_cell2<R, S, 2><<<nbC, BLOCK, 0, s>>>(m, P, rec, fadj, cbar, u[0], u[1], u[2], ain[0], ain[1], ain[2],
                                                     A2[0], A2[1], A2[2], rhoa, rhoUa, rhoEa, sb, dt, c->objective,
-                                                    c->objStart, c->objN, obja, c->vane);
+                                                    c->objStart, c->objN, obja, c->vane, c->objSeed);
         else if (st == 1)
             k_adj_cell2<R, S, 1><<<nbC, BLOCK, 0, s>>>(m, P, rec, fadj, cbar, u[0], u[1], u[2], ain[0], ain[1], ain[2],
                                                     A1[0], A1[1], A1[2], rhoa, rhoUa, rhoEa, sb, dt, c->objective,
-                                                    c->objStart, c->objN, obja, c->vane);
+                                                    c->objStart, c->objN, obja, c->vane, c->objSeed);
         else
             k_adj_cell2<R, S, 0><<<nbC, BLOCK, 0, s>>>(m, P, rec, fadj, cbar, u[0], u[1], u[2], ain[0], ain[1], ain[2],
                                                     nullptr, nullptr, nullptr, rhoa, rhoUa, rhoEa, sb, dt,
-                                                    c->objective, c->objStart, c->objN, obja, c->vane);
+                                                    c->objective, c->objStart, c->objN, obja, c->vane, c->objSeed);
     }
     if (Srhoa || SrhoUa || SrhoEa) {
         ProfScope ps(c, KID_ADJ_MISC, s);
@@ -407,7 +417,7 @@ int adjoint_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double 
 #define AFVM_ADJ_INST(R, S)                                                                                    \
     template int adjoint_step_dev<R, S>(Ctx*, const S*, const S*, const S*, double, const S*, const S*, const S*, \
                                         const S*, const S*, const S*, double, S*, S*, S*, S*, S*, S*,             \
-                                        cudaStream_t, const S*, const R*);
+                                        cudaStream_t, const S*, const R*, const ParamDev*);
 AFVM_ADJ_INST(double, double)
 AFVM_ADJ_INST(float, float)
 AFVM_ADJ_INST(float, double)

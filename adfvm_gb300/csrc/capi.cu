@@ -267,6 +267,7 @@ int build_tables(Ctx* c, const afvm_mesh_tensors* M, const afvm_patch_bc* bcs, H
         c->patchStart.push_back(p.startFace);
         c->patchN.push_back(p.nFaces);
         c->bcKinds.push_back(b.U); c->bcKinds.push_back(b.T); c->bcKinds.push_back(b.p);
+        c->patchDirNormals.push_back(totalpt && !b.U_value ? 1 : 0);
         if (c->objective == AFVM_OBJ_DRAG && pi == c->objPatch) { c->objStart = p.startFace; c->objN = p.nFaces; }
     }
     if (pos != nF) return fail(c, AFVM_ERR_BAD_ARG, "patches do not cover the boundary faces");
@@ -576,6 +577,20 @@ int64_t afvm_ctx_device_bytes(const afvm_ctx* ctx) {
     return c->bytes + c->adjBytes;
 }
 
+int afvm_set_objective_sink(afvm_ctx* ctx, void* prims) {
+    if (!ctx) return AFVM_ERR_BAD_ARG;
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    c->objSink = prims;
+    return AFVM_OK;
+}
+
+int afvm_set_objective_seed(afvm_ctx* ctx, const double* primBar) {
+    if (!ctx) return AFVM_ERR_BAD_ARG;
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    c->objSeed = primBar;
+    return AFVM_OK;
+}
+
 int afvm_set_objective_vane(afvm_ctx* ctx, const afvm_objective_vane* v) {
     if (!ctx) return AFVM_ERR_BAD_ARG;
     Ctx* c = reinterpret_cast<Ctx*>(ctx);
@@ -835,6 +850,83 @@ int afvm_adjoint_step_tape(afvm_ctx* ctx, const void* rho, const void* rhoU, con
                                       (const S*)rhoENa, obja, (S*)rhoa, (S*)rhoUa, (S*)rhoEa, (S*)S_rhoa,
                                       (S*)S_rhoUa, (S*)S_rhoEa, s, (const S*)stages, (const R*)tape);
     });
+}
+
+int afvm_adjoint_step_params(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, double dt,
+                             const void* S_rho, const void* S_rhoU, const void* S_rhoE, const void* stages,
+                             const void* tape, const void* rhoNa, const void* rhoUNa, const void* rhoENa,
+                             double dtca, double obja, void* rhoa, void* rhoUa, void* rhoEa, void* S_rhoa,
+                             void* S_rhoUa, void* S_rhoEa, const afvm_param_grad* pg, void* stream) {
+    if (!ctx) return AFVM_ERR_BAD_ARG;
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!pg) return fail(c, AFVM_ERR_BAD_ARG, "null parameter-gradient description");
+    if (!rho || !rhoU || !rhoE || !rhoNa || !rhoUNa || !rhoENa || !rhoa || !rhoUa || !rhoEa)
+        return fail(c, AFVM_ERR_BAD_ARG, "null pointer");
+    if (c->precision != AFVM_FP64)
+        return fail(c, AFVM_ERR_UNSUPPORTED, "mesh and boundary-input gradients need an AFVM_FP64 context");
+    if (dtca != 0.0) return fail(c, AFVM_ERR_UNSUPPORTED, "dtca != 0 (the CFL-sum output has no adjoint here)");
+    if (tape && !stages) return fail(c, AFVM_ERR_BAD_ARG, "a face tape is read together with the stage states");
+    if (!std::isfinite(dt) || !std::isfinite(obja)) return fail(c, AFVM_ERR_BAD_ARG, "non-finite dt or obja");
+    bool mesh = pg->areas || pg->volumesL || pg->volumesR || pg->weights || pg->deltas || pg->normals ||
+                pg->deltasUnit || pg->linearWeights || pg->quadraticWeights || pg->volumes;
+    if (mesh && c->objective == AFVM_OBJ_VANE && c->vane.b != 0.0)
+        return fail(c, AFVM_ERR_UNSUPPORTED, "mesh gradient of the vane objective's heat-transfer term");
+    ParamDev pd{};
+    pd.areas = pg->areas; pd.volL = pg->volumesL; pd.volR = pg->volumesR; pd.wts = pg->weights;
+    pd.dlt = pg->deltas; pd.nrm = pg->normals; pd.du = pg->deltasUnit; pd.lw = pg->linearWeights;
+    pd.qw = pg->quadraticWeights; pd.vol = pg->volumes;
+    int bcDims = 0;
+    if (pg->bcPatch >= 0) {
+        if (pg->bcPatch >= c->nPatches || pg->bcField < 0 || pg->bcField > 2 || !pg->bc)
+            return fail(c, AFVM_ERR_BAD_ARG, "boundary input: patch, field or output");
+        int kind = c->bcKinds[3 * pg->bcPatch + pg->bcField];
+        if (kind != AFVM_BC_FIXED_VALUE && kind != AFVM_BC_CBC_UPT && kind != AFVM_BC_CBC_TOTAL_PT)
+            return fail(c, AFVM_ERR_BAD_ARG, "boundary input: the field has no input on that patch");
+        if (kind == AFVM_BC_CBC_TOTAL_PT && pg->bcField == 0 && c->patchDirNormals[pg->bcPatch])
+            return fail(c, AFVM_ERR_BAD_ARG, "boundary input: that CBC_TOTAL_PT direction is the face normals");
+        pd.bcStart = c->patchStart[pg->bcPatch];
+        pd.bcN = c->patchN[pg->bcPatch];
+        pd.bcField = pg->bcField;
+        pd.bc = pg->bc;
+        bcDims = pg->bcField == 0 ? 3 : 1;
+    } else if (!mesh) {
+        return fail(c, AFVM_ERR_BAD_ARG, "no parameter gradient asked for");
+    }
+    DeviceGuard dg(c->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    int st = alloc_adjoint<double, double>(c);
+    if (st) return st;
+    // per ghost: the CBC_TOTAL_PT direction is the face normal (a mesh input then)
+    if (!c->gdirn && c->nG > 0) {
+        std::vector<uint8_t> h(c->nG, 0);
+        for (int pi = 0; pi < c->nPatches; pi++)
+            if (c->patchDirNormals[pi])
+                for (int i = 0; i < c->patchN[pi]; i++) h[c->patchStart[pi] - c->nIF + i] = 1;
+        void* p = nullptr;
+        st = ctx_alloc(c, &p, h.size());
+        if (st) return st;
+        cudaError_t e = cudaMemcpy(p, h.data(), h.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_fail(c, e, "ghost direction flags");
+        c->gdirn = (uint8_t*)p;
+    }
+    pd.gdirn = c->gdirn;
+    // the outputs are the step's gradients: cleared, then summed over the three stages
+    const size_t nF = c->nF, nIF = c->nIF, nIC = c->nIC;
+    const std::pair<double*, size_t> outs[] = {{pd.areas, nF}, {pd.volL, nF}, {pd.volR, nIF}, {pd.wts, nF},
+                                               {pd.dlt, nF}, {pd.nrm, 3 * nF}, {pd.du, 3 * nF}, {pd.lw, 2 * nF},
+                                               {pd.qw, 6 * nF}, {pd.vol, nIC},
+                                               {pd.bc, (size_t)pd.bcN * bcDims}};
+    for (const auto& o : outs) {
+        if (!o.first || !o.second) continue;
+        cudaError_t e = cudaMemsetAsync(o.first, 0, o.second * sizeof(double), s);
+        if (e != cudaSuccess) return cuda_fail(c, e, "parameter gradient clear");
+    }
+    return adjoint_step_dev<double, double>(c, (const double*)rho, (const double*)rhoU, (const double*)rhoE, dt,
+                                            (const double*)S_rho, (const double*)S_rhoU, (const double*)S_rhoE,
+                                            (const double*)rhoNa, (const double*)rhoUNa, (const double*)rhoENa, obja,
+                                            (double*)rhoa, (double*)rhoUa, (double*)rhoEa, (double*)S_rhoa,
+                                            (double*)S_rhoUa, (double*)S_rhoEa, s, (const double*)stages,
+                                            (const double*)tape, &pd);
 }
 
 int afvm_adjoint_step(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, double dt,

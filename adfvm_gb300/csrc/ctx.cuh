@@ -151,6 +151,8 @@ struct Ctx {
     // ghost BC values on the host for updates
     std::vector<int> ghostPatchOffset;   // first ghost index of each patch (sorted order)
     std::vector<int> bcKinds;            // per patch: U,T,p kinds
+    std::vector<char> patchDirNormals;   // per patch: a CBC_TOTAL_PT direction taken from the normals
+    uint8_t* gdirn = nullptr;            // per ghost, the same flag (device; on first use)
     // adjoint buffers (allocated on first use)
     void* fadj = nullptr;     // nF x 40 face adjoint records
     void* cbar = nullptr;     // nIC x 20 cell primitive/gradient adjoints
@@ -163,6 +165,11 @@ struct Ctx {
     // sensitivity reduction scratch (grown on demand)
     void* sensScratch = nullptr;
     size_t sensBytes = 0;
+    // an objective evaluated outside the library (afvm_set_objective_sink / _seed): the device
+    // buffer that receives each primal step's objective-stage primitives (nC x 5, record type),
+    // and the gradient of the objective with respect to them (nC x 5 double) the adjoint adds
+    void* objSink = nullptr;
+    const double* objSeed = nullptr;
     // turbine-vane objective inputs (afvm_set_objective_vane)
     bool vaneSet = false;
     VaneDev vane{};
@@ -209,12 +216,34 @@ int primal_run_dev(Ctx* c, S* rho, S* rhoU, S* rhoE, int nSteps, double dt0, dou
                    double* objHist, cudaStream_t s);
 int sensitivity_dev(Ctx* c, int nArrays, const double* const* grad, const double* const* pert,
                     const int64_t* n, double* out, cudaStream_t s);
+// the parameter gradients of an adjoint step (adjoint_params.cu): the mesh tensors in the
+// reference's layouts (any may be NULL) and one boundary input, all double, device
+struct ParamDev {
+    double* areas;       // nF
+    double* volL;        // nF
+    double* volR;        // nIF
+    double* wts;         // nF
+    double* dlt;         // nF
+    double* nrm;         // nF x 3
+    double* du;          // nF x 3
+    double* lw;          // nF x 2
+    double* qw;          // nF x 2 x 3
+    double* vol;         // nIC
+    int bcStart, bcN, bcField;   // faces of the boundary input's patch (bcN 0: none), U/T/p
+    double* bc;          // bcN x (3 for U, else 1)
+    const uint8_t* gdirn;
+};
 template <typename R, typename S = R>
 int adjoint_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double dt,
                      const S* Srho, const S* SrhoU, const S* SrhoE,
                      const S* rhoNa, const S* rhoUNa, const S* rhoENa, double obja,
                      S* rhoa, S* rhoUa, S* rhoEa, S* Srhoa, S* SrhoUa, S* SrhoEa, cudaStream_t s,
-                     const S* stages = nullptr, const R* tape = nullptr);
+                     const S* stages = nullptr, const R* tape = nullptr, const ParamDev* params = nullptr);
+// per stage of the reverse sweep, after the face records and cell sums of the stage (fadj,
+// cbar) and before the stage's cell kernel: adds the stage's share of the parameter gradients
+template <typename R, typename S>
+void launch_param_grads(Ctx* c, const ParamDev& pd, const R* rec, R coef, const S* ar, const S* au, const S* ae,
+                        bool objectiveStage, double obja, cudaStream_t s);
 
 // a step's tape, written by the primal step and read by its adjoint step: in FP64 first the
 // face tapes, one per RK stage, TAPE values a face each (value k of face f of stage st at

@@ -7,6 +7,7 @@
 // expression is differentiated by hand, in reverse order. At the kinks of |x| the derivative
 // taken is sign(x) with sign(0) = 0; at max(a, b) with a == b the whole derivative goes to a.
 #pragma once
+#include <type_traits>
 #include "physics.cuh"
 
 namespace afvm {
@@ -28,6 +29,24 @@ template <typename R>
 AFVM_HD void zero_bar(FaceBar<R>& b) {
     R* p = &b.UP[0];
     for (int k = 0; k < 40; k++) p[k] = R(0);
+}
+
+// Adjoint of a face's geometry inputs (FaceIn's N, D, lw0, lw1, qw0, qw1, 1/deltas), for the
+// gradient with respect to the mesh tensors (the reference's parameters = 'mesh',
+// apps/adjoint.py:108-110). The VJP functions take an optional GeoBar; with none (GeoNone, the
+// default) the geometry terms are not compiled at all.
+template <typename R>
+struct GeoBar {
+    R N[3], D[3], lw0, lw1, qw0[3], qw1[3], rdelta;
+};
+struct GeoNone {};
+template <typename G>
+constexpr bool kGeo = !std::is_same<G, GeoNone>::value;
+
+template <typename R>
+AFVM_HD void zero_geo(GeoBar<R>& g) {
+    R* p = &g.N[0];
+    for (int k = 0; k < 15; k++) p[k] = R(0);
 }
 
 template <typename R>
@@ -125,9 +144,9 @@ AFVM_HD void recon_vjp(R b, R lw, const R* qw, R& phiCb, R& phiDb, R* gb) {
 }
 
 // riemann.eulerRoe; the forward's reciprocals and reciprocal square roots come from the tape
-template <typename R, typename Src>
+template <typename R, typename Src, typename G = GeoNone>
 AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR, const R* N, const R* Fb,
-                     const Src& t, R& pLb, R& pRb, R* ULb, R* URb, R& rhoLb, R& rhoRb) {
+                     const Src& t, R& pLb, R& pRb, R* ULb, R* URb, R& rhoLb, R& rhoRb, G* geo = nullptr) {
     const R g = consts<R>(P).gamma, gm1 = consts<R>(P).gm1, ggm1 = consts<R>(P).ggm1, h = R(0.5);
     // ---- forward values: those dear to recompute from the tape, the cheap ones again (as roe());
     // a lean tape (Src::kFull false) holds only the reciprocals, and the Roe intermediates are
@@ -202,6 +221,8 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL
     R drhoEb = -h * Fb[4] * L1;
     R abv6b = -h * (Fb[0] + dot3(Fu, UF) + Fb[4] * hF);
     R abv7b = h * (dot3(Fu, N) + Fb[4] * UnF);
+    if constexpr (kGeo<G>)
+        for (int k = 0; k < 3; k++) geo->N[k] += h * Fu[k] * abv7;     // - (-abv7 N)/2 in F[1..3]
     R hFb = -h * Fb[4] * abv6;
     R UnFb = h * Fb[4] * abv7;
     // abv7 = abv3*abv5 - abv2*abv4/aF
@@ -218,6 +239,8 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL
     UnFb += abv5b * drho;
     drhob += abv5b * UnF;
     for (int k = 0; k < 3; k++) dUb[k] += -abv5b * N[k];
+    if constexpr (kGeo<G>)
+        for (int k = 0; k < 3; k++) geo->N[k] += -abv5b * dU[k];
     // abv4 = gm1*(qF*drho - UF.dU + drhoE)
     R tb = gm1 * abv4b;
     R qFb = tb * drho;
@@ -257,6 +280,8 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL
     for (int k = 0; k < 3; k++) { URb[k] += dUb[k] * rhoR; ULb[k] += -dUb[k] * rhoL; }
     // UnF = UF.N ; aF = sqrt(a2F) ; a2F = gm1 (hF - qF) ; qF = |UF|^2/2
     for (int k = 0; k < 3; k++) UFb[k] += UnFb * N[k];
+    if constexpr (kGeo<G>)
+        for (int k = 0; k < 3; k++) geo->N[k] += UnFb * UF[k];
     a2Fb += aFb * h * raF;
     hFb += gm1 * a2Fb;
     qFb += -gm1 * a2Fb;
@@ -282,6 +307,8 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL
     R pn = h * dot3(Fu, N);
     pLb += pn;
     pRb += pn;
+    if constexpr (kGeo<G>)
+        for (int k = 0; k < 3; k++) geo->N[k] += h * Fu[k] * (pL + pR);
     // hL = g pL/(gm1 rhoL) + qL/2
     pLb += hLb * ggm1 * rrL;
     rhoLb += -hLb * ggm1 * pL * rrL * rrL;
@@ -293,13 +320,16 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL
     rhoRb += rhoUnRb * UnR;
     R UnLb = rhoUnLb * rhoL + eab, UnRb = rhoUnRb * rhoR - eab;
     for (int k = 0; k < 3; k++) { ULb[k] += UnLb * N[k]; URb[k] += UnRb * N[k]; }
+    if constexpr (kGeo<G>)
+        for (int k = 0; k < 3; k++) geo->N[k] += UnLb * UL[k] + UnRb * UR[k];
 }
 
 // riemann.eulerLaxFriedrichs
-template <typename R, typename Src>
+template <typename R, typename Src, typename G = GeoNone>
 AFVM_HD void laxf_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR, const R* rhoUL,
                       const R* rhoUR, R rhoEL, R rhoER, const R* N, const R* Fb, const Src& t, R& pLb, R& pRb,
-                      R* ULb, R* URb, R& rhoLb, R& rhoRb, R* rhoULb, R* rhoURb, R& rhoELb, R& rhoERb) {
+                      R* ULb, R* URb, R& rhoLb, R& rhoRb, R* rhoULb, R* rhoURb, R& rhoELb, R& rhoERb,
+                      G* geo = nullptr) {
     const R g = consts<R>(P).gamma, h = R(0.5);
     R UnL = dot3(UL, N), UnR = dot3(UR, N);
     R rrL = t.get(T_RRL), rrR = t.get(T_RRR);
@@ -334,6 +364,8 @@ AFVM_HD void laxf_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rho
     pRb += Bb * g * h * rcR * rrR;
     rhoRb += -Bb * h * cR * rrR;
     for (int k = 0; k < 3; k++) { ULb[k] += UnLb * N[k]; URb[k] += UnRb * N[k]; }
+    if constexpr (kGeo<G>)
+        for (int k = 0; k < 3; k++) geo->N[k] += UnLb * UL[k] + UnRb * UR[k] + h * Fu[k] * (pL + pR);
 }
 
 // RCF.viscousFlux: F[1..3] += -sigma, F[4] += -(q + sigma.UF)
@@ -414,9 +446,59 @@ AFVM_HD void viscous_vjp(const Phys& P, R TL, R TR, const R* UL, const R* UR, R 
                      gTFb, gUFb);
 }
 
-template <typename R, typename Src>
+// The geometry part of the viscous flux's VJP (deltasUnit D, normals N, 1/deltas): the forward
+// is evaluated again from the face inputs, and only the geometry adjoints are accumulated (the
+// state adjoints come from viscous_vjp / viscous_vjp_t)
+template <typename R, typename G>
+AFVM_HD void viscous_geo_vjp(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, const R* UF, const R* gTF,
+                             const R* gUF, const R* D, const R* N, R rdel, const R* Fb, G* geo) {
+    R mu = viscosity<R>(P, TF);
+    R kappa = mu * consts<R>(P).kFac;
+    R snT = (TR - TL) * rdel;
+    R gTD = dot3(gTF, D);
+    R gT[3];
+    for (int k = 0; k < 3; k++) gT[k] = gTF[k] + snT * D[k] - gTD * D[k];
+    R snU[3], gUD[3], gU[9];
+    for (int i = 0; i < 3; i++) {
+        snU[i] = (UR[i] - UL[i]) * rdel;
+        gUD[i] = gUF[3 * i] * D[0] + gUF[3 * i + 1] * D[1] + gUF[3 * i + 2] * D[2];
+        for (int k = 0; k < 3; k++) gU[3 * i + k] = gUF[3 * i + k] + snU[i] * D[k] - gUD[i] * D[k];
+    }
+    R tmp3 = gU[0] + gU[4] + gU[8];
+    // reverse: F[1+i] -= sigma_i, F[4] -= qF + sigma.UF
+    R sb[3], tmp2b[3], tmp3b = R(0);
+    R qFb = -Fb[4];
+    for (int i = 0; i < 3; i++) {
+        sb[i] = -Fb[1 + i] - Fb[4] * UF[i];
+        tmp2b[i] = sb[i] * mu;
+        tmp3b += -R(2.0 / 3) * mu * sb[i] * N[i];
+    }
+    // sigma_i = mu (tmp2_i - 2/3 tmp3 N_i) ; tmp2_i = sum_k (gU[i][k] + gU[k][i]) N_k ; qF = kappa gT.N
+    for (int i = 0; i < 3; i++) geo->N[i] += sb[i] * (-R(2.0 / 3) * mu * tmp3);
+    for (int k = 0; k < 3; k++) {
+        R a = R(0);
+        for (int i = 0; i < 3; i++) a += tmp2b[i] * (gU[3 * i + k] + gU[3 * k + i]);
+        geo->N[k] += a + qFb * kappa * gT[k];
+    }
+    R gTb[3], gUb[9];
+    for (int k = 0; k < 3; k++) gTb[k] = qFb * kappa * N[k];
+    for (int i = 0; i < 3; i++)
+        for (int k = 0; k < 3; k++) gUb[3 * i + k] = tmp2b[i] * N[k] + tmp2b[k] * N[i];
+    gUb[0] += tmp3b; gUb[4] += tmp3b; gUb[8] += tmp3b;
+    // gT_k = gTF_k + snT D_k - (gTF.D) D_k, snT = (TR - TL)/deltas; the same per row of gU
+    R snTb = dot3(gTb, D);
+    for (int j = 0; j < 3; j++) geo->D[j] += gTb[j] * (snT - gTD) - gTF[j] * snTb;
+    geo->rdelta += snTb * (TR - TL);
+    for (int i = 0; i < 3; i++) {
+        R snUb = gUb[3 * i] * D[0] + gUb[3 * i + 1] * D[1] + gUb[3 * i + 2] * D[2];
+        for (int j = 0; j < 3; j++) geo->D[j] += gUb[3 * i + j] * (snU[i] - gUD[i]) - gUF[3 * i + j] * snUb;
+        geo->rdelta += snUb * (UR[i] - UL[i]);
+    }
+}
+
+template <typename R, typename Src, typename G = GeoNone>
 AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>& in, const Src& t, const R* Fb,
-                        FaceBar<R>& o);
+                        FaceBar<R>& o, G* geo = nullptr);
 
 // the corrected face gradient of U that viscous() forms (face-averaged cell gradients, or the
 // ghost's on a characteristic face, with the normal component replaced by snGrad)
@@ -431,9 +513,11 @@ AFVM_HD void corrected_gradU(const FaceIn<R>& in, bool chr, R* gU) {
     }
 }
 
-// <Fbar, F> differentiated with respect to all 40 inputs of the face (accumulated into out)
-template <typename R>
-AFVM_HD void face_vjp(const Phys& P, int kind, bool inviscid, const FaceIn<R>& in, const R* Fb, FaceBar<R>& o) {
+// <Fbar, F> differentiated with respect to all 40 inputs of the face (accumulated into out) and,
+// given a GeoBar, with respect to the face geometry as well (accumulated into *geo)
+template <typename R, typename G = GeoNone>
+AFVM_HD void face_vjp(const Phys& P, int kind, bool inviscid, const FaceIn<R>& in, const R* Fb, FaceBar<R>& o,
+                      G* geo = nullptr) {
     if (kind == FACE_BOUNDARY) {
         R rho, rhoU[3], rhoE;
         conservative<R>(P, in.UN, in.TN, in.pN, rho, rhoU, rhoE);
@@ -443,6 +527,8 @@ AFVM_HD void face_vjp(const Phys& P, int kind, bool inviscid, const FaceIn<R>& i
         R Unb = Fb[0] * rho + dot3(Fu, rhoU) + Fb[4] * (rhoE + in.pN);
         o.pN += dot3(Fu, in.N) + Fb[4] * Un;
         for (int k = 0; k < 3; k++) o.UN[k] += Unb * in.N[k];
+        if constexpr (kGeo<G>)
+            for (int k = 0; k < 3; k++) geo->N[k] += Unb * in.UN[k] + Fu[k] * in.pN;
         conservative_vjp<R>(P, in.UN, in.TN, in.pN, rhob, rhoUb, rhoEb, o.UN, o.TN, o.pN);
         if (!inviscid) {
             R TFb = R(0), UFb[3] = {R(0), R(0), R(0)};
@@ -450,20 +536,24 @@ AFVM_HD void face_vjp(const Phys& P, int kind, bool inviscid, const FaceIn<R>& i
                            o.TP, o.TN, o.UP, o.UN, TFb, UFb, o.gTN, o.gUN);
             o.TN += TFb;
             for (int k = 0; k < 3; k++) o.UN[k] += UFb[k];
+            if constexpr (kGeo<G>)
+                viscous_geo_vjp<R>(P, in.TP, in.TN, in.UP, in.UN, in.TN, in.UN, in.gTN, in.gUN, in.D, in.N,
+                                   in.rdelta, Fb, geo);
         }
         return;
     }
     TapeLocal<R, sizeof(R) == 8> t;
     R F[5], maxaF;   // dead after inlining: only the tape values are used
     face_flux<R>(P, kind, inviscid, in, F, maxaF, t);
-    face_vjp_t<R>(P, kind, inviscid, in, t, Fb, o);
+    face_vjp_t<R>(P, kind, inviscid, in, t, Fb, o, geo);
 }
 
 // the VJP of a non-boundary face from the tape of its forward evaluation: of the face inputs
-// only the geometry (N, D, lw, qw, 1/deltas) is read from in
-template <typename R, typename Src>
+// only the geometry (N, D, lw, qw, 1/deltas) is read from in - unless geometry adjoints are
+// asked for (geo), which read every face input
+template <typename R, typename Src, typename G>
 AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>& in, const Src& t, const R* Fb,
-                        FaceBar<R>& o) {
+                        FaceBar<R>& o, G* geo) {
     const bool chr = kind == FACE_CHARACTERISTIC;
     // forward values
     R ULF[3], TLF = t.get(T_TLF), pLF = t.get(T_PLF), URF[3], TRF = t.get(T_TRF), pRF = t.get(T_PRF);
@@ -502,6 +592,12 @@ AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>&
         }
         viscous_vjp_t<R>(P, TF, UF, mu, t.get(T_GTN), tmp2, tmp3, sigma, in.D, in.N, in.rdelta, Fb, o.TP, o.TN, o.UP,
                          o.UN, TFb, UFb, gTFb, gUFb);
+        if constexpr (kGeo<G>) {
+            R gTF[3], gUF[9];
+            for (int k = 0; k < 3; k++) gTF[k] = chr ? in.gTN[k] : R(0.5) * (in.gTP[k] + in.gTN[k]);
+            for (int k = 0; k < 9; k++) gUF[k] = chr ? in.gUN[k] : R(0.5) * (in.gUP[k] + in.gUN[k]);
+            viscous_geo_vjp<R>(P, in.TP, in.TN, in.UP, in.UN, TF, UF, gTF, gUF, in.D, in.N, in.rdelta, Fb, geo);
+        }
         if (chr) {
             o.TN += TFb;
             for (int k = 0; k < 3; k++) { o.UN[k] += UFb[k]; o.gTN[k] += gTFb[k]; }
@@ -523,7 +619,7 @@ AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>&
     R rhoELb = R(0), rhoERb = R(0);
     int solver = chr ? P.briemann : P.riemann;
     if (solver == AFVM_RIEMANN_ROE) {
-        roe_vjp<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, in.N, Fb, t, pLFb, pRFb, ULFb, URFb, rhoLb, rhoRb);
+        roe_vjp<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, in.N, Fb, t, pLFb, pRFb, ULFb, URFb, rhoLb, rhoRb, geo);
     } else {
         // conservative()'s rhoU and rhoE of each side
         R eL = consts<R>(P).Cv * TLF, eR = consts<R>(P).Cv * TRF;
@@ -531,11 +627,28 @@ AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>&
         R rhoUL[3], rhoUR[3];
         for (int k = 0; k < 3; k++) { rhoUL[k] = ULF[k] * rhoL; rhoUR[k] = URF[k] * rhoR; }
         laxf_vjp<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, rhoUL, rhoUR, rhoEL, rhoER, in.N, Fb, t, pLFb, pRFb, ULFb,
-                    URFb, rhoLb, rhoRb, rhoULb, rhoURb, rhoELb, rhoERb);
+                    URFb, rhoLb, rhoRb, rhoULb, rhoURb, rhoELb, rhoERb, geo);
     }
     conservative_vjp_t<R>(P, ULF, TLF, pLF, rdL, rhoLb, rhoULb, rhoELb, ULFb, TLFb, pLFb);
     conservative_vjp_t<R>(P, URF, TRF, pRF, rdR, rhoRb, rhoURb, rhoERb, URFb, TRFb, pRFb);
     // reconstruction
+    if constexpr (kGeo<G>) {
+        // phiF = phiC + (phiD - phiC) lw + qw.grad phiC, per side
+        for (int k = 0; k < 3; k++) {
+            geo->lw0 += ULFb[k] * (in.UN[k] - in.UP[k]);
+            for (int j = 0; j < 3; j++) geo->qw0[j] += ULFb[k] * in.gUP[3 * k + j];
+        }
+        geo->lw0 += TLFb * (in.TN - in.TP) + pLFb * (in.pN - in.pP);
+        for (int j = 0; j < 3; j++) geo->qw0[j] += TLFb * in.gTP[j] + pLFb * in.gpP[j];
+        if (!chr) {
+            for (int k = 0; k < 3; k++) {
+                geo->lw1 += URFb[k] * (in.UP[k] - in.UN[k]);
+                for (int j = 0; j < 3; j++) geo->qw1[j] += URFb[k] * in.gUN[3 * k + j];
+            }
+            geo->lw1 += TRFb * (in.TP - in.TN) + pRFb * (in.pP - in.pN);
+            for (int j = 0; j < 3; j++) geo->qw1[j] += TRFb * in.gTN[j] + pRFb * in.gpN[j];
+        }
+    }
     for (int k = 0; k < 3; k++) recon_vjp<R>(ULFb[k], in.lw0, in.qw0, o.UP[k], o.UN[k], o.gUP + 3 * k);
     recon_vjp<R>(TLFb, in.lw0, in.qw0, o.TP, o.TN, o.gTP);
     recon_vjp<R>(pLFb, in.lw0, in.qw0, o.pP, o.pN, o.gpP);

@@ -18,6 +18,9 @@
 
 namespace afvm {
 
+// max(a, b) that keeps a NaN operand (fmax drops it)
+__device__ __forceinline__ double nan_max(double a, double b) { return (b > a || b != b) ? b : a; }
+
 // RCF.primitive (adFVM/density.py:162-171) in double. One out-of-line body, so that a ghost
 // cell and its source cell get bit-identical values.
 __device__ __noinline__ void primitive_d(const Phys& P, double rho, double r0, double r1, double r2, double rhoE,
@@ -286,15 +289,17 @@ __global__ void __launch_bounds__(BLOCK) k_update(MeshDev<R> m, const R* __restr
     }
     if (STAGE == 1) {
         // reduce_max of the CFL sums (density.py:405-410): warp shuffle, block, then an atomic
-        // max on the bit pattern (non-negative doubles order like their bits)
+        // max on the bit pattern (non-negative doubles order like their bits). A NaN wins every
+        // comparison, as in the reference's max (a NaN's bits are above every finite double's),
+        // so a state gone non-finite gives a non-finite CFL sum and the step reports it
         double d = (double)dtc;
-        for (int off = 16; off > 0; off >>= 1) d = fmax(d, __shfl_down_sync(0xffffffffu, d, off));
+        for (int off = 16; off > 0; off >>= 1) d = nan_max(d, __shfl_down_sync(0xffffffffu, d, off));
         __shared__ double wmax[BLOCK / 32];
         if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = d;
         __syncthreads();
         if (threadIdx.x < 32) {
             d = (threadIdx.x < BLOCK / 32) ? wmax[threadIdx.x] : 0.0;
-            for (int off = 16; off > 0; off >>= 1) d = fmax(d, __shfl_down_sync(0xffffffffu, d, off));
+            for (int off = 16; off > 0; off >>= 1) d = nan_max(d, __shfl_down_sync(0xffffffffu, d, off));
             if (threadIdx.x == 0) atomicMax(dtcBits, (unsigned long long)__double_as_longlong(d));
         }
     }
@@ -518,6 +523,12 @@ int primal_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double d
             // the primitives of stages 1 and 2 were written by the previous stage's update
             ProfScope ps(c, KID_GRAD, s);
             k_grad<R><<<nblocks(m.nIC), BLOCK, 0, s>>>(m, recs[st]);
+        }
+        if (st == 1 && c->objSink) {
+            // the objective stage's primitives U (3), T, p of every cell, ghosts included, for an
+            // objective evaluated by the caller
+            cudaMemcpy2DAsync(c->objSink, 5 * sizeof(R), recs[1], REC * sizeof(R), 5 * sizeof(R), (size_t)m.nC,
+                              cudaMemcpyDeviceToDevice, s);
         }
         if (st == 1 && c->objective == AFVM_OBJ_VANE) {
             // the partial sums now, while rec holds the stage-1 primitives; combined at the end

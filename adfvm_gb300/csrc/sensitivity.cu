@@ -115,14 +115,15 @@ int sensitivity_dev(Ctx* c, int nArrays, const double* const* grad, const double
 // ---------------------------------------------------------------------------------------
 // Allocation-free variant (afvm_sensitivity_noalloc).
 //
-// Some callers cannot allocate device memory: code that runs while a CUDA graph is being
-// captured (cudaMalloc is not capturable), hosts with a fixed device-memory budget that has
-// been handed out up front, or plug-ins that may not touch the allocator of the process that
-// loads them. For them the reduction's scratch (block partials, per-array block counts and
-// the result) is this file-scope device array, sized for at most
-// AFVM_SENSITIVITY_NOALLOC_MAX_ARRAYS arrays. Every GPU that loads the library keeps it
-// (~129 KB) until the process exits. All calls share it: two calls that overlap on the GPU
-// (different streams, or different host threads without ordering) race on it.
+// Some callers may not allocate device memory: an application that gives this library a
+// fixed share of the GPU up front and makes every allocation itself, or a plug-in loaded
+// into a host program whose memory pool it must not touch. Such a caller can create no
+// context and cannot let afvm_sensitivity grow its scratch. For them the reduction's
+// scratch (block partials, per-array block counts and the result) is this file-scope device
+// array, sized for at most AFVM_SENSITIVITY_NOALLOC_MAX_ARRAYS arrays. Every GPU that loads
+// the library keeps it (~129 KB) until the process exits. All calls share it: two calls
+// that overlap on the GPU (different streams, or different host threads without ordering)
+// race on it.
 // ---------------------------------------------------------------------------------------
 
 constexpr int NOALLOC_MAX_ARRAYS = AFVM_SENSITIVITY_NOALLOC_MAX_ARRAYS;
@@ -133,7 +134,9 @@ constexpr size_t NOALLOC_DOUBLES = NOALLOC_PARTIALS + 1 + (NOALLOC_MAX_ARRAYS + 
 static __device__ __align__(256) double g_sens_noalloc_scratch[NOALLOC_DOUBLES];
 
 // Host code must not use the symbol itself as a device address: the device address of the
-// array is looked up once per device, with that device current, and cached here.
+// array is looked up by the first call on each device, with that device current, and cached
+// here (so that first call belongs before any stream capture). cudaDeviceReset unloads the
+// module: the cached address is then stale, and calls after a reset are not supported.
 static std::mutex g_noalloc_mutex;
 static double* g_noalloc_ptr[256] = {nullptr};
 

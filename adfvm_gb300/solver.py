@@ -16,6 +16,14 @@ exposes:
   (density.py:113-158): U, T, p are read with their boundary dicts; rho, rhoU, rhoE, U, T, p
   are written with the ghost-cell values of the boundary map as the patch values;
 * ``run_device(...)`` - n steps resident on the GPU (``afvm_primal_run``).
+
+``objective`` is one of the built-in kinds ('none', 'kinetic_energy', 'sum_T', 'drag:<patch>',
+'vane') or, like a reference case file's ``objective(fields, solver)`` (adFVM/density.py:354-357),
+a function ``objective([U, T, p], solver)`` returning a scalar torch tensor. It is called on
+float64 CUDA tensors of the primitives of the step's second RK stage - every cell, ghosts
+included - and ``solver`` gives ``mesh`` (the Mesh), ``meshTensor(name)`` (a mesh array as a
+CUDA tensor), ``mu(T)``, ``gamma``, ``Cp``, ``Cv``, ``Pr``. Its adjoint seed is torch autograd
+of the same function (afvm_set_objective_sink / afvm_set_objective_seed).
 The GPU library is mandatory: there is no CPU path.
 """
 import collections
@@ -46,6 +54,27 @@ def _torch():
     return torch
 
 
+class ObjectiveSolver(object):
+    """What an objective written as a torch function sees as its ``solver`` argument: the gas
+    constants, ``mu(T)`` (adFVM/density.py:27 for Sutherland), the Mesh, and its arrays as CUDA
+    tensors (``meshTensor``); ``tensors`` replaces some of them (autograd leaves for the mesh
+    gradient)."""
+
+    def __init__(self, rcf, tensors=None):
+        self._rcf = rcf
+        self._tensors = tensors or {}
+        self.mesh = rcf.mesh
+        self.gamma, self.Cp, self.Cv, self.Pr = rcf.gamma, rcf.Cp, rcf.Cv, rcf.Pr
+
+    def meshTensor(self, name):
+        return self._tensors[name] if name in self._tensors else self._rcf.meshTensor(name)
+
+    def mu(self, T):
+        if self._rcf.mu is None:
+            return SUTHERLAND[0] * T ** 1.5 / (T + SUTHERLAND[1])
+        return T * 0 + float(self._rcf.mu)
+
+
 class RCF(object):
     """GB300 drop-in for the reference RCF solver's residual/step evaluation."""
 
@@ -69,6 +98,7 @@ class RCF(object):
         # the turbine-vane objective: 'vane' (adFVM/objectives/vane.py's own plane and weights)
         # or a description from adfvm_gb300.vane.options(...)
         self.vane = None
+        self.objectiveFn = objective if callable(objective) else None
         if isinstance(objective, dict) or objective == 'vane':
             from . import vane as _vane
             self.vane = dict(objective) if isinstance(objective, dict) else _vane.options(self.mesh)
@@ -93,7 +123,9 @@ class RCF(object):
         else:
             model, mu0 = L.AFVM_MU_CONSTANT, float(mu)
         obj, objPatch = L.AFVM_OBJ_NONE, -1
-        if self.vane is not None:
+        if self.objectiveFn is not None:
+            pass                          # evaluated on the host side of the sink (objective_value)
+        elif self.vane is not None:
             obj = L.AFVM_OBJ_VANE
         elif self.objective == 'kinetic_energy':
             obj = L.AFVM_OBJ_KINETIC_ENERGY
@@ -142,6 +174,11 @@ class RCF(object):
         self._bcvals = self.getBoundaryTensor(1)
         if self.vane is not None:
             self._set_vane(self.vane)
+        if self.objectiveFn is not None:
+            torch = _torch()
+            rd = torch.float64 if self.record_dtype == np.float64 else torch.float32
+            self._objPrims = torch.empty((self.mesh.nCells, 5), dtype=rd, device='cuda:%d' % self.device)
+            L.check(L.lib().afvm_set_objective_sink(self._ctx, C.c_void_p(self._objPrims.data_ptr())), self._ctx)
 
     def _set_vane(self, v):
         m = self.mesh
@@ -295,7 +332,7 @@ class RCF(object):
                                            vp(Ss[0]), vp(Ss[1]), vp(Ss[2]), vp(outs[0]), vp(outs[1]), vp(outs[2]),
                                            C.byref(dtc), C.byref(obj), None)
         L.check(st, self._ctx, 'afvm_primal_step_host')
-        return outs + [np.array([[dtc.value]]), np.array([[obj.value]])]
+        return outs + [np.array([[dtc.value]]), np.array([[self._objective_after(obj.value)]])]
 
     # ---- the stages of recent map calls, for Adjoint.map on the same states -------------
     # The reference's adjoint loop re-runs the primal over a checkpoint interval through map
@@ -403,7 +440,7 @@ class RCF(object):
                                            vp(Ss[0]), vp(Ss[1]), vp(Ss[2]), vp(out[0]), vp(out[1]), vp(out[2]),
                                            C.byref(dtc), C.byref(obj), None)
         L.check(st, self._ctx, 'afvm_primal_step_host')
-        return out[0], out[1], out[2], dtc.value, obj.value
+        return out[0], out[1], out[2], dtc.value, self._objective_after(obj.value)
 
     # ------------------------------------------------------------------ per-kernel timing
     def profile(self, on=True):
@@ -467,7 +504,7 @@ class RCF(object):
                                            C.byref(dtc) if want_scalars else None,
                                            C.byref(obj) if want_scalars else None, C.c_void_p(stream))
         L.check(st, self._ctx, 'afvm_primal_step_tape')
-        return out[0], out[1], out[2], dtc.value, obj.value
+        return out[0], out[1], out[2], dtc.value, self._objective_after(obj.value) if want_scalars else obj.value
 
     def _check_stages(self, stages):
         torch = _torch()
@@ -477,14 +514,118 @@ class RCF(object):
             raise ValueError('stages: a contiguous device buffer of 10 x nInternalCells %s values' % td)
         return stages
 
+    # the mesh tensors the reference differentiates for parameters = 'mesh' (Mesh.gradFields,
+    # adFVM/mesh.py:28-31), in the order of its map's outputs
+    MESH_GRAD_FIELDS = ('areas', 'volumesL', 'volumesR', 'weights', 'deltas', 'normals', 'deltasUnit',
+                        'linearWeights', 'quadraticWeights', 'volumes')
+
+    def param_shapes(self, parameters):
+        """Shapes of the gradients that adjoint_step(params=parameters) returns: for 'mesh' those
+        of the ten Mesh.gradFields tensors; for ('BCs', field, patch, key) that of the one
+        boundary input (apps/adjoint.py:104-121)."""
+        m = self.mesh
+        if parameters == 'mesh':
+            return [tuple(np.shape(getattr(m, k))) for k in self.MESH_GRAD_FIELDS]
+        field = self._bc_param(parameters)[1]
+        return [(int(m.boundary[parameters[2]]['nFaces']), 3 if field == 0 else 1)]
+
+    def _bc_param(self, parameters):
+        """('BCs', field, patch, key) -> (sorted patch index, ghost field 0/1/2, active). The
+        input sets the ghost values of the patch: fixedValue 'value' its own field; CBC_UPT U0,
+        T0, p0 and CBC_TOTAL_PT direction, Tt, pt (read from the p field's BC, as the reference's
+        characteristic boundary does, density.py:333-337) U, T, p. The copies held by the U and
+        T fields of a characteristic patch are inputs the step never reads (active False)."""
+        if not (isinstance(parameters, tuple) and len(parameters) == 4 and parameters[0] == 'BCs'):
+            raise ValueError('parameters: source, mesh or (BCs, field, patch, key)')
+        _, phi, patch, key = parameters
+        if phi not in ('U', 'T', 'p') or patch not in self.mesh.sortedPatches:
+            raise ValueError('parameters: unknown field or patch %r' % (parameters,))
+        kind = self.bc[phi][patch]['type']
+        keys = {'fixedValue': {'value': 'UTp'.index(phi)}, 'CBC_UPT': {'U0': 0, 'T0': 1, 'p0': 2},
+                'CBC_TOTAL_PT': {'direction': 0, 'Tt': 1, 'pt': 2}}.get(kind, {})
+        if key not in keys:
+            raise ValueError('parameters: %s on patch %s (%s) has no input %r' % (phi, patch, kind, key))
+        if kind == 'CBC_TOTAL_PT' and key == 'direction' and 'direction' not in self.bc['p'][patch]:
+            raise ValueError('parameters: that CBC_TOTAL_PT direction is the face normals (a mesh input)')
+        active = kind == 'fixedValue' or phi == 'p'
+        return self.mesh.sortedPatches.index(patch), keys[key], active
+
+    # ------------------------------------------------------------------ objectives as torch functions
+    def meshTensor(self, name):
+        """A mesh array as a CUDA tensor: float64, or int64 for the connectivity (cached)."""
+        torch = _torch()
+        cache = self.__dict__.setdefault('_meshT', {})
+        if name not in cache:
+            a = np.ascontiguousarray(getattr(self.mesh, name))
+            dt = torch.int64 if a.dtype.kind in 'iu' else torch.float64
+            cache[name] = torch.as_tensor(a, device='cuda:%d' % self.device).to(dt)
+        return cache[name]
+
+    def _call_objective(self, prims, view=None):
+        P = prims.double()
+        return self.objectiveFn([P[:, 0:3], P[:, 3:4], P[:, 4:5]], view or ObjectiveSolver(self))
+
+    def _objective_after(self, kernel_obj):
+        """The step's objective: the built-in one from the kernels, or the caller's function on
+        the primitives the step copied into the sink."""
+        if self.objectiveFn is None:
+            return kernel_obj
+        torch = _torch()
+        with torch.no_grad():
+            return float(self._call_objective(self._objPrims))
+
+    def _objective_prims(self, rho, rhoU, rhoE, dt, S, tape):
+        """The objective-stage primitives (nCells x 5) of the step from this state: from its
+        tape's second-stage cell records, or by running the step again into the sink."""
+        torch = _torch()
+        m = self.mesh
+        if tape is not None:
+            off = int(L.lib().afvm_tape_elements(self._ctx)) - 3 * 20 * m.nCells + 20 * m.nCells
+            return tape[off:off + 20 * m.nCells].view(m.nCells, 20)[:, :5]
+        tmp = (torch.empty_like(rho), torch.empty_like(rhoU), torch.empty_like(rhoE))
+        self.step(rho, rhoU, rhoE, dt, S=S, out=tmp, want_scalars=False)
+        return self._objPrims.clone()
+
     def adjoint_step(self, rho, rhoU, rhoE, dt, seeds, obja=1.0, S=None, out=None, source_grad=True, stages=None,
-                     tape=None):
+                     tape=None, params=None):
+        """VJP of one step on CUDA tensors (see _adjoint_step); with an objective given as a
+        torch function, its gradient with respect to the objective-stage primitives - torch
+        autograd of the function - is the adjoint seed the kernels add (afvm_set_objective_seed),
+        and for params='mesh' the function's own dependence on the mesh tensors (through
+        solver.meshTensor) is added to the mesh gradients."""
+        if self.objectiveFn is None or obja == 0.0:
+            return self._adjoint_step(rho, rhoU, rhoE, dt, seeds, obja, S, out, source_grad, stages, tape, params)
+        torch = _torch()
+        prims = self._objective_prims(rho, rhoU, rhoE, dt, S, tape).double().detach().requires_grad_(True)
+        leaves = {}
+        if params == 'mesh':
+            leaves = {k: self.meshTensor(k).detach().clone().requires_grad_(True) for k in self.MESH_GRAD_FIELDS}
+        with torch.enable_grad():
+            J = self._call_objective(prims, ObjectiveSolver(self, leaves))
+            ins = [prims] + list(leaves.values())
+            g = torch.autograd.grad(J, ins, allow_unused=True)
+        g = [torch.zeros_like(v) if gi is None else gi for gi, v in zip(g, ins)]
+        seed = g[0].contiguous()
+        L.check(L.lib().afvm_set_objective_seed(self._ctx, C.c_void_p(seed.data_ptr())), self._ctx)
+        try:
+            r = self._adjoint_step(rho, rhoU, rhoE, dt, seeds, obja, S, out, source_grad, stages, tape, params)
+        finally:
+            L.lib().afvm_set_objective_seed(self._ctx, None)
+        if params == 'mesh':
+            for dst, gm in zip(r[4], g[1:]):
+                dst += float(obja) * gm.reshape(dst.shape)
+        return r
+
+    def _adjoint_step(self, rho, rhoU, rhoE, dt, seeds, obja=1.0, S=None, out=None, source_grad=True, stages=None,
+                      tape=None, params=None):
         """VJP of one step on CUDA tensors (afvm_adjoint_step): the adjoint of the input state
         (and of the sources) given the adjoint seeds of the output state and of the objective.
         dt is held fixed, the CFL-sum output gets no seed (dtca = 0, apps/adjoint.py:268).
         stages: the stage_buffer() a step(..., stages=) of this state filled; skips the
         forward recompute. tape: the tape_buffer() the same step filled; skips the face
-        flux's re-evaluation inside the VJP."""
+        flux's re-evaluation inside the VJP. params: 'mesh' or ('BCs', field, patch, key) -
+        also the gradients with respect to those parameters (afvm_adjoint_step_params, FP64
+        contexts), returned as a fifth item: a list of float64 CUDA tensors of param_shapes()."""
         torch = _torch()
         stream = torch.cuda.current_stream(rho.device).cuda_stream
         if out is None:
@@ -495,12 +636,36 @@ class RCF(object):
         gp = [None, None, None] if Sg is None else [vp(t) for t in Sg]
         sp = None if stages is None else vp(self._check_stages(stages))
         tp = None if tape is None else vp(self._check_tape(tape, stages))
-        st = L.lib().afvm_adjoint_step_tape(self._ctx, vp(rho), vp(rhoU), vp(rhoE), float(dt), Sp[0], Sp[1],
-                                            Sp[2], sp, tp, vp(seeds[0]), vp(seeds[1]), vp(seeds[2]), 0.0, float(obja),
-                                            vp(out[0]), vp(out[1]), vp(out[2]), gp[0], gp[1], gp[2],
-                                            C.c_void_p(stream))
-        L.check(st, self._ctx, 'afvm_adjoint_step_tape')
-        return out[0], out[1], out[2], Sg
+        if params is None:
+            st = L.lib().afvm_adjoint_step_tape(self._ctx, vp(rho), vp(rhoU), vp(rhoE), float(dt), Sp[0], Sp[1],
+                                                Sp[2], sp, tp, vp(seeds[0]), vp(seeds[1]), vp(seeds[2]), 0.0,
+                                                float(obja), vp(out[0]), vp(out[1]), vp(out[2]), gp[0], gp[1], gp[2],
+                                                C.c_void_p(stream))
+            L.check(st, self._ctx, 'afvm_adjoint_step_tape')
+            return out[0], out[1], out[2], Sg
+        grads = [torch.empty(sh, dtype=torch.float64, device=rho.device) for sh in self.param_shapes(params)]
+        dp = lambda t: C.cast(C.c_void_p(t.data_ptr()), L._d)
+        pg = L.ParamGrad()
+        pg.bcPatch = -1
+        active = True
+        if params == 'mesh':
+            for k, t in zip(self.MESH_GRAD_FIELDS, grads):
+                if t.numel():
+                    setattr(pg, k, dp(t))
+        else:
+            pi, field, active = self._bc_param(params)
+            pg.bcPatch, pg.bcField, pg.bc = pi, field, dp(grads[0])
+        if not active:
+            # an input the step never reads: its gradient is zero
+            r = self._adjoint_step(rho, rhoU, rhoE, dt, seeds, obja, S, out, source_grad, stages, tape)
+            grads[0].zero_()
+            return r + (grads,)
+        st = L.lib().afvm_adjoint_step_params(self._ctx, vp(rho), vp(rhoU), vp(rhoE), float(dt), Sp[0], Sp[1], Sp[2],
+                                              sp, tp, vp(seeds[0]), vp(seeds[1]), vp(seeds[2]), 0.0, float(obja),
+                                              vp(out[0]), vp(out[1]), vp(out[2]), gp[0], gp[1], gp[2], C.byref(pg),
+                                              C.c_void_p(stream))
+        L.check(st, self._ctx, 'afvm_adjoint_step_params')
+        return out[0], out[1], out[2], Sg, grads
 
     def adjoint_viscosity(self, rho, rhoU, rhoE, adj, dt, kind='turkel', scaling=1e-3, want_fields=False):
         """Artificial-viscosity stabilisation of the adjoint fields ``adj`` (three CUDA tensors,
@@ -560,6 +725,8 @@ class RCF(object):
         (dt <- min(2*CFL/dtc, stepFactor*dt) unless fixedTimeStep). Returns device histories
         (dt, dtc, obj) or None."""
         torch = _torch()
+        if self.objectiveFn is not None:
+            raise NotImplementedError('run_device with an objective given as a function: use run() or step()')
         stream = torch.cuda.current_stream(rho.device).cuda_stream
         hist = torch.zeros((3, max(1, nSteps)), dtype=torch.float64, device=rho.device) if record else None
         hp = [None, None, None] if hist is None else [C.cast(C.c_void_p(hist[k].data_ptr()), L._d) for k in range(3)]

@@ -228,6 +228,19 @@ typedef struct afvm_objective_vane {
 } afvm_objective_vane;
 int afvm_set_objective_vane(afvm_ctx* ctx, const afvm_objective_vane* v);
 
+/* An objective evaluated by the caller instead of one of the AFVM_OBJ_* kinds: the reference
+ * evaluates its case file's objective(fields, solver) on the primitives of the step's second RK
+ * stage, ghost cells included (adFVM/density.py:354-357, 412-413). afvm_set_objective_sink: a
+ * DEVICE buffer of nCells x 5 values of the record type (double for AFVM_FP64, float otherwise)
+ * into which every later primal step copies those primitives, U (3), T, p per cell, internal
+ * cells then ghosts (NULL: no copy). afvm_set_objective_seed: the gradient of the caller's
+ * objective with respect to the same nCells x 5 values (DEVICE, double), which every later
+ * adjoint step adds, times obja, to the adjoint of its objective stage - where the built-in
+ * objectives add theirs - and which afvm_adjoint_step_params passes on to the boundary inputs
+ * (NULL: none). Both pointers are only recorded: they must stay valid while steps use them. */
+int afvm_set_objective_sink(afvm_ctx* ctx, void* prims);
+int afvm_set_objective_seed(afvm_ctx* ctx, const double* primBar);
+
 /* Ghost-cell values of the primitive fields for a conservative state: the boundary map the
  * reference runs before writing fields (RCF.initFields -> mapBoundary, adFVM/density.py:140-143;
  * ghost rows per BCs.py:62-184). rho, rhoU, rhoE: DEVICE state as for afvm_primal_step. out:
@@ -327,6 +340,39 @@ int afvm_adjoint_step_tape(afvm_ctx* ctx, const void* rho, const void* rhoU, con
                            void* rhoa, void* rhoUa, void* rhoEa, void* S_rhoa, void* S_rhoUa,
                            void* S_rhoEa, void* stream);
 
+/* The adjoint step's gradients with respect to parameters other than the state and the
+ * sources - the reference's Adjoint(parameters=...) (apps/adjoint.py:101-126): 'mesh' gives the
+ * gradients of the ten Mesh.gradFields tensors (adFVM/mesh.py:28-31) in the reference's own
+ * layouts, ('BCs', field, patch, key) the gradient of one boundary input
+ * (apps/adjoint.py:111-118). Every pointer is a DEVICE double array that receives the step's
+ * gradient (overwritten, summed over the three RK stages); any mesh pointer may be NULL. */
+typedef struct afvm_param_grad {
+    double* areas;            /* nFaces */
+    double* volumesL;         /* nFaces */
+    double* volumesR;         /* nInternalFaces */
+    double* weights;          /* nFaces */
+    double* deltas;           /* nFaces */
+    double* normals;          /* nFaces x 3 */
+    double* deltasUnit;       /* nFaces x 3 */
+    double* linearWeights;    /* nFaces x 2 */
+    double* quadraticWeights; /* nFaces x 2 x 3 */
+    double* volumes;          /* nInternalCells */
+    int32_t bcPatch;          /* boundary input: patch index (sortedPatches order), -1 for none */
+    int32_t bcField;          /* the ghost field the input sets: 0 U (fixedValue value, CBC_UPT U0,
+                                 CBC_TOTAL_PT direction), 1 T (value, T0, Tt), 2 p (value, p0, pt) */
+    double* bc;               /* the patch's nFaces x (3 for field 0, else 1) */
+} afvm_param_grad;
+
+/* afvm_adjoint_step_tape that also returns the parameter gradients described by *pg. AFVM_FP64
+ * contexts (AFVM_ERR_UNSUPPORTED otherwise, and for the vane objective's heat-transfer term);
+ * AFVM_ERR_BAD_ARG for a patch / field without an input (zeroGradient, cyclic, symmetryPlane,
+ * or a CBC_TOTAL_PT direction that is the face normals - a mesh input). */
+int afvm_adjoint_step_params(afvm_ctx* ctx, const void* rho, const void* rhoU, const void* rhoE, double dt,
+                             const void* S_rho, const void* S_rhoU, const void* S_rhoE, const void* stages,
+                             const void* tape, const void* rhoNa, const void* rhoUNa, const void* rhoENa,
+                             double dtca, double obja, void* rhoa, void* rhoUa, void* rhoEa, void* S_rhoa,
+                             void* S_rhoUa, void* S_rhoEa, const afvm_param_grad* pg, void* stream);
+
 /* FP64 sum over k of dot(grad[k], pert[k]) (adFVM/cpp/cmesh.cpp:309-340). DEVICE arrays of
  * n[k] doubles; result to *out (host) after the stream work completes. */
 /* Adjoint stabilisation by artificial viscosity (adFVM/postpro.py:491-718, the viscous
@@ -358,17 +404,21 @@ int afvm_sensitivity(afvm_ctx* ctx, int32_t nArrays, const double* const* grad,
 int afvm_adjoint_energy(afvm_ctx* ctx, const void* rhoa, const void* rhoUa, const void* rhoEa,
                         const void* rho, const void* rhoU, const void* rhoE, double* out, void* stream);
 
-/* Allocation-free form of afvm_sensitivity, for callers that cannot allocate device memory
- * (code running under CUDA graph capture, where cudaMalloc is not allowed; hosts whose device
- * memory budget is fixed in advance; plug-ins that must not use the host process's
- * allocator). No counterpart in the reference. It needs no context: the grad/pert arrays
- * live on CUDA device `device`; the scratch is a static device array of the library that
- * holds partial sums for at most AFVM_SENSITIVITY_NOALLOC_MAX_ARRAYS arrays (about 129 KB,
- * kept on every GPU that loads the library until the process exits). nArrays above that
- * limit is rejected with AFVM_ERR_BAD_ARG. The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress), so make that first call before any stream capture.
- * Calls share the array: calls that overlap on the GPU race and must be ordered by the
- * caller. Blocks until the result is in *out (host); calls no allocator. */
+/* Allocation-free form of afvm_sensitivity. No counterpart in the reference. It is for
+ * callers that may not allocate device memory: an application that hands this library a
+ * fixed share of the GPU up front and owns every allocation itself, or a plug-in loaded
+ * into a host program whose memory pool it must not touch. Such a caller cannot create a
+ * context (afvm_ctx_create allocates) and cannot let afvm_sensitivity grow its scratch.
+ * It needs no context: the grad/pert arrays live on CUDA device `device`; the scratch is a
+ * static device array of the library that holds partial sums for at most
+ * AFVM_SENSITIVITY_NOALLOC_MAX_ARRAYS arrays (about 129 KB, kept on every GPU that loads
+ * the library until the process exits). nArrays outside 1..that limit, or a device outside
+ * the visible ones, is rejected with AFVM_ERR_BAD_ARG. The first call on a device looks up
+ * the array's device address (cudaGetSymbolAddress) with that device current and caches
+ * it, so make that first call before any stream capture; the cached address does not
+ * survive cudaDeviceReset. Calls share the array: calls that overlap on the GPU race and
+ * must be ordered by the caller. Blocks until the result is in *out (host); calls no
+ * allocator. */
 #define AFVM_SENSITIVITY_NOALLOC_MAX_ARRAYS 16
 int afvm_sensitivity_noalloc(int32_t device, int32_t nArrays, const double* const* grad,
                              const double* const* pert, const int64_t* n, double* out, void* stream);

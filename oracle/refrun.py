@@ -17,7 +17,7 @@ import types
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE = os.environ.get('AFVM_REFERENCE', '/root/reference')
+from .build import REFERENCE  # noqa: E402  (the one place the checkout's location is set)
 
 _loaded = {}
 

@@ -60,6 +60,7 @@ class Problem(object):
         self.boundaryRiemann = cfg['boundaryRiemannSolver']
         self.objective = objective
         m = mesh
+        self.mesh = mesh
         self.nIC = int(m.nInternalCells)
         self.nIF = int(m.nInternalFaces)
         self.nF = int(m.nFaces)
@@ -390,10 +391,24 @@ class Problem(object):
         return R, dtc
 
     # ------------------------------------------------------------ objective
+    _MESH_ATTR = {'linearWeights': 'lw', 'quadraticWeights': 'qw'}
+
+    def meshTensor(self, name):
+        """A mesh array as a torch tensor for objectives written as functions: the residual's
+        own tensors (so that parameter leaves reach the objective too), else the mesh's."""
+        a = getattr(self, self._MESH_ATTR.get(name, name), None)
+        if isinstance(a, torch.Tensor):
+            return a
+        v = np.asarray(getattr(self.mesh, name))
+        return torch.as_tensor(np.ascontiguousarray(v), dtype=torch.int64 if v.dtype.kind in 'iu' else T64)
+
     def objective_value(self, U, T, p):
-        """Objective on the (ghost-completed) primitives of RK stage 1."""
+        """Objective on the (ghost-completed) primitives of RK stage 1: a built-in kind, or a
+        function objective([U, T, p], solver) as a case file gives it (density.py:354-357)."""
         o = self.objective
         nIC = self.nIC
+        if callable(o):
+            return o([U, T, p], self)
         if isinstance(o, dict):
             return self._vane(o, U, T, p)
         if o == 'none':
@@ -531,6 +546,74 @@ def vjp_step(problem, rho, rhoU, rhoE, dt, S, seeds, obja=1.0):
     g = torch.autograd.grad(J, x + [S], allow_unused=True)
     g = [torch.zeros_like(v) if gi is None else gi for gi, v in zip(g, x + [S])]
     return g[0], g[1], g[2], g[3]
+
+
+MESH_GRAD_FIELDS = ('areas', 'volumesL', 'volumesR', 'weights', 'deltas', 'normals', 'deltasUnit',
+                    'linearWeights', 'quadraticWeights', 'volumes')
+_ATTR = {'linearWeights': 'lw', 'quadraticWeights': 'qw'}
+
+
+def with_parameter_leaves(problem, parameters, values=None):
+    """A copy of ``problem`` whose parameters are autograd leaves read directly by the residual:
+    'mesh' - the ten Mesh.gradFields tensors (adFVM/mesh.py:28-31; volumesL and volumesR are
+    inputs of their own, as in the reference's map, apps/adjoint.py:108-110); ('BCs', field,
+    patch, key) - one boundary input (apps/adjoint.py:111-118: fixedValue 'value', CBC_UPT
+    U0/T0/p0 and CBC_TOTAL_PT direction/Tt/pt of the p field, density.py:333-337). values:
+    the parameters' values (default: the problem's own). Returns (copy, leaves)."""
+    import copy
+    P = copy.copy(problem)
+    P.patches = [dict(e) for e in problem.patches]
+    if parameters == 'mesh':
+        leaves = []
+        for i, k in enumerate(MESH_GRAD_FIELDS):
+            base = getattr(problem, _ATTR.get(k, k)) if values is None else \
+                torch.as_tensor(values[i], dtype=T64).reshape(getattr(problem, _ATTR.get(k, k)).shape)
+            t = base.detach().clone().requires_grad_(True)
+            setattr(P, _ATTR.get(k, k), t)
+            leaves.append(t)
+        P.wp = P.areas / P.volumesL
+        P.wnAbs = P.areas[:P.nIF] / P.volumesR
+        for e in P.patches:
+            if 'Tt' in e and 'direction' not in e['bc']['p']:
+                e['direction'] = P.normals[e['start']:e['start'] + e['n']]
+        return P, leaves
+    _, phi, patch, key = parameters
+    e = next(e for e in P.patches if e['name'] == patch)
+    kind = e['kinds'][phi]
+    if kind == 'fixedValue' and key == 'value':
+        attr = phi + '_fixed'
+    elif kind in ('CBC_UPT', 'CBC_TOTAL_PT') and phi == 'p':
+        attr = key
+    elif kind in ('CBC_UPT', 'CBC_TOTAL_PT'):
+        # the U and T fields' copies of a characteristic input are never read by the step
+        n = e['n']
+        return P, [torch.zeros((n, 3 if key in ('U0', 'direction') else 1), dtype=T64, requires_grad=True)]
+    else:
+        raise ValueError(parameters)
+    base = e[attr] if values is None else torch.as_tensor(values[0], dtype=T64).reshape(e[attr].shape)
+    t = base.detach().clone().requires_grad_(True)
+    e[attr] = t
+    return P, [t]
+
+
+def vjp_step_params(problem, rho, rhoU, rhoE, dt, S, seeds, obja=1.0, parameters='mesh'):
+    """vjp_step that also returns the gradients with respect to ``parameters`` (see
+    with_parameter_leaves): (rhoa, rhoUa, rhoEa, S_a, [parameter gradients])."""
+    P, leaves = with_parameter_leaves(problem, parameters)
+    x = [t.detach().clone().requires_grad_(True) for t in (rho, rhoU, rhoE)]
+    if S is None:
+        S = torch.zeros((len(rho), 5), dtype=T64)
+    elif isinstance(S, (list, tuple)):
+        S = torch.cat([torch.as_tensor(s, dtype=T64).reshape(len(rho), -1) for s in S], dim=1)
+    S = S.detach().clone().requires_grad_(True)
+    out = P.step(x[0], x[1], x[2], dt, S)
+    J = (out[0] * seeds[0]).sum() + (out[1] * seeds[1]).sum() + (out[2] * seeds[2]).sum()
+    if obja != 0:
+        J = J + obja * out[4]
+    ins = x + [S] + list(leaves)
+    g = torch.autograd.grad(J, ins, allow_unused=True)
+    g = [torch.zeros_like(v) if gi is None else gi for gi, v in zip(g, ins)]
+    return g[0], g[1], g[2], g[3], g[4:]
 
 
 def adjoint_energy(volumes, gamma, rhoa, rhoUa, rhoEa, rho, rhoU, rhoE):

@@ -285,8 +285,36 @@ def make_viscosity():
     print('viscosity ->', path, os.path.getsize(path), 'bytes')
 
 
+def make_sod_sharp():
+    """The Sod tube with the one-cell jump of the reference's own shock-tube case
+    (cases/shockTube/system/setFieldsDict: p 1e5 | 1e4, T 348.4 | 278.7 K): the reference's first
+    step map call returns a non-finite CFL sum and a state that is non-finite in the cells around
+    the jump, after which its Solver.run stops (Field.info -> MPI Abort, adFVM/field.py:36-53).
+    Records that call's outputs."""
+    refrun.load()
+    case = cases.sod(1000, smooth_cells=None)
+    with tempfile.TemporaryDirectory() as d:
+        cfg, hook = reference_config(case)
+        rcf, cons = refrun.make_rcf(case.meshData, d, case.bc, case.U, case.T, case.p, before_compile=hook, **cfg)
+        inputs = ([c.field for c in cons] + [np.array([[case.dt]])] + rcf.mesh.getTensor() + rcf.mesh.getScalar() +
+                  [x[1] for x in rcf.sourceTerms] + rcf.getBoundaryTensor(1) + [x[1] for x in rcf.extraArgs])
+        out = rcf.map(*inputs, return_reusable=True, replace_reusable=True)
+    res = {'mesh_digest': np.array(mesh_digest(case.meshData)), 'dt0': np.array(case.dt),
+           'dtc': np.array(float(out[3][0, 0])), 'obj': np.array(float(out[4][0, 0]))}
+    for k, name in enumerate(['rho', 'rhoU', 'rhoE']):
+        res[name + '_init'] = np.asarray(cons[k].field)
+        res[name + '_1'] = np.asarray(out[k])
+    path = os.path.join(HERE, 'sod1000_sharp.npz')
+    np.savez_compressed(path, **res)
+    bad = np.where(~np.isfinite(res['rho_1']).all(axis=1))[0]
+    print('sod1000_sharp: dtc %r, non-finite cells %s -> %s' % (float(res['dtc']), bad.tolist(), path))
+
+
 def main(names):
     for name in names:
+        if name == 'sod1000_sharp':
+            make_sod_sharp()
+            continue
         if name == 'geometry':
             make_geometry()
             continue
@@ -306,4 +334,4 @@ def main(names):
 
 
 if __name__ == '__main__':
-    main(sys.argv[1:] or (['geometry', 'energy', 'viscosity'] + list(CASES)))
+    main(sys.argv[1:] or (['geometry', 'energy', 'viscosity', 'sod1000_sharp'] + list(CASES)))

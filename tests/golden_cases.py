@@ -37,3 +37,21 @@ def rel_err(x, ref):
     assert x.shape == ref.shape, (x.shape, ref.shape)
     den = np.max(np.abs(ref))
     return float(np.max(np.abs(x - ref)) / (den if den > 0 else 1.0))
+
+
+def load_sharp_sod():
+    """The reference's first step on the one-cell-jump Sod tube (tests/golden/sod1000_sharp.npz):
+    it returns a non-finite CFL sum and a state non-finite around the jump."""
+    g = dict(np.load(os.path.join(HERE, 'sod1000_sharp.npz')))
+    return cases.sod(1000, smooth_cells=None), g
+
+
+def nonfinite_parity(x, ref):
+    """(same non-finite entries, max|x-ref|/max|ref| over the entries finite in both)."""
+    x = np.asarray(x, np.float64)
+    ref = np.asarray(ref, np.float64)
+    assert x.shape == ref.shape, (x.shape, ref.shape)
+    fx, fr = np.isfinite(x), np.isfinite(ref)
+    ok = fx & fr
+    den = np.max(np.abs(ref[ok])) if ok.any() else 1.0
+    return bool(np.array_equal(fx, fr)), float(np.max(np.abs(x[ok] - ref[ok])) / den) if ok.any() else 0.0

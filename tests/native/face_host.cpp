@@ -71,3 +71,22 @@ extern "C" void afvm_host_face_vjp_f32(int n, int kind, int inviscid, const doub
         for (int k = 0; k < 40; k++) out[40 * (size_t)i + k] = bo[k];
     }
 }
+
+// the VJP with the geometry adjoints too: out holds 55 values per face, the 40 input adjoints
+// then N (3), D (3), lw0, lw1, qw0 (3), qw1 (3) and the adjoint of 1/deltas
+static_assert(sizeof(GeoBar<double>) == 15 * sizeof(double), "GeoBar layout");
+extern "C" void afvm_host_face_vjp_geo(int n, int kind, int inviscid, const double* ph, const double* in,
+                                       const double* Fb, double* out) {
+    Phys P = make_phys(ph);
+    for (int i = 0; i < n; i++) {
+        FaceIn<double> fi;
+        memcpy(&fi, in + 55 * (size_t)i, sizeof(fi));
+        FaceBar<double> b;
+        zero_bar(b);
+        GeoBar<double> g;
+        zero_geo(g);
+        face_vjp<double>(P, kind, inviscid != 0, fi, Fb + 5 * (size_t)i, b, &g);
+        memcpy(out + 55 * (size_t)i, &b, sizeof(b));
+        memcpy(out + 55 * (size_t)i + 40, &g, sizeof(g));
+    }
+}

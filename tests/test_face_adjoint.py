@@ -34,6 +34,7 @@ def host():
     lib.afvm_host_face.argtypes = [C.c_int, C.c_int, C.c_int, d, d, d]
     lib.afvm_host_face_vjp.argtypes = [C.c_int, C.c_int, C.c_int, d, d, d, d]
     lib.afvm_host_face_vjp_f32.argtypes = [C.c_int, C.c_int, C.c_int, d, d, d, d]
+    lib.afvm_host_face_vjp_geo.argtypes = [C.c_int, C.c_int, C.c_int, d, d, d, d]
     return lib
 
 
@@ -193,4 +194,37 @@ def test_fp32_face_adjoint_matches_fp64(host, kind, cfg):
     scale = np.abs(o64).max(axis=0) + 1e-300
     err = np.abs(o32 - o64) / scale
     bad = [(NAMES_IN[k], float(err[:, k].max())) for k in range(40) if err[:, k].max() > 1e-3]
+    assert not bad, bad
+
+
+GEO_NAMES = ['N0', 'N1', 'N2', 'D0', 'D1', 'D2', 'lw0', 'lw1', 'qw0_0', 'qw0_1', 'qw0_2', 'qw1_0', 'qw1_1', 'qw1_2',
+             'deltas']
+
+
+@pytest.mark.parametrize('kind,cfg', CONFIGS)
+def test_face_adjoint_with_geometry_matches_autograd(host, kind, cfg):
+    """The VJP that also returns the adjoints of the face geometry (normals, deltasUnit,
+    linearWeights, quadraticWeights, deltas: the face's share of the reference's mesh
+    gradient, parameters = 'mesh', apps/adjoint.py:108-110) against autograd with respect to
+    those inputs; the 40 state adjoints are the ones of the plain VJP, bit for bit."""
+    n = 64
+    X = random_faces(n, 16)
+    Fb = np.random.default_rng(17).normal(size=(n, 5))
+    out = np.zeros((n, 55))
+    plain = np.zeros((n, 40))
+    inv = 1 if cfg['mu'] == 0.0 else 0
+    host.afvm_host_face_vjp_geo(n, KINDS[kind], inv, dp(phys(cfg)), dp(native_in(X)), dp(Fb), dp(out))
+    host.afvm_host_face_vjp(n, KINDS[kind], inv, dp(phys(cfg)), dp(native_in(X)), dp(Fb), dp(plain))
+    assert np.array_equal(out[:, :40], plain)
+    # the native input is 1/deltas: d/d(deltas) = -(1/deltas)^2 d/d(1/deltas)
+    geo = out[:, 40:].copy()
+    geo[:, 14] = -geo[:, 14] / X[:, 54] ** 2
+    Xt = torch.as_tensor(X).clone().requires_grad_(True)
+    F = torch_face(kind, Xt, cfg)
+    J = (F[:, :5] * torch.as_tensor(Fb)).sum()
+    (g,) = torch.autograd.grad(J, Xt)
+    ref = g.numpy()[:, 40:]
+    scale = np.abs(ref).max(axis=0) + 1e-300
+    err = np.abs(geo - ref) / scale
+    bad = [(GEO_NAMES[k], float(err[:, k].max())) for k in range(15) if err[:, k].max() > 1e-12]
     assert not bad, bad

@@ -17,7 +17,7 @@ import pytest
 from adfvm_gb300 import cases, foam
 from adfvm_gb300.mesh import Mesh
 
-REF = os.environ.get('AFVM_REFERENCE', '/root/reference')
+from oracle.build import REFERENCE as REF  # noqa: E402
 needs_ref = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, 'adFVM')), reason='reference checkout absent')
 
 

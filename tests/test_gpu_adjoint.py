@@ -42,13 +42,13 @@ def test_adjoint_step_matches_autograd(name):
     d = [t.cuda() for t in x]
     Sd = None if S is None else [torch.as_tensor(s).cuda() for s in S]
     a = rcf.adjoint_step(d[0], d[1], d[2], dt, [t.cuda() for t in seeds], obja=1.0, S=Sd)
-    # FP64 adjoint within 1e-11 of the autograd VJP (max|x-ref|/max|ref| per field)
+    # FP64 adjoint within 1e-12 of the autograd VJP (max|x-ref|/max|ref| per field)
     for i in range(3):
         e = G.rel_err(a[i].cpu().numpy(), ref[i].numpy())
-        assert e < 1e-11, (name, i, e)
+        assert e < 1e-12, '%s field %d: rel err %.3e' % (name, i, e)
     sg = torch.cat([t.reshape(len(t), -1) for t in a[3]], dim=1).cpu().numpy()
     e = G.rel_err(sg, ref[3].numpy())
-    assert e < 1e-11, (name, 'source', e)
+    assert e < 1e-12, '%s source gradient: rel err %.3e' % (name, e)
 
 
 @pytest.mark.parametrize('precision,tol', [('fp32', 1e-4), ('mixed', 1e-6)])
@@ -69,7 +69,7 @@ def test_reduced_precision_adjoint_against_fp64_autograd(name, precision, tol):
     for i in range(3):
         assert a[i].dtype == td
         e = G.rel_err(a[i].double().cpu().numpy(), ref[i].numpy())
-        assert e < tol, (name, i, e)
+        assert e < tol, '%s %s field %d: rel err %.3e' % (name, precision, i, e)
 
 
 def test_adjoint_deterministic_and_aliasing():
@@ -157,7 +157,7 @@ def test_autograd_solve_matches_oracle_and_fd():
     g = torch.autograd.grad(J, xd + Sd)
     for i in range(6):
         e = G.rel_err(g[i].cpu().numpy(), gref[i].numpy())
-        assert e < 1e-10, (i, e)
+        assert e < 1e-12, 'autograd chain input %d: rel err %.3e' % (i, e)
 
 
 @pytest.mark.parametrize('name,precision', [('box8', 'fp64'), ('cyl32x16', 'fp64'), ('duct100_totalpt', 'fp64'),
@@ -208,18 +208,20 @@ def test_vane_objective_adjoint_with_heat_term(nx, ny, b, ref):
     ref = torch_ref.vjp_step(prob, x[0], x[1], x[2], case.dt, None, seeds, obja=1.0)
     a = rcf.adjoint_step(d[0], d[1], d[2], case.dt, [t.cuda() for t in seeds], obja=1.0)
     for i in range(3):
-        assert G.rel_err(a[i].cpu().numpy(), ref[i].numpy()) < 1e-11, i
+        e = G.rel_err(a[i].cpu().numpy(), ref[i].numpy())
+        assert e < 1e-12, 'vane field %d: rel err %.3e' % (i, e)
     # the objective's own gradient (no state seeds) is the part that changes with b
     z = [torch.zeros_like(t) for t in seeds]
     ref0 = torch_ref.vjp_step(prob, x[0], x[1], x[2], case.dt, None, z, obja=1.0)
     a0 = rcf.adjoint_step(d[0], d[1], d[2], case.dt, [t.cuda() for t in z], obja=1.0)
     for i in range(3):
-        assert G.rel_err(a0[i].cpu().numpy(), ref0[i].numpy()) < 1e-11, i
+        e = G.rel_err(a0[i].cpu().numpy(), ref0[i].numpy())
+        assert e < 1e-12, 'vane objective gradient field %d: rel err %.3e' % (i, e)
 
 
 @pytest.mark.parametrize('name', ['sod1', 'box1', 'box2', 'vane2x1', 'cyl4x2'])
 def test_tiny_meshes_adjoint_matches_autograd(name):
-    """The adjoint step on the smallest meshes (one cell cyclic to itself, ...) within 1e-11 of
+    """The adjoint step on the smallest meshes (one cell cyclic to itself, ...) within 1e-12 of
     the oracle's autograd VJP."""
     from tests.test_oracle_c import TINY
     case = TINY[name]()
@@ -232,7 +234,20 @@ def test_tiny_meshes_adjoint_matches_autograd(name):
     a = rcf.adjoint_step(*[t.cuda() for t in x], case.dt, [t.cuda() for t in seeds], obja=1.0)
     for i in range(3):
         e = G.rel_err(a[i].cpu().numpy(), ref[i].numpy())
-        assert e < 1e-11, (name, i, e)
+        if name == 'box1' and i == 2:
+            # one cell cyclic to itself: its rhoE adjoint is the seed (~1e-6) plus the kinetic
+            # energy's derivative, which is exactly zero (0.5 |rhoU|^2 V / rho does not depend on
+            # rhoE) but is evaluated, through p and T, as two terms of size |U|^2 V / (2 Cv T)
+            # that cancel: their rounding is measured against that size (measured 7e-16)
+            rho, rhoE = float(x[0].reshape(-1)[0]), float(x[2].reshape(-1)[0])
+            U = (x[1] / x[0]).numpy().ravel()
+            Cv = 1004.5 / 1.4
+            T = (rhoE / rho - 0.5 * float(np.dot(U, U))) / Cv
+            term = 0.5 * float(np.dot(U, U)) * float(np.asarray(mesh.volumes).ravel()[0]) / (Cv * T)
+            err = float(np.abs(a[i].cpu().numpy() - ref[i].numpy()).max())
+            assert err <= 1e-14 * term, 'box1 rhoE: error %.3e against terms of %.3e' % (err, term)
+            continue
+        assert e < 1e-12, '%s field %d: rel err %.3e' % (name, i, e)
 
 
 @pytest.mark.parametrize('name,precision', [('box8', 'fp64'), ('cyl32x16', 'fp64'), ('sod200_sym_lf', 'fp64'),
@@ -241,7 +256,7 @@ def test_tiny_meshes_adjoint_matches_autograd(name):
 def test_taped_adjoint_matches(name, precision):
     """afvm_primal_step_tape / afvm_adjoint_step_tape: the adjoint that reads the forward's face
     tape agrees with the one that re-evaluates the forward (to the rounding of FMA contraction
-    in the two kernels) and, in FP64, with the autograd VJP within 1e-11; the primal step is the
+    in the two kernels) and, in FP64, with the autograd VJP within 1e-12; the primal step is the
     same with and without the tape."""
     case, mesh, x, S, dt = _setup(name)
     rcf = RCF(mesh, case.bc, objective=case.objective, precision=precision, **case.config)
@@ -267,6 +282,6 @@ def test_taped_adjoint_matches(name, precision):
         ref = torch_ref.vjp_step(prob, x[0], x[1], x[2], dt, St, seeds, obja=1.0)
         for i in range(3):
             e = G.rel_err(a2[i].cpu().numpy(), ref[i].numpy())
-            assert e < 1e-11, (name, i, e)
+            assert e < 1e-12, '%s taped field %d: rel err %.3e' % (name, i, e)
     with pytest.raises(ValueError):
         rcf.step(d[0], d[1], d[2], dt, S=Sd, tape=tp)

@@ -139,3 +139,28 @@ def test_tiny_meshes_against_oracle(name):
             assert e < tol, (name, precision, i, e)
         assert abs(out[3] - float(ref[3])) <= max(tol, 1e-12) * abs(float(ref[3])), (name, precision)
         rcf.close()
+
+
+def test_sharp_sod_nonfinite_like_reference():
+    """One-cell Sod jump (the reference's own shock-tube set-up): the reference's first step
+    returns a non-finite CFL sum and a state non-finite around the jump, and its solver stops
+    there (Field.info -> MPI Abort). Through the C ABI the same step returns
+    AFVM_ERR_NONFINITE, leaves non-finite values in exactly the same entries, and matches the
+    reference elsewhere within 1e-12."""
+    from adfvm_gb300 import _lib as L
+    case, g = G.load_sharp_sod()
+    rcf = _solver(case)
+    n = case.build_mesh().nInternalCells
+    d = [torch.as_tensor(g[k + '_init']).reshape(n, -1).cuda() for k in ('rho', 'rhoU', 'rhoE')]
+    out = [torch.empty_like(t) for t in d]
+    with pytest.raises(L.AfvmError) as ei:
+        rcf.step(d[0], d[1], d[2], float(g['dt0']), out=out)
+    assert ei.value.status == L.AFVM_ERR_NONFINITE
+    for i, nm in enumerate(['rho', 'rhoU', 'rhoE']):
+        same, e = G.nonfinite_parity(out[i].cpu().numpy(), g[nm + '_1'])
+        assert same, '%s: non-finite entries differ from the reference' % nm
+        assert e < 1e-12, '%s finite entries: rel err %.3e' % (nm, e)
+    # the same state through the reference-facing map: the error reaches the caller
+    inputs = rcf.mapInputs(*[g[k + '_init'] for k in ('rho', 'rhoU', 'rhoE')], float(g['dt0']))
+    with pytest.raises(L.AfvmError):
+        rcf.map(*inputs)

@@ -51,3 +51,20 @@ def test_oracle_trajectory_matches_reference(name):
         for i, nm in enumerate(['rho', 'rhoU', 'rhoE']):
             e = G.rel_err(states[s][i].numpy(), g['%s_%d' % (nm, s)])
             assert e < 1e-12, (nm, s, e)
+
+
+def test_oracle_sharp_sod_goes_nonfinite_like_reference():
+    """One-cell Sod jump: the reference's first step gives a non-finite CFL sum and a state that
+    is non-finite in the cells around the jump; the oracle's step gives the same non-finite
+    cells and the same values elsewhere."""
+    case, g = G.load_sharp_sod()
+    assert digest(case.meshData) == str(g['mesh_digest'])
+    mesh = case.build_mesh()
+    prob = torch_ref.Problem(mesh, case.bc, case.config, case.objective)
+    x = [torch.as_tensor(g[k + '_init']).reshape(mesh.nInternalCells, -1) for k in ('rho', 'rhoU', 'rhoE')]
+    out = prob.step(x[0], x[1], x[2], float(g['dt0']))
+    assert not np.isfinite(float(g['dtc'])) and not np.isfinite(float(out[3]))
+    for i, nm in enumerate(['rho', 'rhoU', 'rhoE']):
+        same, e = G.nonfinite_parity(out[i].numpy(), g[nm + '_1'])
+        assert same, nm
+        assert e < 1e-12, (nm, e)

@@ -1,9 +1,10 @@
 """The allocation-free sensitivity entry point (afvm_sensitivity_noalloc).
 
-It exists for callers that cannot allocate device memory (code under CUDA graph capture,
-fixed device budgets, plug-ins that must not use the host process's allocator); its scratch
-is a static device array of the library. This file is collected last on purpose: if it fails,
-a run that stops at the first failure has already run every other test.
+It exists for callers that may not allocate device memory: an application that gives this
+library a fixed share of the GPU up front and makes every allocation itself, or a plug-in
+loaded into a host program whose memory pool it must not touch. Its scratch is a static
+device array of the library. This file is collected last on purpose: if it fails, a run that
+stops at the first failure has already run every other test.
 """
 import ctypes as C
 
@@ -28,14 +29,16 @@ def _arrays(k, seed):
     return g, p
 
 
-def _noalloc(g, p):
-    k = len(g)
-    ga = (L._d * k)(*[C.cast(C.c_void_p(t.data_ptr()), L._d) for t in g])
-    pa = (L._d * k)(*[C.cast(C.c_void_p(t.data_ptr()), L._d) for t in p])
-    na = (C.c_int64 * k)(*[t.numel() for t in g])
+def _noalloc(g, p, k=None, device=None):
+    k = len(g) if k is None else k
+    m = max(1, len(g))
+    ga = (L._d * m)(*[C.cast(C.c_void_p(t.data_ptr()), L._d) for t in g])
+    pa = (L._d * m)(*[C.cast(C.c_void_p(t.data_ptr()), L._d) for t in p])
+    na = (C.c_int64 * m)(*[t.numel() for t in g])
     out = C.c_double(float('nan'))
     stream = torch.cuda.current_stream().cuda_stream
-    st = L.lib().afvm_sensitivity_noalloc(torch.cuda.current_device(), k, ga, pa, na, C.byref(out),
+    dev = torch.cuda.current_device() if device is None else device
+    st = L.lib().afvm_sensitivity_noalloc(dev, k, ga, pa, na, C.byref(out),
                                           C.c_void_p(stream))
     return st, out.value
 
@@ -70,3 +73,16 @@ def test_noalloc_rejects_more_arrays_than_its_scratch_holds():
     g, p = _arrays(MAX_ARRAYS + 1, 5)
     st, v = _noalloc(g, p)
     assert st == L.AFVM_ERR_BAD_ARG
+
+
+def test_noalloc_rejects_no_arrays_and_unknown_devices():
+    g, p = _arrays(2, 6)
+    assert _noalloc(g, p, k=0)[0] == L.AFVM_ERR_BAD_ARG
+    assert _noalloc(g, p, k=-1)[0] == L.AFVM_ERR_BAD_ARG
+    assert _noalloc(g, p, device=-1)[0] == L.AFVM_ERR_BAD_ARG
+    assert _noalloc(g, p, device=torch.cuda.device_count())[0] == L.AFVM_ERR_BAD_ARG
+    # a rejected call leaves the next one unaffected
+    st, v = _noalloc(g, p)
+    assert st == L.AFVM_OK
+    ref = sum(float((a * b).sum()) for a, b in zip(g, p))
+    assert abs(v - ref) <= 1e-12 * sum(float((a * b).abs().sum()) for a, b in zip(g, p))
