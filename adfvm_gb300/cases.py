@@ -38,10 +38,11 @@ class Case:
     dt: float = 1e-7
     source: tuple = None                         # (S_rho, S_rhoU, S_rhoE) or None
     mesh: Mesh = None
+    builder: object = None                       # meshData -> mesh; None: Mesh.create (this library)
 
     def build_mesh(self):
         if self.mesh is None:
-            self.mesh = Mesh.create(self.meshData)
+            self.mesh = (self.builder or Mesh.create)(self.meshData)
         return self.mesh
 
 
@@ -93,13 +94,13 @@ def taylor_green(cc, L=1.0, T0=300.0, mach=0.3, noise=0.01, seed=2):
 
 
 def box(n=128, objective='kinetic_energy', riemann='eulerRoe', viscous=True, seed=0, cfl=0.5,
-        reorder=True):
+        reorder=True, builder=None):
     md = meshgen.periodic_box(n, seed_jitter=seed, reorder=reorder)
     bc = _uniform_bc(md[4], lambda patch, b, f: {'type': 'cyclic'})
     cfg = {'riemannSolver': riemann, 'fixedTimeStep': True}
     if not viscous:
         cfg['mu'] = 0.0
-    case = Case('box%d' % n, md, bc, None, None, None, config=cfg, objective=objective)
+    case = Case('box%d' % n, md, bc, None, None, None, config=cfg, objective=objective, builder=builder)
     mesh = case.build_mesh()
     cc = mesh.cellCentres[:mesh.nInternalCells]
     rho0, T0 = 1.2, 300.0

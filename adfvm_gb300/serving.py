@@ -252,6 +252,8 @@ class SensitivityServer(object):
         self.slots = []
         self.bytes_of = {}
         self.used = 0
+        self.evictions = 0          # idle slots released to make room for another mesh's slot
+        self.queued = 0             # requests that waited for a slot after they arrived
 
     def close(self):
         """Release every slot's device context."""
@@ -304,6 +306,7 @@ class SensitivityServer(object):
             self.slots.remove(victim)
             self.used -= victim.bytes()
             victim.rcf.close()
+            self.evictions += 1
         s = Slot(self.lib.get(key), key, self.precision, self.device, self.k, self.nPrimal)
         s.capture()
         self.bytes_of[key] = s.bytes()
@@ -328,6 +331,9 @@ class SensitivityServer(object):
                 r = waiting[0]
                 s = self._slot_for(r.key)
                 if s is None:
+                    if not getattr(r, '_queued', False):
+                        r._queued = True
+                        self.queued += 1
                     break
                 waiting.popleft()
                 state, dS = r.inputs if r.inputs is not None else request_inputs(s.case, r.seed)

@@ -155,10 +155,10 @@ class ClockSampler(object):
                 'reasons': sorted(reasons), 'samples': len(sm)}
 
 
-def make_case(workload):
+def make_case(workload, builder=None):
     from adfvm_gb300 import cases
     if workload.startswith('box'):
-        return cases.box(int(workload[3:]), objective='kinetic_energy')
+        return cases.box(int(workload[3:]), objective='kinetic_energy', builder=builder)
     if workload.startswith('cylinder'):
         a, b = workload[8:].split('x')
         return cases.cylinder(int(a), int(b))
@@ -175,20 +175,23 @@ def describe(case, precision):
         'cells': int(m.nInternalCells), 'faces': int(m.nFaces)}
 
 
-def cpu_baseline(args, threads, case=None, seconds=10.0):
-    """The oracle on the host cores, on a bounded sample of the workload: primal steps of the
-    C/OpenMP FP64 restatement (oracle/c) on the workload's own mesh for ~`seconds`, and the
-    adjoint step as torch autograd of the float64 oracle (the only CPU adjoint: the reference's
-    adpy reverse mode is absent) on a 32^3 box of the same recipe. value = primal+adjoint
-    Mcell-steps/s from the two per-cell-step times."""
-    import torch
+def cpu_baseline(args, threads, seconds=10.0):
+    """The reference path restated for the CPU, timed on the host cores on a bounded sample of
+    the workload itself - the same mesh, state and dt:
+      * the mesh built by the oracle's NumPy restatement of the reference's cmesh
+        (oracle/geometry.py, bit for bit the reference's), so the timed arm loads no library;
+      * FP64 primal steps by the C/OpenMP restatement of the residual and SSP-RK3 step
+        (oracle/c/afvm_oracle.c);
+      * FP64 adjoint steps by the host adjoint (oracle/c/adjoint_host.cpp: the C oracle's
+        forward, the face VJP compiled for the host, the reverse sweep in OpenMP) - the
+        reference has no CPU adjoint that runs (adpy's reverse mode is absent).
+    value = primal+adjoint Mcell-steps/s from the per-cell-step times of the two; primal and
+    adjoint are reported alone too."""
     from adfvm_gb300 import cases
-    from oracle import torch_ref
+    from oracle import geometry
     from oracle.c_ref import COracle
-    os.environ.setdefault('OMP_NUM_THREADS', str(threads))
-    torch.set_num_threads(threads)
-    if case is None:
-        case = make_case(args.workload)
+    os.environ['OMP_NUM_THREADS'] = str(threads)
+    case = make_case(args.workload, builder=geometry.build_mesh)
     m = case.build_mesh()
     co = COracle(m, case.bc, case.config, case.objective)
     x = cases.conservative(case)
@@ -199,23 +202,20 @@ def cpu_baseline(args, threads, case=None, seconds=10.0):
         x = co.step(x[0], x[1], x[2], case.dt)[:3]
         steps += 1
     tp = (time.perf_counter() - t0) / (steps * m.nInternalCells)        # s per cell-step
-    small = cases.box(32, objective='kinetic_energy')
-    sm = small.build_mesh()
-    prob = torch_ref.Problem(sm, small.bc, small.config, small.objective)
-    xs = [torch.as_tensor(a) for a in cases.conservative(small)]
-    seeds = [torch.ones_like(t) * 1e-3 for t in xs]
-    torch_ref.vjp_step(prob, xs[0], xs[1], xs[2], small.dt, None, seeds)
+    seeds = [np.full(np.shape(a), 1e-3) for a in x]
+    co.adjoint_step(x[0], x[1], x[2], case.dt, seeds)
     t0 = time.perf_counter()
     na = 0
-    while time.perf_counter() - t0 < seconds and na < 50:
-        torch_ref.vjp_step(prob, xs[0], xs[1], xs[2], small.dt, None, seeds)
+    while time.perf_counter() - t0 < seconds and na < 200:
+        a = co.adjoint_step(x[0], x[1], x[2], case.dt, seeds)
+        seeds = list(a[:3])
         na += 1
-    ta = (time.perf_counter() - t0) / (na * sm.nInternalCells)
+    ta = (time.perf_counter() - t0) / (na * m.nInternalCells)
     return {'value': 1.0 / (tp + ta) / 1e6, 'unit': UNIT, 'cores': threads, 'kind': 'port',
-            'primal': round(1.0 / tp / 1e6, 4), 'adjoint': round(1.0 / ta / 1e6, 4),
-            'sample': '%d FP64 primal steps of %s (%d cells) by the C/OpenMP oracle; %d adjoint steps of the '
-                      '32^3 box (%d cells) by torch autograd of the float64 oracle' % (
-                          steps, case.name, m.nInternalCells, na, sm.nInternalCells)}
+            'primal': round(1.0 / tp / 1e6, 4), 'adjoint': round(1.0 / ta / 1e6, 4), 'same_mesh': True,
+            'sample': '%d FP64 primal steps (C/OpenMP oracle) and %d FP64 adjoint steps (host adjoint, OpenMP) of '
+                      '%s (%d cells, the workload mesh, built by the oracle\'s restatement of the reference\'s '
+                      'cmesh), %d threads' % (steps, na, case.name, m.nInternalCells, threads)}
 
 
 def measure(case, precision, args, local, dist, world, clocks):
@@ -515,14 +515,67 @@ def serving_bench(local, lams=SERVING_LAMBDAS, seed=4, n_mix=48, window_s=6.0, p
         other = {'precision': compare, 'served_req_per_s': round(n_mix / sm32['elapsed_s'], 3),
                  'max_rel_err_vs_fp64': max(e32.values()), 'rel_err_by_mesh': e32}
         s32.close()
+    # the batching engine alone: the same mix served in FP64 against the plain FP64 form
+    s64 = serving.SensitivityServer(precision='fp64', device=local, k=10, nPrimal=100, library=lib,
+                                    hbm_budget=160e9, max_slots=64)
+    s64.warm(ks)
+    mix64 = serving.prepare([serving.Request(rid=i, key=k, seed=i, nPrimal=100, arrival=0.0)
+                             for i, k in enumerate(ks)], lib)
+    sm64 = s64.serve(mix64, realtime=False)
+    s64.close()
     served_rate = n_mix / sm['elapsed_s']
     plain_rate = n_mix / plain_mix_s
+    fp64_rate = n_mix / sm64['elapsed_s']
     return {'precision': precision, 'mix_requests': n_mix, 'served_req_per_s': round(served_rate, 3),
             'plain_fp64_req_per_s': round(plain_rate, 3), 'speedup_vs_plain': round(served_rate / plain_rate, 2),
+            'served_fp64_req_per_s': round(fp64_rate, 3),
+            'batching_gain_fp64': round(fp64_rate / plain_rate, 2),
+            'small_class': small_class_bench(local, lib),
             'plain_seconds_per_request': {k: round(v, 4) for k, v in t_plain.items()},
             'latency_sweep': sweep, 'max_rel_err_vs_fp64': max(errs.values()), 'rel_err_by_mesh': errs,
             'compare': other, 'slots': nslots, 'meshes': keys,
             'steps_per_request': '100 primal + 100 adjoint (checkpoints every 10)'}
+
+
+SMALL_KEYS = ['box16', 'box24', 'box32', 'cyl64x32']
+
+
+def small_class_bench(local, lib, n_req=48, seed=6, precision='fp32'):
+    """The small meshes of the serving mix, where launch and latency costs weigh most: n_req
+    requests drawn from box16/24/32 and cyl64x32 served together, against the GPU time the same
+    requests' graphs take replayed one request after another on one stream (CUDA events, no
+    server and no overlap). served / sequential < 1 is what the overlap of requests on the GPU
+    buys; close to 1 would leave room for a single ragged launch over all requests."""
+    import torch
+    from adfvm_gb300 import serving
+    rng = np.random.default_rng(seed)
+    ks = [SMALL_KEYS[i] for i in rng.integers(0, len(SMALL_KEYS), size=n_req)]
+    srv = serving.SensitivityServer(precision=precision, device=local, k=10, nPrimal=100, library=lib,
+                                    hbm_budget=60e9, max_slots=64)
+    srv.warm(ks)
+    reqs = serving.prepare([serving.Request(rid=i, key=k, seed=i, nPrimal=100) for i, k in enumerate(ks)], lib)
+    st = srv.serve(reqs, realtime=False)
+    # one request's graph replays per mesh, alone on one slot's stream
+    per_key = {}
+    for key in SMALL_KEYS:
+        slot = next(s for s in srv.slots if s.key == key)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(slot.stream)
+        for _ in range(slot.nck):
+            slot.graphs[0].replay()
+        for _ in range(slot.nck):
+            slot.graphs[1].replay()
+            slot.graphs[2].replay()
+        e1.record(slot.stream)
+        torch.cuda.synchronize()
+        per_key[key] = e0.elapsed_time(e1) / 1e3
+    srv.close()
+    seq = sum(per_key[k] for k in ks)
+    return {'requests': n_req, 'meshes': SMALL_KEYS, 'precision': precision,
+            'served_s': round(st['elapsed_s'], 4), 'served_req_per_s': round(n_req / st['elapsed_s'], 2),
+            'sequential_graph_s': round(seq, 4), 'served_over_sequential': round(st['elapsed_s'] / seq, 3),
+            'graph_s_per_request': {k: round(v, 5) for k, v in per_key.items()}}
 
 
 def run_reference(args):
@@ -606,6 +659,10 @@ def main():
                                             'kernels', 'adjoint_kernels', 'e2e')}
     if args.serving and rank == 0:
         line['serving'] = serving_bench(local)
+    if rank == 0 and args.serving:
+        # FP32 / mixed against FP64 on the cylinder over 2000 steps (adfvm_gb300/studies.py)
+        from adfvm_gb300.studies import precision_study
+        line['precision_study'] = precision_study(device=local)
     if rank == 0:
         line['mesh_build'] = mesh_build_timing(case, local)
         if case.name.startswith('box'):
@@ -627,7 +684,13 @@ def main():
             'peak_source': 'afvm_fma_peak (a DFMA loop on this GPU, FMA = 2 flops)',
             'note': 'issue_frac counts DADD/DMUL/DFMA as one FP64 pipe issue each'}
     if rank == 0 and not args.no_cpu_baseline:
-        line['cpu_baseline'] = cpu_baseline(args, os.cpu_count() or 1, case=case)
+        cb = cpu_baseline(args, os.cpu_count() or 1)
+        line['cpu_baseline'] = cb
+        # the GPU's speed-up on the same mesh, FP64 both: primal and adjoint alone and together
+        line['vs_cpu_baseline'] = {'primal': round(m64['primal']['value'] / cb['primal'], 2),
+                                   'adjoint': round(m64['adjoint']['value'] / cb['adjoint'], 2),
+                                   'primal_adjoint': round(m64['value'] / cb['value'], 2),
+                                   'e2e': round(m64['e2e']['value'] / cb['value'], 2)}
     if rank == 0:
         print(json.dumps(line))
     if dist:

@@ -50,15 +50,31 @@ def build_ref():
 
 def build_c():
     """Compile the C restatements (the residual, oracle/c/afvm_oracle.c; the cell renumbering,
-    oracle/c/reorder_oracle.c) into oracle/_ref/liboracle.so."""
+    oracle/c/reorder_oracle.c) and the host adjoint baseline (oracle/c/adjoint_host.cpp, which
+    compiles the library's face VJP adfvm_gb300/csrc/face.cuh for the host) into
+    oracle/_ref/liboracle.so."""
     os.makedirs(OUT, exist_ok=True)
-    srcs = [os.path.join(HERE, 'c', f) for f in ('afvm_oracle.c', 'reorder_oracle.c')]
-    if not all(os.path.exists(s) for s in srcs):
+    csrc = [os.path.join(HERE, 'c', f) for f in ('afvm_oracle.c', 'reorder_oracle.c')]
+    cxx = os.path.join(HERE, 'c', 'adjoint_host.cpp')
+    root = os.path.dirname(HERE)
+    inc = ['-I' + os.path.join(HERE, 'c'), '-I' + os.path.join(root, 'adfvm_gb300', 'csrc'),
+           '-I' + os.path.join(root, 'include')]
+    deps = csrc + [cxx, os.path.join(HERE, 'c', 'afvm_oracle.h')] + \
+        [os.path.join(root, 'adfvm_gb300', 'csrc', f) for f in ('face.cuh', 'physics.cuh')]
+    if not all(os.path.exists(s) for s in deps):
         return None
     target = os.path.join(OUT, 'liboracle.so')
-    if os.path.exists(target) and all(os.path.getmtime(target) > os.path.getmtime(s) for s in srcs):
+    if os.path.exists(target) and all(os.path.getmtime(target) > os.path.getmtime(s) for s in deps):
         return target
-    _run(['gcc', '-O3', '-std=c11', '-shared', '-fPIC', '-fopenmp', '-ffp-contract=off'] + srcs + ['-o', target, '-lm'])
+    objs = []
+    for src in csrc:
+        obj = os.path.join(OUT, os.path.basename(src) + '.o')
+        _run(['gcc', '-O3', '-std=c11', '-fPIC', '-fopenmp', '-ffp-contract=off'] + inc + ['-c', src, '-o', obj])
+        objs.append(obj)
+    obj = os.path.join(OUT, 'adjoint_host.cpp.o')
+    _run(['g++', '-O3', '-std=c++17', '-fPIC', '-fopenmp', '-ffp-contract=off'] + inc + ['-c', cxx, '-o', obj])
+    objs.append(obj)
+    _run(['g++', '-shared', '-fopenmp'] + objs + ['-o', target, '-lm'])
     return target
 
 

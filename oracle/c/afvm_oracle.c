@@ -23,31 +23,9 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include "afvm_oracle.h"
+
 #define SMALL 1e-30
-
-enum { K_COPY = 0, K_FIXED = 1, K_SYM = 2, K_TOTALPT = 3 };
-enum { F_INTERNAL = 0, F_COUPLED = 1, F_CHAR = 2, F_BOUNDARY = 3 };
-
-typedef struct {
-    int nIC, nIF, nF, nG;
-    const int32_t *own, *nbr;                      /* nF */
-    const double *nrm, *area, *dlt, *du, *lw, *qw; /* AoS as the reference: nrm nF x 3 ... qw nF x 6 */
-    const double *wts;                             /* weights nF */
-    const double *vol;                             /* nIC */
-    const int32_t *cellFaces, *cellNbr, *cellOwn;  /* nIC x 6 */
-    const uint8_t *fkind;                          /* nG: face kind of each boundary face */
-    const int32_t *gsrc, *gkind;                   /* nG */
-    const double *gval;                            /* nG x 5 fixed U T p */
-    const int32_t *accf;                           /* nIC x 6: face (owner side) or ~face */
-    double gamma, Cp, Pr;
-    int muModel; double mu0, muAs, muTs;
-    int riemann, briemann;
-    int objective, objStart, objN;                 /* 0 none 1 KE 2 drag 3 sumT 4 vane */
-    /* turbine-vane objective (adFVM/objectives/vane.py:7-60, 118-131) */
-    int nPlane; const int32_t* planeCells; const double* planeAreas;
-    double vn[3], ptin, Tw, va, vb;
-    int nHeat; const int32_t* heatFaces; const double* heatW; /* faces of the heat patches, weights */
-} oracle_mesh;
 
 static inline double dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
 
@@ -210,41 +188,14 @@ static void face_flux(const oracle_mesh* M, const double* rec, int f, double* ou
     out[5] = fabs(dot3(UF, N)) + aF;
 }
 
+static void gradients(const oracle_mesh* M, double* rec);
+static void prims_ghosts(const oracle_mesh* M, const double* rho, const double* rU, const double* rE, double* rec);
+
 /* residual of state (rho, rU, rE) into R (nIC x 5) and the CFL sums; objective if want */
 static void equation(const oracle_mesh* M, const double* rho, const double* rU, const double* rE, double* rec,
                      double* ff, double* R, double* dtc, double* obj) {
-    int nIC = M->nIC, nG = M->nG;
-#pragma omp parallel for schedule(static)
-    for (int c = 0; c < nIC; c++) {
-        double* r = rec + 20 * (size_t)c;
-        primitive(M, rho[c], rU + 3 * (size_t)c, rE[c], r, r + 3, r + 4);
-    }
-#pragma omp parallel for schedule(static)
-    for (int g = 0; g < nG; g++) {
-        const double* s = rec + 20 * (size_t)M->gsrc[g];
-        double* r = rec + 20 * (size_t)(nIC + g);
-        for (int k = 0; k < 5; k++) r[k] = s[k];
-        int kind = M->gkind[g];
-        int kU = kind & 7, kT = (kind >> 3) & 7, kp = (kind >> 6) & 7;
-        const double* n = M->nrm + 3 * (size_t)(M->nIF + g);
-        if (kU == K_TOTALPT) {
-            /* CBC_TOTAL_PT, BCs.py:178-184 */
-            const double* d = M->gval + 5 * (size_t)g;
-            double Tt = d[3], pt = d[4], T = r[3];
-            double Un = dot3(r, d);
-            for (int k = 0; k < 3; k++) r[k] = Un * d[k];
-            r[3] = Tt - 0.5 * Un * Un / M->Cp;
-            r[4] = pt * pow(T / Tt, M->gamma / (M->gamma - 1));
-            continue;
-        }
-        if (kU == K_FIXED) for (int k = 0; k < 3; k++) r[k] = M->gval[5 * (size_t)g + k] * 1;
-        else if (kU == K_SYM) {
-            double un = dot3(r, n);
-            for (int k = 0; k < 3; k++) r[k] = r[k] - un * n[k];
-        }
-        if (kT == K_FIXED) r[3] = M->gval[5 * (size_t)g + 3] * 1;
-        if (kp == K_FIXED) r[4] = M->gval[5 * (size_t)g + 4] * 1;
-    }
+    int nIC = M->nIC;
+    prims_ghosts(M, rho, rU, rE, rec);
     if (obj) {
         double v = 0.0;
         if (M->objective == 1) {
@@ -293,7 +244,66 @@ static void equation(const oracle_mesh* M, const double* rho, const double* rU, 
         }
         *obj = v;
     }
-    /* gradCell, cellFaces order (op.py:45-63) */
+    gradients(M, rec);
+#pragma omp parallel for schedule(static)
+    for (int f = 0; f < M->nF; f++) face_flux(M, rec, f, ff + 6 * (size_t)f);
+#pragma omp parallel for schedule(static)
+    for (int c = 0; c < nIC; c++) {
+        double acc[5] = {0, 0, 0, 0, 0}, d = 0;
+        for (int s = 0; s < 6; s++) {
+            int e = M->accf[6 * (size_t)c + s];
+            int own = e >= 0, f = own ? e : ~e;
+            double w = own ? M->area[f] / M->vol[M->own[f]] : M->area[f] / M->vol[M->nbr[f]];
+            const double* F = ff + 6 * (size_t)f;
+            for (int q = 0; q < 5; q++) {
+                double t = F[q] * w;
+                acc[q] = acc[q] + (own ? t : -t);
+            }
+            d = d + F[5] * w;
+        }
+        for (int q = 0; q < 5; q++) R[5 * (size_t)c + q] = acc[q];
+        dtc[c] = d;
+    }
+}
+
+/* gradCell, cellFaces order (op.py:45-63), into the records' gradient part */
+static void prims_ghosts(const oracle_mesh* M, const double* rho, const double* rU, const double* rE, double* rec) {
+    int nIC = M->nIC, nG = M->nG;
+#pragma omp parallel for schedule(static)
+    for (int c = 0; c < nIC; c++) {
+        double* r = rec + 20 * (size_t)c;
+        primitive(M, rho[c], rU + 3 * (size_t)c, rE[c], r, r + 3, r + 4);
+    }
+#pragma omp parallel for schedule(static)
+    for (int g = 0; g < nG; g++) {
+        const double* s = rec + 20 * (size_t)M->gsrc[g];
+        double* r = rec + 20 * (size_t)(nIC + g);
+        for (int k = 0; k < 5; k++) r[k] = s[k];
+        int kind = M->gkind[g];
+        int kU = kind & 7, kT = (kind >> 3) & 7, kp = (kind >> 6) & 7;
+        const double* n = M->nrm + 3 * (size_t)(M->nIF + g);
+        if (kU == K_TOTALPT) {
+            /* CBC_TOTAL_PT, BCs.py:178-184 */
+            const double* d = M->gval + 5 * (size_t)g;
+            double Tt = d[3], pt = d[4], T = r[3];
+            double Un = dot3(r, d);
+            for (int k = 0; k < 3; k++) r[k] = Un * d[k];
+            r[3] = Tt - 0.5 * Un * Un / M->Cp;
+            r[4] = pt * pow(T / Tt, M->gamma / (M->gamma - 1));
+            continue;
+        }
+        if (kU == K_FIXED) for (int k = 0; k < 3; k++) r[k] = M->gval[5 * (size_t)g + k] * 1;
+        else if (kU == K_SYM) {
+            double un = dot3(r, n);
+            for (int k = 0; k < 3; k++) r[k] = r[k] - un * n[k];
+        }
+        if (kT == K_FIXED) r[3] = M->gval[5 * (size_t)g + 3] * 1;
+        if (kp == K_FIXED) r[4] = M->gval[5 * (size_t)g + 4] * 1;
+    }
+}
+
+static void gradients(const oracle_mesh* M, double* rec) {
+    int nIC = M->nIC;
 #pragma omp parallel for schedule(static)
     for (int c = 0; c < nIC; c++) {
         double g[15];
@@ -322,25 +332,6 @@ static void equation(const oracle_mesh* M, const double* rho, const double* rU, 
         }
         double* out = rec + 20 * (size_t)c + 5;
         for (int k = 0; k < 15; k++) out[k] = g[k] / M->vol[c];
-    }
-#pragma omp parallel for schedule(static)
-    for (int f = 0; f < M->nF; f++) face_flux(M, rec, f, ff + 6 * (size_t)f);
-#pragma omp parallel for schedule(static)
-    for (int c = 0; c < nIC; c++) {
-        double acc[5] = {0, 0, 0, 0, 0}, d = 0;
-        for (int s = 0; s < 6; s++) {
-            int e = M->accf[6 * (size_t)c + s];
-            int own = e >= 0, f = own ? e : ~e;
-            double w = own ? M->area[f] / M->vol[M->own[f]] : M->area[f] / M->vol[M->nbr[f]];
-            const double* F = ff + 6 * (size_t)f;
-            for (int q = 0; q < 5; q++) {
-                double t = F[q] * w;
-                acc[q] = acc[q] + (own ? t : -t);
-            }
-            d = d + F[5] * w;
-        }
-        for (int q = 0; q < 5; q++) R[5 * (size_t)c + q] = acc[q];
-        dtc[c] = d;
     }
 }
 
@@ -394,4 +385,18 @@ void oracle_step(const oracle_mesh* M, const double* rho, const double* rU, cons
 size_t oracle_work_doubles(const oracle_mesh* M) {
     return 20 * (size_t)(M->nIC + M->nG) + 6 * (size_t)M->nF + 5 * (size_t)M->nIC + (size_t)M->nIC +
            10 * (size_t)M->nIC;
+}
+
+/* the cell records (primitives with ghost rows, then gradients; 20 values a cell) of a state:
+ * what the residual reads, for the host adjoint (oracle/c/adjoint_host.cpp). work: as for
+ * oracle_step (its first 20 (nIC + nG) values are the records). */
+void oracle_records(const oracle_mesh* M, const double* rho, const double* rU, const double* rE, double* work) {
+    prims_ghosts(M, rho, rU, rE, work);
+    gradients(M, work);
+}
+
+/* the RK stage states u1 (k = 1) and u2 (k = 2) a finished oracle_step left in its work */
+double* oracle_work_stage(const oracle_mesh* M, double* work, int k) {
+    double* st1 = work + 20 * (size_t)(M->nIC + M->nG) + 6 * (size_t)M->nF + 5 * (size_t)M->nIC + (size_t)M->nIC;
+    return k == 1 ? st1 : st1 + 5 * (size_t)M->nIC;
 }

@@ -45,6 +45,11 @@ def lib():
         L.oracle_mesh_reorder.argtypes = [C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 3 + [C.c_int] + \
             [C.c_void_p] * 3 + [C.c_void_p] * 6
         L.oracle_mesh_reorder.restype = C.c_int
+        L.oracle_adjoint_work_doubles.argtypes = [C.POINTER(OracleMesh)]
+        L.oracle_adjoint_work_doubles.restype = C.c_size_t
+        L.oracle_adjoint_step.argtypes = [C.POINTER(OracleMesh)] + [C.c_void_p] * 3 + [C.c_double] + \
+            [C.c_void_p] * 4 + [C.c_double] + [C.c_void_p] * 5
+        L.oracle_adjoint_step.restype = C.c_int
         _lib = L
     return _lib
 
@@ -169,6 +174,28 @@ class COracle(object):
         lib().oracle_step(C.byref(self.M), v(x[0]), v(x[1]), v(x[2]), float(dt), v(Sp), v(out[0]), v(out[1]),
                           v(out[2]), C.byref(dtc), C.byref(obj), v(self.work))
         return out[0], out[1], out[2], dtc.value, obj.value
+
+
+def _adjoint_step(self, rho, rhoU, rhoE, dt, seeds, S=None, obja=1.0):
+    """The host adjoint baseline (oracle/c/adjoint_host.cpp): VJP of one FP64 step with dt held
+    fixed. Returns (rhoa, rhoUa, rhoEa, S_a (nIC x 5))."""
+    n = self.nIC
+    if not hasattr(self, 'awork'):
+        self.awork = np.zeros(lib().oracle_adjoint_work_doubles(C.byref(self.M)))
+    x = [np.ascontiguousarray(a, np.float64).reshape(n, d) for a, d in zip((rho, rhoU, rhoE), (1, 3, 1))]
+    sd = [np.ascontiguousarray(a, np.float64).reshape(n, d) for a, d in zip(seeds, (1, 3, 1))]
+    out = [np.empty((n, d)) for d in (1, 3, 1)]
+    Sa = np.empty((n, 5))
+    Sp = None if S is None else np.ascontiguousarray(np.concatenate([np.asarray(s).reshape(n, -1) for s in S], 1))
+    v = lambda a: None if a is None else C.c_void_p(a.ctypes.data)
+    st = lib().oracle_adjoint_step(C.byref(self.M), v(x[0]), v(x[1]), v(x[2]), float(dt), v(Sp), v(sd[0]), v(sd[1]),
+                                   v(sd[2]), float(obja), v(out[0]), v(out[1]), v(out[2]), v(Sa), v(self.awork))
+    if st != 0:
+        raise ValueError('oracle_adjoint_step: objective not supported by the host adjoint')
+    return out[0], out[1], out[2], Sa
+
+
+COracle.adjoint_step = _adjoint_step
 
 
 def mesh_reorder(meshData):

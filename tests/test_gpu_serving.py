@@ -31,26 +31,51 @@ def test_same_result_alone_and_in_the_mix():
         assert abs(r.sensitivity - q.sensitivity) <= 1e-12 * abs(r.sensitivity), (r.key, r.sensitivity, q.sensitivity)
 
 
-def test_fp32_served_within_bound_of_fp64():
+@pytest.mark.parametrize('precision', ['fp32', 'mixed'])
+def test_reduced_precision_served_within_1e5_of_fp64(precision):
+    """The served request as the workload defines it - 100 primal + 100 adjoint steps,
+    checkpoints every 10 - on the smallest box and the smallest cylinder of the serving mix:
+    FP32 storage and flux arithmetic with FP64 sensitivity accumulation ('fp32'), and the same
+    with FP64 state, stages and adjoints ('mixed'), within 1e-5 relative of plain FP64."""
     lib = serving.MeshLibrary()
-    r64 = _reqs(KEYS, [7, 8, 9], 8)
-    serving.plain_one_at_a_time(r64, lib, nPrimal=8)
-    r32 = _reqs(KEYS, [7, 8, 9], 8)
-    srv = serving.SensitivityServer(precision='fp32', k=4, nPrimal=8, library=lib)
-    srv.serve(r32, realtime=False)
-    for a, b in zip(r32, r64):
-        # FP32 storage and flux arithmetic, FP64 sensitivity accumulation: 1e-3 relative over
-        # 8 primal + 8 adjoint steps
-        assert abs(a.sensitivity - b.sensitivity) <= 1e-3 * abs(b.sensitivity), (a.key, a.sensitivity, b.sensitivity)
+    keys = ['box16', 'cyl64x32']
+    r64 = _reqs(keys, [7, 8], 100)
+    serving.plain_one_at_a_time(r64, lib, nPrimal=100)
+    rr = _reqs(keys, [7, 8], 100)
+    srv = serving.SensitivityServer(precision=precision, k=10, nPrimal=100, library=lib)
+    srv.serve(rr, realtime=False)
+    for a, b in zip(rr, r64):
+        e = abs(a.sensitivity - b.sensitivity) / abs(b.sensitivity)
+        assert e <= 1e-5, '%s %s: rel err %.3e' % (precision, a.key, e)
+    srv.close()
 
 
-def test_mixed_served_within_bound_of_fp64():
+def test_admission_under_memory_pressure():
+    """An HBM budget that holds two slots, three meshes, requests arriving in real time while
+    others run: requests queue, an idle slot of one mesh is evicted for another mesh, requests
+    are admitted mid-flight - and every FP64 result is bitwise the one of the same request
+    served alone."""
     lib = serving.MeshLibrary()
-    r64 = _reqs(KEYS, [7, 8, 9], 8)
-    serving.plain_one_at_a_time(r64, lib, nPrimal=8)
-    rm = _reqs(KEYS, [7, 8, 9], 8)
-    srv = serving.SensitivityServer(precision='mixed', k=4, nPrimal=8, library=lib)
-    srv.serve(rm, realtime=False)
-    for a, b in zip(rm, r64):
-        # FP32 face arithmetic, FP64 state, stages, adjoints and sums: 1e-5 relative
-        assert abs(a.sensitivity - b.sensitivity) <= 1e-5 * abs(b.sensitivity), (a.key, a.sensitivity, b.sensitivity)
+    keys = ['box8', 'cyl16x8', 'box6', 'box8', 'box6', 'cyl16x8', 'box8']
+    seeds = [11, 12, 13, 14, 15, 16, 17]
+    alone = []
+    big = serving.SensitivityServer(precision='fp64', k=4, nPrimal=20, library=lib)
+    for k, sd in zip(keys, seeds):
+        r = serving.Request(rid=0, key=k, seed=sd, nPrimal=20)
+        big.serve([r], realtime=False)
+        alone.append(r.sensitivity)
+    sizes = {k: big.bytes_of[k] for k in set(keys)}
+    big.close()
+    budget = sum(sorted(sizes.values())[-2:]) + 1       # the two largest slots, no third
+    srv = serving.SensitivityServer(precision='fp64', k=4, nPrimal=20, library=lib, hbm_budget=budget)
+    srv.bytes_of.update(sizes)
+    reqs = [serving.Request(rid=i, key=k, seed=sd, nPrimal=20, arrival=0.002 * i)
+            for i, (k, sd) in enumerate(zip(keys, seeds))]
+    st = srv.serve(reqs, realtime=True)
+    assert st['requests'] == len(reqs)
+    assert srv.evictions >= 1 and srv.queued >= 1, (srv.evictions, srv.queued)
+    assert len(srv.slots) <= 2 and srv.used <= budget
+    assert any(r.t_admit > r.arrival + 1e-3 for r in reqs)          # waited for a slot
+    for r, ref in zip(reqs, alone):
+        assert r.sensitivity == ref, (r.rid, r.key, r.sensitivity, ref)
+    srv.close()
