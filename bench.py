@@ -561,13 +561,14 @@ def small_class_bench(local, lib, n_req=48, seed=6, precision='fp32'):
         slot = next(s for s in srv.slots if s.key == key)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
-        e0.record(slot.stream)
-        for _ in range(slot.nck):
-            slot.graphs[0].replay()
-        for _ in range(slot.nck):
-            slot.graphs[1].replay()
-            slot.graphs[2].replay()
-        e1.record(slot.stream)
+        with torch.cuda.stream(slot.stream):          # a graph replays on the current stream
+            e0.record(slot.stream)
+            for _ in range(slot.nck):
+                slot.graphs[0].replay()
+            for _ in range(slot.nck):
+                slot.graphs[1].replay()
+                slot.graphs[2].replay()
+            e1.record(slot.stream)
         torch.cuda.synchronize()
         per_key[key] = e0.elapsed_time(e1) / 1e3
     srv.close()
