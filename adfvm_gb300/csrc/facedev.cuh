@@ -21,20 +21,14 @@ __device__ __forceinline__ void load_vec(const float* __restrict__ p, float* o, 
     }
 }
 
-// the 55 inputs of one face: primitives and gradients of both sides, geometry. ownRec: the
-// owner's record where the caller staged it (shared memory), else NULL
+// the 55 inputs of one face: primitives and gradients of both sides, geometry
 template <typename R>
-__device__ __forceinline__ void load_face(const MeshDev<R>& m, const R* __restrict__ rec, int f, FaceIn<R>& in,
-                                          const R* ownRec = nullptr) {
+__device__ __forceinline__ void load_face(const MeshDev<R>& m, const R* __restrict__ rec, int f, FaceIn<R>& in) {
     const size_t nF = m.nF;
     int iP = m.own[f], iN = m.nbr[f];
     int iNg = (f < m.nIF) ? iN : m.gsrc[iN - m.nIC];   // ghost gradient = copy of its source
     R rP[REC], rN[REC], rNg[REC];
-    if (ownRec) {
-        for (int k = 0; k < REC; k++) rP[k] = ownRec[k];
-    } else {
-        load_vec(rec + (size_t)iP * REC, rP, REC);
-    }
+    load_vec(rec + (size_t)iP * REC, rP, REC);
     load_vec(rec + (size_t)iN * REC, rN, REC);
     if (iNg == iN) {
         for (int k = 0; k < REC; k++) rNg[k] = rN[k];
@@ -56,35 +50,6 @@ __device__ __forceinline__ void load_face(const MeshDev<R>& m, const R* __restri
     in.lw0 = m.lw[f];
     in.lw1 = m.lw[nF + f];
     in.rdelta = m.rdlt[f];
-}
-
-// FP32 face kernels: the owners of a block's internal faces (faces sorted by owner) are a
-// short run of consecutive cells, whose records the block copies into shared memory with
-// coalesced 16-byte loads before its threads read them (each record is read by about three
-// faces). Returns the staged record of face f's owner, or NULL (face outside the run, a
-// boundary face, a mesh whose faces are not sorted by owner) for a global load. All threads
-// of the block must call it (it synchronises).
-template <typename R>
-__device__ __forceinline__ const R* stage_owner_records(const MeshDev<R>& m, const R* __restrict__ rec, int f0,
-                                                        int nFaces, int f, R* sOwn) {
-    const int fl = min(f0 + nFaces, m.nIF) - 1;        // the block's last internal face
-    int o0 = 0, no = 0;
-    if (f0 <= fl) {
-        o0 = m.own[f0];
-        no = m.own[fl] - o0 + 1;
-    }
-    const bool ok = no > 0 && no <= nFaces;             // uniform over the block
-    if (ok) {
-        using V = typename Vec16<R>::type;
-        const V* src = reinterpret_cast<const V*>(rec + (size_t)o0 * REC);
-        V* dst = reinterpret_cast<V*>(sOwn);
-        const int nv = no * (REC * (int)sizeof(R) / 16);
-        for (int i = threadIdx.x; i < nv; i += blockDim.x) dst[i] = __ldg(src + i);
-    }
-    __syncthreads();
-    if (!ok || f > fl) return nullptr;
-    const int o = m.own[f] - o0;
-    return (o >= 0 && o < no) ? sOwn + (size_t)o * REC : nullptr;
 }
 
 // a face's column of a device tape (value k of face f at tape[k nF + f]; p = tape + f)

@@ -188,17 +188,10 @@ __global__ void __launch_bounds__(FLUX_BLOCK, sizeof(R) == 8 ? 3 : 8) k_flux(Mes
     // the 20- and 40-value records are, made this kernel slower - 0.217 -> 0.269 ms at 128^3 in
     // FP32 - the barrier costs more than the six partly coalesced stores)
     int f = blockIdx.x * blockDim.x + threadIdx.x;
-    const R* ownRec = nullptr;
-    if constexpr (sizeof(R) == 4) {
-        // FP32: the block's owner records staged in shared memory (FP64 is bound by its FP64
-        // pipe, not by these loads)
-        __shared__ __align__(16) R sOwn[FLUX_BLOCK * REC];
-        ownRec = stage_owner_records<R>(m, rec, blockIdx.x * FLUX_BLOCK, FLUX_BLOCK, f, sOwn);
-    }
     if (f >= m.nF) return;
     int kind = (f < m.nIF) ? FACE_INTERNAL : (int)m.fkind[f - m.nIF];
     FaceIn<R> in;
-    load_face<R>(m, rec, f, in, ownRec);
+    load_face<R>(m, rec, f, in);
     R F[5], maxaF;
     if (TAPED)
         face_flux<R>(P, kind, inviscid != 0, in, F, maxaF, TapeStore<R>{tape + f, (size_t)m.nF});
