@@ -241,3 +241,15 @@ def source_field(mesh, scale=1.0, seed=5):
     G = scale * np.exp(-np.sum((cc - mid) ** 2, axis=1, keepdims=True) / width ** 2)
     S_rhoU = np.zeros((len(cc), 3)); S_rhoU[:, 0] = 100 * G[:, 0]
     return (G.copy(), S_rhoU, 2e5 * G)
+
+
+def copies(case, K):
+    """The case on K disjoint copies of its mesh (meshgen.copies): boundary values and the
+    initial primitive fields repeated per copy, the same options, objective and dt."""
+    md = meshgen.copies(case.meshData, K)
+    rep = lambda a: np.concatenate([np.asarray(a)] * K) if isinstance(a, np.ndarray) else a
+    bc = {f: {p: {k: rep(v) for k, v in e.items()} for p, e in case.bc[f].items()} for f in case.bc}
+    c = Case('%sx%d' % (case.name, K), md, bc, rep(case.U), rep(case.T), rep(case.p), config=dict(case.config),
+             objective=case.objective, dt=case.dt)
+    c.build_mesh()
+    return c

@@ -321,3 +321,36 @@ def channel(nx=64, ny=32, x0=0.0, x1=0.1, y0=0.0, y1=0.044, dz=None, stretch=0.0
           ('back', 'empty', cell(Ii, Jj).ravel(), qz(Ii, Jj, 0).reshape(-1, 4)[:, ::-1], {})]
     faces, owner, neighbour, boundary = _assemble(A, B, Q, bp)
     return P, faces, owner, neighbour, boundary
+
+
+def copies(meshData, K):
+    """K disjoint copies of a mesh as one mesh: points, cells and faces of copy j offset by j
+    times the originals' counts; the internal faces copy after copy (still sorted by owner);
+    each boundary patch keeps its name and holds its faces of every copy, copy after copy
+    (a cyclic pair's faces still pair up face for face). Every cell sees the same neighbours,
+    faces and patch order as in the original, so the residual of each copy is computed with
+    exactly the arithmetic of the single mesh."""
+    points, faces, owner, neighbour, boundary = meshData
+    points = np.asarray(points)
+    faces = np.asarray(faces)
+    owner = np.asarray(owner).reshape(-1)
+    neighbour = np.asarray(neighbour).reshape(-1)
+    nP, nIF, nIC = len(points), len(neighbour), int(owner.max()) + 1
+    pts = np.concatenate([points] * K)
+    shift = lambda f, j: np.concatenate([f[:, :1], f[:, 1:] + j * nP], axis=1)
+    fl = [shift(faces[:nIF], j) for j in range(K)]
+    ol = [owner[:nIF] + j * nIC for j in range(K)]
+    nl = [neighbour + j * nIC for j in range(K)]
+    out = {}
+    start = K * nIF
+    for name, b in sorted(boundary.items(), key=lambda kv: int(kv[1]['startFace'])):
+        s, n = int(b['startFace']), int(b['nFaces'])
+        for j in range(K):
+            fl.append(shift(faces[s:s + n], j))
+            ol.append(owner[s:s + n] + j * nIC)
+        e = dict(b)
+        e['startFace'], e['nFaces'] = start, K * n
+        out[name] = e
+        start += K * n
+    return (pts, np.concatenate(fl).astype(np.int32), np.concatenate(ol).astype(np.int32),
+            np.concatenate(nl).astype(np.int32), out)

@@ -19,6 +19,13 @@ Design:
   so the work of all requests overlaps on the GPU; the host only polls events.
 * Kernels are per request and reductions have fixed orders (no atomics across requests), so a
   request's result is bitwise the same alone and in any mix.
+* Batched slots (``batch={key: K}``): one slot runs up to K requests on the same mesh in the
+  same launches - its context is built on K disjoint copies of the mesh (cases.copies), each
+  request's state and perturbation in its copy's cells, its sensitivity the sum over its own
+  cells. Small meshes (thousands of cells) leave the GPU idle between their short kernels;
+  packed K to a launch they fill it. Every cell of a copy computes exactly what it computes on
+  the single mesh, so a request's result does not depend on which copy it runs in or on the
+  other requests of the batch.
 """
 import collections
 import math
@@ -51,12 +58,13 @@ class MeshLibrary(object):
     def __init__(self):
         self.cases = {}
 
-    def get(self, key):
-        if key not in self.cases:
-            c = make_case(key)
+    def get(self, key, copies=1):
+        ck = key if copies == 1 else (key, copies)
+        if ck not in self.cases:
+            c = make_case(key) if copies == 1 else cases.copies(self.get(key), copies)
             c.build_mesh()
-            self.cases[key] = c
-        return self.cases[key]
+            self.cases[ck] = c
+        return self.cases[ck]
 
 
 @dataclass
@@ -104,10 +112,11 @@ def request_inputs(case, seed):
 
 
 class Slot(object):
-    def __init__(self, case, key, precision, device, k, nPrimal):
+    def __init__(self, case, key, precision, device, k, nPrimal, copies=1):
         torch = _torch()
         self.key = key
         self.case = case
+        self.copies = copies                  # requests a launch serves (disjoint mesh copies)
         self.k = k
         self.nPrimal = nPrimal
         self.nck = nPrimal // k
@@ -127,12 +136,13 @@ class Slot(object):
         self.a = z()
         self.S = z()
         self.dS = [torch.zeros(s, dtype=torch.float64, device=self.dev) for s in shapes]
-        self.acc = torch.zeros(1, dtype=torch.float64, device=self.dev)
+        self.acc = torch.zeros(copies, dtype=torch.float64, device=self.dev)
         self.objacc = torch.zeros(1, dtype=torch.float64, device=self.dev)
         self.dt = case.dt
         self.stream = torch.cuda.Stream(device=self.dev)
         self.busy = False
         self.req = None
+        self.reqs = []
         self.graphs = None
         self.ev = torch.cuda.Event()
 
@@ -155,9 +165,12 @@ class Slot(object):
             y = self.states[j]
             r = self.rcf.adjoint_step(y[0], y[1], y[2], self.dt, self.a, obja=1.0, S=self.S, out=self.a,
                                       stages=self.stages[j], tape=self.tapes[j])
-            # FP64 sensitivity accumulation (cmesh.computeSensitivity summed over time)
-            s = (r[3][0].double() * self.dS[0]).sum() + (r[3][1].double() * self.dS[1]).sum() + \
-                (r[3][2].double() * self.dS[2]).sum()
+            # FP64 sensitivity accumulation (cmesh.computeSensitivity summed over time), one sum a
+            # request over its own cells
+            K = self.copies
+            s = (r[3][0].double() * self.dS[0]).view(K, -1).sum(1) + \
+                (r[3][1].double() * self.dS[1]).view(K, -1).sum(1) + \
+                (r[3][2].double() * self.dS[2]).view(K, -1).sum(1)
             self.acc.add_(s)
 
     def capture(self):
@@ -178,19 +191,28 @@ class Slot(object):
         self.stream.synchronize()
 
     # ---- a request's work as a list of small host closures, run one per engine pass
-    def start(self, req, state, dS):
-        """state, dS: host arrays, or pinned host tensors (copied asynchronously)."""
+    def start(self, reqs, payloads):
+        """reqs: up to ``copies`` requests; payloads: their (state, dS), host arrays or pinned
+        host tensors (copied asynchronously), each into its copy's cells. Copies without a
+        request run the first request's state with a zero perturbation (their results unused)."""
         torch = _torch()
-        self.req = req
+        self.reqs = list(reqs)
+        self.req = self.reqs[0]
         self.busy = True
         host = lambda v: v if isinstance(v, torch.Tensor) else torch.as_tensor(np.ascontiguousarray(v, np.float64))
+        K = self.copies
         with torch.cuda.stream(self.stream):
-            for t, v in zip(self.x, state):
-                v = host(v)
-                t.copy_(v, non_blocking=v.is_pinned())
-            for t, v in zip(self.dS, dS):
-                v = host(v)
-                t.copy_(v, non_blocking=v.is_pinned())
+            for j in range(K):
+                state, dS = payloads[j] if j < len(payloads) else payloads[0]
+                for t, v in zip(self.x, state):
+                    v = host(v)
+                    t.view(K, -1)[j].copy_(v.reshape(-1), non_blocking=v.is_pinned())
+                for t, v in zip(self.dS, dS):
+                    if j < len(payloads):
+                        v = host(v)
+                        t.view(K, -1)[j].copy_(v.reshape(-1), non_blocking=v.is_pinned())
+                    else:
+                        t.view(K, -1)[j].zero_()
             for t in self.a:
                 t.zero_()
             self.acc.zero_()
@@ -241,7 +263,7 @@ class Slot(object):
 
 class SensitivityServer(object):
     def __init__(self, precision='fp32', device=0, hbm_budget=40e9, k=10, nPrimal=100, max_slots=48,
-                 library=None):
+                 library=None, batch=None):
         self.precision = precision
         self.device = device
         self.budget = hbm_budget
@@ -252,6 +274,7 @@ class SensitivityServer(object):
         self.slots = []
         self.bytes_of = {}
         self.used = 0
+        self.batch = dict(batch or {})   # mesh key -> requests per launch (batched slots)
         self.evictions = 0          # idle slots released to make room for another mesh's slot
         self.queued = 0             # requests that waited for a slot after they arrived
 
@@ -280,7 +303,7 @@ class SensitivityServer(object):
     def _estimate(self, key):
         if key in self.bytes_of:
             return self.bytes_of[key]
-        m = self.lib.get(key).mesh
+        m = self.lib.get(key, self.batch.get(key, 1)).mesh
         er = 8 if self.precision == 'fp64' else 4      # mesh tables, records, face fluxes
         es = 4 if self.precision == 'fp32' else 8      # states, stages, checkpoints, adjoints
         # per face: tables, flux records, adjoint face records (and FP64 face tapes); per cell:
@@ -307,7 +330,8 @@ class SensitivityServer(object):
             self.used -= victim.bytes()
             victim.rcf.close()
             self.evictions += 1
-        s = Slot(self.lib.get(key), key, self.precision, self.device, self.k, self.nPrimal)
+        K = self.batch.get(key, 1)
+        s = Slot(self.lib.get(key, K), key, self.precision, self.device, self.k, self.nPrimal, copies=K)
         s.capture()
         self.bytes_of[key] = s.bytes()
         self.used += s.bytes()
@@ -335,23 +359,35 @@ class SensitivityServer(object):
                         r._queued = True
                         self.queued += 1
                     break
-                waiting.popleft()
-                state, dS = r.inputs if r.inputs is not None else request_inputs(s.case, r.seed)
-                s.start(r, state, dS)
-                r.t_admit = time.perf_counter() - t0
+                # a batched slot takes the next waiting requests on the same mesh too, up to its
+                # number of copies
+                group = [waiting.popleft()]
+                for q in list(waiting):
+                    if len(group) >= s.copies:
+                        break
+                    if q.key == r.key:
+                        waiting.remove(q)
+                        group.append(q)
+                base = self.lib.get(r.key)
+                payloads = [q.inputs if q.inputs is not None else request_inputs(base, q.seed) for q in group]
+                s.start(group, payloads)
+                for q in group:
+                    q.t_admit = time.perf_counter() - t0
                 active.append(s)
             progressed = False
             for s in active:
                 progressed |= s.advance()
             for s in list(active):
                 if s.finished():
-                    r = s.req
-                    r.sensitivity = float(s.acc.item()) / r.nPrimal
-                    r.t_done = time.perf_counter() - t0
+                    acc = s.acc.cpu().tolist()
+                    for j, r in enumerate(s.reqs):
+                        r.sensitivity = acc[j] / r.nPrimal
+                        r.t_done = time.perf_counter() - t0
+                        done.append(r)
                     s.busy = False
                     s.req = None
+                    s.reqs = []
                     active.remove(s)
-                    done.append(r)
             if not progressed and not active and pending and realtime:
                 time.sleep(max(0.0, min(0.002, pending[0].arrival - (time.perf_counter() - t0))))
         elapsed = time.perf_counter() - t0

@@ -442,7 +442,8 @@ SERVING_KEYS = ['box16', 'box24', 'box32', 'box48', 'box64', 'box96', 'cyl64x32'
 SERVING_LAMBDAS = (1.0, 2.0, 5.0, 10.0, 20.0, 50.0, 100.0, 200.0)
 
 
-def serving_bench(local, lams=SERVING_LAMBDAS, seed=4, n_mix=48, window_s=6.0, precision='fp32', compare='mixed'):
+def serving_bench(local, lams=SERVING_LAMBDAS, seed=4, n_mix=48, window_s=6.0, precision='fp32', compare='mixed',
+                  cell_ns=None):
     """Sensitivity requests, each a jittered periodic box of side 16-96 or a cylinder O-grid
     64x32-256x128 drawn uniformly (seed 4), 100 primal + 100 adjoint steps.
 
@@ -530,7 +531,7 @@ def serving_bench(local, lams=SERVING_LAMBDAS, seed=4, n_mix=48, window_s=6.0, p
             'plain_fp64_req_per_s': round(plain_rate, 3), 'speedup_vs_plain': round(served_rate / plain_rate, 2),
             'served_fp64_req_per_s': round(fp64_rate, 3),
             'batching_gain_fp64': round(fp64_rate / plain_rate, 2),
-            'small_class': small_class_bench(local, lib),
+            'small_class': small_class_bench(local, lib, batch={k: 4 for k in SMALL_KEYS}, cell_ns=cell_ns),
             'plain_seconds_per_request': {k: round(v, 4) for k, v in t_plain.items()},
             'latency_sweep': sweep, 'max_rel_err_vs_fp64': max(errs.values()), 'rel_err_by_mesh': errs,
             'compare': other, 'slots': nslots, 'meshes': keys,
@@ -540,7 +541,7 @@ def serving_bench(local, lams=SERVING_LAMBDAS, seed=4, n_mix=48, window_s=6.0, p
 SMALL_KEYS = ['box16', 'box24', 'box32', 'cyl64x32']
 
 
-def small_class_bench(local, lib, n_req=48, seed=6, precision='fp32'):
+def small_class_bench(local, lib, n_req=48, seed=6, precision='fp32', batch=None, cell_ns=None):
     """The small meshes of the serving mix, where launch and latency costs weigh most: n_req
     requests drawn from box16/24/32 and cyl64x32 served together, against the GPU time the same
     requests' graphs take replayed one request after another on one stream (CUDA events, no
@@ -555,6 +556,19 @@ def small_class_bench(local, lib, n_req=48, seed=6, precision='fp32'):
     srv.warm(ks)
     reqs = serving.prepare([serving.Request(rid=i, key=k, seed=i, nPrimal=100) for i, k in enumerate(ks)], lib)
     st = srv.serve(reqs, realtime=False)
+    batched = None
+    if batch:
+        # the same requests through batched slots: up to K requests on one mesh a launch
+        sb = serving.SensitivityServer(precision=precision, device=local, k=10, nPrimal=100, library=lib,
+                                       hbm_budget=60e9, max_slots=64, batch=batch)
+        sb.warm([k for k in SMALL_KEYS for _ in range(-(-ks.count(k) // batch.get(k, 1)))])
+        rb = serving.prepare([serving.Request(rid=i, key=k, seed=i, nPrimal=100) for i, k in enumerate(ks)], lib)
+        stb = sb.serve(rb, realtime=False)
+        worst = max(abs(a.sensitivity - b.sensitivity) / abs(b.sensitivity) for a, b in zip(rb, reqs))
+        batched = {'batch': batch, 'served_s': round(stb['elapsed_s'], 4),
+                   'served_req_per_s': round(n_req / stb['elapsed_s'], 2), 'slots': len(sb.slots),
+                   'max_rel_diff_vs_unbatched': float('%.3g' % worst)}
+        sb.close()
     # one request's graph replays per mesh, alone on one slot's stream
     per_key = {}
     for key in SMALL_KEYS:
@@ -573,10 +587,17 @@ def small_class_bench(local, lib, n_req=48, seed=6, precision='fp32'):
         per_key[key] = e0.elapsed_time(e1) / 1e3
     srv.close()
     seq = sum(per_key[k] for k in ks)
+    # the kernel-time bound: the requests' cells at the workload box's cost per cell of two
+    # primal steps (run and recompute) and one adjoint step, times the 100 steps
+    bound = None
+    if cell_ns:
+        bound = sum(lib.get(k).mesh.nInternalCells for k in ks) * 100 * cell_ns * 1e-9
     return {'requests': n_req, 'meshes': SMALL_KEYS, 'precision': precision,
+            'kernel_time_bound_s': None if bound is None else round(bound, 4),
+            'bound_over_served': None if bound is None else round(bound / st['elapsed_s'], 3),
             'served_s': round(st['elapsed_s'], 4), 'served_req_per_s': round(n_req / st['elapsed_s'], 2),
             'sequential_graph_s': round(seq, 4), 'served_over_sequential': round(st['elapsed_s'] / seq, 3),
-            'graph_s_per_request': {k: round(v, 5) for k, v in per_key.items()}}
+            'graph_s_per_request': {k: round(v, 5) for k, v in per_key.items()}, 'batched': batched}
 
 
 def run_reference(args):
@@ -659,7 +680,10 @@ def main():
         line['fp32'] = {k: m32[k] for k in ('value', 'ms_per_step', 'primal', 'adjoint', 'roofline', 'step_model',
                                             'kernels', 'adjoint_kernels', 'e2e')}
     if args.serving and rank == 0:
-        line['serving'] = serving_bench(local)
+        cell_ns = None
+        if m32 is not None:
+            cell_ns = (2 * m32['primal']['ms_per_step'] + m32['adjoint']['ms_per_step']) * 1e6 / nIC
+        line['serving'] = serving_bench(local, cell_ns=cell_ns)
     if rank == 0 and args.serving:
         # FP32 / mixed against FP64 on the cylinder over 2000 steps (adfvm_gb300/studies.py)
         from adfvm_gb300.studies import precision_study

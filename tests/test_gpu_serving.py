@@ -79,3 +79,31 @@ def test_admission_under_memory_pressure():
     for r, ref in zip(reqs, alone):
         assert r.sensitivity == ref, (r.rid, r.key, r.sensitivity, ref)
     srv.close()
+
+
+def test_batched_slots_give_each_request_its_own_result():
+    """A batched slot runs up to K requests on one mesh in the same launches (K disjoint copies
+    of the mesh): each request's FP64 sensitivity is bitwise the same whichever copy it runs in,
+    alone or with others, and equals the plain one-at-a-time result within 1e-12."""
+    lib = serving.MeshLibrary()
+    keys = ['box8', 'box8', 'cyl16x8', 'box8', 'cyl16x8']
+    seeds = [21, 22, 23, 24, 25]
+    srv = serving.SensitivityServer(precision='fp64', k=4, nPrimal=8, library=lib, batch={'box8': 3, 'cyl16x8': 2})
+    mix = _reqs(keys, seeds, 8)
+    srv.serve(mix, realtime=False)
+    assert all(s.copies in (2, 3) for s in srv.slots)
+    # the box8 requests ran as one batch (seeds 21, 22, 24 in copies 0, 1, 2): seed 24 alone in
+    # copy 0 (the other copies idle), and in copy 1 of a batch in another order
+    alone = _reqs(['box8'], [24], 8)
+    srv.serve(alone, realtime=False)
+    assert alone[0].sensitivity == mix[3].sensitivity
+    other = _reqs(['box8', 'box8', 'box8'], [22, 24, 21], 8)
+    srv.serve(other, realtime=False)
+    assert other[1].sensitivity == mix[3].sensitivity
+    assert other[2].sensitivity == mix[0].sensitivity
+    assert other[0].sensitivity == mix[1].sensitivity
+    plain = _reqs(keys, seeds, 8)
+    serving.plain_one_at_a_time(plain, lib, nPrimal=8)
+    for a, b in zip(mix, plain):
+        assert abs(a.sensitivity - b.sensitivity) <= 1e-12 * abs(b.sensitivity), (a.key, a.sensitivity, b.sensitivity)
+    srv.close()
