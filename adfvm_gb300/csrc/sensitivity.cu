@@ -167,6 +167,27 @@ extern "C" int afvm_sensitivity_noalloc(int32_t device, int32_t nArrays, const d
         cudaGetLastError();
         return AFVM_ERR_BAD_ARG;
     }
+    // every array must be memory of `device` and the stream a stream of it: a host pointer or
+    // another GPU's memory would make the kernels fault or read the wrong memory
+    for (int k = 0; k < nArrays; k++) {
+        if (n[k] <= 0) continue;
+        const void* ptrs[2] = {grad[k], pert[k]};
+        for (const void* q : ptrs) {
+            cudaPointerAttributes a;
+            if (!q || cudaPointerGetAttributes(&a, q) != cudaSuccess ||
+                (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged) || a.device != device) {
+                cudaGetLastError();
+                return AFVM_ERR_BAD_ARG;
+            }
+        }
+    }
+    if (stream) {
+        int sdev = -1;
+        if (cudaStreamGetDevice((cudaStream_t)stream, &sdev) != cudaSuccess || sdev != device) {
+            cudaGetLastError();
+            return AFVM_ERR_BAD_ARG;
+        }
+    }
     int prev = -1;
     cudaGetDevice(&prev);
     if (prev != device && cudaSetDevice(device) != cudaSuccess) {

@@ -587,14 +587,15 @@ class RCF(object):
         return self._objPrims.clone()
 
     def adjoint_step(self, rho, rhoU, rhoE, dt, seeds, obja=1.0, S=None, out=None, source_grad=True, stages=None,
-                     tape=None, params=None):
+                     tape=None, params=None, source_out=None):
         """VJP of one step on CUDA tensors (see _adjoint_step); with an objective given as a
         torch function, its gradient with respect to the objective-stage primitives - torch
         autograd of the function - is the adjoint seed the kernels add (afvm_set_objective_seed),
         and for params='mesh' the function's own dependence on the mesh tensors (through
         solver.meshTensor) is added to the mesh gradients."""
         if self.objectiveFn is None or obja == 0.0:
-            return self._adjoint_step(rho, rhoU, rhoE, dt, seeds, obja, S, out, source_grad, stages, tape, params)
+            return self._adjoint_step(rho, rhoU, rhoE, dt, seeds, obja, S, out, source_grad, stages, tape, params,
+                                      source_out)
         torch = _torch()
         prims = self._objective_prims(rho, rhoU, rhoE, dt, S, tape).double().detach().requires_grad_(True)
         leaves = {}
@@ -608,7 +609,8 @@ class RCF(object):
         seed = g[0].contiguous()
         L.check(L.lib().afvm_set_objective_seed(self._ctx, C.c_void_p(seed.data_ptr())), self._ctx)
         try:
-            r = self._adjoint_step(rho, rhoU, rhoE, dt, seeds, obja, S, out, source_grad, stages, tape, params)
+            r = self._adjoint_step(rho, rhoU, rhoE, dt, seeds, obja, S, out, source_grad, stages, tape, params,
+                                   source_out)
         finally:
             L.lib().afvm_set_objective_seed(self._ctx, None)
         if params == 'mesh':
@@ -617,7 +619,7 @@ class RCF(object):
         return r
 
     def _adjoint_step(self, rho, rhoU, rhoE, dt, seeds, obja=1.0, S=None, out=None, source_grad=True, stages=None,
-                      tape=None, params=None):
+                      tape=None, params=None, source_out=None):
         """VJP of one step on CUDA tensors (afvm_adjoint_step): the adjoint of the input state
         (and of the sources) given the adjoint seeds of the output state and of the objective.
         dt is held fixed, the CFL-sum output gets no seed (dtca = 0, apps/adjoint.py:268).
@@ -630,7 +632,10 @@ class RCF(object):
         stream = torch.cuda.current_stream(rho.device).cuda_stream
         if out is None:
             out = (torch.empty_like(rho), torch.empty_like(rhoU), torch.empty_like(rhoE))
-        Sg = (torch.empty_like(rho), torch.empty_like(rhoU), torch.empty_like(rhoE)) if source_grad else None
+        Sg = None
+        if source_grad:
+            Sg = tuple(source_out) if source_out is not None else \
+                (torch.empty_like(rho), torch.empty_like(rhoU), torch.empty_like(rhoE))
         Sp = [None, None, None] if S is None else [C.c_void_p(s.data_ptr()) for s in S]
         vp = lambda t: C.c_void_p(t.data_ptr())
         gp = [None, None, None] if Sg is None else [vp(t) for t in Sg]

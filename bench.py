@@ -212,6 +212,7 @@ def cpu_baseline(args, threads, seconds=10.0):
         na += 1
     ta = (time.perf_counter() - t0) / (na * m.nInternalCells)
     return {'value': 1.0 / (tp + ta) / 1e6, 'unit': UNIT, 'cores': threads, 'kind': 'port',
+            'config': describe(case, args.precision),
             'primal': round(1.0 / tp / 1e6, 4), 'adjoint': round(1.0 / ta / 1e6, 4), 'same_mesh': True,
             'sample': '%d FP64 primal steps (C/OpenMP oracle) and %d FP64 adjoint steps (host adjoint, OpenMP) of '
                       '%s (%d cells, the workload mesh, built by the oracle\'s restatement of the reference\'s '
@@ -270,14 +271,15 @@ def measure(case, precision, args, local, dist, world, clocks):
         cnt['p'] = j + 1
 
     abuf = [torch.ones_like(t) * 1e-3 for t in x]
+    sbuf = [torch.empty_like(t) for t in x]          # the source gradient, as the reference returns it
 
     def adjoint():
         q = cnt['a']
         cnt['a'] = q + 1
         j = cnt['p'] - 1 - (q % min(R, cnt['p']))
         xi = ring[j % (R + 1)]
-        rcf.adjoint_step(xi[0], xi[1], xi[2], dt, abuf, obja=1.0, out=abuf, source_grad=False, stages=stg[j % R],
-                         tape=tps[j % R])
+        rcf.adjoint_step(xi[0], xi[1], xi[2], dt, abuf, obja=1.0, out=abuf, stages=stg[j % R], tape=tps[j % R],
+                         source_out=sbuf)
 
     for _ in range(args.warmup):
         primal()
@@ -609,8 +611,9 @@ def run_reference(args):
     line = {'impl': 'reference', 'metric': METRIC, 'value': base['value'], 'unit': UNIT, 'n_gpus': args.gpus,
             'steps': args.steps, 'warmup': args.warmup, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
-            'config': {'workload': args.workload + ' (CPU sample, see cpu_baseline.sample), Roe, SSP-RK3, '
-                                   'Sutherland viscosity, FP64'},
+            # the workload described as the GPU arm describes it (same mesh, same counts); the
+            # sample the CPU timed is in cpu_baseline.sample
+            'config': dict(base.pop('config'), parallelism='host cores (%d threads)' % threads),
             'cpu_baseline': base,
             'e2e': {'value': base['value'], 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
     print(json.dumps(line))
@@ -710,6 +713,7 @@ def main():
             'note': 'issue_frac counts DADD/DMUL/DFMA as one FP64 pipe issue each'}
     if rank == 0 and not args.no_cpu_baseline:
         cb = cpu_baseline(args, os.cpu_count() or 1)
+        cb.pop('config', None)
         line['cpu_baseline'] = cb
         # the GPU's speed-up on the same mesh, FP64 both: primal and adjoint alone and together
         line['vs_cpu_baseline'] = {'primal': round(m64['primal']['value'] / cb['primal'], 2),

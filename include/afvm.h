@@ -413,7 +413,8 @@ int afvm_adjoint_energy(afvm_ctx* ctx, const void* rhoa, const void* rhoUa, cons
  * static device array of the library that holds partial sums for at most
  * AFVM_SENSITIVITY_NOALLOC_MAX_ARRAYS arrays (about 129 KB, kept on every GPU that loads
  * the library until the process exits). nArrays outside 1..that limit, or a device outside
- * the visible ones, is rejected with AFVM_ERR_BAD_ARG. The first call on a device looks up
+ * the visible ones, or an array that is not memory of that device (or a stream of another
+ * device), is rejected with AFVM_ERR_BAD_ARG. The first call on a device looks up
  * the array's device address (cudaGetSymbolAddress) with that device current and caches
  * it, so make that first call before any stream capture; the cached address does not
  * survive cudaDeviceReset. Calls share the array: calls that overlap on the GPU race and

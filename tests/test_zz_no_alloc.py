@@ -86,3 +86,21 @@ def test_noalloc_rejects_no_arrays_and_unknown_devices():
     assert st == L.AFVM_OK
     ref = sum(float((a * b).sum()) for a, b in zip(g, p))
     assert abs(v - ref) <= 1e-12 * sum(float((a * b).abs().sum()) for a, b in zip(g, p))
+
+
+def test_noalloc_rejects_arrays_that_are_not_on_the_device():
+    g, p = _arrays(2, 7)
+    host = np.random.default_rng(8).normal(size=g[1].numel())
+    k = 2
+    ga = (L._d * k)(C.cast(C.c_void_p(g[0].data_ptr()), L._d), host.ctypes.data_as(L._d))
+    pa = (L._d * k)(*[C.cast(C.c_void_p(t.data_ptr()), L._d) for t in p])
+    na = (C.c_int64 * k)(*[t.numel() for t in g])
+    out = C.c_double(float('nan'))
+    st = L.lib().afvm_sensitivity_noalloc(torch.cuda.current_device(), k, ga, pa, na, C.byref(out),
+                                          C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == L.AFVM_ERR_BAD_ARG
+    # the next valid call is unaffected
+    st, v = _noalloc(g, p)
+    assert st == L.AFVM_OK
+    ref = sum(float((a * b).sum()) for a, b in zip(g, p))
+    assert abs(v - ref) <= 1e-12 * sum(float((a * b).abs().sum()) for a, b in zip(g, p))
