@@ -94,6 +94,8 @@ SIGNATURES = {
     'afvm_ctx_precision': (C.c_int, [_v]),
     'afvm_ctx_device_bytes': (C.c_int64, [_v]),
     'afvm_set_bc_value': (C.c_int, [_v, C.c_int32, C.c_int32, _d]),
+    'afvm_set_gauge': (C.c_int, [_v, C.c_double, C.c_double, C.c_double]),
+    'afvm_get_gauge': (C.c_int, [_v, _d]),
     'afvm_set_objective_vane': (C.c_int, [_v, C.POINTER(ObjectiveVane)]),
     'afvm_set_objective_sink': (C.c_int, [_v, _v]),
     'afvm_set_objective_seed': (C.c_int, [_v, _v]),

@@ -54,6 +54,12 @@ __device__ __forceinline__ void adj_face(const MeshDev<R>& m, const Phys& P, con
         face_vjp_t<R>(P, kind, inviscid != 0, in, TapeLoad<R>{tape + f, (size_t)m.nF}, Fb, b);
     } else {
         load_face<R>(m, rec, f, in);
+        if constexpr (kGauge<R>) {
+            // the VJP differentiates the absolute-form flux (the same function of the state as
+            // the gauge form the forward evaluates)
+            in.TP = rec_abs_T<R>(P, in.TP); in.TN = rec_abs_T<R>(P, in.TN);
+            in.pP = rec_abs_p<R>(P, in.pP); in.pN = rec_abs_p<R>(P, in.pN);
+        }
         face_vjp<R>(P, kind, inviscid != 0, in, Fb, b);
     }
     const R* src = &b.UP[0];
@@ -181,7 +187,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const
             // drag = sum (p0 nx - mu(T0) (U0 - U0i)/delta) A, ghost values p0, T0, U0
             const R* rg = rec + (size_t)(m.nIC + g) * REC;
             const R* ro = rec + (size_t)o * REC;
-            double T0 = rg[R_T], U0 = rg[0], U0i = ro[0];
+            double T0 = rec_T<R>(P, rg[R_T]), U0 = rg[0], U0i = ro[0];
             double A = m.area[f], dl = m.dlt[f], nx = m.nrm[f];
             double mu = viscosity<double>(P, T0);
             double dmu = (P.muModel == AFVM_MU_SUTHERLAND) ? mu * (1.5 / T0 - 1.0 / (T0 + P.muTs)) : 0.0;
@@ -202,7 +208,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const
             R kap = consts<R>(P).ggm1;
             R Unb = dot3(gp, d) - gp[R_T] * Un / consts<R>(P).Cp;
             for (int k = 0; k < 3; k++) pbar[k] += Unb * d[k];
-            pbar[R_T] += gp[R_P] * pt * kap * pow(rs[R_T] / Tt, kap - R(1)) / Tt;
+            pbar[R_T] += gp[R_P] * pt * kap * pow(rec_abs_T<R>(P, rs[R_T]) / Tt, kap - R(1)) / Tt;
             continue;
         }
         if (kU == GK_COPY) {
@@ -222,7 +228,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const
     if (STAGE == 1 && objective != AFVM_OBJ_NONE) {
         const R* rc = rec + (size_t)c * REC;
         if (objective == AFVM_OBJ_KINETIC_ENERGY) {
-            double U[3] = {rc[0], rc[1], rc[2]}, T = rc[R_T], p = rc[R_P], V = m.vol[c];
+            double U[3] = {rc[0], rc[1], rc[2]}, T = rec_T<R>(P, rc[R_T]), p = rec_p<R>(P, rc[R_P]), V = m.vol[c];
             double d = (P.Cv * T) * P.gm1;
             double rho = p / d;
             double q = U[0] * U[0] + U[1] * U[1] + U[2] * U[2];
@@ -236,7 +242,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const
             if (q >= 0) {
                 double g5[5] = {0, 0, 0, 0, 0};
                 double U[3] = {rc[0], rc[1], rc[2]};
-                vane_cell_grad(P, vane, U, (double)rc[R_T], (double)rc[R_P], vane.planeArea[q], vane.sums[0],
+                vane_cell_grad(P, vane, U, rec_T<R>(P, rc[R_T]), rec_p<R>(P, rc[R_P]), vane.planeArea[q], vane.sums[0],
                                vane.sums[1], obja, g5);
                 for (int k = 0; k < 5; k++) pbar[k] += (R)g5[k];
             }
@@ -253,7 +259,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const
                 int e = m.accf[s * n + c];
                 if (e < objStart || e >= objStart + objN) continue;   // owner-side faces of the patch
                 const R* rg = rec + (size_t)m.nbr[e] * REC;
-                double T0 = rg[R_T];
+                double T0 = rec_T<R>(P, rg[R_T]);
                 double mu = viscosity<double>(P, T0);
                 pbar[0] += (R)(obja * mu / (double)m.dlt[e] * (double)m.area[e]);
             }

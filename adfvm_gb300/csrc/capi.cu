@@ -464,6 +464,51 @@ int get_results(Ctx* c, double* dtc_out, double* obj_out, cudaStream_t s) {
 }  // namespace
 }  // namespace afvm
 
+namespace afvm {
+
+// The gauge state of FP32 records (Phys): p, T and H rounded to floats, so that the FP32 face
+// arithmetic holds exactly the values the records' offsets and the update's energy correction
+// use (with float-exact Cp and T, H - Cp T is then exact as well).
+static void set_gauge(Phys& P, double p, double T, double H) {
+    P.gaugeP = (double)(float)p;
+    P.gaugeT = (double)(float)T;
+    P.gaugeH = (double)(float)H;
+    finish_phys(P);
+}
+
+// the default gauge state: the mean fixed boundary pressure and temperature (the totals of
+// CBC_TOTAL_PT patches) and the mean of Cp T + |U|^2/2 over the ghosts with fixed U and T (Cp T
+// without any); zero where the boundary conditions fix none (a periodic box)
+static void derive_gauge(const HostTables& h, Phys& P) {
+    const size_t nG = h.gkind.size();
+    double sp = 0, sT = 0, sH = 0;
+    size_t np = 0, nT = 0, nH = 0;
+    for (size_t g = 0; g < nG; g++) {
+        int kind = h.gkind[g];
+        int kU = kind & 7, kT = (kind >> 3) & 7, kp = (kind >> 6) & 7;
+        double T = h.gval[3 * nG + g], p = h.gval[4 * nG + g];
+        if (kU == GK_TOTALPT) {
+            sT += T; nT++;
+            sp += p; np++;
+            sH += P.Cp * T; nH++;
+            continue;
+        }
+        if (kT == GK_FIXED) {
+            sT += T; nT++;
+            if (kU == GK_FIXED) {
+                double q = 0;
+                for (int k = 0; k < 3; k++) q += h.gval[k * nG + g] * h.gval[k * nG + g];
+                sH += P.Cp * T + 0.5 * q; nH++;
+            }
+        }
+        if (kp == GK_FIXED) { sp += p; np++; }
+    }
+    double gp = np ? sp / np : 0.0, gT = nT ? sT / nT : 0.0;
+    set_gauge(P, gp, gT, nH ? sH / nH : P.Cp * gT);
+}
+
+}  // namespace afvm
+
 using namespace afvm;
 
 extern "C" {
@@ -508,6 +553,7 @@ int afvm_ctx_create(const afvm_mesh_tensors* mesh, const afvm_patch_bc* bcs, con
     DeviceGuard dg(device);
     HostTables h;
     int st = build_tables(c, mesh, bcs, h);
+    if (!st) derive_gauge(h, P);
     if (!st) st = (precision == AFVM_FP64) ? upload_mesh<double>(c, h, c->m64) : upload_mesh<float>(c, h, c->m32);
     if (!st)
         st = dispatch(c, [&](auto r, auto sv) { return alloc_work<decltype(r), decltype(sv)>(c); });
@@ -581,6 +627,22 @@ int afvm_set_objective_sink(afvm_ctx* ctx, void* prims) {
     if (!ctx) return AFVM_ERR_BAD_ARG;
     Ctx* c = reinterpret_cast<Ctx*>(ctx);
     c->objSink = prims;
+    return AFVM_OK;
+}
+
+int afvm_set_gauge(afvm_ctx* ctx, double p, double T, double H) {
+    if (!ctx) return AFVM_ERR_BAD_ARG;
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!std::isfinite(p) || !std::isfinite(T) || !std::isfinite(H))
+        return fail(c, AFVM_ERR_BAD_ARG, "afvm_set_gauge: the gauge state must be finite");
+    set_gauge(c->phys, p, T, H);
+    return AFVM_OK;
+}
+
+int afvm_get_gauge(const afvm_ctx* ctx, double* pTH) {
+    if (!ctx || !pTH) return AFVM_ERR_BAD_ARG;
+    const Phys& P = reinterpret_cast<const Ctx*>(ctx)->phys;
+    pTH[0] = P.gaugeP; pTH[1] = P.gaugeT; pTH[2] = P.gaugeH;
     return AFVM_OK;
 }
 
@@ -973,9 +1035,14 @@ int afvm_boundary_values(afvm_ctx* ctx, const void* rho, const void* rhoU, const
         launch_prim<R, S>(c, (const S*)rho, (const S*)rhoU, (const S*)rhoE, s);
         return 0;
     });
-    // ghost rows of the cell record, columns U, T, p
+    // ghost rows of the cell record, columns U, T, p (FP32 records: the gauge offsets of T and p
+    // made absolute)
     const char* src = (const char*)c->rec + es * REC * (size_t)c->nIC;
-    cudaError_t e = cudaMemcpy2DAsync(out, es * 5, src, es * REC, es * 5, (size_t)c->nG, cudaMemcpyDeviceToDevice, s);
+    cudaError_t e = cudaSuccess;
+    if (c->precision == AFVM_FP64)
+        e = cudaMemcpy2DAsync(out, es * 5, src, es * REC, es * 5, (size_t)c->nG, cudaMemcpyDeviceToDevice, s);
+    else
+        launch_abs_prims(c, (const float*)src, REC, c->nG, (float*)out, s);
     if (e != cudaSuccess) return cuda_fail(c, e, "boundary values copy");
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(c, e, "boundary values launch");

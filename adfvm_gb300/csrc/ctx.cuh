@@ -287,6 +287,10 @@ int host_copy(int32_t device, void* dst, int32_t dstBytes, const void* src, int3
               void* stream, bool toDevice, bool syncPinned);
 static inline int nblocks(long long n) { return (int)((n + BLOCK - 1) / BLOCK); }
 
+// rows of U (3), T, p with absolute T and p from FP32 records (stride values apart), which
+// hold the gauge offsets of T and p
+void launch_abs_prims(const Ctx* c, const float* rec, int stride, int n, float* out, cudaStream_t s);
+
 template <typename R> inline const MeshDev<R>& meshOf(const Ctx* c);
 template <> inline const MeshDev<double>& meshOf<double>(const Ctx* c) { return c->m64; }
 template <> inline const MeshDev<float>& meshOf<float>(const Ctx* c) { return c->m32; }

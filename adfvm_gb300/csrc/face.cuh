@@ -52,11 +52,73 @@ AFVM_HD void zero_geo(GeoBar<R>& g) {
 template <typename R>
 AFVM_HD R sgn(R x) { return (x > R(0)) ? R(1) : ((x < R(0)) ? R(-1) : R(0)); }
 
+// the gauge-form face flux: as face_flux below, from gauge offsets of p and T (the viscous
+// terms use T only through differences and mu(T_F), T_F absolute)
+template <typename R>
+AFVM_HD void face_flux_gauge(const Phys& P, int kind, bool inviscid, const FaceIn<R>& in, R* F, R& maxaF) {
+    const PhysR<R>& Q = consts<R>(P);
+    R TF, UF[3], gTF[3], gUF[9];
+    if (kind == FACE_BOUNDARY) {
+        // RCF.boundaryFlux: (rho Un, rho U Un + p N, rho h Un) less gP N and gH rho Un
+        R rho, rhoU[3], rhoE;
+        conservative<R>(P, in.UN, in.TN + Q.gT, in.pN + Q.gP, rho, rhoU, rhoE);
+        R Un = dot3(in.UN, in.N);
+        R hg = Q.Cp * in.TN + (R(0.5) * dot3(in.UN, in.UN) - Q.gK);
+        F[0] = rho * Un;
+        for (int k = 0; k < 3; k++) F[1 + k] = rhoU[k] * Un + in.pN * in.N[k];
+        F[4] = rho * hg * Un;
+        TF = in.TN + Q.gT;
+        for (int k = 0; k < 3; k++) { UF[k] = in.UN[k]; gTF[k] = in.gTN[k]; }
+        for (int k = 0; k < 9; k++) gUF[k] = in.gUN[k];
+    } else {
+        R ULF[3], TLF, pLF, URF[3], TRF, pRF;
+        for (int k = 0; k < 3; k++) ULF[k] = recon<R>(in.UP[k], in.UN[k], in.gUP + 3 * k, in.lw0, in.qw0);
+        TLF = recon<R>(in.TP, in.TN, in.gTP, in.lw0, in.qw0);
+        pLF = recon<R>(in.pP, in.pN, in.gpP, in.lw0, in.qw0);
+        R rhoL, rhoUL[3], rhoEL, rdL, rdR;
+        conservative<R>(P, ULF, TLF + Q.gT, pLF + Q.gP, rhoL, rhoUL, rhoEL, &rdL);
+        int solver;
+        if (kind == FACE_CHARACTERISTIC) {
+            for (int k = 0; k < 3; k++) URF[k] = in.UN[k];
+            TRF = in.TN; pRF = in.pN;
+            solver = P.briemann;
+        } else {
+            for (int k = 0; k < 3; k++) URF[k] = recon<R>(in.UN[k], in.UP[k], in.gUN + 3 * k, in.lw1, in.qw1);
+            TRF = recon<R>(in.TN, in.TP, in.gTN, in.lw1, in.qw1);
+            pRF = recon<R>(in.pN, in.pP, in.gpN, in.lw1, in.qw1);
+            solver = P.riemann;
+        }
+        R rhoR, rhoUR[3], rhoER;
+        conservative<R>(P, URF, TRF + Q.gT, pRF + Q.gP, rhoR, rhoUR, rhoER, &rdR);
+        if (solver == AFVM_RIEMANN_ROE)
+            roe_gauge<R>(P, pLF, pRF, TLF, TRF, ULF, URF, rhoL, rhoR, rdL, rdR, in.N, F);
+        else
+            laxf_gauge<R>(P, pLF, pRF, TLF, TRF, ULF, URF, rhoL, rhoR, rdL, rdR, in.N, F);
+        if (kind == FACE_CHARACTERISTIC) {
+            TF = in.TN + Q.gT;
+            for (int k = 0; k < 3; k++) { UF[k] = in.UN[k]; gTF[k] = in.gTN[k]; }
+            for (int k = 0; k < 9; k++) gUF[k] = in.gUN[k];
+        } else {
+            TF = R(0.5) * (TLF + TRF) + Q.gT;
+            for (int k = 0; k < 3; k++) { UF[k] = R(0.5) * (ULF[k] + URF[k]); gTF[k] = R(0.5) * (in.gTP[k] + in.gTN[k]); }
+            for (int k = 0; k < 9; k++) gUF[k] = R(0.5) * (in.gUP[k] + in.gUN[k]);
+        }
+    }
+    if (!inviscid) viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, UF, gTF, gUF, in.D, in.N, in.rdelta, F);
+    R aF = sqrt_(Q.Cp * TF * Q.gm1);
+    maxaF = fabs(dot3(UF, in.N)) + aF;
+}
+
 // flux (rho, rhoU, rhoE) through the face and the CFL term |U.n| + a; the tape values of a
-// non-boundary face go to tp
-template <typename R, typename Sink = TapeNone>
+// non-boundary face go to tp. GAUGE: the pressures and temperatures of `in` are gauge offsets
+// (FP32 records) and F is the gauge-form flux (physics.cuh: roe_gauge); never taped.
+template <typename R, bool GAUGE = false, typename Sink = TapeNone>
 AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& in, R* F, R& maxaF,
                        Sink&& tp = Sink()) {
+    if constexpr (GAUGE) {
+        face_flux_gauge<R>(P, kind, inviscid, in, F, maxaF);
+        return;
+    }
     R TF, UF[3], gTF[3], gUF[9];
     if (kind == FACE_BOUNDARY) {
         // RCF.boundaryFlux (density.py:307-331) with RCF.getFlux (density.py:184-190)

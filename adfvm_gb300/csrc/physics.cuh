@@ -5,6 +5,7 @@
 // reference to rounding, not bit for bit.
 #pragma once
 #include <stdint.h>
+#include <type_traits>
 #include "afvm.h"
 
 // The face physics is written once for the device and, for the unit tests of the hand-derived
@@ -76,24 +77,55 @@ struct TapeLocal {
 };
 
 // the gas constants in the working precision, so that the templated physics issues no FP64
-// conversion or division in FP32 (ggm1 = gamma/(gamma-1))
+// conversion or division in FP32 (ggm1 = gamma/(gamma-1), Rg = Cv (gamma-1) the gas constant,
+// gRg = gamma Rg, rgm1 = 1/(gamma-1)); gP, gT, gH, gK: the gauge state of FP32 records (below)
 template <typename R>
 struct PhysR {
     R gamma, gm1, ggm1, Cp, Cv, rCv, kFac, mu0, muAs, muTs, small;
+    R Rg, gRg, rgm1;
+    R gP, gT, gH, gK;
 };
 
+// FP32 cell records hold the pressure and temperature as offsets from a gauge state,
+// p - gaugeP and T - gaugeT, and the FP32 face fluxes carry the momentum flux without
+// gaugeP N and the energy flux less gaugeH times the mass flux (the update adds gaugeH times
+// the mass residual back; gaugeP N sums to zero over the faces of a closed cell, whose face
+// area vectors sum to zero). In a low-Mach flow the pressure (1e5 Pa) varies by ~1e2 Pa: a
+// float holding p keeps four digits of those variations, a float holding p - gaugeP keeps all
+// seven, and the face sums no longer round values 1e3 times larger than their result. FP64
+// records hold the absolute values (gauge unused).
 struct Phys {
     double gamma, gm1, Cp, Cv, rCv, kFac, mu0, muAs, muTs, small;
     int muModel, riemann, briemann;
+    double gaugeP = 0.0, gaugeT = 0.0, gaugeH = 0.0;
     PhysR<double> d;
     PhysR<float> f;
 };
+
+// the record types that hold gauge offsets
+template <typename R>
+constexpr bool kGauge = std::is_same<R, float>::value;
+
+// a record's temperature / pressure as an absolute value: in double (objectives, adjoint
+// viscosity) and in the record type (face VJP inputs, boundary transposes)
+template <typename R>
+AFVM_HD double rec_T(const Phys& P, R v) {
+    if constexpr (kGauge<R>) return (double)v + P.gaugeT;
+    else return (double)v;
+}
+template <typename R>
+AFVM_HD double rec_p(const Phys& P, R v) {
+    if constexpr (kGauge<R>) return (double)v + P.gaugeP;
+    else return (double)v;
+}
 
 template <typename R>
 inline void fill_consts(const Phys& P, PhysR<R>& q) {
     q.gamma = R(P.gamma); q.gm1 = R(P.gm1); q.ggm1 = R(P.gamma / P.gm1); q.Cp = R(P.Cp); q.Cv = R(P.Cv);
     q.rCv = R(P.rCv); q.kFac = R(P.kFac); q.mu0 = R(P.mu0); q.muAs = R(P.muAs); q.muTs = R(P.muTs);
     q.small = R(P.small);
+    q.Rg = R(P.Cv * P.gm1); q.gRg = R(P.gamma * P.Cv * P.gm1); q.rgm1 = R(1.0 / P.gm1);
+    q.gP = R(P.gaugeP); q.gT = R(P.gaugeT); q.gH = R(P.gaugeH); q.gK = R(P.gaugeH - P.Cp * P.gaugeT);
 }
 
 // host: derive the working-precision copies once the double fields are set
@@ -108,6 +140,17 @@ template <>
 AFVM_HD const PhysR<double>& consts<double>(const Phys& P) { return P.d; }
 template <>
 AFVM_HD const PhysR<float>& consts<float>(const Phys& P) { return P.f; }
+
+template <typename R>
+AFVM_HD R rec_abs_T(const Phys& P, R v) {
+    if constexpr (kGauge<R>) return v + consts<R>(P).gT;
+    else return v;
+}
+template <typename R>
+AFVM_HD R rec_abs_p(const Phys& P, R v) {
+    if constexpr (kGauge<R>) return v + consts<R>(P).gP;
+    else return v;
+}
 
 template <typename R>
 AFVM_HD R dot3(const R* a, const R* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
@@ -332,6 +375,110 @@ AFVM_HD void laxf(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R
     for (int k = 0; k < 3; k++)
         F[1 + k] = R(0.5) * (rhoUL[k] * UnL + rhoUR[k] * UnR + (pL + pR) * N[k]) - ha * (rhoUR[k] - rhoUL[k]);
     F[4] = R(0.5) * ((rhoEL + pL) * UnL + (rhoER + pR) * UnR) - ha * (rhoER - rhoEL);
+}
+
+// ---- gauge forms of the Riemann fluxes (FP32 records; the gauge state is in PhysR)
+//
+// Inputs: the face states with pressure and temperature as gauge offsets (pg = p - gP,
+// Tg = T - gT), the densities and 1/(Rg T) of conservative(). Output: eulerRoe's /
+// eulerLaxFriedrichs's flux F with gP N taken out of F[1..3] and gH F[0] out of F[4]. The jumps
+// of rho, rho U and rho E are formed from the gauge offsets and the velocity jump instead of as
+// differences of the two sides' values (rho ~ 1 with 1e-3 variations, rho E ~ 2.5e5 with ~1e2):
+//   rhoR - rhoL = (pR TL - pL TR) / (Rg TL TR),
+//     pR TL - pL TR = (pgR - pgL) gT + pgR TgL - pgL TgR + gP (TgL - TgR)
+//   rhoR UR - rhoL UL = rhoR (UR - UL) + (rhoR - rhoL) UL
+//   rhoER - rhoEL = (pgR - pgL)/(g-1) + (rhoR (qR - qL) + (rhoR - rhoL) qL)/2,  q = |U|^2
+// and the enthalpies as h - gH = Cp Tg + q/2 - gK (gK = gH - Cp gT). In exact arithmetic the
+// flux is the reference's minus those two terms.
+template <typename R>
+struct GaugeJumps {
+    R drho, dU[3], drhoE, drhoEg, hLg, hRg;
+};
+
+template <typename R>
+AFVM_HD void gauge_jumps(const PhysR<R>& Q, R pgL, R pgR, R TgL, R TgR, const R* UL, const R* UR, R rhoL, R rhoR,
+                         R rdL, R rdR, GaugeJumps<R>& j) {
+    R num = (pgR - pgL) * Q.gT + (pgR * TgL - pgL * TgR) + Q.gP * (TgL - TgR);
+    j.drho = num * ((rdL * rdR) * Q.Rg);
+    R dUv[3];
+    for (int k = 0; k < 3; k++) dUv[k] = UR[k] - UL[k];
+    for (int k = 0; k < 3; k++) j.dU[k] = rhoR * dUv[k] + j.drho * UL[k];
+    R qL = dot3(UL, UL), qR = dot3(UR, UR);
+    R dq = dUv[0] * (UR[0] + UL[0]) + dUv[1] * (UR[1] + UL[1]) + dUv[2] * (UR[2] + UL[2]);
+    j.drhoE = (pgR - pgL) * Q.rgm1 + R(0.5) * (rhoR * dq + j.drho * qL);
+    j.drhoEg = j.drhoE - Q.gH * j.drho;
+    j.hLg = Q.Cp * TgL + (R(0.5) * qL - Q.gK);
+    j.hRg = Q.Cp * TgR + (R(0.5) * qR - Q.gK);
+}
+
+// riemann.eulerRoe (adFVM/riemann.py:21-70) in gauge form
+template <typename R>
+AFVM_HD void roe_gauge(const Phys& P, R pgL, R pgR, R TgL, R TgR, const R* UL, const R* UR, R rhoL, R rhoR, R rdL,
+                       R rdR, const R* N, R* F) {
+    const PhysR<R>& Q = consts<R>(P);
+    const R gm1 = Q.gm1;
+    GaugeJumps<R> j;
+    gauge_jumps<R>(Q, pgL, pgR, TgL, TgR, UL, UR, rhoL, rhoR, rdL, rdR, j);
+    R UnL = dot3(UL, N), UnR = dot3(UR, N);
+    R rhoUnL = rhoL * UnL, rhoUnR = rhoR * UnR;
+    R fr = R(0.5) * (rhoUnL + rhoUnR);
+    R pgLR = pgL + pgR;
+    R fu[3], UF[3];
+    for (int k = 0; k < 3; k++) fu[k] = R(0.5) * (rhoUnL * UL[k] + rhoUnR * UR[k] + pgLR * N[k]);
+    R fe = R(0.5) * (rhoUnL * j.hLg + rhoUnR * j.hRg);
+    R rsL = rsqrt_(rhoL), rsR = rsqrt_(rhoR);
+    R sL = rhoL * rsL, sR = rhoR * rsR;
+    R rD = rcp(sL + sR);
+    for (int k = 0; k < 3; k++) UF[k] = (UL[k] * sL + UR[k] * sR) * rD;
+    R hFg = (j.hLg * sL + j.hRg * sR) * rD;
+    R qF = R(0.5) * dot3(UF, UF);
+    R a2F = gm1 * (Q.gH + (hFg - qF));
+    R raF = rsqrt_(a2F);
+    R aF = a2F * raF;
+    R ra2F = raF * raF;
+    R UnF = dot3(UF, N);
+    R lam1 = fabs(UnF), lam2 = fabs(UnF + aF), lam3 = fabs(UnF - aF);
+    // sound speeds sqrt(g p / rho) = sqrt(g Rg T)
+    R c2L = Q.gRg * (TgL + Q.gT), c2R = Q.gRg * (TgR + Q.gT);
+    R cL = sqrt_(c2L), cR = sqrt_(c2R);
+    R eps = R(0.5) * fabs(UnL - UnR);
+    eps = eps + R(0.5) * fabs(cL - cR);
+    eps = (eps < R(0)) ? eps - Q.small : eps + Q.small;
+    R eps2 = R(2) * eps;
+    if (lam1 < eps2 || lam2 < eps2 || lam3 < eps2) {
+        R re = rcp(eps);
+        if (lam1 < eps2) lam1 = R(0.25) * lam1 * lam1 * re + eps;
+        if (lam2 < eps2) lam2 = R(0.25) * lam2 * lam2 * re + eps;
+        if (lam3 < eps2) lam3 = R(0.25) * lam3 * lam3 * re + eps;
+    }
+    R abv1 = R(0.5) * (lam2 + lam3);
+    R abv2 = R(0.5) * (lam2 - lam3);
+    R abv3 = abv1 - lam1;
+    R abv4 = gm1 * (qF * j.drho - dot3(UF, j.dU) + j.drhoE);
+    R abv5 = UnF * j.drho - dot3(j.dU, N);
+    R abv6 = abv3 * abv4 * ra2F - abv2 * abv5 * raF;
+    R abv7 = abv3 * abv5 - abv2 * abv4 * raF;
+    F[0] = fr - R(0.5) * (lam1 * j.drho + abv6);
+    for (int k = 0; k < 3; k++) F[1 + k] = fu[k] - R(0.5) * (lam1 * j.dU[k] + UF[k] * abv6 - abv7 * N[k]);
+    F[4] = fe - R(0.5) * (lam1 * j.drhoEg + hFg * abv6 - UnF * abv7);
+}
+
+// riemann.eulerLaxFriedrichs (adFVM/riemann.py:6-18) in gauge form
+template <typename R>
+AFVM_HD void laxf_gauge(const Phys& P, R pgL, R pgR, R TgL, R TgR, const R* UL, const R* UR, R rhoL, R rhoR, R rdL,
+                        R rdR, const R* N, R* F) {
+    const PhysR<R>& Q = consts<R>(P);
+    GaugeJumps<R> j;
+    gauge_jumps<R>(Q, pgL, pgR, TgL, TgR, UL, UR, rhoL, rhoR, rdL, rdR, j);
+    R UnL = dot3(UL, N), UnR = dot3(UR, N);
+    R cL = sqrt_(Q.gRg * (TgL + Q.gT)), cR = sqrt_(Q.gRg * (TgR + Q.gT));
+    R aF = fmax(fabs(UnL) + cL, fabs(UnR) + cR);
+    R ha = R(0.5) * aF;
+    R pgLR = pgL + pgR;
+    F[0] = R(0.5) * (rhoL * UnL + rhoR * UnR) - ha * j.drho;
+    for (int k = 0; k < 3; k++)
+        F[1 + k] = R(0.5) * (rhoL * UL[k] * UnL + rhoR * UR[k] * UnR + pgLR * N[k]) - ha * j.dU[k];
+    F[4] = R(0.5) * (rhoL * j.hLg * UnL + rhoR * j.hRg * UnR) - ha * j.drhoEg;
 }
 
 // RCF.viscousFlux (adFVM/density.py:192-222): adds -sigma to F[1..3] and -(q + sigma.UF) to F[4];

@@ -42,8 +42,8 @@ __device__ __noinline__ void primitive_f(const Phys& P, float rho, float r0, flo
     out[0] = r0 * rr; out[1] = r1 * rr; out[2] = r2 * rr;
     double q = (double)r0 * r0 + (double)r1 * r1 + (double)r2 * r2;
     double rhoe = (double)rhoE - 0.5 * q * (double)rr;
-    out[4] = (float)(P.gm1 * rhoe);
-    out[3] = (float)(rhoe * (double)rr * P.rCv);
+    out[4] = (float)(P.gm1 * rhoe - P.gaugeP);
+    out[3] = (float)(rhoe * (double)rr * P.rCv - P.gaugeT);
 }
 
 // primitives of one state (element type S) into the record type R
@@ -55,11 +55,14 @@ __device__ __forceinline__ void prim_values(const Phys& P, float r, float u0, fl
                                             float* out) {
     primitive_f(P, r, u0, u1, u2, e, out);
 }
-// FP64 state, FP32 record: the primitives in double, then rounded once
+// FP64 state, FP32 record: the primitives in double, the gauge offsets of T and p taken in
+// double, then rounded once
 __device__ __forceinline__ void prim_values(const Phys& P, double r, double u0, double u1, double u2, double e,
                                             float* out) {
     double v[5];
     primitive_d(P, r, u0, u1, u2, e, v);
+    v[3] -= P.gaugeT;
+    v[4] -= P.gaugeP;
     for (int k = 0; k < 5; k++) out[k] = (float)v[k];
 }
 
@@ -82,21 +85,27 @@ __device__ __forceinline__ void store_prims(double* r, const double* v) {
 }
 
 // ghost cell g's primitives from its source cell's (v, replaced in place): the boundary
-// conditions of BCs.py:62-184
+// conditions of BCs.py:62-184 (FP32 records: T and p as gauge offsets, so a zero-gradient
+// ghost keeps its source's bits)
 template <typename R>
 __device__ __forceinline__ void ghost_prims(const MeshDev<R>& m, const Phys& P, int g, R* v) {
     int kind = m.gkind[g];
     int kU = kind & 7, kT = (kind >> 3) & 7, kp = (kind >> 6) & 7;
+    const R gT = kGauge<R> ? consts<R>(P).gT : R(0), gP = kGauge<R> ? consts<R>(P).gP : R(0);
     if (kU == GK_TOTALPT) {
         // CBC_TOTAL_PT (BCs.py:178-184): Un = U.d, Ub = Un d, Tb = Tt - Un^2/(2 Cp),
         // pb = pt (T/Tt)^(gamma/(gamma-1)) with U, T of the owner cell
         R d[3] = {m.gval[g], m.gval[(size_t)m.nG + g], m.gval[2 * (size_t)m.nG + g]};
         R Tt = m.gval[3 * (size_t)m.nG + g], pt = m.gval[4 * (size_t)m.nG + g];
         R Un = dot3(v, d);
-        R T = v[3];
+        R T = kGauge<R> ? v[3] + gT : v[3];
         for (int k = 0; k < 3; k++) v[k] = Un * d[k];
         v[3] = Tt - R(0.5) * Un * Un / consts<R>(P).Cp;
         v[4] = pt * pow(T / Tt, consts<R>(P).ggm1);
+        if constexpr (kGauge<R>) {
+            v[3] = v[3] - gT;
+            v[4] = v[4] - gP;
+        }
         return;
     }
     if (kU == GK_FIXED) {
@@ -107,8 +116,8 @@ __device__ __forceinline__ void ghost_prims(const MeshDev<R>& m, const Phys& P, 
         R un = dot3(v, n);
         for (int k = 0; k < 3; k++) v[k] = v[k] - un * n[k];
     }
-    if (kT == GK_FIXED) v[3] = m.gval[3 * (size_t)m.nG + g];
-    if (kp == GK_FIXED) v[4] = m.gval[4 * (size_t)m.nG + g];
+    if (kT == GK_FIXED) v[3] = kGauge<R> ? m.gval[3 * (size_t)m.nG + g] - gT : m.gval[3 * (size_t)m.nG + g];
+    if (kp == GK_FIXED) v[4] = kGauge<R> ? m.gval[4 * (size_t)m.nG + g] - gP : m.gval[4 * (size_t)m.nG + g];
 }
 
 template <typename R, typename S>
@@ -193,10 +202,12 @@ __global__ void __launch_bounds__(FLUX_BLOCK, sizeof(R) == 8 ? 3 : 8) k_flux(Mes
     FaceIn<R> in;
     load_face<R>(m, rec, f, in);
     R F[5], maxaF;
-    if (TAPED)
+    // (FP32 records hold gauge offsets and their fluxes are the gauge form; only FP64
+    // contexts keep face tapes)
+    if constexpr (TAPED && !kGauge<R>)
         face_flux<R>(P, kind, inviscid != 0, in, F, maxaF, TapeStore<R>{tape + f, (size_t)m.nF});
     else
-        face_flux<R>(P, kind, inviscid != 0, in, F, maxaF);
+        face_flux<R, kGauge<R>>(P, kind, inviscid != 0, in, F, maxaF);
     R* out = fflux + (size_t)f * FREC;
     for (int k = 0; k < 5; k++) out[k] = F[k];
     out[5] = CFL ? maxaF : R(0);
@@ -254,20 +265,25 @@ __global__ void __launch_bounds__(BLOCK) k_update(MeshDev<R> m, const R* __restr
             }
             dtc = dtc + F[5] * w;
         }
+        S rs[5];
+        for (int q = 0; q < 5; q++) rs[q] = S(res[q]);
+        // gauge-form fluxes (FP32): the energy residual is the gathered one plus gaugeH times
+        // the mass residual, added in the state's type
+        if constexpr (kGauge<R>) rs[4] = rs[4] + S(P.gaugeH) * rs[0];
         S Sv[5] = {Sr[c], Su[3 * c], Su[3 * c + 1], Su[3 * c + 2], Se[c]};
         S a[5] = {u0r[c], u0u[3 * c], u0u[3 * c + 1], u0u[3 * c + 2], u0e[c]};
         S o[5];
         const S rdt = S(dtp ? *dtp : dtv);
         if (STAGE == 0) {
-            for (int q = 0; q < 5; q++) o[q] = a[q] + (S(-1.0) * (S(res[q]) - Sv[q])) * rdt;
+            for (int q = 0; q < 5; q++) o[q] = a[q] + (S(-1.0) * (rs[q] - Sv[q])) * rdt;
         } else if (STAGE == 1) {
             S b[5] = {u1r[c], u1u[3 * c], u1u[3 * c + 1], u1u[3 * c + 2], u1e[c]};
             for (int q = 0; q < 5; q++)
-                o[q] = (S(3. / 4) * a[q] + S(1. / 4) * b[q]) + (S(-(1. / 4)) * (S(res[q]) - Sv[q])) * rdt;
+                o[q] = (S(3. / 4) * a[q] + S(1. / 4) * b[q]) + (S(-(1. / 4)) * (rs[q] - Sv[q])) * rdt;
         } else {
             S b[5] = {u2r[c], u2u[3 * c], u2u[3 * c + 1], u2u[3 * c + 2], u2e[c]};
             for (int q = 0; q < 5; q++)
-                o[q] = (S(1. / 3) * a[q] + S(2. / 3) * b[q]) + (S(-(2. / 3)) * (S(res[q]) - Sv[q])) * rdt;
+                o[q] = (S(1. / 3) * a[q] + S(2. / 3) * b[q]) + (S(-(2. / 3)) * (rs[q] - Sv[q])) * rdt;
         }
         outr[c] = o[0];
         outu[3 * c] = o[1]; outu[3 * c + 1] = o[2]; outu[3 * c + 2] = o[3];
@@ -305,6 +321,23 @@ __global__ void __launch_bounds__(BLOCK) k_update(MeshDev<R> m, const R* __restr
     }
 }
 
+// rows of U (3), T, p with absolute T and p from records of stride `stride` (FP32 records hold
+// gauge offsets) into out (n x 5)
+template <typename R>
+__global__ void __launch_bounds__(BLOCK) k_abs_prims(const R* __restrict__ rec, int stride, int n, Phys P,
+                                                     R* __restrict__ out) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const R* r = rec + (size_t)t * stride;
+    R* o = out + (size_t)t * 5;
+    o[0] = r[0]; o[1] = r[1]; o[2] = r[2];
+    o[3] = rec_abs_T<R>(P, r[3]);
+    o[4] = rec_abs_p<R>(P, r[4]);
+}
+void launch_abs_prims(const Ctx* c, const float* rec, int stride, int n, float* out, cudaStream_t s) {
+    if (n > 0) k_abs_prims<float><<<nblocks(n), BLOCK, 0, s>>>(rec, stride, n, c->phys, out);
+}
+
 // ---- objectives, evaluated on the ghost-completed primitives of stage 1 ----
 
 __device__ __forceinline__ double block_sum(double v, double* sh) {
@@ -331,15 +364,15 @@ __global__ void __launch_bounds__(BLOCK) k_objective(MeshDev<R> m, Phys P, const
         if (kind == AFVM_OBJ_KINETIC_ENERGY) {
             // per-cell term in the working precision R, accumulated in double
             const R* r = rec + (size_t)t * REC;
-            R rho = r[R_P] / ((consts<R>(P).Cv * r[R_T]) * consts<R>(P).gm1);
+            R rho = rec_abs_p<R>(P, r[R_P]) / ((consts<R>(P).Cv * rec_abs_T<R>(P, r[R_T])) * consts<R>(P).gm1);
             v = (double)(R(0.5) * rho * (r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) * m.vol[t]);
         } else if (kind == AFVM_OBJ_SUM_T) {
-            v = (double)rec[(size_t)t * REC + R_T];
+            v = rec_T<R>(P, rec[(size_t)t * REC + R_T]);
         } else {
             int f = start + t;
             const R* rN = rec + (size_t)m.nbr[f] * REC;
             const R* rP = rec + (size_t)m.own[f] * REC;
-            double U0 = rN[0], U0i = rP[0], p0 = rN[R_P], T0 = rN[R_T];
+            double U0 = rN[0], U0i = rP[0], p0 = rec_p<R>(P, rN[R_P]), T0 = rec_T<R>(P, rN[R_T]);
             double nx = m.nrm[f];
             double mu = (P.muModel == AFVM_MU_SUTHERLAND) ? (P.muAs * (T0 * sqrt(T0))) / (T0 + P.muTs) : P.mu0;
             double mungUx = mu * (U0 - U0i) / (double)m.dlt[f];
@@ -362,11 +395,11 @@ __global__ void __launch_bounds__(BLOCK) k_obj_vane(MeshDev<R> m, Phys P, const 
     if (t < v.nPlane) {
         const R* r = rec + (size_t)v.planeCells[t] * REC;
         double U[3] = {r[0], r[1], r[2]};
-        vane_cell(P, v, U, (double)r[R_T], (double)r[R_P], v.planeArea[t], l, w);
+        vane_cell(P, v, U, rec_T<R>(P, r[R_T]), rec_p<R>(P, r[R_P]), v.planeArea[t], l, w);
     } else if (t < v.nPlane + v.nHeat) {
         int q = t - v.nPlane;
         int f = v.heatFaces[q];
-        h = v.heatCoef[q] * (v.Tw - (double)rec[(size_t)m.own[f] * REC + R_T]);
+        h = v.heatCoef[q] * (v.Tw - rec_T<R>(P, rec[(size_t)m.own[f] * REC + R_T]));
     }
     double s0 = block_sum(l, sh0), s1 = block_sum(w, sh1), s2 = block_sum(h, sh2);
     if (threadIdx.x == 0) {
@@ -526,9 +559,12 @@ int primal_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double d
         }
         if (st == 1 && c->objSink) {
             // the objective stage's primitives U (3), T, p of every cell, ghosts included, for an
-            // objective evaluated by the caller
-            cudaMemcpy2DAsync(c->objSink, 5 * sizeof(R), recs[1], REC * sizeof(R), 5 * sizeof(R), (size_t)m.nC,
-                              cudaMemcpyDeviceToDevice, s);
+            // objective evaluated by the caller (absolute values: FP32 records add their gauge)
+            if constexpr (kGauge<R>)
+                k_abs_prims<R><<<nblocks(m.nC), BLOCK, 0, s>>>(recs[1], REC, m.nC, P, (R*)c->objSink);
+            else
+                cudaMemcpy2DAsync(c->objSink, 5 * sizeof(R), recs[1], REC * sizeof(R), 5 * sizeof(R), (size_t)m.nC,
+                                  cudaMemcpyDeviceToDevice, s);
         }
         if (st == 1 && c->objective == AFVM_OBJ_VANE) {
             // the partial sums now, while rec holds the stage-1 primitives; combined at the end

@@ -108,12 +108,12 @@ __global__ void __launch_bounds__(BLOCK) k_visc_cell(MeshDev<R> m, Phys P, const
                 double w = m.wts[f];
                 for (int i = 0; i < 3; i++) UF[i] = (double)rO[i] * w + (double)rN[i] * (-w + 1);
                 pF = (double)rO[R_P] * w + (double)rN[R_P] * (-w + 1);
-                double cL = sqrt(g * (double)rO[R_T] * Rg), cR = sqrt(g * (double)rN[R_T] * Rg);
+                double cL = sqrt(g * rec_T<R>(P, rO[R_T]) * Rg), cR = sqrt(g * rec_T<R>(P, rN[R_T]) * Rg);
                 cF = cR * (-w + 1) + cL * w;
             } else {
                 for (int i = 0; i < 3; i++) UF[i] = rN[i];
                 pF = rN[R_P];
-                cF = sqrt(g * (double)rN[R_T] * Rg);
+                cF = sqrt(g * rec_T<R>(P, rN[R_T]) * Rg);
             }
             double N[3] = {(double)m.nrm[f], (double)m.nrm[nF + f], (double)m.nrm[2 * nF + f]};
             double sw = ownerSide ? wt : -wt;
@@ -121,6 +121,7 @@ __global__ void __launch_bounds__(BLOCK) k_visc_cell(MeshDev<R> m, Phys P, const
                 for (int j = 0; j < 3; j++) gU[i][j] += (UF[i] * N[j]) * sw;
             dU += (UF[0] * N[0] + UF[1] * N[1] + UF[2] * N[2]) * sw;
             for (int j = 0; j < 3; j++) {
+                // (the pressure gradient: a gauge offset of FP32 records drops out of this closed sum)
                 gp[j] += (pF * N[j]) * sw;
                 gc[j] += (cF * N[j]) * sw;
             }
@@ -128,7 +129,7 @@ __global__ void __launch_bounds__(BLOCK) k_visc_cell(MeshDev<R> m, Phys P, const
         double val = 1.0;
         if (kind != AFVM_VISC_UNIFORM) {
             const R* r = rec + (size_t)c * REC;
-            double T = r[R_T], p = r[R_P];
+            double T = rec_T<R>(P, r[R_T]), p = rec_p<R>(P, r[R_P]);
             double rho = p / ((P.Cv * T) * (g - 1));
             double cc = sqrt(g * p / rho);
             double grho[3];

@@ -81,7 +81,7 @@ class RCF(object):
     names = ['rho', 'rhoU', 'rhoE']
     dimensions = [(1,), (3,), (1,)]
 
-    def __init__(self, mesh, bc, objective='none', precision='fp64', device=0, **config):
+    def __init__(self, mesh, bc, objective='none', precision='fp64', device=0, gauge=None, **config):
         for k in config:
             if k not in DEFAULTS:
                 raise ValueError('unknown RCF option %r' % k)
@@ -112,6 +112,10 @@ class RCF(object):
         self.device = device
         self._ctx = None
         self._create()
+        # the gauge state (p, T, H) of the FP32 records ('fp32', 'mixed'): by default the
+        # boundary conditions' (afvm_set_gauge); give one for a case whose boundaries fix no p or T
+        if gauge is not None:
+            L.check(L.lib().afvm_set_gauge(self._ctx, *[float(v) for v in gauge]), self._ctx, 'afvm_set_gauge')
 
     # ------------------------------------------------------------------ set-up
     def _physics(self):
@@ -561,6 +565,13 @@ class RCF(object):
             cache[name] = torch.as_tensor(a, device='cuda:%d' % self.device).to(dt)
         return cache[name]
 
+    @property
+    def gauge(self):
+        """(p, T, H) of the gauge state of the FP32 records (afvm_get_gauge)."""
+        out = np.zeros(3)
+        L.check(L.lib().afvm_get_gauge(self._ctx, out.ctypes.data_as(C.POINTER(C.c_double))), self._ctx)
+        return tuple(float(v) for v in out)
+
     def _call_objective(self, prims, view=None):
         P = prims.double()
         return self.objectiveFn([P[:, 0:3], P[:, 3:4], P[:, 4:5]], view or ObjectiveSolver(self))
@@ -581,7 +592,13 @@ class RCF(object):
         m = self.mesh
         if tape is not None:
             off = int(L.lib().afvm_tape_elements(self._ctx)) - 3 * 20 * m.nCells + 20 * m.nCells
-            return tape[off:off + 20 * m.nCells].view(m.nCells, 20)[:, :5]
+            prims = tape[off:off + 20 * m.nCells].view(m.nCells, 20)[:, :5]
+            if self.record_dtype == np.float64:
+                return prims
+            # FP32 records hold T and p as offsets from the gauge state
+            g = self.gauge
+            return prims.double() + torch.tensor([0.0, 0.0, 0.0, g[1], g[0]], dtype=torch.float64,
+                                                 device=prims.device)
         tmp = (torch.empty_like(rho), torch.empty_like(rhoU), torch.empty_like(rhoE))
         self.step(rho, rhoU, rhoE, dt, S=S, out=tmp, want_scalars=False)
         return self._objPrims.clone()

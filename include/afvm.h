@@ -202,6 +202,19 @@ int afvm_ctx_precision(const afvm_ctx* ctx);
 /* Device bytes held by the context (mesh + work buffers). */
 int64_t afvm_ctx_device_bytes(const afvm_ctx* ctx);
 
+/* The gauge state of FP32 cell records (AFVM_FP32 and AFVM_FP32_STATE64 contexts): their
+ * records hold p - p_g and T - T_g, and their face fluxes leave out p_g N (momentum) and H_g
+ * times the mass flux (energy; added back to the energy residual in the state's type), so that
+ * float arithmetic keeps the digits of a low-Mach flow's small pressure and temperature
+ * variations. Not part of the reference's arithmetic: results are the same to rounding. The
+ * default, set by afvm_ctx_create, is the mean fixed boundary p and T (totals on CBC_TOTAL_PT
+ * patches) and the mean Cp T + |U|^2/2 of ghosts with fixed U and T; 0 without such boundary
+ * values. p_g and T_g are rounded to floats. Set it before the first step: records, tapes and
+ * CUDA graphs made earlier keep the old gauge. FP64 contexts store it and do not use it.
+ * afvm_get_gauge writes p_g, T_g, H_g. */
+int afvm_set_gauge(afvm_ctx* ctx, double p, double T, double H);
+int afvm_get_gauge(const afvm_ctx* ctx, double* pTH);
+
 /* Replace the values of a fixedValue / CBC_UPT boundary input (host pointer, nFaces x dims)
  * - the per-call BC tensors of Solver.getBoundaryTensor (adFVM/solver.py:91-92). field: 0=U,
  * 1=T, 2=p. */

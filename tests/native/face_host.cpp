@@ -90,3 +90,54 @@ extern "C" void afvm_host_face_vjp_geo(int n, int kind, int inviscid, const doub
         memcpy(out + 55 * (size_t)i + 40, &g, sizeof(g));
     }
 }
+
+// The gauge-form flux of FP32 records (face_flux<R, true>): `in` holds absolute values; the
+// offsets p - gauge[0], T - gauge[1] are taken in double (as the records' are) and then rounded
+// to R. F receives the gauge-form flux and the CFL term, in double.
+template <typename R>
+static void gauge_faces(int n, int kind, int inviscid, const Phys& P, const double* in, double* F) {
+    for (int i = 0; i < n; i++) {
+        const double* x = in + 55 * (size_t)i;
+        double y[55];
+        for (int k = 0; k < 55; k++) y[k] = x[k];
+        y[3] -= P.gaugeT; y[8] -= P.gaugeT;
+        y[4] -= P.gaugeP; y[9] -= P.gaugeP;
+        FaceIn<R> fi;
+        R* f = &fi.UP[0];
+        for (int k = 0; k < 55; k++) f[k] = (R)y[k];
+        R Fo[5], maxaF;
+        face_flux<R, true>(P, kind, inviscid != 0, fi, Fo, maxaF);
+        for (int k = 0; k < 5; k++) F[6 * (size_t)i + k] = Fo[k];
+        F[6 * (size_t)i + 5] = maxaF;
+    }
+}
+
+extern "C" void afvm_host_face_gauge(int n, int kind, int inviscid, const double* ph, const double* gauge, int f32,
+                                     const double* in, double* F) {
+    Phys P = make_phys(ph);
+    if (f32) P.small = 1e-9;
+    P.gaugeP = gauge[0];
+    P.gaugeT = gauge[1];
+    P.gaugeH = gauge[2];
+    finish_phys(P);
+    if (f32)
+        gauge_faces<float>(n, kind, inviscid, P, in, F);
+    else
+        gauge_faces<double>(n, kind, inviscid, P, in, F);
+}
+
+// the absolute-form flux in FP32 (the form FP32 records had without a gauge)
+extern "C" void afvm_host_face_f32(int n, int kind, int inviscid, const double* ph, const double* in, double* F) {
+    Phys P = make_phys(ph);
+    P.small = 1e-9;
+    finish_phys(P);
+    for (int i = 0; i < n; i++) {
+        FaceIn<float> fi;
+        float* f = &fi.UP[0];
+        for (int k = 0; k < 55; k++) f[k] = (float)in[55 * (size_t)i + k];
+        float Fo[5], maxaF;
+        face_flux<float>(P, kind, inviscid != 0, fi, Fo, maxaF);
+        for (int k = 0; k < 5; k++) F[6 * (size_t)i + k] = Fo[k];
+        F[6 * (size_t)i + 5] = maxaF;
+    }
+}

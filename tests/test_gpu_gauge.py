@@ -1,0 +1,83 @@
+"""The gauge state of FP32 cell records ('fp32' and 'mixed' contexts): records hold p - p_g and
+T - T_g and the face fluxes leave out p_g N and H_g times the mass flux (afvm_set_gauge).
+
+* the default gauge is the far field's p, T and total enthalpy (afvm_ctx_create);
+* over 50 steps of the cylinder the mixed form with the gauge is much closer to FP64 than with
+  a zero gauge (the form FP32 records had before), and both are within 1e-5;
+* what leaves the records - the boundary map, the objective-stage primitives handed to an
+  objective function - is absolute: the same as the FP64 context's to FP32 rounding.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from adfvm_gb300 import cases
+from adfvm_gb300.solver import RCF
+from tests import objective_fns as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _cyl():
+    case = cases.cylinder(64, 32, objective='drag:cylinder')
+    mesh = case.build_mesh()
+    x = [torch.as_tensor(np.asarray(a).reshape(mesh.nInternalCells, -1)) for a in cases.conservative(case)]
+    return case, mesh, x
+
+
+def test_default_gauge_is_the_far_field():
+    case, mesh, _ = _cyl()
+    r = RCF(mesh, case.bc, objective=case.objective, precision='mixed', **case.config)
+    U0 = 0.3 * math.sqrt(cases.GAMMA * cases.R_GAS * 300.0)
+    H = float(np.float32(1004.5 * 300.0 + 0.5 * U0 * U0))
+    assert r.gauge == (1e5, 300.0, H), r.gauge
+    box = cases.box(8)
+    rb = RCF(box.build_mesh(), box.bc, objective=box.objective, precision='fp32', **box.config)
+    assert rb.gauge == (0.0, 0.0, 0.0)          # a periodic box fixes no boundary value
+    rb.close()
+    r.close()
+
+
+def _run(case, mesh, x, precision, gauge=None, n=50):
+    r = RCF(mesh, case.bc, objective=case.objective, precision=precision, gauge=gauge, **case.config)
+    td = torch.float32 if r.dtype == np.float32 else torch.float64
+    y = [t.to(td).cuda() for t in x]
+    for _ in range(n):
+        y = list(r.step(y[0], y[1], y[2], case.dt)[:3])
+    out = [t.double().cpu().numpy() for t in y]
+    r.close()
+    return out
+
+
+def test_gauge_brings_mixed_closer_to_fp64():
+    case, mesh, x = _cyl()
+    ref = _run(case, mesh, x, 'fp64')
+    g = _run(case, mesh, x, 'mixed')
+    z = _run(case, mesh, x, 'mixed', gauge=(0.0, 0.0, 0.0))
+    for i, name in enumerate(('rho', 'rhoU', 'rhoE')):
+        scale = np.abs(ref[i]).max()
+        eg = np.abs(g[i] - ref[i]).max() / scale
+        ez = np.abs(z[i] - ref[i]).max() / scale
+        assert eg <= 1e-5 and ez <= 1e-5, (name, eg, ez)
+        assert eg * 2 < ez, '%s: gauge %.3e, no gauge %.3e' % (name, eg, ez)
+
+
+@pytest.mark.parametrize('precision', ['fp32', 'mixed'])
+def test_values_leaving_the_records_are_absolute(precision):
+    case, mesh, x = _cyl()
+    a = RCF(mesh, case.bc, objective=case.objective, **case.config)
+    b = RCF(mesh, case.bc, objective=O.drag('cylinder'), precision=precision, **case.config)
+    td = torch.float32 if b.dtype == np.float32 else torch.float64
+    xa = [t.cuda() for t in x]
+    xb = [t.to(td).cuda() for t in x]
+    ga = a.boundary_values(*xa).double().cpu().numpy()
+    gb = b.boundary_values(*xb).double().cpu().numpy()
+    err = np.abs(gb - ga).max(axis=0) / np.abs(ga).max(axis=0).clip(1.0)
+    assert (err < 1e-6).all(), err
+    oa = float(a.step(*xa, case.dt)[4])
+    ob = float(b.step(*xb, case.dt)[4])
+    assert abs(ob - oa) <= 1e-5 * abs(oa), (oa, ob)
+    a.close()
+    b.close()
