@@ -148,25 +148,21 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const
     R pbar[5];
     for (int k = 0; k < 5; k++) pbar[k] = cb[k];
     const R* G = cb + 5;
-    R rv = m.rvol[c];
     {
-        // the cell's own slots at once: sum_s (1 - w'_s) (G . S N'_s) = G . sum_s (1 - w'_s) S N'_s
-        R A[3] = {m.gA[c], m.gA[n + c], m.gA[2 * n + c]};
-        R pb[5];
-        phi_bar<R>(G, A, rv, pb);
-        for (int k = 0; k < 5; k++) pbar[k] += pb[k];
+        // the cell's own slots at once: sum_s (1 - w'_s) (G . S N'_s) / V = G . gAv
+        R A[3] = {m.gAv[c], m.gAv[n + c], m.gAv[2 * n + c]};
+        for (int i = 0; i < 5; i++) pbar[i] += G[3 * i] * A[0] + G[3 * i + 1] * A[1] + G[3 * i + 2] * A[2];
     }
     for (int s = 0; s < 6; s++) {
-        R sn[3] = {m.gsn[(3 * s) * n + c], m.gsn[(3 * s + 1) * n + c], m.gsn[(3 * s + 2) * n + c]};
         int nb = m.gnb[s * n + c];
         if (nb < m.nIC) {
-            // neighbour's gradient: its slot for this face has S N'' = -S N' and weight gwb
-            R msn[3] = {-sn[0], -sn[1], -sn[2]};
-            R pn[5], cn[CBAR];
+            // neighbour's gradient: its slot for this face has S N'' = -S N' and weight gwb;
+            // gbs_s = -gwb_s S N'_s / V_nb
+            R b[3] = {m.gbs[(3 * s) * n + c], m.gbs[(3 * s + 1) * n + c], m.gbs[(3 * s + 2) * n + c]};
+            R cn[CBAR];
             load_vec(cbar + (size_t)nb * CBAR, cn, CBAR);
-            phi_bar<R>(cn + 5, msn, m.rvol[nb], pn);
-            R wb = m.gwb[s * n + c];
-            for (int k = 0; k < 5; k++) pbar[k] += wb * pn[k];
+            const R* Gn = cn + 5;
+            for (int i = 0; i < 5; i++) pbar[i] += Gn[3 * i] * b[0] + Gn[3 * i + 1] * b[1] + Gn[3 * i + 2] * b[2];
         }
     }
     // ghost cells whose boundary value comes from this cell: transpose of the BC

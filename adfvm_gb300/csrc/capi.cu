@@ -98,7 +98,7 @@ struct HostTables {
     std::vector<int32_t> gnb, accf;
     std::vector<double> gw, gsn, rvol, accw, vol;
     // adjoint
-    std::vector<double> wpf, wnf, gwb, gA;
+    std::vector<double> wpf, wnf, gwb, gA, gws, gAv, gbs;
     std::vector<int32_t> gsStart, gsList, gslot;
 };
 
@@ -142,6 +142,9 @@ int upload_mesh(Ctx* c, const HostTables& h, MeshDev<R>& m) {
     if ((st = upload(c, &m.wnf, cast<R>(h.wnf)))) return st;
     if ((st = upload(c, &m.gwb, cast<R>(h.gwb)))) return st;
     if ((st = upload(c, &m.gA, cast<R>(h.gA)))) return st;
+    if ((st = upload(c, &m.gws, cast<R>(h.gws)))) return st;
+    if ((st = upload(c, &m.gAv, cast<R>(h.gAv)))) return st;
+    if ((st = upload(c, &m.gbs, cast<R>(h.gbs)))) return st;
     if ((st = upload(c, &m.gsStart, h.gsStart))) return st;
     if ((st = upload(c, &m.gsList, h.gsList))) return st;
     if ((st = upload(c, &m.gslot, h.gslot))) return st;
@@ -354,6 +357,24 @@ int build_tables(Ctx* c, const afvm_mesh_tensors* M, const afvm_patch_bc* bcs, H
             for (int s = 0; s < 6; s++) a += (1.0 - h.gw[s * n + ci]) * h.gsn[(3 * s + k) * n + ci];
             h.gA[k * n + ci] = a;
         }
+    // the same products with 1/V folded in, for the gradient gather and its transpose:
+    //   grad phi_c = phi_c gA_c / V_c + sum_s phi_nb(s) w'_s S N'_s / V_c
+    // and the neighbour slots' share of the transpose, -gwb_s S N'_s / V_nb(s)
+    h.gws.assign(18 * n, 0.0);
+    h.gAv.assign(3 * n, 0.0);
+    h.gbs.assign(18 * n, 0.0);
+#pragma omp parallel for
+    for (int ci = 0; ci < nIC; ci++) {
+        for (int k = 0; k < 3; k++) h.gAv[k * n + ci] = h.gA[k * n + ci] * h.rvol[ci];
+        for (int s = 0; s < 6; s++) {
+            int nb = h.gnb[s * n + ci];
+            for (int k = 0; k < 3; k++) {
+                double sn = h.gsn[(3 * s + k) * n + ci];
+                h.gws[(3 * s + k) * n + ci] = (h.gw[s * n + ci] * sn) * h.rvol[ci];
+                if (nb < nIC) h.gbs[(3 * s + k) * n + ci] = -(h.gwb[s * n + ci] * sn) * h.rvol[nb];
+            }
+        }
+    }
     h.gsStart.assign(nIC + 1, 0);
     for (int g = 0; g < nG; g++) h.gsStart[h.gsrc[g] + 1]++;
     for (int ci = 0; ci < nIC; ci++) h.gsStart[ci + 1] += h.gsStart[ci];

@@ -95,6 +95,10 @@ struct MeshDev {
     const R* wnf;             // nIF A/V_R per internal face
     const R* gwb;             // 6 x nIC: w' of the neighbour's slot that points back at this cell
     const R* gA;              // 3 x nIC: sum over the slots of (1 - w') S N
+    // the gradient's mesh-only products, 1/V folded in: grad phi_c = phi_c gAv + sum_s phi_nb gws_s
+    const R* gws;             // 3 x 6 x nIC: w' S N' / V
+    const R* gAv;             // 3 x nIC: gA / V
+    const R* gbs;             // 3 x 6 x nIC: -gwb S N' / V_nb (internal neighbours; 0 for ghosts)
     const int32_t* gsStart;   // nIC + 1: ghosts whose source is the cell, CSR offsets
     const int32_t* gsList;    // nG ghost ids ordered by source cell
     const int32_t* gslot;     // nG: slot of the ghost's face in its owner's cellFaces

@@ -155,9 +155,9 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
         tp.put(T_TLF, TLF); tp.put(T_PLF, pLF); tp.put(T_TRF, TRF); tp.put(T_PRF, pRF);
         tp.put(T_RDL, rdL); tp.put(T_RDR, rdR);
         if (solver == AFVM_RIEMANN_ROE)
-            roe<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, in.N, F, tp);
+            roe<R>(P, pLF, pRF, TLF, TRF, ULF, URF, rhoL, rhoR, in.N, F, tp);
         else
-            laxf<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, rhoUL, rhoUR, rhoEL, rhoER, in.N, F, tp);
+            laxf<R>(P, pLF, pRF, TLF, TRF, ULF, URF, rhoL, rhoR, rhoUL, rhoUR, rhoEL, rhoER, in.N, F, tp);
         if (kind == FACE_CHARACTERISTIC) {
             TF = in.TN;
             for (int k = 0; k < 3; k++) { UF[k] = in.UN[k]; gTF[k] = in.gTN[k]; }
@@ -207,23 +207,30 @@ AFVM_HD void recon_vjp(R b, R lw, const R* qw, R& phiCb, R& phiDb, R* gb) {
 
 // riemann.eulerRoe; the forward's reciprocals and reciprocal square roots come from the tape
 template <typename R, typename Src, typename G = GeoNone>
-AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR, const R* N, const R* Fb,
-                     const Src& t, R& pLb, R& pRb, R* ULb, R* URb, R& rhoLb, R& rhoRb, G* geo = nullptr) {
-    const R g = consts<R>(P).gamma, gm1 = consts<R>(P).gm1, ggm1 = consts<R>(P).ggm1, h = R(0.5);
+AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R* UR, R rhoL, R rhoR, const R* N,
+                     const R* Fb, const Src& t, R& pLb, R& pRb, R& TLb, R& TRb, R* ULb, R* URb, R& rhoLb, R& rhoRb,
+                     G* geo = nullptr) {
+    const R gm1 = consts<R>(P).gm1, gRg = consts<R>(P).gRg, Cp = consts<R>(P).Cp, h = R(0.5);
     // ---- forward values: those dear to recompute from the tape, the cheap ones again (as roe());
-    // a lean tape (Src::kFull false) holds only the reciprocals, and the Roe intermediates are
-    // re-evaluated here
-    R UnL = dot3(UL, N), UnR = dot3(UR, N);
-    R rhoUnL = rhoL * UnL, rhoUnR = rhoR * UnR;
-    R rrL = t.get(T_RRL), rrR = t.get(T_RRR);
+    // a lean tape (Src::kFull false) holds only the reciprocals and the normal velocities, and
+    // the Roe intermediates are re-evaluated here
+    R UnL = t.get(T_UNL), UnR = t.get(T_UNR);
     R rsL = t.get(T_RSL), rsR = t.get(T_RSR);
-    R sL = rhoL * rsL, sR = rhoR * rsR;
     R rD = t.get(T_RD);
     R raF = t.get(T_RAF);
     R rcL = t.get(T_RCL), rcR = t.get(T_RCR);
     R re = t.get(T_RE);
-    R c2L = g * pL * rrL, c2R = g * pR * rrR;
-    R cL = c2L > R(0) ? c2L * rcL : R(0), cR = c2R > R(0) ? c2R * rcR : R(0);
+    R rhoUnL, rhoUnR, sL, sR, cL, cR;
+    if constexpr (Src::kFull) {
+        rhoUnL = t.get(T_RUNL); rhoUnR = t.get(T_RUNR);
+        sL = t.get(T_SL); sR = t.get(T_SR);
+        cL = t.get(T_CL); cR = t.get(T_CR);
+    } else {
+        rhoUnL = rhoL * UnL; rhoUnR = rhoR * UnR;
+        sL = rhoL * rsL; sR = rhoR * rsR;
+        R c2L = gRg * TL, c2R = gRg * TR;
+        cL = c2L > R(0) ? c2L * rcL : R(0); cR = c2R > R(0) ? c2R * rcR : R(0);
+    }
     R eb_ = cL - cR;
     R ea = UnL - UnR;
     R drho = rhoR - rhoL;
@@ -240,14 +247,12 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL
         L1 = t.get(T_L1); L2 = t.get(T_L2); L3 = t.get(T_L3);
         abv4 = t.get(T_ABV4); abv5 = t.get(T_ABV5); abv6 = t.get(T_ABV6); abv7 = t.get(T_ABV7);
     }
-    R a2F = gm1 * (hF - qF);
     if constexpr (!Src::kFull) {
-        hL = ggm1 * pL * rrL + h * dot3(UL, UL);
-        hR = ggm1 * pR * rrR + h * dot3(UR, UR);
+        hL = Cp * TL + h * dot3(UL, UL);
+        hR = Cp * TR + h * dot3(UR, UR);
         for (int k = 0; k < 3; k++) UF[k] = (UL[k] * sL + UR[k] * sR) * rD;
         hF = (hL * sL + hR * sR) * rD;
         qF = h * dot3(UF, UF);
-        a2F = gm1 * (hF - qF);
         UnF = dot3(UF, N);
         for (int k = 0; k < 3; k++) dU[k] = rhoR * UR[k] - rhoL * UL[k];
         drhoE = (hR * rhoR - pR) - (hL * rhoL - pL);
@@ -255,8 +260,14 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL
         eps = eps + h * fabs(eb_);
         eps = (eps < R(0)) ? eps - consts<R>(P).small : eps + consts<R>(P).small;
     }
-    R aF = a2F * raF;
-    R ra2F = raF * raF;
+    R aF, ra2F;
+    if constexpr (Src::kFull) {
+        aF = t.get(T_AF);
+        ra2F = t.get(T_RA2F);
+    } else {
+        aF = (gm1 * (hF - qF)) * raF;
+        ra2F = raF * raF;
+    }
     R l1 = fabs(UnF), l2 = fabs(UnF + aF), l3 = fabs(UnF - aF);
     R eps2 = R(2) * eps;
     bool s1 = l1 < eps2, s2 = l2 < eps2, s3 = l3 < eps2;
@@ -265,8 +276,14 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL
         L2 = s2 ? R(0.25) * l2 * l2 * re + eps : l2;
         L3 = s3 ? R(0.25) * l3 * l3 * re + eps : l3;
     }
-    R abv2 = h * (L2 - L3);
-    R abv3 = h * (L2 + L3) - L1;
+    R abv2, abv3;
+    if constexpr (Src::kFull) {
+        abv2 = t.get(T_ABV2);
+        abv3 = t.get(T_ABV3);
+    } else {
+        abv2 = h * (L2 - L3);
+        abv3 = h * (L2 + L3) - L1;
+    }
     if constexpr (!Src::kFull) {
         abv4 = gm1 * (qF * drho - dot3(UF, dU) + drhoE);
         abv5 = UnF * drho - dot3(dU, N);
@@ -320,12 +337,9 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL
     if (s3) { l3b = L3b * h * l3 * re; epsb += L3b * (R(1) - R(0.25) * l3 * l3 * re * re); } else l3b = L3b;
     R eab = h * epsb * sgn(ea);
     R ebb = h * epsb * sgn(eb_);
-    // c = sqrt(g p / rho): dc/dp = c/(2p) = g/(2 c rho), dc/drho = -c/(2 rho)
-    R cLb = ebb, cRb = -ebb;
-    pLb += cLb * g * h * rcL * rrL;
-    rhoLb += -cLb * h * cL * rrL;
-    pRb += cRb * g * h * rcR * rrR;
-    rhoRb += -cRb * h * cR * rrR;
+    // c = sqrt(g Rg T): dc/dT = g Rg / (2 c)
+    TLb += ebb * (h * gRg) * rcL;
+    TRb += -ebb * (h * gRg) * rcR;
     // lam = |UnF|, |UnF + aF|, |UnF - aF|
     R t2 = sgn(UnF + aF), t3 = sgn(UnF - aF);
     UnFb += l1b * sgn(UnF) + l2b * t2 + l3b * t3;
@@ -371,11 +385,9 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL
     pRb += pn;
     if constexpr (kGeo<G>)
         for (int k = 0; k < 3; k++) geo->N[k] += h * Fu[k] * (pL + pR);
-    // hL = g pL/(gm1 rhoL) + qL/2
-    pLb += hLb * ggm1 * rrL;
-    rhoLb += -hLb * ggm1 * pL * rrL * rrL;
-    pRb += hRb * ggm1 * rrR;
-    rhoRb += -hRb * ggm1 * pR * rrR * rrR;
+    // hL = Cp TL + qL/2
+    TLb += hLb * Cp;
+    TRb += hRb * Cp;
     for (int k = 0; k < 3; k++) { ULb[k] += hLb * UL[k]; URb[k] += hRb * UR[k]; }
     // rhoUn = rho Un ; Un = U.N ; eps term ea = UnL - UnR
     rhoLb += rhoUnLb * UnL;
@@ -388,16 +400,20 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL
 
 // riemann.eulerLaxFriedrichs
 template <typename R, typename Src, typename G = GeoNone>
-AFVM_HD void laxf_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR, const R* rhoUL,
-                      const R* rhoUR, R rhoEL, R rhoER, const R* N, const R* Fb, const Src& t, R& pLb, R& pRb,
-                      R* ULb, R* URb, R& rhoLb, R& rhoRb, R* rhoULb, R* rhoURb, R& rhoELb, R& rhoERb,
-                      G* geo = nullptr) {
-    const R g = consts<R>(P).gamma, h = R(0.5);
-    R UnL = dot3(UL, N), UnR = dot3(UR, N);
-    R rrL = t.get(T_RRL), rrR = t.get(T_RRR);
-    R c2L = g * pL * rrL, c2R = g * pR * rrR;
+AFVM_HD void laxf_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R* UR, R rhoL, R rhoR,
+                      const R* rhoUL, const R* rhoUR, R rhoEL, R rhoER, const R* N, const R* Fb, const Src& t,
+                      R& pLb, R& pRb, R& TLb, R& TRb, R* ULb, R* URb, R& rhoLb, R& rhoRb, R* rhoULb, R* rhoURb,
+                      R& rhoELb, R& rhoERb, G* geo = nullptr) {
+    const R gRg = consts<R>(P).gRg, h = R(0.5);
+    R UnL = t.get(T_UNL), UnR = t.get(T_UNR);
     R rcL = t.get(T_RCL), rcR = t.get(T_RCR);
-    R cL = c2L > R(0) ? c2L * rcL : R(0), cR = c2R > R(0) ? c2R * rcR : R(0);
+    R cL, cR;
+    if constexpr (Src::kFull) {
+        cL = t.get(T_CL); cR = t.get(T_CR);
+    } else {
+        R c2L = gRg * TL, c2R = gRg * TR;
+        cL = c2L > R(0) ? c2L * rcL : R(0); cR = c2R > R(0) ? c2R * rcR : R(0);
+    }
     R A = fabs(UnL) + cL, B = fabs(UnR) + cR;
     R aF = (A >= B) ? A : B;
     R ha = h * aF;
@@ -421,10 +437,8 @@ AFVM_HD void laxf_vjp(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rho
     R Ab = (A >= B) ? aFb : R(0), Bb = (A >= B) ? R(0) : aFb;
     UnLb += Ab * sgn(UnL);
     UnRb += Bb * sgn(UnR);
-    pLb += Ab * g * h * rcL * rrL;
-    rhoLb += -Ab * h * cL * rrL;
-    pRb += Bb * g * h * rcR * rrR;
-    rhoRb += -Bb * h * cR * rrR;
+    TLb += Ab * (h * gRg) * rcL;
+    TRb += Bb * (h * gRg) * rcR;
     for (int k = 0; k < 3; k++) { ULb[k] += UnLb * N[k]; URb[k] += UnRb * N[k]; }
     if constexpr (kGeo<G>)
         for (int k = 0; k < 3; k++) geo->N[k] += UnLb * UL[k] + UnRb * UR[k] + h * Fu[k] * (pL + pR);
@@ -681,15 +695,16 @@ AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>&
     R rhoELb = R(0), rhoERb = R(0);
     int solver = chr ? P.briemann : P.riemann;
     if (solver == AFVM_RIEMANN_ROE) {
-        roe_vjp<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, in.N, Fb, t, pLFb, pRFb, ULFb, URFb, rhoLb, rhoRb, geo);
+        roe_vjp<R>(P, pLF, pRF, TLF, TRF, ULF, URF, rhoL, rhoR, in.N, Fb, t, pLFb, pRFb, TLFb, TRFb, ULFb, URFb,
+                   rhoLb, rhoRb, geo);
     } else {
         // conservative()'s rhoU and rhoE of each side
         R eL = consts<R>(P).Cv * TLF, eR = consts<R>(P).Cv * TRF;
         R rhoEL = rhoL * (eL + R(0.5) * dot3(ULF, ULF)), rhoER = rhoR * (eR + R(0.5) * dot3(URF, URF));
         R rhoUL[3], rhoUR[3];
         for (int k = 0; k < 3; k++) { rhoUL[k] = ULF[k] * rhoL; rhoUR[k] = URF[k] * rhoR; }
-        laxf_vjp<R>(P, pLF, pRF, ULF, URF, rhoL, rhoR, rhoUL, rhoUR, rhoEL, rhoER, in.N, Fb, t, pLFb, pRFb, ULFb,
-                    URFb, rhoLb, rhoRb, rhoULb, rhoURb, rhoELb, rhoERb, geo);
+        laxf_vjp<R>(P, pLF, pRF, TLF, TRF, ULF, URF, rhoL, rhoR, rhoUL, rhoUR, rhoEL, rhoER, in.N, Fb, t, pLFb, pRFb,
+                    TLFb, TRFb, ULFb, URFb, rhoLb, rhoRb, rhoULb, rhoURb, rhoELb, rhoERb, geo);
     }
     conservative_vjp_t<R>(P, ULF, TLF, pLF, rdL, rhoLb, rhoULb, rhoELb, ULFb, TLFb, pLFb);
     conservative_vjp_t<R>(P, URF, TRF, pRF, rdR, rhoRb, rhoURb, rhoERb, URFb, TRFb, pRFb);

@@ -39,7 +39,7 @@ constexpr int FACE_INTERNAL = 0, FACE_COUPLED = 1, FACE_CHARACTERISTIC = 2, FACE
 // a sink (nothing, a local array, or a column of a device tape); the VJP reads them back.
 constexpr int T_ULF = 0, T_TLF = 3, T_PLF = 4, T_URF = 5, T_TRF = 8, T_PRF = 9;   // face states
 constexpr int T_RDL = 10, T_RDR = 11;            // 1/(Cv T (g-1)) of each side (conservative)
-constexpr int T_RRL = 12, T_RRR = 13;            // 1/rho
+constexpr int T_UNL = 12, T_UNR = 13;            // U.n of each side
 constexpr int T_RSL = 14, T_RSR = 15;            // 1/sqrt(rho)
 constexpr int T_RD = 16, T_RAF = 17;             // 1/(sL + sR), 1/a_F (Roe average)
 constexpr int T_RCL = 18, T_RCR = 19;            // 1/c of each side
@@ -55,7 +55,11 @@ constexpr int T_L1 = 36, T_L2 = 37, T_L3 = 38;   // |eigenvalues| after the entr
 constexpr int T_ABV4 = 39, T_ABV5 = 40, T_ABV6 = 41, T_ABV7 = 42;
 // viscous intermediates: (grad U + grad U^T).n (3), sigma (3), tr grad U (corrected face gradient)
 constexpr int T_TMP2 = 43, T_SIG = 46, T_TMP3 = 49;
-constexpr int TAPE = 50;
+// more Roe forward values, so that the reverse sweep re-derives none: rho U.n and sqrt(rho) of
+// each side, the sound speeds, the Roe-average sound speed and 1/a_F^2, and abv2, abv3
+constexpr int T_RUNL = 50, T_RUNR = 51, T_SL = 52, T_SR = 53, T_CL = 54, T_CR = 55;
+constexpr int T_AF = 56, T_RA2F = 57, T_ABV2 = 58, T_ABV3 = 59;
+constexpr int TAPE = 60;
 constexpr int T_LEAN = 23;   // the values up to here: those that cost the most to re-evaluate
 
 struct TapeNone {
@@ -265,26 +269,30 @@ AFVM_HD void conservative(const Phys& P, const R* U, R T, R p, R& rho, R* rhoU, 
     rhoU[0] = U[0] * rho; rhoU[1] = U[1] * rho; rhoU[2] = U[2] * rho;
 }
 
-// interp.secondOrder for one side (adFVM/interp.py:20-28): phiC + (phiD-phiC)*lw + qw.grad
+// interp.secondOrder for one side (adFVM/interp.py:20-28): phiC + (phiD-phiC)*lw + qw.grad,
+// as one chain of FMAs
 template <typename R>
 AFVM_HD R recon(R phiC, R phiD, const R* g, R lw, const R* qw) {
     R phiF = phiC + (phiD - phiC) * lw;
-    return phiF + (qw[0] * g[0] + qw[1] * g[1] + qw[2] * g[2]);
+    return qw[2] * g[2] + (qw[1] * g[1] + (qw[0] * g[0] + phiF));
 }
 
 // riemann.eulerRoe (adFVM/riemann.py:21-70). Divisions become products with shared
-// reciprocals; rhoUn/rho is Un (the same number in exact arithmetic).
+// reciprocals; rhoUn/rho is Un (the same number in exact arithmetic). With rho = p / (Rg T)
+// (conservative()), the enthalpy g p / ((g-1) rho) + |U|^2/2 is Cp T + |U|^2/2 and the sound
+// speed sqrt(g p / rho) is sqrt(g Rg T): the same numbers in exact arithmetic, without 1/rho.
 template <typename R, typename Sink = TapeNone>
-AFVM_HD void roe(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR,
+AFVM_HD void roe(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R* UR, R rhoL, R rhoR,
                  const R* N, R* F, Sink&& tp = Sink()) {
-    const R g = consts<R>(P).gamma, gm1 = consts<R>(P).gm1, ggm1 = consts<R>(P).ggm1;
+    const R gm1 = consts<R>(P).gm1, Cp = consts<R>(P).Cp;
     R UnL = dot3(UL, N), UnR = dot3(UR, N);
+    tp.put(T_UNL, UnL);
+    tp.put(T_UNR, UnR);
     R rhoUnL = rhoL * UnL, rhoUnR = rhoR * UnR;
-    R rrL = rcp(rhoL), rrR = rcp(rhoR);
-    tp.put(T_RRL, rrL);
-    tp.put(T_RRR, rrR);
-    R hL = ggm1 * pL * rrL + R(0.5) * dot3(UL, UL);
-    R hR = ggm1 * pR * rrR + R(0.5) * dot3(UR, UR);
+    tp.put(T_RUNL, rhoUnL);
+    tp.put(T_RUNR, rhoUnR);
+    R hL = Cp * TL + R(0.5) * dot3(UL, UL);
+    R hR = Cp * TR + R(0.5) * dot3(UR, UR);
     tp.put(T_HL, hL);
     tp.put(T_HR, hR);
     R fr = R(0.5) * (rhoUnL + rhoUnR);
@@ -296,6 +304,8 @@ AFVM_HD void roe(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R 
     R rD = rcp(sL + sR);
     tp.put(T_RSL, rsL);
     tp.put(T_RSR, rsR);
+    tp.put(T_SL, sL);
+    tp.put(T_SR, sR);
     tp.put(T_RD, rD);
     for (int k = 0; k < 3; k++) UF[k] = (UL[k] * sL + UR[k] * sR) * rD;
     R hF = (hL * sL + hR * sR) * rD;
@@ -305,6 +315,8 @@ AFVM_HD void roe(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R 
     tp.put(T_RAF, raF);
     R aF = a2F * raF;
     R ra2F = raF * raF;
+    tp.put(T_AF, aF);
+    tp.put(T_RA2F, ra2F);
     R UnF = dot3(UF, N);
     R drho = rhoR - rhoL;
     for (int k = 0; k < 3; k++) dU[k] = rhoR * UR[k] - rhoL * UL[k];
@@ -315,12 +327,14 @@ AFVM_HD void roe(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R 
     tp.put(T_UNF, UnF);
     tp.put(T_DRHOE, drhoE);
     R lam1 = fabs(UnF), lam2 = fabs(UnF + aF), lam3 = fabs(UnF - aF);
-    // sound speeds c = sqrt(g p / rho) as c^2 / c with the reciprocal kept for the VJP
-    R c2L = g * pL * rrL, c2R = g * pR * rrR;
+    // sound speeds c = sqrt(g Rg T) as c^2 / c with the reciprocal kept for the VJP
+    R c2L = consts<R>(P).gRg * TL, c2R = consts<R>(P).gRg * TR;
     R rcL = rsqrt_(c2L), rcR = rsqrt_(c2R);
     tp.put(T_RCL, rcL);
     tp.put(T_RCR, rcR);
     R cL = c2L > R(0) ? c2L * rcL : R(0), cR = c2R > R(0) ? c2R * rcR : R(0);
+    tp.put(T_CL, cL);
+    tp.put(T_CR, cR);
     R eps = R(0.5) * fabs(UnL - UnR);
     eps = eps + R(0.5) * fabs(cL - cR);
     eps = (eps < R(0)) ? eps - consts<R>(P).small : eps + consts<R>(P).small;
@@ -344,6 +358,8 @@ AFVM_HD void roe(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R 
     R abv5 = UnF * drho - dot3(dU, N);
     R abv6 = abv3 * abv4 * ra2F - abv2 * abv5 * raF;
     R abv7 = abv3 * abv5 - abv2 * abv4 * raF;
+    tp.put(T_ABV2, abv2);
+    tp.put(T_ABV3, abv3);
     tp.put(T_ABV4, abv4);
     tp.put(T_ABV5, abv5);
     tp.put(T_ABV6, abv6);
@@ -355,20 +371,20 @@ AFVM_HD void roe(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R 
 
 // riemann.eulerLaxFriedrichs (adFVM/riemann.py:6-18)
 template <typename R, typename Sink = TapeNone>
-AFVM_HD void laxf(const Phys& P, R pL, R pR, const R* UL, const R* UR, R rhoL, R rhoR,
-                                     const R* rhoUL, const R* rhoUR, R rhoEL, R rhoER, const R* N, R* F,
-                                     Sink&& tp = Sink()) {
-    const R g = consts<R>(P).gamma;
+AFVM_HD void laxf(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R* UR, R rhoL, R rhoR,
+                  const R* rhoUL, const R* rhoUR, R rhoEL, R rhoER, const R* N, R* F, Sink&& tp = Sink()) {
     R UnL = dot3(UL, N), UnR = dot3(UR, N);
-    R rrL = rcp(rhoL), rrR = rcp(rhoR);
-    R c2L = g * pL * rrL, c2R = g * pR * rrR;
+    // c = sqrt(g p / rho) = sqrt(g Rg T) (roe())
+    R c2L = consts<R>(P).gRg * TL, c2R = consts<R>(P).gRg * TR;
     R rcL = rsqrt_(c2L), rcR = rsqrt_(c2R);
-    tp.put(T_RRL, rrL);
-    tp.put(T_RRR, rrR);
+    tp.put(T_UNL, UnL);
+    tp.put(T_UNR, UnR);
     tp.put(T_RCL, rcL);
     tp.put(T_RCR, rcR);
     R cL = c2L > R(0) ? c2L * rcL : R(0);
     R cR = c2R > R(0) ? c2R * rcR : R(0);
+    tp.put(T_CL, cL);
+    tp.put(T_CR, cR);
     R aF = fmax(fabs(UnL) + cL, fabs(UnR) + cR);
     R ha = R(0.5) * aF;
     F[0] = R(0.5) * (rhoL * UnL + rhoR * UnR) - ha * (rhoR - rhoL);
