@@ -49,8 +49,6 @@ AFVM_HD void zero_geo(GeoBar<R>& g) {
     for (int k = 0; k < 15; k++) p[k] = R(0);
 }
 
-template <typename R>
-AFVM_HD R sgn(R x) { return (x > R(0)) ? R(1) : ((x < R(0)) ? R(-1) : R(0)); }
 
 // the gauge-form face flux: as face_flux below, from gauge offsets of p and T (the viscous
 // terms use T only through differences and mu(T_F), T_F absolute)
@@ -258,7 +256,7 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R
         drhoE = (hR * rhoR - pR) - (hL * rhoL - pL);
         eps = h * fabs(ea);
         eps = eps + h * fabs(eb_);
-        eps = (eps < R(0)) ? eps - consts<R>(P).small : eps + consts<R>(P).small;
+        eps = eps + consts<R>(P).small;      // eps >= 0 (roe())
     }
     R aF, ra2F;
     if constexpr (Src::kFull) {
@@ -270,7 +268,7 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R
     }
     R l1 = fabs(UnF), l2 = fabs(UnF + aF), l3 = fabs(UnF - aF);
     R eps2 = R(2) * eps;
-    bool s1 = l1 < eps2, s2 = l2 < eps2, s3 = l3 < eps2;
+    bool s1 = lt_nonneg(l1, eps2), s2 = lt_nonneg(l2, eps2), s3 = lt_nonneg(l3, eps2);
     if constexpr (!Src::kFull) {
         L1 = s1 ? R(0.25) * l1 * l1 * re + eps : l1;
         L2 = s2 ? R(0.25) * l2 * l2 * re + eps : l2;
@@ -290,20 +288,20 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R
         abv6 = abv3 * abv4 * ra2F - abv2 * abv5 * raF;
         abv7 = abv3 * abv5 - abv2 * abv4 * raF;
     }
-    // ---- reverse
-    R Fu[3] = {Fb[1], Fb[2], Fb[3]};
-    R frb = Fb[0], feb = Fb[4];
-    R L1b = -h * (Fb[0] * drho + dot3(Fu, dU) + Fb[4] * drhoE);
-    R drhob = -h * Fb[0] * L1;
+    // ---- reverse (every flux component carries a factor 1/2: G = Fbar / 2)
+    const R G0 = h * Fb[0], G4 = h * Fb[4];
+    const R Gu[3] = {h * Fb[1], h * Fb[2], h * Fb[3]};
+    R L1b = -(G0 * drho + dot3(Gu, dU) + G4 * drhoE);
+    R drhob = -G0 * L1;
     R dUb[3], UFb[3];
-    for (int k = 0; k < 3; k++) { dUb[k] = -h * Fu[k] * L1; UFb[k] = -h * Fu[k] * abv6; }
-    R drhoEb = -h * Fb[4] * L1;
-    R abv6b = -h * (Fb[0] + dot3(Fu, UF) + Fb[4] * hF);
-    R abv7b = h * (dot3(Fu, N) + Fb[4] * UnF);
+    for (int k = 0; k < 3; k++) { dUb[k] = -Gu[k] * L1; UFb[k] = -Gu[k] * abv6; }
+    R drhoEb = -G4 * L1;
+    R abv6b = -(G0 + dot3(Gu, UF) + G4 * hF);
+    R abv7b = dot3(Gu, N) + G4 * UnF;
     if constexpr (kGeo<G>)
-        for (int k = 0; k < 3; k++) geo->N[k] += h * Fu[k] * abv7;     // - (-abv7 N)/2 in F[1..3]
-    R hFb = -h * Fb[4] * abv6;
-    R UnFb = h * Fb[4] * abv7;
+        for (int k = 0; k < 3; k++) geo->N[k] += Gu[k] * abv7;     // - (-abv7 N)/2 in F[1..3]
+    R hFb = -G4 * abv6;
+    R UnFb = G4 * abv7;
     // abv7 = abv3*abv5 - abv2*abv4/aF
     R abv3b = abv7b * abv5, abv5b = abv7b * abv3, abv2b = -abv7b * abv4 * raF, abv4b = -abv7b * abv2 * raF;
     R aFb = abv7b * abv2 * abv4 * ra2F;
@@ -335,15 +333,15 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R
     if (s1) { l1b = L1b * h * l1 * re; epsb += L1b * (R(1) - R(0.25) * l1 * l1 * re * re); } else l1b = L1b;
     if (s2) { l2b = L2b * h * l2 * re; epsb += L2b * (R(1) - R(0.25) * l2 * l2 * re * re); } else l2b = L2b;
     if (s3) { l3b = L3b * h * l3 * re; epsb += L3b * (R(1) - R(0.25) * l3 * l3 * re * re); } else l3b = L3b;
-    R eab = h * epsb * sgn(ea);
-    R ebb = h * epsb * sgn(eb_);
+    R eab = mul_sgn(ea, h * epsb);
+    R ebb = mul_sgn(eb_, h * epsb);
     // c = sqrt(g Rg T): dc/dT = g Rg / (2 c)
     TLb += ebb * (h * gRg) * rcL;
     TRb += -ebb * (h * gRg) * rcR;
     // lam = |UnF|, |UnF + aF|, |UnF - aF|
-    R t2 = sgn(UnF + aF), t3 = sgn(UnF - aF);
-    UnFb += l1b * sgn(UnF) + l2b * t2 + l3b * t3;
-    aFb += l2b * t2 - l3b * t3;
+    R b2 = mul_sgn(UnF + aF, l2b), b3 = mul_sgn(UnF - aF, l3b);
+    UnFb += mul_sgn(UnF, l1b) + b2 + b3;
+    aFb += b2 - b3;
     // drhoE = (hR rhoR - pR) - (hL rhoL - pL)
     R hLb = -drhoEb * rhoL, hRb = drhoEb * rhoR;
     rhoRb += drhoEb * hR;
@@ -362,29 +360,31 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R
     hFb += gm1 * a2Fb;
     qFb += -gm1 * a2Fb;
     for (int k = 0; k < 3; k++) UFb[k] += qFb * UF[k];
-    // hF = (hL sL + hR sR)/Dn ; UF = (UL sL + UR sR)/Dn
-    hLb += hFb * sL * rD;
-    hRb += hFb * sR * rD;
-    R sLb = hFb * (hL - hF) * rD, sRb = hFb * (hR - hF) * rD;
+    // hF = hL wL + hR wR, UF = UL wL + UR wR with the weights wL = sL/(sL + sR), wR = sR/(sL + sR):
+    // d/dsL of (xL sL + xR sR)/(sL + sR) = (xL - xR) wR/(sL + sR), d/dsR = -(xL - xR) wL/(sL + sR)
+    R wL = sL * rD, wR = sR * rD;
+    hLb += hFb * wL;
+    hRb += hFb * wR;
     for (int k = 0; k < 3; k++) {
-        ULb[k] += UFb[k] * sL * rD;
-        URb[k] += UFb[k] * sR * rD;
-        sLb += UFb[k] * (UL[k] - UF[k]) * rD;
-        sRb += UFb[k] * (UR[k] - UF[k]) * rD;
+        ULb[k] += UFb[k] * wL;
+        URb[k] += UFb[k] * wR;
     }
-    rhoLb += sLb * h * rsL;
-    rhoRb += sRb * h * rsR;
+    R X = hFb * (hL - hR) + (UFb[0] * (UL[0] - UR[0]) + UFb[1] * (UL[1] - UR[1]) + UFb[2] * (UL[2] - UR[2]));
+    R Xr = X * rD;
+    // sL = rho rsL: dsL/drho = 1/(2 sqrt(rho))
+    rhoLb += (Xr * wR) * (h * rsL);
+    rhoRb += -(Xr * wL) * (h * rsR);
     // fe = (rhoUnL hL + rhoUnR hR)/2 ; fu = (rhoUnL UL + rhoUnR UR + (pL+pR) N)/2 ; fr = (rhoUnL + rhoUnR)/2
-    R rhoUnLb = h * feb * hL + h * dot3(Fu, UL) + h * frb;
-    R rhoUnRb = h * feb * hR + h * dot3(Fu, UR) + h * frb;
-    hLb += h * feb * rhoUnL;
-    hRb += h * feb * rhoUnR;
-    for (int k = 0; k < 3; k++) { ULb[k] += h * Fu[k] * rhoUnL; URb[k] += h * Fu[k] * rhoUnR; }
-    R pn = h * dot3(Fu, N);
+    R rhoUnLb = G4 * hL + dot3(Gu, UL) + G0;
+    R rhoUnRb = G4 * hR + dot3(Gu, UR) + G0;
+    hLb += G4 * rhoUnL;
+    hRb += G4 * rhoUnR;
+    for (int k = 0; k < 3; k++) { ULb[k] += Gu[k] * rhoUnL; URb[k] += Gu[k] * rhoUnR; }
+    R pn = dot3(Gu, N);
     pLb += pn;
     pRb += pn;
     if constexpr (kGeo<G>)
-        for (int k = 0; k < 3; k++) geo->N[k] += h * Fu[k] * (pL + pR);
+        for (int k = 0; k < 3; k++) geo->N[k] += Gu[k] * (pL + pR);
     // hL = Cp TL + qL/2
     TLb += hLb * Cp;
     TRb += hRb * Cp;
@@ -435,8 +435,8 @@ AFVM_HD void laxf_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const 
     rhoELb += h * Fb[4] * UnL + ha * Fb[4];
     rhoERb += h * Fb[4] * UnR - ha * Fb[4];
     R Ab = (A >= B) ? aFb : R(0), Bb = (A >= B) ? R(0) : aFb;
-    UnLb += Ab * sgn(UnL);
-    UnRb += Bb * sgn(UnR);
+    UnLb += mul_sgn(UnL, Ab);
+    UnRb += mul_sgn(UnR, Bb);
     TLb += Ab * (h * gRg) * rcL;
     TRb += Bb * (h * gRg) * rcR;
     for (int k = 0; k < 3; k++) { ULb[k] += UnLb * N[k]; URb[k] += UnRb * N[k]; }
@@ -502,15 +502,15 @@ AFVM_HD void viscous_vjp(const Phys& P, R TL, R TR, const R* UL, const R* UR, R 
                          const R* gUF, const R* D, const R* N, R rdel, const R* Fb, R& TLb, R& TRb, R* ULb, R* URb,
                          R& TFb, R* UFb, R* gTFb, R* gUFb) {
     R mu = viscosity<R>(P, TF);
-    R snT = (TR - TL) * rdel;
     R gTD = dot3(gTF, D);
+    R cT = (TR - TL) * rdel - gTD;
     R gT[3];
-    for (int k = 0; k < 3; k++) gT[k] = gTF[k] + snT * D[k] - gTD * D[k];
+    for (int k = 0; k < 3; k++) gT[k] = gTF[k] + cT * D[k];
     R gU[9];
     for (int i = 0; i < 3; i++) {
-        R snU = (UR[i] - UL[i]) * rdel;
         R gUD = gUF[3 * i] * D[0] + gUF[3 * i + 1] * D[1] + gUF[3 * i + 2] * D[2];
-        for (int k = 0; k < 3; k++) gU[3 * i + k] = gUF[3 * i + k] + snU * D[k] - gUD * D[k];
+        R cU = (UR[i] - UL[i]) * rdel - gUD;
+        for (int k = 0; k < 3; k++) gU[3 * i + k] = gUF[3 * i + k] + cU * D[k];
     }
     R tmp3 = gU[0] + gU[4] + gU[8];
     R tmp2[3], sigma[3];
@@ -583,9 +583,9 @@ AFVM_HD void corrected_gradU(const FaceIn<R>& in, bool chr, R* gU) {
     R gUF[9];
     for (int k = 0; k < 9; k++) gUF[k] = chr ? in.gUN[k] : R(0.5) * (in.gUP[k] + in.gUN[k]);
     for (int i = 0; i < 3; i++) {
-        R snU = (in.UN[i] - in.UP[i]) * in.rdelta;
         R gUD = gUF[3 * i] * in.D[0] + gUF[3 * i + 1] * in.D[1] + gUF[3 * i + 2] * in.D[2];
-        for (int k = 0; k < 3; k++) gU[3 * i + k] = gUF[3 * i + k] + snU * in.D[k] - gUD * in.D[k];
+        R cU = (in.UN[i] - in.UP[i]) * in.rdelta - gUD;
+        for (int k = 0; k < 3; k++) gU[3 * i + k] = gUF[3 * i + k] + cU * in.D[k];
     }
 }
 
@@ -697,6 +697,13 @@ AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>&
     if (solver == AFVM_RIEMANN_ROE) {
         roe_vjp<R>(P, pLF, pRF, TLF, TRF, ULF, URF, rhoL, rhoR, in.N, Fb, t, pLFb, pRFb, TLFb, TRFb, ULFb, URFb,
                    rhoLb, rhoRb, geo);
+        // conservative(): the Roe flux uses only rho = p rd of each side (rd = 1/(Cv T (g-1)),
+        // drho/dp = rd, drho/dT = -rho/T = -rho rd (g-1) Cv)
+        const R k = consts<R>(P).gm1 * consts<R>(P).Cv;
+        pLFb += rhoLb * rdL;
+        TLFb += -rhoLb * (rhoL * (rdL * k));
+        pRFb += rhoRb * rdR;
+        TRFb += -rhoRb * (rhoR * (rdR * k));
     } else {
         // conservative()'s rhoU and rhoE of each side
         R eL = consts<R>(P).Cv * TLF, eR = consts<R>(P).Cv * TRF;
@@ -705,9 +712,9 @@ AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>&
         for (int k = 0; k < 3; k++) { rhoUL[k] = ULF[k] * rhoL; rhoUR[k] = URF[k] * rhoR; }
         laxf_vjp<R>(P, pLF, pRF, TLF, TRF, ULF, URF, rhoL, rhoR, rhoUL, rhoUR, rhoEL, rhoER, in.N, Fb, t, pLFb, pRFb,
                     TLFb, TRFb, ULFb, URFb, rhoLb, rhoRb, rhoULb, rhoURb, rhoELb, rhoERb, geo);
+        conservative_vjp_t<R>(P, ULF, TLF, pLF, rdL, rhoLb, rhoULb, rhoELb, ULFb, TLFb, pLFb);
+        conservative_vjp_t<R>(P, URF, TRF, pRF, rdR, rhoRb, rhoURb, rhoERb, URFb, TRFb, pRFb);
     }
-    conservative_vjp_t<R>(P, ULF, TLF, pLF, rdL, rhoLb, rhoULb, rhoELb, ULFb, TLFb, pLFb);
-    conservative_vjp_t<R>(P, URF, TRF, pRF, rdR, rhoRb, rhoURb, rhoERb, URFb, TRFb, pRFb);
     // reconstruction
     if constexpr (kGeo<G>) {
         // phiF = phiC + (phiD - phiC) lw + qw.grad phiC, per side

@@ -159,6 +159,43 @@ AFVM_HD R rec_abs_p(const Phys& P, R v) {
 template <typename R>
 AFVM_HD R dot3(const R* a, const R* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
 
+// y sign(x) with sign(0) = 0 (and 0 for a NaN x, as the comparisons give). On the device it is
+// formed from the bits of x with integer operations: an FP64 compare issues on the FP64 pipe,
+// the face kernels' bound.
+template <typename R>
+AFVM_HD R mul_sgn(R x, R y) {
+#if defined(__CUDA_ARCH__)
+    if constexpr (sizeof(R) == 8) {
+        int hi = __double2hiint(x);
+        unsigned lo = (unsigned)__double2loint(x);
+        unsigned mag = (unsigned)hi & 0x7fffffffu;
+        bool zero = (mag | lo) == 0u;
+        bool nan = mag > 0x7ff00000u || (mag == 0x7ff00000u && lo != 0u);
+        double r = __hiloint2double(__double2hiint(y) ^ (hi & (int)0x80000000), __double2loint(y));
+        return (zero || nan) ? 0.0 : r;
+    } else {
+        unsigned b = __float_as_uint(x);
+        unsigned mag = b & 0x7fffffffu;
+        float r = __uint_as_float(__float_as_uint(y) ^ (b & 0x80000000u));
+        return (mag == 0u || mag > 0x7f800000u) ? 0.0f : r;
+    }
+#else
+    return (x > R(0)) ? y : ((x < R(0)) ? -y : R(0));
+#endif
+}
+
+// a < b for non-negative a, b: such floating-point numbers order like their bit patterns, so
+// the device compares them as integers (no FP64 compare)
+template <typename R>
+AFVM_HD bool lt_nonneg(R a, R b) {
+#if defined(__CUDA_ARCH__)
+    if constexpr (sizeof(R) == 8) return __double_as_longlong(a) < __double_as_longlong(b);
+    else return __float_as_int(a) < __float_as_int(b);
+#else
+    return a < b;
+#endif
+}
+
 // ---- reciprocal and reciprocal square root
 //
 // On the GB300 the FP64 pipe runs at 1/57 of the FP32 rate, and an IEEE FP64 division or
@@ -247,9 +284,20 @@ AFVM_HD float rsqrt_(float x) {
 #endif
 }
 
-// sqrt(x) for x >= 0 as x / sqrt(x)
+// x > 0 from the bits (true for +inf and a positive NaN): no FP64 compare on the device
 template <typename R>
-AFVM_HD R sqrt_(R x) { return x > R(0) ? x * rsqrt_(x) : R(0); }
+AFVM_HD bool pos_(R x) {
+#if defined(__CUDA_ARCH__)
+    if constexpr (sizeof(R) == 8) return __double_as_longlong(x) > 0;
+    else return __float_as_int(x) > 0;
+#else
+    return x > R(0);
+#endif
+}
+
+// sqrt(x) for x >= 0 as x / sqrt(x) (0 for x <= 0)
+template <typename R>
+AFVM_HD R sqrt_(R x) { return pos_(x) ? x * rsqrt_(x) : R(0); }
 
 // mu(T): constant, or Sutherland 1.4792e-06*T**1.5/(T+116.) (adFVM/density.py:27)
 template <typename R>
@@ -332,19 +380,22 @@ AFVM_HD void roe(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R* UR
     R rcL = rsqrt_(c2L), rcR = rsqrt_(c2R);
     tp.put(T_RCL, rcL);
     tp.put(T_RCR, rcR);
-    R cL = c2L > R(0) ? c2L * rcL : R(0), cR = c2R > R(0) ? c2R * rcR : R(0);
+    R cL = pos_(c2L) ? c2L * rcL : R(0), cR = pos_(c2R) ? c2R * rcR : R(0);
     tp.put(T_CL, cL);
     tp.put(T_CR, cR);
+    // the entropy-fix width; eps >= 0 (a sum of magnitudes), so the reference's
+    // eps < 0 ? eps - small : eps + small is eps + small
     R eps = R(0.5) * fabs(UnL - UnR);
     eps = eps + R(0.5) * fabs(cL - cR);
-    eps = (eps < R(0)) ? eps - consts<R>(P).small : eps + consts<R>(P).small;
+    eps = eps + consts<R>(P).small;
     R eps2 = R(2) * eps;
     R re = R(0);
-    if (lam1 < eps2 || lam2 < eps2 || lam3 < eps2) {
+    bool s1 = lt_nonneg(lam1, eps2), s2 = lt_nonneg(lam2, eps2), s3 = lt_nonneg(lam3, eps2);
+    if (s1 || s2 || s3) {
         re = rcp(eps);
-        if (lam1 < eps2) lam1 = R(0.25) * lam1 * lam1 * re + eps;
-        if (lam2 < eps2) lam2 = R(0.25) * lam2 * lam2 * re + eps;
-        if (lam3 < eps2) lam3 = R(0.25) * lam3 * lam3 * re + eps;
+        if (s1) lam1 = R(0.25) * lam1 * lam1 * re + eps;
+        if (s2) lam2 = R(0.25) * lam2 * lam2 * re + eps;
+        if (s3) lam3 = R(0.25) * lam3 * lam3 * re + eps;
     }
     tp.put(T_RE, re);
     tp.put(T_EPS, eps);
@@ -381,8 +432,8 @@ AFVM_HD void laxf(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R* U
     tp.put(T_UNR, UnR);
     tp.put(T_RCL, rcL);
     tp.put(T_RCR, rcR);
-    R cL = c2L > R(0) ? c2L * rcL : R(0);
-    R cR = c2R > R(0) ? c2R * rcR : R(0);
+    R cL = pos_(c2L) ? c2L * rcL : R(0);
+    R cR = pos_(c2R) ? c2R * rcR : R(0);
     tp.put(T_CL, cL);
     tp.put(T_CR, cR);
     R aF = fmax(fabs(UnL) + cL, fabs(UnR) + cR);
@@ -459,13 +510,14 @@ AFVM_HD void roe_gauge(const Phys& P, R pgL, R pgR, R TgL, R TgR, const R* UL, c
     R cL = sqrt_(c2L), cR = sqrt_(c2R);
     R eps = R(0.5) * fabs(UnL - UnR);
     eps = eps + R(0.5) * fabs(cL - cR);
-    eps = (eps < R(0)) ? eps - Q.small : eps + Q.small;
+    eps = eps + Q.small;                     // eps >= 0 (roe())
     R eps2 = R(2) * eps;
-    if (lam1 < eps2 || lam2 < eps2 || lam3 < eps2) {
+    bool s1 = lt_nonneg(lam1, eps2), s2 = lt_nonneg(lam2, eps2), s3 = lt_nonneg(lam3, eps2);
+    if (s1 || s2 || s3) {
         R re = rcp(eps);
-        if (lam1 < eps2) lam1 = R(0.25) * lam1 * lam1 * re + eps;
-        if (lam2 < eps2) lam2 = R(0.25) * lam2 * lam2 * re + eps;
-        if (lam3 < eps2) lam3 = R(0.25) * lam3 * lam3 * re + eps;
+        if (s1) lam1 = R(0.25) * lam1 * lam1 * re + eps;
+        if (s2) lam2 = R(0.25) * lam2 * lam2 * re + eps;
+        if (s3) lam3 = R(0.25) * lam3 * lam3 * re + eps;
     }
     R abv1 = R(0.5) * (lam2 + lam3);
     R abv2 = R(0.5) * (lam2 - lam3);
@@ -506,15 +558,16 @@ AFVM_HD void viscous(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, 
     R mu = viscosity<R>(P, TF);
     tp.put(T_MU, mu);
     R kappa = mu * consts<R>(P).kFac;
-    R snT = (TR - TL) * rdel;
+    // the face gradient with its normal component replaced by snGrad: g + (snGrad - g.D) D
     R gTD = dot3(gTF, D);
+    R cT = (TR - TL) * rdel - gTD;
     R gT[3];
-    for (int k = 0; k < 3; k++) gT[k] = gTF[k] + snT * D[k] - gTD * D[k];
+    for (int k = 0; k < 3; k++) gT[k] = gTF[k] + cT * D[k];
     R gU[9];
     for (int i = 0; i < 3; i++) {
-        R snU = (UR[i] - UL[i]) * rdel;
         R gUD = gUF[3 * i] * D[0] + gUF[3 * i + 1] * D[1] + gUF[3 * i + 2] * D[2];
-        for (int k = 0; k < 3; k++) gU[3 * i + k] = gUF[3 * i + k] + snU * D[k] - gUD * D[k];
+        R cU = (UR[i] - UL[i]) * rdel - gUD;
+        for (int k = 0; k < 3; k++) gU[3 * i + k] = gUF[3 * i + k] + cU * D[k];
     }
     R gTn = dot3(gT, N);
     tp.put(T_GTN, gTn);
