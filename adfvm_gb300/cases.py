@@ -243,6 +243,16 @@ def source_field(mesh, scale=1.0, seed=5):
     return (G.copy(), S_rhoU, 2e5 * G)
 
 
+def gauge(case):
+    """A gauge state for the FP32 records of the case's contexts (RCF(gauge=...)): the mean
+    initial pressure, temperature and total enthalpy Cp T + |U|^2/2 - for a case whose boundary
+    conditions fix no p or T (a periodic box), whose contexts would otherwise have none."""
+    U = np.asarray(case.U, np.float64).reshape(-1, 3)
+    T = np.asarray(case.T, np.float64).reshape(-1)
+    p = np.asarray(case.p, np.float64).reshape(-1)
+    return (float(p.mean()), float(T.mean()), float((CP * T + 0.5 * (U * U).sum(axis=1)).mean()))
+
+
 def copies(case, K):
     """The case on K disjoint copies of its mesh (meshgen.copies): boundary values and the
     initial primitive fields repeated per copy, the same options, objective and dt."""

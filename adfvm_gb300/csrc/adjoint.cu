@@ -34,17 +34,18 @@ __device__ __forceinline__ void adj_face(const MeshDev<R>& m, const Phys& P, con
                                          const R* __restrict__ tape) {
     int kind = (f < m.nIF) ? FACE_INTERNAL : (int)m.fkind[f - m.nIF];
     int iP = m.own[f];
-    R wp = m.wpf[f];
+    // Fbar = coef (abar_P A/V_L - abar_N A/V_R), coef folded into the two weights
+    R wp = coef * m.wpf[f];
     R Fb[5];
-    Fb[0] = (coef * R(ar[iP])) * wp;
-    for (int k = 0; k < 3; k++) Fb[1 + k] = (coef * R(au[3 * iP + k])) * wp;
-    Fb[4] = (coef * R(ae[iP])) * wp;
+    Fb[0] = R(ar[iP]) * wp;
+    for (int k = 0; k < 3; k++) Fb[1 + k] = R(au[3 * iP + k]) * wp;
+    Fb[4] = R(ae[iP]) * wp;
     if (f < m.nIF) {
         int iN = m.nbr[f];
-        R wn = m.wnf[f];
-        Fb[0] = Fb[0] - (coef * R(ar[iN])) * wn;
-        for (int k = 0; k < 3; k++) Fb[1 + k] = Fb[1 + k] - (coef * R(au[3 * iN + k])) * wn;
-        Fb[4] = Fb[4] - (coef * R(ae[iN])) * wn;
+        R wn = coef * m.wnf[f];
+        Fb[0] = Fb[0] - R(ar[iN]) * wn;
+        for (int k = 0; k < 3; k++) Fb[1 + k] = Fb[1 + k] - R(au[3 * iN + k]) * wn;
+        Fb[4] = Fb[4] - R(ae[iN]) * wn;
     }
     FaceIn<R> in;
     FaceBar<R> b;

@@ -303,15 +303,17 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R
     R hFb = -G4 * abv6;
     R UnFb = G4 * abv7;
     // abv7 = abv3*abv5 - abv2*abv4/aF
-    R abv3b = abv7b * abv5, abv5b = abv7b * abv3, abv2b = -abv7b * abv4 * raF, abv4b = -abv7b * abv2 * raF;
-    R aFb = abv7b * abv2 * abv4 * ra2F;
+    R b7r = abv7b * raF;
+    R abv3b = abv7b * abv5, abv5b = abv7b * abv3, abv2b = -b7r * abv4, abv4b = -b7r * abv2;
+    R aFb = (b7r * raF) * (abv2 * abv4);
     // abv6 = abv3*abv4/a2F - abv2*abv5/aF
-    abv3b += abv6b * abv4 * ra2F;
-    abv4b += abv6b * abv3 * ra2F;
-    R a2Fb = -abv6b * abv3 * abv4 * ra2F * ra2F;
-    abv2b += -abv6b * abv5 * raF;
-    abv5b += -abv6b * abv2 * raF;
-    aFb += abv6b * abv2 * abv5 * ra2F;
+    R b6q = abv6b * ra2F, b6r = abv6b * raF;
+    abv3b += b6q * abv4;
+    abv4b += b6q * abv3;
+    R a2Fb = -(b6q * ra2F) * (abv3 * abv4);
+    abv2b += -b6r * abv5;
+    abv5b += -b6r * abv2;
+    aFb += (b6r * raF) * (abv2 * abv5);
     // abv5 = UnF*drho - dU.N
     UnFb += abv5b * drho;
     drhob += abv5b * UnF;
@@ -356,9 +358,10 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R
     for (int k = 0; k < 3; k++) UFb[k] += UnFb * N[k];
     if constexpr (kGeo<G>)
         for (int k = 0; k < 3; k++) geo->N[k] += UnFb * UF[k];
-    a2Fb += aFb * h * raF;
-    hFb += gm1 * a2Fb;
-    qFb += -gm1 * a2Fb;
+    a2Fb += aFb * (h * raF);
+    R g2 = gm1 * a2Fb;
+    hFb += g2;
+    qFb += -g2;
     for (int k = 0; k < 3; k++) UFb[k] += qFb * UF[k];
     // hF = hL wL + hR wR, UF = UL wL + UR wR with the weights wL = sL/(sL + sR), wR = sR/(sL + sR):
     // d/dsL of (xL sL + xR sR)/(sL + sR) = (xL - xR) wR/(sL + sR), d/dsR = -(xL - xR) wL/(sL + sR)
@@ -460,12 +463,12 @@ AFVM_HD void viscous_vjp_t(const Phys& P, R TF, const R* UF, R mu, R gTn, const 
     R qFb = -Fb[4];
     R mub = R(0);
     R tmp2b[3];
-    R tmp3b = R(0);
+    R c23 = R(2.0 / 3) * tmp3;
     for (int i = 0; i < 3; i++) {
-        mub += sb[i] * (tmp2[i] - R(2.0 / 3) * tmp3 * N[i]);
+        mub += sb[i] * (tmp2[i] - c23 * N[i]);
         tmp2b[i] = sb[i] * mu;
-        tmp3b += -R(2.0 / 3) * mu * sb[i] * N[i];
     }
+    R tmp3b = (-R(2.0 / 3) * mu) * dot3(sb, N);
     R kappab = qFb * gTn;
     R gTb[3];
     for (int k = 0; k < 3; k++) gTb[k] = qFb * kappa * N[k];

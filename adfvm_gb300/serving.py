@@ -121,8 +121,10 @@ class Slot(object):
         self.nPrimal = nPrimal
         self.nck = nPrimal // k
         self.dev = torch.device('cuda', device)
+        # FP32 records: the gauge of the case's initial field (the far field's on a cylinder, the
+        # mean state of a periodic box, which fixes no boundary value)
         self.rcf = RCF(case.mesh, case.bc, objective=case.objective, precision=precision, device=device,
-                       **case.config)
+                       gauge=None if precision == 'fp64' else cases.gauge(case), **case.config)
         self.td = torch.float32 if precision == 'fp32' else torch.float64      # state type
         n = case.mesh.nInternalCells
         shapes = [(n, 1), (n, 3), (n, 1)]
@@ -309,7 +311,7 @@ class SensitivityServer(object):
         # per face: tables, flux records, adjoint face records (and FP64 face tapes); per cell:
         # tables and cell records, RK and adjoint work states, checkpoints, interval states,
         # stage buffers and the tapes' cell records
-        face_tape = 3 * 50 * 8 * self.k if self.precision == 'fp64' else 0
+        face_tape = 3 * 60 * 8 * self.k if self.precision == 'fp64' else 0
         return int(m.nFaces * (60 + 28 * er + 40 * er + face_tape) + m.nInternalCells * (150 + 40 * er + 40 * es
                    + (self.nPrimal // self.k + 3 * self.k + 8) * 5 * es) + m.nCells * 3 * 20 * er * self.k)
 
