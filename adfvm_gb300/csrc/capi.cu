@@ -98,7 +98,7 @@ struct HostTables {
     std::vector<int32_t> gnb, accf;
     std::vector<double> gw, gsn, rvol, accw, vol;
     // adjoint
-    std::vector<double> wpf, wnf, gwb, gA, gws, gAv, gbs;
+    std::vector<double> wpf, wnf, gwb, gA, gws, gAv, gbs, gcl;
     std::vector<int32_t> gsStart, gsList, gslot;
 };
 
@@ -145,6 +145,8 @@ int upload_mesh(Ctx* c, const HostTables& h, MeshDev<R>& m) {
     if ((st = upload(c, &m.gws, cast<R>(h.gws)))) return st;
     if ((st = upload(c, &m.gAv, cast<R>(h.gAv)))) return st;
     if ((st = upload(c, &m.gbs, cast<R>(h.gbs)))) return st;
+    if ((st = upload(c, &m.gcl, cast<R>(h.gcl)))) return st;
+    if ((st = upload(c, &m.gclD, h.gcl))) return st;
     if ((st = upload(c, &m.gsStart, h.gsStart))) return st;
     if ((st = upload(c, &m.gsList, h.gsList))) return st;
     if ((st = upload(c, &m.gslot, h.gslot))) return st;
@@ -363,9 +365,15 @@ int build_tables(Ctx* c, const afvm_mesh_tensors* M, const afvm_patch_bc* bcs, H
     h.gws.assign(18 * n, 0.0);
     h.gAv.assign(3 * n, 0.0);
     h.gbs.assign(18 * n, 0.0);
+    h.gcl.assign(3 * n, 0.0);
 #pragma omp parallel for
     for (int ci = 0; ci < nIC; ci++) {
-        for (int k = 0; k < 3; k++) h.gAv[k * n + ci] = h.gA[k * n + ci] * h.rvol[ci];
+        for (int k = 0; k < 3; k++) {
+            h.gAv[k * n + ci] = h.gA[k * n + ci] * h.rvol[ci];
+            double a = 0.0;
+            for (int s = 0; s < 6; s++) a += h.gsn[(3 * s + k) * n + ci];
+            h.gcl[k * n + ci] = a * h.rvol[ci];
+        }
         for (int s = 0; s < 6; s++) {
             int nb = h.gnb[s * n + ci];
             for (int k = 0; k < 3; k++) {

@@ -99,6 +99,11 @@ struct MeshDev {
     const R* gws;             // 3 x 6 x nIC: w' S N' / V
     const R* gAv;             // 3 x nIC: gA / V
     const R* gbs;             // 3 x 6 x nIC: -gwb S N' / V_nb (internal neighbours; 0 for ghosts)
+    // 3 x nIC: sum over the cell's faces of S N' / V (= sum of A/V N, outward): zero for a cell
+    // whose face area vectors close, not for cells with warped faces, whose normals come from
+    // three of their points; in the record type and in double (the FP32 gauge terms)
+    const R* gcl;
+    const double* gclD;
     const int32_t* gsStart;   // nIC + 1: ghosts whose source is the cell, CSR offsets
     const int32_t* gsList;    // nG ghost ids ordered by source cell
     const int32_t* gslot;     // nG: slot of the ghost's face in its owner's cellFaces

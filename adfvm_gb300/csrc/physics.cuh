@@ -92,12 +92,14 @@ struct PhysR {
 
 // FP32 cell records hold the pressure and temperature as offsets from a gauge state,
 // p - gaugeP and T - gaugeT, and the FP32 face fluxes carry the momentum flux without
-// gaugeP N and the energy flux less gaugeH times the mass flux (the update adds gaugeH times
-// the mass residual back; gaugeP N sums to zero over the faces of a closed cell, whose face
-// area vectors sum to zero). In a low-Mach flow the pressure (1e5 Pa) varies by ~1e2 Pa: a
-// float holding p keeps four digits of those variations, a float holding p - gaugeP keeps all
-// seven, and the face sums no longer round values 1e3 times larger than their result. FP64
-// records hold the absolute values (gauge unused).
+// gaugeP N and the energy flux less gaugeH times the mass flux. The update adds gaugeH times
+// the mass residual and gaugeP times the cell's sum of A/V N back, and the gradient kernel
+// gaugeT and gaugeP times that sum (it vanishes when a cell's face area vectors close, but
+// the reference takes a face's normal from three of its points, so warped faces leave it
+// nonzero). In a low-Mach flow the pressure (1e5 Pa) varies by ~1e2 Pa: a float holding p
+// keeps four digits of those variations, a float holding p - gaugeP keeps all seven, and the
+// face sums no longer round values 1e3 times larger than their result. FP64 records hold the
+// absolute values (gauge unused).
 struct Phys {
     double gamma, gm1, Cp, Cv, rCv, kFac, mu0, muAs, muTs, small;
     int muModel, riemann, briemann;

@@ -140,7 +140,8 @@ __global__ void __launch_bounds__(BLOCK) k_prim(MeshDev<R> m, Phys P, const S* _
 }
 
 template <typename R>
-__device__ __forceinline__ void grad_cell(const MeshDev<R>& m, const R* __restrict__ rec, int c, R* row) {
+__device__ __forceinline__ void grad_cell(const MeshDev<R>& m, const Phys& P, const R* __restrict__ rec, int c,
+                                          R* row) {
     // the five primitives of a record as one 16-byte load and a scalar (records are 16-byte
     // aligned)
     R phic[5];
@@ -166,6 +167,15 @@ __device__ __forceinline__ void grad_cell(const MeshDev<R>& m, const R* __restri
         for (int i = 0; i < 5; i++)
             for (int j = 0; j < 3; j++) g[3 * i + j] = g[3 * i + j] + rn[i] * ws[j];
     }
+    if constexpr (kGauge<R>) {
+        // FP32 records hold T - gT, p - gP: the gradient of the constant offsets is the offset
+        // times the cell's sum of S N'/V, which warped faces leave nonzero
+        R cl[3] = {m.gcl[c], m.gcl[n + c], m.gcl[2 * n + c]};
+        for (int j = 0; j < 3; j++) {
+            g[9 + j] = g[9 + j] + consts<R>(P).gT * cl[j];
+            g[12 + j] = g[12 + j] + consts<R>(P).gP * cl[j];
+        }
+    }
     R v[REC];
     for (int k = 0; k < 5; k++) v[k] = phic[k];
     for (int k = 0; k < 15; k++) v[R_GU + k] = g[k];
@@ -178,11 +188,11 @@ __device__ __forceinline__ void grad_cell(const MeshDev<R>& m, const R* __restri
 // from its own record and written back unchanged), so every read sees the same value whether
 // it lands before or after the store.
 template <typename R>
-__global__ void __launch_bounds__(BLOCK) k_grad(MeshDev<R> m, R* __restrict__ rec) {
+__global__ void __launch_bounds__(BLOCK) k_grad(MeshDev<R> m, Phys P, R* __restrict__ rec) {
     __shared__ __align__(16) R stage[BLOCK * REC];
     const int c0 = blockIdx.x * BLOCK;
     const int c = c0 + threadIdx.x;
-    if (c < m.nIC) grad_cell<R>(m, rec, c, stage + threadIdx.x * REC);
+    if (c < m.nIC) grad_cell<R>(m, P, rec, c, stage + threadIdx.x * REC);
     __syncthreads();
     if (c0 < m.nIC) store_staged<R, REC, BLOCK>(rec, c0, min(BLOCK, m.nIC - c0), stage);
 }
@@ -270,8 +280,13 @@ __global__ void __launch_bounds__(BLOCK) k_update(MeshDev<R> m, const R* __restr
         S rs[5];
         for (int q = 0; q < 5; q++) rs[q] = S(res[q]);
         // gauge-form fluxes (FP32): the energy residual is the gathered one plus gaugeH times
-        // the mass residual, added in the state's type
-        if constexpr (kGauge<R>) rs[4] = rs[4] + S(P.gaugeH) * rs[0];
+        // the mass residual, the momentum residual the gathered one plus gaugeP times the
+        // cell's sum of A/V N (the gaugeP N the face fluxes leave out; zero when the cell's
+        // face area vectors close), both added in the state's type
+        if constexpr (kGauge<R>) {
+            rs[4] = rs[4] + S(P.gaugeH) * rs[0];
+            for (int k = 0; k < 3; k++) rs[1 + k] = rs[1 + k] + S(P.gaugeP) * S(m.gclD[k * n + c]);
+        }
         S Sv[5] = {Sr[c], Su[3 * c], Su[3 * c + 1], Su[3 * c + 2], Se[c]};
         S a[5] = {u0r[c], u0u[3 * c], u0u[3 * c + 1], u0u[3 * c + 2], u0e[c]};
         S o[5];
@@ -473,7 +488,7 @@ void launch_prim_grad(Ctx* c, const S* r, const S* ru, const S* re, cudaStream_t
     launch_prim<R, S>(c, r, ru, re, s, rec);
     {
         ProfScope ps(c, KID_GRAD, s);
-        k_grad<R><<<nblocks(m.nIC), BLOCK, 0, s>>>(m, rec);
+        k_grad<R><<<nblocks(m.nIC), BLOCK, 0, s>>>(m, c->phys, rec);
     }
 }
 
@@ -557,7 +572,7 @@ int primal_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double d
         } else {
             // the primitives of stages 1 and 2 were written by the previous stage's update
             ProfScope ps(c, KID_GRAD, s);
-            k_grad<R><<<nblocks(m.nIC), BLOCK, 0, s>>>(m, recs[st]);
+            k_grad<R><<<nblocks(m.nIC), BLOCK, 0, s>>>(m, c->phys, recs[st]);
         }
         if (st == 1 && c->objSink) {
             // the objective stage's primitives U (3), T, p of every cell, ghosts included, for an

@@ -65,6 +65,34 @@ def test_gauge_brings_mixed_closer_to_fp64():
 
 
 @pytest.mark.parametrize('precision', ['fp32', 'mixed'])
+def test_gauge_on_warped_faces(precision):
+    """The jittered periodic box, whose warped faces leave each cell's sum of A N nonzero (the
+    reference takes a face's normal from three of its points): with the gauge of its initial
+    field, 20 steps and an adjoint step stay as close to FP64 as without one."""
+    case = cases.box(16, objective='kinetic_energy')
+    mesh = case.build_mesh()
+    x = [torch.as_tensor(np.asarray(a).reshape(mesh.nInternalCells, -1)) for a in cases.conservative(case)]
+
+    def run(prec, gauge):
+        r = RCF(mesh, case.bc, objective=case.objective, precision=prec, gauge=gauge, **case.config)
+        td = torch.float32 if r.dtype == np.float32 else torch.float64
+        y = [t.to(td).cuda() for t in x]
+        for _ in range(20):
+            y = list(r.step(y[0], y[1], y[2], case.dt)[:3])
+        a = r.adjoint_step(y[0], y[1], y[2], case.dt, [torch.ones_like(t) for t in y], obja=1.0)
+        out = [t.double().cpu().numpy() for t in y] + [t.double().cpu().numpy() for t in a[:3]]
+        r.close()
+        return out
+
+    ref = run('fp64', None)
+    g = run(precision, cases.gauge(case))
+    assert cases.gauge(case)[0] > 1e5
+    for i in range(6):
+        e = np.abs(g[i] - ref[i]).max() / np.abs(ref[i]).max()
+        assert e <= 1e-5, 'field %d: rel err %.3e' % (i, e)
+
+
+@pytest.mark.parametrize('precision', ['fp32', 'mixed'])
 def test_values_leaving_the_records_are_absolute(precision):
     case, mesh, x = _cyl()
     a = RCF(mesh, case.bc, objective=case.objective, **case.config)
