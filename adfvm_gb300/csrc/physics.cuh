@@ -186,6 +186,23 @@ AFVM_HD R mul_sgn(R x, R y) {
 #endif
 }
 
+// a * b rounded on its own, never contracted into an FMA: sums of such products cancel exactly
+// where their terms do (a uniform field's face fluxes in the cell gather)
+AFVM_HD double mul_rn(double a, double b) {
+#if defined(__CUDA_ARCH__)
+    return __dmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+AFVM_HD float mul_rn(float a, float b) {
+#if defined(__CUDA_ARCH__)
+    return __fmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+
 // a < b for non-negative a, b: such floating-point numbers order like their bit patterns, so
 // the device compares them as integers (no FP64 compare)
 template <typename R>

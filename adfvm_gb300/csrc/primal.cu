@@ -271,10 +271,11 @@ __global__ void __launch_bounds__(BLOCK) k_update(MeshDev<R> m, const R* __restr
             int f = ownerSide ? e : ~e;
             R F[FREC];
             load_flux_record(fflux + (size_t)f * FREC, F);
-            for (int q = 0; q < 5; q++) {
-                R t = F[q] * w;
-                res[q] = res[q] + (ownerSide ? t : -t);
-            }
+            // the side's sign on the weight (one select a face, not one a term); each product
+            // rounded before it is added, as the reference's collate sum does, so that equal
+            // and opposite terms cancel exactly
+            R ws = ownerSide ? w : -w;
+            for (int q = 0; q < 5; q++) res[q] = res[q] + mul_rn(F[q], ws);
             dtc = dtc + F[5] * w;
         }
         S rs[5];
@@ -285,22 +286,26 @@ __global__ void __launch_bounds__(BLOCK) k_update(MeshDev<R> m, const R* __restr
         // face area vectors close), both added in the state's type
         if constexpr (kGauge<R>) {
             rs[4] = rs[4] + S(P.gaugeH) * rs[0];
-            for (int k = 0; k < 3; k++) rs[1 + k] = rs[1 + k] + S(P.gaugeP) * S(m.gclD[k * n + c]);
+            // (a float state reads the float copy of the closure sums: half the bytes)
+            for (int k = 0; k < 3; k++)
+                rs[1 + k] = rs[1 + k] + S(P.gaugeP) * (sizeof(S) == 4 ? S(m.gcl[k * n + c]) : S(m.gclD[k * n + c]));
         }
         S Sv[5] = {Sr[c], Su[3 * c], Su[3 * c + 1], Su[3 * c + 2], Se[c]};
         S a[5] = {u0r[c], u0u[3 * c], u0u[3 * c + 1], u0u[3 * c + 2], u0e[c]};
         S o[5];
         const S rdt = S(dtp ? *dtp : dtv);
+        // u = sum_j alpha_j u_j - beta dt (R - S) with -beta dt formed once a cell
         if (STAGE == 0) {
-            for (int q = 0; q < 5; q++) o[q] = a[q] + (S(-1.0) * (rs[q] - Sv[q])) * rdt;
+            const S k = -rdt;
+            for (int q = 0; q < 5; q++) o[q] = a[q] + k * (rs[q] - Sv[q]);
         } else if (STAGE == 1) {
             S b[5] = {u1r[c], u1u[3 * c], u1u[3 * c + 1], u1u[3 * c + 2], u1e[c]};
-            for (int q = 0; q < 5; q++)
-                o[q] = (S(3. / 4) * a[q] + S(1. / 4) * b[q]) + (S(-(1. / 4)) * (rs[q] - Sv[q])) * rdt;
+            const S k = S(-(1. / 4)) * rdt;
+            for (int q = 0; q < 5; q++) o[q] = (S(3. / 4) * a[q] + S(1. / 4) * b[q]) + k * (rs[q] - Sv[q]);
         } else {
             S b[5] = {u2r[c], u2u[3 * c], u2u[3 * c + 1], u2u[3 * c + 2], u2e[c]};
-            for (int q = 0; q < 5; q++)
-                o[q] = (S(1. / 3) * a[q] + S(2. / 3) * b[q]) + (S(-(2. / 3)) * (rs[q] - Sv[q])) * rdt;
+            const S k = S(-(2. / 3)) * rdt;
+            for (int q = 0; q < 5; q++) o[q] = (S(1. / 3) * a[q] + S(2. / 3) * b[q]) + k * (rs[q] - Sv[q]);
         }
         outr[c] = o[0];
         outu[3 * c] = o[1]; outu[3 * c + 1] = o[2]; outu[3 * c + 2] = o[3];
