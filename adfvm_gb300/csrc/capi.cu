@@ -7,6 +7,7 @@
 // weights, density.py:390-402 accumulation order).
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <cstdint>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -809,6 +810,7 @@ int afvm_primal_step_tape(afvm_ctx* ctx, const void* rho, const void* rhoU, cons
     if (!rho || !rhoU || !rhoE || !rhoN || !rhoUN || !rhoEN) return fail(c, AFVM_ERR_BAD_ARG, "null state pointer");
     if (!std::isfinite(dt)) return fail(c, AFVM_ERR_BAD_ARG, "non-finite dt");
     if (tape && !stages) return fail(c, AFVM_ERR_BAD_ARG, "a face tape is kept together with the stage states");
+    if (((uintptr_t)tape & 15) != 0) return fail(c, AFVM_ERR_BAD_ARG, "the tape must be 16-byte aligned");
     DeviceGuard dg(c->device);
     cudaStream_t s = (cudaStream_t)stream;
     int st = dispatch(c, [&](auto r, auto sv) {
@@ -928,6 +930,7 @@ int afvm_adjoint_step_tape(afvm_ctx* ctx, const void* rho, const void* rhoU, con
         return fail(c, AFVM_ERR_BAD_ARG, "null pointer");
     if (dtca != 0.0) return fail(c, AFVM_ERR_UNSUPPORTED, "dtca != 0 (the CFL-sum output has no adjoint here)");
     if (tape && !stages) return fail(c, AFVM_ERR_BAD_ARG, "a face tape is read together with the stage states");
+    if (((uintptr_t)tape & 15) != 0) return fail(c, AFVM_ERR_BAD_ARG, "the tape must be 16-byte aligned");
     if (!std::isfinite(dt) || !std::isfinite(obja)) return fail(c, AFVM_ERR_BAD_ARG, "non-finite dt or obja");
     DeviceGuard dg(c->device);
     cudaStream_t s = (cudaStream_t)stream;
@@ -957,6 +960,7 @@ int afvm_adjoint_step_params(afvm_ctx* ctx, const void* rho, const void* rhoU, c
         return fail(c, AFVM_ERR_UNSUPPORTED, "mesh and boundary-input gradients need an AFVM_FP64 context");
     if (dtca != 0.0) return fail(c, AFVM_ERR_UNSUPPORTED, "dtca != 0 (the CFL-sum output has no adjoint here)");
     if (tape && !stages) return fail(c, AFVM_ERR_BAD_ARG, "a face tape is read together with the stage states");
+    if (((uintptr_t)tape & 15) != 0) return fail(c, AFVM_ERR_BAD_ARG, "the tape must be 16-byte aligned");
     if (!std::isfinite(dt) || !std::isfinite(obja)) return fail(c, AFVM_ERR_BAD_ARG, "non-finite dt or obja");
     bool mesh = pg->areas || pg->volumesL || pg->volumesR || pg->weights || pg->deltas || pg->normals ||
                 pg->deltasUnit || pg->linearWeights || pg->quadraticWeights || pg->volumes;

@@ -304,8 +304,12 @@ template <typename R> inline const MeshDev<R>& meshOf(const Ctx* c);
 template <> inline const MeshDev<double>& meshOf<double>(const Ctx* c) { return c->m64; }
 template <> inline const MeshDev<float>& meshOf<float>(const Ctx* c) { return c->m32; }
 
+// the three stages' face tapes, padded to a multiple of four values: the cell records that
+// follow them are read with 16-byte vector loads, and 3 TAPE nF values (TAPE odd, nF odd)
+// would leave them on an 8-byte boundary
 inline size_t face_tape_elements(const Ctx* c) {
-    return c->precision == AFVM_FP64 ? (size_t)3 * TAPE * (size_t)c->nF : 0;
+    if (c->precision != AFVM_FP64) return 0;
+    return ((size_t)3 * TAPE * (size_t)c->nF + 3) & ~(size_t)3;
 }
 inline size_t tape_elements(const Ctx* c) { return face_tape_elements(c) + (size_t)3 * REC * (size_t)c->nC; }
 template <typename R>

@@ -450,9 +450,9 @@ AFVM_HD void laxf_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const 
 // RCF.viscousFlux: F[1..3] += -sigma, F[4] += -(q + sigma.UF)
 // (mu = mu(TF), gT and gU the corrected face gradients: the forward's values)
 template <typename R>
-AFVM_HD void viscous_vjp_t(const Phys& P, R TF, const R* UF, R mu, R gTn, const R* tmp2, R tmp3, const R* sigma,
-                           const R* D, const R* N, R rdel, const R* Fb, R& TLb, R& TRb, R* ULb, R* URb, R& TFb,
-                           R* UFb, R* gTFb, R* gUFb) {
+AFVM_HD void viscous_vjp_t(const Phys& P, R TF, const R* UF, R mu, R dmu, R gTn, const R* tmp2, R tmp3,
+                           const R* sigma, const R* D, const R* N, R rdel, const R* Fb, R& TLb, R& TRb, R* ULb,
+                           R* URb, R& TFb, R* UFb, R* gTFb, R* gUFb) {
     R kappa = mu * consts<R>(P).kFac;
     // reverse
     R sb[3];
@@ -493,18 +493,16 @@ AFVM_HD void viscous_vjp_t(const Phys& P, R TF, const R* UF, R mu, R gTn, const 
     for (int k = 0; k < 3; k++) gTFb[k] += gTb[k] + gTDb * D[k];
     TRb += snTb * rdel;
     TLb += -snTb * rdel;
-    // d mu/dT = mu (1.5/T - 1/(T + Ts)) = mu (0.5 T + 1.5 Ts) / (T (T + Ts)): one reciprocal
-    if (P.muModel == AFVM_MU_SUTHERLAND) {
-        R Ts = consts<R>(P).muTs;
-        TFb += mub * mu * ((R(0.5) * TF + R(1.5) * Ts) * rcp(TF * (TF + Ts)));
-    }
+    // d mu/dT (viscosity(); 0 for a constant mu)
+    TFb += mub * dmu;
 }
 
 template <typename R>
 AFVM_HD void viscous_vjp(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, const R* UF, const R* gTF,
                          const R* gUF, const R* D, const R* N, R rdel, const R* Fb, R& TLb, R& TRb, R* ULb, R* URb,
                          R& TFb, R* UFb, R* gTFb, R* gUFb) {
-    R mu = viscosity<R>(P, TF);
+    R dmu;
+    R mu = viscosity<R>(P, TF, &dmu);
     R gTD = dot3(gTF, D);
     R cT = (TR - TL) * rdel - gTD;
     R gT[3];
@@ -521,7 +519,7 @@ AFVM_HD void viscous_vjp(const Phys& P, R TL, R TR, const R* UL, const R* UR, R 
         tmp2[i] = (gU[3 * i] + gU[i]) * N[0] + (gU[3 * i + 1] + gU[3 + i]) * N[1] + (gU[3 * i + 2] + gU[6 + i]) * N[2];
         sigma[i] = mu * (tmp2[i] - R(2.0 / 3) * tmp3 * N[i]);
     }
-    viscous_vjp_t<R>(P, TF, UF, mu, dot3(gT, N), tmp2, tmp3, sigma, D, N, rdel, Fb, TLb, TRb, ULb, URb, TFb, UFb,
+    viscous_vjp_t<R>(P, TF, UF, mu, dmu, dot3(gT, N), tmp2, tmp3, sigma, D, N, rdel, Fb, TLb, TRb, ULb, URb, TFb, UFb,
                      gTFb, gUFb);
 }
 
@@ -654,11 +652,13 @@ AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>&
 
         R TFb = R(0), UFb[3] = {R(0), R(0), R(0)}, gTFb[3] = {R(0), R(0), R(0)}, gUFb[9];
         for (int k = 0; k < 9; k++) gUFb[k] = R(0);
-        R tmp2[3], sigma[3], tmp3, mu = t.get(T_MU);
+        R tmp2[3], sigma[3], tmp3, mu = t.get(T_MU), dmu;
         if constexpr (Src::kFull) {
             for (int k = 0; k < 3; k++) { tmp2[k] = t.get(T_TMP2 + k); sigma[k] = t.get(T_SIG + k); }
             tmp3 = t.get(T_TMP3);
+            dmu = t.get(T_DMU);
         } else {
+            viscosity<R>(P, TF, &dmu);
             // the stress terms from the corrected face gradient, as viscous() forms them
             R gUl[9];
             corrected_gradU<R>(in, chr, gUl);
@@ -669,7 +669,7 @@ AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>&
                 sigma[i] = mu * (tmp2[i] - R(2.0 / 3) * tmp3 * in.N[i]);
             }
         }
-        viscous_vjp_t<R>(P, TF, UF, mu, t.get(T_GTN), tmp2, tmp3, sigma, in.D, in.N, in.rdelta, Fb, o.TP, o.TN, o.UP,
+        viscous_vjp_t<R>(P, TF, UF, mu, dmu, t.get(T_GTN), tmp2, tmp3, sigma, in.D, in.N, in.rdelta, Fb, o.TP, o.TN, o.UP,
                          o.UN, TFb, UFb, gTFb, gUFb);
         if constexpr (kGeo<G>) {
             R gTF[3], gUF[9];

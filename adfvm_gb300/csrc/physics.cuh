@@ -59,7 +59,8 @@ constexpr int T_TMP2 = 43, T_SIG = 46, T_TMP3 = 49;
 // each side, the sound speeds, the Roe-average sound speed and 1/a_F^2, and abv2, abv3
 constexpr int T_RUNL = 50, T_RUNR = 51, T_SL = 52, T_SR = 53, T_CL = 54, T_CR = 55;
 constexpr int T_AF = 56, T_RA2F = 57, T_ABV2 = 58, T_ABV3 = 59;
-constexpr int TAPE = 60;
+constexpr int T_DMU = 60;                        // d mu / d T at T_F
+constexpr int TAPE = 61;
 constexpr int T_LEAN = 23;   // the values up to here: those that cost the most to re-evaluate
 
 struct TapeNone {
@@ -318,10 +319,25 @@ AFVM_HD bool pos_(R x) {
 template <typename R>
 AFVM_HD R sqrt_(R x) { return pos_(x) ? x * rsqrt_(x) : R(0); }
 
-// mu(T): constant, or Sutherland 1.4792e-06*T**1.5/(T+116.) (adFVM/density.py:27)
+// mu(T): constant, or Sutherland 1.4792e-06*T**1.5/(T+116.) (adFVM/density.py:27), written as
+// As T^2 / sqrt(T (T + Ts)^2): one reciprocal square root (0 for T <= 0, as T sqrt(T) was).
+// With dmu, also d mu / dT = mu (T/2 + 3 Ts/2) / (T (T + Ts)), where 1/(T (T + Ts)) is
+// (T + Ts) y^2 with the same y = 1/sqrt(T (T + Ts)^2).
 template <typename R>
-AFVM_HD R viscosity(const Phys& P, R T) {
-    if (P.muModel == AFVM_MU_SUTHERLAND) return (consts<R>(P).muAs * (T * sqrt_(T))) * rcp(T + consts<R>(P).muTs);
+AFVM_HD R viscosity(const Phys& P, R T, R* dmu = nullptr) {
+    if (P.muModel == AFVM_MU_SUTHERLAND) {
+        if (!pos_(T)) {
+            if (dmu) *dmu = R(0);
+            return R(0);
+        }
+        const R Ts = consts<R>(P).muTs;
+        R a = T + Ts;
+        R y = rsqrt_(T * (a * a));
+        R mu = (consts<R>(P).muAs * (T * T)) * y;
+        if (dmu) *dmu = (mu * (R(0.5) * T + R(1.5) * Ts)) * (a * (y * y));
+        return mu;
+    }
+    if (dmu) *dmu = R(0);
     return consts<R>(P).mu0;
 }
 
@@ -574,8 +590,10 @@ template <typename R, typename Sink = TapeNone>
 AFVM_HD void viscous(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, const R* UF,
                                         const R* gTF, const R* gUF, const R* D, const R* N, R rdel, R* F,
                                         Sink&& tp = Sink()) {
-    R mu = viscosity<R>(P, TF);
+    R dmu;
+    R mu = viscosity<R>(P, TF, &dmu);
     tp.put(T_MU, mu);
+    tp.put(T_DMU, dmu);
     R kappa = mu * consts<R>(P).kFac;
     // the face gradient with its normal component replaced by snGrad: g + (snGrad - g.D) D
     R gTD = dot3(gTF, D);

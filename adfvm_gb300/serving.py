@@ -311,7 +311,7 @@ class SensitivityServer(object):
         # per face: tables, flux records, adjoint face records (and FP64 face tapes); per cell:
         # tables and cell records, RK and adjoint work states, checkpoints, interval states,
         # stage buffers and the tapes' cell records
-        face_tape = 3 * 60 * 8 * self.k if self.precision == 'fp64' else 0
+        face_tape = 3 * 61 * 8 * self.k if self.precision == 'fp64' else 0
         return int(m.nFaces * (60 + 28 * er + 40 * er + face_tape) + m.nInternalCells * (150 + 40 * er + 40 * es
                    + (self.nPrimal // self.k + 3 * self.k + 8) * 5 * es) + m.nCells * 3 * 20 * er * self.k)
 

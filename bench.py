@@ -50,10 +50,10 @@ def peaks():
 # algorithmic (compulsory) bytes per launch of each primal kernel, FP64 / FP32 element size
 # es and int32 indices (per-unit counts in the comments below)
 def algorithmic_bytes(kernel, nIC, nIF, nF, nG, es, taped=False):
-    REC, FREC, TAPE = 20, 6, 60
+    REC, FREC, TAPE = 20, 6, 61
     if kernel == 'k_flux':
         # per face: own+nbr (8), normals 3, deltas 1, deltasUnit 3, linearWeights 2,
-        # quadraticWeights 6 -> 15 values, flux record write 6 (and the 60-value face tape when
+        # quadraticWeights 6 -> 15 values, flux record write 6 (and the 61-value face tape when
         # taped); cell records read once
         return nF * (8 + 15 * es + FREC * es + (TAPE * es if taped else 0)) + (nIC + nG) * REC * es
     if kernel == 'k_grad':
@@ -67,7 +67,7 @@ def algorithmic_bytes(kernel, nIC, nIF, nF, nG, es, taped=False):
     if kernel == 'k_prim':
         return nIC * 10 * es + nG * (8 + 5 * es + 5 * es)
     if kernel == 'k_adj_flux' and taped:
-        # per face: own+nbr (8), A/V weights 2, geometry 15, the 60-value face tape, 40-value
+        # per face: own+nbr (8), A/V weights 2, geometry 15, the 61-value face tape, 40-value
         # adjoint record write; the 5 adjoint seeds of every cell once; the two cell records of
         # each boundary face (boundary faces are not taped)
         return nF * (8 + (17 + TAPE + 40) * es) + nIC * 5 * es + (nF - nIF) * 2 * REC * es

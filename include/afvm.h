@@ -326,14 +326,16 @@ int afvm_adjoint_step_stages(afvm_ctx* ctx, const void* rho, const void* rhoU, c
 /* The tape of a step: what the primal step computed that its adjoint step would otherwise
  * compute again. In every precision the three RK stages' cell records (20 values a cell:
  * primitives and gradients), which spare the adjoint its primitive and gradient launches; in
- * AFVM_FP64 first also the face tape: per stage and face the 50 values of the forward face
+ * AFVM_FP64 first also the face tape: per stage and face the 61 values of the forward face
  * flux that its VJP would otherwise re-evaluate (the reconstructed face states, the
  * reciprocals and reciprocal square roots of the Roe / Rusanov flux and of the conservative
- * variables, mu(T_F), the Roe average and eigenvalue terms, the viscous stress terms), the
+ * variables, the normal velocities and sound speeds, mu(T_F) and its derivative, the Roe
+ * average and eigenvalue terms, the viscous stress terms), the
  * face VJP being bound by the FP64 pipe there while HBM idles. Element type: the record type
- * (double for AFVM_FP64, float otherwise); afvm_tape_elements values a step (3 x 50 x nFaces
- * + 3 x 20 x nCells in FP64, 3 x 20 x nCells otherwise). No reference counterpart (adpy's
- * reverse mode re-runs the forward). */
+ * (double for AFVM_FP64, float otherwise); afvm_tape_elements values a step (3 x 61 x nFaces,
+ * rounded up to a multiple of 4, + 3 x 20 x nCells in FP64; 3 x 20 x nCells otherwise), 16-byte
+ * aligned (AFVM_ERR_BAD_ARG otherwise). No reference counterpart (adpy's reverse mode re-runs
+ * the forward). */
 int64_t afvm_tape_elements(const afvm_ctx* ctx);
 
 /* afvm_primal_step_stages that also writes the step's tape (DEVICE, afvm_tape_elements
