@@ -109,3 +109,22 @@ def test_values_leaving_the_records_are_absolute(precision):
     assert abs(ob - oa) <= 1e-5 * abs(oa), (oa, ob)
     a.close()
     b.close()
+
+
+def test_gauge_and_tape_arguments_are_checked():
+    """afvm_set_gauge rejects a non-finite gauge state; a tape that is not 16-byte aligned is
+    rejected before any launch (the tape's cell records are read with 16-byte loads)."""
+    from adfvm_gb300 import _lib as L
+    case, mesh, x = _cyl()
+    r = RCF(mesh, case.bc, objective=case.objective, precision='fp64', **case.config)
+    assert L.lib().afvm_set_gauge(r._ctx, float('nan'), 300.0, 3e5) == L.AFVM_ERR_BAD_ARG
+    assert L.lib().afvm_set_gauge(r._ctx, 1e5, float('inf'), 3e5) == L.AFVM_ERR_BAD_ARG
+    xd = [t.cuda() for t in x]
+    st = r.stage_buffer()
+    tape = r.tape_buffer()
+    shifted = torch.empty(tape.numel() + 1, dtype=tape.dtype, device=tape.device)[1:]
+    with pytest.raises(L.AfvmError) as ei:
+        r.step(xd[0], xd[1], xd[2], case.dt, stages=st, tape=shifted)
+    assert ei.value.status == L.AFVM_ERR_BAD_ARG
+    r.step(xd[0], xd[1], xd[2], case.dt, stages=st, tape=tape)     # the aligned one runs
+    r.close()
