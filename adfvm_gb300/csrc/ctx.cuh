@@ -285,7 +285,8 @@ void launch_prim_grad(Ctx* c, const S* r, const S* ru, const S* re, cudaStream_t
 template <typename R, typename S = R>
 void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const S* const* u0, const S* const* u1,
                         const S* const* u2, const S* Sr, const S* Su, const S* Se, S* const* out, cudaStream_t s,
-                        bool nextPrims = false, R* tape = nullptr, R* recIn = nullptr, R* recOut = nullptr);
+                        bool nextPrims = false, R* tape = nullptr, R* recIn = nullptr, R* recOut = nullptr,
+                        double* objPartials = nullptr);
 template <typename S>
 void default_sources(Ctx* c, const S*& Srho, const S*& SrhoU, const S*& SrhoE);
 // count values between host memory of any kind and the device (element sizes 4 or 8, converted

@@ -84,6 +84,34 @@ __device__ __forceinline__ void store_prims(double* r, const double* v) {
     r[4] = v[4];
 }
 
+// one cell's term of a cell-sum objective on its primitives U (3), T, p (record values: FP32
+// ones hold gauge offsets): AFVM_OBJ_KINETIC_ENERGY 0.5 rho |U|^2 V in the record type, or
+// AFVM_OBJ_SUM_T the temperature; accumulated in double
+template <typename R>
+__device__ __forceinline__ double cell_objective(const Phys& P, int kind, const R* r, R vol) {
+    if (kind == AFVM_OBJ_KINETIC_ENERGY) {
+        R rho = rec_abs_p<R>(P, r[R_P]) / ((consts<R>(P).Cv * rec_abs_T<R>(P, r[R_T])) * consts<R>(P).gm1);
+        return (double)(R(0.5) * rho * (r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) * vol);
+    }
+    return rec_T<R>(P, r[R_T]);
+}
+
+// the objectives that are sums over cells (evaluated in the stage-0 update, which writes the
+// objective stage's primitives)
+inline bool cell_sum_objective(int kind) { return kind == AFVM_OBJ_KINETIC_ENERGY || kind == AFVM_OBJ_SUM_T; }
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x < 32) {
+        r = (threadIdx.x < BLOCK / 32) ? sh[threadIdx.x] : 0.0;
+        for (int off = 16; off > 0; off >>= 1) r += __shfl_down_sync(0xffffffffu, r, off);
+    }
+    return r;
+}
+
 // ghost cell g's primitives from its source cell's (v, replaced in place): the boundary
 // conditions of BCs.py:62-184 (FP32 records: T and p as gauge offsets, so a zero-gradient
 // ghost keeps its source's bits)
@@ -253,13 +281,15 @@ __global__ void __launch_bounds__(BLOCK) k_update(MeshDev<R> m, const R* __restr
                                                   const S* __restrict__ Sr, const S* __restrict__ Su,
                                                   const S* __restrict__ Se,
                                                   S* outr, S* outu, S* oute,
-                                                  unsigned long long* dtcBits, Phys P, R* __restrict__ recNext) {
+                                                  unsigned long long* dtcBits, Phys P, R* __restrict__ recNext,
+                                                  int objKind, double* __restrict__ objPartials) {
     // the gather (and the CFL sum) in the flux type R, the stage update in the state's type S:
     // under FP32 fluxes with an FP64 state the six fluxes are summed in FP32 (each carries FP32
     // rounding already; summing them in FP64 cost six FP64 conversions, products and sums a
     // cell and component) and the state is updated in FP64
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     R dtc = R(0);
+    double objv = 0.0;     // this cell's term of a cell-sum objective (stage 0, objPartials)
     if (c < m.nIC) {
         const size_t n = m.nIC;
         R res[5] = {R(0), R(0), R(0), R(0), R(0)};
@@ -317,6 +347,7 @@ __global__ void __launch_bounds__(BLOCK) k_update(MeshDev<R> m, const R* __restr
             R v[5];
             prim_values(P, o[0], o[1], o[2], o[3], o[4], v);
             store_prims(recNext + (size_t)c * REC, v);
+            if (STAGE == 0 && objPartials) objv = cell_objective<R>(P, objKind, v, m.vol[c]);
             for (int q = m.gsStart[c]; q < m.gsStart[c + 1]; q++) {
                 int g = m.gsList[q];
                 R w[5] = {v[0], v[1], v[2], v[3], v[4]};
@@ -324,6 +355,13 @@ __global__ void __launch_bounds__(BLOCK) k_update(MeshDev<R> m, const R* __restr
                 store_prims(recNext + (size_t)(m.nIC + g) * REC, w);
             }
         }
+    }
+    if (STAGE == 0 && objPartials) {
+        // the objective stage's primitives are the ones this stage-0 update writes: the
+        // objective's block partial sums (the same terms and order as k_objective)
+        __shared__ double osh[BLOCK / 32];
+        double sum = block_sum(objv, osh);
+        if (threadIdx.x == 0) objPartials[blockIdx.x] = sum;
     }
     if (STAGE == 1) {
         // reduce_max of the CFL sums (density.py:405-410): warp shuffle, block, then an atomic
@@ -362,18 +400,6 @@ void launch_abs_prims(const Ctx* c, const float* rec, int stride, int n, float* 
 
 // ---- objectives, evaluated on the ghost-completed primitives of stage 1 ----
 
-__device__ __forceinline__ double block_sum(double v, double* sh) {
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
-    __syncthreads();
-    double r = 0.0;
-    if (threadIdx.x < 32) {
-        r = (threadIdx.x < BLOCK / 32) ? sh[threadIdx.x] : 0.0;
-        for (int off = 16; off > 0; off >>= 1) r += __shfl_down_sync(0xffffffffu, r, off);
-    }
-    return r;
-}
-
 // per-block partial sums; kinds: AFVM_OBJ_KINETIC_ENERGY, AFVM_OBJ_SUM_T (cells) and
 // AFVM_OBJ_DRAG (faces [start, start+n) of one patch, templates/cylinder_test.py:9-19)
 template <typename R>
@@ -383,13 +409,9 @@ __global__ void __launch_bounds__(BLOCK) k_objective(MeshDev<R> m, Phys P, const
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     double v = 0.0;
     if (t < n) {
-        if (kind == AFVM_OBJ_KINETIC_ENERGY) {
+        if (kind == AFVM_OBJ_KINETIC_ENERGY || kind == AFVM_OBJ_SUM_T) {
             // per-cell term in the working precision R, accumulated in double
-            const R* r = rec + (size_t)t * REC;
-            R rho = rec_abs_p<R>(P, r[R_P]) / ((consts<R>(P).Cv * rec_abs_T<R>(P, r[R_T])) * consts<R>(P).gm1);
-            v = (double)(R(0.5) * rho * (r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) * m.vol[t]);
-        } else if (kind == AFVM_OBJ_SUM_T) {
-            v = rec_T<R>(P, rec[(size_t)t * REC + R_T]);
+            v = cell_objective<R>(P, kind, rec + (size_t)t * REC, m.vol[t]);
         } else {
             int f = start + t;
             const R* rN = rec + (size_t)m.nbr[f] * REC;
@@ -501,7 +523,7 @@ void launch_prim_grad(Ctx* c, const S* r, const S* ru, const S* re, cudaStream_t
 template <typename R, typename S>
 void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const S* const* u0, const S* const* u1,
                         const S* const* u2, const S* Sr, const S* Su, const S* Se, S* const* out, cudaStream_t s,
-                        bool nextPrims, R* tape, R* recIn, R* recOut) {
+                        bool nextPrims, R* tape, R* recIn, R* recOut, double* objPartials) {
     const MeshDev<R>& m = meshOf<R>(c);
     const Phys& P = c->phys;
     R* rec = recIn ? recIn : (R*)c->rec;
@@ -525,15 +547,15 @@ void launch_flux_update(Ctx* c, int st, double dt, const double* dtDev, const S*
     if (st == 0)
         k_update<R, S, 0><<<nb, BLOCK, 0, s>>>(m, ff, dt, dtDev, u0[0], u0[1], u0[2], nullptr, nullptr, nullptr, nullptr,
                                             nullptr, nullptr, Sr, Su, Se, out[0], out[1], out[2], c->dtcBits, P,
-                                            recNext);
+                                            recNext, c->objective, recNext ? objPartials : nullptr);
     else if (st == 1)
         k_update<R, S, 1><<<nb, BLOCK, 0, s>>>(m, ff, dt, dtDev, u0[0], u0[1], u0[2], u1[0], u1[1], u1[2], nullptr,
                                             nullptr, nullptr, Sr, Su, Se, out[0], out[1], out[2], c->dtcBits, P,
-                                            recNext);
+                                            recNext, c->objective, nullptr);
     else
         k_update<R, S, 2><<<nb, BLOCK, 0, s>>>(m, ff, dt, dtDev, u0[0], u0[1], u0[2], nullptr, nullptr, nullptr, u2[0],
                                             u2[1], u2[2], Sr, Su, Se, out[0], out[1], out[2], c->dtcBits, P,
-                                            recNext);
+                                            recNext, c->objective, nullptr);
 }
 
 template <typename S>
@@ -600,16 +622,21 @@ int primal_step_dev(Ctx* c, const S* rho, const S* rhoU, const S* rhoE, double d
             if (c->objective == AFVM_OBJ_DRAG) { start = c->objStart; n = c->objN; }
             nObjBlocks = nblocks(n);
             if (nObjBlocks > c->nPartials) return fail(c, AFVM_ERR_BAD_ARG, "objective partials overflow");
-            if (n > 0) {
+            // a cell-sum objective's partials were written by the stage-0 update
+            if (n > 0 && !cell_sum_objective(c->objective)) {
                 ProfScope ps(c, KID_OBJECTIVE, s);
                 k_objective<R><<<nObjBlocks, BLOCK, 0, s>>>(m, P, (const R*)recs[1], c->objective, start, n,
                                                             c->partials);
             }
         }
         S* const* out = st == 0 ? u1 : (st == 1 ? u2 : outN);
+        double* objPartials = (st == 0 && cell_sum_objective(c->objective) && nblocks(m.nIC) <= c->nPartials)
+                                  ? c->partials : nullptr;
+        if (st == 0 && cell_sum_objective(c->objective) && !objPartials)
+            return fail(c, AFVM_ERR_BAD_ARG, "objective partials overflow");
         launch_flux_update<R, S>(c, st, dt, dtDev, u0c, u1c, u2c, Srho, SrhoU, SrhoE, out, s, st < 2,
                                  faceTape ? faceTape + (size_t)st * TAPE * m.nF : nullptr, recs[st],
-                                 st < 2 ? recs[st + 1] : nullptr);
+                                 st < 2 ? recs[st + 1] : nullptr, objPartials);
     }
     if (vaneDone) {
         ProfScope ps(c, KID_FINISH, s);
@@ -659,7 +686,7 @@ int primal_run_dev(Ctx* c, S* rho, S* rhoU, S* rhoE, int nSteps, double dt0, dou
     template void launch_prim_grad<R, S>(Ctx*, const S*, const S*, const S*, cudaStream_t, R*);                  \
     template void launch_flux_update<R, S>(Ctx*, int, double, const double*, const S* const*, const S* const*,   \
                                            const S* const*, const S*, const S*, const S*, S* const*, cudaStream_t,  \
-                                           bool, R*, R*, R*);
+                                           bool, R*, R*, R*, double*);
 AFVM_PRIMAL_INST(double, double)
 AFVM_PRIMAL_INST(float, float)
 AFVM_PRIMAL_INST(float, double)
