@@ -178,6 +178,25 @@ def describe(case, precision):
         'cells': int(m.nInternalCells), 'faces': int(m.nFaces)}
 
 
+def reference_python():
+    """The reference's own primal path (its Solver.run through the NumPy adpy stand-in), timed
+    in the build container by oracle/time_reference.py - the GPU machine has no reference checkout -
+    and read from the fixture that script writes; None without it."""
+    path = os.path.join(ROOT, 'oracle', 'reference_timing.json')
+    try:
+        with open(path) as f:
+            d = json.load(f)
+    except (OSError, ValueError):
+        return None
+    c = max(d['cases'], key=lambda x: x['cells'])
+    return {'value': c['primal_mcell_steps_per_s'], 'unit': 'primal ' + UNIT, 'workload': c['workload'],
+            'threads': d['threads'], 'host': '%s, %s cores' % (d['host'], d['cores']),
+            'measured': 'in the build container on %s (oracle/time_reference.py; not on the GPU box, which has '
+                        'no reference checkout); the reference adjoint (adpy reverse mode) is absent from the '
+                        'checkout' % d['measured_utc'],
+            'cases': {x['workload'].split(':')[0]: x['primal_mcell_steps_per_s'] for x in d['cases']}}
+
+
 def cpu_baseline(args, threads, seconds=10.0):
     """The reference path restated for the CPU, timed on the host cores on a bounded sample of
     the workload itself - the same mesh, state and dt:
@@ -622,6 +641,7 @@ def run_reference(args):
             # sample the CPU timed is in cpu_baseline.sample
             'config': dict(base.pop('config'), parallelism='host cores (%d threads)' % threads),
             'cpu_baseline': base,
+            'reference_python': reference_python(),
             'e2e': {'value': base['value'], 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
     print(json.dumps(line))
     return 0
@@ -727,6 +747,10 @@ def main():
                                    'adjoint': round(m64['adjoint']['value'] / cb['adjoint'], 2),
                                    'primal_adjoint': round(m64['value'] / cb['value'], 2),
                                    'e2e': round(m64['e2e']['value'] / cb['value'], 2)}
+        rp = reference_python()
+        if rp is not None:
+            line['reference_python'] = rp
+            line['vs_reference_python'] = {'primal': round(m64['primal']['value'] / rp['value'], 1)}
     if rank == 0:
         print(json.dumps(line))
     if dist:
