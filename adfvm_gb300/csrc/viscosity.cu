@@ -121,11 +121,14 @@ __global__ void __launch_bounds__(BLOCK) k_visc_cell(MeshDev<R> m, Phys P, const
                 for (int j = 0; j < 3; j++) gU[i][j] += (UF[i] * N[j]) * sw;
             dU += (UF[0] * N[0] + UF[1] * N[1] + UF[2] * N[2]) * sw;
             for (int j = 0; j < 3; j++) {
-                // (the pressure gradient: a gauge offset of FP32 records drops out of this closed sum)
                 gp[j] += (pF * N[j]) * sw;
                 gc[j] += (cF * N[j]) * sw;
             }
         }
+        // FP32 records hold p - gaugeP: the sum above missed gaugeP times the cell's sum of A/V N
+        // (zero when the cell's face area vectors close, not for warped faces)
+        if constexpr (kGauge<R>)
+            for (int j = 0; j < 3; j++) gp[j] += P.gaugeP * m.gclD[j * n + c];
         double val = 1.0;
         if (kind != AFVM_VISC_UNIFORM) {
             const R* r = rec + (size_t)c * REC;
