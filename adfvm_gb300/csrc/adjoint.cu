@@ -227,11 +227,12 @@ __global__ void __launch_bounds__(BLOCK) k_adj_cell2(MeshDev<R> m, Phys P, const
         if (objective == AFVM_OBJ_KINETIC_ENERGY) {
             double U[3] = {rc[0], rc[1], rc[2]}, T = rec_T<R>(P, rc[R_T]), p = rec_p<R>(P, rc[R_P]), V = m.vol[c];
             double d = (P.Cv * T) * P.gm1;
-            double rho = p / d;
+            double rd = rcp(d);           // (Newton reciprocals: no IEEE divisions on the FP64 pipe)
+            double rho = p * rd;
             double q = U[0] * U[0] + U[1] * U[1] + U[2] * U[2];
             for (int k = 0; k < 3; k++) pbar[k] += (R)(obja * rho * U[k] * V);
-            pbar[R_P] += (R)(obja * 0.5 * q * V / d);
-            pbar[R_T] += (R)(-obja * 0.5 * q * V * rho / T);
+            pbar[R_P] += (R)(obja * 0.5 * q * V * rd);
+            pbar[R_T] += (R)(-obja * 0.5 * q * V * rho * rcp(T));
         } else if (objective == AFVM_OBJ_SUM_T) {
             pbar[R_T] += (R)obja;
         } else if (objective == AFVM_OBJ_VANE) {

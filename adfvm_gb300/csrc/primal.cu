@@ -90,7 +90,7 @@ __device__ __forceinline__ void store_prims(double* r, const double* v) {
 template <typename R>
 __device__ __forceinline__ double cell_objective(const Phys& P, int kind, const R* r, R vol) {
     if (kind == AFVM_OBJ_KINETIC_ENERGY) {
-        R rho = rec_abs_p<R>(P, r[R_P]) / ((consts<R>(P).Cv * rec_abs_T<R>(P, r[R_T])) * consts<R>(P).gm1);
+        R rho = rec_abs_p<R>(P, r[R_P]) * rcp((consts<R>(P).Cv * rec_abs_T<R>(P, r[R_T])) * consts<R>(P).gm1);
         return (double)(R(0.5) * rho * (r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) * vol);
     }
     return rec_T<R>(P, r[R_T]);
