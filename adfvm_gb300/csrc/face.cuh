@@ -55,7 +55,7 @@ AFVM_HD void zero_geo(GeoBar<R>& g) {
 template <typename R>
 AFVM_HD void face_flux_gauge(const Phys& P, int kind, bool inviscid, const FaceIn<R>& in, R* F, R& maxaF) {
     const PhysR<R>& Q = consts<R>(P);
-    R TF, UF[3], gTF[3], gUF[9];
+    R TF, Us[3], gTs[3], gUs[9], hs, rhs;
     if (kind == FACE_BOUNDARY) {
         // RCF.boundaryFlux: (rho Un, rho U Un + p N, rho h Un) less gP N and gH rho Un
         R rho, rhoU[3], rhoE;
@@ -66,8 +66,9 @@ AFVM_HD void face_flux_gauge(const Phys& P, int kind, bool inviscid, const FaceI
         for (int k = 0; k < 3; k++) F[1 + k] = rhoU[k] * Un + in.pN * in.N[k];
         F[4] = rho * hg * Un;
         TF = in.TN + Q.gT;
-        for (int k = 0; k < 3; k++) { UF[k] = in.UN[k]; gTF[k] = in.gTN[k]; }
-        for (int k = 0; k < 9; k++) gUF[k] = in.gUN[k];
+        for (int k = 0; k < 3; k++) { Us[k] = in.UN[k]; gTs[k] = in.gTN[k]; }
+        for (int k = 0; k < 9; k++) gUs[k] = in.gUN[k];
+        hs = R(1); rhs = R(1);
     } else {
         R ULF[3], TLF, pLF, URF[3], TRF, pRF;
         for (int k = 0; k < 3; k++) ULF[k] = recon<R>(in.UP[k], in.UN[k], in.gUP + 3 * k, in.lw0, in.qw0);
@@ -94,17 +95,19 @@ AFVM_HD void face_flux_gauge(const Phys& P, int kind, bool inviscid, const FaceI
             laxf_gauge<R>(P, pLF, pRF, TLF, TRF, ULF, URF, rhoL, rhoR, rdL, rdR, in.N, F);
         if (kind == FACE_CHARACTERISTIC) {
             TF = in.TN + Q.gT;
-            for (int k = 0; k < 3; k++) { UF[k] = in.UN[k]; gTF[k] = in.gTN[k]; }
-            for (int k = 0; k < 9; k++) gUF[k] = in.gUN[k];
+            for (int k = 0; k < 3; k++) { Us[k] = in.UN[k]; gTs[k] = in.gTN[k]; }
+            for (int k = 0; k < 9; k++) gUs[k] = in.gUN[k];
+            hs = R(1); rhs = R(1);
         } else {
             TF = R(0.5) * (TLF + TRF) + Q.gT;
-            for (int k = 0; k < 3; k++) { UF[k] = R(0.5) * (ULF[k] + URF[k]); gTF[k] = R(0.5) * (in.gTP[k] + in.gTN[k]); }
-            for (int k = 0; k < 9; k++) gUF[k] = R(0.5) * (in.gUP[k] + in.gUN[k]);
+            for (int k = 0; k < 3; k++) { Us[k] = ULF[k] + URF[k]; gTs[k] = in.gTP[k] + in.gTN[k]; }
+            for (int k = 0; k < 9; k++) gUs[k] = in.gUP[k] + in.gUN[k];
+            hs = R(0.5); rhs = R(2);
         }
     }
-    if (!inviscid) viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, UF, gTF, gUF, in.D, in.N, in.rdelta, F);
+    if (!inviscid) viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, Us, gTs, gUs, hs, rhs, in.D, in.N, in.rdelta, F);
     R aF = sqrt_(Q.Cp * TF * Q.gm1);
-    maxaF = fabs(dot3(UF, in.N)) + aF;
+    maxaF = fabs(hs * dot3(Us, in.N)) + aF;
 }
 
 // flux (rho, rhoU, rhoE) through the face and the CFL term |U.n| + a; the tape values of a
@@ -117,7 +120,7 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
         face_flux_gauge<R>(P, kind, inviscid, in, F, maxaF);
         return;
     }
-    R TF, UF[3], gTF[3], gUF[9];
+    R TF, Us[3], gTs[3], gUs[9], hs, rhs;
     if (kind == FACE_BOUNDARY) {
         // RCF.boundaryFlux (density.py:307-331) with RCF.getFlux (density.py:184-190)
         R rho, rhoU[3], rhoE;
@@ -127,8 +130,9 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
         for (int k = 0; k < 3; k++) F[1 + k] = rhoU[k] * Un + in.pN * in.N[k];
         F[4] = (rhoE + in.pN) * Un;
         TF = in.TN;
-        for (int k = 0; k < 3; k++) { UF[k] = in.UN[k]; gTF[k] = in.gTN[k]; }
-        for (int k = 0; k < 9; k++) gUF[k] = in.gUN[k];
+        for (int k = 0; k < 3; k++) { Us[k] = in.UN[k]; gTs[k] = in.gTN[k]; }
+        for (int k = 0; k < 9; k++) gUs[k] = in.gUN[k];
+        hs = R(1); rhs = R(1);
     } else {
         R ULF[3], TLF, pLF, URF[3], TRF, pRF;
         for (int k = 0; k < 3; k++) ULF[k] = recon<R>(in.UP[k], in.UN[k], in.gUP + 3 * k, in.lw0, in.qw0);
@@ -158,17 +162,21 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
             laxf<R>(P, pLF, pRF, TLF, TRF, ULF, URF, rhoL, rhoR, rhoUL, rhoUR, rhoEL, rhoER, in.N, F, tp);
         if (kind == FACE_CHARACTERISTIC) {
             TF = in.TN;
-            for (int k = 0; k < 3; k++) { UF[k] = in.UN[k]; gTF[k] = in.gTN[k]; }
-            for (int k = 0; k < 9; k++) gUF[k] = in.gUN[k];
+            for (int k = 0; k < 3; k++) { Us[k] = in.UN[k]; gTs[k] = in.gTN[k]; }
+            for (int k = 0; k < 9; k++) gUs[k] = in.gUN[k];
+            hs = R(1); rhs = R(1);
         } else {
+            // the face averages (density.py:290-291) as hs = 1/2 times the two sides' sums
             TF = R(0.5) * (TLF + TRF);
-            for (int k = 0; k < 3; k++) { UF[k] = R(0.5) * (ULF[k] + URF[k]); gTF[k] = R(0.5) * (in.gTP[k] + in.gTN[k]); }
-            for (int k = 0; k < 9; k++) gUF[k] = R(0.5) * (in.gUP[k] + in.gUN[k]);
+            for (int k = 0; k < 3; k++) { Us[k] = ULF[k] + URF[k]; gTs[k] = in.gTP[k] + in.gTN[k]; }
+            for (int k = 0; k < 9; k++) gUs[k] = in.gUP[k] + in.gUN[k];
+            hs = R(0.5); rhs = R(2);
         }
     }
-    if (!inviscid) viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, UF, gTF, gUF, in.D, in.N, in.rdelta, F, tp);
+    if (!inviscid)
+        viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, Us, gTs, gUs, hs, rhs, in.D, in.N, in.rdelta, F, tp);
     R aF = sqrt_(consts<R>(P).Cp * TF * consts<R>(P).gm1);
-    maxaF = fabs(dot3(UF, in.N)) + aF;
+    maxaF = fabs(hs * dot3(Us, in.N)) + aF;
 }
 
 // ---------------------------------------------------------------------------- adjoints
@@ -450,7 +458,7 @@ AFVM_HD void laxf_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const 
 // RCF.viscousFlux: F[1..3] += -sigma, F[4] += -(q + sigma.UF)
 // (mu = mu(TF), gT and gU the corrected face gradients: the forward's values)
 template <typename R>
-AFVM_HD void viscous_vjp_t(const Phys& P, R TF, const R* UF, R mu, R dmu, R gTn, const R* tmp2, R tmp3,
+AFVM_HD void viscous_vjp_t(const Phys& P, R TF, const R* UF, R mu, R dmu, R gTn, const R* tmp2, R tmp3, R ts,
                            const R* sigma, const R* D, const R* N, R rdel, const R* Fb, R& TLb, R& TRb, R* ULb,
                            R* URb, R& TFb, R* UFb, R* gTFb, R* gUFb) {
     R kappa = mu * consts<R>(P).kFac;
@@ -463,11 +471,13 @@ AFVM_HD void viscous_vjp_t(const Phys& P, R TF, const R* UF, R mu, R dmu, R gTn,
     R qFb = -Fb[4];
     R mub = R(0);
     R tmp2b[3];
+    // (tmp2, tmp3: the forward's, divided by ts)
     R c23 = R(2.0 / 3) * tmp3;
     for (int i = 0; i < 3; i++) {
         mub += sb[i] * (tmp2[i] - c23 * N[i]);
         tmp2b[i] = sb[i] * mu;
     }
+    mub = mub * ts;
     R tmp3b = (-R(2.0 / 3) * mu) * dot3(sb, N);
     R kappab = qFb * gTn;
     R gTb[3];
@@ -519,7 +529,7 @@ AFVM_HD void viscous_vjp(const Phys& P, R TL, R TR, const R* UL, const R* UR, R 
         tmp2[i] = (gU[3 * i] + gU[i]) * N[0] + (gU[3 * i + 1] + gU[3 + i]) * N[1] + (gU[3 * i + 2] + gU[6 + i]) * N[2];
         sigma[i] = mu * (tmp2[i] - R(2.0 / 3) * tmp3 * N[i]);
     }
-    viscous_vjp_t<R>(P, TF, UF, mu, dmu, dot3(gT, N), tmp2, tmp3, sigma, D, N, rdel, Fb, TLb, TRb, ULb, URb, TFb, UFb,
+    viscous_vjp_t<R>(P, TF, UF, mu, dmu, dot3(gT, N), tmp2, tmp3, R(1), sigma, D, N, rdel, Fb, TLb, TRb, ULb, URb, TFb, UFb,
                      gTFb, gUFb);
 }
 
@@ -652,12 +662,15 @@ AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>&
 
         R TFb = R(0), UFb[3] = {R(0), R(0), R(0)}, gTFb[3] = {R(0), R(0), R(0)}, gUFb[9];
         for (int k = 0; k < 9; k++) gUFb[k] = R(0);
-        R tmp2[3], sigma[3], tmp3, mu = t.get(T_MU), dmu;
+        R tmp2[3], sigma[3], tmp3, mu = t.get(T_MU), dmu, ts;
         if constexpr (Src::kFull) {
+            // the taped stress terms are the forward's divided by its scale (viscous())
             for (int k = 0; k < 3; k++) { tmp2[k] = t.get(T_TMP2 + k); sigma[k] = t.get(T_SIG + k); }
             tmp3 = t.get(T_TMP3);
             dmu = t.get(T_DMU);
+            ts = chr ? R(1) : R(0.5);
         } else {
+            ts = R(1);
             viscosity<R>(P, TF, &dmu);
             // the stress terms from the corrected face gradient, as viscous() forms them
             R gUl[9];
@@ -669,7 +682,7 @@ AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>&
                 sigma[i] = mu * (tmp2[i] - R(2.0 / 3) * tmp3 * in.N[i]);
             }
         }
-        viscous_vjp_t<R>(P, TF, UF, mu, dmu, t.get(T_GTN), tmp2, tmp3, sigma, in.D, in.N, in.rdelta, Fb, o.TP, o.TN, o.UP,
+        viscous_vjp_t<R>(P, TF, UF, mu, dmu, t.get(T_GTN), tmp2, tmp3, ts, sigma, in.D, in.N, in.rdelta, Fb, o.TP, o.TN, o.UP,
                          o.UN, TFb, UFb, gTFb, gUFb);
         if constexpr (kGeo<G>) {
             R gTF[3], gUF[9];

@@ -378,10 +378,7 @@ AFVM_HD void roe(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R* UR
     R hR = Cp * TR + R(0.5) * dot3(UR, UR);
     tp.put(T_HL, hL);
     tp.put(T_HR, hR);
-    R fr = R(0.5) * (rhoUnL + rhoUnR);
-    R fu[3], UF[3], dU[3];
-    for (int k = 0; k < 3; k++) fu[k] = R(0.5) * (rhoUnL * UL[k] + rhoUnR * UR[k] + (pL + pR) * N[k]);
-    R fe = R(0.5) * (rhoUnL * hL + rhoUnR * hR);
+    R UF[3], dU[3];
     R rsL = rsqrt_(rhoL), rsR = rsqrt_(rhoR);
     R sL = rhoL * rsL, sR = rhoR * rsR;
     R rD = rcp(sL + sR);
@@ -450,9 +447,13 @@ AFVM_HD void roe(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R* UR
     tp.put(T_ABV5, abv5);
     tp.put(T_ABV6, abv6);
     tp.put(T_ABV7, abv7);
-    F[0] = fr - R(0.5) * (lam1 * drho + abv6);
-    for (int k = 0; k < 3; k++) F[1 + k] = fu[k] - R(0.5) * (lam1 * dU[k] + UF[k] * abv6 - abv7 * N[k]);
-    F[4] = fe - R(0.5) * (lam1 * drhoE + hF * abv6 - UnF * abv7);
+    // central flux minus the dissipation, (F_L + F_R)/2 - |A| dq/2, with the common half taken
+    // once: the pressure term's N and the dissipation's abv7 N share one product
+    F[0] = R(0.5) * ((rhoUnL + rhoUnR) - (lam1 * drho + abv6));
+    const R pa = (pL + pR) + abv7;
+    for (int k = 0; k < 3; k++)
+        F[1 + k] = R(0.5) * (rhoUnL * UL[k] + rhoUnR * UR[k] + pa * N[k] - lam1 * dU[k] - UF[k] * abv6);
+    F[4] = R(0.5) * (rhoUnL * hL + rhoUnR * hR - lam1 * drhoE - hF * abv6 + UnF * abv7);
 }
 
 // riemann.eulerLaxFriedrichs (adFVM/riemann.py:6-18)
@@ -585,43 +586,49 @@ AFVM_HD void laxf_gauge(const Phys& P, R pgL, R pgR, R TgL, R TgR, const R* UL, 
 }
 
 // RCF.viscousFlux (adFVM/density.py:192-222): adds -sigma to F[1..3] and -(q + sigma.UF) to F[4];
-// rdel = 1/deltas (a mesh table), the divisor of snGrad (op.py:66-67)
+// rdel = 1/deltas (a mesh table), the divisor of snGrad (op.py:66-67). The face velocity and
+// gradients arrive as hs times Us, gTs, gUs: hs = 1/2 with the two sides' sums (the reference's
+// averages), hs = 1 with the ghost's values (rhs = 1/hs). The corrected gradients are formed
+// divided by hs, and so are the (grad U + grad U^T).n and tr grad U the tape keeps (the VJP
+// scales them back); sigma, (grad T).n and the flux are the reference's.
 template <typename R, typename Sink = TapeNone>
-AFVM_HD void viscous(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, const R* UF,
-                                        const R* gTF, const R* gUF, const R* D, const R* N, R rdel, R* F,
-                                        Sink&& tp = Sink()) {
+AFVM_HD void viscous(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, const R* Us, const R* gTs,
+                     const R* gUs, R hs, R rhs, const R* D, const R* N, R rdel, R* F, Sink&& tp = Sink()) {
     R dmu;
     R mu = viscosity<R>(P, TF, &dmu);
     tp.put(T_MU, mu);
     tp.put(T_DMU, dmu);
     R kappa = mu * consts<R>(P).kFac;
-    // the face gradient with its normal component replaced by snGrad: g + (snGrad - g.D) D
-    R gTD = dot3(gTF, D);
-    R cT = (TR - TL) * rdel - gTD;
+    // the face gradient with its normal component replaced by snGrad: g + (snGrad - g.D) D,
+    // here divided by hs
+    R rdh = rdel * rhs;
+    R gTD = dot3(gTs, D);
+    R cT = (TR - TL) * rdh - gTD;
     R gT[3];
-    for (int k = 0; k < 3; k++) gT[k] = gTF[k] + cT * D[k];
+    for (int k = 0; k < 3; k++) gT[k] = gTs[k] + cT * D[k];
     R gU[9];
     for (int i = 0; i < 3; i++) {
-        R gUD = gUF[3 * i] * D[0] + gUF[3 * i + 1] * D[1] + gUF[3 * i + 2] * D[2];
-        R cU = (UR[i] - UL[i]) * rdel - gUD;
-        for (int k = 0; k < 3; k++) gU[3 * i + k] = gUF[3 * i + k] + cU * D[k];
+        R gUD = gUs[3 * i] * D[0] + gUs[3 * i + 1] * D[1] + gUs[3 * i + 2] * D[2];
+        R cU = (UR[i] - UL[i]) * rdh - gUD;
+        for (int k = 0; k < 3; k++) gU[3 * i + k] = gUs[3 * i + k] + cU * D[k];
     }
-    R gTn = dot3(gT, N);
+    R gTn = hs * dot3(gT, N);
     tp.put(T_GTN, gTn);
     R qF = kappa * gTn;
     R tmp3 = gU[0] + gU[4] + gU[8];
     tp.put(T_TMP3, tmp3);
+    R muh = mu * hs;
     R sigma[3];
     for (int i = 0; i < 3; i++) {
         R tmp2 = (gU[3 * i] + gU[i]) * N[0] + (gU[3 * i + 1] + gU[3 + i]) * N[1] + (gU[3 * i + 2] + gU[6 + i]) * N[2];
-        sigma[i] = mu * (tmp2 - R(2.0 / 3) * tmp3 * N[i]);
+        sigma[i] = muh * (tmp2 - R(2.0 / 3) * tmp3 * N[i]);
         tp.put(T_TMP2 + i, tmp2);
         tp.put(T_SIG + i, sigma[i]);
     }
     F[1] = F[1] + (-sigma[0]);
     F[2] = F[2] + (-sigma[1]);
     F[3] = F[3] + (-sigma[2]);
-    F[4] = F[4] + (-(qF + dot3(sigma, UF)));
+    F[4] = F[4] + (-(qF + hs * dot3(sigma, Us)));
 }
 
 }  // namespace afvm

@@ -91,12 +91,12 @@ STEP_BYTES = {('primal', 8): 2904, ('primal', 4): 1524, ('adjoint', 8): 6288, ('
 # the untaped and FP32 ones from earlier captures of the same kernels.
 MEASURED_TRAFFIC = {('k_flux', 8): (172.68e6, 798720), ('k_flux', 4): (81.56e6, 798720),
                     ('k_adj_flux', 8): (407.63e6, 798720), ('k_adj_flux', 4): (170.37e6, 798720),
-                    ('k_flux+tape', 8): (522.3e6, 798720), ('k_adj_flux+tape', 8): (727.8e6, 798720)}
+                    ('k_flux+tape', 8): (522.4e6, 798720), ('k_adj_flux+tape', 8): (727.6e6, 798720)}
 # FP64 thread instructions per face (DADD, DMUL, DFMA) of a launch in the same captures
 # (smsp__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on); the forward flux issues the same
 # FP64 instructions with or without the tape writes
-MEASURED_FP64_INST = {'k_flux': (64.0, 132.4, 171.9), 'k_adj_flux': (108.0, 307.9, 456.9),
-                      'k_flux+tape': (64.0, 132.4, 171.9), 'k_adj_flux+tape': (47.0, 92.0, 227.9)}
+MEASURED_FP64_INST = {'k_flux': (68.0, 115.4, 165.9), 'k_adj_flux': (108.0, 307.9, 456.9),
+                      'k_flux+tape': (68.0, 115.4, 165.9), 'k_adj_flux+tape': (47.0, 93.0, 227.9)}
 
 
 def measured_traffic(kernel, es, nF):
