@@ -48,3 +48,14 @@ def test_reference_arm_line():
         assert k in line, k
     assert line['impl'] == 'reference' and line['value'] > 0
     assert line['e2e']['h2d_bytes_per_step'] == 0 and line['cpu_baseline']['kind'] in ('port', 'reference')
+
+
+def test_reference_python_fixture():
+    """The reference's own primal timing (oracle/time_reference.py, measured where the reference
+    checkout is) is read into the bench line's reference_python with where it was measured."""
+    import bench
+    rp = bench.reference_python()
+    assert rp is not None
+    assert rp['value'] > 0 and rp['unit'].startswith('primal')
+    assert 'not on the GPU box' in rp['measured']
+    assert set(rp['cases']) >= {'box16', 'box32'}
