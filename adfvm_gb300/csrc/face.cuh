@@ -55,7 +55,7 @@ AFVM_HD void zero_geo(GeoBar<R>& g) {
 template <typename R>
 AFVM_HD void face_flux_gauge(const Phys& P, int kind, bool inviscid, const FaceIn<R>& in, R* F, R& maxaF) {
     const PhysR<R>& Q = consts<R>(P);
-    R TF, Us[3], gTs[3], gUs[9], hs, rhs;
+    R TF, Us[3], gTs[3], gUs[9];
     if (kind == FACE_BOUNDARY) {
         // RCF.boundaryFlux: (rho Un, rho U Un + p N, rho h Un) less gP N and gH rho Un
         R rho, rhoU[3], rhoE;
@@ -68,7 +68,6 @@ AFVM_HD void face_flux_gauge(const Phys& P, int kind, bool inviscid, const FaceI
         TF = in.TN + Q.gT;
         for (int k = 0; k < 3; k++) { Us[k] = in.UN[k]; gTs[k] = in.gTN[k]; }
         for (int k = 0; k < 9; k++) gUs[k] = in.gUN[k];
-        hs = R(1); rhs = R(1);
     } else {
         R ULF[3], TLF, pLF, URF[3], TRF, pRF;
         for (int k = 0; k < 3; k++) ULF[k] = recon<R>(in.UP[k], in.UN[k], in.gUP + 3 * k, in.lw0, in.qw0);
@@ -97,17 +96,17 @@ AFVM_HD void face_flux_gauge(const Phys& P, int kind, bool inviscid, const FaceI
             TF = in.TN + Q.gT;
             for (int k = 0; k < 3; k++) { Us[k] = in.UN[k]; gTs[k] = in.gTN[k]; }
             for (int k = 0; k < 9; k++) gUs[k] = in.gUN[k];
-            hs = R(1); rhs = R(1);
         } else {
+            // the face averages themselves (scale 1 below: the float kernel, capped at 64
+            // registers, spills less than with the sums and a runtime scale)
             TF = R(0.5) * (TLF + TRF) + Q.gT;
-            for (int k = 0; k < 3; k++) { Us[k] = ULF[k] + URF[k]; gTs[k] = in.gTP[k] + in.gTN[k]; }
-            for (int k = 0; k < 9; k++) gUs[k] = in.gUP[k] + in.gUN[k];
-            hs = R(0.5); rhs = R(2);
+            for (int k = 0; k < 3; k++) { Us[k] = R(0.5) * (ULF[k] + URF[k]); gTs[k] = R(0.5) * (in.gTP[k] + in.gTN[k]); }
+            for (int k = 0; k < 9; k++) gUs[k] = R(0.5) * (in.gUP[k] + in.gUN[k]);
         }
     }
-    if (!inviscid) viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, Us, gTs, gUs, hs, rhs, in.D, in.N, in.rdelta, F);
+    if (!inviscid) viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, Us, gTs, gUs, R(1), R(1), in.D, in.N, in.rdelta, F);
     R aF = sqrt_(Q.Cp * TF * Q.gm1);
-    maxaF = fabs(hs * dot3(Us, in.N)) + aF;
+    maxaF = fabs(dot3(Us, in.N)) + aF;
 }
 
 // flux (rho, rhoU, rhoE) through the face and the CFL term |U.n| + a; the tape values of a
