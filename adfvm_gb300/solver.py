@@ -29,6 +29,7 @@ The GPU library is mandatory: there is no CPU path.
 import collections
 import ctypes as C
 import os
+import sys
 
 import numpy as np
 
@@ -369,10 +370,25 @@ class RCF(object):
         dev = 'cuda:%d' % self.device
         return [L.to_device(a, torch.empty(a.shape, dtype=td, device=dev)) for a in self._host_fields(arrays)]
 
-    @staticmethod
-    def download(tensors, dtype=np.float64):
-        """New host arrays of `dtype` holding the device tensors (pipelined host copy)."""
-        return [L.to_host(t, np.empty(tuple(t.shape), dtype)) for t in tensors]
+    def download(self, tensors, dtype=np.float64):
+        """Host arrays of `dtype` holding the device tensors (pipelined host copy). An array this
+        context returned before is written again only when nothing else refers to it any more
+        (its reference count shows only this context's pool): a caller that keeps a result, or
+        a view of it, keeps its values. The reused arrays' pages are already mapped, so the copy
+        runs at the link's rate instead of the first-touch page-fault rate of a new array."""
+        return [L.to_host(t, self._host_array(tuple(t.shape), dtype)) for t in tensors]
+
+    def _host_array(self, shape, dtype):
+        pool = self.__dict__.setdefault('_hostPool', [])
+        dtype = np.dtype(dtype)
+        for i in range(len(pool)):
+            # 2: the pool's own reference and getrefcount's argument
+            if pool[i].shape == shape and pool[i].dtype == dtype and sys.getrefcount(pool[i]) == 2:
+                return pool[i]
+        a = np.empty(shape, dtype)
+        if len(pool) < 12:
+            pool.append(a)
+        return a
 
     def _fingerprint(self, arrays, dt):
         parts = [repr(float(dt)).encode(), str(getattr(self, '_bcVersion', 0)).encode()]
