@@ -179,9 +179,10 @@ def describe(case, precision):
 
 
 def reference_python():
-    """The reference's own primal path (its Solver.run through the NumPy adpy stand-in), timed
-    in the build container by oracle/time_reference.py - the GPU machine has no reference checkout -
-    and read from the fixture that script writes; None without it."""
+    """The reference's own primal path (its Solver.run through the NumPy adpy stand-in), timed by
+    oracle/time_reference.py on a development host that has the reference checkout (the machines
+    that run this benchmark have none) and read from the fixture that script writes; None
+    without it."""
     path = os.path.join(ROOT, 'oracle', 'reference_timing.json')
     try:
         with open(path) as f:
@@ -191,9 +192,9 @@ def reference_python():
     c = max(d['cases'], key=lambda x: x['cells'])
     return {'value': c['primal_mcell_steps_per_s'], 'unit': 'primal ' + UNIT, 'workload': c['workload'],
             'threads': d['threads'], 'host': '%s, %s cores' % (d['host'], d['cores']),
-            'measured': 'in the build container on %s (oracle/time_reference.py; not on the GPU box, which has '
-                        'no reference checkout); the reference adjoint (adpy reverse mode) is absent from the '
-                        'checkout' % d['measured_utc'],
+            'measured': 'on a development host with the reference checkout, %s (oracle/time_reference.py; not '
+                        'on the benchmark machine, which has no checkout); the reference adjoint (adpy reverse '
+                        'mode) is absent from the checkout' % d['measured_utc'],
             'cases': {x['workload'].split(':')[0]: x['primal_mcell_steps_per_s'] for x in d['cases']}}
 
 

@@ -1,11 +1,13 @@
-"""Time the reference's own primal path on CPU (test infrastructure, this container only).
+"""Time the reference's own primal path on CPU (test infrastructure; runs where the reference
+checkout is).
 
 The reference's ``Solver.run`` (adFVM/solver.py:210-411) in forward mode, its RCF step
 (adFVM/density.py:339-414) evaluated through the NumPy adpy stand-in of ``oracle/refshim`` and
 its own cmesh (``oracle/refrun.py``), on the periodic jittered boxes 16^3 and 32^3 of the
-throughput recipe. The GPU machine has no reference checkout, so the numbers are measured here and
-written to ``oracle/reference_timing.json``, which ``bench.py`` reports as ``reference_python``
-beside its CPU baseline (the C/OpenMP restatement, timed on the GPU machine). The reference's
+throughput recipe. The machines that run the benchmark have no reference checkout, so the
+numbers are measured here and written to ``oracle/reference_timing.json``, which ``bench.py``
+reports as ``reference_python`` beside its CPU baseline (the C/OpenMP restatement, timed where
+the benchmark runs). The reference's
 adjoint runs through adpy's reverse mode, which the checkout does not contain: only the primal
 is timed.
 

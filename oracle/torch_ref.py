@@ -1,7 +1,7 @@
 """Oracle: CPU float64 restatement of the reference's residual, SSP-RK3 step and objectives.
 
 TEST INFRASTRUCTURE ONLY. Imported by tests/, __graft_entry__.smoke() and bench.py's CPU
-baseline as the checker; the product never calls it.
+baseline as the reference the GPU results are compared with; the product never calls it.
 
 Written in torch (CPU, float64) so that ``torch.autograd`` of the same code gives the exact
 discrete adjoint of a step (the reference obtains its adjoint by automatic differentiation

@@ -57,5 +57,5 @@ def test_reference_python_fixture():
     rp = bench.reference_python()
     assert rp is not None
     assert rp['value'] > 0 and rp['unit'].startswith('primal')
-    assert 'not on the GPU box' in rp['measured']
+    assert 'not on the benchmark machine' in rp['measured']
     assert set(rp['cases']) >= {'box16', 'box32'}

@@ -1,5 +1,5 @@
 """The oracle's parameter gradients (torch_ref.vjp_step_params: autograd with the mesh tensors
-or one boundary input as leaves, the checker of the GPU's afvm_adjoint_step_params) against
+or one boundary input as leaves, the oracle of the GPU's afvm_adjoint_step_params) against
 central finite differences of the oracle's own step, so that every use of a parameter in the
 restated residual is seen by the leaves."""
 import numpy as np
