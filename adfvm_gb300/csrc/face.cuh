@@ -70,9 +70,12 @@ AFVM_HD void face_flux_gauge(const Phys& P, int kind, bool inviscid, const FaceI
         for (int k = 0; k < 9; k++) gUs[k] = in.gUN[k];
     } else {
         R ULF[3], TLF, pLF, URF[3], TRF, pRF;
-        for (int k = 0; k < 3; k++) ULF[k] = recon<R>(in.UP[k], in.UN[k], in.gUP + 3 * k, in.lw0, in.qw0);
-        TLF = recon<R>(in.TP, in.TN, in.gTP, in.lw0, in.qw0);
-        pLF = recon<R>(in.pP, in.pN, in.gpP, in.lw0, in.qw0);
+        // the jumps neighbour - owner, shared by the two sides' reconstructions
+        R dU[3], dT = in.TN - in.TP, dp = in.pN - in.pP;
+        for (int k = 0; k < 3; k++) dU[k] = in.UN[k] - in.UP[k];
+        for (int k = 0; k < 3; k++) ULF[k] = recon<R>(in.UP[k], dU[k], in.gUP + 3 * k, in.lw0, in.qw0);
+        TLF = recon<R>(in.TP, dT, in.gTP, in.lw0, in.qw0);
+        pLF = recon<R>(in.pP, dp, in.gpP, in.lw0, in.qw0);
         R rhoL, rhoUL[3], rhoEL, rdL, rdR;
         conservative<R>(P, ULF, TLF + Q.gT, pLF + Q.gP, rhoL, rhoUL, rhoEL, &rdL);
         int solver;
@@ -81,9 +84,9 @@ AFVM_HD void face_flux_gauge(const Phys& P, int kind, bool inviscid, const FaceI
             TRF = in.TN; pRF = in.pN;
             solver = P.briemann;
         } else {
-            for (int k = 0; k < 3; k++) URF[k] = recon<R>(in.UN[k], in.UP[k], in.gUN + 3 * k, in.lw1, in.qw1);
-            TRF = recon<R>(in.TN, in.TP, in.gTN, in.lw1, in.qw1);
-            pRF = recon<R>(in.pN, in.pP, in.gpN, in.lw1, in.qw1);
+            for (int k = 0; k < 3; k++) URF[k] = recon<R>(in.UN[k], -dU[k], in.gUN + 3 * k, in.lw1, in.qw1);
+            TRF = recon<R>(in.TN, -dT, in.gTN, in.lw1, in.qw1);
+            pRF = recon<R>(in.pN, -dp, in.gpN, in.lw1, in.qw1);
             solver = P.riemann;
         }
         R rhoR, rhoUR[3], rhoER;
@@ -134,9 +137,12 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
         hs = R(1); rhs = R(1);
     } else {
         R ULF[3], TLF, pLF, URF[3], TRF, pRF;
-        for (int k = 0; k < 3; k++) ULF[k] = recon<R>(in.UP[k], in.UN[k], in.gUP + 3 * k, in.lw0, in.qw0);
-        TLF = recon<R>(in.TP, in.TN, in.gTP, in.lw0, in.qw0);
-        pLF = recon<R>(in.pP, in.pN, in.gpP, in.lw0, in.qw0);
+        // the jumps neighbour - owner, shared by the two sides' reconstructions
+        R dU[3], dT = in.TN - in.TP, dp = in.pN - in.pP;
+        for (int k = 0; k < 3; k++) dU[k] = in.UN[k] - in.UP[k];
+        for (int k = 0; k < 3; k++) ULF[k] = recon<R>(in.UP[k], dU[k], in.gUP + 3 * k, in.lw0, in.qw0);
+        TLF = recon<R>(in.TP, dT, in.gTP, in.lw0, in.qw0);
+        pLF = recon<R>(in.pP, dp, in.gpP, in.lw0, in.qw0);
         R rhoL, rhoUL[3], rhoEL, rdL, rdR;
         conservative<R>(P, ULF, TLF, pLF, rhoL, rhoUL, rhoEL, &rdL);
         int solver;
@@ -145,9 +151,9 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
             TRF = in.TN; pRF = in.pN;
             solver = P.briemann;
         } else {
-            for (int k = 0; k < 3; k++) URF[k] = recon<R>(in.UN[k], in.UP[k], in.gUN + 3 * k, in.lw1, in.qw1);
-            TRF = recon<R>(in.TN, in.TP, in.gTN, in.lw1, in.qw1);
-            pRF = recon<R>(in.pN, in.pP, in.gpN, in.lw1, in.qw1);
+            for (int k = 0; k < 3; k++) URF[k] = recon<R>(in.UN[k], -dU[k], in.gUN + 3 * k, in.lw1, in.qw1);
+            TRF = recon<R>(in.TN, -dT, in.gTN, in.lw1, in.qw1);
+            pRF = recon<R>(in.pN, -dp, in.gpN, in.lw1, in.qw1);
             solver = P.riemann;
         }
         R rhoR, rhoUR[3], rhoER;
@@ -198,7 +204,7 @@ AFVM_HD void conservative_vjp_t(const Phys& P, const R* U, R T, R p, R rd, R rho
 template <typename R>
 AFVM_HD void conservative_vjp(const Phys& P, const R* U, R T, R p, R rhob, const R* rhoUb, R rhoEb, R* Ub,
                               R& Tb, R& pb) {
-    R rd = rcp(consts<R>(P).Cv * T * consts<R>(P).gm1);
+    R rd = rcp(T * consts<R>(P).Rg);          // as conservative()
     conservative_vjp_t<R>(P, U, T, p, rd, rhob, rhoUb, rhoEb, Ub, Tb, pb);
 }
 
@@ -225,14 +231,14 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R
     R raF = t.get(T_RAF);
     R rcL = t.get(T_RCL), rcR = t.get(T_RCR);
     R re = t.get(T_RE);
-    R rhoUnL, rhoUnR, sL, sR, cL, cR;
+    R rhoUnL, rhoUnR, wL, wR, cL, cR;
     if constexpr (Src::kFull) {
         rhoUnL = t.get(T_RUNL); rhoUnR = t.get(T_RUNR);
-        sL = t.get(T_SL); sR = t.get(T_SR);
+        wL = t.get(T_WL); wR = t.get(T_WR);
         cL = t.get(T_CL); cR = t.get(T_CR);
     } else {
         rhoUnL = rhoL * UnL; rhoUnR = rhoR * UnR;
-        sL = rhoL * rsL; sR = rhoR * rsR;
+        wL = (rhoL * rsL) * rD; wR = (rhoR * rsR) * rD;
         R c2L = gRg * TL, c2R = gRg * TR;
         cL = c2L > R(0) ? c2L * rcL : R(0); cR = c2R > R(0) ? c2R * rcR : R(0);
     }
@@ -255,15 +261,13 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R
     if constexpr (!Src::kFull) {
         hL = Cp * TL + h * dot3(UL, UL);
         hR = Cp * TR + h * dot3(UR, UR);
-        for (int k = 0; k < 3; k++) UF[k] = (UL[k] * sL + UR[k] * sR) * rD;
-        hF = (hL * sL + hR * sR) * rD;
+        for (int k = 0; k < 3; k++) UF[k] = UL[k] * wL + UR[k] * wR;
+        hF = hL * wL + hR * wR;
         qF = h * dot3(UF, UF);
         UnF = dot3(UF, N);
         for (int k = 0; k < 3; k++) dU[k] = rhoR * UR[k] - rhoL * UL[k];
         drhoE = (hR * rhoR - pR) - (hL * rhoL - pL);
-        eps = h * fabs(ea);
-        eps = eps + h * fabs(eb_);
-        eps = eps + consts<R>(P).small;      // eps >= 0 (roe())
+        eps = h * (fabs(ea) + fabs(eb_)) + consts<R>(P).small;      // eps >= 0 (roe())
     }
     R aF, ra2F;
     if constexpr (Src::kFull) {
@@ -274,8 +278,7 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R
         ra2F = raF * raF;
     }
     R l1 = fabs(UnF), l2 = fabs(UnF + aF), l3 = fabs(UnF - aF);
-    R eps2 = R(2) * eps;
-    bool s1 = lt_nonneg(l1, eps2), s2 = lt_nonneg(l2, eps2), s3 = lt_nonneg(l3, eps2);
+    bool s1 = lt_twice(l1, eps), s2 = lt_twice(l2, eps), s3 = lt_twice(l3, eps);
     if constexpr (!Src::kFull) {
         L1 = s1 ? R(0.25) * l1 * l1 * re + eps : l1;
         L2 = s2 ? R(0.25) * l2 * l2 * re + eps : l2;
@@ -372,7 +375,6 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R
     for (int k = 0; k < 3; k++) UFb[k] += qFb * UF[k];
     // hF = hL wL + hR wR, UF = UL wL + UR wR with the weights wL = sL/(sL + sR), wR = sR/(sL + sR):
     // d/dsL of (xL sL + xR sR)/(sL + sR) = (xL - xR) wR/(sL + sR), d/dsR = -(xL - xR) wL/(sL + sR)
-    R wL = sL * rD, wR = sR * rD;
     hLb += hFb * wL;
     hRb += hFb * wR;
     for (int k = 0; k < 3; k++) {

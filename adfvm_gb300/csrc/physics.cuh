@@ -38,7 +38,7 @@ constexpr int FACE_INTERNAL = 0, FACE_COUPLED = 1, FACE_CHARACTERISTIC = 2, FACE
 // square roots, mu(T_F), the Roe and viscous intermediates. The forward flux writes them through
 // a sink (nothing, a local array, or a column of a device tape); the VJP reads them back.
 constexpr int T_ULF = 0, T_TLF = 3, T_PLF = 4, T_URF = 5, T_TRF = 8, T_PRF = 9;   // face states
-constexpr int T_RDL = 10, T_RDR = 11;            // 1/(Cv T (g-1)) of each side (conservative)
+constexpr int T_RDL = 10, T_RDR = 11;            // 1/(Rg T), Rg = Cv (g-1), of each side (conservative)
 constexpr int T_UNL = 12, T_UNR = 13;            // U.n of each side
 constexpr int T_RSL = 14, T_RSR = 15;            // 1/sqrt(rho)
 constexpr int T_RD = 16, T_RAF = 17;             // 1/(sL + sR), 1/a_F (Roe average)
@@ -55,9 +55,10 @@ constexpr int T_L1 = 36, T_L2 = 37, T_L3 = 38;   // |eigenvalues| after the entr
 constexpr int T_ABV4 = 39, T_ABV5 = 40, T_ABV6 = 41, T_ABV7 = 42;
 // viscous intermediates: (grad U + grad U^T).n (3), sigma (3), tr grad U (corrected face gradient)
 constexpr int T_TMP2 = 43, T_SIG = 46, T_TMP3 = 49;
-// more Roe forward values, so that the reverse sweep re-derives none: rho U.n and sqrt(rho) of
-// each side, the sound speeds, the Roe-average sound speed and 1/a_F^2, and abv2, abv3
-constexpr int T_RUNL = 50, T_RUNR = 51, T_SL = 52, T_SR = 53, T_CL = 54, T_CR = 55;
+// more Roe forward values, so that the reverse sweep re-derives none: rho U.n and the Roe
+// weight sqrt(rho)/(sqrt(rhoL) + sqrt(rhoR)) of each side, the sound speeds, the Roe-average
+// sound speed and 1/a_F^2, and abv2, abv3
+constexpr int T_RUNL = 50, T_RUNR = 51, T_WL = 52, T_WR = 53, T_CL = 54, T_CR = 55;
 constexpr int T_AF = 56, T_RA2F = 57, T_ABV2 = 58, T_ABV3 = 59;
 constexpr int T_DMU = 60;                        // d mu / d T at T_F
 constexpr int TAPE = 61;
@@ -216,15 +217,33 @@ AFVM_HD bool lt_nonneg(R a, R b) {
 #endif
 }
 
+// a < 2 b for non-negative a and a positive normal b, as a/2 < b: on the device a's exponent
+// field is lowered by one with an integer subtraction (exact for normal a; a zero or
+// subnormal a turns negative and compares below b, as a/2 does), so no FP64 product is issued.
+// An inf or NaN b compares above every finite a, as 2 b does.
+template <typename R>
+AFVM_HD bool lt_twice(R a, R b) {
+#if defined(__CUDA_ARCH__)
+    if constexpr (sizeof(R) == 8) return __double_as_longlong(a) - (1LL << 52) < __double_as_longlong(b);
+    else return __float_as_int(a) - (1 << 23) < __float_as_int(b);
+#else
+    return a < R(2) * b;
+#endif
+}
+
 // ---- reciprocal and reciprocal square root
 //
 // On the GB300 the FP64 pipe runs at 1/57 of the FP32 rate, and an IEEE FP64 division or
 // square root costs about nine FP64 instructions. In double these are built here from a
-// 23-bit FP32 seed (PTX rcp.approx / rsqrt.approx on the mantissa, the exponent handled with
-// integer operations, so no FP64 conversion instruction is issued) and two Newton-Raphson
-// steps - y <- y + y (1 - x y) for 1/x, y <- y + y (1 - x y^2)/2 for 1/sqrt(x) - each of which
-// doubles the number of correct bits (23 -> 46 -> full precision): a relative error of about
-// one unit in the last place, against half a unit for the IEEE operations. Arguments outside
+// 23-bit FP32 seed y (PTX rcp.approx / rsqrt.approx on the mantissa, the exponent handled with
+// integer operations, so no FP64 conversion instruction is issued) and one third-order
+// correction from the series of the exact answer in the seed's residual e (|e| < 2^-21):
+//   1/x       = y / (1 - e)        = y (1 + e + e^2 + ...),          e = 1 - x y
+//   1/sqrt(x) = y (1 - e)^(-1/2)   = y (1 + e/2 + 3 e^2/8 + ...),    e = 1 - x y^2
+// The dropped terms are below 2^-63 relative. The seed has 24 significant bits, so x y is
+// formed exactly inside the FMA and y^2 is exact in double; the last FMA rounds once: about
+// half a unit in the last place, as the IEEE operations (3 FP64 instructions for 1/x and 5
+// for 1/sqrt(x), against 4 and 8 for two Newton-Raphson steps). Arguments outside
 // 2^[-120, 120] (and 0, inf, NaN) take the IEEE operation. In float the hardware
 // approximations are used directly (about two units in the last place).
 #if defined(__CUDACC__)
@@ -242,9 +261,7 @@ __device__ __forceinline__ double rcp_nr(double x) {
                               ((unsigned long long)dexp << 52) | ((unsigned long long)(rb & 0x7fffffu) << 29);
     double y = __longlong_as_double((long long)bits);
     double e = fma(-x, y, 1.0);
-    y = fma(y, e, y);
-    e = fma(-x, y, 1.0);
-    return fma(y, e, y);
+    return fma(y, fma(e, e, e), y);
 }
 
 __device__ __forceinline__ double rsqrt_nr(double x) {
@@ -263,12 +280,8 @@ __device__ __forceinline__ double rsqrt_nr(double x) {
     long long dexp = (long long)((int)(rb >> 23) - 127 - half + 1023);
     unsigned long long bits = ((unsigned long long)dexp << 52) | ((unsigned long long)(rb & 0x7fffffu) << 29);
     double y = __longlong_as_double((long long)bits);
-    double t = y * y;
-    double e = fma(-x, t, 1.0);
-    y = fma(0.5 * y, e, y);
-    t = y * y;
-    e = fma(-x, t, 1.0);
-    return fma(0.5 * y, e, y);
+    double e = fma(-x, y * y, 1.0);
+    return fma(y * e, fma(e, 0.375, 0.5), y);
 }
 #endif
 
@@ -345,7 +358,7 @@ AFVM_HD R viscosity(const Phys& P, R T, R* dmu = nullptr) {
 template <typename R>
 AFVM_HD void conservative(const Phys& P, const R* U, R T, R p, R& rho, R* rhoU, R& rhoE, R* rdOut = nullptr) {
     R e = consts<R>(P).Cv * T;
-    R rd = rcp(e * consts<R>(P).gm1);
+    R rd = rcp(T * consts<R>(P).Rg);        // 1/(e (g-1)); e itself only for rhoE
     if (rdOut) *rdOut = rd;
     rho = p * rd;
     rhoE = rho * (e + R(0.5) * dot3(U, U));
@@ -353,10 +366,11 @@ AFVM_HD void conservative(const Phys& P, const R* U, R T, R p, R& rho, R* rhoU, 
 }
 
 // interp.secondOrder for one side (adFVM/interp.py:20-28): phiC + (phiD-phiC)*lw + qw.grad,
-// as one chain of FMAs
+// as one chain of FMAs, given dCD = phiD - phiC. A face's two sides share one difference: the
+// neighbour side passes the owner side's negated, the same number as its own phiD - phiC.
 template <typename R>
-AFVM_HD R recon(R phiC, R phiD, const R* g, R lw, const R* qw) {
-    R phiF = phiC + (phiD - phiC) * lw;
+AFVM_HD R recon(R phiC, R dCD, const R* g, R lw, const R* qw) {
+    R phiF = phiC + dCD * lw;
     return qw[2] * g[2] + (qw[1] * g[1] + (qw[0] * g[0] + phiF));
 }
 
@@ -382,13 +396,15 @@ AFVM_HD void roe(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R* UR
     R rsL = rsqrt_(rhoL), rsR = rsqrt_(rhoR);
     R sL = rhoL * rsL, sR = rhoR * rsR;
     R rD = rcp(sL + sR);
+    // the Roe averages with the weights sL/(sL + sR), sR/(sL + sR) formed once
+    R wL = sL * rD, wR = sR * rD;
     tp.put(T_RSL, rsL);
     tp.put(T_RSR, rsR);
-    tp.put(T_SL, sL);
-    tp.put(T_SR, sR);
+    tp.put(T_WL, wL);
+    tp.put(T_WR, wR);
     tp.put(T_RD, rD);
-    for (int k = 0; k < 3; k++) UF[k] = (UL[k] * sL + UR[k] * sR) * rD;
-    R hF = (hL * sL + hR * sR) * rD;
+    for (int k = 0; k < 3; k++) UF[k] = UL[k] * wL + UR[k] * wR;
+    R hF = hL * wL + hR * wR;
     R qF = R(0.5) * dot3(UF, UF);
     R a2F = gm1 * (hF - qF);
     R raF = rsqrt_(a2F);
@@ -416,13 +432,11 @@ AFVM_HD void roe(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R* UR
     tp.put(T_CL, cL);
     tp.put(T_CR, cR);
     // the entropy-fix width; eps >= 0 (a sum of magnitudes), so the reference's
-    // eps < 0 ? eps - small : eps + small is eps + small
-    R eps = R(0.5) * fabs(UnL - UnR);
-    eps = eps + R(0.5) * fabs(cL - cR);
-    eps = eps + consts<R>(P).small;
-    R eps2 = R(2) * eps;
+    // eps < 0 ? eps - small : eps + small is eps + small. 0.5 |a| + 0.5 |b| is taken as
+    // 0.5 (|a| + |b|): halving is exact, so the bits are the same.
+    R eps = R(0.5) * (fabs(UnL - UnR) + fabs(cL - cR)) + consts<R>(P).small;
     R re = R(0);
-    bool s1 = lt_nonneg(lam1, eps2), s2 = lt_nonneg(lam2, eps2), s3 = lt_nonneg(lam3, eps2);
+    bool s1 = lt_twice(lam1, eps), s2 = lt_twice(lam2, eps), s3 = lt_twice(lam3, eps);
     if (s1 || s2 || s3) {
         re = rcp(eps);
         if (s1) lam1 = R(0.25) * lam1 * lam1 * re + eps;
@@ -544,11 +558,8 @@ AFVM_HD void roe_gauge(const Phys& P, R pgL, R pgR, R TgL, R TgR, const R* UL, c
     // sound speeds sqrt(g p / rho) = sqrt(g Rg T)
     R c2L = Q.gRg * (TgL + Q.gT), c2R = Q.gRg * (TgR + Q.gT);
     R cL = sqrt_(c2L), cR = sqrt_(c2R);
-    R eps = R(0.5) * fabs(UnL - UnR);
-    eps = eps + R(0.5) * fabs(cL - cR);
-    eps = eps + Q.small;                     // eps >= 0 (roe())
-    R eps2 = R(2) * eps;
-    bool s1 = lt_nonneg(lam1, eps2), s2 = lt_nonneg(lam2, eps2), s3 = lt_nonneg(lam3, eps2);
+    R eps = R(0.5) * (fabs(UnL - UnR) + fabs(cL - cR)) + Q.small;   // eps >= 0 (roe())
+    bool s1 = lt_twice(lam1, eps), s2 = lt_twice(lam2, eps), s3 = lt_twice(lam3, eps);
     if (s1 || s2 || s3) {
         R re = rcp(eps);
         if (s1) lam1 = R(0.25) * lam1 * lam1 * re + eps;
