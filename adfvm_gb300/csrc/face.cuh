@@ -25,10 +25,17 @@ struct FaceBar {
     R gUP[9], gTP[3], gpP[3], gUN[9], gTN[3], gpN[3];
 };
 
+// The start of a sum that the compiler may drop: -0 + x is x for every x (IEEE 754), while
+// +0 + x turns x = -0 into +0, so a sum started at +0 costs one add (in double an FP64 pipe
+// issue) for its first term. The adjoint accumulators start at -0; one that receives no term
+// ends as -0.
+template <typename R>
+AFVM_HD constexpr R acc0() { return R(-0.0); }
+
 template <typename R>
 AFVM_HD void zero_bar(FaceBar<R>& b) {
     R* p = &b.UP[0];
-    for (int k = 0; k < 40; k++) p[k] = R(0);
+    for (int k = 0; k < 40; k++) p[k] = acc0<R>();
 }
 
 // Adjoint of a face's geometry inputs (FaceIn's N, D, lw0, lw1, qw0, qw1, 1/deltas), for the
@@ -46,7 +53,7 @@ constexpr bool kGeo = !std::is_same<G, GeoNone>::value;
 template <typename R>
 AFVM_HD void zero_geo(GeoBar<R>& g) {
     R* p = &g.N[0];
-    for (int k = 0; k < 15; k++) p[k] = R(0);
+    for (int k = 0; k < 15; k++) p[k] = acc0<R>();
 }
 
 
@@ -341,7 +348,7 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R
     L1b += -abv3b;
     R L2b = h * (abv1b + abv2b), L3b = h * (abv1b - abv2b);
     // entropy fix
-    R epsb = R(0), l1b, l2b, l3b;
+    R epsb = acc0<R>(), l1b, l2b, l3b;
     if (s1) { l1b = L1b * h * l1 * re; epsb += L1b * (R(1) - R(0.25) * l1 * l1 * re * re); } else l1b = L1b;
     if (s2) { l2b = L2b * h * l2 * re; epsb += L2b * (R(1) - R(0.25) * l2 * l2 * re * re); } else l2b = L2b;
     if (s3) { l3b = L3b * h * l3 * re; epsb += L3b * (R(1) - R(0.25) * l3 * l3 * re * re); } else l3b = L3b;
@@ -457,11 +464,14 @@ AFVM_HD void laxf_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const 
 }
 
 // RCF.viscousFlux: F[1..3] += -sigma, F[4] += -(q + sigma.UF)
-// (mu = mu(TF), gT and gU the corrected face gradients: the forward's values)
+// (mu = mu(TF), gT and gU the corrected face gradients: the forward's values). gTFb and gUFb
+// receive the adjoints of the cell gradients the face gradient is formed from: gs times those
+// of the face gradient (gs = 1/2 where it is the two sides' average, 1 where it is the ghost's
+// own; rgs = 1/gs), so that each side's share needs no further product.
 template <typename R>
 AFVM_HD void viscous_vjp_t(const Phys& P, R TF, const R* UF, R mu, R dmu, R gTn, const R* tmp2, R tmp3, R ts,
-                           const R* sigma, const R* D, const R* N, R rdel, const R* Fb, R& TLb, R& TRb, R* ULb,
-                           R* URb, R& TFb, R* UFb, R* gTFb, R* gUFb) {
+                           const R* sigma, const R* D, const R* N, R rdel, R gs, R rgs, const R* Fb, R& TLb, R& TRb,
+                           R* ULb, R* URb, R& TFb, R* UFb, R* gTFb, R* gUFb) {
     R kappa = mu * consts<R>(P).kFac;
     // reverse
     R sb[3];
@@ -470,40 +480,38 @@ AFVM_HD void viscous_vjp_t(const Phys& P, R TF, const R* UF, R mu, R dmu, R gTn,
         UFb[i] += -Fb[4] * sigma[i];
     }
     R qFb = -Fb[4];
-    R mub = R(0);
+    R mub = acc0<R>();
     R tmp2b[3];
-    // (tmp2, tmp3: the forward's, divided by ts)
+    // (tmp2, tmp3: the forward's, divided by ts); the gradient adjoints below carry the factor gs
     R c23 = R(2.0 / 3) * tmp3;
+    R mug = mu * gs;
     for (int i = 0; i < 3; i++) {
         mub += sb[i] * (tmp2[i] - c23 * N[i]);
-        tmp2b[i] = sb[i] * mu;
+        tmp2b[i] = sb[i] * mug;
     }
     mub = mub * ts;
-    R tmp3b = (-R(2.0 / 3) * mu) * dot3(sb, N);
+    R tmp3b = (-R(2.0 / 3) * mug) * dot3(sb, N);
     R kappab = qFb * gTn;
     R gTb[3];
-    for (int k = 0; k < 3; k++) gTb[k] = qFb * kappa * N[k];
+    R qk = (qFb * kappa) * gs;
+    for (int k = 0; k < 3; k++) gTb[k] = qk * N[k];
     mub += kappab * consts<R>(P).kFac;
     R gUb[9];
     for (int i = 0; i < 3; i++)
         for (int k = 0; k < 3; k++) gUb[3 * i + k] = tmp2b[i] * N[k] + tmp2b[k] * N[i];
     gUb[0] += tmp3b; gUb[4] += tmp3b; gUb[8] += tmp3b;
+    // snGrad = (phi_N - phi_P) / deltas: the cell values' share, less the factor gs
+    R rdg = rdel * rgs;
     for (int i = 0; i < 3; i++) {
-        R snUb = R(0), gUDb = R(0);
-        for (int k = 0; k < 3; k++) {
-            gUFb[3 * i + k] += gUb[3 * i + k];
-            snUb += gUb[3 * i + k] * D[k];
-        }
-        gUDb = -snUb;
-        for (int k = 0; k < 3; k++) gUFb[3 * i + k] += gUDb * D[k];
-        URb[i] += snUb * rdel;
-        ULb[i] += -snUb * rdel;
+        R snUb = gUb[3 * i] * D[0] + gUb[3 * i + 1] * D[1] + gUb[3 * i + 2] * D[2];
+        for (int k = 0; k < 3; k++) gUFb[3 * i + k] += gUb[3 * i + k] - snUb * D[k];
+        URb[i] += snUb * rdg;
+        ULb[i] += -snUb * rdg;
     }
     R snTb = dot3(gTb, D);
-    R gTDb = -snTb;
-    for (int k = 0; k < 3; k++) gTFb[k] += gTb[k] + gTDb * D[k];
-    TRb += snTb * rdel;
-    TLb += -snTb * rdel;
+    for (int k = 0; k < 3; k++) gTFb[k] += gTb[k] - snTb * D[k];
+    TRb += snTb * rdg;
+    TLb += -snTb * rdg;
     // d mu/dT (viscosity(); 0 for a constant mu)
     TFb += mub * dmu;
 }
@@ -530,8 +538,8 @@ AFVM_HD void viscous_vjp(const Phys& P, R TL, R TR, const R* UL, const R* UR, R 
         tmp2[i] = (gU[3 * i] + gU[i]) * N[0] + (gU[3 * i + 1] + gU[3 + i]) * N[1] + (gU[3 * i + 2] + gU[6 + i]) * N[2];
         sigma[i] = mu * (tmp2[i] - R(2.0 / 3) * tmp3 * N[i]);
     }
-    viscous_vjp_t<R>(P, TF, UF, mu, dmu, dot3(gT, N), tmp2, tmp3, R(1), sigma, D, N, rdel, Fb, TLb, TRb, ULb, URb, TFb, UFb,
-                     gTFb, gUFb);
+    viscous_vjp_t<R>(P, TF, UF, mu, dmu, dot3(gT, N), tmp2, tmp3, R(1), sigma, D, N, rdel, R(1), R(1), Fb, TLb, TRb, ULb,
+                     URb, TFb, UFb, gTFb, gUFb);
 }
 
 // The geometry part of the viscous flux's VJP (deltasUnit D, normals N, 1/deltas): the forward
@@ -619,7 +627,7 @@ AFVM_HD void face_vjp(const Phys& P, int kind, bool inviscid, const FaceIn<R>& i
             for (int k = 0; k < 3; k++) geo->N[k] += Unb * in.UN[k] + Fu[k] * in.pN;
         conservative_vjp<R>(P, in.UN, in.TN, in.pN, rhob, rhoUb, rhoEb, o.UN, o.TN, o.pN);
         if (!inviscid) {
-            R TFb = R(0), UFb[3] = {R(0), R(0), R(0)};
+            R TFb = acc0<R>(), UFb[3] = {acc0<R>(), acc0<R>(), acc0<R>()};
             viscous_vjp<R>(P, in.TP, in.TN, in.UP, in.UN, in.TN, in.UN, in.gTN, in.gUN, in.D, in.N, in.rdelta, Fb,
                            o.TP, o.TN, o.UP, o.UN, TFb, UFb, o.gTN, o.gUN);
             o.TN += TFb;
@@ -648,8 +656,8 @@ AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>&
     for (int k = 0; k < 3; k++) { ULF[k] = t.get(T_ULF + k); URF[k] = t.get(T_URF + k); }
     R rdL = t.get(T_RDL), rdR = t.get(T_RDR);
     R rhoL = pLF * rdL, rhoR = pRF * rdR;      // conservative(): rho = p * rd
-    R ULFb[3] = {R(0), R(0), R(0)}, URFb[3] = {R(0), R(0), R(0)};
-    R TLFb = R(0), TRFb = R(0), pLFb = R(0), pRFb = R(0);
+    R ULFb[3] = {acc0<R>(), acc0<R>(), acc0<R>()}, URFb[3] = {acc0<R>(), acc0<R>(), acc0<R>()};
+    R TLFb = acc0<R>(), TRFb = acc0<R>(), pLFb = acc0<R>(), pRFb = acc0<R>();
     // viscous part
     if (!inviscid) {
         R TF, UF[3];
@@ -661,8 +669,10 @@ AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>&
             for (int k = 0; k < 3; k++) UF[k] = R(0.5) * (ULF[k] + URF[k]);
         }
 
-        R TFb = R(0), UFb[3] = {R(0), R(0), R(0)}, gTFb[3] = {R(0), R(0), R(0)}, gUFb[9];
-        for (int k = 0; k < 9; k++) gUFb[k] = R(0);
+        // gTFb, gUFb: each side's share of the face gradients' adjoints (viscous_vjp_t)
+        R TFb = acc0<R>(), UFb[3] = {acc0<R>(), acc0<R>(), acc0<R>()}, gTFb[3], gUFb[9];
+        for (int k = 0; k < 3; k++) gTFb[k] = acc0<R>();
+        for (int k = 0; k < 9; k++) gUFb[k] = acc0<R>();
         R tmp2[3], sigma[3], tmp3, mu = t.get(T_MU), dmu, ts;
         if constexpr (Src::kFull) {
             // the taped stress terms are the forward's divided by its scale (viscous())
@@ -683,8 +693,8 @@ AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>&
                 sigma[i] = mu * (tmp2[i] - R(2.0 / 3) * tmp3 * in.N[i]);
             }
         }
-        viscous_vjp_t<R>(P, TF, UF, mu, dmu, t.get(T_GTN), tmp2, tmp3, ts, sigma, in.D, in.N, in.rdelta, Fb, o.TP, o.TN, o.UP,
-                         o.UN, TFb, UFb, gTFb, gUFb);
+        viscous_vjp_t<R>(P, TF, UF, mu, dmu, t.get(T_GTN), tmp2, tmp3, ts, sigma, in.D, in.N, in.rdelta,
+                         chr ? R(1) : R(0.5), chr ? R(1) : R(2), Fb, o.TP, o.TN, o.UP, o.UN, TFb, UFb, gTFb, gUFb);
         if constexpr (kGeo<G>) {
             R gTF[3], gUF[9];
             for (int k = 0; k < 3; k++) gTF[k] = chr ? in.gTN[k] : R(0.5) * (in.gTP[k] + in.gTN[k]);
@@ -701,15 +711,16 @@ AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>&
             for (int k = 0; k < 3; k++) {
                 ULFb[k] += R(0.5) * UFb[k];
                 URFb[k] += R(0.5) * UFb[k];
-                o.gTP[k] += R(0.5) * gTFb[k];
-                o.gTN[k] += R(0.5) * gTFb[k];
+                o.gTP[k] += gTFb[k];
+                o.gTN[k] += gTFb[k];
             }
-            for (int k = 0; k < 9; k++) { o.gUP[k] += R(0.5) * gUFb[k]; o.gUN[k] += R(0.5) * gUFb[k]; }
+            for (int k = 0; k < 9; k++) { o.gUP[k] += gUFb[k]; o.gUN[k] += gUFb[k]; }
         }
     }
     // Riemann part
-    R rhoLb = R(0), rhoRb = R(0), rhoULb[3] = {R(0), R(0), R(0)}, rhoURb[3] = {R(0), R(0), R(0)};
-    R rhoELb = R(0), rhoERb = R(0);
+    R rhoLb = acc0<R>(), rhoRb = acc0<R>(), rhoULb[3] = {acc0<R>(), acc0<R>(), acc0<R>()};
+    R rhoURb[3] = {acc0<R>(), acc0<R>(), acc0<R>()};
+    R rhoELb = acc0<R>(), rhoERb = acc0<R>();
     int solver = chr ? P.briemann : P.riemann;
     if (solver == AFVM_RIEMANN_ROE) {
         roe_vjp<R>(P, pLF, pRF, TLF, TRF, ULF, URF, rhoL, rhoR, in.N, Fb, t, pLFb, pRFb, TLFb, TRFb, ULFb, URFb,
