@@ -114,7 +114,12 @@ AFVM_HD void face_flux_gauge(const Phys& P, int kind, bool inviscid, const FaceI
             for (int k = 0; k < 9; k++) gUs[k] = R(0.5) * (in.gUP[k] + in.gUN[k]);
         }
     }
-    if (!inviscid) viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, Us, gTs, gUs, R(1), R(1), in.D, in.N, in.rdelta, F);
+    if (!inviscid) {
+        R Fv[4];
+        viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, Us, gTs, gUs, R(1), R(1), in.D, in.N, in.rdelta, Fv);
+        for (int k = 0; k < 3; k++) F[1 + k] = F[1 + k] - Fv[k];
+        F[4] = F[4] - Fv[3];
+    }
     R aF = sqrt_(Q.Cp * TF * Q.gm1);
     maxaF = fabs(dot3(Us, in.N)) + aF;
 }
@@ -130,6 +135,8 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
         return;
     }
     R TF, Us[3], gTs[3], gUs[9], hs, rhs;
+    // the viscous terms (sigma and q + sigma.U_F), subtracted from the inviscid flux
+    R Fv[4] = {R(0), R(0), R(0), R(0)};
     if (kind == FACE_BOUNDARY) {
         // RCF.boundaryFlux (density.py:307-331) with RCF.getFlux (density.py:184-190)
         R rho, rhoU[3], rhoE;
@@ -142,6 +149,11 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
         for (int k = 0; k < 3; k++) { Us[k] = in.UN[k]; gTs[k] = in.gTN[k]; }
         for (int k = 0; k < 9; k++) gUs[k] = in.gUN[k];
         hs = R(1); rhs = R(1);
+        if (!inviscid) {
+            viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, Us, gTs, gUs, hs, rhs, in.D, in.N, in.rdelta, Fv, tp);
+            for (int k = 0; k < 3; k++) F[1 + k] = F[1 + k] - Fv[k];
+            F[4] = F[4] - Fv[3];
+        }
     } else {
         R ULF[3], TLF, pLF, URF[3], TRF, pRF;
         // the jumps neighbour - owner, shared by the two sides' reconstructions
@@ -168,10 +180,6 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
         for (int k = 0; k < 3; k++) { tp.put(T_ULF + k, ULF[k]); tp.put(T_URF + k, URF[k]); }
         tp.put(T_TLF, TLF); tp.put(T_PLF, pLF); tp.put(T_TRF, TRF); tp.put(T_PRF, pRF);
         tp.put(T_RDL, rdL); tp.put(T_RDR, rdR);
-        if (solver == AFVM_RIEMANN_ROE)
-            roe<R>(P, pLF, pRF, TLF, TRF, ULF, URF, rhoL, rhoR, in.N, F, tp);
-        else
-            laxf<R>(P, pLF, pRF, TLF, TRF, ULF, URF, rhoL, rhoR, rhoUL, rhoUR, rhoEL, rhoER, in.N, F, tp);
         if (kind == FACE_CHARACTERISTIC) {
             TF = in.TN;
             for (int k = 0; k < 3; k++) { Us[k] = in.UN[k]; gTs[k] = in.gTN[k]; }
@@ -184,9 +192,16 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
             for (int k = 0; k < 9; k++) gUs[k] = in.gUP[k] + in.gUN[k];
             hs = R(0.5); rhs = R(2);
         }
+        if (!inviscid)
+            viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, Us, gTs, gUs, hs, rhs, in.D, in.N, in.rdelta, Fv, tp);
+        if (solver == AFVM_RIEMANN_ROE) {
+            roe<R>(P, pLF, pRF, TLF, TRF, ULF, URF, rhoL, rhoR, in.N, Fv, F, tp);
+        } else {
+            laxf<R>(P, pLF, pRF, TLF, TRF, ULF, URF, rhoL, rhoR, rhoUL, rhoUR, rhoEL, rhoER, in.N, F, tp);
+            for (int k = 0; k < 3; k++) F[1 + k] = F[1 + k] - Fv[k];
+            F[4] = F[4] - Fv[3];
+        }
     }
-    if (!inviscid)
-        viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, Us, gTs, gUs, hs, rhs, in.D, in.N, in.rdelta, F, tp);
     R aF = sqrt_(consts<R>(P).Cp * TF * consts<R>(P).gm1);
     maxaF = fabs(hs * dot3(Us, in.N)) + aF;
 }
@@ -464,20 +479,23 @@ AFVM_HD void laxf_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const 
 }
 
 // RCF.viscousFlux: F[1..3] += -sigma, F[4] += -(q + sigma.UF)
-// (mu = mu(TF), gT and gU the corrected face gradients: the forward's values). gTFb and gUFb
-// receive the adjoints of the cell gradients the face gradient is formed from: gs times those
-// of the face gradient (gs = 1/2 where it is the two sides' average, 1 where it is the ghost's
-// own; rgs = 1/gs), so that each side's share needs no further product.
+// (mu = mu(TF), gT and gU the corrected face gradients: the forward's values). The face
+// velocity is passed as UFs with UF = us UFs (us = 1/2: UFs is the two sides' sum; 1: the
+// ghost's own), and UFb receives the adjoint of each side's velocity, us times UF's. Likewise
+// gTFb and gUFb receive the adjoints of the cell gradients the face gradient is formed from:
+// gs times those of the face gradient (gs = 1/2 where it is the two sides' average, 1 where it
+// is the ghost's own; rgs = 1/gs). So each side's share needs no further product.
 template <typename R>
-AFVM_HD void viscous_vjp_t(const Phys& P, R TF, const R* UF, R mu, R dmu, R gTn, const R* tmp2, R tmp3, R ts,
+AFVM_HD void viscous_vjp_t(const Phys& P, const R* UFs, R us, R mu, R dmu, R gTn, const R* tmp2, R tmp3, R ts,
                            const R* sigma, const R* D, const R* N, R rdel, R gs, R rgs, const R* Fb, R& TLb, R& TRb,
                            R* ULb, R* URb, R& TFb, R* UFb, R* gTFb, R* gUFb) {
     R kappa = mu * consts<R>(P).kFac;
     // reverse
     R sb[3];
+    R f4 = Fb[4] * us;
     for (int i = 0; i < 3; i++) {
-        sb[i] = -Fb[1 + i] - Fb[4] * UF[i];
-        UFb[i] += -Fb[4] * sigma[i];
+        sb[i] = -Fb[1 + i] - f4 * UFs[i];
+        UFb[i] += -f4 * sigma[i];
     }
     R qFb = -Fb[4];
     R mub = acc0<R>();
@@ -538,8 +556,8 @@ AFVM_HD void viscous_vjp(const Phys& P, R TL, R TR, const R* UL, const R* UR, R 
         tmp2[i] = (gU[3 * i] + gU[i]) * N[0] + (gU[3 * i + 1] + gU[3 + i]) * N[1] + (gU[3 * i + 2] + gU[6 + i]) * N[2];
         sigma[i] = mu * (tmp2[i] - R(2.0 / 3) * tmp3 * N[i]);
     }
-    viscous_vjp_t<R>(P, TF, UF, mu, dmu, dot3(gT, N), tmp2, tmp3, R(1), sigma, D, N, rdel, R(1), R(1), Fb, TLb, TRb, ULb,
-                     URb, TFb, UFb, gTFb, gUFb);
+    viscous_vjp_t<R>(P, UF, R(1), mu, dmu, dot3(gT, N), tmp2, tmp3, R(1), sigma, D, N, rdel, R(1), R(1), Fb, TLb, TRb,
+                     ULb, URb, TFb, UFb, gTFb, gUFb);
 }
 
 // The geometry part of the viscous flux's VJP (deltasUnit D, normals N, 1/deltas): the forward
@@ -660,13 +678,16 @@ AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>&
     R TLFb = acc0<R>(), TRFb = acc0<R>(), pLFb = acc0<R>(), pRFb = acc0<R>();
     // viscous part
     if (!inviscid) {
-        R TF, UF[3];
+        // TF and the face velocity as us times UFs (the two sides' sum, or the ghost's own)
+        R TF, UFs[3], us;
         if (chr) {
             TF = TRF;                            // the ghost's values (in.TN, in.UN)
-            for (int k = 0; k < 3; k++) UF[k] = URF[k];
+            for (int k = 0; k < 3; k++) UFs[k] = URF[k];
+            us = R(1);
         } else {
             TF = R(0.5) * (TLF + TRF);
-            for (int k = 0; k < 3; k++) UF[k] = R(0.5) * (ULF[k] + URF[k]);
+            for (int k = 0; k < 3; k++) UFs[k] = ULF[k] + URF[k];
+            us = R(0.5);
         }
 
         // gTFb, gUFb: each side's share of the face gradients' adjoints (viscous_vjp_t)
@@ -693,12 +714,14 @@ AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>&
                 sigma[i] = mu * (tmp2[i] - R(2.0 / 3) * tmp3 * in.N[i]);
             }
         }
-        viscous_vjp_t<R>(P, TF, UF, mu, dmu, t.get(T_GTN), tmp2, tmp3, ts, sigma, in.D, in.N, in.rdelta,
+        viscous_vjp_t<R>(P, UFs, us, mu, dmu, t.get(T_GTN), tmp2, tmp3, ts, sigma, in.D, in.N, in.rdelta,
                          chr ? R(1) : R(0.5), chr ? R(1) : R(2), Fb, o.TP, o.TN, o.UP, o.UN, TFb, UFb, gTFb, gUFb);
         if constexpr (kGeo<G>) {
             R gTF[3], gUF[9];
             for (int k = 0; k < 3; k++) gTF[k] = chr ? in.gTN[k] : R(0.5) * (in.gTP[k] + in.gTN[k]);
             for (int k = 0; k < 9; k++) gUF[k] = chr ? in.gUN[k] : R(0.5) * (in.gUP[k] + in.gUN[k]);
+            R UF[3];
+            for (int k = 0; k < 3; k++) UF[k] = us * UFs[k];
             viscous_geo_vjp<R>(P, in.TP, in.TN, in.UP, in.UN, TF, UF, gTF, gUF, in.D, in.N, in.rdelta, Fb, geo);
         }
         if (chr) {
@@ -709,8 +732,8 @@ AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>&
             TLFb += R(0.5) * TFb;
             TRFb += R(0.5) * TFb;
             for (int k = 0; k < 3; k++) {
-                ULFb[k] += R(0.5) * UFb[k];
-                URFb[k] += R(0.5) * UFb[k];
+                ULFb[k] += UFb[k];
+                URFb[k] += UFb[k];
                 o.gTP[k] += gTFb[k];
                 o.gTN[k] += gTFb[k];
             }

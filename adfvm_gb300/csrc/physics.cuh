@@ -378,9 +378,10 @@ AFVM_HD R recon(R phiC, R dCD, const R* g, R lw, const R* qw) {
 // reciprocals; rhoUn/rho is Un (the same number in exact arithmetic). With rho = p / (Rg T)
 // (conservative()), the enthalpy g p / ((g-1) rho) + |U|^2/2 is Cp T + |U|^2/2 and the sound
 // speed sqrt(g p / rho) is sqrt(g Rg T): the same numbers in exact arithmetic, without 1/rho.
+// Fv: the viscous terms (viscous()), subtracted from the momentum and energy fluxes.
 template <typename R, typename Sink = TapeNone>
 AFVM_HD void roe(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R* UR, R rhoL, R rhoR,
-                 const R* N, R* F, Sink&& tp = Sink()) {
+                 const R* N, const R* Fv, R* F, Sink&& tp = Sink()) {
     const R gm1 = consts<R>(P).gm1, Cp = consts<R>(P).Cp;
     R UnL = dot3(UL, N), UnR = dot3(UR, N);
     tp.put(T_UNL, UnL);
@@ -462,12 +463,13 @@ AFVM_HD void roe(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R* UR
     tp.put(T_ABV6, abv6);
     tp.put(T_ABV7, abv7);
     // central flux minus the dissipation, (F_L + F_R)/2 - |A| dq/2, with the common half taken
-    // once: the pressure term's N and the dissipation's abv7 N share one product
+    // once: the pressure term's N and the dissipation's abv7 N share one product. The halving
+    // is exact, so the viscous terms go in with it in one FMA, with the bits of a separate sum.
     F[0] = R(0.5) * ((rhoUnL + rhoUnR) - (lam1 * drho + abv6));
     const R pa = (pL + pR) + abv7;
     for (int k = 0; k < 3; k++)
-        F[1 + k] = R(0.5) * (rhoUnL * UL[k] + rhoUnR * UR[k] + pa * N[k] - lam1 * dU[k] - UF[k] * abv6);
-    F[4] = R(0.5) * (rhoUnL * hL + rhoUnR * hR - lam1 * drhoE - hF * abv6 + UnF * abv7);
+        F[1 + k] = R(0.5) * (rhoUnL * UL[k] + rhoUnR * UR[k] + pa * N[k] - lam1 * dU[k] - UF[k] * abv6) - Fv[k];
+    F[4] = R(0.5) * (rhoUnL * hL + rhoUnR * hR - lam1 * drhoE - hF * abv6 + UnF * abv7) - Fv[3];
 }
 
 // riemann.eulerLaxFriedrichs (adFVM/riemann.py:6-18)
@@ -596,7 +598,8 @@ AFVM_HD void laxf_gauge(const Phys& P, R pgL, R pgR, R TgL, R TgR, const R* UL, 
     F[4] = R(0.5) * (rhoL * j.hLg * UnL + rhoR * j.hRg * UnR) - ha * j.drhoEg;
 }
 
-// RCF.viscousFlux (adFVM/density.py:192-222): adds -sigma to F[1..3] and -(q + sigma.UF) to F[4];
+// RCF.viscousFlux (adFVM/density.py:192-222): the terms the flux subtracts, Fv[0..2] = sigma
+// (from F[1..3]) and Fv[3] = q + sigma.UF (from F[4]);
 // rdel = 1/deltas (a mesh table), the divisor of snGrad (op.py:66-67). The face velocity and
 // gradients arrive as hs times Us, gTs, gUs: hs = 1/2 with the two sides' sums (the reference's
 // averages), hs = 1 with the ghost's values (rhs = 1/hs). The corrected gradients are formed
@@ -604,7 +607,7 @@ AFVM_HD void laxf_gauge(const Phys& P, R pgL, R pgR, R TgL, R TgR, const R* UL, 
 // scales them back); sigma, (grad T).n and the flux are the reference's.
 template <typename R, typename Sink = TapeNone>
 AFVM_HD void viscous(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, const R* Us, const R* gTs,
-                     const R* gUs, R hs, R rhs, const R* D, const R* N, R rdel, R* F, Sink&& tp = Sink()) {
+                     const R* gUs, R hs, R rhs, const R* D, const R* N, R rdel, R* Fv, Sink&& tp = Sink()) {
     R dmu;
     R mu = viscosity<R>(P, TF, &dmu);
     tp.put(T_MU, mu);
@@ -636,10 +639,10 @@ AFVM_HD void viscous(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, 
         tp.put(T_TMP2 + i, tmp2);
         tp.put(T_SIG + i, sigma[i]);
     }
-    F[1] = F[1] + (-sigma[0]);
-    F[2] = F[2] + (-sigma[1]);
-    F[3] = F[3] + (-sigma[2]);
-    F[4] = F[4] + (-(qF + hs * dot3(sigma, Us)));
+    Fv[0] = sigma[0];
+    Fv[1] = sigma[1];
+    Fv[2] = sigma[2];
+    Fv[3] = qF + hs * dot3(sigma, Us);
 }
 
 }  // namespace afvm
