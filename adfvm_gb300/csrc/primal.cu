@@ -292,7 +292,9 @@ __global__ void __launch_bounds__(BLOCK) k_update(MeshDev<R> m, const R* __restr
     double objv = 0.0;     // this cell's term of a cell-sum objective (stage 0, objPartials)
     if (c < m.nIC) {
         const size_t n = m.nIC;
-        R res[5] = {R(0), R(0), R(0), R(0), R(0)};
+        // the sums start at -0, which the compiler drops from the first term's add (-0 + x is x,
+        // while +0 + x is one more add; the values differ at most in the sign of a zero)
+        R res[5] = {R(-0.0), R(-0.0), R(-0.0), R(-0.0), R(-0.0)};
 #pragma unroll
         for (int k = 0; k < 6; k++) {
             int e = m.accf[k * n + c];
