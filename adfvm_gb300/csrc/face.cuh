@@ -514,10 +514,13 @@ AFVM_HD void viscous_vjp_t(const Phys& P, const R* UFs, R us, R mu, R dmu, R gTn
     R qk = (qFb * kappa) * gs;
     for (int k = 0; k < 3; k++) gTb[k] = qk * N[k];
     mub += kappab * consts<R>(P).kFac;
+    // gUb[i][k] = tmp2b_i N_k + tmp2b_k N_i (+ tmp3b on the diagonal) is symmetric: each
+    // off-diagonal pair is formed once
     R gUb[9];
-    for (int i = 0; i < 3; i++)
-        for (int k = 0; k < 3; k++) gUb[3 * i + k] = tmp2b[i] * N[k] + tmp2b[k] * N[i];
-    gUb[0] += tmp3b; gUb[4] += tmp3b; gUb[8] += tmp3b;
+    for (int i = 0; i < 3; i++) gUb[4 * i] = (R(2) * tmp2b[i]) * N[i] + tmp3b;
+    gUb[1] = gUb[3] = tmp2b[0] * N[1] + tmp2b[1] * N[0];
+    gUb[2] = gUb[6] = tmp2b[0] * N[2] + tmp2b[2] * N[0];
+    gUb[5] = gUb[7] = tmp2b[1] * N[2] + tmp2b[2] * N[1];
     // snGrad = (phi_N - phi_P) / deltas: the cell values' share, less the factor gs
     R rdg = rdel * rgs;
     for (int i = 0; i < 3; i++) {
