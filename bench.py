@@ -86,17 +86,17 @@ STEP_BYTES = {('primal', 8): 2904, ('primal', 4): 1524, ('adjoint', 8): 6288, ('
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch from an ncu capture of
 # the 64^3 box (798,720 faces, 262,144 cells; profiles/), scaled to a launch of the benchmarked
-# mesh by its number of faces (the kernel's traffic grows in proportion to the faces). The taped
-# FP64 kernels (the benchmarked step: 61-value face tape) are from the current build's capture;
-# the untaped and FP32 ones from earlier captures of the same kernels.
-MEASURED_TRAFFIC = {('k_flux', 8): (172.68e6, 798720), ('k_flux', 4): (81.56e6, 798720),
-                    ('k_adj_flux', 8): (407.63e6, 798720), ('k_adj_flux', 4): (170.37e6, 798720),
+# mesh by its number of faces (the kernel's traffic grows in proportion to the faces). The FP64
+# kernels (taped: the benchmarked step with its 61-value face tape; untaped: --tape 0) are from
+# captures of the current build, the FP32 ones from earlier captures of the same kernels.
+MEASURED_TRAFFIC = {('k_flux', 8): (174.3e6, 798720), ('k_flux', 4): (81.56e6, 798720),
+                    ('k_adj_flux', 8): (428.5e6, 798720), ('k_adj_flux', 4): (170.37e6, 798720),
                     ('k_flux+tape', 8): (522.3e6, 798720), ('k_adj_flux+tape', 8): (726.1e6, 798720)}
 # FP64 thread instructions per face (DADD, DMUL, DFMA) of a launch in the same captures
-# (smsp__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on; the taped kernels and the forward
-# flux from the current build, the untaped VJP from an earlier one); the forward flux issues the
-# same FP64 instructions with or without the tape writes
-MEASURED_FP64_INST = {'k_flux': (52.0, 94.4, 162.4), 'k_adj_flux': (108.0, 307.9, 456.9),
+# (smsp__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on), current build; the untaped
+# forward flux issues a few FP64 instructions fewer than the taped one (the tape's values it
+# need not form)
+MEASURED_FP64_INST = {'k_flux': (50.0, 88.4, 163.4), 'k_adj_flux': (81.0, 192.6, 325.4),
                       'k_flux+tape': (52.0, 94.4, 162.4), 'k_adj_flux+tape': (37.0, 113.9, 187.4)}
 
 
