@@ -98,6 +98,9 @@ MEASURED_TRAFFIC = {('k_flux', 8): (174.3e6, 798720), ('k_flux', 4): (81.56e6, 7
 # need not form)
 MEASURED_FP64_INST = {'k_flux': (50.0, 88.4, 163.4), 'k_adj_flux': (81.0, 192.6, 325.4),
                       'k_flux+tape': (52.0, 94.4, 162.4), 'k_adj_flux+tape': (37.0, 113.9, 187.4)}
+# every warp instruction the FP64 pipe issued, per face (smsp__inst_executed_pipe_fp64 x 32 / faces,
+# the same captures): the arithmetic above plus the other instructions that pipe executes
+MEASURED_FP64_PIPE_INST = {'k_flux': 307.0, 'k_adj_flux': 624.8, 'k_flux+tape': 314.0, 'k_adj_flux+tape': 361.8}
 
 
 def measured_traffic(kernel, es, nF):
@@ -738,8 +741,10 @@ def main():
             'bound': 'fp64', 'kernel': top, 'achieved': round(ach, 3), 'peak': fpk, 'unit': 'TFLOP/s',
             'frac': round(ach / fpk, 4), 'flops_per_face': round(da + dm + 2 * df, 1),
             'issue_frac': round((da + dm + df) * nF / avg_s / (fpk * 1e12 / 2), 4),
+            'pipe_issue_frac': round(MEASURED_FP64_PIPE_INST[top] * nF / avg_s / (fpk * 1e12 / 2), 4),
             'peak_source': 'afvm_fma_peak (a DFMA loop on this GPU, FMA = 2 flops)',
-            'note': 'issue_frac counts DADD/DMUL/DFMA as one FP64 pipe issue each'}
+            'note': 'issue_frac counts DADD/DMUL/DFMA as one FP64 pipe issue each; pipe_issue_frac '
+                    'every instruction the FP64 pipe issued (ncu), against the same issue rate'}
     if rank == 0 and not args.no_cpu_baseline:
         cb = cpu_baseline(args, os.cpu_count() or 1)
         cb.pop('config', None)
