@@ -337,7 +337,6 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R
     // abv7 = abv3*abv5 - abv2*abv4/aF
     R b7r = abv7b * raF;
     R abv3b = abv7b * abv5, abv5b = abv7b * abv3, abv2b = -b7r * abv4, abv4b = -b7r * abv2;
-    R aFb = (b7r * raF) * (abv2 * abv4);
     // abv6 = abv3*abv4/a2F - abv2*abv5/aF
     R b6q = abv6b * ra2F, b6r = abv6b * raF;
     abv3b += b6q * abv4;
@@ -345,7 +344,8 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R
     R a2Fb = -(b6q * ra2F) * (abv3 * abv4);
     abv2b += -b6r * abv5;
     abv5b += -b6r * abv2;
-    aFb += (b6r * raF) * (abv2 * abv5);
+    // both terms' d/daF (abv2 b7r abv4 + abv2 b6r abv5)/aF are -abv2 abv2b/aF
+    R aFb = -(raF * abv2) * abv2b;
     // abv5 = UnF*drho - dU.N
     UnFb += abv5b * drho;
     drhob += abv5b * UnF;
@@ -370,8 +370,8 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R
     R eab = mul_sgn(ea, h * epsb);
     R ebb = mul_sgn(eb_, h * epsb);
     // c = sqrt(g Rg T): dc/dT = g Rg / (2 c)
-    TLb += ebb * (h * gRg) * rcL;
-    TRb += -ebb * (h * gRg) * rcR;
+    TLb += ebb * consts<R>(P).hgRg * rcL;
+    TRb += -ebb * consts<R>(P).hgRg * rcR;
     // lam = |UnF|, |UnF + aF|, |UnF - aF|
     R b2 = mul_sgn(UnF + aF, l2b), b3 = mul_sgn(UnF - aF, l3b);
     UnFb += mul_sgn(UnF, l1b) + b2 + b3;
@@ -471,8 +471,8 @@ AFVM_HD void laxf_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const 
     R Ab = (A >= B) ? aFb : R(0), Bb = (A >= B) ? R(0) : aFb;
     UnLb += mul_sgn(UnL, Ab);
     UnRb += mul_sgn(UnR, Bb);
-    TLb += Ab * (h * gRg) * rcL;
-    TRb += Bb * (h * gRg) * rcR;
+    TLb += Ab * consts<R>(P).hgRg * rcL;
+    TRb += Bb * consts<R>(P).hgRg * rcR;
     for (int k = 0; k < 3; k++) { ULb[k] += UnLb * N[k]; URb[k] += UnRb * N[k]; }
     if constexpr (kGeo<G>)
         for (int k = 0; k < 3; k++) geo->N[k] += UnLb * UL[k] + UnRb * UR[k] + h * Fu[k] * (pL + pR);
@@ -751,9 +751,9 @@ AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>&
     if (solver == AFVM_RIEMANN_ROE) {
         roe_vjp<R>(P, pLF, pRF, TLF, TRF, ULF, URF, rhoL, rhoR, in.N, Fb, t, pLFb, pRFb, TLFb, TRFb, ULFb, URFb,
                    rhoLb, rhoRb, geo);
-        // conservative(): the Roe flux uses only rho = p rd of each side (rd = 1/(Cv T (g-1)),
-        // drho/dp = rd, drho/dT = -rho/T = -rho rd (g-1) Cv)
-        const R k = consts<R>(P).gm1 * consts<R>(P).Cv;
+        // conservative(): the Roe flux uses only rho = p rd of each side (rd = 1/(Rg T),
+        // drho/dp = rd, drho/dT = -rho/T = -rho rd Rg)
+        const R k = consts<R>(P).Rg;
         pLFb += rhoLb * rdL;
         TLFb += -rhoLb * (rhoL * (rdL * k));
         pRFb += rhoRb * rdR;

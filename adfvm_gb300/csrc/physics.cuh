@@ -84,11 +84,12 @@ struct TapeLocal {
 
 // the gas constants in the working precision, so that the templated physics issues no FP64
 // conversion or division in FP32 (ggm1 = gamma/(gamma-1), Rg = Cv (gamma-1) the gas constant,
-// gRg = gamma Rg, rgm1 = 1/(gamma-1)); gP, gT, gH, gK: the gauge state of FP32 records (below)
+// gRg = gamma Rg, rgm1 = 1/(gamma-1); hgRg = gRg/2, muTs15 = 3 Ts/2: products that would
+// otherwise cost an instruction a face); gP, gT, gH, gK: the gauge state of FP32 records (below)
 template <typename R>
 struct PhysR {
     R gamma, gm1, ggm1, Cp, Cv, rCv, kFac, mu0, muAs, muTs, small;
-    R Rg, gRg, rgm1;
+    R Rg, gRg, rgm1, hgRg, muTs15;
     R gP, gT, gH, gK;
 };
 
@@ -133,6 +134,7 @@ inline void fill_consts(const Phys& P, PhysR<R>& q) {
     q.rCv = R(P.rCv); q.kFac = R(P.kFac); q.mu0 = R(P.mu0); q.muAs = R(P.muAs); q.muTs = R(P.muTs);
     q.small = R(P.small);
     q.Rg = R(P.Cv * P.gm1); q.gRg = R(P.gamma * P.Cv * P.gm1); q.rgm1 = R(1.0 / P.gm1);
+    q.hgRg = R(0.5 * P.gamma * P.Cv * P.gm1); q.muTs15 = R(1.5 * P.muTs);
     q.gP = R(P.gaugeP); q.gT = R(P.gaugeT); q.gH = R(P.gaugeH); q.gK = R(P.gaugeH - P.Cp * P.gaugeT);
 }
 
@@ -347,7 +349,7 @@ AFVM_HD R viscosity(const Phys& P, R T, R* dmu = nullptr) {
         R a = T + Ts;
         R y = rsqrt_(T * (a * a));
         R mu = (consts<R>(P).muAs * (T * T)) * y;
-        if (dmu) *dmu = (mu * (R(0.5) * T + R(1.5) * Ts)) * (a * (y * y));
+        if (dmu) *dmu = (mu * (R(0.5) * T + consts<R>(P).muTs15)) * (a * (y * y));
         return mu;
     }
     if (dmu) *dmu = R(0);
