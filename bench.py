@@ -90,17 +90,17 @@ STEP_BYTES = {('primal', 8): 2904, ('primal', 4): 1524, ('adjoint', 8): 6288, ('
 # kernels (taped: the benchmarked step with its 61-value face tape; untaped: --tape 0) are from
 # captures of the current build, the FP32 ones from earlier captures of the same kernels.
 MEASURED_TRAFFIC = {('k_flux', 8): (174.3e6, 798720), ('k_flux', 4): (81.56e6, 798720),
-                    ('k_adj_flux', 8): (428.5e6, 798720), ('k_adj_flux', 4): (170.37e6, 798720),
-                    ('k_flux+tape', 8): (522.3e6, 798720), ('k_adj_flux+tape', 8): (726.1e6, 798720)}
+                    ('k_adj_flux', 8): (429.4e6, 798720), ('k_adj_flux', 4): (170.37e6, 798720),
+                    ('k_flux+tape', 8): (522.3e6, 798720), ('k_adj_flux+tape', 8): (728.5e6, 798720)}
 # FP64 thread instructions per face (DADD, DMUL, DFMA) of a launch in the same captures
 # (smsp__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on), current build; the untaped
 # forward flux issues a few FP64 instructions fewer than the taped one (the tape's values it
 # need not form)
-MEASURED_FP64_INST = {'k_flux': (50.0, 88.4, 163.4), 'k_adj_flux': (81.0, 192.6, 325.4),
-                      'k_flux+tape': (52.0, 93.4, 162.4), 'k_adj_flux+tape': (39.0, 105.5, 184.4)}
+MEASURED_FP64_INST = {'k_flux': (50.0, 88.4, 163.4), 'k_adj_flux': (82.0, 187.6, 323.4),
+                      'k_flux+tape': (52.0, 93.4, 162.4), 'k_adj_flux+tape': (39.0, 105.9, 184.4)}
 # every warp instruction the FP64 pipe issued, per face (smsp__inst_executed_pipe_fp64 x 32 / faces,
 # the same captures): the arithmetic above plus the other instructions that pipe executes
-MEASURED_FP64_PIPE_INST = {'k_flux': 307.0, 'k_adj_flux': 624.8, 'k_flux+tape': 313.0, 'k_adj_flux+tape': 352.8}
+MEASURED_FP64_PIPE_INST = {'k_flux': 307.0, 'k_adj_flux': 618.8, 'k_flux+tape': 313.0, 'k_adj_flux+tape': 352.8}
 
 
 def measured_traffic(kernel, es, nF):
