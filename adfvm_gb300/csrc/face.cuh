@@ -362,11 +362,14 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R
     R abv1b = abv3b;
     L1b += -abv3b;
     R L2b = h * (abv1b + abv2b), L3b = h * (abv1b - abv2b);
-    // entropy fix
+    // entropy fix L = l^2/(4 eps) + eps: dL/dl = t and dL/deps = 1 - t^2 with t = l/(2 eps). A
+    // warp runs a branch when any of its faces takes it (most warps do for the first
+    // eigenvalue), so the branches are kept short.
     R epsb = acc0<R>(), l1b, l2b, l3b;
-    if (s1) { l1b = L1b * h * l1 * re; epsb += L1b * (R(1) - R(0.25) * l1 * l1 * re * re); } else l1b = L1b;
-    if (s2) { l2b = L2b * h * l2 * re; epsb += L2b * (R(1) - R(0.25) * l2 * l2 * re * re); } else l2b = L2b;
-    if (s3) { l3b = L3b * h * l3 * re; epsb += L3b * (R(1) - R(0.25) * l3 * l3 * re * re); } else l3b = L3b;
+    const R hre = h * re;
+    if (s1) { R t = hre * l1; l1b = L1b * t; epsb += L1b * (R(1) - t * t); } else l1b = L1b;
+    if (s2) { R t = hre * l2; l2b = L2b * t; epsb += L2b * (R(1) - t * t); } else l2b = L2b;
+    if (s3) { R t = hre * l3; l3b = L3b * t; epsb += L3b * (R(1) - t * t); } else l3b = L3b;
     R eab = mul_sgn(ea, h * epsb);
     R ebb = mul_sgn(eb_, h * epsb);
     // c = sqrt(g Rg T): dc/dT = g Rg / (2 c)
