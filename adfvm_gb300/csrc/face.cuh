@@ -368,8 +368,14 @@ AFVM_HD void roe_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R
     R epsb = acc0<R>(), l1b, l2b, l3b;
     const R hre = h * re;
     if (s1) { R t = hre * l1; l1b = L1b * t; epsb += L1b * (R(1) - t * t); } else l1b = L1b;
-    if (s2) { R t = hre * l2; l2b = L2b * t; epsb += L2b * (R(1) - t * t); } else l2b = L2b;
-    if (s3) { R t = hre * l3; l3b = L3b * t; epsb += L3b * (R(1) - t * t); } else l3b = L3b;
+    l2b = L2b;
+    l3b = L3b;
+    // the acoustic eigenvalues |U_F.n +- a_F| fall under 2 eps only near sonic faces: one branch
+    // that warps skip, instead of two short ones that a warp would run with its lanes masked
+    if (__builtin_expect(s2 || s3, 0)) {
+        if (s2) { R t = hre * l2; l2b = L2b * t; epsb += L2b * (R(1) - t * t); }
+        if (s3) { R t = hre * l3; l3b = L3b * t; epsb += L3b * (R(1) - t * t); }
+    }
     R eab = mul_sgn(ea, h * epsb);
     R ebb = mul_sgn(eb_, h * epsb);
     // c = sqrt(g Rg T): dc/dT = g Rg / (2 c)

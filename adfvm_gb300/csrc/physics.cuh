@@ -443,8 +443,11 @@ AFVM_HD void roe(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const R* UR
     if (s1 || s2 || s3) {
         re = rcp(eps);
         if (s1) lam1 = R(0.25) * lam1 * lam1 * re + eps;
-        if (s2) lam2 = R(0.25) * lam2 * lam2 * re + eps;
-        if (s3) lam3 = R(0.25) * lam3 * lam3 * re + eps;
+        // (the acoustic eigenvalues take the fix only near sonic faces: a branch warps skip)
+        if (__builtin_expect(s2 || s3, 0)) {
+            if (s2) lam2 = R(0.25) * lam2 * lam2 * re + eps;
+            if (s3) lam3 = R(0.25) * lam3 * lam3 * re + eps;
+        }
     }
     tp.put(T_RE, re);
     tp.put(T_EPS, eps);
