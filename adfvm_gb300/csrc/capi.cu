@@ -122,6 +122,19 @@ int upload_mesh(Ctx* c, const HostTables& h, MeshDev<R>& m) {
         for (size_t i = 0; i < r.size(); i++) r[i] = 1.0 / h.dlt[i];
         if ((st = upload(c, &m.rdlt, cast<R>(r)))) return st;
     }
+    {
+        // N - (N.D) D and N.D in double (face_derived() forms the same numbers)
+        const size_t nF = h.dlt.size();
+        std::vector<double> t(4 * nF);
+        for (size_t f = 0; f < nF; f++) {
+            double N[3] = {h.nrm[f], h.nrm[nF + f], h.nrm[2 * nF + f]};
+            double D[3] = {h.du[f], h.du[nF + f], h.du[2 * nF + f]};
+            double nd = N[0] * D[0] + N[1] * D[1] + N[2] * D[2];
+            for (int k = 0; k < 3; k++) t[k * nF + f] = N[k] - nd * D[k];
+            t[3 * nF + f] = nd;
+        }
+        if ((st = upload(c, &m.ntd, cast<R>(t)))) return st;
+    }
     if ((st = upload(c, &m.du, cast<R>(h.du)))) return st;
     if ((st = upload(c, &m.wts, cast<R>(h.wts)))) return st;
     if ((st = upload(c, &m.lw, cast<R>(h.lw)))) return st;

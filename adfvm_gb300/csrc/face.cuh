@@ -17,7 +17,17 @@ struct FaceIn {
     R UP[3], TP, pP, UN[3], TN, pN;                    // owner cell and neighbour (or ghost) primitives
     R gUP[9], gTP[3], gpP[3], gUN[9], gTN[3], gpN[3];  // gradients ([component][direction])
     R N[3], D[3], lw0, lw1, qw0[3], qw1[3], rdelta;    // normals, deltasUnit, weights, 1/deltas
+    R Nt[3], ND;                                       // derived: N - (N.D) D and N.D (face_derived)
 };
+
+// the derived geometry of a face from its normal and deltasUnit, formed in double (the device
+// reads the same values from mesh tables built this way)
+template <typename R>
+AFVM_HD void face_derived(FaceIn<R>& in) {
+    double nd = (double)in.N[0] * in.D[0] + (double)in.N[1] * in.D[1] + (double)in.N[2] * in.D[2];
+    in.ND = R(nd);
+    for (int k = 0; k < 3; k++) in.Nt[k] = R((double)in.N[k] - nd * (double)in.D[k]);
+}
 
 template <typename R>
 struct FaceBar {
@@ -116,7 +126,8 @@ AFVM_HD void face_flux_gauge(const Phys& P, int kind, bool inviscid, const FaceI
     }
     if (!inviscid) {
         R Fv[4];
-        viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, Us, gTs, gUs, R(1), R(1), in.D, in.N, in.rdelta, Fv);
+        viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, Us, gTs, gUs, R(1), R(1), in.D, in.N, in.Nt, in.ND, in.rdelta,
+                   Fv);
         for (int k = 0; k < 3; k++) F[1 + k] = F[1 + k] - Fv[k];
         F[4] = F[4] - Fv[3];
     }
@@ -150,7 +161,8 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
         for (int k = 0; k < 9; k++) gUs[k] = in.gUN[k];
         hs = R(1); rhs = R(1);
         if (!inviscid) {
-            viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, Us, gTs, gUs, hs, rhs, in.D, in.N, in.rdelta, Fv, tp);
+            viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, Us, gTs, gUs, hs, rhs, in.D, in.N, in.Nt, in.ND, in.rdelta,
+                       Fv, tp);
             for (int k = 0; k < 3; k++) F[1 + k] = F[1 + k] - Fv[k];
             F[4] = F[4] - Fv[3];
         }
@@ -193,7 +205,8 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
             hs = R(0.5); rhs = R(2);
         }
         if (!inviscid)
-            viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, Us, gTs, gUs, hs, rhs, in.D, in.N, in.rdelta, Fv, tp);
+            viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, Us, gTs, gUs, hs, rhs, in.D, in.N, in.Nt, in.ND, in.rdelta,
+                       Fv, tp);
         if (solver == AFVM_RIEMANN_ROE) {
             roe<R>(P, pLF, pRF, TLF, TRF, ULF, URF, rhoL, rhoR, in.N, Fv, F, tp);
         } else {
@@ -496,8 +509,8 @@ AFVM_HD void laxf_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const 
 // is the ghost's own; rgs = 1/gs). So each side's share needs no further product.
 template <typename R>
 AFVM_HD void viscous_vjp_t(const Phys& P, const R* UFs, R us, R mu, R dmu, R gTn, const R* tmp2, R tmp3, R ts,
-                           const R* sigma, const R* D, const R* N, R rdel, R gs, R rgs, const R* Fb, R& TLb, R& TRb,
-                           R* ULb, R* URb, R& TFb, R* UFb, R* gTFb, R* gUFb) {
+                           const R* sigma, const R* D, const R* N, const R* Nt, R ND, R rdel, R gs, R rgs,
+                           const R* Fb, R& TLb, R& TRb, R* ULb, R* URb, R& TFb, R* UFb, R* gTFb, R* gUFb) {
     R kappa = mu * consts<R>(P).kFac;
     // reverse
     R sb[3];
@@ -519,9 +532,7 @@ AFVM_HD void viscous_vjp_t(const Phys& P, const R* UFs, R us, R mu, R dmu, R gTn
     mub = mub * ts;
     R tmp3b = (-R(2.0 / 3) * mug) * dot3(sb, N);
     R kappab = qFb * gTn;
-    R gTb[3];
     R qk = (qFb * kappa) * gs;
-    for (int k = 0; k < 3; k++) gTb[k] = qk * N[k];
     mub += kappab * consts<R>(P).kFac;
     // gUb[i][k] = tmp2b_i N_k + tmp2b_k N_i (+ tmp3b on the diagonal) is symmetric: each
     // off-diagonal pair is formed once
@@ -538,8 +549,10 @@ AFVM_HD void viscous_vjp_t(const Phys& P, const R* UFs, R us, R mu, R dmu, R gTn
         URb[i] += snUb * rdg;
         ULb[i] += -snUb * rdg;
     }
-    R snTb = dot3(gTb, D);
-    for (int k = 0; k < 3; k++) gTFb[k] += gTb[k] - snTb * D[k];
+    // the temperature gradient enters through its corrected normal component gTs.Nt + snGrad ND
+    // (viscous())
+    for (int k = 0; k < 3; k++) gTFb[k] += qk * Nt[k];
+    R snTb = qk * ND;
     TRb += snTb * rdg;
     TLb += -snTb * rdg;
     // d mu/dT (viscosity(); 0 for a constant mu)
@@ -568,8 +581,10 @@ AFVM_HD void viscous_vjp(const Phys& P, R TL, R TR, const R* UL, const R* UR, R 
         tmp2[i] = (gU[3 * i] + gU[i]) * N[0] + (gU[3 * i + 1] + gU[3 + i]) * N[1] + (gU[3 * i + 2] + gU[6 + i]) * N[2];
         sigma[i] = mu * (tmp2[i] - R(2.0 / 3) * tmp3 * N[i]);
     }
-    viscous_vjp_t<R>(P, UF, R(1), mu, dmu, dot3(gT, N), tmp2, tmp3, R(1), sigma, D, N, rdel, R(1), R(1), Fb, TLb, TRb,
-                     ULb, URb, TFb, UFb, gTFb, gUFb);
+    R ND = dot3(N, D), Nt[3];
+    for (int k = 0; k < 3; k++) Nt[k] = N[k] - ND * D[k];
+    viscous_vjp_t<R>(P, UF, R(1), mu, dmu, dot3(gT, N), tmp2, tmp3, R(1), sigma, D, N, Nt, ND, rdel, R(1), R(1), Fb,
+                     TLb, TRb, ULb, URb, TFb, UFb, gTFb, gUFb);
 }
 
 // The geometry part of the viscous flux's VJP (deltasUnit D, normals N, 1/deltas): the forward
@@ -726,8 +741,9 @@ AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>&
                 sigma[i] = mu * (tmp2[i] - R(2.0 / 3) * tmp3 * in.N[i]);
             }
         }
-        viscous_vjp_t<R>(P, UFs, us, mu, dmu, t.get(T_GTN), tmp2, tmp3, ts, sigma, in.D, in.N, in.rdelta,
-                         chr ? R(1) : R(0.5), chr ? R(1) : R(2), Fb, o.TP, o.TN, o.UP, o.UN, TFb, UFb, gTFb, gUFb);
+        viscous_vjp_t<R>(P, UFs, us, mu, dmu, t.get(T_GTN), tmp2, tmp3, ts, sigma, in.D, in.N, in.Nt, in.ND,
+                         in.rdelta, chr ? R(1) : R(0.5), chr ? R(1) : R(2), Fb, o.TP, o.TN, o.UP, o.UN, TFb, UFb, gTFb,
+                         gUFb);
         if constexpr (kGeo<G>) {
             R gTF[3], gUF[9];
             for (int k = 0; k < 3; k++) gTF[k] = chr ? in.gTN[k] : R(0.5) * (in.gTP[k] + in.gTN[k]);

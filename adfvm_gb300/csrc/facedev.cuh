@@ -50,6 +50,8 @@ __device__ __forceinline__ void load_face(const MeshDev<R>& m, const R* __restri
     in.lw0 = m.lw[f];
     in.lw1 = m.lw[nF + f];
     in.rdelta = m.rdlt[f];
+    for (int k = 0; k < 3; k++) in.Nt[k] = m.ntd[k * nF + f];
+    in.ND = m.ntd[3 * nF + f];
 }
 
 // a face's column of a device tape (value k of face f at tape[k nF + f]; p = tape + f)
@@ -80,6 +82,8 @@ __device__ __forceinline__ void load_face_geometry(const MeshDev<R>& m, int f, F
     in.lw0 = m.lw[f];
     in.lw1 = m.lw[nF + f];
     in.rdelta = m.rdlt[f];
+    for (int k = 0; k < 3; k++) in.Nt[k] = m.ntd[k * nF + f];
+    in.ND = m.ntd[3 * nF + f];
 }
 
 }  // namespace afvm

@@ -609,10 +609,12 @@ AFVM_HD void laxf_gauge(const Phys& P, R pgL, R pgR, R TgL, R TgR, const R* UL, 
 // gradients arrive as hs times Us, gTs, gUs: hs = 1/2 with the two sides' sums (the reference's
 // averages), hs = 1 with the ghost's values (rhs = 1/hs). The corrected gradients are formed
 // divided by hs, and so are the (grad U + grad U^T).n and tr grad U the tape keeps (the VJP
-// scales them back); sigma, (grad T).n and the flux are the reference's.
+// scales them back); sigma, (grad T).n and the flux are the reference's. Nt = N - (N.D) D and
+// ND = N.D: mesh-only factors of the corrected gradient's normal component.
 template <typename R, typename Sink = TapeNone>
 AFVM_HD void viscous(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, const R* Us, const R* gTs,
-                     const R* gUs, R hs, R rhs, const R* D, const R* N, R rdel, R* Fv, Sink&& tp = Sink()) {
+                     const R* gUs, R hs, R rhs, const R* D, const R* N, const R* Nt, R ND, R rdel, R* Fv,
+                     Sink&& tp = Sink()) {
     R dmu;
     R mu = viscosity<R>(P, TF, &dmu);
     tp.put(T_MU, mu);
@@ -621,17 +623,16 @@ AFVM_HD void viscous(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, 
     // the face gradient with its normal component replaced by snGrad: g + (snGrad - g.D) D,
     // here divided by hs
     R rdh = rdel * rhs;
-    R gTD = dot3(gTs, D);
-    R cT = (TR - TL) * rdh - gTD;
-    R gT[3];
-    for (int k = 0; k < 3; k++) gT[k] = gTs[k] + cT * D[k];
     R gU[9];
     for (int i = 0; i < 3; i++) {
         R gUD = gUs[3 * i] * D[0] + gUs[3 * i + 1] * D[1] + gUs[3 * i + 2] * D[2];
         R cU = (UR[i] - UL[i]) * rdh - gUD;
         for (int k = 0; k < 3; k++) gU[3 * i + k] = gUs[3 * i + k] + cU * D[k];
     }
-    R gTn = hs * dot3(gT, N);
+    // of the corrected temperature gradient only its normal component enters: (gTs + cT D).N with
+    // cT = (TR - TL) rdh - gTs.D is gTs.Nt + (TR - TL) rdh ND (Nt = N - (N.D) D, ND = N.D:
+    // mesh-only tables)
+    R gTn = hs * (dot3(gTs, Nt) + ((TR - TL) * rdh) * ND);
     tp.put(T_GTN, gTn);
     R qF = kappa * gTn;
     R tmp3 = gU[0] + gU[4] + gU[8];

@@ -53,9 +53,9 @@ def algorithmic_bytes(kernel, nIC, nIF, nF, nG, es, taped=False):
     REC, FREC, TAPE = 20, 6, 61
     if kernel == 'k_flux':
         # per face: own+nbr (8), normals 3, deltas 1, deltasUnit 3, linearWeights 2,
-        # quadraticWeights 6 -> 15 values, flux record write 6 (and the 61-value face tape when
-        # taped); cell records read once
-        return nF * (8 + 15 * es + FREC * es + (TAPE * es if taped else 0)) + (nIC + nG) * REC * es
+        # quadraticWeights 6, N - (N.D) D and N.D 4 -> 19 values, flux record write 6 (and the
+        # 61-value face tape when taped); cell records read once
+        return nF * (8 + 19 * es + FREC * es + (TAPE * es if taped else 0)) + (nIC + nG) * REC * es
     if kernel == 'k_grad':
         # per cell: 6 slots x (nbr 4 + w' + S*N' (3)) + 1/V, primitives of every cell once,
         # gradient write 15
@@ -67,14 +67,14 @@ def algorithmic_bytes(kernel, nIC, nIF, nF, nG, es, taped=False):
     if kernel == 'k_prim':
         return nIC * 10 * es + nG * (8 + 5 * es + 5 * es)
     if kernel == 'k_adj_flux' and taped:
-        # per face: own+nbr (8), A/V weights 2, geometry 15, the 61-value face tape, 40-value
+        # per face: own+nbr (8), A/V weights 2, geometry 19, the 61-value face tape, 40-value
         # adjoint record write; the 5 adjoint seeds of every cell once; the two cell records of
         # each boundary face (boundary faces are not taped)
-        return nF * (8 + (17 + TAPE + 40) * es) + nIC * 5 * es + (nF - nIF) * 2 * REC * es
+        return nF * (8 + (21 + TAPE + 40) * es) + nIC * 5 * es + (nF - nIF) * 2 * REC * es
     if kernel == 'k_adj_flux':
-        # per face: own+nbr (8), A/V weights 2, geometry 15, 40-value adjoint record write;
+        # per face: own+nbr (8), A/V weights 2, geometry 19, 40-value adjoint record write;
         # cell records and the 5 adjoint seeds of every cell read once
-        return nF * (8 + 17 * es + 40 * es) + (nIC + nG) * REC * es + nIC * 5 * es
+        return nF * (8 + 21 * es + 40 * es) + (nIC + nG) * REC * es + nIC * 5 * es
     return 0
 
 
@@ -91,17 +91,17 @@ STEP_BYTES = {('primal', 8): 2904, ('primal', 4): 1524, ('adjoint', 8): 6288, ('
 # captures of the current build, the FP32 ones from earlier captures of the same kernels.
 MEASURED_TRAFFIC = {('k_flux', 8): (173.8e6, 798720), ('k_flux', 4): (81.56e6, 798720),
                     ('k_adj_flux', 8): (417.2e6, 798720), ('k_adj_flux', 4): (170.37e6, 798720),
-                    ('k_flux+tape', 8): (522.3e6, 798720), ('k_adj_flux+tape', 8): (733.4e6, 798720)}
+                    ('k_flux+tape', 8): (522.3e6, 798720), ('k_adj_flux+tape', 8): (763.8e6, 798720)}
 # FP64 thread instructions per face (DADD, DMUL, DFMA) of a launch in the same captures
 # (smsp__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on), current build; the untaped
 # forward flux issues a few FP64 instructions fewer than the taped one (the tape's values it
 # need not form)
 MEASURED_FP64_INST = {'k_flux': (50.0, 86.1, 162.2), 'k_adj_flux': (82.0, 184.5, 322.4),
-                      'k_flux+tape': (52.0, 91.1, 161.2), 'k_adj_flux+tape': (40.0, 106.7, 182.4)}
+                      'k_flux+tape': (52.0, 91.1, 161.2), 'k_adj_flux+tape': (40.0, 106.5, 177.4)}
 # every warp instruction the FP64 pipe issued, per face (smsp__inst_executed_pipe_fp64 x 32 / faces,
 # the same captures): the arithmetic above plus the issues of warps whose lanes were partly masked
 # (branches that only some of a warp's faces take)
-MEASURED_FP64_PIPE_INST = {'k_flux': 301.0, 'k_adj_flux': 593.8, 'k_flux+tape': 307.0, 'k_adj_flux+tape': 334.8}
+MEASURED_FP64_PIPE_INST = {'k_flux': 301.0, 'k_adj_flux': 593.8, 'k_flux+tape': 307.0, 'k_adj_flux+tape': 329.8}
 
 
 def measured_traffic(kernel, es, nF):

@@ -64,6 +64,7 @@ inline void face_in(const oracle_mesh* M, const double* rec, int f, FaceIn<doubl
     in.lw0 = M->lw[2 * (size_t)f];
     in.lw1 = M->lw[2 * (size_t)f + 1];
     in.rdelta = 1.0 / M->dlt[f];
+    face_derived(in);
 }
 
 // w' and S N' of a gradient slot (op.py:45-63): O = 1 when the cell owns the face
