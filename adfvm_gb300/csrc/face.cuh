@@ -126,7 +126,7 @@ AFVM_HD void face_flux_gauge(const Phys& P, int kind, bool inviscid, const FaceI
     }
     if (!inviscid) {
         R Fv[4];
-        viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, Us, gTs, gUs, R(1), R(1), in.D, in.N, in.Nt, in.ND, in.rdelta,
+        viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, Us, gTs, gUs, R(1), false, in.D, in.N, in.Nt, in.ND, in.rdelta,
                    Fv);
         for (int k = 0; k < 3; k++) F[1 + k] = F[1 + k] - Fv[k];
         F[4] = F[4] - Fv[3];
@@ -145,7 +145,8 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
         face_flux_gauge<R>(P, kind, inviscid, in, F, maxaF);
         return;
     }
-    R TF, Us[3], gTs[3], gUs[9], hs, rhs;
+    R TF, Us[3], gTs[3], gUs[9], hs;
+    bool sums;
     // the viscous terms (sigma and q + sigma.U_F), subtracted from the inviscid flux
     R Fv[4] = {R(0), R(0), R(0), R(0)};
     if (kind == FACE_BOUNDARY) {
@@ -159,9 +160,9 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
         TF = in.TN;
         for (int k = 0; k < 3; k++) { Us[k] = in.UN[k]; gTs[k] = in.gTN[k]; }
         for (int k = 0; k < 9; k++) gUs[k] = in.gUN[k];
-        hs = R(1); rhs = R(1);
+        hs = R(1); sums = false;
         if (!inviscid) {
-            viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, Us, gTs, gUs, hs, rhs, in.D, in.N, in.Nt, in.ND, in.rdelta,
+            viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, Us, gTs, gUs, hs, sums, in.D, in.N, in.Nt, in.ND, in.rdelta,
                        Fv, tp);
             for (int k = 0; k < 3; k++) F[1 + k] = F[1 + k] - Fv[k];
             F[4] = F[4] - Fv[3];
@@ -196,16 +197,16 @@ AFVM_HD void face_flux(const Phys& P, int kind, bool inviscid, const FaceIn<R>& 
             TF = in.TN;
             for (int k = 0; k < 3; k++) { Us[k] = in.UN[k]; gTs[k] = in.gTN[k]; }
             for (int k = 0; k < 9; k++) gUs[k] = in.gUN[k];
-            hs = R(1); rhs = R(1);
+            hs = R(1); sums = false;
         } else {
             // the face averages (density.py:290-291) as hs = 1/2 times the two sides' sums
             TF = R(0.5) * (TLF + TRF);
             for (int k = 0; k < 3; k++) { Us[k] = ULF[k] + URF[k]; gTs[k] = in.gTP[k] + in.gTN[k]; }
             for (int k = 0; k < 9; k++) gUs[k] = in.gUP[k] + in.gUN[k];
-            hs = R(0.5); rhs = R(2);
+            hs = R(0.5); sums = true;
         }
         if (!inviscid)
-            viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, Us, gTs, gUs, hs, rhs, in.D, in.N, in.Nt, in.ND, in.rdelta,
+            viscous<R>(P, in.TP, in.TN, in.UP, in.UN, TF, Us, gTs, gUs, hs, sums, in.D, in.N, in.Nt, in.ND, in.rdelta,
                        Fv, tp);
         if (solver == AFVM_RIEMANN_ROE) {
             roe<R>(P, pLF, pRF, TLF, TRF, ULF, URF, rhoL, rhoR, in.N, Fv, F, tp);
@@ -505,11 +506,11 @@ AFVM_HD void laxf_vjp(const Phys& P, R pL, R pR, R TL, R TR, const R* UL, const 
 // velocity is passed as UFs with UF = us UFs (us = 1/2: UFs is the two sides' sum; 1: the
 // ghost's own), and UFb receives the adjoint of each side's velocity, us times UF's. Likewise
 // gTFb and gUFb receive the adjoints of the cell gradients the face gradient is formed from:
-// gs times those of the face gradient (gs = 1/2 where it is the two sides' average, 1 where it
-// is the ghost's own; rgs = 1/gs). So each side's share needs no further product.
+// gs times those of the face gradient (gs = 1/2 where it is the two sides' average - avg true -
+// and 1 where it is the ghost's own). So each side's share needs no further product.
 template <typename R>
 AFVM_HD void viscous_vjp_t(const Phys& P, const R* UFs, R us, R mu, R dmu, R gTn, const R* tmp2, R tmp3, R ts,
-                           const R* sigma, const R* D, const R* N, const R* Nt, R ND, R rdel, R gs, R rgs,
+                           const R* sigma, const R* D, const R* N, const R* Nt, R ND, R rdel, R gs, bool avg,
                            const R* Fb, R& TLb, R& TRb, R* ULb, R* URb, R& TFb, R* UFb, R* gTFb, R* gUFb) {
     R kappa = mu * consts<R>(P).kFac;
     // reverse
@@ -542,7 +543,7 @@ AFVM_HD void viscous_vjp_t(const Phys& P, const R* UFs, R us, R mu, R dmu, R gTn
     gUb[2] = gUb[6] = tmp2b[0] * N[2] + tmp2b[2] * N[0];
     gUb[5] = gUb[7] = tmp2b[1] * N[2] + tmp2b[2] * N[1];
     // snGrad = (phi_N - phi_P) / deltas: the cell values' share, less the factor gs
-    R rdg = rdel * rgs;
+    R rdg = avg ? twice_pos(rdel) : rdel;
     for (int i = 0; i < 3; i++) {
         R snUb = gUb[3 * i] * D[0] + gUb[3 * i + 1] * D[1] + gUb[3 * i + 2] * D[2];
         for (int k = 0; k < 3; k++) gUFb[3 * i + k] += gUb[3 * i + k] - snUb * D[k];
@@ -583,7 +584,7 @@ AFVM_HD void viscous_vjp(const Phys& P, R TL, R TR, const R* UL, const R* UR, R 
     }
     R ND = dot3(N, D), Nt[3];
     for (int k = 0; k < 3; k++) Nt[k] = N[k] - ND * D[k];
-    viscous_vjp_t<R>(P, UF, R(1), mu, dmu, dot3(gT, N), tmp2, tmp3, R(1), sigma, D, N, Nt, ND, rdel, R(1), R(1), Fb,
+    viscous_vjp_t<R>(P, UF, R(1), mu, dmu, dot3(gT, N), tmp2, tmp3, R(1), sigma, D, N, Nt, ND, rdel, R(1), false, Fb,
                      TLb, TRb, ULb, URb, TFb, UFb, gTFb, gUFb);
 }
 
@@ -742,7 +743,7 @@ AFVM_HD void face_vjp_t(const Phys& P, int kind, bool inviscid, const FaceIn<R>&
             }
         }
         viscous_vjp_t<R>(P, UFs, us, mu, dmu, t.get(T_GTN), tmp2, tmp3, ts, sigma, in.D, in.N, in.Nt, in.ND,
-                         in.rdelta, chr ? R(1) : R(0.5), chr ? R(1) : R(2), Fb, o.TP, o.TN, o.UP, o.UN, TFb, UFb, gTFb,
+                         in.rdelta, chr ? R(1) : R(0.5), !chr, Fb, o.TP, o.TN, o.UP, o.UN, TFb, UFb, gTFb,
                          gUFb);
         if constexpr (kGeo<G>) {
             R gTF[3], gUF[9];

@@ -233,6 +233,18 @@ AFVM_HD bool lt_twice(R a, R b) {
 #endif
 }
 
+// 2 x for a positive normal x below 2^1023 (2^127 in float): on the device the exponent field
+// is raised by one with an integer add, exactly, and no FP64 product is issued
+template <typename R>
+AFVM_HD R twice_pos(R x) {
+#if defined(__CUDA_ARCH__)
+    if constexpr (sizeof(R) == 8) return __longlong_as_double(__double_as_longlong(x) + (1LL << 52));
+    else return __int_as_float(__float_as_int(x) + (1 << 23));
+#else
+    return R(2) * x;
+#endif
+}
+
 // ---- reciprocal and reciprocal square root
 //
 // On the GB300 the FP64 pipe runs at 1/57 of the FP32 rate, and an IEEE FP64 division or
@@ -606,14 +618,14 @@ AFVM_HD void laxf_gauge(const Phys& P, R pgL, R pgR, R TgL, R TgR, const R* UL, 
 // RCF.viscousFlux (adFVM/density.py:192-222): the terms the flux subtracts, Fv[0..2] = sigma
 // (from F[1..3]) and Fv[3] = q + sigma.UF (from F[4]);
 // rdel = 1/deltas (a mesh table), the divisor of snGrad (op.py:66-67). The face velocity and
-// gradients arrive as hs times Us, gTs, gUs: hs = 1/2 with the two sides' sums (the reference's
-// averages), hs = 1 with the ghost's values (rhs = 1/hs). The corrected gradients are formed
+// gradients arrive as hs times Us, gTs, gUs: hs = 1/2 with the two sides' sums (sums true; the
+// reference's averages), hs = 1 with the ghost's values. The corrected gradients are formed
 // divided by hs, and so are the (grad U + grad U^T).n and tr grad U the tape keeps (the VJP
 // scales them back); sigma, (grad T).n and the flux are the reference's. Nt = N - (N.D) D and
 // ND = N.D: mesh-only factors of the corrected gradient's normal component.
 template <typename R, typename Sink = TapeNone>
 AFVM_HD void viscous(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, const R* Us, const R* gTs,
-                     const R* gUs, R hs, R rhs, const R* D, const R* N, const R* Nt, R ND, R rdel, R* Fv,
+                     const R* gUs, R hs, bool sums, const R* D, const R* N, const R* Nt, R ND, R rdel, R* Fv,
                      Sink&& tp = Sink()) {
     R dmu;
     R mu = viscosity<R>(P, TF, &dmu);
@@ -621,8 +633,8 @@ AFVM_HD void viscous(const Phys& P, R TL, R TR, const R* UL, const R* UR, R TF, 
     tp.put(T_DMU, dmu);
     R kappa = mu * consts<R>(P).kFac;
     // the face gradient with its normal component replaced by snGrad: g + (snGrad - g.D) D,
-    // here divided by hs
-    R rdh = rdel * rhs;
+    // here divided by hs (1/deltas doubled on the integer pipe for the sums)
+    R rdh = sums ? twice_pos(rdel) : rdel;
     R gU[9];
     for (int i = 0; i < 3; i++) {
         R gUD = gUs[3 * i] * D[0] + gUs[3 * i + 1] * D[1] + gUs[3 * i + 2] * D[2];
