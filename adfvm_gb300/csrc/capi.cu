@@ -122,8 +122,10 @@ int upload_mesh(Ctx* c, const HostTables& h, MeshDev<R>& m) {
         for (size_t i = 0; i < r.size(); i++) r[i] = 1.0 / h.dlt[i];
         if ((st = upload(c, &m.rdlt, cast<R>(r)))) return st;
     }
-    {
-        // N - (N.D) D and N.D in double (face_derived() forms the same numbers)
+    m.ntd = nullptr;
+    if constexpr (sizeof(R) == 8) {
+        // N - (N.D) D and N.D in double (face_derived() forms the same numbers); FP32 face
+        // kernels form them in registers instead (their loads, not their arithmetic, bind them)
         const size_t nF = h.dlt.size();
         std::vector<double> t(4 * nF);
         for (size_t f = 0; f < nF; f++) {

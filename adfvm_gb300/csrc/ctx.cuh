@@ -73,7 +73,7 @@ struct MeshDev {
     const R* area;            // nF
     const R* dlt;             // nF  deltas
     const R* rdlt;            // nF  1/deltas (the viscous snGrad divisor, mesh-only)
-    const R* ntd;             // 4 x nF  N - (N.D) D (3) and N.D, D = deltasUnit (mesh-only)
+    const R* ntd;             // 4 x nF  N - (N.D) D (3) and N.D, D = deltasUnit (mesh-only; FP64 only)
     const R* du;              // 3 x nF deltasUnit
     const R* wts;             // nF  weights (central interpolation, interp.py:15-18)
     const R* lw;              // 2 x nF linearWeights

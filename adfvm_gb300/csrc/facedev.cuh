@@ -50,8 +50,14 @@ __device__ __forceinline__ void load_face(const MeshDev<R>& m, const R* __restri
     in.lw0 = m.lw[f];
     in.lw1 = m.lw[nF + f];
     in.rdelta = m.rdlt[f];
-    for (int k = 0; k < 3; k++) in.Nt[k] = m.ntd[k * nF + f];
-    in.ND = m.ntd[3 * nF + f];
+    if constexpr (sizeof(R) == 8) {
+        for (int k = 0; k < 3; k++) in.Nt[k] = m.ntd[k * nF + f];
+        in.ND = m.ntd[3 * nF + f];
+    } else {
+        // FP32 face kernels are bound by their loads, not by their (FP32) arithmetic: formed here
+        in.ND = dot3(in.N, in.D);
+        for (int k = 0; k < 3; k++) in.Nt[k] = in.N[k] - in.ND * in.D[k];
+    }
 }
 
 // a face's column of a device tape (value k of face f at tape[k nF + f]; p = tape + f)
@@ -82,8 +88,14 @@ __device__ __forceinline__ void load_face_geometry(const MeshDev<R>& m, int f, F
     in.lw0 = m.lw[f];
     in.lw1 = m.lw[nF + f];
     in.rdelta = m.rdlt[f];
-    for (int k = 0; k < 3; k++) in.Nt[k] = m.ntd[k * nF + f];
-    in.ND = m.ntd[3 * nF + f];
+    if constexpr (sizeof(R) == 8) {
+        for (int k = 0; k < 3; k++) in.Nt[k] = m.ntd[k * nF + f];
+        in.ND = m.ntd[3 * nF + f];
+    } else {
+        // FP32 face kernels are bound by their loads, not by their (FP32) arithmetic: formed here
+        in.ND = dot3(in.N, in.D);
+        for (int k = 0; k < 3; k++) in.Nt[k] = in.N[k] - in.ND * in.D[k];
+    }
 }
 
 }  // namespace afvm

@@ -50,12 +50,12 @@ def peaks():
 # algorithmic (compulsory) bytes per launch of each primal kernel, FP64 / FP32 element size
 # es and int32 indices (per-unit counts in the comments below)
 def algorithmic_bytes(kernel, nIC, nIF, nF, nG, es, taped=False):
-    REC, FREC, TAPE = 20, 6, 61
+    REC, FREC, TAPE, GEO = 20, 6, 61, 15
     if kernel == 'k_flux':
         # per face: own+nbr (8), normals 3, deltas 1, deltasUnit 3, linearWeights 2,
-        # quadraticWeights 6, N - (N.D) D and N.D 4 -> 19 values, flux record write 6 (and the
-        # 61-value face tape when taped); cell records read once
-        return nF * (8 + 19 * es + FREC * es + (TAPE * es if taped else 0)) + (nIC + nG) * REC * es
+        # quadraticWeights 6 -> 15 values, and in FP64 N - (N.D) D and N.D (4 more), flux record
+        # write 6 (and the 61-value face tape when taped); cell records read once
+        return nF * (8 + (GEO + 4 * (es == 8)) * es + FREC * es + (TAPE * es if taped else 0)) + (nIC + nG) * REC * es
     if kernel == 'k_grad':
         # per cell: 6 slots x (nbr 4 + w' + S*N' (3)) + 1/V, primitives of every cell once,
         # gradient write 15
@@ -67,14 +67,14 @@ def algorithmic_bytes(kernel, nIC, nIF, nF, nG, es, taped=False):
     if kernel == 'k_prim':
         return nIC * 10 * es + nG * (8 + 5 * es + 5 * es)
     if kernel == 'k_adj_flux' and taped:
-        # per face: own+nbr (8), A/V weights 2, geometry 19, the 61-value face tape, 40-value
-        # adjoint record write; the 5 adjoint seeds of every cell once; the two cell records of
-        # each boundary face (boundary faces are not taped)
-        return nF * (8 + (21 + TAPE + 40) * es) + nIC * 5 * es + (nF - nIF) * 2 * REC * es
+        # per face: own+nbr (8), A/V weights 2, geometry 15 (19 in FP64), the 61-value face tape,
+        # 40-value adjoint record write; the 5 adjoint seeds of every cell once; the two cell
+        # records of each boundary face (boundary faces are not taped)
+        return nF * (8 + (2 + GEO + 4 * (es == 8) + TAPE + 40) * es) + nIC * 5 * es + (nF - nIF) * 2 * REC * es
     if kernel == 'k_adj_flux':
-        # per face: own+nbr (8), A/V weights 2, geometry 19, 40-value adjoint record write;
-        # cell records and the 5 adjoint seeds of every cell read once
-        return nF * (8 + 21 * es + 40 * es) + (nIC + nG) * REC * es + nIC * 5 * es
+        # per face: own+nbr (8), A/V weights 2, geometry 15 (19 in FP64), 40-value adjoint record
+        # write; cell records and the 5 adjoint seeds of every cell read once
+        return nF * (8 + (2 + GEO + 4 * (es == 8)) * es + 40 * es) + (nIC + nG) * REC * es + nIC * 5 * es
     return 0
 
 
