@@ -89,19 +89,19 @@ STEP_BYTES = {('primal', 8): 2904, ('primal', 4): 1524, ('adjoint', 8): 6288, ('
 # mesh by its number of faces (the kernel's traffic grows in proportion to the faces). The FP64
 # kernels (taped: the benchmarked step with its 61-value face tape; untaped: --tape 0) are from
 # captures of the current build, the FP32 ones from earlier captures of the same kernels.
-MEASURED_TRAFFIC = {('k_flux', 8): (173.8e6, 798720), ('k_flux', 4): (81.56e6, 798720),
-                    ('k_adj_flux', 8): (417.2e6, 798720), ('k_adj_flux', 4): (170.37e6, 798720),
-                    ('k_flux+tape', 8): (547.5e6, 798720), ('k_adj_flux+tape', 8): (763.6e6, 798720)}
+MEASURED_TRAFFIC = {('k_flux', 8): (200.3e6, 798720), ('k_flux', 4): (81.56e6, 798720),
+                    ('k_adj_flux', 8): (455.5e6, 798720), ('k_adj_flux', 4): (170.37e6, 798720),
+                    ('k_flux+tape', 8): (547.1e6, 798720), ('k_adj_flux+tape', 8): (763.2e6, 798720)}
 # FP64 thread instructions per face (DADD, DMUL, DFMA) of a launch in the same captures
 # (smsp__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on), current build; the untaped
 # forward flux issues a few FP64 instructions fewer than the taped one (the tape's values it
 # need not form)
-MEASURED_FP64_INST = {'k_flux': (50.0, 86.1, 162.2), 'k_adj_flux': (82.0, 184.5, 322.4),
-                      'k_flux+tape': (52.0, 90.1, 156.2), 'k_adj_flux+tape': (40.0, 105.5, 177.4)}
+MEASURED_FP64_INST = {'k_flux': (50.0, 85.1, 157.2), 'k_adj_flux': (82.0, 188.5, 314.4),
+                      'k_flux+tape': (52.0, 90.1, 156.2), 'k_adj_flux+tape': (40.0, 105.7, 177.4)}
 # every warp instruction the FP64 pipe issued, per face (smsp__inst_executed_pipe_fp64 x 32 / faces,
 # the same captures): the arithmetic above plus the issues of warps whose lanes were partly masked
 # (branches that only some of a warp's faces take)
-MEASURED_FP64_PIPE_INST = {'k_flux': 301.0, 'k_adj_flux': 593.8, 'k_flux+tape': 301.0, 'k_adj_flux+tape': 328.8}
+MEASURED_FP64_PIPE_INST = {'k_flux': 295.0, 'k_adj_flux': 589.8, 'k_flux+tape': 301.0, 'k_adj_flux+tape': 328.8}
 
 
 def measured_traffic(kernel, es, nF):
