@@ -6,7 +6,7 @@
 // arrays): a pageable device-to-host cudaMemcpy into a new array runs at about 22 GB/s and a
 // precision change costs a further single-threaded pass over the array, while the pageable
 // host-to-device copy of equal types already runs at about 180 GB/s, and so does the download
-// into pages that are already mapped. So copies of equal types go straight to the driver (a
+// into pages that are already mapped. So copies of equal types go straight to the CUDA driver (a
 // download first touches its destination's pages with all host threads); conversions use a
 // ring of two pinned staging chunks per device: the host threads (OpenMP) fill or drain chunk i,
 // converting, while the copy engine moves chunk i-1, at the lower of the host's multi-threaded
@@ -97,7 +97,7 @@ bool pinned(const void* p) {
 }
 
 int to_device(Stager& st, void* dst, int ds, const void* src, int ss, size_t n, cudaStream_t s) {
-    // same type: the driver's own path, pinned or not (on a GB300's Grace host its pageable
+    // same type: the CUDA driver's own path, pinned or not (on a GB300's Grace host its pageable
     // host-to-device copy runs at about 180 GB/s, against about 100 GB/s through the staging)
     if (ds == ss) {
         if (cudaMemcpyAsync(dst, src, n * (size_t)ds, cudaMemcpyHostToDevice, s) != cudaSuccess) {
@@ -126,7 +126,7 @@ int to_device(Stager& st, void* dst, int ds, const void* src, int ss, size_t n, 
 
 // writes a zero into every 4 KB page of [p, p + bytes), split over the host threads: a new
 // (never touched) array takes its page faults in parallel here instead of one by one inside
-// the driver's copy
+// the CUDA driver's copy
 void touch_pages(void* p, size_t bytes) {
     if (!bytes) return;
     unsigned char* b = (unsigned char*)p;
@@ -137,7 +137,7 @@ void touch_pages(void* p, size_t bytes) {
 }
 
 int to_host(Stager& st, void* dst, int ds, const void* src, int ss, size_t n, cudaStream_t s, bool syncPinned) {
-    // same type: the driver's own path (a pageable device-to-host copy runs at about 185 GB/s
+    // same type: the CUDA driver's own path (a pageable device-to-host copy runs at about 185 GB/s
     // into pages that are already mapped but 21 GB/s into a new array; with the parallel touch
     // first, about 48 GB/s - the page faults themselves - and 168 GB/s into mapped pages)
     if (ds == ss) {

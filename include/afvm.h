@@ -446,7 +446,7 @@ int afvm_sensitivity_noalloc(int32_t device, int32_t nArrays, const double* cons
  * values of srcBytes bytes each (8: double, 4: float) become `count` values of dstBytes bytes,
  * converted (round to nearest) when the sizes differ. Host memory may be pageable or pinned;
  * device arrays live on CUDA device `device`, and the copy is ordered on `stream`.
- * Copies of equal types take the driver's copy directly (a download into pageable memory first
+ * Copies of equal types take the CUDA driver's copy directly (a download into pageable memory first
  * touches the destination's pages with all OpenMP threads, so a new array takes its page faults
  * in parallel); converted data moves through two pinned 8 MB staging chunks per device, filled
  * or drained by all OpenMP threads while the other chunk is on the link; calls on one device
