@@ -213,6 +213,14 @@ int build_tables(Ctx* c, const afvm_mesh_tensors* M, const afvm_patch_bc* bcs, H
     h.lw.resize(2 * (size_t)nF); h.qw.resize(6 * (size_t)nF);
     h.area.assign(M->areas, M->areas + nF);
     h.dlt.assign(M->deltas, M->deltas + nF);
+    // the viscous snGrad divides by deltas, and the face kernels double 1/deltas by raising its
+    // exponent: every deltas must be a positive, finite number of ordinary size (a NaN fails
+    // both comparisons)
+    int badDelta = 0;
+#pragma omp parallel for reduction(max : badDelta)
+    for (int f = 0; f < nF; f++)
+        if (!(h.dlt[f] >= 1e-30 && h.dlt[f] <= 1e30)) badDelta = 1;
+    if (badDelta) return fail(c, AFVM_ERR_BAD_ARG, "deltas must lie in [1e-30, 1e30]");
     h.wts.assign(M->weights, M->weights + nF);
     c->volTotal = 0.0;
     for (int i = 0; i < nIC; i++) c->volTotal += M->volumes[i];

@@ -131,7 +131,7 @@ typedef struct afvm_mesh_tensors {
     const double* volumesL;         /* nFaces */
     const double* volumesR;         /* nInternalFaces */
     const double* weights;          /* nFaces */
-    const double* deltas;           /* nFaces */
+    const double* deltas;           /* nFaces; each in [1e-30, 1e30] (else AFVM_ERR_BAD_ARG) */
     const double* normals;          /* nFaces x 3 */
     const double* deltasUnit;       /* nFaces x 3 */
     const double* linearWeights;    /* nFaces x 2 */
